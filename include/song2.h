@@ -1,0 +1,242 @@
+/*
+ * song2.h - C ABI of the GB300 second-order perturbation evolver.
+ *
+ * This header is the drop-in boundary that replaces the "Solve differential
+ * system" block of SONG's perturb2_init (source/perturbations2.c:283-362),
+ * i.e. the OpenMP loop that calls perturb2_solve() for every (k1,k2,k3)
+ * triplet and fills ppt2->sources.  Every entry point takes plain C types:
+ * pointers, sizes and flat arrays; no torch or CUDA type appears here.
+ *
+ * Output layout (unchanged from the reference, include/perturbations2.h:397-414
+ * and include/perturbations2_macros.h:35-38):
+ *
+ *   sources[index_tp2][index_k1][index_k2][index_tau*k3_size[k1][k2] + index_k3]
+ *
+ * with index_k2 <= index_k1.  The flat device/host buffer used internally stores
+ * the same rows back to back: for each tp2, pairs (k1,k2<=k1) in row-major order,
+ * each pair a block of tau_size*k3_size doubles (see song2_pair_offset()).
+ *
+ * Error convention (perturbations2.h:1802-1814): 0 on success, 1 on failure
+ * with a message in the caller's char[SONG2_ERRLEN] buffer; nothing aborts.
+ */
+#ifndef SONG2_H
+#define SONG2_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SONG2_ERRLEN 1024
+#define SONG2_MAX_M 5          /* azimuthal modes m = 0..4 */
+#define SONG2_MAX_L 64         /* largest hierarchy l_max supported */
+
+/* Per-triplet status codes.  A triplet that breaches an iteration limit
+   retires with one of these codes; no kernel traps or hangs. */
+enum song2_status_code {
+  SONG2_OK = 0,
+  SONG2_E_MAXSTEPS = 1,   /* more than spec.max_steps accepted+rejected steps */
+  SONG2_E_HMIN = 2,       /* step size fell below the minimum */
+  SONG2_E_NAN = 3,        /* non-finite value in the state or the sources */
+  SONG2_E_NEWTON = 4,     /* Newton iteration failed with a current Jacobian at h_min */
+  SONG2_E_SINGULAR = 5,   /* zero pivot in the iteration matrix */
+  SONG2_E_CONFIG = 6      /* geometry or configuration check failed */
+};
+
+/* Initial conditions (source/input2.c:2116-2121, perturbations2.c:3789-4210) */
+enum song2_ic { SONG2_IC_AD = 0, SONG2_IC_AD_FIRST_ORDER = 1, SONG2_IC_ZERO = 2 };
+
+/* Iteration-matrix precision of the GPU evolver */
+enum song2_precision { SONG2_PREC_FP64 = 0, SONG2_PREC_MIXED = 1 };
+
+/* Background/thermodynamics table columns.  Values are tabulated on a uniform
+   grid in x = ln(tau) and interpolated with a natural cubic spline in x.
+   Densities follow CLASS units (8 pi G/3 rho, Mpc^-2). */
+enum song2_bg_column {
+  SONG2_BG_LN_A = 0,        /* ln a */
+  SONG2_BG_LN_HC,           /* ln (a H), conformal Hubble rate [1/Mpc] */
+  SONG2_BG_HC_PRIME_TAU2,   /* (d(aH)/dtau) * tau^2 */
+  SONG2_BG_LN_RHO_G,        /* ln rho_photon */
+  SONG2_BG_LN_RHO_B,        /* ln rho_baryon */
+  SONG2_BG_LN_RHO_CDM,      /* ln rho_cdm */
+  SONG2_BG_LN_RHO_UR,       /* ln rho_massless_neutrinos */
+  SONG2_BG_LN_KAPPA_DOT,    /* ln (a n_e sigma_T) [1/Mpc] */
+  SONG2_BG_KAPPA,           /* optical depth from tau to today */
+  SONG2_BG_SIZE
+};
+
+/* First-order quantity layout (the replacement for CLASS's ppt->index_qs_*,
+   perturbations2.c:3782-3822, 9173-9332, 10794-10923).  The multipole blocks
+   start at SONG2_FO_I etc. and hold l = 0..fo_l_max. */
+enum song2_fo_index {
+  SONG2_FO_PHI = 0, SONG2_FO_PSI, SONG2_FO_PHI_P, SONG2_FO_PSI_P, SONG2_FO_PHI_PP,
+  SONG2_FO_DELTA_G, SONG2_FO_V_G,
+  SONG2_FO_DELTA_B, SONG2_FO_V_B, SONG2_FO_DELTA_B_P, SONG2_FO_V_B_P,
+  SONG2_FO_DELTA_CDM, SONG2_FO_V_CDM, SONG2_FO_V_CDM_P,
+  SONG2_FO_DELTA_UR, SONG2_FO_V_UR,
+  SONG2_FO_DIPOLE_B, SONG2_FO_DIPOLE_CDM,
+  SONG2_FO_I  /* first multipole block; E, N follow, see song2_fo_size() */
+};
+
+/* Cosmological parameters of the flat LCDM background. */
+typedef struct {
+  double h, omega_b, omega_cdm, N_eff, T_cmb, YHe;
+} song2_cosmo;
+
+/* Problem specification: the hot-path subset of SONG's precision2/perturbs2
+   (include/common2.h:24-214, source/input2.c:2027-2371). */
+typedef struct {
+  /* hierarchies (ppr2->l_max_g, l_max_pol_g, l_max_ur) */
+  int l_max_g, l_max_pol_g, l_max_ur;
+  int l_max_los_t, l_max_los_p;            /* LOS source multipoles */
+  int m_size;                              /* modes_song */
+  int m[SONG2_MAX_M];                      /* ascending */
+  /* physics switches (input2.c:2059-2121) */
+  int has_polarization2;
+  int has_quadratic_sources, has_quadratic_liouville, has_quadratic_collision;
+  int tight_coupling;                      /* 0: tca2_none, 1: tca2_first_order_pitrou */
+  double tca_trigger_tau_c_over_tau_h;     /* 0.01 */
+  double tca_trigger_tau_c_over_tau_k;     /* 0.007 */
+  int ic;                                  /* enum song2_ic */
+  double primordial_local_fnl_phi;
+  /* line-of-sight source switches (input2.c:619-690) */
+  int has_pure_scattering_in_los, has_quad_scattering_in_los;
+  int has_pure_metric_in_los, has_quad_metric_in_los;
+  int has_time_delay_in_los, has_redshift_in_los, has_lensing_in_los;
+  int has_sw, has_isw, use_exponential_potentials;
+  int has_source_T, has_source_E, has_source_B, has_source_delta_cdm;
+  /* integrator (tol_perturb_integration_song, smallest variation) */
+  double rtol;                             /* relative tolerance */
+  double threshold;                        /* absolute floor of the error weights */
+  int max_steps;                           /* per triplet (steps + rejections) */
+  double start_small_k_at_tau_c_over_tau_h;/* 0.0015 */
+  double start_large_k_at_tau_h_over_tau_k;/* 0.07 */
+  double tol_tau_approx;                   /* relative bisection tolerance */
+  /* grids (ppt2->k, k3, tau_sampling) */
+  int k_size;
+  const double *k;                         /* [k_size] ascending */
+  const int *k3_size;                      /* [k_size*k_size]; entry i1*k_size+i2 for i2<=i1 */
+  const double *k3;                        /* concatenated k3 grids of the pairs, pair order */
+  int tau_size;
+  const double *tau;                       /* [tau_size] ascending */
+} song2_spec;
+
+/* Background/thermo and first-order interpolation tables, owned by the caller
+   (the replacement for CLASS's pba/pth/ppt->quadsources). */
+typedef struct {
+  double tau0;                             /* conformal age [Mpc] */
+  double a_eq;                             /* scale factor at equality */
+  int bg_size;                             /* number of ln tau nodes */
+  double bg_lntau0, bg_dlntau;             /* uniform grid */
+  const double *bg;                        /* [bg_size][SONG2_BG_SIZE] values */
+  const double *bg_dd;                     /* [bg_size][SONG2_BG_SIZE] spline d2/dx2 */
+  int fo_k_size;                           /* must equal spec.k_size (same k nodes) */
+  int fo_tau_size;
+  double fo_lntau0, fo_dlntau;             /* uniform ln tau grid of the first-order table */
+  int fo_l_max;                            /* multipoles stored: l = 0..fo_l_max */
+  int fo_size;                             /* quantities per node = song2_fo_size(fo_l_max) */
+  const double *fo;                        /* [k][tau][q] values */
+  const double *fo_dd;                     /* [k][tau][q] spline d2/dx2 */
+} song2_tables;
+
+/* Per-triplet diagnostics (the reference's per-workspace counters,
+   perturbations2.h:1594-1602). */
+typedef struct {
+  int32_t status;
+  int32_t n_steps, n_rejected, n_rhs, n_jac, n_lu, n_newton_fail, sources_calls;
+} song2_triplet_stats;
+
+typedef struct song2_ctx song2_ctx;
+
+/* ---------------------------------------------------------------- host side */
+
+/* Number of first-order quantities per node for a given stored l_max. */
+int song2_fo_size(int fo_l_max);
+/* Total number of triplets and of source types for a spec. */
+int64_t song2_n_triplets(const song2_spec *spec);
+int song2_tp2_size(const song2_spec *spec);
+/* Offset (in doubles, within one source type) of the (k1,k2) block of the flat
+   source buffer, and the length of one source type. */
+int64_t song2_pair_offset(const song2_spec *spec, int index_k1, int index_k2);
+int64_t song2_sources_per_type(const song2_spec *spec);
+/* Default spec values from source/input2.c:2027-2371 (pointers left NULL). */
+void song2_spec_defaults(song2_spec *spec);
+
+/* Background + recombination of a flat LCDM model on a uniform ln(tau) grid
+   (replaces CLASS background_init/thermodynamics_init, called at
+   main/song.c:55-60).  bg and bg_dd must hold bg_size*SONG2_BG_SIZE doubles. */
+int song2_background_compute(const song2_cosmo *cosmo, int bg_size,
+                             double *bg, double *bg_dd,
+                             double *lntau0, double *dlntau,
+                             double *tau0, double *a_eq, char *err);
+
+/* Natural cubic spline second derivatives in x on a uniform grid, column-wise:
+   y[n][ncol] -> dd[n][ncol]. */
+void song2_spline_uniform(int n, int ncol, double dx, const double *y, double *dd);
+
+/* Coupling coefficients C and D (perturbations2.c:1236-1271) of one (l,m1,m),
+   closed forms derived from Clebsch-Gordan coefficients. */
+double song2_coupling_c_minus(int l, int m1, int m);
+double song2_coupling_c_plus(int l, int m1, int m);
+double song2_coupling_d_minus(int l, int m1, int m);
+double song2_coupling_d_plus(int l, int m1, int m);
+double song2_coupling_d_zero(int l, int m1, int m);
+
+/* Grids: lin/log k sampling (sources2_k_sampling = lin/log), per-pair k3 grids
+   with the reference's clipping (sources2_k3_sampling = lin/log), custom tau
+   sampling (custom_time_sampling_song_sources).  k3_size_out has k_size*k_size
+   entries; k3_out receives the concatenated grids in pair order and may be NULL
+   to query the sizes. */
+int song2_k_grid(int log_sampling, double k_min, double k_max, int k_size, double *k_out);
+int song2_k3_grids(const double *k, int k_size, int k3_size, int log_sampling, int *k3_size_out,
+                   double *k3_out, char *err);
+int song2_tau_grid(int log_sampling, double tau_ini, double tau_end, int tau_size, double *out);
+
+/* Evolution start time for wavenumber k (perturbations2.c:3388-3524). */
+int song2_start_time(const song2_spec *spec, const song2_tables *tab, double k,
+                     double tau_upper, double *tau_ini, char *err);
+
+/* ---------------------------------------------------------------- GPU side */
+
+/* Create a context on the current CUDA device: uploads the spec grids and the
+   tables once to a device arena (cudaMemcpyAsync).  Not thread safe per ctx. */
+int song2_ctx_create(const song2_spec *spec, const song2_tables *tab,
+                     int precision, song2_ctx **out, char *err);
+int song2_ctx_destroy(song2_ctx *ctx);
+
+/* Evolve every triplet on the device and leave the sources in device memory.
+   stream may be NULL (legacy default stream).  Blocking on return. */
+int song2_ctx_run(song2_ctx *ctx, void *stream, char *err);
+/* Device pointer of the flat source buffer and of the per-triplet stats. */
+double *song2_ctx_device_sources(song2_ctx *ctx);
+song2_triplet_stats *song2_ctx_device_stats(song2_ctx *ctx);
+/* Copy the flat sources / stats to host memory. */
+int song2_ctx_download(song2_ctx *ctx, double *flat_sources_host,
+                       song2_triplet_stats *stats_host, char *err);
+/* Device time of the last run's evolver kernel, milliseconds (CUDA events on
+   the launching stream), and its launch count. */
+double song2_ctx_last_kernel_ms(song2_ctx *ctx);
+int song2_ctx_last_launches(song2_ctx *ctx);
+
+/* One-shot drop-in for the reference's triplet loop: creates a context,
+   evolves every triplet and scatters the result into the caller-allocated
+   ppt2->sources slabs sources[tp2][k1][k2][tau*k3_size+k3]. */
+int song2_gpu_evolve(const song2_spec *spec, const song2_tables *tab, int precision,
+                     double ****sources_out, song2_triplet_stats *per_triplet,
+                     char *err);
+
+/* First-order provider: evolves SONG's own equations in first-order mode
+   (quadratic sources off, has_ad_first_order initial conditions, m = 0)
+   for every k of spec->k and fills the first-order table fo[k][tau][q] on the
+   given uniform ln(tau) grid (values only; call song2_spline_uniform for the
+   second derivatives).  Replaces CLASS perturb_init (perturbations2.c:153). */
+int song2_gpu_first_order(const song2_spec *spec2, const song2_tables *bg_only,
+                          int fo_l_max, int fo_tau_size, double fo_lntau0,
+                          double fo_dlntau, double *fo_out, char *err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SONG2_H */

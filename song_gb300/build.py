@@ -1,0 +1,80 @@
+"""Build the in-tree shared library song_gb300/_build/libsong2.so.
+
+Host C is compiled with gcc, the CUDA translation units with nvcc for sm_103a
+only (one -gencode), in parallel; the result is linked with the static CUDA
+runtime so the library carries no dependency on torch.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+INC = os.path.join(ROOT, "include")
+LIB = os.path.join(OUT, "libsong2.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
+CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall"]
+
+C_SOURCES = ["song2_host.c"]
+CU_SOURCES = ["song2_kernels.cu", "song2_capi.cu"]
+
+
+def _nvcc():
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def _run(cmd, log):
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    with open(log, "w") as f:
+        f.write(" ".join(cmd) + "\n" + p.stdout)
+    if p.returncode != 0:
+        sys.stderr.write(p.stdout)
+        raise RuntimeError(f"build step failed: {' '.join(cmd)}")
+    return p.stdout
+
+
+def sources_newer_than_lib():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INC, "song2.h")]
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False):
+    if not force and not sources_newer_than_lib():
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    nvcc = _nvcc()
+    jobs = []
+    objs = []
+    for f in C_SOURCES:
+        o = os.path.join(OUT, f + ".o")
+        objs.append(o)
+        jobs.append((["gcc", *CC_FLAGS, "-I", INC, "-c", os.path.join(CSRC, f), "-o", o], o + ".log"))
+    for f in CU_SOURCES:
+        o = os.path.join(OUT, f + ".o")
+        objs.append(o)
+        jobs.append(([nvcc, *ARCH, *NVCC_FLAGS, "-I", INC, "-I", CSRC, "-c", os.path.join(CSRC, f), "-o", o],
+                     o + ".log"))
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        outs = list(ex.map(lambda j: _run(*j), jobs))
+    if verbose:
+        for o in outs:
+            print(o)
+    tmp = LIB + ".tmp"
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lm"], os.path.join(OUT, "link.log"))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)
+    print(LIB)

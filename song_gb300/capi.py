@@ -1,0 +1,166 @@
+"""ctypes mirror of include/song2.h.
+
+This module is the binding a maintainer of the reference would add to drive
+the C ABI from Python (the reference itself is driven from C: see
+INTEGRATION.md).  Every structure here matches song2.h field by field.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libsong2.so")
+
+SONG2_ERRLEN = 1024
+SONG2_MAX_M = 5
+SONG2_MAX_L = 64
+
+# status codes
+SONG2_OK, SONG2_E_MAXSTEPS, SONG2_E_HMIN, SONG2_E_NAN, SONG2_E_NEWTON, SONG2_E_SINGULAR, SONG2_E_CONFIG = range(7)
+# initial conditions
+SONG2_IC_AD, SONG2_IC_AD_FIRST_ORDER, SONG2_IC_ZERO = range(3)
+# precision
+SONG2_PREC_FP64, SONG2_PREC_MIXED = 0, 1
+
+# background columns
+(BG_LN_A, BG_LN_HC, BG_HC_PRIME_TAU2, BG_LN_RHO_G, BG_LN_RHO_B, BG_LN_RHO_CDM, BG_LN_RHO_UR,
+ BG_LN_KAPPA_DOT, BG_KAPPA, BG_SIZE) = range(10)
+
+# first-order quantities
+(FO_PHI, FO_PSI, FO_PHI_P, FO_PSI_P, FO_PHI_PP, FO_DELTA_G, FO_V_G, FO_DELTA_B, FO_V_B,
+ FO_DELTA_B_P, FO_V_B_P, FO_DELTA_CDM, FO_V_CDM, FO_V_CDM_P, FO_DELTA_UR, FO_V_UR,
+ FO_DIPOLE_B, FO_DIPOLE_CDM, FO_I) = range(19)
+
+
+def fo_size(fo_l_max):
+    return FO_I + 4 * (fo_l_max + 1)
+
+
+class Cosmo(C.Structure):
+    _fields_ = [("h", C.c_double), ("omega_b", C.c_double), ("omega_cdm", C.c_double),
+                ("N_eff", C.c_double), ("T_cmb", C.c_double), ("YHe", C.c_double)]
+
+
+class Spec(C.Structure):
+    _fields_ = [
+        ("l_max_g", C.c_int), ("l_max_pol_g", C.c_int), ("l_max_ur", C.c_int),
+        ("l_max_los_t", C.c_int), ("l_max_los_p", C.c_int),
+        ("m_size", C.c_int), ("m", C.c_int * SONG2_MAX_M),
+        ("has_polarization2", C.c_int),
+        ("has_quadratic_sources", C.c_int), ("has_quadratic_liouville", C.c_int),
+        ("has_quadratic_collision", C.c_int),
+        ("tight_coupling", C.c_int),
+        ("tca_trigger_tau_c_over_tau_h", C.c_double), ("tca_trigger_tau_c_over_tau_k", C.c_double),
+        ("ic", C.c_int), ("primordial_local_fnl_phi", C.c_double),
+        ("has_pure_scattering_in_los", C.c_int), ("has_quad_scattering_in_los", C.c_int),
+        ("has_pure_metric_in_los", C.c_int), ("has_quad_metric_in_los", C.c_int),
+        ("has_time_delay_in_los", C.c_int), ("has_redshift_in_los", C.c_int),
+        ("has_lensing_in_los", C.c_int),
+        ("has_sw", C.c_int), ("has_isw", C.c_int), ("use_exponential_potentials", C.c_int),
+        ("has_source_T", C.c_int), ("has_source_E", C.c_int), ("has_source_B", C.c_int),
+        ("has_source_delta_cdm", C.c_int),
+        ("rtol", C.c_double), ("threshold", C.c_double), ("max_steps", C.c_int),
+        ("start_small_k_at_tau_c_over_tau_h", C.c_double),
+        ("start_large_k_at_tau_h_over_tau_k", C.c_double),
+        ("tol_tau_approx", C.c_double),
+        ("k_size", C.c_int), ("k", C.POINTER(C.c_double)),
+        ("k3_size", C.POINTER(C.c_int)), ("k3", C.POINTER(C.c_double)),
+        ("tau_size", C.c_int), ("tau", C.POINTER(C.c_double)),
+    ]
+
+
+class Tables(C.Structure):
+    _fields_ = [
+        ("tau0", C.c_double), ("a_eq", C.c_double),
+        ("bg_size", C.c_int), ("bg_lntau0", C.c_double), ("bg_dlntau", C.c_double),
+        ("bg", C.POINTER(C.c_double)), ("bg_dd", C.POINTER(C.c_double)),
+        ("fo_k_size", C.c_int), ("fo_tau_size", C.c_int),
+        ("fo_lntau0", C.c_double), ("fo_dlntau", C.c_double),
+        ("fo_l_max", C.c_int), ("fo_size", C.c_int),
+        ("fo", C.POINTER(C.c_double)), ("fo_dd", C.POINTER(C.c_double)),
+    ]
+
+
+class TripletStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("n_steps", C.c_int32), ("n_rejected", C.c_int32),
+                ("n_rhs", C.c_int32), ("n_jac", C.c_int32), ("n_lu", C.c_int32),
+                ("n_newton_fail", C.c_int32), ("sources_calls", C.c_int32)]
+
+
+STATS_DTYPE = np.dtype([("status", np.int32), ("n_steps", np.int32), ("n_rejected", np.int32),
+                        ("n_rhs", np.int32), ("n_jac", np.int32), ("n_lu", np.int32),
+                        ("n_newton_fail", np.int32), ("sources_calls", np.int32)])
+
+# Every extern "C" symbol declared in include/song2.h, with its ctypes signature.
+_P = C.c_void_p
+_D = C.c_double
+_I = C.c_int
+_PD = C.POINTER(C.c_double)
+_PI = C.POINTER(C.c_int)
+SIGNATURES = {
+    "song2_fo_size": (_I, [_I]),
+    "song2_n_triplets": (C.c_int64, [C.POINTER(Spec)]),
+    "song2_tp2_size": (_I, [C.POINTER(Spec)]),
+    "song2_pair_offset": (C.c_int64, [C.POINTER(Spec), _I, _I]),
+    "song2_sources_per_type": (C.c_int64, [C.POINTER(Spec)]),
+    "song2_spec_defaults": (None, [C.POINTER(Spec)]),
+    "song2_background_compute": (_I, [C.POINTER(Cosmo), _I, _PD, _PD, _PD, _PD, _PD, _PD, C.c_char_p]),
+    "song2_spline_uniform": (None, [_I, _I, _D, _PD, _PD]),
+    "song2_coupling_c_minus": (_D, [_I, _I, _I]),
+    "song2_coupling_c_plus": (_D, [_I, _I, _I]),
+    "song2_coupling_d_minus": (_D, [_I, _I, _I]),
+    "song2_coupling_d_plus": (_D, [_I, _I, _I]),
+    "song2_coupling_d_zero": (_D, [_I, _I, _I]),
+    "song2_k_grid": (_I, [_I, _D, _D, _I, _PD]),
+    "song2_k3_grids": (_I, [_PD, _I, _I, _I, _PI, _PD, C.c_char_p]),
+    "song2_tau_grid": (_I, [_I, _D, _D, _I, _PD]),
+    "song2_start_time": (_I, [C.POINTER(Spec), C.POINTER(Tables), _D, _D, _PD, C.c_char_p]),
+    "song2_ctx_create": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.POINTER(_P), C.c_char_p]),
+    "song2_ctx_destroy": (_I, [_P]),
+    "song2_ctx_run": (_I, [_P, _P, C.c_char_p]),
+    "song2_ctx_device_sources": (_P, [_P]),
+    "song2_ctx_device_stats": (_P, [_P]),
+    "song2_ctx_download": (_I, [_P, _PD, C.POINTER(TripletStats), C.c_char_p]),
+    "song2_ctx_last_kernel_ms": (_D, [_P]),
+    "song2_ctx_last_launches": (_I, [_P]),
+    "song2_gpu_evolve": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _P, C.POINTER(TripletStats),
+                              C.c_char_p]),
+    "song2_gpu_first_order": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _D, _D, _PD, C.c_char_p]),
+}
+
+
+def bind(lib):
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the in-tree product library (build it with song_gb300.build.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"song2 library not built: {path} is missing (run song_gb300.build.build())")
+        _lib = bind(C.CDLL(path))
+    return _lib
+
+
+def dptr(a):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_PD)
+
+
+def iptr(a):
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_PI)
+
+
+def errbuf():
+    return C.create_string_buffer(SONG2_ERRLEN)

@@ -1,0 +1,642 @@
+/*
+ * song2_capi.cu - host side of the C ABI declared in include/song2.h.
+ *
+ * Builds the device layout of a run (state vector grouped by azimuthal m,
+ * quadratic-source vector, source types, coupling tables), uploads it once
+ * with cudaMemcpyAsync into a device arena owned by a song2_ctx, launches the
+ * persistent evolver and copies the sources back.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "song2_internal.h"
+
+struct song2_ctx {
+  DevSpec spec;
+  DevPtrs ptrs;
+  int precision;
+  int block, grid;
+  size_t smem;
+  std::vector<void *> allocs;
+  double *d_sources;
+  size_t sources_len;
+  song2_triplet_stats *d_stats;
+  double *d_fo_out;
+  size_t fo_out_len;
+  int *d_queue;
+  int n_items;
+  int tp2_size;
+  int64_t per_type;
+  cudaEvent_t ev0, ev1;
+  float last_ms;
+  int last_launches;
+};
+
+namespace {
+
+#define CK(x)                                                                        \
+  do {                                                                               \
+    cudaError_t e_ = (x);                                                            \
+    if (e_ != cudaSuccess) {                                                         \
+      snprintf(err, SONG2_ERRLEN, "%s failed: %s", #x, cudaGetErrorString(e_));      \
+      return 1;                                                                      \
+    }                                                                                \
+  } while (0)
+
+int size_l_indexm(int l_max, const int *m, int m_size) {
+  int n = 0;
+  for (int l = 0; l <= l_max; ++l)
+    for (int i = 0; i < m_size; ++i)
+      if (m[i] <= l) ++n;
+  return n;
+}
+
+struct HostLayout {
+  DevSpec s;
+  std::vector<short> eq_sp, eq_l, eq_m, idx_I, idx_E, idx_B, idx_N, qs_sp, qs_l, qs_m;
+  std::vector<double> cmin, cplu, dmin, dplu, dzer;
+};
+
+/* Build everything that depends only on the spec. */
+int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_mode, HostLayout &H, char *err) {
+  DevSpec &s = H.s;
+  memset(&s, 0, sizeof(s));
+  s.l_max_g = sp->l_max_g;
+  s.l_max_pol = sp->has_polarization2 ? sp->l_max_pol_g : -1;
+  s.l_max_ur = sp->l_max_ur;
+  s.l_los_t = sp->l_max_los_t;
+  s.l_los_p = sp->l_max_los_p;
+  s.m_size = sp->m_size;
+  if (sp->m_size < 1 || sp->m_size > SONG2_MAX_M) { snprintf(err, SONG2_ERRLEN, "bad m_size"); return 1; }
+  for (int i = 0; i < SONG2_MAX_M; ++i) s.index_m[i] = -1;
+  int m_max = 0;
+  for (int i = 0; i < sp->m_size; ++i) {
+    int m = sp->m[i];
+    if (m < 0 || m >= SONG2_MAX_M || (i > 0 && m <= sp->m[i - 1])) {
+      snprintf(err, SONG2_ERRLEN, "modes must be ascending in 0..%d", SONG2_MAX_M - 1);
+      return 1;
+    }
+    s.m[i] = m; s.compute_m[m] = 1; s.index_m[m] = i;
+    m_max = std::max(m_max, m);
+  }
+  if (sp->l_max_g < 2 || sp->l_max_ur < 2 || (sp->has_polarization2 && sp->l_max_pol_g < 2)) {
+    snprintf(err, SONG2_ERRLEN, "l_max_* must be at least 2");
+    return 1;
+  }
+  int L = std::max(sp->l_max_g, sp->l_max_ur);
+  if (sp->has_polarization2) L = std::max(L, sp->l_max_pol_g);
+  L = std::max(L, std::max(sp->l_max_los_t, sp->l_max_los_p));
+  if (L + 2 >= S2_LMAXP) { snprintf(err, SONG2_ERRLEN, "l_max too large (max %d)", SONG2_MAX_L); return 1; }
+  s.L_big = L;
+  s.Lq = L + 1;
+  s.mq_max = std::min(m_max + 1, s.Lq);
+  for (int l = 0; l < S2_LMAXP; ++l) {
+    s.index_m_max[l] = -1;
+    for (int i = 0; i < s.m_size; ++i)
+      if (s.m[i] <= l) s.index_m_max[l] = i;
+  }
+  int n = 0;
+  for (int l = 0; l < S2_LMAXP; ++l)
+    for (int i = 0; i < SONG2_MAX_M; ++i) s.lm_array[l][i] = -1;
+  for (int l = 0; l <= s.Lq; ++l)
+    for (int i = 0; i < s.m_size; ++i)
+      if (s.m[i] <= l) s.lm_array[l][i] = (short)n++;
+  s.n_lm = n;
+  n = 0;
+  for (int l = 0; l < S2_LMAXP; ++l)
+    for (int m = 0; m < SONG2_MAX_M + 2; ++m) s.lmq[l][m] = -1;
+  for (int l = 0; l <= s.Lq; ++l)
+    for (int m = 0; m <= std::min(l, s.mq_max); ++m) s.lmq[l][m] = (short)n++;
+  s.n_lmq = n;
+  s.has_pol = sp->has_polarization2;
+  s.has_qs = sp->has_quadratic_sources && !first_order_mode;
+  s.has_liou = sp->has_quadratic_liouville;
+  s.has_coll = sp->has_quadratic_collision;
+  s.tca_on = sp->tight_coupling;
+  s.tca_h = sp->tca_trigger_tau_c_over_tau_h;
+  s.tca_k = sp->tca_trigger_tau_c_over_tau_k;
+  s.ic = sp->ic;
+  s.fnl = sp->primordial_local_fnl_phi;
+  s.los_pure_scat = sp->has_pure_scattering_in_los;
+  s.los_quad_scat = sp->has_quad_scattering_in_los;
+  s.los_pure_metric = sp->has_pure_metric_in_los;
+  s.los_quad_metric = sp->has_quad_metric_in_los;
+  s.los_time_delay = sp->has_time_delay_in_los;
+  s.los_redshift = sp->has_redshift_in_los;
+  s.los_lensing = sp->has_lensing_in_los;
+  s.los_sw = sp->has_sw;
+  s.los_isw = sp->has_isw;
+  s.los_exp_pot = sp->use_exponential_potentials;
+  s.rtol = sp->rtol;
+  s.threshold = sp->threshold;
+  s.max_steps = sp->max_steps;
+  s.start_h = sp->start_small_k_at_tau_c_over_tau_h;
+  s.start_k = sp->start_large_k_at_tau_h_over_tau_k;
+  s.tol_tau = sp->tol_tau_approx;
+  auto LM = [&](int l, int m) { return (int)s.lm_array[l][s.index_m[m]]; };
+
+  /* quadratic-source layout (same order as perturb2_workspace_init) */
+  int q = 0;
+  H.qs_sp.clear(); H.qs_l.clear(); H.qs_m.clear();
+  auto push_q = [&](int sp_, int l, int m) { H.qs_sp.push_back((short)sp_); H.qs_l.push_back((short)l); H.qs_m.push_back((short)m); ++q; };
+  auto push_hier = [&](int sp_, int lmax) {
+    for (int l = 0; l <= lmax; ++l)
+      for (int i = 0; i < s.m_size; ++i)
+        if (s.m[i] <= l) push_q(sp_, l, s.m[i]);
+  };
+  s.iq_g = q; push_hier(SP_I, s.l_max_g);
+  s.iq_E = q; if (s.has_pol) push_hier(SP_E, s.l_max_pol);
+  s.iq_B = q; if (s.has_pol) push_hier(SP_B, s.l_max_pol);
+  s.iq_ur = q; push_hier(SP_N, s.l_max_ur);
+  s.iq_b = q;
+  s.iq_b000 = s.iq_c000 = -1;
+  s.iq_b11[0] = s.iq_b11[1] = s.iq_c11[0] = s.iq_c11[1] = -1;
+  if (s.compute_m[0]) { s.iq_b000 = (short)q; push_q(SP_B000, 0, 0); }
+  for (int i = 0; i < s.m_size; ++i) if (s.m[i] <= 1) { s.iq_b11[s.m[i]] = (short)q; push_q(SP_B11, 1, s.m[i]); }
+  s.iq_cdm = q;
+  if (s.compute_m[0]) { s.iq_c000 = (short)q; push_q(SP_C000, 0, 0); }
+  for (int i = 0; i < s.m_size; ++i) if (s.m[i] <= 1) { s.iq_c11[s.m[i]] = (short)q; push_q(SP_C11, 1, s.m[i]); }
+  s.iq_psi = q; push_q(SP_METRIC, 0, 0);
+  s.iq_psi_prime = q; push_q(SP_METRIC, 0, 0);
+  s.iq_phi_prime_poisson = q; push_q(SP_METRIC, 0, 0);
+  s.iq_phi_prime_longitudinal = q; push_q(SP_METRIC, 0, 0);
+  s.iq_phi_prime_prime = q; push_q(SP_METRIC, 0, 0);
+  s.iq_omega_m1_prime = q; push_q(SP_METRIC, 0, 0);
+  s.iq_gamma_m2_prime_prime = q; push_q(SP_METRIC, 0, 0);
+  s.iq_vv_g = q; push_q(SP_METRIC, 0, 0);
+  s.iq_vv_ur = q; push_q(SP_METRIC, 0, 0);
+  s.iq_dd_b = q; push_q(SP_METRIC, 0, 0);
+  s.iq_vv_b = q; push_q(SP_METRIC, 0, 0);
+  s.iq_vv_cdm = q; push_q(SP_METRIC, 0, 0);
+  s.qs2_size = q;
+
+  /* state vector, grouped in m blocks */
+  H.eq_sp.clear(); H.eq_l.clear(); H.eq_m.clear();
+  H.idx_I.assign(s.n_lm, -1); H.idx_E.assign(s.n_lm, -1); H.idx_B.assign(s.n_lm, -1); H.idx_N.assign(s.n_lm, -1);
+  int ni = 0;
+  auto push_e = [&](int sp_, int l, int m) { H.eq_sp.push_back((short)sp_); H.eq_l.push_back((short)l); H.eq_m.push_back((short)m); return ni++; };
+  s.idx_phi = s.idx_phip = s.idx_omega = s.idx_gamma = s.idx_gammap = s.idx_b000 = s.idx_c000 = -1;
+  s.idx_b11[0] = s.idx_b11[1] = s.idx_c11[0] = s.idx_c11[1] = -1;
+  s.nblk = s.m_size;
+  for (int b = 0; b < s.m_size; ++b) {
+    int m = s.m[b];
+    s.blk_start[b] = ni;
+    if (m == 0) {
+      s.idx_phi = push_e(SP_PHI, 0, 0);
+      s.idx_phip = push_e(SP_PHIP, 0, 0);
+      s.idx_b000 = push_e(SP_B000, 0, 0);
+      s.idx_b11[0] = push_e(SP_B11, 1, 0);
+      s.idx_c000 = push_e(SP_C000, 0, 0);
+      s.idx_c11[0] = push_e(SP_C11, 1, 0);
+    } else if (m == 1) {
+      s.idx_omega = push_e(SP_OMEGA, 0, 1);
+      s.idx_b11[1] = push_e(SP_B11, 1, 1);
+      s.idx_c11[1] = push_e(SP_C11, 1, 1);
+    } else if (m == 2) {
+      s.idx_gamma = push_e(SP_GAMMA, 0, 2);
+      s.idx_gammap = push_e(SP_GAMMAP, 0, 2);
+    }
+    for (int l = m; l <= s.L_big; ++l) {
+      int lm = LM(l, m);
+      if (l <= s.l_max_g) H.idx_I[lm] = (short)push_e(SP_I, l, m);
+      if (s.has_pol && l >= 2 && l <= s.l_max_pol) H.idx_E[lm] = (short)push_e(SP_E, l, m);
+      if (s.has_pol && m >= 1 && l >= 2 && l <= s.l_max_pol) H.idx_B[lm] = (short)push_e(SP_B, l, m);
+      if (l <= s.l_max_ur) H.idx_N[lm] = (short)push_e(SP_N, l, m);
+    }
+    s.blk_size[b] = ni - s.blk_start[b];
+  }
+  s.n = ni;
+  if (s.n > 32767) { snprintf(err, SONG2_ERRLEN, "system too large"); return 1; }
+  int off = 0;
+  for (int b = 0; b < s.nblk; ++b) {
+    s.lu_off[b] = off;
+    off += s.blk_size[b] * s.blk_size[b];
+  }
+  s.lu_elems = off;
+
+  /* coupling tables for l <= Lq */
+  H.cmin.assign((size_t)s.n_lm * 3, 0.0); H.cplu = H.cmin; H.dmin = H.cmin; H.dplu = H.cmin; H.dzer = H.cmin;
+  for (int l = 0; l <= s.Lq; ++l)
+    for (int i = 0; i < s.m_size; ++i) {
+      int m = s.m[i];
+      if (m > l) continue;
+      int lm = LM(l, m);
+      for (int m1 = m - 1; m1 <= m + 1; ++m1) {
+        H.cmin[lm * 3 + m - m1 + 1] = song2_coupling_c_minus(l, m1, m);
+        H.cplu[lm * 3 + m - m1 + 1] = song2_coupling_c_plus(l, m1, m);
+        H.dmin[lm * 3 + m - m1 + 1] = song2_coupling_d_minus(l, m1, m);
+        H.dplu[lm * 3 + m - m1 + 1] = song2_coupling_d_plus(l, m1, m);
+        H.dzer[lm * 3 + m - m1 + 1] = song2_coupling_d_zero(l, m1, m);
+      }
+    }
+
+  /* source types (perturb2_indices_of_perturbs, perturbations2.c:667-1075) */
+  int tp = 0;
+  auto add_tp = [&](int kind, int lmax) {
+    int base = tp;
+    for (int l = 0; l <= lmax; ++l)
+      for (int i = 0; i < s.m_size; ++i)
+        if (s.m[i] <= l) {
+          int t = base + LM(l, s.m[i]);
+          if (t >= S2_MAXTP) continue;
+          s.tp_kind[t] = kind; s.tp_l[t] = l; s.tp_m[t] = s.m[i];
+        }
+    tp = base + size_l_indexm(lmax, s.m, s.m_size);
+  };
+  if (!first_order_mode) {
+    if (sp->has_source_T) add_tp(TP_T, sp->l_max_los_t);
+    if (sp->has_source_E) add_tp(TP_E, sp->l_max_los_p);
+    if (sp->has_source_B) add_tp(TP_B, sp->l_max_los_p);
+    if (sp->has_source_delta_cdm) { s.tp_kind[tp] = TP_D; s.tp_l[tp] = 0; s.tp_m[tp] = 0; ++tp; }
+  }
+  if (tp > S2_MAXTP) { snprintf(err, SONG2_ERRLEN, "too many source types"); return 1; }
+  s.tp2_size = tp;
+  s.mode_first_order = first_order_mode;
+  s.tau_size = sp->tau_size;
+  s.k_size = sp->k_size;
+  /* tables */
+  s.bg_size = tab->bg_size;
+  s.bg_lntau0 = tab->bg_lntau0;
+  s.bg_dlntau = tab->bg_dlntau;
+  if (!first_order_mode) {
+    s.fo_l_max = tab->fo_l_max;
+    s.nfo = song2_fo_size(tab->fo_l_max);
+    if (tab->fo_size != s.nfo || tab->fo_k_size != sp->k_size || !tab->fo || !tab->fo_dd) {
+      snprintf(err, SONG2_ERRLEN, "first-order table does not match the spec");
+      return 1;
+    }
+    if (tab->fo_l_max < s.L_big + 1) {
+      snprintf(err, SONG2_ERRLEN, "first-order table stores l <= %d, need %d", tab->fo_l_max, s.L_big + 1);
+      return 1;
+    }
+    s.fo_tau_size = tab->fo_tau_size;
+    s.fo_lntau0 = tab->fo_lntau0;
+    s.fo_dlntau = tab->fo_dlntau;
+    s.fo_k_size = tab->fo_k_size;
+  }
+  s.fo_E = SONG2_FO_I + (s.fo_l_max + 1);
+  s.fo_N = SONG2_FO_I + 2 * (s.fo_l_max + 1);
+  s.fo_CG = SONG2_FO_I + 3 * (s.fo_l_max + 1);
+  return 0;
+}
+
+template <typename V> int upload(song2_ctx *c, const V &v, const typename V::value_type **dst, cudaStream_t st, char *err) {
+  void *p = nullptr;
+  size_t bytes = std::max<size_t>(1, v.size() * sizeof(typename V::value_type));
+  CK(cudaMalloc(&p, bytes));
+  c->allocs.push_back(p);
+  if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(typename V::value_type), cudaMemcpyHostToDevice, st));
+  *dst = (const typename V::value_type *)p;
+  return 0;
+}
+
+int upload_raw(song2_ctx *c, const void *src, size_t bytes, void **dst, cudaStream_t st, char *err) {
+  void *p = nullptr;
+  CK(cudaMalloc(&p, std::max<size_t>(1, bytes)));
+  c->allocs.push_back(p);
+  if (bytes) CK(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, st));
+  *dst = p;
+  return 0;
+}
+
+int alloc_dev(song2_ctx *c, size_t bytes, void **dst, char *err) {
+  void *p = nullptr;
+  CK(cudaMalloc(&p, std::max<size_t>(1, bytes)));
+  c->allocs.push_back(p);
+  *dst = p;
+  return 0;
+}
+
+/* Shared set-up of a context: spec layout, tables, work items. */
+int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int precision, int first_order_mode,
+              const std::vector<WorkItem> &items, const std::vector<double> &k3, const std::vector<int> &k3_off,
+              const std::vector<int> &k3_size, const std::vector<int64_t> &pair_off, int fo_tau_size,
+              double fo_lntau0, double fo_dlntau, int fo_l_max, char *err) {
+  HostLayout H;
+  if (first_order_mode) {
+    /* the layout needs fo sizes for the output table */
+    memset(&H.s, 0, sizeof(H.s));
+  }
+  if (build_layout(sp, tab, first_order_mode, H, err)) return 1;
+  DevSpec &s = H.s;
+  if (first_order_mode) {
+    s.fo_l_max = fo_l_max;
+    s.nfo = song2_fo_size(fo_l_max);
+    s.fo_tau_size = fo_tau_size;
+    s.fo_lntau0 = fo_lntau0;
+    s.fo_dlntau = fo_dlntau;
+    s.fo_k_size = sp->k_size;
+    s.fo_E = SONG2_FO_I + (fo_l_max + 1);
+    s.fo_N = SONG2_FO_I + 2 * (fo_l_max + 1);
+    s.fo_CG = SONG2_FO_I + 3 * (fo_l_max + 1);
+  }
+  s.n_items = (int)items.size();
+  c->precision = precision;
+  c->n_items = s.n_items;
+  c->tp2_size = s.tp2_size;
+  int64_t per_type = 0;
+  if (!first_order_mode) per_type = song2_sources_per_type(sp);
+  s.per_type = per_type;
+  c->per_type = per_type;
+
+  int dev = 0, nsm = 0, smem_optin = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  c->block = 256;
+  size_t with_lu = song2_smem_bytes(s, precision, c->block, 1);
+  s.lu_in_smem = with_lu <= (size_t)smem_optin ? 1 : 0;
+  c->smem = song2_smem_bytes(s, precision, c->block, s.lu_in_smem);
+  if (c->smem > (size_t)smem_optin) {
+    snprintf(err, SONG2_ERRLEN, "shared-memory plan %zu B exceeds the %d B limit", c->smem, smem_optin);
+    return 1;
+  }
+  int per_sm = song2_max_ctas_per_sm(precision, c->block, c->smem);
+  if (per_sm < 1) per_sm = 1;
+  c->grid = std::max(1, std::min(s.n_items, nsm * per_sm));
+
+  cudaStream_t st = 0;
+  DevPtrs &p = c->ptrs;
+  memset(&p, 0, sizeof(p));
+  std::vector<double> kv(sp->k, sp->k + sp->k_size);
+  if (upload(c, kv, &p.k, st, err)) return 1;
+  if (upload(c, k3, &p.k3, st, err)) return 1;
+  if (!first_order_mode) {
+    std::vector<double> tv(sp->tau, sp->tau + sp->tau_size);
+    if (upload(c, tv, &p.tau, st, err)) return 1;
+  } else {
+    std::vector<double> tv(1, 0.0);
+    if (upload(c, tv, &p.tau, st, err)) return 1;
+  }
+  if (upload(c, k3_off, &p.k3_off, st, err)) return 1;
+  if (upload(c, k3_size, &p.k3_size, st, err)) return 1;
+  if (upload(c, pair_off, &p.pair_off, st, err)) return 1;
+  size_t bgb = (size_t)tab->bg_size * SONG2_BG_SIZE * sizeof(double);
+  void *tmp;
+  if (upload_raw(c, tab->bg, bgb, &tmp, st, err)) return 1;
+  p.bg = (const double *)tmp;
+  if (upload_raw(c, tab->bg_dd, bgb, &tmp, st, err)) return 1;
+  p.bg_dd = (const double *)tmp;
+  if (!first_order_mode) {
+    size_t fob = (size_t)tab->fo_k_size * tab->fo_tau_size * tab->fo_size * sizeof(double);
+    if (upload_raw(c, tab->fo, fob, &tmp, st, err)) return 1;
+    p.fo = (const double *)tmp;
+    if (upload_raw(c, tab->fo_dd, fob, &tmp, st, err)) return 1;
+    p.fo_dd = (const double *)tmp;
+  } else {
+    p.fo = p.fo_dd = p.bg;  /* never read in first-order mode */
+  }
+  if (upload(c, H.cmin, &p.cmin, st, err) || upload(c, H.cplu, &p.cplu, st, err) || upload(c, H.dmin, &p.dmin, st, err) ||
+      upload(c, H.dplu, &p.dplu, st, err) || upload(c, H.dzer, &p.dzer, st, err))
+    return 1;
+  if (upload(c, H.eq_sp, &p.eq_sp, st, err) || upload(c, H.eq_l, &p.eq_l, st, err) || upload(c, H.eq_m, &p.eq_m, st, err))
+    return 1;
+  if (upload(c, H.idx_I, &p.idx_I, st, err) || upload(c, H.idx_E, &p.idx_E, st, err) ||
+      upload(c, H.idx_B, &p.idx_B, st, err) || upload(c, H.idx_N, &p.idx_N, st, err))
+    return 1;
+  if (upload(c, H.qs_sp, &p.qs_sp, st, err) || upload(c, H.qs_l, &p.qs_l, st, err) || upload(c, H.qs_m, &p.qs_m, st, err))
+    return 1;
+  if (upload(c, items, &p.items, st, err)) return 1;
+  if (!first_order_mode) {
+    c->sources_len = (size_t)s.tp2_size * per_type;
+    if (alloc_dev(c, std::max<size_t>(1, c->sources_len) * sizeof(double), &tmp, err)) return 1;
+    c->d_sources = (double *)tmp;
+    CK(cudaMemsetAsync(c->d_sources, 0, std::max<size_t>(1, c->sources_len) * sizeof(double), st));
+    p.sources = c->d_sources;
+  } else {
+    c->fo_out_len = (size_t)sp->k_size * fo_tau_size * s.nfo;
+    if (alloc_dev(c, c->fo_out_len * sizeof(double), &tmp, err)) return 1;
+    c->d_fo_out = (double *)tmp;
+    p.fo_out = c->d_fo_out;
+  }
+  if (alloc_dev(c, sizeof(song2_triplet_stats) * std::max(1, s.n_items), &tmp, err)) return 1;
+  c->d_stats = (song2_triplet_stats *)tmp;
+  p.stats = c->d_stats;
+  /* Evolver scratch: the Jacobian blocks of each resident CTA, and the LU
+     blocks when they do not fit in shared memory. */
+  if (alloc_dev(c, (size_t)c->grid * s.lu_elems * sizeof(double), &tmp, err)) return 1;
+  p.jac = (double *)tmp;
+  if (!s.lu_in_smem) {
+    size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
+    if (alloc_dev(c, (size_t)c->grid * s.lu_elems * ts, &tmp, err)) return 1;
+    p.lu_global = tmp;
+  }
+  if (alloc_dev(c, sizeof(int), &tmp, err)) return 1;
+  c->d_queue = (int *)tmp;
+  p.queue = c->d_queue;
+  CK(cudaStreamSynchronize(st));
+  c->spec = s;
+  CK(cudaEventCreate(&c->ev0));
+  CK(cudaEventCreate(&c->ev1));
+  return 0;
+}
+
+void pair_tables(const song2_spec *sp, std::vector<int> &k3_off, std::vector<int> &k3_size,
+                 std::vector<int64_t> &pair_off) {
+  k3_off.clear(); k3_size.clear(); pair_off.clear();
+  int off = 0;
+  int64_t po = 0;
+  for (int i1 = 0; i1 < sp->k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2) {
+      int n3 = sp->k3_size[i1 * sp->k_size + i2];
+      k3_off.push_back(off);
+      k3_size.push_back(n3);
+      pair_off.push_back(po);
+      off += n3;
+      po += (int64_t)sp->tau_size * n3;
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+int song2_ctx_create(const song2_spec *spec, const song2_tables *tab, int precision, song2_ctx **out, char *err) {
+  *out = nullptr;
+  if (precision != SONG2_PREC_FP64 && precision != SONG2_PREC_MIXED) {
+    snprintf(err, SONG2_ERRLEN, "unknown precision %d", precision);
+    return 1;
+  }
+  std::vector<int> k3_off, k3_size;
+  std::vector<int64_t> pair_off;
+  pair_tables(spec, k3_off, k3_size, pair_off);
+  int n3tot = k3_off.empty() ? 0 : k3_off.back() + k3_size.back();
+  std::vector<double> k3(spec->k3, spec->k3 + n3tot);
+  /* work items, largest wavenumber first: the expensive triplets start early so the
+     persistent CTAs finish together (longest-processing-time order) */
+  std::vector<WorkItem> items;
+  std::vector<double> cost;
+  int pair = 0;
+  for (int i1 = 0; i1 < spec->k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2, ++pair)
+      for (int i3 = 0; i3 < k3_size[pair]; ++i3) {
+        items.push_back(WorkItem{i1, i2, i3, pair});
+        double kk = std::max(spec->k[i1], std::max(spec->k[i2], k3[k3_off[pair] + i3]));
+        cost.push_back(kk);
+      }
+  std::vector<size_t> order(items.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+  std::vector<WorkItem> sorted(items.size());
+  for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
+  song2_ctx *c = new song2_ctx();
+  memset((void *)&c->spec, 0, sizeof(c->spec));
+  if (ctx_setup(c, spec, tab, precision, 0, sorted, k3, k3_off, k3_size, pair_off, 0, 0, 0, 0, err)) {
+    song2_ctx_destroy(c);
+    return 1;
+  }
+  /* map of the sorted work order back to the natural order for the stats */
+  *out = c;
+  return 0;
+}
+
+int song2_ctx_destroy(song2_ctx *c) {
+  if (!c) return 0;
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  delete c;
+  return 0;
+}
+
+int song2_ctx_run(song2_ctx *c, void *stream, char *err) {
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
+  CK(cudaEventRecord(c->ev0, st));
+  if (song2_launch_evolver(c->spec, c->ptrs, c->precision, c->grid, c->block, c->smem, st)) {
+    snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return 1;
+  }
+  CK(cudaEventRecord(c->ev1, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  c->last_launches = 1;
+  return 0;
+}
+
+double *song2_ctx_device_sources(song2_ctx *c) { return c->d_sources; }
+song2_triplet_stats *song2_ctx_device_stats(song2_ctx *c) { return c->d_stats; }
+double song2_ctx_last_kernel_ms(song2_ctx *c) { return c->last_ms; }
+int song2_ctx_last_launches(song2_ctx *c) { return c->last_launches; }
+
+int song2_ctx_download(song2_ctx *c, double *flat, song2_triplet_stats *stats, char *err) {
+  if (flat && c->sources_len) CK(cudaMemcpy(flat, c->d_sources, c->sources_len * sizeof(double), cudaMemcpyDeviceToHost));
+  if (stats && c->n_items) {
+    /* stats are stored per sorted work item: return them in the reference's
+       work order (k1 descending, k2 <= k1, k3) */
+    std::vector<song2_triplet_stats> tmp(c->n_items);
+    std::vector<WorkItem> items(c->n_items);
+    CK(cudaMemcpy(tmp.data(), c->d_stats, sizeof(song2_triplet_stats) * c->n_items, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(items.data(), c->ptrs.items, sizeof(WorkItem) * c->n_items, cudaMemcpyDeviceToHost));
+    /* rank of (i1,i2,i3) in the reference order */
+    int ksz = c->spec.k_size;
+    std::vector<int64_t> k3s;
+    std::vector<int> k3size(c->n_items);
+    std::vector<int> h_k3size;
+    /* pair sizes */
+    int npairs = ksz * (ksz + 1) / 2;
+    h_k3size.resize(npairs);
+    CK(cudaMemcpy(h_k3size.data(), c->ptrs.k3_size, sizeof(int) * npairs, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> start(npairs, 0);
+    int64_t acc = 0;
+    for (int i1 = ksz - 1; i1 >= 0; --i1)
+      for (int i2 = 0; i2 <= i1; ++i2) {
+        int pr = i1 * (i1 + 1) / 2 + i2;
+        start[pr] = acc;
+        acc += h_k3size[pr];
+      }
+    for (int i = 0; i < c->n_items; ++i) stats[start[items[i].pair] + items[i].i3] = tmp[i];
+  }
+  return 0;
+}
+
+int song2_gpu_evolve(const song2_spec *spec, const song2_tables *tab, int precision, double ****sources_out,
+                     song2_triplet_stats *per_triplet, char *err) {
+  song2_ctx *c = nullptr;
+  if (song2_ctx_create(spec, tab, precision, &c, err)) return 1;
+  int rc = song2_ctx_run(c, nullptr, err);
+  std::vector<double> flat;
+  if (!rc) {
+    flat.resize(c->sources_len);
+    rc = song2_ctx_download(c, flat.data(), per_triplet, err);
+  }
+  if (!rc && sources_out) {
+    for (int tp = 0; tp < c->tp2_size; ++tp)
+      for (int i1 = 0; i1 < spec->k_size; ++i1)
+        for (int i2 = 0; i2 <= i1; ++i2) {
+          int64_t off = song2_pair_offset(spec, i1, i2);
+          int64_t len = (int64_t)spec->tau_size * spec->k3_size[i1 * spec->k_size + i2];
+          memcpy(sources_out[tp][i1][i2], flat.data() + (size_t)tp * c->per_type + off, sizeof(double) * len);
+        }
+  }
+  if (!rc && per_triplet) {
+    int64_t nt = song2_n_triplets(spec);
+    for (int64_t i = 0; i < nt; ++i)
+      if (per_triplet[i].status != SONG2_OK) {
+        snprintf(err, SONG2_ERRLEN, "triplet %lld failed with status %d", (long long)i, per_triplet[i].status);
+        rc = 1;
+        break;
+      }
+  }
+  song2_ctx_destroy(c);
+  return rc;
+}
+
+int song2_gpu_first_order(const song2_spec *spec2, const song2_tables *bg_only, int fo_l_max, int fo_tau_size,
+                          double fo_lntau0, double fo_dlntau, double *fo_out, char *err) {
+  song2_spec s = *spec2;
+  s.ic = SONG2_IC_AD_FIRST_ORDER;
+  /* first-order normalisation: primordial curvature zeta = 1 (C = -1/2) */
+  s.primordial_local_fnl_phi = 5.0 / 6.0;
+  s.m_size = 1;
+  s.m[0] = 0;
+  s.has_quadratic_sources = 0;
+  s.has_source_T = s.has_source_E = s.has_source_B = s.has_source_delta_cdm = 0;
+  /* evolve more multipoles than stored, so the truncation stays away from the table */
+  s.l_max_g = s.l_max_pol_g = s.l_max_ur = fo_l_max + 5;
+  s.l_max_los_t = s.l_max_los_p = 0;
+  /* one "triplet" (k, k, k) per k: without quadratic sources only k matters */
+  std::vector<int> k3_size_full((size_t)s.k_size * s.k_size, 0);
+  std::vector<WorkItem> items;
+  std::vector<double> k3;
+  std::vector<int> k3_off, k3_size;
+  std::vector<int64_t> pair_off;
+  for (int ik = 0; ik < s.k_size; ++ik) {
+    items.push_back(WorkItem{ik, ik, 0, ik});
+    k3.push_back(s.k[ik]);
+    k3_off.push_back(ik);
+    k3_size.push_back(1);
+    pair_off.push_back(0);
+  }
+  std::reverse(items.begin(), items.end());
+  song2_ctx *c = new song2_ctx();
+  memset((void *)&c->spec, 0, sizeof(c->spec));
+  song2_tables t = *bg_only;
+  if (ctx_setup(c, &s, &t, SONG2_PREC_FP64, 1, items, k3, k3_off, k3_size, pair_off, fo_tau_size, fo_lntau0, fo_dlntau,
+                fo_l_max, err)) {
+    song2_ctx_destroy(c);
+    return 1;
+  }
+  int rc = song2_ctx_run(c, nullptr, err);
+  if (!rc) {
+    cudaError_t e = cudaMemcpy(fo_out, c->d_fo_out, c->fo_out_len * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { snprintf(err, SONG2_ERRLEN, "download: %s", cudaGetErrorString(e)); rc = 1; }
+  }
+  if (!rc) {
+    std::vector<song2_triplet_stats> st(c->n_items);
+    cudaMemcpy(st.data(), c->d_stats, sizeof(song2_triplet_stats) * c->n_items, cudaMemcpyDeviceToHost);
+    for (auto &x : st)
+      if (x.status != SONG2_OK) {
+        snprintf(err, SONG2_ERRLEN, "first-order mode failed with status %d", x.status);
+        rc = 1;
+        break;
+      }
+  }
+  song2_ctx_destroy(c);
+  return rc;
+}
+
+} /* extern "C" */

@@ -1,0 +1,485 @@
+/*
+ * song2_host.c - host-side C of the GB300 second-order evolver.
+ *
+ * Contents:
+ *  - spec helpers: triplet counting, pair offsets of the flat source buffer;
+ *  - defaults of the hot-path parameters (source/input2.c:2027-2371);
+ *  - a flat LCDM background and a Peebles-type hydrogen recombination, the
+ *    stand-in for CLASS background_init/thermodynamics_init, which SONG calls
+ *    before perturb2_init (main/song.c:55-69) but which is not part of the
+ *    reference tree (the CLASS submodule is empty);
+ *  - uniform-grid natural cubic splines (both the device evolver and the
+ *    first-order provider interpolate with them);
+ *  - the coupling coefficients C and D used by perturb2_get_lm_lists
+ *    (perturbations2.c:1236-1271), written as closed forms of the
+ *    Clebsch-Gordan coefficients <l' m1; 1 q | l m>;
+ *  - the start-time bisection of perturb2_start_time_evolution
+ *    (perturbations2.c:3388-3524).
+ */
+#include "song2.h"
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+/* ------------------------------------------------------------------ spec */
+
+int song2_fo_size(int fo_l_max) {
+  /* scalars + I_l, E_l, N_l, collision_g_l for l = 0..fo_l_max */
+  return SONG2_FO_I + 4 * (fo_l_max + 1);
+}
+
+int64_t song2_n_triplets(const song2_spec *s) {
+  int64_t n = 0;
+  for (int i1 = 0; i1 < s->k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2) n += s->k3_size[i1 * s->k_size + i2];
+  return n;
+}
+
+static int size_l_indexm(int l_max, const int *m, int m_size) {
+  /* number of (l,m) pairs with l <= l_max, m in the list, m <= l */
+  int n = 0;
+  for (int l = 0; l <= l_max; ++l)
+    for (int i = 0; i < m_size; ++i)
+      if (m[i] <= l) ++n;
+  return n;
+}
+
+int song2_tp2_size(const song2_spec *s) {
+  /* perturb2_indices_of_perturbs (perturbations2.c:667-1075): T, E, B blocks
+     of size_l_indexm(l_max_los) each, then delta_cdm. */
+  int n = 0;
+  if (s->has_source_T) n += size_l_indexm(s->l_max_los_t, s->m, s->m_size);
+  if (s->has_source_E) n += size_l_indexm(s->l_max_los_p, s->m, s->m_size);
+  if (s->has_source_B) n += size_l_indexm(s->l_max_los_p, s->m, s->m_size);
+  if (s->has_source_delta_cdm) n += 1;
+  return n;
+}
+
+int64_t song2_pair_offset(const song2_spec *s, int index_k1, int index_k2) {
+  int64_t off = 0;
+  for (int i1 = 0; i1 < s->k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2) {
+      if (i1 == index_k1 && i2 == index_k2) return off;
+      off += (int64_t)s->tau_size * s->k3_size[i1 * s->k_size + i2];
+    }
+  return off;
+}
+
+int64_t song2_sources_per_type(const song2_spec *s) {
+  return (int64_t)s->tau_size * song2_n_triplets(s);
+}
+
+void song2_spec_defaults(song2_spec *s) {
+  memset(s, 0, sizeof(*s));
+  s->l_max_g = s->l_max_pol_g = s->l_max_ur = 8;         /* input2.c:2257-2259 */
+  s->l_max_los_t = s->l_max_los_p = 2;                   /* input2.c:2265-2266 */
+  s->m_size = 1; s->m[0] = 0;                            /* input2.c:2268-2270 */
+  s->has_polarization2 = 1;
+  s->has_quadratic_sources = 1;
+  s->has_quadratic_liouville = 1;
+  s->has_quadratic_collision = 1;
+  s->tight_coupling = 1;                                 /* tca2_first_order_pitrou */
+  s->tca_trigger_tau_c_over_tau_h = 0.01;                /* input2.c:2136 */
+  s->tca_trigger_tau_c_over_tau_k = 0.007;               /* input2.c:2137 */
+  s->ic = SONG2_IC_AD;
+  s->has_source_T = 1; s->has_source_E = 1; s->has_source_B = 0;
+  s->rtol = 1e-4;                                        /* input2.c:2248 */
+  s->threshold = 1e-6;
+  s->max_steps = 200000;
+  s->start_small_k_at_tau_c_over_tau_h = 0.0015;         /* input2.c:2280 */
+  s->start_large_k_at_tau_h_over_tau_k = 0.07;           /* input2.c:2281 */
+  s->tol_tau_approx = 1e-10;
+}
+
+/* ------------------------------------------------------------- splines */
+
+void song2_spline_uniform(int n, int ncol, double dx, const double *y, double *dd) {
+  /* Natural cubic spline on a uniform grid: solve the tridiagonal system
+     dd[i-1] + 4 dd[i] + dd[i+1] = 6 (y[i+1]-2y[i]+y[i-1])/dx^2, dd[0]=dd[n-1]=0,
+     column by column with the Thomas algorithm. */
+  double *c = (double *)malloc(sizeof(double) * (size_t)n);
+  for (int q = 0; q < ncol; ++q) {
+    dd[q] = 0.0;
+    if (n < 3) { for (int i = 0; i < n; ++i) dd[(size_t)i * ncol + q] = 0.0; continue; }
+    c[0] = 0.0;
+    double prev = 0.0; /* modified rhs of the previous row */
+    for (int i = 1; i < n - 1; ++i) {
+      double r = 6.0 * (y[(size_t)(i + 1) * ncol + q] - 2.0 * y[(size_t)i * ncol + q] +
+                        y[(size_t)(i - 1) * ncol + q]) / (dx * dx);
+      double b = 4.0 - c[i - 1];
+      c[i] = 1.0 / b;
+      prev = (r - prev) / b;
+      dd[(size_t)i * ncol + q] = prev;
+    }
+    dd[(size_t)(n - 1) * ncol + q] = 0.0;
+    for (int i = n - 2; i >= 1; --i)
+      dd[(size_t)i * ncol + q] -= c[i] * dd[(size_t)(i + 1) * ncol + q];
+  }
+  free(c);
+}
+
+static double spline_eval_uniform(int n, int ncol, double x0, double dx, const double *y,
+                                  const double *dd, int q, double x) {
+  double u = (x - x0) / dx;
+  int i = (int)floor(u);
+  if (i < 0) i = 0;
+  if (i > n - 2) i = n - 2;
+  double b = u - i, a = 1.0 - b;
+  return a * y[(size_t)i * ncol + q] + b * y[(size_t)(i + 1) * ncol + q] +
+         ((a * a * a - a) * dd[(size_t)i * ncol + q] + (b * b * b - b) * dd[(size_t)(i + 1) * ncol + q]) *
+             (dx * dx) / 6.0;
+}
+
+/* --------------------------------------------------------- background */
+
+/* Physical constants (SI) */
+#define C_LIGHT 2.99792458e8
+#define MPC_M 3.0856775814913673e22
+#define SIGMA_T 6.6524587158e-29
+#define K_B 1.380649e-23
+#define M_ELECTRON 9.1093837015e-31
+#define H_PLANCK 6.62607015e-34
+#define M_H 1.673575e-27
+#define EV 1.602176634e-19
+#define RHO_CRIT_H2 1.87834e-26 /* kg/m^3 for h = 1 */
+
+typedef struct {
+  double rho_g0, rho_ur0, rho_b0, rho_cdm0, rho_L0; /* CLASS units, Mpc^-2 */
+} bg_params;
+
+static void bg_rhos(const bg_params *p, double a, double *rg, double *rur, double *rb, double *rc, double *rl) {
+  double a2 = a * a, a3 = a2 * a, a4 = a2 * a2;
+  *rg = p->rho_g0 / a4; *rur = p->rho_ur0 / a4;
+  *rb = p->rho_b0 / a3; *rc = p->rho_cdm0 / a3; *rl = p->rho_L0;
+}
+
+static double bg_H(const bg_params *p, double a) {
+  double rg, rur, rb, rc, rl;
+  bg_rhos(p, a, &rg, &rur, &rb, &rc, &rl);
+  return sqrt(rg + rur + rb + rc + rl);
+}
+
+/* dtau / dln a = 1 / (a H) */
+static double dtau_dlna(const bg_params *p, double lna) {
+  double a = exp(lna);
+  return 1.0 / (a * bg_H(p, a));
+}
+
+/* Peebles three-level hydrogen recombination (Peebles 1968, with the
+   case-B recombination fit of Pequignot et al. 1991 and the fudge factor 1.14
+   of Seager, Sasselov & Scott 1999); helium is taken as neutral and the
+   matter temperature equal to the radiation temperature.  Returns x_e(z) on
+   a table of z. */
+typedef struct { int n; double z0, dz; double *xe; } xe_table;
+
+static double saha_xe(double T, double nH) {
+  /* x^2/(1-x) = (2 pi m_e k T / h^2)^{3/2} e^{-13.6eV/kT} / n_H */
+  double S = pow(2.0 * M_PI * M_ELECTRON * K_B * T / (H_PLANCK * H_PLANCK), 1.5) *
+             exp(-13.605693 * EV / (K_B * T)) / nH;
+  if (S > 1e20) return 1.0;
+  return 0.5 * (-S + sqrt(S * S + 4.0 * S));
+}
+
+static int recombination(const song2_cosmo *c, const bg_params *bp, xe_table *tab) {
+  double h = c->h;
+  double nH0 = (1.0 - c->YHe) * c->omega_b * RHO_CRIT_H2 / M_H; /* m^-3 (omega_b = Omega_b h^2) */
+  tab->n = 40001; tab->z0 = 0.0; tab->dz = 0.25; /* z in [0, 10000] */
+  tab->xe = (double *)malloc(sizeof(double) * tab->n);
+  if (!tab->xe) return 1;
+  (void)h;
+  const double lambda_a = 121.5682e-9, Lambda2s = 8.2245809, E2s = 13.605693 * EV / 4.0;
+  const double Ealpha = 13.605693 * EV * 0.75;
+  /* march from z = 10000 down; Saha until x drops below 0.985, then Peebles
+     with a backward-Euler step solved by Newton iteration on x */
+  int peebles = 0;
+  double x = 1.0;
+  for (int i = tab->n - 1; i >= 0; --i) {
+    double z = tab->z0 + i * tab->dz;
+    double T = c->T_cmb * (1.0 + z);
+    double nH = nH0 * pow(1.0 + z, 3);
+    if (!peebles) {
+      double xs = saha_xe(T, nH);
+      if (xs > 0.985) { x = xs; tab->xe[i] = x; continue; }
+      peebles = 1;
+      x = xs;
+      tab->xe[i] = x;
+      continue;
+    }
+    /* one backward-Euler step from z+dz to z: x_new = x_old - dz * f(z, x_new) where
+       f = dx/dz of the Peebles equation */
+    double a = 1.0 / (1.0 + z);
+    double H_si = bg_H(bp, a) * C_LIGHT / MPC_M; /* 1/s */
+    double tt = T / 1e4;
+    double alphaB = 1.14 * 1e-19 * 4.309 * pow(tt, -0.6166) / (1.0 + 0.6703 * pow(tt, 0.5300)); /* m^3/s */
+    double betaB = alphaB * pow(2.0 * M_PI * M_ELECTRON * K_B * T / (H_PLANCK * H_PLANCK), 1.5) * exp(-E2s / (K_B * T));
+    double K = pow(lambda_a, 3) / (8.0 * M_PI * H_si);
+    double boltz = exp(-Ealpha / (K_B * T));
+    double xold = x, xn = x;
+    for (int it = 0; it < 50; ++it) {
+      double one_m = 1.0 - xn;
+      double Cr = (1.0 + K * Lambda2s * nH * one_m) / (1.0 + K * (Lambda2s + betaB) * nH * one_m);
+      double rate = Cr * (alphaB * nH * xn * xn - betaB * one_m * boltz); /* -dx/dt [1/s] */
+      double f = rate / (H_si * (1.0 + z)); /* dx/dz */
+      double g = xn - xold + tab->dz * f;   /* going down in z: x(z) = x(z+dz) - dz*dx/dz */
+      /* derivative of g wrt xn (numerical) */
+      double eps = 1e-7 * (fabs(xn) + 1e-12);
+      double xp = xn + eps, om2 = 1.0 - xp;
+      double Cr2 = (1.0 + K * Lambda2s * nH * om2) / (1.0 + K * (Lambda2s + betaB) * nH * om2);
+      double f2 = Cr2 * (alphaB * nH * xp * xp - betaB * om2 * boltz) / (H_si * (1.0 + z));
+      double dg = 1.0 + tab->dz * (f2 - f) / eps;
+      double step = g / dg;
+      xn -= step;
+      if (xn < 1e-12) xn = 1e-12;
+      if (xn > 1.0) xn = 1.0;
+      if (fabs(step) < 1e-14 * fabs(xn)) break;
+    }
+    x = xn;
+    tab->xe[i] = x;
+  }
+  return 0;
+}
+
+static double xe_at_z(const xe_table *t, double z) {
+  if (z >= t->z0 + (t->n - 1) * t->dz) return t->xe[t->n - 1];
+  if (z <= t->z0) return t->xe[0];
+  double u = (z - t->z0) / t->dz;
+  int i = (int)u;
+  double f = u - i;
+  return (1 - f) * t->xe[i] + f * t->xe[i + 1];
+}
+
+int song2_background_compute(const song2_cosmo *c, int bg_size, double *bg, double *bg_dd,
+                             double *lntau0_out, double *dlntau_out, double *tau0_out,
+                             double *a_eq_out, char *err) {
+  if (bg_size < 16) { snprintf(err, SONG2_ERRLEN, "bg_size too small"); return 1; }
+  bg_params p;
+  double H0 = c->h / 2997.92458; /* 1/Mpc */
+  double Og = 2.472819e-5 * pow(c->T_cmb / 2.7255, 4) / (c->h * c->h);
+  double Our = c->N_eff * 7.0 / 8.0 * pow(4.0 / 11.0, 4.0 / 3.0) * Og;
+  double Ob = c->omega_b / (c->h * c->h), Oc = c->omega_cdm / (c->h * c->h);
+  double OL = 1.0 - Og - Our - Ob - Oc;
+  p.rho_g0 = H0 * H0 * Og; p.rho_ur0 = H0 * H0 * Our;
+  p.rho_b0 = H0 * H0 * Ob; p.rho_cdm0 = H0 * H0 * Oc; p.rho_L0 = H0 * H0 * OL;
+  *a_eq_out = (Og + Our) / (Ob + Oc);
+
+  /* tau(a) by Simpson integration on a fine ln a grid, starting from the
+     radiation-era limit tau = a / sqrt(rho_r0). */
+  const int NA = 200001;
+  const double lna_min = log(1e-12), lna_max = 0.0;
+  double dl = (lna_max - lna_min) / (NA - 1);
+  double *lntau_a = (double *)malloc(sizeof(double) * NA);
+  double tau = exp(lna_min) / sqrt(p.rho_g0 + p.rho_ur0);
+  lntau_a[0] = log(tau);
+  for (int i = 1; i < NA; ++i) {
+    double l0 = lna_min + (i - 1) * dl;
+    tau += dl / 6.0 * (dtau_dlna(&p, l0) + 4.0 * dtau_dlna(&p, l0 + 0.5 * dl) + dtau_dlna(&p, l0 + dl));
+    lntau_a[i] = log(tau);
+  }
+  double tau0 = tau;
+  *tau0_out = tau0;
+
+  xe_table xt;
+  if (recombination(c, &p, &xt)) { free(lntau_a); snprintf(err, SONG2_ERRLEN, "recombination alloc"); return 1; }
+
+  /* ln tau grid from tau = 1e-3 Mpc to tau0 */
+  double lt0 = log(1e-3), lt1 = log(tau0);
+  double dlt = (lt1 - lt0) / (bg_size - 1);
+  *lntau0_out = lt0; *dlntau_out = dlt;
+  double nH0 = (1.0 - c->YHe) * c->omega_b * RHO_CRIT_H2 / M_H;
+  double *kdot = (double *)malloc(sizeof(double) * bg_size);
+  int j = 0;
+  for (int i = 0; i < bg_size; ++i) {
+    double lt = lt0 + i * dlt;
+    if (i == bg_size - 1) lt = lt1;
+    /* invert ln tau(ln a): bracket, then cubic Hermite with d ln tau / d ln a = 1/(tau a H) */
+    while (j < NA - 2 && lntau_a[j + 1] < lt) ++j;
+    double lna;
+    if (lt <= lntau_a[0]) {
+      lna = lna_min + (lt - lntau_a[0]); /* radiation era: a proportional to tau */
+    } else {
+      double x0 = lntau_a[j], x1 = lntau_a[j + 1];
+      double y0 = lna_min + j * dl, y1 = y0 + dl;
+      double d0 = exp(x0) / dtau_dlna(&p, y0), d1 = exp(x1) / dtau_dlna(&p, y1); /* dln a/dln tau */
+      double hh = x1 - x0, t = (lt - x0) / hh;
+      double h00 = 2 * t * t * t - 3 * t * t + 1, h10 = t * t * t - 2 * t * t + t;
+      double h01 = -2 * t * t * t + 3 * t * t, h11 = t * t * t - t * t;
+      lna = h00 * y0 + h10 * hh * d0 + h01 * y1 + h11 * hh * d1;
+    }
+    double a = exp(lna);
+    double rg, rur, rb, rc, rl;
+    bg_rhos(&p, a, &rg, &rur, &rb, &rc, &rl);
+    double H = sqrt(rg + rur + rb + rc + rl);
+    double Hc = a * H;
+    /* d(aH)/dtau = a^2 H^2 - 3/2 a^2 sum (rho + p) */
+    double Hcp = a * a * H * H - 1.5 * a * a * (4.0 / 3.0 * (rg + rur) + rb + rc);
+    double taun = exp(lt);
+    double z = 1.0 / a - 1.0;
+    double xe = xe_at_z(&xt, z);
+    double ne = xe * nH0 / (a * a * a);
+    kdot[i] = a * ne * SIGMA_T * MPC_M;
+    double *row = bg + (size_t)i * SONG2_BG_SIZE;
+    row[SONG2_BG_LN_A] = lna;
+    row[SONG2_BG_LN_HC] = log(Hc);
+    row[SONG2_BG_HC_PRIME_TAU2] = Hcp * taun * taun;
+    row[SONG2_BG_LN_RHO_G] = log(rg);
+    row[SONG2_BG_LN_RHO_B] = log(rb);
+    row[SONG2_BG_LN_RHO_CDM] = log(rc);
+    row[SONG2_BG_LN_RHO_UR] = log(rur);
+    row[SONG2_BG_LN_KAPPA_DOT] = log(kdot[i]);
+  }
+  /* optical depth kappa(tau) = int_tau^tau0 kappa_dot dtau' (trapezoid in ln tau) */
+  double kap = 0.0;
+  bg[(size_t)(bg_size - 1) * SONG2_BG_SIZE + SONG2_BG_KAPPA] = 0.0;
+  for (int i = bg_size - 2; i >= 0; --i) {
+    double t0 = exp(lt0 + i * dlt), t1 = exp(lt0 + (i + 1) * dlt);
+    kap += 0.5 * dlt * (kdot[i] * t0 + kdot[i + 1] * t1);
+    bg[(size_t)i * SONG2_BG_SIZE + SONG2_BG_KAPPA] = kap;
+  }
+  song2_spline_uniform(bg_size, SONG2_BG_SIZE, dlt, bg, bg_dd);
+  free(kdot); free(lntau_a); free(xt.xe);
+  return 0;
+}
+
+/* ---------------------------------------------------- coupling coefficients */
+/* With the SONG multipole convention f(n) = sum_lm (-i)^l sqrt(4pi/(2l+1)) f_lm Y_lm(n)
+   the (l,m) multipole of (n . v) f, v = sum_q v_[q] n_[q]-components, is
+   sum_q v_[q] [ c_minus(l,m-q,m) f_{l-1,m-q} - c_plus(l,m-q,m) f_{l+1,m-q} ] (times i),
+   with c_minus = <l-1 0;1 0|l 0><l-1 m1;1 q|l m> and
+        c_plus  = <l+1 0;1 0|l 0><l+1 m1;1 q|l m>  (Condon-Shortley phases).
+   The spin-2 coefficients differ by the ratio of the spin-2 and spin-0 3j symbols,
+   and d_zero is the l' = l coupling of the spin-2 harmonics that mixes E and B. */
+
+double song2_coupling_c_minus(int l, int m1, int m) {
+  if (l < 1 || abs(m) > l || abs(m1) > l - 1) return 0.0;
+  double L = l;
+  if (m1 == m) return sqrt(L * L - (double)m * m) / (2 * L - 1);
+  if (m1 == m - 1) return sqrt((L + m - 1) * (L + m) / 2.0) / (2 * L - 1);
+  if (m1 == m + 1) return sqrt((L - m - 1) * (L - m) / 2.0) / (2 * L - 1);
+  return 0.0;
+}
+
+double song2_coupling_c_plus(int l, int m1, int m) {
+  if (l < 0 || abs(m) > l || abs(m1) > l + 1) return 0.0;
+  double L = l;
+  if (m1 == m) return sqrt((L + 1) * (L + 1) - (double)m * m) / (2 * L + 3);
+  if (m1 == m - 1) return -sqrt((L - m + 1) * (L - m + 2) / 2.0) / (2 * L + 3);
+  if (m1 == m + 1) return -sqrt((L + m + 1) * (L + m + 2) / 2.0) / (2 * L + 3);
+  return 0.0;
+}
+
+double song2_coupling_d_minus(int l, int m1, int m) {
+  if (l <= 2) return 0.0;
+  return song2_coupling_c_minus(l, m1, m) * sqrt((double)l * l - 4.0) / l;
+}
+
+double song2_coupling_d_plus(int l, int m1, int m) {
+  if (l < 2) return 0.0;
+  return song2_coupling_c_plus(l, m1, m) * sqrt((double)(l + 1) * (l + 1) - 4.0) / (l + 1);
+}
+
+double song2_coupling_d_zero(int l, int m1, int m) {
+  if (l < 2 || abs(m) > l || abs(m1) > l) return 0.0;
+  double L = l, pre = 2.0 / (L * (L + 1));
+  if (m1 == m) return pre * m;
+  if (m1 == m - 1) return -pre * sqrt((L + m) * (L - m + 1) / 2.0);
+  if (m1 == m + 1) return pre * sqrt((L - m) * (L + m + 1) / 2.0);
+  return 0.0;
+}
+
+/* ------------------------------------------------------------ start time */
+
+static void bg_eval_host(const song2_tables *t, double tau, double *Hc, double *kappa_dot) {
+  double x = log(tau);
+  *Hc = exp(spline_eval_uniform(t->bg_size, SONG2_BG_SIZE, t->bg_lntau0, t->bg_dlntau, t->bg, t->bg_dd,
+                                SONG2_BG_LN_HC, x));
+  *kappa_dot = exp(spline_eval_uniform(t->bg_size, SONG2_BG_SIZE, t->bg_lntau0, t->bg_dlntau, t->bg,
+                                       t->bg_dd, SONG2_BG_LN_KAPPA_DOT, x));
+}
+
+int song2_start_time(const song2_spec *s, const song2_tables *t, double k, double tau_upper,
+                     double *tau_ini, char *err) {
+  double tau_lower = exp(t->bg_lntau0);
+  double Hc, kd;
+  bg_eval_host(t, tau_lower, &Hc, &kd);
+  if (Hc / kd > s->start_small_k_at_tau_c_over_tau_h || k / Hc > s->start_large_k_at_tau_h_over_tau_k) {
+    snprintf(err, SONG2_ERRLEN, "start time: background table starts too late for k=%g (tau_c/tau_h=%g, k/aH=%g)",
+             k, Hc / kd, k / Hc);
+    return 1;
+  }
+  double tau_mid = 0.5 * (tau_lower + tau_upper);
+  int it = 0;
+  while ((tau_upper - tau_lower) / tau_lower > s->tol_tau_approx && it < 200) {
+    bg_eval_host(t, tau_mid, &Hc, &kd);
+    if (Hc / kd > s->start_small_k_at_tau_c_over_tau_h || k / Hc > s->start_large_k_at_tau_h_over_tau_k)
+      tau_upper = tau_mid;
+    else
+      tau_lower = tau_mid;
+    tau_mid = 0.5 * (tau_lower + tau_upper);
+    ++it;
+  }
+  *tau_ini = tau_mid;
+  return 0;
+}
+
+/* --------------------------------------------------------------- grids */
+/* perturb2_get_k_lists (perturbations2.c:1573-2530), lin/log sampling only,
+   and the custom time sampling of perturb2_timesampling_for_sources
+   (perturbations2.c:2580-2598). */
+
+static void lin_space(double *out, double a, double b, int n) {
+  for (int i = 0; i < n; ++i) out[i] = (n > 1) ? a + i * (b - a) / (n - 1) : a;
+}
+
+static void log_space(double *out, double a, double b, int n) {
+  double la = log(a), lb = log(b);
+  for (int i = 0; i < n; ++i) out[i] = (n > 1) ? exp(la + i * (lb - la) / (n - 1)) : a;
+}
+
+int song2_k_grid(int log_sampling, double k_min, double k_max, int k_size, double *k_out) {
+  if (k_size < 1 || k_min <= 0 || k_max < k_min) return 1;
+  if (log_sampling) log_space(k_out, k_min, k_max, k_size);
+  else lin_space(k_out, k_min, k_max, k_size);
+  return 0;
+}
+
+int song2_k3_grids(const double *k, int k_size, int k3_size, int log_sampling, int *k3_size_out,
+                   double *k3_out, char *err) {
+  /* k3 in [max(|k1-k2| + 1e-10, (k1+k2)/100, k_min), min(k1+k2 - 1e-10, k_max)]
+     (perturbations2.c:1973-1984, _MIN_K3_DISTANCE_ and _MIN_K3_RATIO_ of
+     include/perturbations2.h:178,187) */
+  int64_t off = 0;
+  for (int i1 = 0; i1 < k_size; ++i1)
+    for (int i2 = 0; i2 < k_size; ++i2) k3_size_out[i1 * k_size + i2] = 0;
+  for (int i1 = 0; i1 < k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2) {
+      double k1 = k[i1], k2 = k[i2];
+      double k3_min = fabs(k1 - k2) + 1e-10, k3_max = k1 + k2 - 1e-10;
+      if ((k1 + k2) / 100 > k3_min) k3_min = (k1 + k2) / 100;
+      if (k[0] > k3_min) k3_min = k[0];
+      if (k[k_size - 1] < k3_max) k3_max = k[k_size - 1];
+      if (k3_min >= k3_max) {
+        snprintf(err, SONG2_ERRLEN, "found k3_min=%g>k3_max=%g for k1(%d)=%g and k2(%d)=%g", k3_min, k3_max,
+                 i1, k1, i2, k2);
+        return 1;
+      }
+      k3_size_out[i1 * k_size + i2] = k3_size;
+      if (k3_out) {
+        if (log_sampling) log_space(k3_out + off, k3_min, k3_max, k3_size);
+        else lin_space(k3_out + off, k3_min, k3_max, k3_size);
+      }
+      off += k3_size;
+    }
+  return 0;
+}
+
+int song2_tau_grid(int log_sampling, double tau_ini, double tau_end, int tau_size, double *out) {
+  if (tau_size < 1 || tau_ini <= 0 || tau_end < tau_ini) return 1;
+  if (log_sampling) log_space(out, tau_ini, tau_end, tau_size);
+  else lin_space(out, tau_ini, tau_end, tau_size);
+  return 0;
+}

@@ -1,0 +1,102 @@
+/*
+ * song2_internal.h - device-side data layout shared by the evolver kernel
+ * (song2_kernels.cu) and the C ABI host code (song2_capi.cu).
+ */
+#ifndef SONG2_INTERNAL_H
+#define SONG2_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "song2.h"
+
+#define S2_LMAXP (SONG2_MAX_L + 4)
+#define S2_MAXBLK SONG2_MAX_M
+#define S2_MAXTP 64
+
+/* species codes of the state vector and of the quadratic-source vector */
+enum { SP_I = 0, SP_E, SP_B, SP_N, SP_B000, SP_B11, SP_C000, SP_C11, SP_PHI, SP_PHIP, SP_OMEGA, SP_GAMMA, SP_GAMMAP,
+       SP_METRIC, SP_NONE };
+
+/* source types */
+enum { TP_T = 0, TP_E, TP_B, TP_D };
+
+/* Everything that is constant for a run; passed to the kernel by value. */
+struct DevSpec {
+  int l_max_g, l_max_pol, l_max_ur, l_los_t, l_los_p;
+  int m_size, m[SONG2_MAX_M], compute_m[SONG2_MAX_M], index_m[SONG2_MAX_M];
+  int index_m_max[S2_LMAXP];
+  int L_big, Lq, mq_max;          /* rotation coefficients for l <= Lq, 0 <= m <= mq_max */
+  int has_pol, has_qs, has_liou, has_coll, tca_on;
+  double tca_h, tca_k;
+  int ic;
+  double fnl;
+  int los_pure_scat, los_quad_scat, los_pure_metric, los_quad_metric, los_time_delay, los_redshift, los_lensing;
+  int los_sw, los_isw, los_exp_pot;
+  double rtol, threshold;
+  int max_steps;
+  double start_h, start_k, tol_tau;
+  /* (l,m) tables */
+  int n_lm;                        /* pairs l <= Lq, m in the list, m <= l */
+  short lm_array[S2_LMAXP][SONG2_MAX_M];
+  int n_lmq;                       /* pairs l <= Lq, 0 <= m <= min(l, mq_max) */
+  short lmq[S2_LMAXP][SONG2_MAX_M + 2];
+  /* quadratic-source layout */
+  int qs2_size, iq_g, iq_E, iq_B, iq_ur, iq_b, iq_cdm;
+  int iq_psi, iq_psi_prime, iq_phi_prime_poisson, iq_phi_prime_longitudinal, iq_phi_prime_prime;
+  int iq_omega_m1_prime, iq_gamma_m2_prime_prime, iq_vv_g, iq_vv_ur, iq_dd_b, iq_vv_b, iq_vv_cdm;
+  short iq_b11[2], iq_c11[2], iq_b000, iq_c000;
+  /* state layout (grouped by m blocks) */
+  int n;
+  int nblk, blk_start[S2_MAXBLK], blk_size[S2_MAXBLK];
+  int idx_phi, idx_phip, idx_omega, idx_gamma, idx_gammap, idx_b000, idx_c000, idx_b11[2], idx_c11[2];
+  /* first-order table */
+  int fo_l_max, nfo, fo_E, fo_N, fo_CG, fo_tau_size, fo_k_size;
+  double fo_lntau0, fo_dlntau;
+  int bg_size;
+  double bg_lntau0, bg_dlntau;
+  /* sources */
+  int tp2_size;
+  int tp_kind[S2_MAXTP], tp_l[S2_MAXTP], tp_m[S2_MAXTP];
+  int mode_first_order;
+  int tau_size;
+  int64_t per_type;
+  int k_size;
+  int n_items;
+  /* shared-memory plan */
+  int lu_in_smem;
+  int lu_elems;                    /* sum of blk_size^2 */
+  int lu_off[S2_MAXBLK];
+};
+
+/* Per-triplet work item: indices and where its sources go. */
+struct WorkItem {
+  int i1, i2, i3, pair;            /* pair = index of (i1,i2) in pair order */
+};
+
+/* Device pointers of a run. */
+struct DevPtrs {
+  const double *k, *k3, *tau;
+  const int *k3_off, *k3_size;     /* per pair */
+  const int64_t *pair_off;         /* per pair, in doubles, within one source type */
+  const double *bg, *bg_dd, *fo, *fo_dd;
+  const double *cmin, *cplu, *dmin, *dplu, *dzer;   /* [n_lm][3] */
+  const short *eq_sp, *eq_l, *eq_m;                  /* [n] */
+  const short *idx_I, *idx_E, *idx_B, *idx_N;        /* [n_lm] -> state index or -1 */
+  const short *qs_sp, *qs_l, *qs_m;                  /* [qs2_size] */
+  const WorkItem *items;
+  double *sources;                 /* [tp2][per_type] */
+  double *fo_out;                  /* first-order mode: [k][tau][q] */
+  song2_triplet_stats *stats;      /* [n_items] */
+  double *jac;                     /* per-CTA scratch: sum blk^2 doubles each */
+  void *lu_global;                 /* per-CTA LU scratch when not in smem */
+  int *queue;                      /* work-queue counter */
+};
+
+/* host-side launcher implemented in song2_kernels.cu */
+int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int grid, int block,
+                         size_t smem, cudaStream_t stream);
+size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in_smem);
+int song2_max_ctas_per_sm(int precision, int block, size_t smem);
+
+#endif

@@ -1,0 +1,1751 @@
+/*
+ * song2_kernels.cu - the GB300 evolver of SONG's second-order system.
+ *
+ * One CTA evolves one (k1,k2,k3) triplet at a time and pulls the next one from
+ * a device work queue (persistent kernel).  Inside a CTA:
+ *   - background/thermo and first-order interpolation (cubic splines in ln tau)
+ *     and the quadratic sources (perturbations2.c:10643-11813) are computed
+ *     thread-parallel into shared memory;
+ *   - the right-hand side of perturb2_derivs (perturbations2.c:7636-8451) is
+ *     evaluated by a per-equation row function, one thread per equation, after
+ *     thread 0 has formed the shared "workspace" scalars (workspace_at_tau,
+ *     tca_variables, einstein: perturbations2.c:8484-9738);
+ *   - the system is affine, dy = A(tau) y + s(tau), so the Jacobian is exact:
+ *     column j is the row function applied to the unit vector e_j, one thread
+ *     per column, with the sources switched off;
+ *   - azimuthal modes never couple, so the NDF iteration matrix I - h*gamma*J is
+ *     block diagonal in m; every m block is LU-factorised (partial pivoting) and
+ *     solved by one warp, in FP64 (plain form) or FP32 (mixed form: the Newton
+ *     residual, error estimate and step control stay FP64, the simplified Newton
+ *     iteration doubles as iterative refinement);
+ *   - the integrator is the variable-order NDF method of Shampine & Reichelt
+ *     (1997), the same algorithm as the CPU restatement in oracle/.
+ * Every loop is bounded (max_steps, 4 Newton iterations, 200 bisection steps);
+ * a triplet that breaches a bound retires with a status code.  No kernel spins.
+ */
+#include <math.h>
+#include <stdio.h>
+
+#include "song2_internal.h"
+
+#define SQRT_2 1.4142135623730950488
+#define SQRT_3 1.7320508075688772935
+#define SQRT_6 2.4494897427831780982
+#define FOUR_THIRDS (4.0 / 3.0)
+
+namespace {
+
+/* ------------------------------------------------------------------ smem */
+
+struct BgV {
+  double a, a_sq, Hc, Hc_prime, rho_g, rho_b, rho_cdm, rho_ur, kappa_dot, exp_m_kappa, g, r;
+};
+
+struct Tri {
+  double k1, k2, k, k_sq, cosk1k2, cosk1k, cosk2k, k1_dot_k2;
+  double k1_m[3], k2_m[3], k1_ten_k2[5], k1_ten_k1[5], k2_ten_k2[5];
+  double tau_ini, tau_switch, tau_end;
+  int i1, i2, i3, pair, item, tca0, nint, k3_size;
+  int64_t pair_off;
+};
+
+/* Shared "workspace" scalars; every entry is affine in y. */
+struct WS {
+  double I_00, N_00, N_1m[3], I_1m[3], I_2m[3], E_2m[3], B_2m[3], C_1m[3], b_200, b_22m[3], cdm_200, cdm_22m[3];
+  double I_1m_tca1[3], I_2m_tca1[3], E_2m_tca1[3], B_2m_tca1[3], Pi_tca1[3];
+  double psi, phi_prime, phi_pp, omega_m1_prime, gamma_m2_pp;
+};
+
+/* Scalars of the NDF state, written by thread 0 only where noted. */
+struct Shared {
+  Tri tri;
+  BgV bg;
+  WS ws;
+  double psi_prime;
+  double red[32];
+  int item;
+  int lu_fail;
+  int tca;
+};
+
+/* Offsets (in bytes) of the dynamic shared-memory plan. */
+struct Plan {
+  size_t y, f, ynew, difkp1, psiv, del, invwt, yout, dyout, dif, fo1, fo2, qs, qc, rot1, rot2, sc, bgraw, shared,
+      xsol, piv, lu, total;
+};
+
+__host__ __device__ inline size_t al(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_smem) {
+  Plan p;
+  size_t o = 0, n = (size_t)s.n, d = sizeof(double);
+  p.y = o; o = al(o + n * d);
+  p.f = o; o = al(o + n * d);
+  p.ynew = o; o = al(o + n * d);
+  p.difkp1 = o; o = al(o + n * d);
+  p.psiv = o; o = al(o + n * d);
+  p.del = o; o = al(o + n * d);
+  p.invwt = o; o = al(o + n * d);
+  p.yout = o; o = al(o + n * d);
+  p.dyout = o; o = al(o + n * d);
+  p.dif = o; o = al(o + 7 * n * d);
+  p.fo1 = o; o = al(o + (size_t)s.nfo * d);
+  p.fo2 = o; o = al(o + (size_t)s.nfo * d);
+  p.qs = o; o = al(o + (size_t)s.qs2_size * d);
+  p.qc = o; o = al(o + (size_t)s.qs2_size * d);
+  p.rot1 = o; o = al(o + (size_t)s.n_lmq * d);
+  p.rot2 = o; o = al(o + (size_t)s.n_lmq * d);
+  p.sc = o; o = al(o + 20 * (size_t)s.n_lm * d);
+  p.bgraw = o; o = al(o + 16 * d);
+  p.shared = o; o = al(o + sizeof(Shared));
+  size_t ts = prec == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
+  p.xsol = o; o = al(o + n * ts);
+  p.piv = o; o = al(o + n * sizeof(int));
+  p.lu = o;
+  if (lu_in_smem) o = al(o + (size_t)s.lu_elems * ts);
+  p.total = o;
+  return p;
+}
+
+/* ------------------------------------------------------------------ context */
+
+struct K {
+  const DevSpec &s;
+  const DevPtrs &p;
+  double *y, *f, *ynew, *difkp1, *psiv, *del, *invwt, *yout, *dyout, *dif, *fo1, *fo2, *qs, *qc, *rot1, *rot2, *sc,
+      *bgraw;
+  Shared *sh;
+  void *xsol;
+  int *piv;
+  void *lu;
+  double *jac;
+  __device__ K(const DevSpec &s_, const DevPtrs &p_, char *smem, int prec) : s(s_), p(p_) {
+    Plan pl = make_plan(s_, prec, s_.lu_in_smem);
+    y = (double *)(smem + pl.y); f = (double *)(smem + pl.f); ynew = (double *)(smem + pl.ynew);
+    difkp1 = (double *)(smem + pl.difkp1); psiv = (double *)(smem + pl.psiv); del = (double *)(smem + pl.del);
+    invwt = (double *)(smem + pl.invwt); yout = (double *)(smem + pl.yout); dyout = (double *)(smem + pl.dyout);
+    dif = (double *)(smem + pl.dif); fo1 = (double *)(smem + pl.fo1); fo2 = (double *)(smem + pl.fo2);
+    qs = (double *)(smem + pl.qs); qc = (double *)(smem + pl.qc); rot1 = (double *)(smem + pl.rot1);
+    rot2 = (double *)(smem + pl.rot2); sc = (double *)(smem + pl.sc); bgraw = (double *)(smem + pl.bgraw);
+    sh = (Shared *)(smem + pl.shared);
+    xsol = smem + pl.xsol;
+    piv = (int *)(smem + pl.piv);
+    size_t ts = prec == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
+    if (s_.lu_in_smem) lu = smem + pl.lu;
+    else lu = (char *)p_.lu_global + (size_t)blockIdx.x * s_.lu_elems * ts;
+    jac = p_.jac + (size_t)blockIdx.x * s_.lu_elems;
+  }
+  __device__ int LM(int l, int m) const { return s.lm_array[l][s.index_m[m]]; }
+  __device__ int LMQ(int l, int m) const { return s.lmq[l][m]; }
+  /* summed couplings, index X in 0..19 */
+  __device__ double S(int X, int l, int m) const { return sc[X * s.n_lm + LM(l, m)]; }
+  __device__ double cmin(int l, int m1, int m) const { return __ldg(p.cmin + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double cplu(int l, int m1, int m) const { return __ldg(p.cplu + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double dmin(int l, int m1, int m) const { return __ldg(p.dmin + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double dplu(int l, int m1, int m) const { return __ldg(p.dplu + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double dzer(int l, int m1, int m) const { return __ldg(p.dzer + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double rot_1(int l, int m) const {
+    if (l < 0 || abs(m) > l) return 0.0;
+    double v = rot1[LMQ(l, abs(m))];
+    return (m < 0 && (m & 1)) ? -v : v;
+  }
+  __device__ double rot_2(int l, int m) const {
+    if (l < 0 || abs(m) > l) return 0.0;
+    double v = rot2[LMQ(l, abs(m))];
+    return (m < 0 && (m & 1)) ? -v : v;
+  }
+  __device__ double I1r(int l) const { return l < 0 ? 0.0 : fo1[SONG2_FO_I + l]; }
+  __device__ double I2r(int l) const { return l < 0 ? 0.0 : fo2[SONG2_FO_I + l]; }
+  __device__ double E1r(int l) const { return (l < 0 || !s.has_pol) ? 0.0 : fo1[s.fo_E + l]; }
+  __device__ double E2r(int l) const { return (l < 0 || !s.has_pol) ? 0.0 : fo2[s.fo_E + l]; }
+  __device__ double N1r(int l) const { return l < 0 ? 0.0 : fo1[s.fo_N + l]; }
+  __device__ double N2r(int l) const { return l < 0 ? 0.0 : fo2[s.fo_N + l]; }
+};
+
+enum { CM12 = 0, CM21, CP12, CP21, CM11, CM22, CP11, CP22, DM12, DM21, DP12, DP21, DM11, DM22, DP11, DP22, DZ12, DZ21,
+       DZ11, DZ22 };
+
+/* ------------------------------------------------------------------ state accessors */
+
+struct YVec {
+  const double *v;
+  __device__ double operator()(int i) const { return i < 0 ? 0.0 : v[i]; }
+};
+struct YUnit {
+  int j;
+  __device__ double operator()(int i) const { return (i >= 0 && i == j) ? 1.0 : 0.0; }
+};
+
+template <class Y> __device__ inline double getI(const K &c, int tca, const Y &y, int l, int m) {
+  if (l < 0 || m < 0 || m > l || l > c.s.l_max_g || (tca && l >= 1)) return 0.0;
+  return y(c.p.idx_I[c.LM(l, m)]);
+}
+template <class Y> __device__ inline double getE(const K &c, int tca, const Y &y, int l, int m) {
+  if (!c.s.has_pol || tca || l < 2 || m < 0 || m > l || l > c.s.l_max_pol) return 0.0;
+  return y(c.p.idx_E[c.LM(l, m)]);
+}
+template <class Y> __device__ inline double getB(const K &c, int tca, const Y &y, int l, int m) {
+  if (!c.s.has_pol || tca || l < 2 || m <= 0 || m > l || l > c.s.l_max_pol) return 0.0;
+  return y(c.p.idx_B[c.LM(l, m)]);
+}
+template <class Y> __device__ inline double getN(const K &c, const Y &y, int l, int m) {
+  if (l < 0 || m < 0 || m > l || l > c.s.l_max_ur) return 0.0;
+  return y(c.p.idx_N[c.LM(l, m)]);
+}
+template <class Y> __device__ inline double getb(const K &c, const Y &y, int n, int m) {
+  /* n = 0: b000 ; n = 1: b11m */
+  if (n == 0) return y(c.s.idx_b000);
+  return (m <= 1) ? y(c.s.idx_b11[m]) : 0.0;
+}
+template <class Y> __device__ inline double getc(const K &c, const Y &y, int n, int m) {
+  if (n == 0) return y(c.s.idx_c000);
+  return (m <= 1) ? y(c.s.idx_c11[m]) : 0.0;
+}
+
+/* ------------------------------------------------------------------ interpolation */
+
+__device__ inline double spl(const double *yv, const double *dd, int n, int ncol, double x0, double dx, int q,
+                             double x) {
+  double u = (x - x0) / dx;
+  int i = (int)floor(u);
+  i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+  double b = u - i, a = 1.0 - b;
+  const double *y0 = yv + (size_t)i * ncol, *d0 = dd + (size_t)i * ncol;
+  return a * __ldg(y0 + q) + b * __ldg(y0 + ncol + q) +
+         ((a * a * a - a) * __ldg(d0 + q) + (b * b * b - b) * __ldg(d0 + ncol + q)) * (dx * dx) / 6.0;
+}
+
+__device__ inline double bg_col(const K &c, int q, double tau) {
+  return spl(c.p.bg, c.p.bg_dd, c.s.bg_size, SONG2_BG_SIZE, c.s.bg_lntau0, c.s.bg_dlntau, q, log(tau));
+}
+
+__device__ inline void bg_derive(const double *raw, double tau, BgV &b) {
+  b.a = exp(raw[SONG2_BG_LN_A]);
+  b.a_sq = b.a * b.a;
+  b.Hc = exp(raw[SONG2_BG_LN_HC]);
+  b.Hc_prime = raw[SONG2_BG_HC_PRIME_TAU2] / (tau * tau);
+  b.rho_g = exp(raw[SONG2_BG_LN_RHO_G]);
+  b.rho_b = exp(raw[SONG2_BG_LN_RHO_B]);
+  b.rho_cdm = exp(raw[SONG2_BG_LN_RHO_CDM]);
+  b.rho_ur = exp(raw[SONG2_BG_LN_RHO_UR]);
+  b.kappa_dot = exp(raw[SONG2_BG_LN_KAPPA_DOT]);
+  b.exp_m_kappa = exp(-raw[SONG2_BG_KAPPA]);
+  b.g = b.kappa_dot * b.exp_m_kappa;
+  b.r = b.rho_g / b.rho_b;
+}
+
+/* Hc and kappa_dot only (start time, TCA trigger) */
+__device__ inline void bg_hk(const K &c, double tau, double &Hc, double &kd) {
+  Hc = exp(bg_col(c, SONG2_BG_LN_HC, tau));
+  kd = exp(bg_col(c, SONG2_BG_LN_KAPPA_DOT, tau));
+}
+
+/* ------------------------------------------------------------------ quadratic sources */
+
+__device__ double coll_I(const K &c, const BgV &bg, int l, int m) {
+  const Tri &t = c.sh->tri;
+  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  double vb1 = fo1[SONG2_FO_V_B], vb2 = fo2[SONG2_FO_V_B], db1 = fo1[SONG2_FO_DELTA_B], db2 = fo2[SONG2_FO_DELTA_B];
+  if (l == 0) {
+    double vg1 = fo1[SONG2_FO_V_G], vg2 = fo2[SONG2_FO_V_G];
+    return FOUR_THIRDS * t.k1_dot_k2 * (vb1 * (vg2 - vb2) + vb2 * (vg1 - vb1));
+  }
+  double v01 = -t.k1 * vb1, v02 = -t.k2 * vb2;
+  double A1 = fo1[SONG2_FO_PSI], A2 = fo2[SONG2_FO_PSI];
+  double c1, c2, spec = 0;
+  if (l == 1) {
+    double ub1 = -t.k1_m[m + 1] * vb1, ub2 = -t.k2_m[m + 1] * vb2;
+    c1 = 4 * ub1 - c.rot_1(1, m) * c.I1r(1);
+    c2 = 4 * ub2 - c.rot_2(1, m) * c.I2r(1);
+    spec = 3 * (c.S(CM12, 1, m) * v01 * c.I2r(0) + c.S(CM21, 1, m) * v02 * c.I1r(0)) - 4 * (db1 * ub2 + db2 * ub1);
+  } else if (l == 2) {
+    double I1 = c.rot_1(2, m) * c.I1r(2), I2 = c.rot_2(2, m) * c.I2r(2);
+    double E1 = c.rot_1(2, m) * c.E1r(2), E2 = c.rot_2(2, m) * c.E2r(2);
+    c1 = -I1 + 0.1 * (I1 - SQRT_6 * E1);
+    c2 = -I2 + 0.1 * (I2 - SQRT_6 * E2);
+    spec = c.S(CM12, 2, m) * v01 * (7 * v02 - 0.5 * c.I2r(1)) + c.S(CM21, 2, m) * v02 * (7 * v01 - 0.5 * c.I1r(1));
+  } else if (l == 3) {
+    c1 = -c.rot_1(3, m) * c.I1r(3);
+    c2 = -c.rot_2(3, m) * c.I2r(3);
+    spec = 0.5 * (c.S(CM12, 3, m) * v01 * (c.I2r(2) - SQRT_6 * c.E2r(2)) +
+                  c.S(CM21, 3, m) * v02 * (c.I1r(2) - SQRT_6 * c.E1r(2)));
+  } else {
+    c1 = -c.rot_1(l, m) * c.I1r(l);
+    c2 = -c.rot_2(l, m) * c.I2r(l);
+  }
+  double loss = (A1 + db1) * c2 + (A2 + db2) * c1 + c.S(CM12, l, m) * v01 * c.I2r(l - 1) -
+                c.S(CP12, l, m) * v01 * c.I2r(l + 1) + c.S(CM21, l, m) * v02 * c.I1r(l - 1) -
+                c.S(CP21, l, m) * v02 * c.I1r(l + 1);
+  return spec + loss;
+}
+
+__device__ double coll_E(const K &c, int l, int m) {
+  const Tri &t = c.sh->tri;
+  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  double vb1 = fo1[SONG2_FO_V_B], vb2 = fo2[SONG2_FO_V_B], db1 = fo1[SONG2_FO_DELTA_B], db2 = fo2[SONG2_FO_DELTA_B];
+  double v01 = -t.k1 * vb1, v02 = -t.k2 * vb2;
+  double A1 = fo1[SONG2_FO_PSI], A2 = fo2[SONG2_FO_PSI];
+  double c1, c2, spec = 0;
+  if (l == 2) {
+    double I1 = c.rot_1(2, m) * c.I1r(2), I2 = c.rot_2(2, m) * c.I2r(2);
+    double E1 = c.rot_1(2, m) * c.E1r(2), E2 = c.rot_2(2, m) * c.E2r(2);
+    c1 = -E1 - SQRT_6 * 0.1 * (I1 - SQRT_6 * E1);
+    c2 = -E2 - SQRT_6 * 0.1 * (I2 - SQRT_6 * E2);
+    spec = 0.5 * SQRT_6 *
+           (c.S(CM12, 2, m) * v01 * (c.I2r(1) - 2 * v02) + c.S(CM21, 2, m) * v02 * (c.I1r(1) - 2 * v01));
+  } else if (l == 3) {
+    c1 = -c.rot_1(3, m) * c.E1r(3);
+    c2 = -c.rot_2(3, m) * c.E2r(3);
+    spec = -0.5 * SQRT_6 *
+           (c.S(DM12, 3, m) * v01 * (c.I2r(2) - SQRT_6 * c.E2r(2)) + c.S(DM21, 3, m) * v02 * (c.I1r(2) - SQRT_6 * c.E1r(2)));
+  } else {
+    c1 = -c.rot_1(l, m) * c.E1r(l);
+    c2 = -c.rot_2(l, m) * c.E2r(l);
+  }
+  double loss = (A1 + db1) * c2 + (A2 + db2) * c1 + c.S(DM12, l, m) * v01 * c.E2r(l - 1) -
+                c.S(DP12, l, m) * v01 * c.E2r(l + 1) + c.S(DM21, l, m) * v02 * c.E1r(l - 1) -
+                c.S(DP21, l, m) * v02 * c.E1r(l + 1);
+  return spec + loss;
+}
+
+__device__ double coll_B(const K &c, int l, int m) {
+  const Tri &t = c.sh->tri;
+  double v01 = -t.k1 * c.fo1[SONG2_FO_V_B], v02 = -t.k2 * c.fo2[SONG2_FO_V_B];
+  double v = 0;
+  if (l == 2)
+    v = -0.2 * SQRT_6 *
+        (c.S(DZ12, 2, m) * v01 * (c.I2r(2) - SQRT_6 * c.E2r(2)) + c.S(DZ21, 2, m) * v02 * (c.I1r(2) - SQRT_6 * c.E1r(2)));
+  return v + c.S(DZ12, l, m) * v01 * c.E2r(l) + c.S(DZ21, l, m) * v02 * c.E1r(l);
+}
+
+/* Liouville part of the photon / neutrino intensity hierarchy (before the sign flip) */
+__device__ double liou_IN(const K &c, int nu, int l, int m) {
+  const Tri &t = c.sh->tri;
+  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  double phi1 = fo1[SONG2_FO_PHI], phi2 = fo2[SONG2_FO_PHI], psi1 = fo1[SONG2_FO_PSI], psi2 = fo2[SONG2_FO_PSI];
+  double php1 = fo1[SONG2_FO_PHI_P], php2 = fo2[SONG2_FO_PHI_P];
+  double k1 = t.k1, k2 = t.k2;
+  double v = 0;
+  if (l == 0) v = -8 * (phi1 * php2 + phi2 * php1);
+  if (l == 1) v = 4 * (t.k1_m[m + 1] * psi1 * (psi2 - phi2) + t.k2_m[m + 1] * psi2 * (psi1 - phi1));
+  double R1p = c.I1r(l + 1), R1m = c.I1r(l - 1), R2p = c.I2r(l + 1), R2m = c.I2r(l - 1), X1 = c.I1r(l), X2 = c.I2r(l);
+  if (nu) { R1p = c.N1r(l + 1); R1m = c.N1r(l - 1); R2p = c.N2r(l + 1); R2m = c.N2r(l - 1); X1 = c.N1r(l); X2 = c.N2r(l); }
+  double cm12 = c.S(CM12, l, m), cm21 = c.S(CM21, l, m), cp12 = c.S(CP12, l, m), cp21 = c.S(CP21, l, m);
+  double cm11 = c.S(CM11, l, m), cm22 = c.S(CM22, l, m), cp11 = c.S(CP11, l, m), cp22 = c.S(CP22, l, m);
+  double rm12 = (l - 1) * cm12, rm21 = (l - 1) * cm21, rp12 = -(l + 2) * cp12, rp21 = -(l + 2) * cp21;
+  /* the same terms as the reference, grouped as in its neutrino block (perturbations2.c:11261-11277) */
+  v += -4 * php1 * c.rot_2(l, m) * X2 +
+       R2p * (rp12 * k1 * (phi1 + psi1) + cp22 * k2 * (phi1 + psi1) + 4 * cp12 * k1 * psi1) -
+       R2m * (rm12 * k1 * (phi1 + psi1) + cm22 * k2 * (phi1 + psi1) + 4 * cm12 * k1 * psi1) -
+       4 * php2 * c.rot_1(l, m) * X1 +
+       R1p * (rp21 * k2 * (phi2 + psi2) + cp11 * k1 * (phi2 + psi2) + 4 * cp21 * k2 * psi2) -
+       R1m * (rm21 * k2 * (phi2 + psi2) + cm11 * k1 * (phi2 + psi2) + 4 * cm21 * k2 * psi2);
+  return v;
+}
+
+__device__ void liou_EB(const K &c, int l, int m, double &e, double &bb) {
+  const Tri &t = c.sh->tri;
+  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  double phi1 = fo1[SONG2_FO_PHI], phi2 = fo2[SONG2_FO_PHI], psi1 = fo1[SONG2_FO_PSI], psi2 = fo2[SONG2_FO_PSI];
+  double php1 = fo1[SONG2_FO_PHI_P], php2 = fo2[SONG2_FO_PHI_P];
+  double k1 = t.k1, k2 = t.k2;
+  double dm12 = c.S(DM12, l, m), dm21 = c.S(DM21, l, m), dp12 = c.S(DP12, l, m), dp21 = c.S(DP21, l, m);
+  double dm11 = c.S(DM11, l, m), dm22 = c.S(DM22, l, m), dp11 = c.S(DP11, l, m), dp22 = c.S(DP22, l, m);
+  double dz12 = c.S(DZ12, l, m), dz21 = c.S(DZ21, l, m), dz11 = c.S(DZ11, l, m), dz22 = c.S(DZ22, l, m);
+  double km12 = (l - 1) * dm12, km21 = (l - 1) * dm21, kp12 = -(l + 2) * dp12, kp21 = -(l + 2) * dp21;
+  double kz12 = -dz12, kz21 = -dz21;
+  e = -4 * php1 * c.rot_2(l, m) * c.E2r(l) +
+      c.E2r(l + 1) * (kp12 * k1 * (phi1 + psi1) + dp22 * k2 * (phi1 + psi1) + 4 * dp12 * k1 * psi1) -
+      c.E2r(l - 1) * (km12 * k1 * (phi1 + psi1) + dm22 * k2 * (phi1 + psi1) + 4 * dm12 * k1 * psi1) -
+      4 * php2 * c.rot_1(l, m) * c.E1r(l) +
+      c.E1r(l + 1) * (kp21 * k2 * (phi2 + psi2) + dp11 * k1 * (phi2 + psi2) + 4 * dp21 * k2 * psi2) -
+      c.E1r(l - 1) * (km21 * k2 * (phi2 + psi2) + dm11 * k1 * (phi2 + psi2) + 4 * dm21 * k2 * psi2);
+  bb = -c.E2r(l) * (kz12 * k1 * (phi1 + psi1) + dz22 * k2 * (phi1 + psi1) + 4 * dz12 * k1 * psi1) -
+       c.E1r(l) * (kz21 * k2 * (phi2 + psi2) + dz11 * k1 * (phi2 + psi2) + 4 * dz21 * k2 * psi2);
+}
+
+__device__ double liou_matter(const K &c, int cdm, int n, int m) {
+  const Tri &t = c.sh->tri;
+  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  double phi1 = fo1[SONG2_FO_PHI], phi2 = fo2[SONG2_FO_PHI], psi1 = fo1[SONG2_FO_PSI], psi2 = fo2[SONG2_FO_PSI];
+  double php1 = fo1[SONG2_FO_PHI_P], php2 = fo2[SONG2_FO_PHI_P];
+  double d1 = fo1[cdm ? SONG2_FO_DELTA_CDM : SONG2_FO_DELTA_B], d2 = fo2[cdm ? SONG2_FO_DELTA_CDM : SONG2_FO_DELTA_B];
+  double v1 = fo1[cdm ? SONG2_FO_V_CDM : SONG2_FO_V_B], v2 = fo2[cdm ? SONG2_FO_V_CDM : SONG2_FO_V_B];
+  double k1k2 = t.k1_dot_k2, k1sq = t.k1 * t.k1, k2sq = t.k2 * t.k2;
+  if (n == 0)
+    return 2 * k1k2 * (psi1 - phi1) * v2 + k2sq * (phi1 + psi1) * v2 + 3 * php1 * (d2 + 2 * phi2) +
+           2 * k1k2 * (psi2 - phi2) * v1 + k1sq * (phi2 + psi2) * v1 + 3 * php2 * (d1 + 2 * phi1);
+  return 3 * t.k1_m[m + 1] * (d2 * psi1 - 4 * v1 * php2 + phi2 * psi1) +
+         3 * t.k2_m[m + 1] * (d1 * psi2 - 4 * v2 * php1 + phi1 * psi2) - 3 * psi1 * psi2 * (t.k1_m[m + 1] + t.k2_m[m + 1]);
+}
+
+/* Einstein-tensor quadratic terms (perturbations2.c:10905-11060) into qs */
+__device__ void qs_metric(const K &c, const BgV &bg) {
+  const Tri &t = c.sh->tri;
+  const DevSpec &s = c.s;
+  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  double *qs = c.qs;
+  double phi_1 = fo1[SONG2_FO_PHI], phi_2 = fo2[SONG2_FO_PHI], psi_1 = fo1[SONG2_FO_PSI], psi_2 = fo2[SONG2_FO_PSI];
+  double psi_prime_1 = fo1[SONG2_FO_PSI_P], psi_prime_2 = fo2[SONG2_FO_PSI_P];
+  double phi_prime_1 = fo1[SONG2_FO_PHI_P], phi_prime_2 = fo2[SONG2_FO_PHI_P];
+  double phi_prime_prime_1 = fo1[SONG2_FO_PHI_PP], phi_prime_prime_2 = fo2[SONG2_FO_PHI_PP];
+  double k1 = t.k1, k2 = t.k2, k = t.k, k_sq = t.k_sq, k1_sq = k1 * k1, k2_sq = k2 * k2, k1_dot_k2 = t.k1_dot_k2;
+  const double *k1_m = t.k1_m, *k2_m = t.k2_m, *k1_ten_k2 = t.k1_ten_k2, *k1_ten_k1 = t.k1_ten_k1,
+               *k2_ten_k2 = t.k2_ten_k2;
+  double Hc = bg.Hc, Hc_sq = Hc * Hc, Hc_prime = bg.Hc_prime, a_sq = bg.a_sq;
+  if (s.compute_m[0]) {
+    double rho_dipole_1 = bg.rho_g * c.I1r(1) + bg.rho_b * fo1[SONG2_FO_DIPOLE_B] + bg.rho_cdm * fo1[SONG2_FO_DIPOLE_CDM] +
+                          bg.rho_ur * c.N1r(1);
+    double rho_dipole_2 = bg.rho_g * c.I2r(1) + bg.rho_b * fo2[SONG2_FO_DIPOLE_B] + bg.rho_cdm * fo2[SONG2_FO_DIPOLE_CDM] +
+                          bg.rho_ur * c.N2r(1);
+    double Q_TT = -12 * psi_1 * psi_2 * Hc_sq + phi_1 * phi_2 * (3 * k1_dot_k2 + 4 * k1_sq + 4 * k2_sq) +
+                  6 * phi_prime_2 * (phi_1 - psi_1) * Hc + 6 * phi_prime_1 * (phi_2 - psi_2) * Hc -
+                  3 * phi_prime_1 * phi_prime_2;
+    double Q_ST = +2 * psi_1 * psi_2 * Hc * (k1_m[1] + k2_m[1]) - 2 * psi_1 * phi_2 * Hc * (k1_m[1]) -
+                  2 * psi_2 * phi_1 * Hc * (+k2_m[1]) - 2 * phi_1 * phi_prime_2 * (k1_m[1] + 2 * k2_m[1]) -
+                  2 * phi_2 * phi_prime_1 * (2 * k1_m[1] + k2_m[1]) + psi_1 * phi_prime_2 * (k1_m[1]) +
+                  psi_2 * phi_prime_1 * (k2_m[1]) +
+                  0.5 * a_sq * (k1_m[1] / k1 * rho_dipole_1 * (psi_2 + phi_2) + k2_m[1] / k2 * rho_dipole_2 * (psi_1 + phi_1));
+    double Q_TR = -12 * psi_1 * psi_2 * (Hc * Hc + 2 * Hc_prime) + psi_1 * psi_2 * (k_sq + k1_sq + k2_sq) +
+                  phi_1 * phi_2 * (3 * k1_dot_k2 + 4 * k1_sq + 4 * k2_sq) + phi_1 * psi_2 * (k1_dot_k2 - 2 * k2_sq) +
+                  phi_2 * psi_1 * (k1_dot_k2 - 2 * k1_sq) + 6 * (phi_prime_prime_2 + 2 * Hc * phi_prime_2) * (phi_1 - psi_1) +
+                  6 * (phi_prime_prime_1 + 2 * Hc * phi_prime_1) * (phi_2 - psi_2) -
+                  3 * psi_prime_2 * (4 * Hc * psi_1 + phi_prime_1) - 3 * psi_prime_1 * (4 * Hc * psi_2 + phi_prime_2) +
+                  3 * phi_prime_1 * phi_prime_2;
+    double Q_SS = phi_1 * phi_2 * (-3 * k1_ten_k2[2] - 2 * k1_ten_k1[2] - 2 * k2_ten_k2[2]) +
+                  psi_1 * psi_2 * (-k1_ten_k2[2] - k1_ten_k1[2] - k2_ten_k2[2]) +
+                  psi_1 * phi_2 * (k1_ten_k2[2] + k1_ten_k1[2]) + psi_2 * phi_1 * (k1_ten_k2[2] + k2_ten_k2[2]);
+    double Q_SS_prime =
+        (phi_prime_1 * phi_2 + phi_1 * phi_prime_2) * (-3 * k1_ten_k2[2] - 2 * k1_ten_k1[2] - 2 * k2_ten_k2[2]) +
+        (psi_prime_1 * psi_2 + psi_1 * psi_prime_2) * (-k1_ten_k2[2] - k1_ten_k1[2] - k2_ten_k2[2]) +
+        (psi_prime_1 * phi_2 + psi_1 * phi_prime_2) * (k1_ten_k2[2] + k1_ten_k1[2]) +
+        (psi_prime_2 * phi_1 + psi_2 * phi_prime_1) * (k1_ten_k2[2] + k2_ten_k2[2]);
+    Q_TT *= 2; Q_ST *= 2; Q_TR *= 2; Q_SS *= 2; Q_SS_prime *= 2;
+    qs[s.iq_phi_prime_poisson] = -Q_TT / (6 * Hc);
+    qs[s.iq_phi_prime_longitudinal] = Q_ST / (2 * k);
+    qs[s.iq_psi] = -Q_SS * 3 / (2 * k_sq);
+    qs[s.iq_psi_prime] = -Q_SS_prime * 3 / (2 * k_sq) - Q_SS * 3 * Hc / k_sq;
+    qs[s.iq_phi_prime_prime] = -(Q_TR + Q_TT) / 6;
+  }
+  if (s.compute_m[1]) {
+    double Q_SS = phi_1 * phi_2 * (-3 * k1_ten_k2[3] - 2 * k1_ten_k1[3] - 2 * k2_ten_k2[3]) +
+                  psi_1 * psi_2 * (-k1_ten_k2[3] - k1_ten_k1[3] - k2_ten_k2[3]) +
+                  psi_1 * phi_2 * (k1_ten_k2[3] + k1_ten_k1[3]) + psi_2 * phi_1 * (k1_ten_k2[3] + k2_ten_k2[3]);
+    qs[s.iq_omega_m1_prime] = SQRT_3 / k * 2 * Q_SS;
+  }
+  if (s.compute_m[2]) {
+    double Q_SS = phi_1 * phi_2 * (-3 * k1_ten_k2[4] - 2 * k1_ten_k1[4] - 2 * k2_ten_k2[4]) +
+                  psi_1 * psi_2 * (-k1_ten_k2[4] - k1_ten_k1[4] - k2_ten_k2[4]) +
+                  psi_1 * phi_2 * (k1_ten_k2[4] + k1_ten_k1[4]) + psi_2 * phi_1 * (k1_ten_k2[4] + k2_ten_k2[4]);
+    qs[s.iq_gamma_m2_prime_prime] = -2 * Q_SS;
+  }
+  qs[s.iq_vv_g] = fo1[SONG2_FO_V_G] * fo2[SONG2_FO_V_G];
+  qs[s.iq_vv_ur] = fo1[SONG2_FO_V_UR] * fo2[SONG2_FO_V_UR];
+  qs[s.iq_dd_b] = fo1[SONG2_FO_DELTA_B] * fo2[SONG2_FO_DELTA_B];
+  qs[s.iq_vv_b] = fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B];
+  qs[s.iq_vv_cdm] = fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM];
+}
+
+/* One entry of the quadratic-source vector: total (qs) and collisional (qc) part. */
+__device__ void qs_entry(const K &c, const BgV &bg, int q) {
+  const DevSpec &s = c.s;
+  int sp = __ldg(c.p.qs_sp + q), l = __ldg(c.p.qs_l + q), m = __ldg(c.p.qs_m + q);
+  double lv = 0, cv = 0;
+  switch (sp) {
+  case SP_I:
+    if (s.has_liou) lv = -liou_IN(c, 0, l, m);
+    if (s.has_coll) cv = coll_I(c, bg, l, m) * bg.kappa_dot;
+    break;
+  case SP_E:
+    if (l >= 2) {
+      double e, bb;
+      if (s.has_liou) { liou_EB(c, l, m, e, bb); lv = -e; }
+      if (s.has_coll) cv = coll_E(c, l, m) * bg.kappa_dot;
+    }
+    break;
+  case SP_B:
+    if (l >= 2) {
+      double e, bb;
+      if (s.has_liou) { liou_EB(c, l, m, e, bb); lv = -bb; }
+      if (s.has_coll) cv = coll_B(c, l, m) * bg.kappa_dot;
+    }
+    break;
+  case SP_N:
+    if (s.has_liou) lv = -liou_IN(c, 1, l, m);
+    break;
+  case SP_B000:
+    if (s.has_liou) lv = liou_matter(c, 0, 0, 0);
+    if (s.has_coll) cv = -bg.r * coll_I(c, bg, 0, 0) * bg.kappa_dot;
+    break;
+  case SP_B11:
+    if (s.has_liou) lv = liou_matter(c, 0, 1, m);
+    if (s.has_coll) cv = -bg.r * coll_I(c, bg, 1, m) * bg.kappa_dot;
+    break;
+  case SP_C000:
+    if (s.has_liou) lv = liou_matter(c, 1, 0, 0);
+    break;
+  case SP_C11:
+    if (s.has_liou) lv = liou_matter(c, 1, 1, m);
+    break;
+  case SP_METRIC:
+    if (q == s.iq_psi) qs_metric(c, bg);
+    return;
+  default:
+    return;
+  }
+  c.qs[q] = lv + cv;
+  c.qc[q] = cv;
+}
+
+/* ------------------------------------------------------------------ prepare(tau) */
+
+/* Background, first-order quantities and quadratic sources at tau, block-wide.
+   Leaves sh->bg and the qs/qc/fo arrays ready; ends with a barrier. */
+__device__ void prepare(const K &c, double tau, int with_sources) {
+  const DevSpec &s = c.s;
+  const Tri &t = c.sh->tri;
+  int tid = threadIdx.x, nt = blockDim.x;
+  double x = log(tau);
+  if (tid < SONG2_BG_SIZE) c.bgraw[tid] = bg_col(c, tid, tau);
+  int use_fo = with_sources && s.has_qs && !s.mode_first_order;
+  for (int q = tid; q < 2 * s.nfo; q += nt) {
+    int which = q >= s.nfo, qq = which ? q - s.nfo : q;
+    double v = 0.0;
+    if (use_fo) {
+      int ik = which ? t.i2 : t.i1;
+      size_t stride = (size_t)s.fo_tau_size * s.nfo;
+      v = spl(c.p.fo + stride * ik, c.p.fo_dd + stride * ik, s.fo_tau_size, s.nfo, s.fo_lntau0, s.fo_dlntau, qq, x);
+    }
+    (which ? c.fo2 : c.fo1)[qq] = v;
+  }
+  __syncthreads();
+  BgV bg;
+  bg_derive(c.bgraw, tau, bg);
+  if (tid == 0) c.sh->bg = bg;
+  for (int q = tid; q < s.qs2_size; q += nt) {
+    c.qs[q] = 0.0;
+    c.qc[q] = 0.0;
+  }
+  __syncthreads();
+  if (use_fo)
+    for (int q = tid; q < s.qs2_size; q += nt) qs_entry(c, bg, q);
+  __syncthreads();
+}
+
+/* ------------------------------------------------------------------ workspace */
+
+template <class Y> __device__ void compute_ws(const K &c, int tca, const Y &y, int lin, WS &w) {
+  const DevSpec &s = c.s;
+  const Tri &t = c.sh->tri;
+  const BgV &bg = c.sh->bg;
+  const double *qs = c.qs, *qc = c.qc, *fo1 = c.fo1, *fo2 = c.fo2;
+  double k = t.k, Hc = bg.Hc, kd = bg.kappa_dot, r = bg.r;
+  for (int mm = 0; mm < 3; ++mm) {
+    w.N_1m[mm] = w.I_1m[mm] = w.I_2m[mm] = w.E_2m[mm] = w.B_2m[mm] = w.C_1m[mm] = 0;
+    w.b_22m[mm] = w.cdm_22m[mm] = 0;
+    w.I_1m_tca1[mm] = w.I_2m_tca1[mm] = w.E_2m_tca1[mm] = w.B_2m_tca1[mm] = w.Pi_tca1[mm] = 0;
+  }
+  w.I_00 = w.N_00 = 0;
+  if (s.compute_m[0]) {
+    w.I_00 = getI(c, tca, y, 0, 0);
+    w.N_00 = getN(c, y, 0, 0);
+  }
+  for (int im = 0; im <= s.index_m_max[1]; ++im) {
+    int m = s.m[im];
+    w.I_1m[m] = getI(c, tca, y, 1, m);
+    w.N_1m[m] = getN(c, y, 1, m);
+    w.C_1m[m] = kd * (FOUR_THIRDS * getb(c, y, 1, m) - getI(c, tca, y, 1, m));
+  }
+  for (int im = 0; im <= s.index_m_max[2]; ++im) {
+    int m = s.m[im];
+    w.I_2m[m] = getI(c, tca, y, 2, m);
+    w.E_2m[m] = getE(c, tca, y, 2, m);
+    w.B_2m[m] = getB(c, tca, y, 2, m);
+  }
+  double vv_b = lin ? 0.0 : qs[s.iq_vv_b], vv_cdm = lin ? 0.0 : qs[s.iq_vv_cdm];
+  w.b_200 = -2 * t.k1_dot_k2 * vv_b;
+  w.cdm_200 = -2 * t.k1_dot_k2 * vv_cdm;
+  for (int im = 0; im <= s.index_m_max[2]; ++im) {
+    int m = s.m[im];
+    w.b_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_b;
+    w.cdm_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_cdm;
+  }
+  if (tca) {
+    /* perturb2_tca_variables (perturbations2.c:9374-9738) */
+    double tau_c = 1.0 / kd;
+    double f1[SONG2_FO_I], f2[SONG2_FO_I];
+    for (int q = 0; q < SONG2_FO_I; ++q) { f1[q] = lin ? 0.0 : fo1[q]; f2[q] = lin ? 0.0 : fo2[q]; }
+    double vpot_g_1 = f1[SONG2_FO_V_G], vpot_g_2 = f2[SONG2_FO_V_G];
+    double delta_g_1 = f1[SONG2_FO_DELTA_G], delta_g_2 = f2[SONG2_FO_DELTA_G];
+    double v_dot_v_g = -t.k1_dot_k2 * vpot_g_1 * vpot_g_2;
+    double delta_g = w.I_00 - 8 / 3. * v_dot_v_g;
+    double vpot_b_1 = f1[SONG2_FO_V_B], vpot_b_2 = f2[SONG2_FO_V_B];
+    double vpot_b_1_prime = f1[SONG2_FO_V_B_P], vpot_b_2_prime = f2[SONG2_FO_V_B_P];
+    double delta_b_1 = f1[SONG2_FO_DELTA_B], delta_b_2 = f2[SONG2_FO_DELTA_B];
+    double delta_b_1_prime = f1[SONG2_FO_DELTA_B_P], delta_b_2_prime = f2[SONG2_FO_DELTA_B_P];
+    double c1tca[3] = {0.0, 0.0, 0.0};
+    for (int im = 0; im <= s.index_m_max[1]; ++im) {
+      int m = s.m[im];
+      double u_g_1 = -t.k1_m[m + 1] * vpot_g_1, u_g_2 = -t.k2_m[m + 1] * vpot_g_2;
+      double u_b_1 = -t.k1_m[m + 1] * vpot_b_1, u_b_2 = -t.k2_m[m + 1] * vpot_b_2;
+      double u_b_1_prime = -t.k1_m[m + 1] * vpot_b_1_prime, u_b_2_prime = -t.k2_m[m + 1] * vpot_b_2_prime;
+      double u_b = getb(c, y, 1, m) / 3 - delta_b_1 * u_b_2 - delta_b_2 * u_b_1;
+      double qcI1 = lin ? 0.0 : qc[s.iq_g + c.LM(1, m)];
+      double qsI1 = lin ? 0.0 : qs[s.iq_g + c.LM(1, m)];
+      double qsb = lin ? 0.0 : qs[s.iq_b11[m]], qcb = lin ? 0.0 : qc[s.iq_b11[m]];
+      double quadC_u_g_m = qcI1 / kd / 4 + (u_b_1 * delta_b_2 + u_b_2 * delta_b_1) - (u_g_1 * delta_g_2 + u_g_2 * delta_g_1);
+      double delta_u_prime_b_m = delta_b_1_prime * u_b_2 + delta_b_2_prime * u_b_1 + delta_b_1 * u_b_2_prime +
+                                 delta_b_2 * u_b_1_prime;
+      double quadL_b_11M = -(qsb - qcb), quadL_I_1M = -(qsI1 - qcI1);
+      double quadL_diff = quadL_b_11M / 3 - quadL_I_1M / 4 - FOUR_THIRDS * delta_u_prime_b_m / 4 +
+                          Hc * (u_b_1 * delta_b_2 + u_b_2 * delta_b_1);
+      double R = 3 / (4 * r);
+      double om = (m == 1) ? y(s.idx_omega) : 0.0;
+      double core = Hc * (u_b + om) + k / 4 * (m == 0 ? delta_g : 0) + quadL_diff;
+      double U_slip = -quadC_u_g_m - R / (1 + R) * tau_c * core;
+      c1tca[m] = -qcI1 - 4 * R / (1 + R) * core;
+      double u_g_tca1 = u_b - U_slip;
+      w.I_1m_tca1[m] = 4 * (u_g_tca1 + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
+    }
+    for (int im = 0; im <= s.index_m_max[2]; ++im) {
+      int m = s.m[im];
+      double v_ten_v_g = -t.k1_ten_k2[m + 2] * vpot_g_1 * vpot_g_2;
+      double v_ten_v_b_prime = -t.k1_ten_k2[m + 2] * (vpot_b_1 * vpot_b_2_prime + vpot_b_2 * vpot_b_1_prime);
+      double gp = (m == 2) ? y(s.idx_gammap) : 0.0;
+      double cm2 = c.cmin(2, m, m);
+      double shear = 8 / 45. * tau_c * (-k * w.I_1m_tca1[m] * cm2 - 4 * gp);
+      double quadC_I_2M = (lin ? 0.0 : qc[s.iq_g + c.LM(2, m)]) / kd;
+      double quadC_E_2M = 0, quadC_B_2M = 0, quadL_E_2M = 0;
+      double quadL_I_2M = lin ? 0.0 : -(qs[s.iq_g + c.LM(2, m)] - qc[s.iq_g + c.LM(2, m)]);
+      if (s.has_pol && !lin) {
+        quadC_E_2M = qc[s.iq_E + c.LM(2, m)] / kd;
+        quadC_B_2M = (m != 0 ? qc[s.iq_B + c.LM(2, m)] : 0.0) / kd;
+        quadL_E_2M = -(qs[s.iq_E + c.LM(2, m)] - qc[s.iq_E + c.LM(2, m)]);
+      }
+      shear += 8 / 45. * (-quadC_I_2M + SQRT_6 / 4 * quadC_E_2M - 15 * v_ten_v_g);
+      shear += 8 / 45. * tau_c * (quadL_I_2M - SQRT_6 / 4 * quadL_E_2M - 20 * v_ten_v_b_prime);
+      if (!s.has_pol)
+        shear = -4 / 27. * (quadC_I_2M + 18 * v_ten_v_g -
+                            tau_c * (-20 * v_ten_v_b_prime - k * w.I_1m[m] * cm2 - 4 * gp + quadL_I_2M));
+      w.I_2m_tca1[m] = -15 / 2. * shear - 20 * v_ten_v_g;
+      if (s.has_pol) {
+        w.Pi_tca1[m] = (w.I_2m_tca1[m] - SQRT_6 * (quadC_E_2M - tau_c * quadL_E_2M)) / 4;
+        w.E_2m_tca1[m] = -SQRT_6 * w.Pi_tca1[m] + quadC_E_2M - tau_c * quadL_E_2M;
+        w.B_2m_tca1[m] = (m != 0 ? quadC_B_2M : 0.0);
+      } else {
+        w.Pi_tca1[m] = 0.1 * w.I_2m_tca1[m];
+      }
+    }
+    /* the TCA values replace the evolved ones only now (perturbations2.c:8999-9020) */
+    for (int im = 0; im <= s.index_m_max[1]; ++im) {
+      w.I_1m[s.m[im]] = w.I_1m_tca1[s.m[im]];
+      w.C_1m[s.m[im]] = c1tca[s.m[im]];
+    }
+    for (int im = 0; im <= s.index_m_max[2]; ++im) {
+      int m = s.m[im];
+      w.I_2m[m] = w.I_2m_tca1[m];
+      if (s.has_pol) {
+        w.E_2m[m] = w.E_2m_tca1[m];
+        w.B_2m[m] = (m != 0 ? w.B_2m_tca1[m] : 0.0);
+      }
+    }
+  }
+  /* perturb2_einstein (perturbations2.c:8484-8814), Newtonian gauge, phi_eq = huang */
+  double a_sq = bg.a_sq, k_sq = t.k_sq;
+  if (s.compute_m[0]) {
+    double rho_quadrupole = bg.rho_g * w.I_2m[0] + bg.rho_b * w.b_22m[0] + bg.rho_cdm * w.cdm_22m[0] + bg.rho_ur * getN(c, y, 2, 0);
+    double rho_mono_b = bg.rho_b * getb(c, y, 0, 0), rho_mono_c = bg.rho_cdm * getc(c, y, 0, 0);
+    double phi = y(s.idx_phi);
+    w.psi = phi - 3 / 5. * (a_sq / k_sq) * rho_quadrupole + (lin ? 0.0 : qs[s.iq_psi]);
+    w.phi_prime = y(s.idx_phip);
+    w.phi_pp = k_sq / 3 * (w.psi - 2 * phi) - Hc * (3 * w.phi_prime) - 2 * w.psi * (Hc * Hc + bg.Hc_prime) -
+               a_sq / 2 * (rho_mono_b + rho_mono_c) + (lin ? 0.0 : qs[s.iq_phi_prime_prime]);
+  } else {
+    w.psi = w.phi_prime = w.phi_pp = 0;
+  }
+  w.omega_m1_prime = 0;
+  if (s.compute_m[1]) {
+    double rq1 = bg.rho_g * w.I_2m[1] + bg.rho_b * w.b_22m[1] + bg.rho_cdm * w.cdm_22m[1] + bg.rho_ur * getN(c, y, 2, 1);
+    w.omega_m1_prime = -2 * Hc * y(s.idx_omega) + 2 * SQRT_3 / (5. * k) * a_sq * rq1 + (lin ? 0.0 : qs[s.iq_omega_m1_prime]);
+  }
+  w.gamma_m2_pp = 0;
+  if (s.compute_m[2]) {
+    double rq2 = bg.rho_g * w.I_2m[2] + bg.rho_b * w.b_22m[2] + bg.rho_cdm * w.cdm_22m[2] + bg.rho_ur * getN(c, y, 2, 2);
+    w.gamma_m2_pp = -2 * Hc * y(s.idx_gammap) - k_sq * y(s.idx_gamma) - 2 / 5. * a_sq * rq2 +
+                    (lin ? 0.0 : qs[s.iq_gamma_m2_prime_prime]);
+  }
+}
+
+/* ------------------------------------------------------------------ derivs rows */
+
+template <class Y>
+__device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
+  const DevSpec &s = c.s;
+  const Tri &t = c.sh->tri;
+  const BgV &bg = c.sh->bg;
+  int sp = __ldg(c.p.eq_sp + i), l = __ldg(c.p.eq_l + i), m = __ldg(c.p.eq_m + i);
+  double k = t.k, kd = bg.kappa_dot, Hc = bg.Hc;
+  double mc = s.compute_m[0] ? -3 * w.phi_prime : 0.0, me = s.compute_m[0] ? k * w.psi : 0.0;
+  double omp = w.omega_m1_prime, om = s.compute_m[1] ? y(s.idx_omega) : 0.0;
+  double gp = s.compute_m[2] ? y(s.idx_gammap) : 0.0;
+  int use_qs = !lin && s.has_qs;
+  double d = 0.0;
+  switch (sp) {
+  case SP_I: {
+    if (tca && l >= 1) return 0.0;
+    if (!tca && l == s.l_max_g) {
+      double c_pre = (m == 0 ? (2 * l + 1) / (2 * l - 1.) : sqrt((double)(l + m) / (l - m)) * (2 * l + 1) / (2 * l - 1.));
+      double cc = (l + 1 + m) / (k * tau);
+      d = k * (c_pre * getI(c, tca, y, l - 1, m) - cc * getI(c, tca, y, l, m)) - kd * getI(c, tca, y, l, m);
+    } else if (l == 0) {
+      d = -FOUR_THIRDS * (k * w.I_1m[0] / 4 + mc);
+    } else if (l == 1) {
+      d = k * (c.cmin(1, m, m) * w.I_00 - c.cplu(1, m, m) * w.I_2m[m]) + w.C_1m[m];
+      if (m == 0) d += 4 * me;
+      if (m == 1) d += -4 * omp;
+    } else if (l == 2) {
+      double Pi = 0.1 * (w.I_2m[m] - SQRT_6 * w.E_2m[m]);
+      d = k * (c.cmin(2, m, m) * w.I_1m[m] - c.cplu(2, m, m) * getI(c, tca, y, 3, m)) - kd * (w.I_2m[m] - Pi);
+      if (m == 2) d += 4 * gp;
+    } else {
+      d = k * (c.cmin(l, m, m) * getI(c, tca, y, l - 1, m) - c.cplu(l, m, m) * getI(c, tca, y, l + 1, m)) -
+          kd * getI(c, tca, y, l, m);
+    }
+    if (use_qs) d += c.qs[s.iq_g + c.LM(l, m)];
+    return d;
+  }
+  case SP_E: {
+    if (tca) return 0.0;
+    if (l == s.l_max_pol) {
+      double c_pre = sqrt(1 - ((double)m * m) / (l * l) * (l + 2) / (l - 2.)) * (2 * l + 1) / (2 * l - 1.);
+      double cc = (l + 3) / (k * tau), cmix = (double)m / l;
+      d = k * (c_pre * getE(c, tca, y, l - 1, m) - cc * getE(c, tca, y, l, m) - cmix * getB(c, tca, y, l, m)) -
+          kd * getE(c, tca, y, l, m);
+    } else if (l == 2) {
+      double Pi = 0.1 * (w.I_2m[m] - SQRT_6 * w.E_2m[m]);
+      d = k * (-c.dplu(2, m, m) * getE(c, tca, y, 3, m) - c.dzer(2, m, m) * w.B_2m[m]) - kd * (w.E_2m[m] + SQRT_6 * Pi);
+    } else {
+      d = k * (c.dmin(l, m, m) * getE(c, tca, y, l - 1, m) - c.dplu(l, m, m) * getE(c, tca, y, l + 1, m) -
+               c.dzer(l, m, m) * getB(c, tca, y, l, m)) -
+          kd * getE(c, tca, y, l, m);
+    }
+    if (use_qs) d += c.qs[s.iq_E + c.LM(l, m)];
+    return d;
+  }
+  case SP_B: {
+    if (tca) return 0.0;
+    if (l == s.l_max_pol) {
+      double c_pre = sqrt(1 - ((double)m * m) / (l * l) * (l + 2) / (l - 2.)) * (2 * l + 1) / (2 * l - 1.);
+      double cc = (l + 3) / (k * tau), cmix = (double)m / l;
+      d = k * (c_pre * getB(c, tca, y, l - 1, m) - cc * getB(c, tca, y, l, m) + cmix * getE(c, tca, y, l, m)) -
+          kd * getB(c, tca, y, l, m);
+    } else {
+      d = k * (c.dmin(l, m, m) * getB(c, tca, y, l - 1, m) - c.dplu(l, m, m) * getB(c, tca, y, l + 1, m) +
+               c.dzer(l, m, m) * getE(c, tca, y, l, m)) -
+          kd * getB(c, tca, y, l, m);
+    }
+    if (use_qs) d += c.qs[s.iq_B + c.LM(l, m)];
+    return d;
+  }
+  case SP_N: {
+    if (l == s.l_max_ur) {
+      double c_pre = (m == 0 ? (2 * l + 1) / (2 * l - 1.) : sqrt((double)(l + m) / (l - m)) * (2 * l + 1) / (2 * l - 1.));
+      double cc = (l + 1 + m) / (k * tau);
+      d = k * (c_pre * getN(c, y, l - 1, m) - cc * getN(c, y, l, m));
+    } else if (l == 0) {
+      d = -FOUR_THIRDS * (k * w.N_1m[0] * 0.25 + mc);
+    } else if (l == 1) {
+      d = k * (c.cmin(1, m, m) * w.N_00 - c.cplu(1, m, m) * getN(c, y, 2, m));
+      if (m == 0) d += 4 * me;
+      if (m == 1) d += -4 * omp;
+    } else {
+      d = k * (c.cmin(l, m, m) * getN(c, y, l - 1, m) - c.cplu(l, m, m) * getN(c, y, l + 1, m));
+      if (l == 2 && m == 2) d += 4 * gp;
+    }
+    if (use_qs) d += c.qs[s.iq_ur + c.LM(l, m)];
+    return d;
+  }
+  case SP_B000:
+    d = -(k * getb(c, y, 1, 0) / 3.0 + mc) - Hc * w.b_200;
+    if (use_qs) d += c.qs[s.iq_b000];
+    return d;
+  case SP_B11:
+    d = -Hc * getb(c, y, 1, m) + k * (c.cmin(1, m, m) * w.b_200 - c.cplu(1, m, m) * w.b_22m[m]) - bg.r * w.C_1m[m];
+    if (m == 0) d += 3 * me;
+    if (m == 1) d += -3 * (omp + Hc * om);
+    if (use_qs) d += c.qs[s.iq_b11[m]];
+    return d;
+  case SP_C000:
+    d = -(k * getc(c, y, 1, 0) / 3.0 + mc) - Hc * w.cdm_200;
+    if (use_qs) d += c.qs[s.iq_c000];
+    return d;
+  case SP_C11:
+    d = -Hc * getc(c, y, 1, m) + k * (c.cmin(1, m, m) * w.cdm_200 - c.cplu(1, m, m) * w.cdm_22m[m]);
+    if (m == 0) d += 3 * me;
+    if (m == 1) d += -3 * (omp + Hc * om);
+    if (use_qs) d += c.qs[s.iq_c11[m]];
+    return d;
+  case SP_PHI:
+    return w.phi_prime;
+  case SP_PHIP: {
+    /* phi'' = (einstein part) - Hc psi' (perturb2_compute_psi_prime, perturbations2.c:10188-10383) */
+    double dI20;
+    if (!tca) dI20 = row(c, tca, c.p.idx_I[c.LM(2, 0)], y, w, lin, tau);
+    else dI20 = 2 / 3. * k * w.I_1m_tca1[0] - kd * (w.I_2m_tca1[0] - w.Pi_tca1[0]) + (use_qs ? c.qs[s.iq_g + c.LM(2, 0)] : 0.0);
+    double dN20 = row(c, tca, c.p.idx_N[c.LM(2, 0)], y, w, lin, tau);
+    double rqp = bg.rho_g * dI20 + bg.rho_ur * dN20;
+    if (!lin) {
+      const double *fo1 = c.fo1, *fo2 = c.fo2;
+      rqp += bg.rho_b * 15 * t.k1_ten_k2[2] * (fo1[SONG2_FO_V_B_P] * fo2[SONG2_FO_V_B] + fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B_P]);
+      rqp += bg.rho_cdm * 15 * t.k1_ten_k2[2] *
+             (fo1[SONG2_FO_V_CDM_P] * fo2[SONG2_FO_V_CDM] + fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM_P]);
+    }
+    double psi_prime = w.phi_prime - 2 * Hc * (w.psi - y(s.idx_phi)) -
+                       3 / 5. * (bg.a_sq / t.k_sq) * (rqp + Hc * bg.rho_b * w.b_22m[0] + Hc * bg.rho_cdm * w.cdm_22m[0]) +
+                       (lin ? 0.0 : c.qs[s.iq_psi_prime]);
+    return w.phi_pp - Hc * psi_prime;
+  }
+  case SP_OMEGA:
+    return omp;
+  case SP_GAMMA:
+    return gp;
+  case SP_GAMMAP:
+    return w.gamma_m2_pp;
+  }
+  return 0.0;
+}
+
+/* dy = f(tau, y): block-wide; prepare(tau) must have run.  Ends with a barrier. */
+__device__ void rhs(const K &c, int tca, double tau, const double *y, double *dy) {
+  const DevSpec &s = c.s;
+  YVec yv{y};
+  if (threadIdx.x == 0) compute_ws(c, tca, yv, 0, c.sh->ws);
+  __syncthreads();
+  for (int i = threadIdx.x; i < s.n; i += blockDim.x) dy[i] = row(c, tca, i, yv, c.sh->ws, 0, tau);
+  __syncthreads();
+}
+
+/* Exact Jacobian of the affine system at tau (prepare(tau) must have run):
+   J[:, j] = A e_j, one thread per column; stored per m block in global scratch. */
+__device__ void jacobian(const K &c, int tca, double tau) {
+  const DevSpec &s = c.s;
+  for (int j = threadIdx.x; j < s.n; j += blockDim.x) {
+    int b = 0;
+    while (b + 1 < s.nblk && j >= s.blk_start[b + 1]) ++b;
+    int b0 = s.blk_start[b], nb = s.blk_size[b];
+    YUnit yu{j};
+    WS w;
+    compute_ws(c, tca, yu, 1, w);
+    double *J = c.jac + s.lu_off[b];
+    for (int i = b0; i < b0 + nb; ++i) J[(size_t)(i - b0) * nb + (j - b0)] = row(c, tca, i, yu, w, 1, tau);
+  }
+  __syncthreads();
+}
+
+/* ------------------------------------------------------------------ block LU per m (one warp each) */
+
+template <typename T> __device__ inline T tabs(T x) { return x < T(0) ? -x : x; }
+
+template <typename T> __device__ void form_and_factor(const K &c, double hinvGak) {
+  const DevSpec &s = c.s;
+  T *LU = (T *)c.lu;
+  for (int e = threadIdx.x; e < s.lu_elems; e += blockDim.x) {
+    int b = 0;
+    while (b + 1 < s.nblk && e >= s.lu_off[b + 1]) ++b;
+    int nb = s.blk_size[b], r = (e - s.lu_off[b]) / nb, col = (e - s.lu_off[b]) % nb;
+    double v = -hinvGak * c.jac[e];
+    if (r == col) v += 1.0;
+    LU[e] = (T)v;
+  }
+  __syncthreads();
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < s.nblk) {
+    int nb = s.blk_size[warp];
+    T *A = LU + s.lu_off[warp];
+    int *pv = c.piv + s.blk_start[warp];
+    for (int kk = 0; kk < nb; ++kk) {
+      T best = T(-1);
+      int bi = kk;
+      for (int i = kk + lane; i < nb; i += 32) {
+        T v = tabs(A[i * nb + kk]);
+        if (v > best) { best = v; bi = i; }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        T ob = __shfl_xor_sync(0xffffffffu, best, off);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (lane == 0) pv[kk] = bi;
+      if (!(best > T(0))) {
+        if (lane == 0) c.sh->lu_fail = 1;
+        A[kk * nb + kk] = T(1);
+        __syncwarp();
+        continue;
+      }
+      if (bi != kk)
+        for (int j = lane; j < nb; j += 32) {
+          T tmp = A[kk * nb + j];
+          A[kk * nb + j] = A[bi * nb + j];
+          A[bi * nb + j] = tmp;
+        }
+      __syncwarp();
+      T inv = T(1) / A[kk * nb + kk];
+      for (int i = kk + 1 + lane; i < nb; i += 32) A[i * nb + kk] *= inv;
+      __syncwarp();
+      for (int i = kk + 1; i < nb; ++i) {
+        T lik = A[i * nb + kk];
+        if (lik != T(0))
+          for (int j = kk + 1 + lane; j < nb; j += 32) A[i * nb + j] -= lik * A[kk * nb + j];
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+}
+
+/* del <- M^{-1} rhs (rhs given in c.del, result written back to c.del) */
+template <typename T> __device__ void lu_solve(const K &c) {
+  const DevSpec &s = c.s;
+  T *x = (T *)c.xsol;
+  for (int i = threadIdx.x; i < s.n; i += blockDim.x) x[i] = (T)c.del[i];
+  __syncthreads();
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < s.nblk) {
+    int nb = s.blk_size[warp];
+    const T *A = (const T *)c.lu + s.lu_off[warp];
+    const int *pv = c.piv + s.blk_start[warp];
+    T *xb = x + s.blk_start[warp];
+    if (lane == 0)
+      for (int kk = 0; kk < nb; ++kk) {
+        int p = pv[kk];
+        if (p != kk) { T tmp = xb[kk]; xb[kk] = xb[p]; xb[p] = tmp; }
+      }
+    __syncwarp();
+    for (int j = 0; j < nb; ++j) {
+      T xj = xb[j];
+      for (int i = j + 1 + lane; i < nb; i += 32) xb[i] -= A[i * nb + j] * xj;
+      __syncwarp();
+    }
+    for (int j = nb - 1; j >= 0; --j) {
+      if (lane == 0) xb[j] /= A[j * nb + j];
+      __syncwarp();
+      T xj = xb[j];
+      for (int i = lane; i < j; i += 32) xb[i] -= A[i * nb + j] * xj;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < s.n; i += blockDim.x) c.del[i] = (double)x[i];
+  __syncthreads();
+}
+
+/* ------------------------------------------------------------------ reductions */
+
+__device__ double block_max(const K &c, double v) {
+  if (!(v == v)) v = INFINITY;
+  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) c.sh->red[warp] = v;
+  __syncthreads();
+  double r = 0.0;
+  int nw = (blockDim.x + 31) >> 5;
+  for (int i = 0; i < nw; ++i) r = fmax(r, c.sh->red[i]);
+  return r;
+}
+
+/* ------------------------------------------------------------------ outputs */
+
+__device__ void store_sources(const K &c, int index_tau, double tau, const double *y, const double *dy) {
+  const DevSpec &s = c.s;
+  const Tri &t = c.sh->tri;
+  int tca = c.sh->tca;
+  YVec yv{y};
+  /* psi' from the phi' row: psi' = (phi_pp - dy[phi']) / Hc */
+  if (threadIdx.x == 0) {
+    const WS &w = c.sh->ws;
+    double psi_prime = 0.0;
+    if (s.compute_m[0]) psi_prime = (w.phi_pp - dy[s.idx_phip]) / c.sh->bg.Hc;
+    c.sh->psi_prime = psi_prime;
+  }
+  __syncthreads();
+  const WS &w = c.sh->ws;
+  const BgV &bg = c.sh->bg;
+  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  double k1 = t.k1, k2 = t.k2, k = t.k;
+  double psi_1 = fo1[SONG2_FO_PSI], psi_2 = fo2[SONG2_FO_PSI], phi_1 = fo1[SONG2_FO_PHI], phi_2 = fo2[SONG2_FO_PHI];
+  double phi_prime_1 = fo1[SONG2_FO_PHI_P], phi_prime_2 = fo2[SONG2_FO_PHI_P];
+  double psi_prime_1 = fo1[SONG2_FO_PSI_P], psi_prime_2 = fo2[SONG2_FO_PSI_P];
+  double psi = w.psi, phi_prime = w.phi_prime, psi_prime = c.sh->psi_prime;
+  if (s.compute_m[0] && s.los_exp_pot) {
+    psi = psi - 2 * psi_1 * psi_2;
+    phi_prime = phi_prime + 2 * (phi_1 * phi_prime_2 + phi_prime_1 * phi_2);
+    psi_prime = psi_prime - 2 * (psi_1 * psi_prime_2 + psi_prime_1 * psi_2);
+  }
+  double omp = w.omega_m1_prime, gp = s.compute_m[2] ? y[s.idx_gammap] : 0.0;
+  double kd = bg.kappa_dot;
+  int64_t col = t.pair_off + (int64_t)index_tau * t.k3_size + t.i3;
+  for (int tp = threadIdx.x; tp < s.tp2_size; tp += blockDim.x) {
+    int kind = s.tp_kind[tp], l = s.tp_l[tp], m = s.tp_m[tp];
+    double src = 0.0;
+    if (kind == TP_T) {
+      if (l == 0) {
+        src += kd * w.I_00;
+        if (s.los_pure_metric) src += 4 * phi_prime;
+        else {
+          src += (s.los_sw ? 1 : 0) * (4 * kd * psi);
+          src += (s.los_isw ? 1 : 0) * (4 * (phi_prime + psi_prime));
+        }
+        if (s.los_quad_metric && !s.los_exp_pot) src += 8 * (phi_1 * phi_prime_2 + phi_2 * phi_prime_1);
+      } else if (l == 1) {
+        if (s.los_pure_scat) src += FOUR_THIRDS * kd * getb(c, yv, 1, m);
+        if (s.los_pure_metric) {
+          if (m == 0) src += 4 * k * psi;
+          if (m == 1) src += -4 * omp;
+        } else if (m == 1)
+          src += (s.los_isw ? 1 : 0) * (-4 * omp);
+        if (s.los_quad_metric) {
+          if (!s.los_exp_pot) src += -4 * (t.k1_m[m + 1] * psi_1 * (psi_2 - phi_2) + t.k2_m[m + 1] * psi_2 * (psi_1 - phi_1));
+          else src += -4 * (t.k1_m[m + 1] * psi_1 * (-psi_2 - phi_2) + t.k2_m[m + 1] * psi_2 * (-psi_1 - phi_1));
+        }
+      } else if (l == 2) {
+        if (s.los_pure_scat) src += kd * 0.1 * (w.I_2m[m] - SQRT_6 * w.E_2m[m]);
+        if (s.los_pure_metric && m == 2) src += 4 * gp;
+      }
+      if (s.los_quad_scat) src += c.qc[s.iq_g + c.LM(l, m)];
+      if (s.los_time_delay)
+        src -= c.I2r(l + 1) * c.S(CP22, l, m) * k2 * (phi_1 + psi_1) - c.I2r(l - 1) * c.S(CM22, l, m) * k2 * (phi_1 + psi_1) +
+               c.I1r(l + 1) * c.S(CP11, l, m) * k1 * (phi_2 + psi_2) - c.I1r(l - 1) * c.S(CM11, l, m) * k1 * (phi_2 + psi_2);
+      if (s.los_redshift)
+        src -= -4 * phi_prime_1 * c.rot_2(l, m) * c.I2r(l) + c.I2r(l + 1) * 4 * c.S(CP12, l, m) * k1 * psi_1 -
+               c.I2r(l - 1) * 4 * c.S(CM12, l, m) * k1 * psi_1 - 4 * phi_prime_2 * c.rot_1(l, m) * c.I1r(l) +
+               c.I1r(l + 1) * 4 * c.S(CP21, l, m) * k2 * psi_2 - c.I1r(l - 1) * 4 * c.S(CM21, l, m) * k2 * psi_2;
+      if (s.los_lensing)
+        src -= c.I2r(l + 1) * (-(l + 2) * c.S(CP12, l, m)) * k1 * (phi_1 + psi_1) -
+               c.I2r(l - 1) * ((l - 1) * c.S(CM12, l, m)) * k1 * (phi_1 + psi_1) +
+               c.I1r(l + 1) * (-(l + 2) * c.S(CP21, l, m)) * k2 * (phi_2 + psi_2) -
+               c.I1r(l - 1) * ((l - 1) * c.S(CM21, l, m)) * k2 * (phi_2 + psi_2);
+    } else if (kind == TP_E) {
+      if (l >= 2) {
+        if (l == 2 && s.los_pure_scat) src += -SQRT_6 * kd * 0.1 * (w.I_2m[m] - SQRT_6 * w.E_2m[m]);
+        if (s.los_quad_scat) src += c.qc[s.iq_E + c.LM(l, m)];
+        if (s.los_time_delay)
+          src -= c.E2r(l + 1) * c.S(DP22, l, m) * k2 * (phi_1 + psi_1) - c.E2r(l - 1) * c.S(DM22, l, m) * k2 * (phi_1 + psi_1) +
+                 c.E1r(l + 1) * c.S(DP11, l, m) * k1 * (phi_2 + psi_2) - c.E1r(l - 1) * c.S(DM11, l, m) * k1 * (phi_2 + psi_2);
+        if (s.los_redshift)
+          src -= -4 * phi_prime_1 * c.rot_2(l, m) * c.E2r(l) + c.E2r(l + 1) * 4 * c.S(DP12, l, m) * k1 * psi_1 -
+                 c.E2r(l - 1) * 4 * c.S(DM12, l, m) * k1 * psi_1 - 4 * phi_prime_2 * c.rot_1(l, m) * c.E1r(l) +
+                 c.E1r(l + 1) * 4 * c.S(DP21, l, m) * k2 * psi_2 - c.E1r(l - 1) * 4 * c.S(DM21, l, m) * k2 * psi_2;
+        if (s.los_lensing)
+          src -= c.E2r(l + 1) * (-(l + 2) * c.S(DP12, l, m)) * k1 * (phi_1 + psi_1) -
+                 c.E2r(l - 1) * ((l - 1) * c.S(DM12, l, m)) * k1 * (phi_1 + psi_1) +
+                 c.E1r(l + 1) * (-(l + 2) * c.S(DP21, l, m)) * k2 * (phi_2 + psi_2) -
+                 c.E1r(l - 1) * ((l - 1) * c.S(DM21, l, m)) * k2 * (phi_2 + psi_2);
+      }
+    } else if (kind == TP_B) {
+      if (l >= 2 && m != 0) {
+        if (s.los_quad_scat) src += c.qc[s.iq_B + c.LM(l, m)];
+        if (s.los_time_delay)
+          src -= -k2 * c.E2r(l) * c.S(DZ22, l, m) * (phi_1 + psi_1) - k1 * c.E1r(l) * c.S(DZ11, l, m) * (phi_2 + psi_2);
+        if (s.los_redshift)
+          src -= -c.E2r(l) * 4 * c.S(DZ12, l, m) * k1 * psi_1 - c.E1r(l) * 4 * c.S(DZ21, l, m) * k2 * psi_2;
+        if (s.los_lensing)
+          src -= -c.E2r(l) * (-c.S(DZ12, l, m)) * k1 * (phi_1 + psi_1) - c.E1r(l) * (-c.S(DZ21, l, m)) * k2 * (phi_2 + psi_2);
+      }
+    } else if (kind == TP_D) {
+      if (s.compute_m[0]) {
+        double v_dot_v_cdm = -t.k1_dot_k2 * fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM];
+        src = 0.5 * (getc(c, yv, 0, 0) - 2 * v_dot_v_cdm);
+      }
+      c.p.sources[(int64_t)tp * s.per_type + col] = src;
+      continue;
+    }
+    c.p.sources[(int64_t)tp * s.per_type + col] = src * bg.exp_m_kappa;
+  }
+  (void)tca;
+}
+
+__device__ void store_first_order(const K &c, int index_tau, const double *y, const double *dy) {
+  const DevSpec &s = c.s;
+  const Tri &t = c.sh->tri;
+  int tca = c.sh->tca;
+  YVec yv{y};
+  const WS &w = c.sh->ws;
+  const BgV &bg = c.sh->bg;
+  double k = t.k;
+  double *o = c.p.fo_out + ((size_t)t.i1 * s.fo_tau_size + index_tau) * s.nfo;
+  int L1 = s.fo_l_max + 1;
+  for (int q = threadIdx.x; q < s.nfo; q += blockDim.x) {
+    double v = 0.0;
+    if (q < SONG2_FO_I) {
+      switch (q) {
+      case SONG2_FO_PHI: v = y[s.idx_phi]; break;
+      case SONG2_FO_PSI: v = w.psi; break;
+      case SONG2_FO_PHI_P: v = y[s.idx_phip]; break;
+      case SONG2_FO_PSI_P: v = (w.phi_pp - dy[s.idx_phip]) / bg.Hc; break;
+      case SONG2_FO_PHI_PP: v = dy[s.idx_phip]; break;
+      case SONG2_FO_DELTA_G: v = w.I_00; break;
+      case SONG2_FO_V_G: v = -w.I_1m[0] / (4 * k); break;
+      case SONG2_FO_DELTA_B: v = y[s.idx_b000]; break;
+      case SONG2_FO_V_B: v = -y[s.idx_b11[0]] / (3 * k); break;
+      case SONG2_FO_DELTA_B_P: v = dy[s.idx_b000]; break;
+      case SONG2_FO_V_B_P: v = -dy[s.idx_b11[0]] / (3 * k); break;
+      case SONG2_FO_DELTA_CDM: v = y[s.idx_c000]; break;
+      case SONG2_FO_V_CDM: v = -y[s.idx_c11[0]] / (3 * k); break;
+      case SONG2_FO_V_CDM_P: v = -dy[s.idx_c11[0]] / (3 * k); break;
+      case SONG2_FO_DELTA_UR: v = w.N_00; break;
+      case SONG2_FO_V_UR: v = -w.N_1m[0] / (4 * k); break;
+      case SONG2_FO_DIPOLE_B: v = y[s.idx_b11[0]]; break;
+      case SONG2_FO_DIPOLE_CDM: v = y[s.idx_c11[0]]; break;
+      }
+    } else {
+      int blk = (q - SONG2_FO_I) / L1, l = (q - SONG2_FO_I) % L1;
+      if (blk == 0) v = (l == 0) ? w.I_00 : (l == 1) ? w.I_1m[0] : (l == 2) ? w.I_2m[0] : getI(c, tca, yv, l, 0);
+      else if (blk == 1) v = (l < 2) ? 0.0 : (l == 2) ? w.E_2m[0] : getE(c, tca, yv, l, 0);
+      else if (blk == 2) v = (l == 0) ? w.N_00 : (l == 1) ? w.N_1m[0] : getN(c, yv, l, 0);
+      else
+        v = (l == 0) ? 0.0 : (l == 1) ? w.C_1m[0] / bg.kappa_dot
+          : (l == 2) ? -w.I_2m[0] + 0.1 * (w.I_2m[0] - SQRT_6 * w.E_2m[0]) : -getI(c, tca, yv, l, 0);
+    }
+    o[q] = v;
+  }
+}
+
+/* ------------------------------------------------------------------ geometry */
+
+/* sqrt((l-m)!/(l+m)!) P_l^m(x), Condon-Shortley phase, normalised recurrence */
+__device__ double legendre_norm(int l, int m, double x) {
+  double sx = sqrt(fmax(0.0, 1.0 - x * x));
+  double q = 1.0;
+  for (int i = 1; i <= m; ++i) q *= -sqrt((2.0 * i - 1.0) / (2.0 * i)) * sx;
+  if (l == m) return q;
+  double q0 = q, q1 = x * sqrt(2.0 * m + 1.0) * q;
+  for (int ll = m + 2; ll <= l; ++ll) {
+    double q2 = ((2.0 * ll - 1.0) * x * q1 - sqrt((double)(ll - 1) * (ll - 1) - (double)m * m) * q0) /
+                sqrt((double)ll * ll - (double)m * m);
+    q0 = q1; q1 = q2;
+  }
+  return q1;
+}
+
+__device__ int geometry(const K &c) {
+  const DevSpec &s = c.s;
+  Tri &t = c.sh->tri;
+  int tid = threadIdx.x;
+  if (tid == 0) {
+    double k1 = t.k1, k2 = t.k2, k = t.k;
+    t.k_sq = k * k;
+    t.cosk1k2 = (t.k_sq - k1 * k1 - k2 * k2) / (2 * k1 * k2);
+    t.cosk1k = (k1 + k2 * t.cosk1k2) / k;
+    t.cosk2k = (k2 + k1 * t.cosk1k2) / k;
+    t.k1_dot_k2 = k1 * k2 * t.cosk1k2;
+  }
+  __syncthreads();
+  if (fabs(t.cosk1k2) > 1 || fabs(t.cosk1k) > 1 || fabs(t.cosk2k) > 1) return 1;
+  for (int e = tid; e < (s.Lq + 1) * (s.mq_max + 1); e += blockDim.x) {
+    int l = e / (s.mq_max + 1), m = e % (s.mq_max + 1);
+    if (m > l) continue;
+    double r1 = legendre_norm(l, m, t.cosk1k), r2 = legendre_norm(l, m, t.cosk2k);
+    if (m & 1) r2 = -r2;
+    c.rot1[c.LMQ(l, m)] = r1;
+    c.rot2[c.LMQ(l, m)] = r2;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double k1 = t.k1, k2 = t.k2;
+    double k1_M1 = t.k1_m[0] = k1 * c.rot_1(1, -1), k1_0 = t.k1_m[1] = k1 * c.rot_1(1, 0), k1_P1 = t.k1_m[2] = k1 * c.rot_1(1, 1);
+    double k2_M1 = t.k2_m[0] = k2 * c.rot_2(1, -1), k2_0 = t.k2_m[1] = k2 * c.rot_2(1, 0), k2_P1 = t.k2_m[2] = k2 * c.rot_2(1, 1);
+    double kk = t.k1_dot_k2;
+    t.k1_ten_k2[0] = SQRT_2 / SQRT_3 * k1_M1 * k2_M1;
+    t.k1_ten_k2[1] = (k1_M1 * k2_0 + k2_M1 * k1_0) / SQRT_3;
+    t.k1_ten_k2[2] = k1_0 * k2_0 - kk / 3.;
+    t.k1_ten_k2[3] = (k1_P1 * k2_0 + k2_P1 * k1_0) / SQRT_3;
+    t.k1_ten_k2[4] = SQRT_2 / SQRT_3 * k1_P1 * k2_P1;
+    t.k1_ten_k1[0] = SQRT_2 / SQRT_3 * k1_M1 * k1_M1;
+    t.k1_ten_k1[1] = (k1_M1 * k1_0 + k1_M1 * k1_0) / SQRT_3;
+    t.k1_ten_k1[2] = k1_0 * k1_0 - k1 * k1 / 3.;
+    t.k1_ten_k1[3] = (k1_P1 * k1_0 + k1_P1 * k1_0) / SQRT_3;
+    t.k1_ten_k1[4] = SQRT_2 / SQRT_3 * k1_P1 * k1_P1;
+    t.k2_ten_k2[0] = SQRT_2 / SQRT_3 * k2_M1 * k2_M1;
+    t.k2_ten_k2[1] = (k2_M1 * k2_0 + k2_M1 * k2_0) / SQRT_3;
+    t.k2_ten_k2[2] = k2_0 * k2_0 - k2 * k2 / 3.;
+    t.k2_ten_k2[3] = (k2_P1 * k2_0 + k2_P1 * k2_0) / SQRT_3;
+    t.k2_ten_k2[4] = SQRT_2 / SQRT_3 * k2_P1 * k2_P1;
+  }
+  /* summed couplings (perturbations2.c:5752-5845) for l <= L_big */
+  for (int e = tid; e < (s.L_big + 1) * s.m_size; e += blockDim.x) {
+    int l = e / s.m_size, im = e % s.m_size, m = s.m[im];
+    if (m > l) continue;
+    int lm = c.LM(l, m);
+    double a[20];
+    for (int X = 0; X < 20; ++X) a[X] = 0.0;
+    for (int m2 = -1; m2 <= 1; ++m2) {
+      int m1 = m - m2;
+      double cm = __ldg(c.p.cmin + lm * 3 + m - m1 + 1), cp = __ldg(c.p.cplu + lm * 3 + m - m1 + 1);
+      double dm = __ldg(c.p.dmin + lm * 3 + m - m1 + 1), dp = __ldg(c.p.dplu + lm * 3 + m - m1 + 1);
+      double dz = __ldg(c.p.dzer + lm * 3 + m - m1 + 1);
+      double r11 = c.rot_1(1, m2), r21 = c.rot_2(1, m2);
+      double r1m = c.rot_1(l - 1, m1), r2m = c.rot_2(l - 1, m1), r1p = c.rot_1(l + 1, m1), r2p = c.rot_2(l + 1, m1);
+      double r10 = c.rot_1(l, m1), r20 = c.rot_2(l, m1);
+      a[CM12] += r11 * r2m * cm; a[CM21] += r21 * r1m * cm; a[CP12] += r11 * r2p * cp; a[CP21] += r21 * r1p * cp;
+      a[CM11] += r11 * r1m * cm; a[CM22] += r21 * r2m * cm; a[CP11] += r11 * r1p * cp; a[CP22] += r21 * r2p * cp;
+      a[DM12] += r11 * r2m * dm; a[DM21] += r21 * r1m * dm; a[DP12] += r11 * r2p * dp; a[DP21] += r21 * r1p * dp;
+      a[DM11] += r11 * r1m * dm; a[DM22] += r21 * r2m * dm; a[DP11] += r11 * r1p * dp; a[DP22] += r21 * r2p * dp;
+      a[DZ12] += r11 * r20 * dz; a[DZ21] += r21 * r10 * dz; a[DZ11] += r11 * r10 * dz; a[DZ22] += r21 * r20 * dz;
+    }
+    for (int X = 0; X < 20; ++X) c.sc[X * s.n_lm + lm] = a[X];
+  }
+  __syncthreads();
+  return 0;
+}
+
+/* start time (perturbations2.c:3388-3524) and TCA interval (perturbations2.c:4854-5403), thread 0 */
+__device__ int intervals(const K &c) {
+  const DevSpec &s = c.s;
+  Tri &t = c.sh->tri;
+  double kmax = fmax(t.k, fmax(t.k1, t.k2));
+  double tau_lower = exp(s.bg_lntau0), tau_upper = c.p.tau[0];
+  if (s.mode_first_order) tau_upper = exp(s.fo_lntau0);
+  double Hc, kd;
+  bg_hk(c, tau_lower, Hc, kd);
+  if (Hc / kd > s.start_h || kmax / Hc > s.start_k) return 1;
+  double tau_mid = 0.5 * (tau_lower + tau_upper);
+  for (int it = 0; it < 200 && (tau_upper - tau_lower) / tau_lower > s.tol_tau; ++it) {
+    bg_hk(c, tau_mid, Hc, kd);
+    if (Hc / kd > s.start_h || kmax / Hc > s.start_k) tau_upper = tau_mid;
+    else tau_lower = tau_mid;
+    tau_mid = 0.5 * (tau_lower + tau_upper);
+  }
+  t.tau_ini = tau_mid;
+  t.tau_end = s.mode_first_order ? exp(s.fo_lntau0 + (s.fo_tau_size - 1) * s.fo_dlntau) : c.p.tau[s.tau_size - 1];
+  if (s.mode_first_order) t.tau_end = exp(s.fo_lntau0 + (s.fo_tau_size - 1) * s.fo_dlntau);
+  /* TCA trigger: tau_c/tau_h < trig_h and tau_c * max(k1,k2,k) < trig_k */
+  auto tca_on = [&](double tau) {
+    double h, kk;
+    bg_hk(c, tau, h, kk);
+    return s.tca_on && ((1.0 / kk) / (1.0 / h) < s.tca_h) && ((1.0 / kk) * kmax < s.tca_k);
+  };
+  t.tca0 = tca_on(t.tau_ini);
+  t.nint = 1;
+  t.tau_switch = t.tau_end;
+  if (t.tca0 && !tca_on(t.tau_end)) {
+    double lo = t.tau_ini, hi = t.tau_end;
+    for (int it = 0; it < 200 && (hi - lo) / lo > s.tol_tau; ++it) {
+      double mid = 0.5 * (lo + hi);
+      if (tca_on(mid)) lo = mid; else hi = mid;
+    }
+    t.tau_switch = 0.5 * (lo + hi);
+    t.nint = 2;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------ initial conditions (thread 0) */
+
+__device__ void initial_conditions(const K &c, double tau) {
+  const DevSpec &s = c.s;
+  const Tri &t = c.sh->tri;
+  const BgV &bg = c.sh->bg;
+  double *y = c.y;
+  for (int i = 0; i < s.n; ++i) y[i] = 0.0;
+  if (s.ic == SONG2_IC_ZERO || !s.compute_m[0]) return;
+  int tca = c.sh->tca;
+  double k = t.k, k_sq = t.k_sq, Hc = bg.Hc, Hc_sq = Hc * Hc, a_sq = bg.a_sq;
+  double rho_r = bg.rho_g + bg.rho_ur, frac_ur = bg.rho_ur / rho_r, frac_g = 1 - frac_ur;
+  double rho_tot = Hc_sq / a_sq, Omega_m = (bg.rho_b + bg.rho_cdm) / rho_tot, Omega_r = rho_r / rho_tot;
+  const double *fo1 = c.fo1, *fo2 = c.fo2, *qs = c.qs;
+  if (s.ic == SONG2_IC_AD) {
+    double k1_0 = t.k1_m[1], k2_0 = t.k2_m[1];
+    double delta_g_1 = fo1[SONG2_FO_DELTA_G], delta_g_2 = fo2[SONG2_FO_DELTA_G];
+    double vpot_g_1 = fo1[SONG2_FO_V_G], vpot_g_2 = fo2[SONG2_FO_V_G];
+    double delta_b_1 = fo1[SONG2_FO_DELTA_B], delta_b_2 = fo2[SONG2_FO_DELTA_B];
+    double vpot_b_1 = fo1[SONG2_FO_V_B], vpot_b_2 = fo2[SONG2_FO_V_B];
+    double delta_cdm_1 = fo1[SONG2_FO_DELTA_CDM], delta_cdm_2 = fo2[SONG2_FO_DELTA_CDM];
+    double vpot_cdm_1 = fo1[SONG2_FO_V_CDM], vpot_cdm_2 = fo2[SONG2_FO_V_CDM];
+    double delta_ur_1 = fo1[SONG2_FO_DELTA_UR], delta_ur_2 = fo2[SONG2_FO_DELTA_UR];
+    double vpot_ur_1 = fo1[SONG2_FO_V_UR], vpot_ur_2 = fo2[SONG2_FO_V_UR];
+    double phi_1 = fo1[SONG2_FO_PHI], phi_2 = fo2[SONG2_FO_PHI], psi_1 = fo1[SONG2_FO_PSI], psi_2 = fo2[SONG2_FO_PSI];
+    double zeta = 2 * (3 / 5. * s.fnl);
+    double A_quad = qs[s.iq_psi];
+    double I_2_0_quad = 5 / 8. * (c.S(CM12, 2, 0) * c.I1r(1) * c.I2r(1) + c.S(CM21, 2, 0) * c.I2r(1) * c.I1r(1));
+    double N_2_0_quad = 1 / 3. * (k / Hc_sq) * qs[s.iq_ur + c.LM(1, 0)] + 1 / (2 * Hc) * qs[s.iq_ur + c.LM(2, 0)] +
+                        8 / 3. * (k_sq / Hc_sq) * psi_1 * psi_2;
+    double quadrupole_quad = (frac_g * I_2_0_quad + frac_ur * N_2_0_quad) * 3 / 5. * (Hc_sq / k_sq);
+    double B_quad = A_quad - quadrupole_quad;
+    double frac_g_factor = 1 + 4 / 15. * (1 - frac_g);
+    double psi = 1. / frac_g_factor * 2 / 3. * (-zeta + psi_1 * psi_2 - 2 * phi_1 * phi_2 + B_quad);
+    double I_2_0 = I_2_0_quad;
+    double N_2_0 = 2 / 3. * (k_sq / Hc_sq) * psi + N_2_0_quad;
+    double phi = (1 + 2 / 5. * frac_ur) * psi - B_quad;
+    double L_quad = qs[s.iq_phi_prime_longitudinal];
+    double u0 = 2 * (k / Hc) * (psi - L_quad / Hc) - (-k1_0 * vpot_cdm_1) * (3 * Omega_m * delta_cdm_2 + 4 * Omega_r * delta_g_2) -
+                (-k2_0 * vpot_cdm_2) * (3 * Omega_m * delta_cdm_1 + 4 * Omega_r * delta_g_1);
+    u0 *= 1 / (3 * Omega_m + 4 * Omega_r);
+    double I_1_0 = 4 * (u0 + delta_g_1 * (-k2_0 * vpot_g_2) + delta_g_2 * (-k1_0 * vpot_g_1));
+    double N_1_0 = 4 * (u0 + delta_ur_1 * (-k2_0 * vpot_ur_2) + delta_ur_2 * (-k1_0 * vpot_ur_1));
+    double b_1_1_0 = 3 * (u0 + delta_b_1 * (-k2_0 * vpot_b_2) + delta_b_2 * (-k1_0 * vpot_b_1));
+    double cdm_1_1_0 = 3 * (u0 + delta_cdm_1 * (-k2_0 * vpot_cdm_2) + delta_cdm_2 * (-k1_0 * vpot_cdm_1));
+    double I_0_0 = -2 * psi + 8 * psi_1 * psi_2;
+    double b_0_0_0 = 3 * (I_0_0 / 4 - delta_g_1 * delta_g_2 / 16);
+    y[s.idx_phi] = phi;
+    y[c.p.idx_I[c.LM(0, 0)]] = I_0_0;
+    if (!tca) {
+      y[c.p.idx_I[c.LM(1, 0)]] = I_1_0;
+      y[c.p.idx_I[c.LM(2, 0)]] = I_2_0;
+    }
+    y[s.idx_b000] = b_0_0_0;
+    y[s.idx_b11[0]] = b_1_1_0;
+    y[s.idx_c000] = b_0_0_0;
+    y[s.idx_c11[0]] = cdm_1_1_0;
+    y[c.p.idx_N[c.LM(0, 0)]] = I_0_0;
+    y[c.p.idx_N[c.LM(1, 0)]] = N_1_0;
+    y[c.p.idx_N[c.LM(2, 0)]] = N_2_0;
+    double rho_monopole = bg.rho_g * I_0_0 + bg.rho_b * b_0_0_0 + bg.rho_cdm * b_0_0_0 + bg.rho_ur * I_0_0;
+    y[s.idx_phip] = -Hc * psi - k_sq / (3 * Hc) * phi - a_sq * rho_monopole / (2 * Hc) + qs[s.iq_phi_prime_poisson];
+  } else if (s.ic == SONG2_IC_AD_FIRST_ORDER) {
+    double C = 0.5 * (2 * (-(3 / 5. * s.fnl)));
+    double psi = 20 * C / (15 + 4 * frac_ur);
+    y[s.idx_phi] = (1 + 2 / 5. * frac_ur) * psi;
+    double u0 = 0.5 * k * tau * psi;
+    double I_0_0 = -2 * psi;
+    y[c.p.idx_I[c.LM(0, 0)]] = I_0_0;
+    if (!tca) y[c.p.idx_I[c.LM(1, 0)]] = 4 * u0;
+    y[s.idx_b000] = 0.75 * I_0_0;
+    y[s.idx_b11[0]] = 3 * u0;
+    y[s.idx_c000] = 0.75 * I_0_0;
+    y[s.idx_c11[0]] = 3 * u0;
+    y[c.p.idx_N[c.LM(0, 0)]] = I_0_0;
+    y[c.p.idx_N[c.LM(1, 0)]] = 4 * u0;
+    /* I_20 = 10 shear, consistent with the second-order initial conditions */
+    y[c.p.idx_N[c.LM(2, 0)]] = 10 * (1 / 15. * k * k * tau * tau * psi);
+    y[s.idx_phip] = 0.0;
+  }
+}
+
+/* ------------------------------------------------------------------ NDF15 */
+
+__constant__ double c_G[5] = {1.0, 1.5, 11.0 / 6.0, 25.0 / 12.0, 137.0 / 60.0};
+__constant__ double c_alpha[5] = {-0.1850, -1.0 / 9.0, -0.0823, -0.0415, 0.0};
+
+/* dif[:,0..k-1] <- dif * (R(r) U): every thread handles its own components */
+__device__ void rescale_dif(const K &c, int k, double r) {
+  double RU[5][5];
+  {
+    double Rm[5][5], U[5][5];
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < k; ++j) {
+        double prod = 1.0;
+        for (int p = 1; p <= i + 1; ++p) prod *= ((p - 1) - (j + 1) * r) / p;
+        Rm[i][j] = prod;
+        double binom = 0.0;
+        if (j >= i) {
+          binom = 1.0;
+          for (int p = 1; p <= i + 1; ++p) binom = binom * (j + 1 - (i + 1) + p) / p;
+        }
+        U[i][j] = ((i + 1) % 2 ? -binom : binom);
+      }
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < k; ++j) {
+        double sm = 0;
+        for (int p = 0; p < k; ++p) sm += Rm[i][p] * U[p][j];
+        RU[i][j] = sm;
+      }
+  }
+  int n = c.s.n;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    double tmp[5];
+    for (int j = 0; j < k; ++j) {
+      double sm = 0;
+      for (int i = 0; i < k; ++i) sm += c.dif[(size_t)i * n + e] * RU[i][j];
+      tmp[j] = sm;
+    }
+    for (int j = 0; j < k; ++j) c.dif[(size_t)j * n + e] = tmp[j];
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ int refactor(const K &c, double hinvGak, song2_triplet_stats &st) {
+  if (threadIdx.x == 0) c.sh->lu_fail = 0;
+  __syncthreads();
+  form_and_factor<T>(c, hinvGak);
+  st.n_lu++;
+  return c.sh->lu_fail ? SONG2_E_SINGULAR : SONG2_OK;
+}
+
+/* output of one sampling time: y interpolated in c.yout */
+__device__ void do_output(const K &c, int jout, double to) {
+  prepare(c, to, 1);
+  rhs(c, c.sh->tca, to, c.yout, c.dyout);
+  if (c.s.mode_first_order) store_first_order(c, jout, c.yout, c.dyout);
+  else store_sources(c, jout, to, c.yout, c.dyout);
+  __syncthreads();
+}
+
+__device__ inline double tout_at(const K &c, int j) {
+  return c.s.mode_first_order ? exp(c.s.fo_lntau0 + j * c.s.fo_dlntau) : c.p.tau[j];
+}
+
+template <typename T>
+__device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0, song2_triplet_stats &st) {
+  const DevSpec &s = c.s;
+  int n = s.n, tid = threadIdx.x, nt = blockDim.x;
+  int nout = s.mode_first_order ? s.fo_tau_size : s.tau_size;
+  int tca = c.sh->tca;
+  double rtol = s.rtol, threshold = s.threshold;
+  const double eps = 2.220446049250313e-16;
+  const int maxk = 5, maxit = 4;
+  double invGa[5], erconst[5];
+  for (int i = 0; i < 5; ++i) {
+    invGa[i] = 1.0 / (c_G[i] * (1.0 - c_alpha[i]));
+    erconst[i] = c_alpha[i] * c_G[i] + 1.0 / (i + 2);
+  }
+  double *y = c.y, *f = c.f, *ynew = c.ynew, *difkp1 = c.difkp1, *psiv = c.psiv, *del = c.del, *invwt = c.invwt;
+  double *dif = c.dif;
+  double t = t0, hmax = 0.1 * fabs(t1 - t0);
+  if (include_t0)
+    while (jout < nout && tout_at(c, jout) <= t0) {
+      if (tout_at(c, jout) == t0) {
+        for (int i = tid; i < n; i += nt) c.yout[i] = y[i];
+        __syncthreads();
+        do_output(c, jout, t0);
+      }
+      ++jout;
+    }
+  prepare(c, t, 1);
+  rhs(c, tca, t, y, f);
+  st.n_rhs++;
+  jacobian(c, tca, t);
+  st.n_jac++;
+  int Jcurrent = 1;
+  double hmin = 16 * eps * fabs(t);
+  double absh = fmin(hmax, fabs(t1 - t0));
+  double v = 0;
+  for (int i = tid; i < n; i += nt) v = fmax(v, fabs(f[i]) / fmax(fabs(y[i]), threshold));
+  double rh = 1.25 * block_max(c, v) / sqrt(rtol);
+  if (absh * rh > 1) absh = 1.0 / rh;
+  absh = fmax(absh, hmin);
+  double h = absh;
+  int k = 1;
+  for (int e = tid; e < 7 * n; e += nt) dif[e] = 0.0;
+  __syncthreads();
+  for (int i = tid; i < n; i += nt) dif[i] = h * f[i];
+  double hinvGak = h * invGa[k - 1];
+  int nconhk = 0;
+  if (refactor<T>(c, hinvGak, st)) return SONG2_E_SINGULAR;
+  int havrate = 0;
+  double rate = 0, abshlast = absh;
+  int klast = k, done = 0, attempts = 0;
+  while (!done) {
+    hmin = 16 * eps * fabs(t);
+    absh = fmin(hmax, fmax(hmin, absh));
+    h = absh;
+    if (1.1 * absh >= fabs(t1 - t)) {
+      h = t1 - t;
+      absh = fabs(h);
+      done = 1;
+    }
+    if (absh != abshlast || k != klast) {
+      rescale_dif(c, k, absh / abshlast);
+      hinvGak = h * invGa[k - 1];
+      nconhk = 0;
+      if (refactor<T>(c, hinvGak, st)) return SONG2_E_SINGULAR;
+      havrate = 0;
+    }
+    int nofailed = 1;
+    double err = 0, tnew = t;
+    for (;;) {
+      int gotynew = 0;
+      while (!gotynew) {
+        if (++attempts > s.max_steps) return SONG2_E_MAXSTEPS;
+        for (int i = tid; i < n; i += nt) {
+          double ps = 0, pr = y[i];
+          for (int j = 0; j < k; ++j) {
+            double dj = dif[(size_t)j * n + i];
+            ps += dj * c_G[j];
+            pr += dj;
+          }
+          psiv[i] = ps * invGa[k - 1];
+          ynew[i] = pr;
+          difkp1[i] = 0.0;
+        }
+        tnew = t + h;
+        if (done) tnew = t1;
+        h = tnew - t;
+        double vm = 0;
+        for (int i = tid; i < n; i += nt) {
+          invwt[i] = 1.0 / fmax(fmax(fabs(y[i]), fabs(ynew[i])), threshold);
+          vm = fmax(vm, fabs(ynew[i] * invwt[i]));
+        }
+        double minnrm = 100 * eps * block_max(c, vm);
+        double oldnrm = 0;
+        prepare(c, tnew, 1);
+        for (int iter = 1; iter <= maxit; ++iter) {
+          rhs(c, tca, tnew, ynew, f);
+          st.n_rhs++;
+          for (int i = tid; i < n; i += nt) del[i] = hinvGak * f[i] - (psiv[i] + difkp1[i]);
+          __syncthreads();
+          lu_solve<T>(c);
+          double vn = 0;
+          for (int i = tid; i < n; i += nt) {
+            vn = fmax(vn, fabs(del[i] * invwt[i]));
+            difkp1[i] += del[i];
+            ynew[i] += del[i];
+          }
+          double newnrm = block_max(c, vn);
+          if (!(newnrm < INFINITY)) break;
+          if (newnrm <= minnrm) { gotynew = 1; break; }
+          else if (iter == 1) {
+            if (havrate) {
+              double errit = newnrm * rate / (1 - rate);
+              if (errit <= 0.05 * rtol) { gotynew = 1; break; }
+            } else rate = 0;
+          } else if (newnrm > 0.9 * oldnrm) break;
+          else {
+            rate = fmax(0.9 * rate, newnrm / oldnrm);
+            havrate = 1;
+            double errit = newnrm * rate / (1 - rate);
+            if (errit <= 0.5 * rtol) { gotynew = 1; break; }
+            else if (iter == maxit) break;
+            else if (0.5 * rtol < errit * pow(rate, (double)(maxit - iter))) break;
+          }
+          oldnrm = newnrm;
+        }
+        if (!gotynew) {
+          st.n_newton_fail++;
+          if (absh <= hmin) return SONG2_E_NEWTON;
+          if (Jcurrent) {
+            double abshold = absh;
+            absh = fmax(0.3 * absh, hmin);
+            h = absh;
+            done = 0;
+            rescale_dif(c, k, absh / abshold);
+            abshlast = absh;
+            hinvGak = h * invGa[k - 1];
+            nconhk = 0;
+          } else {
+            prepare(c, t, 0);
+            jacobian(c, tca, t);
+            st.n_jac++;
+            Jcurrent = 1;
+          }
+          if (refactor<T>(c, hinvGak, st)) return SONG2_E_SINGULAR;
+          havrate = 0;
+        }
+      }
+      double ve = 0, vfin = 0;
+      for (int i = tid; i < n; i += nt) {
+        ve = fmax(ve, fabs(difkp1[i] * invwt[i]));
+        vfin = fmax(vfin, fabs(ynew[i]));
+      }
+      err = block_max(c, ve) * erconst[k - 1];
+      double ymax = block_max(c, vfin);
+      if (!(ymax < 1e300)) return SONG2_E_NAN;
+      if (err > rtol) {
+        st.n_rejected++;
+        if (absh <= hmin) return SONG2_E_HMIN;
+        double abshl = absh;
+        if (nofailed) {
+          nofailed = 0;
+          double hopt = absh * fmax(0.1, 0.833 * pow(rtol / err, 1.0 / (k + 1)));
+          if (k > 1) {
+            double vk = 0;
+            for (int i = tid; i < n; i += nt) vk = fmax(vk, fabs((dif[(size_t)(k - 1) * n + i] + difkp1[i]) * invwt[i]));
+            double errkm1 = block_max(c, vk) * erconst[k - 2];
+            double hkm1 = absh * fmax(0.1, 0.769 * pow(rtol / errkm1, 1.0 / k));
+            if (hkm1 > hopt) {
+              hopt = fmin(absh, hkm1);
+              k = k - 1;
+            }
+          }
+          absh = fmax(hmin, hopt);
+        } else {
+          absh = fmax(hmin, 0.5 * absh);
+        }
+        h = absh;
+        if (absh < abshl) done = 0;
+        rescale_dif(c, k, absh / abshl);
+        abshlast = absh;
+        klast = k;
+        hinvGak = h * invGa[k - 1];
+        nconhk = 0;
+        if (refactor<T>(c, hinvGak, st)) return SONG2_E_SINGULAR;
+        havrate = 0;
+      } else
+        break;
+    }
+    /* accepted step */
+    st.n_steps++;
+    for (int i = tid; i < n; i += nt) {
+      double dk = dif[(size_t)k * n + i];
+      dif[(size_t)(k + 1) * n + i] = difkp1[i] - dk;
+      dif[(size_t)k * n + i] = difkp1[i];
+      for (int j = k - 1; j >= 0; --j) dif[(size_t)j * n + i] += dif[(size_t)(j + 1) * n + i];
+    }
+    __syncthreads();
+    while (jout < nout && tout_at(c, jout) <= tnew) {
+      double to = tout_at(c, jout);
+      if (to > t || (include_t0 && to == t)) {
+        double sv = (to - tnew) / h;
+        for (int i = tid; i < n; i += nt) {
+          double acc = ynew[i], term = 1.0;
+          if (to != tnew)
+            for (int j = 0; j < k; ++j) {
+              term *= (sv + j) / (j + 1);
+              acc += dif[(size_t)j * n + i] * term;
+            }
+          c.yout[i] = acc;
+        }
+        __syncthreads();
+        do_output(c, jout, to);
+        st.sources_calls++;
+      }
+      ++jout;
+    }
+    klast = k;
+    abshlast = absh;
+    nconhk = (nconhk + 1 < maxk + 2) ? nconhk + 1 : maxk + 2;
+    if (nconhk >= k + 2) {
+      double temp = 1.2 * pow(err / rtol, 1.0 / (k + 1));
+      double hopt = (temp > 0.1) ? absh / temp : 10 * absh;
+      int kopt = k;
+      double vk = 0, vp = 0;
+      for (int i = tid; i < n; i += nt) {
+        if (k > 1) vk = fmax(vk, fabs(dif[(size_t)(k - 1) * n + i] * invwt[i]));
+        if (k < maxk) vp = fmax(vp, fabs(dif[(size_t)(k + 1) * n + i] * invwt[i]));
+      }
+      double errkm1 = block_max(c, vk), errkp1 = block_max(c, vp);
+      if (k > 1) {
+        errkm1 *= erconst[k - 2];
+        temp = 1.3 * pow(errkm1 / rtol, 1.0 / k);
+        double hkm1 = (temp > 0.1) ? absh / temp : 10 * absh;
+        if (hkm1 > hopt) { hopt = hkm1; kopt = k - 1; }
+      }
+      if (k < maxk) {
+        errkp1 *= erconst[k];
+        temp = 1.4 * pow(errkp1 / rtol, 1.0 / (k + 2));
+        double hkp1 = (temp > 0.1) ? absh / temp : 10 * absh;
+        if (hkp1 > hopt) { hopt = hkp1; kopt = k + 1; }
+      }
+      if (hopt > absh) {
+        absh = hopt;
+        if (k != kopt) k = kopt;
+      }
+    }
+    t = tnew;
+    for (int i = tid; i < n; i += nt) y[i] = ynew[i];
+    __syncthreads();
+    Jcurrent = 0;
+  }
+  return SONG2_OK;
+}
+
+/* ------------------------------------------------------------------ one triplet */
+
+template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_stats &st) {
+  const DevSpec &s = c.s;
+  int tid = threadIdx.x;
+  if (geometry(c)) return SONG2_E_CONFIG;
+  if (tid == 0) c.sh->lu_fail = intervals(c);
+  __syncthreads();
+  if (c.sh->lu_fail) return SONG2_E_CONFIG;
+  Tri &t = c.sh->tri;
+  int jout = 0;
+  for (int iv = 0; iv < t.nint; ++iv) {
+    double ta = iv == 0 ? t.tau_ini : t.tau_switch;
+    double tb = (iv == 0 && t.nint == 2) ? t.tau_switch : t.tau_end;
+    if (iv == 0) {
+      if (tid == 0) c.sh->tca = t.tca0;
+      __syncthreads();
+      prepare(c, ta, 1);
+      if (tid == 0) initial_conditions(c, ta);
+      __syncthreads();
+    } else {
+      /* TCA -> full remap (perturbations2.c:7233-7285): the frozen moments take the
+         TCA values at the switching time; everything else carries over */
+      prepare(c, ta, 1);
+      if (tid == 0) {
+        YVec yv{c.y};
+        compute_ws(c, 1, yv, 0, c.sh->ws);
+        WS &w = c.sh->ws;
+        for (int im = 0; im <= s.index_m_max[1]; ++im) c.y[c.p.idx_I[c.LM(1, s.m[im])]] = w.I_1m_tca1[s.m[im]];
+        for (int im = 0; im <= s.index_m_max[2]; ++im) {
+          int m = s.m[im];
+          c.y[c.p.idx_I[c.LM(2, m)]] = w.I_2m_tca1[m];
+          if (s.has_pol) {
+            c.y[c.p.idx_E[c.LM(2, m)]] = w.E_2m_tca1[m];
+            if (m != 0) c.y[c.p.idx_B[c.LM(2, m)]] = w.B_2m_tca1[m];
+          }
+        }
+        c.sh->tca = 0;
+      }
+      __syncthreads();
+    }
+    int stc = ndf15<T>(c, ta, tb, jout, iv == 0, st);
+    if (stc != SONG2_OK) return stc;
+  }
+  int nout = s.mode_first_order ? s.fo_tau_size : s.tau_size;
+  if (st.sources_calls != nout) return SONG2_E_CONFIG;
+  return SONG2_OK;
+}
+
+template <typename T> __global__ void __launch_bounds__(256) evolver_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
+  extern __shared__ __align__(16) char smem[];
+  K c(s, p, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64);
+  for (int guard = 0; guard < s.n_items + 1; ++guard) {
+    if (threadIdx.x == 0) c.sh->item = atomicAdd(p.queue, 1);
+    __syncthreads();
+    int item = c.sh->item;
+    if (item >= s.n_items) break;
+    WorkItem wi = p.items[item];
+    if (threadIdx.x == 0) {
+      Tri &t = c.sh->tri;
+      t.i1 = wi.i1; t.i2 = wi.i2; t.i3 = wi.i3; t.pair = wi.pair; t.item = item;
+      t.k1 = p.k[wi.i1];
+      t.k2 = p.k[wi.i2];
+      t.k3_size = p.k3_size[wi.pair];
+      t.k = p.k3[p.k3_off[wi.pair] + wi.i3];
+      t.pair_off = p.pair_off[wi.pair];
+    }
+    __syncthreads();
+    song2_triplet_stats st;
+    st.status = 0; st.n_steps = 0; st.n_rejected = 0; st.n_rhs = 0; st.n_jac = 0; st.n_lu = 0; st.n_newton_fail = 0;
+    st.sources_calls = 0;
+    int stc = solve_triplet<T>(c, st);
+    st.status = stc;
+    if (threadIdx.x == 0) p.stats[item] = st;
+    __syncthreads();
+  }
+}
+
+} // namespace
+
+size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in_smem) {
+  (void)block;
+  return make_plan(spec, precision, lu_in_smem).total;
+}
+
+int song2_max_ctas_per_sm(int precision, int block, size_t smem) {
+  int nb = 0;
+  cudaError_t e;
+  if (precision == SONG2_PREC_MIXED) {
+    cudaFuncSetAttribute(evolver_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, evolver_kernel<float>, block, smem);
+  } else {
+    cudaFuncSetAttribute(evolver_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, evolver_kernel<double>, block, smem);
+  }
+  return e == cudaSuccess ? nb : 0;
+}
+
+int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int grid, int block, size_t smem,
+                         cudaStream_t stream) {
+  if (precision == SONG2_PREC_MIXED) {
+    cudaFuncSetAttribute(evolver_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    evolver_kernel<float><<<grid, block, smem, stream>>>(spec, ptrs);
+  } else {
+    cudaFuncSetAttribute(evolver_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    evolver_kernel<double><<<grid, block, smem, stream>>>(spec, ptrs);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
