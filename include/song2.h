@@ -198,12 +198,24 @@ int song2_tau_grid(int log_sampling, double tau_ini, double tau_end, int tau_siz
 int song2_start_time(const song2_spec *spec, const song2_tables *tab, double k,
                      double tau_upper, double *tau_ini, char *err);
 
+/* Sharding over ranks (one GPU per rank, triplets are independent: no data
+   exchange).  Triplets are ordered by decreasing cost estimate max(k1,k2,k3)
+   and dealt round-robin, so every shard gets a similar mix.  Writes the
+   reference work-order indices of shard `shard` (k1 descending, k2 <= k1, k3)
+   into out (may be NULL) and returns their number.  Replaces nothing in the
+   reference, whose OpenMP loop shares one node (perturbations2.c:291-333). */
+int64_t song2_shard_items(const song2_spec *spec, int shard, int n_shards, int64_t *out);
+
 /* ---------------------------------------------------------------- GPU side */
 
 /* Create a context on the current CUDA device: uploads the spec grids and the
    tables once to a device arena (cudaMemcpyAsync).  Not thread safe per ctx. */
 int song2_ctx_create(const song2_spec *spec, const song2_tables *tab,
                      int precision, song2_ctx **out, char *err);
+/* Same, restricted to the triplets of song2_shard_items(spec, shard, n_shards);
+   the flat source buffer keeps the full layout, entries of other shards stay 0. */
+int song2_ctx_create_shard(const song2_spec *spec, const song2_tables *tab, int precision,
+                           int shard, int n_shards, song2_ctx **out, char *err);
 int song2_ctx_destroy(song2_ctx *ctx);
 
 /* Evolve every triplet on the device and leave the sources in device memory.

@@ -33,6 +33,10 @@ def load():
         lib.song2_oracle_evolve_range.argtypes = [C.POINTER(capi.Spec), C.POINTER(capi.Tables),
                                                   C.POINTER(C.c_double), C.POINTER(capi.TripletStats),
                                                   C.c_int64, C.c_int64, C.c_int, C.c_char_p]
+        lib.song2_oracle_evolve_list.restype = C.c_int
+        lib.song2_oracle_evolve_list.argtypes = [C.POINTER(capi.Spec), C.POINTER(capi.Tables),
+                                                 C.POINTER(C.c_double), C.POINTER(capi.TripletStats),
+                                                 C.POINTER(C.c_int64), C.c_int64, C.c_int, C.c_char_p]
         lib.song2_oracle_first_order.restype = C.c_int
         lib.song2_oracle_first_order.argtypes = [C.POINTER(capi.Spec), C.POINTER(capi.Tables), C.c_int, C.c_int,
                                                  C.c_double, C.c_double, C.POINTER(C.c_double), C.c_int,
@@ -63,7 +67,7 @@ def first_order(prob, nthreads=0):
     return fo
 
 
-def evolve(prob, nthreads=0, first=None, count=None, rtol=None):
+def evolve(prob, nthreads=0, first=None, count=None, rtol=None, items=None):
     """Flat sources [tp2][per_type] and per-triplet stats (work order)."""
     from song_gb300 import capi
     lib = load()
@@ -74,7 +78,11 @@ def evolve(prob, nthreads=0, first=None, count=None, rtol=None):
     n = prob.n_triplets
     stats = (capi.TripletStats * n)()
     err = capi.errbuf()
-    if first is None:
+    if items is not None:
+        items = np.ascontiguousarray(items, dtype=np.int64)
+        rc = lib.song2_oracle_evolve_list(C.byref(spec), C.byref(prob.tables), capi.dptr(src), stats,
+                                          items.ctypes.data_as(C.POINTER(C.c_int64)), len(items), nthreads, err)
+    elif first is None:
         rc = lib.song2_oracle_evolve(C.byref(spec), C.byref(prob.tables), capi.dptr(src), stats, nthreads, err)
     else:
         rc = lib.song2_oracle_evolve_range(C.byref(spec), C.byref(prob.tables), capi.dptr(src), stats, first,

@@ -33,6 +33,11 @@ int song2_oracle_evolve_range(const song2_spec *spec, const song2_tables *tab, d
                               song2_triplet_stats *stats, int64_t first, int64_t count,
                               int nthreads, char *err);
 
+/* Same, for an explicit list of work-order indices (one rank's shard). */
+int song2_oracle_evolve_list(const song2_spec *spec, const song2_tables *tab, double *sources_flat,
+                             song2_triplet_stats *stats, const int64_t *items, int64_t count, int nthreads,
+                             char *err);
+
 /* First-order mode (SONG with quadratic sources off and has_ad_first_order
    initial conditions, perturbations2.c:4096-4185) for every k of spec->k:
    fills fo_out[k][tau][q] on a uniform ln(tau) grid. */

@@ -117,7 +117,9 @@ SIGNATURES = {
     "song2_k3_grids": (_I, [_PD, _I, _I, _I, _PI, _PD, C.c_char_p]),
     "song2_tau_grid": (_I, [_I, _D, _D, _I, _PD]),
     "song2_start_time": (_I, [C.POINTER(Spec), C.POINTER(Tables), _D, _D, _PD, C.c_char_p]),
+    "song2_shard_items": (C.c_int64, [C.POINTER(Spec), _I, _I, C.POINTER(C.c_int64)]),
     "song2_ctx_create": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.POINTER(_P), C.c_char_p]),
+    "song2_ctx_create_shard": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _I, C.POINTER(_P), C.c_char_p]),
     "song2_ctx_destroy": (_I, [_P]),
     "song2_ctx_run": (_I, [_P, _P, C.c_char_p]),
     "song2_ctx_device_sources": (_P, [_P]),

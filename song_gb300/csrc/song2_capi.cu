@@ -344,6 +344,10 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
 
   int dev = 0, nsm = 0, smem_optin = 0;
   CK(cudaGetDevice(&dev));
+  /* the evolver keeps its per-thread workspace copy (Jacobian probes) on the stack */
+  size_t stack = 0;
+  CK(cudaDeviceGetLimit(&stack, cudaLimitStackSize));
+  if (stack < 4096) CK(cudaDeviceSetLimit(cudaLimitStackSize, 4096));
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   c->block = 256;
@@ -452,10 +456,67 @@ void pair_tables(const song2_spec *sp, std::vector<int> &k3_off, std::vector<int
 
 } // namespace
 
+/* cost-sorted work list: (reference work-order index, item) */
+static void sorted_items(const song2_spec *spec, const std::vector<double> &k3, const std::vector<int> &k3_off,
+                         const std::vector<int> &k3_size, std::vector<WorkItem> &sorted, std::vector<int64_t> &ref_index) {
+  std::vector<WorkItem> items;
+  std::vector<double> cost;
+  int pair = 0;
+  for (int i1 = 0; i1 < spec->k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2, ++pair)
+      for (int i3 = 0; i3 < k3_size[pair]; ++i3) {
+        items.push_back(WorkItem{i1, i2, i3, pair});
+        double kk = std::max(spec->k[i1], std::max(spec->k[i2], k3[k3_off[pair] + i3]));
+        cost.push_back(kk);
+      }
+  /* reference order start of every pair */
+  int npairs = pair;
+  std::vector<int64_t> start(npairs, 0);
+  int64_t acc = 0;
+  for (int i1 = spec->k_size - 1; i1 >= 0; --i1)
+    for (int i2 = 0; i2 <= i1; ++i2) {
+      int pr = i1 * (i1 + 1) / 2 + i2;
+      start[pr] = acc;
+      acc += k3_size[pr];
+    }
+  std::vector<size_t> order(items.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+  sorted.resize(items.size());
+  ref_index.resize(items.size());
+  for (size_t i = 0; i < order.size(); ++i) {
+    sorted[i] = items[order[i]];
+    ref_index[i] = start[sorted[i].pair] + sorted[i].i3;
+  }
+}
+
 extern "C" {
 
-int song2_ctx_create(const song2_spec *spec, const song2_tables *tab, int precision, song2_ctx **out, char *err) {
+int64_t song2_shard_items(const song2_spec *spec, int shard, int n_shards, int64_t *out) {
+  if (n_shards < 1 || shard < 0 || shard >= n_shards) return -1;
+  std::vector<int> k3_off, k3_size;
+  std::vector<int64_t> pair_off;
+  pair_tables(spec, k3_off, k3_size, pair_off);
+  int n3tot = k3_off.empty() ? 0 : k3_off.back() + k3_size.back();
+  std::vector<double> k3(spec->k3, spec->k3 + n3tot);
+  std::vector<WorkItem> sorted;
+  std::vector<int64_t> ref;
+  sorted_items(spec, k3, k3_off, k3_size, sorted, ref);
+  int64_t n = 0;
+  for (size_t i = shard; i < sorted.size(); i += n_shards) {
+    if (out) out[n] = ref[i];
+    ++n;
+  }
+  return n;
+}
+
+static int ctx_create_impl(const song2_spec *spec, const song2_tables *tab, int precision, int shard, int n_shards,
+                           song2_ctx **out, char *err) {
   *out = nullptr;
+  if (n_shards < 1 || shard < 0 || shard >= n_shards) {
+    snprintf(err, SONG2_ERRLEN, "bad shard %d of %d", shard, n_shards);
+    return 1;
+  }
   if (precision != SONG2_PREC_FP64 && precision != SONG2_PREC_MIXED) {
     snprintf(err, SONG2_ERRLEN, "unknown precision %d", precision);
     return 1;
@@ -467,30 +528,27 @@ int song2_ctx_create(const song2_spec *spec, const song2_tables *tab, int precis
   std::vector<double> k3(spec->k3, spec->k3 + n3tot);
   /* work items, largest wavenumber first: the expensive triplets start early so the
      persistent CTAs finish together (longest-processing-time order) */
-  std::vector<WorkItem> items;
-  std::vector<double> cost;
-  int pair = 0;
-  for (int i1 = 0; i1 < spec->k_size; ++i1)
-    for (int i2 = 0; i2 <= i1; ++i2, ++pair)
-      for (int i3 = 0; i3 < k3_size[pair]; ++i3) {
-        items.push_back(WorkItem{i1, i2, i3, pair});
-        double kk = std::max(spec->k[i1], std::max(spec->k[i2], k3[k3_off[pair] + i3]));
-        cost.push_back(kk);
-      }
-  std::vector<size_t> order(items.size());
-  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
-  std::vector<WorkItem> sorted(items.size());
-  for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
+  std::vector<WorkItem> sorted, mine;
+  std::vector<int64_t> ref;
+  sorted_items(spec, k3, k3_off, k3_size, sorted, ref);
+  for (size_t i = shard; i < sorted.size(); i += n_shards) mine.push_back(sorted[i]);
   song2_ctx *c = new song2_ctx();
   memset((void *)&c->spec, 0, sizeof(c->spec));
-  if (ctx_setup(c, spec, tab, precision, 0, sorted, k3, k3_off, k3_size, pair_off, 0, 0, 0, 0, err)) {
+  if (ctx_setup(c, spec, tab, precision, 0, mine, k3, k3_off, k3_size, pair_off, 0, 0, 0, 0, err)) {
     song2_ctx_destroy(c);
     return 1;
   }
-  /* map of the sorted work order back to the natural order for the stats */
   *out = c;
   return 0;
+}
+
+int song2_ctx_create(const song2_spec *spec, const song2_tables *tab, int precision, song2_ctx **out, char *err) {
+  return ctx_create_impl(spec, tab, precision, 0, 1, out, err);
+}
+
+int song2_ctx_create_shard(const song2_spec *spec, const song2_tables *tab, int precision, int shard, int n_shards,
+                           song2_ctx **out, char *err) {
+  return ctx_create_impl(spec, tab, precision, shard, n_shards, out, err);
 }
 
 int song2_ctx_destroy(song2_ctx *c) {

@@ -63,6 +63,8 @@ struct Shared {
   WS ws;
   double psi_prime;
   double red[32];
+  double RU[5][5];
+  double ctl[4];
   int item;
   int lu_fail;
   int tca;
@@ -505,9 +507,9 @@ __device__ void prepare(const K &c, double tau, int with_sources) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   int tid = threadIdx.x, nt = blockDim.x;
-  double x = log(tau);
   if (tid < SONG2_BG_SIZE) c.bgraw[tid] = bg_col(c, tid, tau);
   int use_fo = with_sources && s.has_qs && !s.mode_first_order;
+  double x = (use_fo && tid < 2 * s.nfo) ? log(tau) : 0.0;
   for (int q = tid; q < 2 * s.nfo; q += nt) {
     int which = q >= s.nfo, qq = which ? q - s.nfo : q;
     double v = 0.0;
@@ -519,16 +521,17 @@ __device__ void prepare(const K &c, double tau, int with_sources) {
     (which ? c.fo2 : c.fo1)[qq] = v;
   }
   __syncthreads();
-  BgV bg;
-  bg_derive(c.bgraw, tau, bg);
-  if (tid == 0) c.sh->bg = bg;
+  /* FP64 transcendental work is done once, not once per thread */
+  if (tid == 0) bg_derive(c.bgraw, tau, c.sh->bg);
   for (int q = tid; q < s.qs2_size; q += nt) {
     c.qs[q] = 0.0;
     c.qc[q] = 0.0;
   }
   __syncthreads();
-  if (use_fo)
+  if (use_fo) {
+    const BgV &bg = c.sh->bg;
     for (int q = tid; q < s.qs2_size; q += nt) qs_entry(c, bg, q);
+  }
   __syncthreads();
 }
 
@@ -678,8 +681,9 @@ template <class Y> __device__ void compute_ws(const K &c, int tca, const Y &y, i
 
 /* ------------------------------------------------------------------ derivs rows */
 
+/* every row except phi' (which needs two other rows, see row() below) */
 template <class Y>
-__device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
+__device__ double row_h(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
@@ -787,12 +791,33 @@ __device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int l
     return d;
   case SP_PHI:
     return w.phi_prime;
-  case SP_PHIP: {
+  case SP_OMEGA:
+    return omp;
+  case SP_GAMMA:
+    return gp;
+  case SP_GAMMAP:
+    return w.gamma_m2_pp;
+  }
+  return 0.0;
+}
+
+
+/* Row i of dy = f(tau, y).  The phi' row is phi'' = (Einstein part) - Hc psi',
+   where psi' (perturb2_compute_psi_prime, perturbations2.c:10188-10383) needs the
+   I_20 and N_20 rows. */
+template <class Y>
+__device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
+  const DevSpec &s = c.s;
+  if (__ldg(c.p.eq_sp + i) != SP_PHIP) return row_h(c, tca, i, y, w, lin, tau);
+  const Tri &t = c.sh->tri;
+  const BgV &bg = c.sh->bg;
+  double k = t.k, kd = bg.kappa_dot, Hc = bg.Hc;
+  int use_qs = !lin && s.has_qs;
     /* phi'' = (einstein part) - Hc psi' (perturb2_compute_psi_prime, perturbations2.c:10188-10383) */
     double dI20;
-    if (!tca) dI20 = row(c, tca, c.p.idx_I[c.LM(2, 0)], y, w, lin, tau);
+    if (!tca) dI20 = row_h(c, tca, c.p.idx_I[c.LM(2, 0)], y, w, lin, tau);
     else dI20 = 2 / 3. * k * w.I_1m_tca1[0] - kd * (w.I_2m_tca1[0] - w.Pi_tca1[0]) + (use_qs ? c.qs[s.iq_g + c.LM(2, 0)] : 0.0);
-    double dN20 = row(c, tca, c.p.idx_N[c.LM(2, 0)], y, w, lin, tau);
+    double dN20 = row_h(c, tca, c.p.idx_N[c.LM(2, 0)], y, w, lin, tau);
     double rqp = bg.rho_g * dI20 + bg.rho_ur * dN20;
     if (!lin) {
       const double *fo1 = c.fo1, *fo2 = c.fo2;
@@ -804,15 +829,6 @@ __device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int l
                        3 / 5. * (bg.a_sq / t.k_sq) * (rqp + Hc * bg.rho_b * w.b_22m[0] + Hc * bg.rho_cdm * w.cdm_22m[0]) +
                        (lin ? 0.0 : c.qs[s.iq_psi_prime]);
     return w.phi_pp - Hc * psi_prime;
-  }
-  case SP_OMEGA:
-    return omp;
-  case SP_GAMMA:
-    return gp;
-  case SP_GAMMAP:
-    return w.gamma_m2_pp;
-  }
-  return 0.0;
 }
 
 /* dy = f(tau, y): block-wide; prepare(tau) must have run.  Ends with a barrier. */
@@ -959,7 +975,6 @@ __device__ double block_max(const K &c, double v) {
 __device__ void store_sources(const K &c, int index_tau, double tau, const double *y, const double *dy) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
-  int tca = c.sh->tca;
   YVec yv{y};
   /* psi' from the phi' row: psi' = (phi_pp - dy[phi']) / Hc */
   if (threadIdx.x == 0) {
@@ -1062,7 +1077,6 @@ __device__ void store_sources(const K &c, int index_tau, double tau, const doubl
     }
     c.p.sources[(int64_t)tp * s.per_type + col] = src * bg.exp_m_kappa;
   }
-  (void)tca;
 }
 
 __device__ void store_first_order(const K &c, int index_tau, const double *y, const double *dy) {
@@ -1327,10 +1341,10 @@ __device__ void initial_conditions(const K &c, double tau) {
 __constant__ double c_G[5] = {1.0, 1.5, 11.0 / 6.0, 25.0 / 12.0, 137.0 / 60.0};
 __constant__ double c_alpha[5] = {-0.1850, -1.0 / 9.0, -0.0823, -0.0415, 0.0};
 
-/* dif[:,0..k-1] <- dif * (R(r) U): every thread handles its own components */
+/* dif[:,0..k-1] <- dif * (R(r) U): thread 0 forms R U, every thread updates its own components */
 __device__ void rescale_dif(const K &c, int k, double r) {
-  double RU[5][5];
-  {
+  double (*RU)[5] = c.sh->RU;
+  if (threadIdx.x == 0) {
     double Rm[5][5], U[5][5];
     for (int i = 0; i < k; ++i)
       for (int j = 0; j < k; ++j) {
@@ -1351,6 +1365,7 @@ __device__ void rescale_dif(const K &c, int k, double r) {
         RU[i][j] = sm;
       }
   }
+  __syncthreads();
   int n = c.s.n;
   for (int e = threadIdx.x; e < n; e += blockDim.x) {
     double tmp[5];
@@ -1507,7 +1522,11 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
             double errit = newnrm * rate / (1 - rate);
             if (errit <= 0.5 * rtol) { gotynew = 1; break; }
             else if (iter == maxit) break;
-            else if (0.5 * rtol < errit * pow(rate, (double)(maxit - iter))) break;
+            else {
+              double rp = 1.0;
+              for (int q = 0; q < maxit - iter; ++q) rp *= rate;
+              if (0.5 * rtol < errit * rp) break;
+            }
           }
           oldnrm = newnrm;
         }
@@ -1547,17 +1566,29 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
         double abshl = absh;
         if (nofailed) {
           nofailed = 0;
-          double hopt = absh * fmax(0.1, 0.833 * pow(rtol / err, 1.0 / (k + 1)));
+          double errkm1 = 0;
           if (k > 1) {
             double vk = 0;
             for (int i = tid; i < n; i += nt) vk = fmax(vk, fabs((dif[(size_t)(k - 1) * n + i] + difkp1[i]) * invwt[i]));
-            double errkm1 = block_max(c, vk) * erconst[k - 2];
-            double hkm1 = absh * fmax(0.1, 0.769 * pow(rtol / errkm1, 1.0 / k));
-            if (hkm1 > hopt) {
-              hopt = fmin(absh, hkm1);
-              k = k - 1;
-            }
+            errkm1 = block_max(c, vk) * erconst[k - 2];
           }
+          /* the FP64 powers are evaluated once and broadcast */
+          if (tid == 0) {
+            double hopt = absh * fmax(0.1, 0.833 * pow(rtol / err, 1.0 / (k + 1)));
+            int knew = k;
+            if (k > 1) {
+              double hkm1 = absh * fmax(0.1, 0.769 * pow(rtol / errkm1, 1.0 / k));
+              if (hkm1 > hopt) {
+                hopt = fmin(absh, hkm1);
+                knew = k - 1;
+              }
+            }
+            c.sh->ctl[0] = hopt;
+            c.sh->ctl[1] = knew;
+          }
+          __syncthreads();
+          double hopt = c.sh->ctl[0];
+          k = (int)c.sh->ctl[1];
           absh = fmax(hmin, hopt);
         } else {
           absh = fmax(hmin, 0.5 * absh);
@@ -1606,27 +1637,34 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
     abshlast = absh;
     nconhk = (nconhk + 1 < maxk + 2) ? nconhk + 1 : maxk + 2;
     if (nconhk >= k + 2) {
-      double temp = 1.2 * pow(err / rtol, 1.0 / (k + 1));
-      double hopt = (temp > 0.1) ? absh / temp : 10 * absh;
-      int kopt = k;
       double vk = 0, vp = 0;
       for (int i = tid; i < n; i += nt) {
         if (k > 1) vk = fmax(vk, fabs(dif[(size_t)(k - 1) * n + i] * invwt[i]));
         if (k < maxk) vp = fmax(vp, fabs(dif[(size_t)(k + 1) * n + i] * invwt[i]));
       }
       double errkm1 = block_max(c, vk), errkp1 = block_max(c, vp);
-      if (k > 1) {
-        errkm1 *= erconst[k - 2];
-        temp = 1.3 * pow(errkm1 / rtol, 1.0 / k);
-        double hkm1 = (temp > 0.1) ? absh / temp : 10 * absh;
-        if (hkm1 > hopt) { hopt = hkm1; kopt = k - 1; }
+      if (tid == 0) {
+        double temp = 1.2 * pow(err / rtol, 1.0 / (k + 1));
+        double hopt = (temp > 0.1) ? absh / temp : 10 * absh;
+        int kopt = k;
+        if (k > 1) {
+          errkm1 *= erconst[k - 2];
+          temp = 1.3 * pow(errkm1 / rtol, 1.0 / k);
+          double hkm1 = (temp > 0.1) ? absh / temp : 10 * absh;
+          if (hkm1 > hopt) { hopt = hkm1; kopt = k - 1; }
+        }
+        if (k < maxk) {
+          errkp1 *= erconst[k];
+          temp = 1.4 * pow(errkp1 / rtol, 1.0 / (k + 2));
+          double hkp1 = (temp > 0.1) ? absh / temp : 10 * absh;
+          if (hkp1 > hopt) { hopt = hkp1; kopt = k + 1; }
+        }
+        c.sh->ctl[0] = hopt;
+        c.sh->ctl[1] = kopt;
       }
-      if (k < maxk) {
-        errkp1 *= erconst[k];
-        temp = 1.4 * pow(errkp1 / rtol, 1.0 / (k + 2));
-        double hkp1 = (temp > 0.1) ? absh / temp : 10 * absh;
-        if (hkp1 > hopt) { hopt = hkp1; kopt = k + 1; }
-      }
+      __syncthreads();
+      double hopt = c.sh->ctl[0];
+      int kopt = (int)c.sh->ctl[1];
       if (hopt > absh) {
         absh = hopt;
         if (k != kopt) k = kopt;

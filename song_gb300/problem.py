@@ -72,6 +72,8 @@ class Problem:
             s.has_sw = 1
             s.has_isw = 1
             s.use_exponential_potentials = 1
+        elif los == "none":
+            pass
         elif los == "all":
             for f in ("has_pure_scattering_in_los", "has_quad_scattering_in_los", "has_pure_metric_in_los",
                       "has_quad_metric_in_los", "has_time_delay_in_los", "has_redshift_in_los",

@@ -1,0 +1,40 @@
+"""Regenerate the golden fixtures of the CPU oracle.
+
+The reference (coccoinomane/song) cannot be built here (its CLASS submodule is
+empty) and ships no golden vectors, so these fixtures pin the oracle against
+itself: any later change of its numerics shows up as a failing
+tests/test_golden.py.  Run from the repository root:
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+from song_gb300 import build  # noqa: E402
+
+build.build()
+import oracle  # noqa: E402
+from helpers import problem  # noqa: E402
+
+CASES = {
+    "tiny_m012": dict(),
+    "tiny_m0_nopol": dict(m=(0,), has_polarization2=0, sources="T"),
+    "tiny_tca_off_TEB": dict(tight_coupling=0, sources="TEBD", l_max=5),
+}
+
+if __name__ == "__main__":
+    for name, kw in CASES.items():
+        p = problem(**kw)
+        fo = oracle.first_order(p, nthreads=8)
+        p.set_first_order(fo)
+        src, st = oracle.evolve(p, nthreads=8)
+        np.savez_compressed(os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz"),
+                            fo=fo, sources=src, n_steps=st["n_steps"])
+        print(name, fo.shape, src.shape, int(st["n_steps"].sum()))

@@ -1,0 +1,160 @@
+"""GPU evolver (through the C ABI) against the CPU oracle on identical inputs.
+
+Tolerances: both sides run the same NDF algorithm at the same rtol, so they
+agree to round-off until a step-size decision flips; the bound below is the
+rtol contract of the run (errors are max_tau|S - S_ref| / max_tau|S_ref| per
+source type and triplet, floored at 1e-10 of the triplet's largest source,
+see helpers.floored_errors).  The FP32 iteration matrix of the mixed form only
+changes the Newton iterates, so the same bound applies."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from song_gb300 import capi
+from helpers import floored_errors, fo_errors, gpu_run, problem
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def tiny(lib):
+    p = problem()
+    p.set_first_order(oracle.first_order(p, nthreads=8))
+    ref, st = oracle.evolve(p, nthreads=8)
+    return p, ref, st
+
+
+def test_first_order_mode_matches_oracle(lib, olib):
+    p = problem(k_size=4, rtol=1e-5)
+    ref = oracle.first_order(p, nthreads=8)
+    got = p.first_order_gpu()
+    assert np.all(np.isfinite(got))
+    assert np.max(fo_errors(got, ref)) < 1e-4
+
+
+@pytest.mark.parametrize("precision", [capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED])
+def test_second_order_matches_oracle(lib, tiny, precision):
+    p, ref, st_ref = tiny
+    src, st, _ = gpu_run(lib, p, precision)
+    assert np.all(st["status"] == capi.SONG2_OK)
+    assert np.all(st["sources_calls"] == len(p.tau))
+    e = floored_errors(src, ref, p)
+    assert np.max(e) < 10 * p.spec.rtol, np.max(e)
+    # the same algorithm takes the same steps up to a few flipped decisions
+    assert np.all(np.abs(st["n_steps"] - st_ref["n_steps"]) <= 0.05 * st_ref["n_steps"] + 5)
+
+
+def test_against_tight_oracle(lib, tiny):
+    """Every source of an rtol=1e-5 GPU run lies within 1e-4 (relative to its
+    maximum over time) of the FP64 oracle at rtol=1e-8."""
+    p, _, _ = tiny
+    tight, _ = oracle.evolve(p, nthreads=8, rtol=1e-8)
+    spec = p.spec
+    old = spec.rtol
+    spec.rtol = 1e-5
+    try:
+        for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+            src, st, _ = gpu_run(lib, p, precision)
+            assert np.max(floored_errors(src, tight, p)) < 1e-4
+    finally:
+        spec.rtol = old
+
+
+@pytest.mark.parametrize("kw", [
+    dict(m=(0,), has_polarization2=0, sources="T"),
+    dict(tight_coupling=0, sources="TEBD", l_max=5),
+    dict(l_max=2, m=(0, 2)),
+    dict(m=(0, 1, 2, 3, 4), l_max=6, sources="TEB"),
+    dict(k_size=2, k3_size=1),
+    dict(los="all", sources="TEB"),
+])
+def test_edge_cases(lib, olib, kw):
+    p = problem(**kw)
+    p.set_first_order(oracle.first_order(p, nthreads=8))
+    ref, _ = oracle.evolve(p, nthreads=8)
+    for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+        src, st, _ = gpu_run(lib, p, precision)
+        assert np.all(st["status"] == capi.SONG2_OK)
+        assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+
+
+def test_give_up_path_returns_status(lib, tiny):
+    """A triplet that breaches its step limit retires with SONG2_E_MAXSTEPS; the
+    kernel neither traps nor hangs."""
+    p, _, _ = tiny
+    spec = capi.Spec.from_buffer_copy(p.spec)
+    spec.max_steps = 3
+    c = C.c_void_p()
+    err = capi.errbuf()
+    assert lib.song2_ctx_create(C.byref(spec), C.byref(p.tables), capi.SONG2_PREC_MIXED, C.byref(c), err) == 0
+    assert lib.song2_ctx_run(c, None, err) == 0, err.value
+    st = (capi.TripletStats * p.n_triplets)()
+    lib.song2_ctx_download(c, None, st, err)
+    lib.song2_ctx_destroy(c)
+    status = np.frombuffer(st, dtype=capi.STATS_DTYPE)["status"]
+    assert np.all(status == capi.SONG2_E_MAXSTEPS)
+
+
+def test_drop_in_entry_fills_nested_slabs(lib, tiny):
+    """song2_gpu_evolve writes ppt2->sources[tp][k1][k2][tau*k3_size+k3]."""
+    p, ref, _ = tiny
+    n = len(p.k)
+    keep = []
+    tp_level = (C.POINTER(C.POINTER(C.POINTER(C.c_double))) * p.tp2_size)()
+    for tp in range(p.tp2_size):
+        k1_level = (C.POINTER(C.POINTER(C.c_double)) * n)()
+        for i1 in range(n):
+            k2_level = (C.POINTER(C.c_double) * (i1 + 1))()
+            for i2 in range(i1 + 1):
+                buf = np.zeros(len(p.tau) * int(p.k3_size[i1 * n + i2]))
+                keep.append((tp, i1, i2, buf))
+                k2_level[i2] = capi.dptr(buf)
+            keep.append(k2_level)
+            k1_level[i1] = k2_level
+        keep.append(k1_level)
+        tp_level[tp] = k1_level
+    st = (capi.TripletStats * p.n_triplets)()
+    err = capi.errbuf()
+    assert lib.song2_gpu_evolve(C.byref(p.spec), C.byref(p.tables), capi.SONG2_PREC_FP64,
+                                C.cast(tp_level, C.c_void_p), st, err) == 0, err.value
+    flat = np.zeros_like(ref)
+    nested = p.to_nested(flat)
+    for item in keep:
+        if isinstance(item, tuple):
+            tp, i1, i2, buf = item
+            nested[tp][i1][i2][:] = buf
+    assert np.max(floored_errors(flat, ref, p)) < 10 * p.spec.rtol
+
+
+def test_shards_sum_to_full_run(lib, tiny):
+    p, ref, _ = tiny
+    total = np.zeros_like(ref)
+    for r in range(3):
+        c = C.c_void_p()
+        err = capi.errbuf()
+        assert lib.song2_ctx_create_shard(C.byref(p.spec), C.byref(p.tables), capi.SONG2_PREC_MIXED, r, 3,
+                                          C.byref(c), err) == 0, err.value
+        assert lib.song2_ctx_run(c, None, err) == 0
+        part = np.zeros_like(ref)
+        lib.song2_ctx_download(c, capi.dptr(part), None, err)
+        lib.song2_ctx_destroy(c)
+        total += part
+    full, _, _ = gpu_run(lib, p, capi.SONG2_PREC_MIXED)
+    assert np.array_equal(total, full)
+
+
+def test_gpu_matches_golden_fixture(lib):
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    from make_golden import CASES
+    for name, kw in CASES.items():
+        g = np.load(os.path.join(HERE, "golden", name + ".npz"))
+        p = problem(**kw)
+        p.set_first_order(g["fo"])
+        for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+            src, st, _ = gpu_run(lib, p, precision)
+            assert np.max(floored_errors(src, g["sources"], p)) < 10 * p.spec.rtol, name
