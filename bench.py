@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--k-size", type=int, default=None, help="override the k grid size (small profiling cases)")
+    ap.add_argument("--k3-size", type=int, default=None, help="override the k3 grid size (small profiling cases)")
     return ap.parse_args()
 
 
@@ -124,9 +126,9 @@ def measured_peaks():
         return {}
 
 
-def build_problem(cfg):
+def build_problem(cfg, overrides):
     from song_gb300.problem import config_problem
-    p = config_problem(cfg)
+    p = config_problem(cfg, **overrides)
     p.first_order_gpu()          # first-order tables from the GPU first-order mode (untimed set-up)
     return p
 
@@ -244,8 +246,13 @@ def main():
     rank, world, local = dist_env()
     cfg_name = None
     from song_gb300.problem import CONFIGS
-    cfg = CONFIGS[args.config]
-    cfg_name = cfg["name"]
+    cfg = dict(CONFIGS[args.config])
+    overrides = {}
+    if args.k_size:
+        overrides["k_size"] = cfg["k_size"] = args.k_size
+    if args.k3_size:
+        overrides["k3_size"] = cfg["k3_size"] = args.k3_size
+    cfg_name = cfg["name"] + ("" if not overrides else "_reduced")
     config = {"workload": cfg_name, "triplets_per_gpu": None, "k_min": cfg["k_min"], "k_max": cfg["k_max"],
               "k_size": cfg["k_size"], "k3_size": cfg["k3_size"], "l_max": cfg["l_max"], "m": list(cfg["m"]),
               "rtol": cfg["rtol"], "tau_size": cfg["tau_size"], "sources": cfg["sources"],
@@ -259,7 +266,7 @@ def main():
         from song_gb300.problem import config_problem
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
-        p = config_problem(args.config)
+        p = config_problem(args.config, **overrides)
         p.set_first_order(oracle.first_order(p, nthreads=os.cpu_count()))
         threads = os.cpu_count()
         vals = []
@@ -295,7 +302,7 @@ def main():
     if world > 1:
         dist.barrier()
     lib = capi.load()
-    p = build_problem(args.config)
+    p = build_problem(args.config, overrides)
     n_trip = p.n_triplets
     config["triplets_per_gpu"] = n_trip
 

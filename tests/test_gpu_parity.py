@@ -67,7 +67,7 @@ def test_against_tight_oracle(lib, tiny):
 @pytest.mark.parametrize("kw", [
     dict(m=(0,), has_polarization2=0, sources="T"),
     dict(tight_coupling=0, sources="TEBD", l_max=5),
-    dict(l_max=2, m=(0, 2)),
+    dict(l_max=3, m=(0, 2)),
     dict(m=(0, 1, 2, 3, 4), l_max=6, sources="TEB"),
     dict(k_size=2, k3_size=1),
     dict(los="all", sources="TEB"),
