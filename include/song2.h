@@ -150,6 +150,18 @@ typedef struct {
 
 typedef struct song2_ctx song2_ctx;
 
+/* Launch configuration of the persistent evolver.  A "team" evolves one
+   triplet: one CTA of threads_per_team threads (warp_team = 0) or one warp
+   (warp_team = 1, teams_per_cta warps per CTA).  lu_in_smem keeps the
+   iteration-matrix blocks in shared memory instead of an L2-resident global
+   scratch.  Zeros everywhere mean "choose automatically". */
+typedef struct {
+  int warp_team;
+  int teams_per_cta;
+  int threads_per_team;
+  int lu_in_smem;
+} song2_launch;
+
 /* ---------------------------------------------------------------- host side */
 
 /* Number of first-order quantities per node for a given stored l_max. */
@@ -212,6 +224,15 @@ int64_t song2_shard_items(const song2_spec *spec, int shard, int n_shards, int64
    tables once to a device arena (cudaMemcpyAsync).  Not thread safe per ctx. */
 int song2_ctx_create(const song2_spec *spec, const song2_tables *tab,
                      int precision, song2_ctx **out, char *err);
+/* Same with an explicit launch configuration (NULL = automatic) and shard. */
+int song2_ctx_create_ex(const song2_spec *spec, const song2_tables *tab, int precision,
+                        const song2_launch *launch, int shard, int n_shards, song2_ctx **out, char *err);
+/* The launch configuration a context uses. */
+void song2_ctx_get_launch(song2_ctx *ctx, song2_launch *out, int *grid, int *block, size_t *smem);
+/* Autotuner: times every candidate configuration on a sample of the most
+   expensive triplets (largest max(k1,k2,k3)) and returns the fastest. */
+int song2_autotune(const song2_spec *spec, const song2_tables *tab, int precision, int sample,
+                   song2_launch *best, double *best_ms, char *err);
 /* Same, restricted to the triplets of song2_shard_items(spec, shard, n_shards);
    the flat source buffer keeps the full layout, entries of other shards stay 0. */
 int song2_ctx_create_shard(const song2_spec *spec, const song2_tables *tab, int precision,

@@ -170,6 +170,14 @@ static int cfg_init(cfg_t *c, const song2_spec *s, const song2_tables *t, int fo
     snprintf(err, SONG2_ERRLEN, "l_max_* must be at least 2");
     return 1;
   }
+  if (s->has_polarization2)
+    for (int i = 0; i < s->m_size; ++i) {
+      double l = s->l_max_pol_g, m = s->m[i];
+      if (l <= 2 || 1 - m * m / (l * l) * (l + 2) / (l - 2) < 0) {
+        snprintf(err, SONG2_ERRLEN, "l_max_pol_g too small for m = %d (polarisation closure)", s->m[i]);
+        return 1;
+      }
+    }
   c->L_big = L; c->Lq = L + 1;
   for (int l = 0; l < LMAXP; ++l) {
     c->index_m_max[l] = -1;

@@ -83,6 +83,11 @@ class Tables(C.Structure):
     ]
 
 
+class Launch(C.Structure):
+    _fields_ = [("warp_team", C.c_int), ("teams_per_cta", C.c_int), ("threads_per_team", C.c_int),
+                ("lu_in_smem", C.c_int)]
+
+
 class TripletStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("n_steps", C.c_int32), ("n_rejected", C.c_int32),
                 ("n_rhs", C.c_int32), ("n_jac", C.c_int32), ("n_lu", C.c_int32),
@@ -120,6 +125,10 @@ SIGNATURES = {
     "song2_shard_items": (C.c_int64, [C.POINTER(Spec), _I, _I, C.POINTER(C.c_int64)]),
     "song2_ctx_create": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.POINTER(_P), C.c_char_p]),
     "song2_ctx_create_shard": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _I, C.POINTER(_P), C.c_char_p]),
+    "song2_ctx_create_ex": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.c_void_p, _I, _I, C.POINTER(_P),
+                                 C.c_char_p]),
+    "song2_ctx_get_launch": (None, [_P, C.c_void_p, C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_size_t)]),
+    "song2_autotune": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, C.c_void_p, _PD, C.c_char_p]),
     "song2_ctx_destroy": (_I, [_P]),
     "song2_ctx_run": (_I, [_P, _P, C.c_char_p]),
     "song2_ctx_device_sources": (_P, [_P]),

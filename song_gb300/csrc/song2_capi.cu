@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -33,6 +34,8 @@ struct song2_ctx {
   cudaEvent_t ev0, ev1;
   float last_ms;
   int last_launches;
+  song2_launch launch;
+  int n_teams;
 };
 
 namespace {
@@ -86,6 +89,17 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
     snprintf(err, SONG2_ERRLEN, "l_max_* must be at least 2");
     return 1;
   }
+  /* the E/B closure of the reference (perturbations2.c:8033-8036) needs
+     1 - m^2/l^2 (l+2)/(l-2) >= 0 at l = l_max_pol for every evolved m */
+  if (sp->has_polarization2)
+    for (int i = 0; i < sp->m_size; ++i) {
+      double l = sp->l_max_pol_g, m = sp->m[i];
+      if (l <= 2 || 1 - m * m / (l * l) * (l + 2) / (l - 2) < 0) {
+        snprintf(err, SONG2_ERRLEN, "l_max_pol_g = %d is too small for m = %d (polarisation closure)",
+                 sp->l_max_pol_g, sp->m[i]);
+        return 1;
+      }
+    }
   int L = std::max(sp->l_max_g, sp->l_max_ur);
   if (sp->has_polarization2) L = std::max(L, sp->l_max_pol_g);
   L = std::max(L, std::max(sp->l_max_los_t, sp->l_max_los_p));
@@ -350,17 +364,52 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   if (stack < 4096) CK(cudaDeviceSetLimit(cudaLimitStackSize, 4096));
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  c->block = 256;
-  size_t with_lu = song2_smem_bytes(s, precision, c->block, 1);
-  s.lu_in_smem = with_lu <= (size_t)smem_optin ? 1 : 0;
-  c->smem = song2_smem_bytes(s, precision, c->block, s.lu_in_smem);
+  /* launch configuration: explicit, or the default (one warp per triplet, four per
+     CTA, iteration matrices in the L2-resident scratch) */
+  song2_launch L = c->launch;
+  /* SONG2_LAUNCH="warp_team,teams_per_cta,threads_per_team,lu_in_smem" overrides the
+     automatic choice (used to pin a configuration in profiling commands) */
+  const char *env = getenv("SONG2_LAUNCH");
+  if (env && L.teams_per_cta <= 0 && L.threads_per_team <= 0 && !L.warp_team) {
+    int a = 0, b = 0, t = 0, d = 0;
+    if (sscanf(env, "%d,%d,%d,%d", &a, &b, &t, &d) == 4) {
+      L.warp_team = a; L.teams_per_cta = b; L.threads_per_team = t; L.lu_in_smem = d;
+    }
+  }
+  if (L.teams_per_cta <= 0 && L.threads_per_team <= 0 && !L.warp_team) {
+    L.warp_team = 0;
+    L.teams_per_cta = 1;
+    L.threads_per_team = 256;
+    L.lu_in_smem = 0;
+  }
+  if (L.warp_team) {
+    if (L.teams_per_cta < 1) L.teams_per_cta = 4;
+    if (L.teams_per_cta > 8) L.teams_per_cta = 8;
+    L.threads_per_team = 32;
+    c->block = 32 * L.teams_per_cta;
+  } else {
+    L.teams_per_cta = 1;
+    if (L.threads_per_team < 32) L.threads_per_team = 256;
+    L.threads_per_team = std::min(256, (L.threads_per_team / 32) * 32);
+    c->block = L.threads_per_team;
+  }
+  size_t with_lu = song2_smem_bytes(s, precision, c->block, 1) * L.teams_per_cta;
+  if (L.lu_in_smem && with_lu > (size_t)smem_optin) L.lu_in_smem = 0;
+  s.lu_in_smem = L.lu_in_smem;
+  c->smem = song2_smem_bytes(s, precision, c->block, s.lu_in_smem) * L.teams_per_cta;
   if (c->smem > (size_t)smem_optin) {
     snprintf(err, SONG2_ERRLEN, "shared-memory plan %zu B exceeds the %d B limit", c->smem, smem_optin);
     return 1;
   }
-  int per_sm = song2_max_ctas_per_sm(precision, c->block, c->smem);
-  if (per_sm < 1) per_sm = 1;
-  c->grid = std::max(1, std::min(s.n_items, nsm * per_sm));
+  c->launch = L;
+  int per_sm = song2_max_ctas_per_sm(precision, L.warp_team, c->block, c->smem);
+  if (per_sm < 1) {
+    snprintf(err, SONG2_ERRLEN, "launch configuration does not fit on an SM");
+    return 1;
+  }
+  int ctas_needed = (s.n_items + L.teams_per_cta - 1) / L.teams_per_cta;
+  c->grid = std::max(1, std::min(ctas_needed, nsm * per_sm));
+  c->n_teams = c->grid * L.teams_per_cta;
 
   cudaStream_t st = 0;
   DevPtrs &p = c->ptrs;
@@ -421,11 +470,11 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   p.stats = c->d_stats;
   /* Evolver scratch: the Jacobian blocks of each resident CTA, and the LU
      blocks when they do not fit in shared memory. */
-  if (alloc_dev(c, (size_t)c->grid * s.lu_elems * sizeof(double), &tmp, err)) return 1;
+  if (alloc_dev(c, (size_t)c->n_teams * s.lu_elems * sizeof(double), &tmp, err)) return 1;
   p.jac = (double *)tmp;
   if (!s.lu_in_smem) {
     size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
-    if (alloc_dev(c, (size_t)c->grid * s.lu_elems * ts, &tmp, err)) return 1;
+    if (alloc_dev(c, (size_t)c->n_teams * s.lu_elems * ts, &tmp, err)) return 1;
     p.lu_global = tmp;
   }
   if (alloc_dev(c, sizeof(int), &tmp, err)) return 1;
@@ -510,8 +559,8 @@ int64_t song2_shard_items(const song2_spec *spec, int shard, int n_shards, int64
   return n;
 }
 
-static int ctx_create_impl(const song2_spec *spec, const song2_tables *tab, int precision, int shard, int n_shards,
-                           song2_ctx **out, char *err) {
+static int ctx_create_impl(const song2_spec *spec, const song2_tables *tab, int precision, const song2_launch *launch,
+                           int shard, int n_shards, song2_ctx **out, char *err) {
   *out = nullptr;
   if (n_shards < 1 || shard < 0 || shard >= n_shards) {
     snprintf(err, SONG2_ERRLEN, "bad shard %d of %d", shard, n_shards);
@@ -534,6 +583,7 @@ static int ctx_create_impl(const song2_spec *spec, const song2_tables *tab, int 
   for (size_t i = shard; i < sorted.size(); i += n_shards) mine.push_back(sorted[i]);
   song2_ctx *c = new song2_ctx();
   memset((void *)&c->spec, 0, sizeof(c->spec));
+  if (launch) c->launch = *launch;
   if (ctx_setup(c, spec, tab, precision, 0, mine, k3, k3_off, k3_size, pair_off, 0, 0, 0, 0, err)) {
     song2_ctx_destroy(c);
     return 1;
@@ -543,12 +593,72 @@ static int ctx_create_impl(const song2_spec *spec, const song2_tables *tab, int 
 }
 
 int song2_ctx_create(const song2_spec *spec, const song2_tables *tab, int precision, song2_ctx **out, char *err) {
-  return ctx_create_impl(spec, tab, precision, 0, 1, out, err);
+  return ctx_create_impl(spec, tab, precision, nullptr, 0, 1, out, err);
 }
 
 int song2_ctx_create_shard(const song2_spec *spec, const song2_tables *tab, int precision, int shard, int n_shards,
                            song2_ctx **out, char *err) {
-  return ctx_create_impl(spec, tab, precision, shard, n_shards, out, err);
+  return ctx_create_impl(spec, tab, precision, nullptr, shard, n_shards, out, err);
+}
+
+int song2_ctx_create_ex(const song2_spec *spec, const song2_tables *tab, int precision, const song2_launch *launch,
+                        int shard, int n_shards, song2_ctx **out, char *err) {
+  return ctx_create_impl(spec, tab, precision, launch, shard, n_shards, out, err);
+}
+
+void song2_ctx_get_launch(song2_ctx *c, song2_launch *out, int *grid, int *block, size_t *smem) {
+  if (out) *out = c->launch;
+  if (grid) *grid = c->grid;
+  if (block) *block = c->block;
+  if (smem) *smem = c->smem;
+}
+
+int song2_autotune(const song2_spec *spec, const song2_tables *tab, int precision, int sample, song2_launch *best,
+                   double *best_ms, char *err) {
+  /* sample: the `sample` most expensive triplets (the head of the cost-sorted order),
+     evolved as one run with each candidate configuration */
+  if (sample < 1) sample = 1;
+  std::vector<int> k3_off, k3_size;
+  std::vector<int64_t> pair_off;
+  pair_tables(spec, k3_off, k3_size, pair_off);
+  int n3tot = k3_off.empty() ? 0 : k3_off.back() + k3_size.back();
+  std::vector<double> k3(spec->k3, spec->k3 + n3tot);
+  std::vector<WorkItem> sorted;
+  std::vector<int64_t> ref;
+  sorted_items(spec, k3, k3_off, k3_size, sorted, ref);
+  /* spread the sample over the cost range so that the timing reflects the mix */
+  std::vector<WorkItem> pick;
+  size_t stride = std::max<size_t>(1, sorted.size() / (size_t)sample);
+  for (size_t i = 0; i < sorted.size() && (int)pick.size() < sample; i += stride) pick.push_back(sorted[i]);
+  const song2_launch cands[] = {
+      {1, 2, 32, 0}, {1, 4, 32, 0}, {1, 8, 32, 0}, {1, 4, 32, 1}, {0, 1, 128, 1}, {0, 1, 256, 1}, {0, 1, 256, 0},
+  };
+  double bestv = 1e300;
+  int found = 0;
+  for (const song2_launch &cand : cands) {
+    song2_ctx *c = new song2_ctx();
+    memset((void *)&c->spec, 0, sizeof(c->spec));
+    c->launch = cand;
+    char lerr[SONG2_ERRLEN];
+    if (ctx_setup(c, spec, tab, precision, 0, pick, k3, k3_off, k3_size, pair_off, 0, 0, 0, 0, lerr) ||
+        song2_ctx_run(c, nullptr, lerr)) {
+      song2_ctx_destroy(c);
+      continue;
+    }
+    double ms = c->last_ms;
+    if (ms < bestv) {
+      bestv = ms;
+      *best = c->launch;
+      found = 1;
+    }
+    song2_ctx_destroy(c);
+  }
+  if (!found) {
+    snprintf(err, SONG2_ERRLEN, "autotune: no candidate configuration ran");
+    return 1;
+  }
+  if (best_ms) *best_ms = bestv;
+  return 0;
 }
 
 int song2_ctx_destroy(song2_ctx *c) {
@@ -564,7 +674,7 @@ int song2_ctx_run(song2_ctx *c, void *stream, char *err) {
   cudaStream_t st = (cudaStream_t)stream;
   CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
   CK(cudaEventRecord(c->ev0, st));
-  if (song2_launch_evolver(c->spec, c->ptrs, c->precision, c->grid, c->block, c->smem, st)) {
+  if (song2_launch_evolver(c->spec, c->ptrs, c->precision, c->launch.warp_team, c->grid, c->block, c->smem, st)) {
     snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     return 1;
   }

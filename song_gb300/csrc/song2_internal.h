@@ -94,9 +94,11 @@ struct DevPtrs {
 };
 
 /* host-side launcher implemented in song2_kernels.cu */
-int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int grid, int block,
+/* warp_team = 1: one warp per triplet (several per CTA); 0: one CTA per triplet */
+int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int warp_team, int grid, int block,
                          size_t smem, cudaStream_t stream);
+/* shared memory of one team (one CTA in block mode, one warp in warp mode) */
 size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in_smem);
-int song2_max_ctas_per_sm(int precision, int block, size_t smem);
+int song2_max_ctas_per_sm(int precision, int warp_team, int block, size_t smem);
 
 #endif

@@ -62,6 +62,7 @@ struct Shared {
   BgV bg;
   WS ws;
   double psi_prime;
+  double lntau;
   double red[32];
   double RU[5][5];
   double ctl[4];
@@ -73,7 +74,7 @@ struct Shared {
 /* Offsets (in bytes) of the dynamic shared-memory plan. */
 struct Plan {
   size_t y, f, ynew, difkp1, psiv, del, invwt, yout, dyout, dif, fo1, fo2, qs, qc, rot1, rot2, sc, bgraw, shared,
-      xsol, piv, lu, total;
+      tab, xsol, piv, lu, total;
 };
 
 __host__ __device__ inline size_t al(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -88,8 +89,10 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
   p.psiv = o; o = al(o + n * d);
   p.del = o; o = al(o + n * d);
   p.invwt = o; o = al(o + n * d);
-  p.yout = o; o = al(o + n * d);
-  p.dyout = o; o = al(o + n * d);
+  /* the dense-output state lives in the Newton scratch (psiv, del), which is dead
+     between an accepted step and the next predictor */
+  p.yout = p.psiv;
+  p.dyout = p.del;
   p.dif = o; o = al(o + 7 * n * d);
   p.fo1 = o; o = al(o + (size_t)s.nfo * d);
   p.fo2 = o; o = al(o + (size_t)s.nfo * d);
@@ -100,6 +103,11 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
   p.sc = o; o = al(o + 20 * (size_t)s.n_lm * d);
   p.bgraw = o; o = al(o + 16 * d);
   p.shared = o; o = al(o + sizeof(Shared));
+  /* index tables copied from the launch parameters / global memory: the hot
+     loops index them per thread, which the constant bank would serialise */
+  p.tab = o;
+  o = al(o + sizeof(short) * ((size_t)(s.Lq + 1) * (SONG2_MAX_M + SONG2_MAX_M + 2) + SONG2_MAX_M + 3 * n +
+                              4 * (size_t)s.n_lm + 3 * (size_t)s.qs2_size));
   size_t ts = prec == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
   p.xsol = o; o = al(o + n * ts);
   p.piv = o; o = al(o + n * sizeof(int));
@@ -114,15 +122,29 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
 struct K {
   const DevSpec &s;
   const DevPtrs &p;
+  int rank, size, warp_team, team;   /* team = one CTA (block mode) or one warp (warp mode) */
   double *y, *f, *ynew, *difkp1, *psiv, *del, *invwt, *yout, *dyout, *dif, *fo1, *fo2, *qs, *qc, *rot1, *rot2, *sc,
       *bgraw;
   Shared *sh;
+  short *lm_s, *lmq_s, *im_s, *eq_sp, *eq_l, *eq_m, *idx_I, *idx_E, *idx_B, *idx_N, *qs_sp, *qs_l, *qs_m;
   void *xsol;
   int *piv;
   void *lu;
   double *jac;
-  __device__ K(const DevSpec &s_, const DevPtrs &p_, char *smem, int prec) : s(s_), p(p_) {
+  __device__ K(const DevSpec &s_, const DevPtrs &p_, char *smem_all, int prec, int warp_team_) : s(s_), p(p_) {
+    warp_team = warp_team_;
     Plan pl = make_plan(s_, prec, s_.lu_in_smem);
+    char *smem = smem_all;
+    if (warp_team) {
+      rank = threadIdx.x & 31;
+      size = 32;
+      team = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+      smem = smem_all + (size_t)(threadIdx.x >> 5) * pl.total;
+    } else {
+      rank = threadIdx.x;
+      size = blockDim.x;
+      team = blockIdx.x;
+    }
     y = (double *)(smem + pl.y); f = (double *)(smem + pl.f); ynew = (double *)(smem + pl.ynew);
     difkp1 = (double *)(smem + pl.difkp1); psiv = (double *)(smem + pl.psiv); del = (double *)(smem + pl.del);
     invwt = (double *)(smem + pl.invwt); yout = (double *)(smem + pl.yout); dyout = (double *)(smem + pl.dyout);
@@ -130,15 +152,49 @@ struct K {
     qs = (double *)(smem + pl.qs); qc = (double *)(smem + pl.qc); rot1 = (double *)(smem + pl.rot1);
     rot2 = (double *)(smem + pl.rot2); sc = (double *)(smem + pl.sc); bgraw = (double *)(smem + pl.bgraw);
     sh = (Shared *)(smem + pl.shared);
+    short *tb = (short *)(smem + pl.tab);
+    lm_s = tb; tb += (s_.Lq + 1) * SONG2_MAX_M;
+    lmq_s = tb; tb += (s_.Lq + 1) * (SONG2_MAX_M + 2);
+    im_s = tb; tb += SONG2_MAX_M;
+    eq_sp = tb; tb += s_.n;
+    eq_l = tb; tb += s_.n;
+    eq_m = tb; tb += s_.n;
+    idx_I = tb; tb += s_.n_lm;
+    idx_E = tb; tb += s_.n_lm;
+    idx_B = tb; tb += s_.n_lm;
+    idx_N = tb; tb += s_.n_lm;
+    qs_sp = tb; tb += s_.qs2_size;
+    qs_l = tb; tb += s_.qs2_size;
+    qs_m = tb;
     xsol = smem + pl.xsol;
     piv = (int *)(smem + pl.piv);
     size_t ts = prec == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
     if (s_.lu_in_smem) lu = smem + pl.lu;
-    else lu = (char *)p_.lu_global + (size_t)blockIdx.x * s_.lu_elems * ts;
-    jac = p_.jac + (size_t)blockIdx.x * s_.lu_elems;
+    else lu = (char *)p_.lu_global + (size_t)team * s_.lu_elems * ts;
+    jac = p_.jac + (size_t)team * s_.lu_elems;
   }
-  __device__ int LM(int l, int m) const { return s.lm_array[l][s.index_m[m]]; }
-  __device__ int LMQ(int l, int m) const { return s.lmq[l][m]; }
+  __device__ void sync() const {
+    if (warp_team) __syncwarp();
+    else __syncthreads();
+  }
+  __device__ int LM(int l, int m) const { return lm_s[l * SONG2_MAX_M + im_s[m]]; }
+  __device__ int LMQ(int l, int m) const { return lmq_s[l * (SONG2_MAX_M + 2) + m]; }
+  /* copy the index tables into the team's shared workspace (once per kernel) */
+  __device__ void load_tables() const {
+    for (int e = rank; e < (s.Lq + 1) * SONG2_MAX_M; e += size) lm_s[e] = s.lm_array[e / SONG2_MAX_M][e % SONG2_MAX_M];
+    for (int e = rank; e < (s.Lq + 1) * (SONG2_MAX_M + 2); e += size)
+      lmq_s[e] = s.lmq[e / (SONG2_MAX_M + 2)][e % (SONG2_MAX_M + 2)];
+    for (int e = rank; e < SONG2_MAX_M; e += size) im_s[e] = (short)s.index_m[e];
+    for (int e = rank; e < s.n; e += size) {
+      eq_sp[e] = p.eq_sp[e]; eq_l[e] = p.eq_l[e]; eq_m[e] = p.eq_m[e];
+    }
+    for (int e = rank; e < s.n_lm; e += size) {
+      idx_I[e] = p.idx_I[e]; idx_E[e] = p.idx_E[e]; idx_B[e] = p.idx_B[e]; idx_N[e] = p.idx_N[e];
+    }
+    for (int e = rank; e < s.qs2_size; e += size) {
+      qs_sp[e] = p.qs_sp[e]; qs_l[e] = p.qs_l[e]; qs_m[e] = p.qs_m[e];
+    }
+  }
   /* summed couplings, index X in 0..19 */
   __device__ double S(int X, int l, int m) const { return sc[X * s.n_lm + LM(l, m)]; }
   __device__ double cmin(int l, int m1, int m) const { return __ldg(p.cmin + LM(l, m) * 3 + m - m1 + 1); }
@@ -180,19 +236,19 @@ struct YUnit {
 
 template <class Y> __device__ inline double getI(const K &c, int tca, const Y &y, int l, int m) {
   if (l < 0 || m < 0 || m > l || l > c.s.l_max_g || (tca && l >= 1)) return 0.0;
-  return y(c.p.idx_I[c.LM(l, m)]);
+  return y(c.idx_I[c.LM(l, m)]);
 }
 template <class Y> __device__ inline double getE(const K &c, int tca, const Y &y, int l, int m) {
   if (!c.s.has_pol || tca || l < 2 || m < 0 || m > l || l > c.s.l_max_pol) return 0.0;
-  return y(c.p.idx_E[c.LM(l, m)]);
+  return y(c.idx_E[c.LM(l, m)]);
 }
 template <class Y> __device__ inline double getB(const K &c, int tca, const Y &y, int l, int m) {
   if (!c.s.has_pol || tca || l < 2 || m <= 0 || m > l || l > c.s.l_max_pol) return 0.0;
-  return y(c.p.idx_B[c.LM(l, m)]);
+  return y(c.idx_B[c.LM(l, m)]);
 }
 template <class Y> __device__ inline double getN(const K &c, const Y &y, int l, int m) {
   if (l < 0 || m < 0 || m > l || l > c.s.l_max_ur) return 0.0;
-  return y(c.p.idx_N[c.LM(l, m)]);
+  return y(c.idx_N[c.LM(l, m)]);
 }
 template <class Y> __device__ inline double getb(const K &c, const Y &y, int n, int m) {
   /* n = 0: b000 ; n = 1: b11m */
@@ -345,7 +401,7 @@ __device__ double liou_IN(const K &c, int nu, int l, int m) {
   return v;
 }
 
-__device__ void liou_EB(const K &c, int l, int m, double &e, double &bb) {
+template <int WANT_B> __device__ double liou_EB(const K &c, int l, int m) {
   const Tri &t = c.sh->tri;
   const double *fo1 = c.fo1, *fo2 = c.fo2;
   double phi1 = fo1[SONG2_FO_PHI], phi2 = fo2[SONG2_FO_PHI], psi1 = fo1[SONG2_FO_PSI], psi2 = fo2[SONG2_FO_PSI];
@@ -356,14 +412,15 @@ __device__ void liou_EB(const K &c, int l, int m, double &e, double &bb) {
   double dz12 = c.S(DZ12, l, m), dz21 = c.S(DZ21, l, m), dz11 = c.S(DZ11, l, m), dz22 = c.S(DZ22, l, m);
   double km12 = (l - 1) * dm12, km21 = (l - 1) * dm21, kp12 = -(l + 2) * dp12, kp21 = -(l + 2) * dp21;
   double kz12 = -dz12, kz21 = -dz21;
-  e = -4 * php1 * c.rot_2(l, m) * c.E2r(l) +
+  if (WANT_B)
+    return -c.E2r(l) * (kz12 * k1 * (phi1 + psi1) + dz22 * k2 * (phi1 + psi1) + 4 * dz12 * k1 * psi1) -
+           c.E1r(l) * (kz21 * k2 * (phi2 + psi2) + dz11 * k1 * (phi2 + psi2) + 4 * dz21 * k2 * psi2);
+  return -4 * php1 * c.rot_2(l, m) * c.E2r(l) +
       c.E2r(l + 1) * (kp12 * k1 * (phi1 + psi1) + dp22 * k2 * (phi1 + psi1) + 4 * dp12 * k1 * psi1) -
       c.E2r(l - 1) * (km12 * k1 * (phi1 + psi1) + dm22 * k2 * (phi1 + psi1) + 4 * dm12 * k1 * psi1) -
       4 * php2 * c.rot_1(l, m) * c.E1r(l) +
       c.E1r(l + 1) * (kp21 * k2 * (phi2 + psi2) + dp11 * k1 * (phi2 + psi2) + 4 * dp21 * k2 * psi2) -
       c.E1r(l - 1) * (km21 * k2 * (phi2 + psi2) + dm11 * k1 * (phi2 + psi2) + 4 * dm21 * k2 * psi2);
-  bb = -c.E2r(l) * (kz12 * k1 * (phi1 + psi1) + dz22 * k2 * (phi1 + psi1) + 4 * dz12 * k1 * psi1) -
-       c.E1r(l) * (kz21 * k2 * (phi2 + psi2) + dz11 * k1 * (phi2 + psi2) + 4 * dz21 * k2 * psi2);
 }
 
 __device__ double liou_matter(const K &c, int cdm, int n, int m) {
@@ -451,7 +508,7 @@ __device__ void qs_metric(const K &c, const BgV &bg) {
 /* One entry of the quadratic-source vector: total (qs) and collisional (qc) part. */
 __device__ void qs_entry(const K &c, const BgV &bg, int q) {
   const DevSpec &s = c.s;
-  int sp = __ldg(c.p.qs_sp + q), l = __ldg(c.p.qs_l + q), m = __ldg(c.p.qs_m + q);
+  int sp = c.qs_sp[q], l = c.qs_l[q], m = c.qs_m[q];
   double lv = 0, cv = 0;
   switch (sp) {
   case SP_I:
@@ -460,15 +517,13 @@ __device__ void qs_entry(const K &c, const BgV &bg, int q) {
     break;
   case SP_E:
     if (l >= 2) {
-      double e, bb;
-      if (s.has_liou) { liou_EB(c, l, m, e, bb); lv = -e; }
+      if (s.has_liou) lv = -liou_EB<0>(c, l, m);
       if (s.has_coll) cv = coll_E(c, l, m) * bg.kappa_dot;
     }
     break;
   case SP_B:
     if (l >= 2) {
-      double e, bb;
-      if (s.has_liou) { liou_EB(c, l, m, e, bb); lv = -bb; }
+      if (s.has_liou) lv = -liou_EB<1>(c, l, m);
       if (s.has_coll) cv = coll_B(c, l, m) * bg.kappa_dot;
     }
     break;
@@ -506,10 +561,14 @@ __device__ void qs_entry(const K &c, const BgV &bg, int q) {
 __device__ void prepare(const K &c, double tau, int with_sources) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
-  int tid = threadIdx.x, nt = blockDim.x;
-  if (tid < SONG2_BG_SIZE) c.bgraw[tid] = bg_col(c, tid, tau);
+  int tid = c.rank, nt = c.size;
+  /* one FP64 logarithm per call, shared through the workspace */
+  if (tid == 0) c.sh->lntau = log(tau);
+  c.sync();
+  double x = c.sh->lntau;
+  if (tid < SONG2_BG_SIZE)
+    c.bgraw[tid] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, tid, x);
   int use_fo = with_sources && s.has_qs && !s.mode_first_order;
-  double x = (use_fo && tid < 2 * s.nfo) ? log(tau) : 0.0;
   for (int q = tid; q < 2 * s.nfo; q += nt) {
     int which = q >= s.nfo, qq = which ? q - s.nfo : q;
     double v = 0.0;
@@ -520,19 +579,19 @@ __device__ void prepare(const K &c, double tau, int with_sources) {
     }
     (which ? c.fo2 : c.fo1)[qq] = v;
   }
-  __syncthreads();
+  c.sync();
   /* FP64 transcendental work is done once, not once per thread */
   if (tid == 0) bg_derive(c.bgraw, tau, c.sh->bg);
   for (int q = tid; q < s.qs2_size; q += nt) {
     c.qs[q] = 0.0;
     c.qc[q] = 0.0;
   }
-  __syncthreads();
+  c.sync();
   if (use_fo) {
     const BgV &bg = c.sh->bg;
     for (int q = tid; q < s.qs2_size; q += nt) qs_entry(c, bg, q);
   }
-  __syncthreads();
+  c.sync();
 }
 
 /* ------------------------------------------------------------------ workspace */
@@ -687,7 +746,7 @@ __device__ double row_h(const K &c, int tca, int i, const Y &y, const WS &w, int
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
-  int sp = __ldg(c.p.eq_sp + i), l = __ldg(c.p.eq_l + i), m = __ldg(c.p.eq_m + i);
+  int sp = c.eq_sp[i], l = c.eq_l[i], m = c.eq_m[i];
   double k = t.k, kd = bg.kappa_dot, Hc = bg.Hc;
   double mc = s.compute_m[0] ? -3 * w.phi_prime : 0.0, me = s.compute_m[0] ? k * w.psi : 0.0;
   double omp = w.omega_m1_prime, om = s.compute_m[1] ? y(s.idx_omega) : 0.0;
@@ -808,16 +867,16 @@ __device__ double row_h(const K &c, int tca, int i, const Y &y, const WS &w, int
 template <class Y>
 __device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
   const DevSpec &s = c.s;
-  if (__ldg(c.p.eq_sp + i) != SP_PHIP) return row_h(c, tca, i, y, w, lin, tau);
+  if (c.eq_sp[i] != SP_PHIP) return row_h(c, tca, i, y, w, lin, tau);
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
   double k = t.k, kd = bg.kappa_dot, Hc = bg.Hc;
   int use_qs = !lin && s.has_qs;
     /* phi'' = (einstein part) - Hc psi' (perturb2_compute_psi_prime, perturbations2.c:10188-10383) */
     double dI20;
-    if (!tca) dI20 = row_h(c, tca, c.p.idx_I[c.LM(2, 0)], y, w, lin, tau);
+    if (!tca) dI20 = row_h(c, tca, c.idx_I[c.LM(2, 0)], y, w, lin, tau);
     else dI20 = 2 / 3. * k * w.I_1m_tca1[0] - kd * (w.I_2m_tca1[0] - w.Pi_tca1[0]) + (use_qs ? c.qs[s.iq_g + c.LM(2, 0)] : 0.0);
-    double dN20 = row_h(c, tca, c.p.idx_N[c.LM(2, 0)], y, w, lin, tau);
+    double dN20 = row_h(c, tca, c.idx_N[c.LM(2, 0)], y, w, lin, tau);
     double rqp = bg.rho_g * dI20 + bg.rho_ur * dN20;
     if (!lin) {
       const double *fo1 = c.fo1, *fo2 = c.fo2;
@@ -835,17 +894,17 @@ __device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int l
 __device__ void rhs(const K &c, int tca, double tau, const double *y, double *dy) {
   const DevSpec &s = c.s;
   YVec yv{y};
-  if (threadIdx.x == 0) compute_ws(c, tca, yv, 0, c.sh->ws);
-  __syncthreads();
-  for (int i = threadIdx.x; i < s.n; i += blockDim.x) dy[i] = row(c, tca, i, yv, c.sh->ws, 0, tau);
-  __syncthreads();
+  if (c.rank == 0) compute_ws(c, tca, yv, 0, c.sh->ws);
+  c.sync();
+  for (int i = c.rank; i < s.n; i += c.size) dy[i] = row(c, tca, i, yv, c.sh->ws, 0, tau);
+  c.sync();
 }
 
 /* Exact Jacobian of the affine system at tau (prepare(tau) must have run):
    J[:, j] = A e_j, one thread per column; stored per m block in global scratch. */
 __device__ void jacobian(const K &c, int tca, double tau) {
   const DevSpec &s = c.s;
-  for (int j = threadIdx.x; j < s.n; j += blockDim.x) {
+  for (int j = c.rank; j < s.n; j += c.size) {
     int b = 0;
     while (b + 1 < s.nblk && j >= s.blk_start[b + 1]) ++b;
     int b0 = s.blk_start[b], nb = s.blk_size[b];
@@ -855,17 +914,61 @@ __device__ void jacobian(const K &c, int tca, double tau) {
     double *J = c.jac + s.lu_off[b];
     for (int i = b0; i < b0 + nb; ++i) J[(size_t)(i - b0) * nb + (j - b0)] = row(c, tca, i, yu, w, 1, tau);
   }
-  __syncthreads();
+  c.sync();
 }
 
 /* ------------------------------------------------------------------ block LU per m (one warp each) */
 
 template <typename T> __device__ inline T tabs(T x) { return x < T(0) ? -x : x; }
 
+/* one m block, factorised by one warp: partial pivoting, row-major in place */
+template <typename T> __device__ void warp_lu(const K &c, int b, int lane) {
+  const DevSpec &s = c.s;
+  T *A = (T *)c.lu + s.lu_off[b];
+  int nb = s.blk_size[b];
+  int *pv = c.piv + s.blk_start[b];
+  for (int kk = 0; kk < nb; ++kk) {
+    T best = T(-1);
+    int bi = kk;
+    for (int i = kk + lane; i < nb; i += 32) {
+      T v = tabs(A[i * nb + kk]);
+      if (v > best) { best = v; bi = i; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      T ob = __shfl_xor_sync(0xffffffffu, best, off);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) pv[kk] = bi;
+    if (!(best > T(0))) {
+      if (lane == 0) c.sh->lu_fail = 1;
+      A[kk * nb + kk] = T(1);
+      __syncwarp();
+      continue;
+    }
+    if (bi != kk)
+      for (int j = lane; j < nb; j += 32) {
+        T tmp = A[kk * nb + j];
+        A[kk * nb + j] = A[bi * nb + j];
+        A[bi * nb + j] = tmp;
+      }
+    __syncwarp();
+    T inv = T(1) / A[kk * nb + kk];
+    for (int i = kk + 1 + lane; i < nb; i += 32) A[i * nb + kk] *= inv;
+    __syncwarp();
+    for (int i = kk + 1; i < nb; ++i) {
+      T lik = A[i * nb + kk];
+      if (lik != T(0))
+        for (int j = kk + 1 + lane; j < nb; j += 32) A[i * nb + j] -= lik * A[kk * nb + j];
+    }
+    __syncwarp();
+  }
+}
+
 template <typename T> __device__ void form_and_factor(const K &c, double hinvGak) {
   const DevSpec &s = c.s;
   T *LU = (T *)c.lu;
-  for (int e = threadIdx.x; e < s.lu_elems; e += blockDim.x) {
+  for (int e = c.rank; e < s.lu_elems; e += c.size) {
     int b = 0;
     while (b + 1 < s.nblk && e >= s.lu_off[b + 1]) ++b;
     int nb = s.blk_size[b], r = (e - s.lu_off[b]) / nb, col = (e - s.lu_off[b]) % nb;
@@ -873,101 +976,99 @@ template <typename T> __device__ void form_and_factor(const K &c, double hinvGak
     if (r == col) v += 1.0;
     LU[e] = (T)v;
   }
-  __syncthreads();
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp < s.nblk) {
-    int nb = s.blk_size[warp];
-    T *A = LU + s.lu_off[warp];
-    int *pv = c.piv + s.blk_start[warp];
-    for (int kk = 0; kk < nb; ++kk) {
-      T best = T(-1);
-      int bi = kk;
-      for (int i = kk + lane; i < nb; i += 32) {
-        T v = tabs(A[i * nb + kk]);
-        if (v > best) { best = v; bi = i; }
-      }
-      for (int off = 16; off > 0; off >>= 1) {
-        T ob = __shfl_xor_sync(0xffffffffu, best, off);
-        int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-      }
-      if (lane == 0) pv[kk] = bi;
-      if (!(best > T(0))) {
-        if (lane == 0) c.sh->lu_fail = 1;
-        A[kk * nb + kk] = T(1);
-        __syncwarp();
-        continue;
-      }
-      if (bi != kk)
-        for (int j = lane; j < nb; j += 32) {
-          T tmp = A[kk * nb + j];
-          A[kk * nb + j] = A[bi * nb + j];
-          A[bi * nb + j] = tmp;
-        }
-      __syncwarp();
-      T inv = T(1) / A[kk * nb + kk];
-      for (int i = kk + 1 + lane; i < nb; i += 32) A[i * nb + kk] *= inv;
-      __syncwarp();
-      for (int i = kk + 1; i < nb; ++i) {
-        T lik = A[i * nb + kk];
-        if (lik != T(0))
-          for (int j = kk + 1 + lane; j < nb; j += 32) A[i * nb + j] -= lik * A[kk * nb + j];
-      }
-      __syncwarp();
-    }
+  c.sync();
+  if (c.warp_team) {
+    for (int b = 0; b < s.nblk; ++b) warp_lu<T>(c, b, c.rank);
+  } else {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int b = warp; b < s.nblk; b += nw) warp_lu<T>(c, b, lane);
   }
-  __syncthreads();
+  c.sync();
+}
+
+/* one m block, solved by one warp */
+template <typename T> __device__ void warp_solve(const K &c, int b, int lane) {
+  const DevSpec &s = c.s;
+  T *x = (T *)c.xsol;
+  int nb = s.blk_size[b];
+  const T *A = (const T *)c.lu + s.lu_off[b];
+  const int *pv = c.piv + s.blk_start[b];
+  T *xb = x + s.blk_start[b];
+  if (lane == 0)
+    for (int kk = 0; kk < nb; ++kk) {
+      int p = pv[kk];
+      if (p != kk) { T tmp = xb[kk]; xb[kk] = xb[p]; xb[p] = tmp; }
+    }
+  __syncwarp();
+  for (int j = 0; j < nb; ++j) {
+    T xj = xb[j];
+    for (int i = j + 1 + lane; i < nb; i += 32) xb[i] -= A[i * nb + j] * xj;
+    __syncwarp();
+  }
+  for (int j = nb - 1; j >= 0; --j) {
+    if (lane == 0) xb[j] /= A[j * nb + j];
+    __syncwarp();
+    T xj = xb[j];
+    for (int i = lane; i < j; i += 32) xb[i] -= A[i * nb + j] * xj;
+    __syncwarp();
+  }
 }
 
 /* del <- M^{-1} rhs (rhs given in c.del, result written back to c.del) */
 template <typename T> __device__ void lu_solve(const K &c) {
   const DevSpec &s = c.s;
   T *x = (T *)c.xsol;
-  for (int i = threadIdx.x; i < s.n; i += blockDim.x) x[i] = (T)c.del[i];
-  __syncthreads();
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp < s.nblk) {
-    int nb = s.blk_size[warp];
-    const T *A = (const T *)c.lu + s.lu_off[warp];
-    const int *pv = c.piv + s.blk_start[warp];
-    T *xb = x + s.blk_start[warp];
-    if (lane == 0)
-      for (int kk = 0; kk < nb; ++kk) {
-        int p = pv[kk];
-        if (p != kk) { T tmp = xb[kk]; xb[kk] = xb[p]; xb[p] = tmp; }
-      }
-    __syncwarp();
-    for (int j = 0; j < nb; ++j) {
-      T xj = xb[j];
-      for (int i = j + 1 + lane; i < nb; i += 32) xb[i] -= A[i * nb + j] * xj;
-      __syncwarp();
-    }
-    for (int j = nb - 1; j >= 0; --j) {
-      if (lane == 0) xb[j] /= A[j * nb + j];
-      __syncwarp();
-      T xj = xb[j];
-      for (int i = lane; i < j; i += 32) xb[i] -= A[i * nb + j] * xj;
-      __syncwarp();
-    }
+  for (int i = c.rank; i < s.n; i += c.size) x[i] = (T)c.del[i];
+  c.sync();
+  if (c.warp_team) {
+    for (int b = 0; b < s.nblk; ++b) warp_solve<T>(c, b, c.rank);
+  } else {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int b = warp; b < s.nblk; b += nw) warp_solve<T>(c, b, lane);
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < s.n; i += blockDim.x) c.del[i] = (double)x[i];
-  __syncthreads();
+  c.sync();
+  for (int i = c.rank; i < s.n; i += c.size) c.del[i] = (double)x[i];
+  c.sync();
 }
 
 /* ------------------------------------------------------------------ reductions */
 
+/* Max of non-negative doubles over the team.  The reduction runs on the bit
+   patterns: for x >= 0 the IEEE-754 order equals the unsigned-integer order, and
+   a NaN compares above +inf, so no FP64 instruction is spent on it. */
+__device__ inline unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
+
+__device__ double block_max_bits(const K &c, unsigned long long v) {
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
+    v = o > v ? o : v;
+  }
+  if (!c.warp_team) {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) ((unsigned long long *)c.sh->red)[warp] = v;
+    __syncthreads();
+    int nw = (blockDim.x + 31) >> 5;
+    v = 0;
+    for (int i = 0; i < nw; ++i) {
+      unsigned long long o = ((unsigned long long *)c.sh->red)[i];
+      v = o > v ? o : v;
+    }
+  }
+  /* any NaN maps to +inf, so callers test a single "< inf" */
+  if (v > 0x7ff0000000000000ull) v = 0x7ff0000000000000ull;
+  return __longlong_as_double((long long)v);
+}
+
+/* running max of |x| in the bit domain (the sign bit is cleared, NaN stays above inf) */
+__device__ inline void bmax(unsigned long long &acc, double x) {
+  unsigned long long b = dbits(x) & 0x7fffffffffffffffull;
+  acc = b > acc ? b : acc;
+}
+
 __device__ double block_max(const K &c, double v) {
-  if (!(v == v)) v = INFINITY;
-  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __syncthreads();
-  if (lane == 0) c.sh->red[warp] = v;
-  __syncthreads();
-  double r = 0.0;
-  int nw = (blockDim.x + 31) >> 5;
-  for (int i = 0; i < nw; ++i) r = fmax(r, c.sh->red[i]);
-  return r;
+  unsigned long long b = dbits(v) & 0x7fffffffffffffffull;
+  return block_max_bits(c, b);
 }
 
 /* ------------------------------------------------------------------ outputs */
@@ -977,13 +1078,13 @@ __device__ void store_sources(const K &c, int index_tau, double tau, const doubl
   const Tri &t = c.sh->tri;
   YVec yv{y};
   /* psi' from the phi' row: psi' = (phi_pp - dy[phi']) / Hc */
-  if (threadIdx.x == 0) {
+  if (c.rank == 0) {
     const WS &w = c.sh->ws;
     double psi_prime = 0.0;
     if (s.compute_m[0]) psi_prime = (w.phi_pp - dy[s.idx_phip]) / c.sh->bg.Hc;
     c.sh->psi_prime = psi_prime;
   }
-  __syncthreads();
+  c.sync();
   const WS &w = c.sh->ws;
   const BgV &bg = c.sh->bg;
   const double *fo1 = c.fo1, *fo2 = c.fo2;
@@ -1000,7 +1101,7 @@ __device__ void store_sources(const K &c, int index_tau, double tau, const doubl
   double omp = w.omega_m1_prime, gp = s.compute_m[2] ? y[s.idx_gammap] : 0.0;
   double kd = bg.kappa_dot;
   int64_t col = t.pair_off + (int64_t)index_tau * t.k3_size + t.i3;
-  for (int tp = threadIdx.x; tp < s.tp2_size; tp += blockDim.x) {
+  for (int tp = c.rank; tp < s.tp2_size; tp += c.size) {
     int kind = s.tp_kind[tp], l = s.tp_l[tp], m = s.tp_m[tp];
     double src = 0.0;
     if (kind == TP_T) {
@@ -1089,7 +1190,7 @@ __device__ void store_first_order(const K &c, int index_tau, const double *y, co
   double k = t.k;
   double *o = c.p.fo_out + ((size_t)t.i1 * s.fo_tau_size + index_tau) * s.nfo;
   int L1 = s.fo_l_max + 1;
-  for (int q = threadIdx.x; q < s.nfo; q += blockDim.x) {
+  for (int q = c.rank; q < s.nfo; q += c.size) {
     double v = 0.0;
     if (q < SONG2_FO_I) {
       switch (q) {
@@ -1145,7 +1246,7 @@ __device__ double legendre_norm(int l, int m, double x) {
 __device__ int geometry(const K &c) {
   const DevSpec &s = c.s;
   Tri &t = c.sh->tri;
-  int tid = threadIdx.x;
+  int tid = c.rank, nt = c.size;
   if (tid == 0) {
     double k1 = t.k1, k2 = t.k2, k = t.k;
     t.k_sq = k * k;
@@ -1154,9 +1255,9 @@ __device__ int geometry(const K &c) {
     t.cosk2k = (k2 + k1 * t.cosk1k2) / k;
     t.k1_dot_k2 = k1 * k2 * t.cosk1k2;
   }
-  __syncthreads();
+  c.sync();
   if (fabs(t.cosk1k2) > 1 || fabs(t.cosk1k) > 1 || fabs(t.cosk2k) > 1) return 1;
-  for (int e = tid; e < (s.Lq + 1) * (s.mq_max + 1); e += blockDim.x) {
+  for (int e = tid; e < (s.Lq + 1) * (s.mq_max + 1); e += nt) {
     int l = e / (s.mq_max + 1), m = e % (s.mq_max + 1);
     if (m > l) continue;
     double r1 = legendre_norm(l, m, t.cosk1k), r2 = legendre_norm(l, m, t.cosk2k);
@@ -1164,7 +1265,7 @@ __device__ int geometry(const K &c) {
     c.rot1[c.LMQ(l, m)] = r1;
     c.rot2[c.LMQ(l, m)] = r2;
   }
-  __syncthreads();
+  c.sync();
   if (tid == 0) {
     double k1 = t.k1, k2 = t.k2;
     double k1_M1 = t.k1_m[0] = k1 * c.rot_1(1, -1), k1_0 = t.k1_m[1] = k1 * c.rot_1(1, 0), k1_P1 = t.k1_m[2] = k1 * c.rot_1(1, 1);
@@ -1187,7 +1288,7 @@ __device__ int geometry(const K &c) {
     t.k2_ten_k2[4] = SQRT_2 / SQRT_3 * k2_P1 * k2_P1;
   }
   /* summed couplings (perturbations2.c:5752-5845) for l <= L_big */
-  for (int e = tid; e < (s.L_big + 1) * s.m_size; e += blockDim.x) {
+  for (int e = tid; e < (s.L_big + 1) * s.m_size; e += nt) {
     int l = e / s.m_size, im = e % s.m_size, m = s.m[im];
     if (m > l) continue;
     int lm = c.LM(l, m);
@@ -1209,7 +1310,7 @@ __device__ int geometry(const K &c) {
     }
     for (int X = 0; X < 20; ++X) c.sc[X * s.n_lm + lm] = a[X];
   }
-  __syncthreads();
+  c.sync();
   return 0;
 }
 
@@ -1302,18 +1403,18 @@ __device__ void initial_conditions(const K &c, double tau) {
     double I_0_0 = -2 * psi + 8 * psi_1 * psi_2;
     double b_0_0_0 = 3 * (I_0_0 / 4 - delta_g_1 * delta_g_2 / 16);
     y[s.idx_phi] = phi;
-    y[c.p.idx_I[c.LM(0, 0)]] = I_0_0;
+    y[c.idx_I[c.LM(0, 0)]] = I_0_0;
     if (!tca) {
-      y[c.p.idx_I[c.LM(1, 0)]] = I_1_0;
-      y[c.p.idx_I[c.LM(2, 0)]] = I_2_0;
+      y[c.idx_I[c.LM(1, 0)]] = I_1_0;
+      y[c.idx_I[c.LM(2, 0)]] = I_2_0;
     }
     y[s.idx_b000] = b_0_0_0;
     y[s.idx_b11[0]] = b_1_1_0;
     y[s.idx_c000] = b_0_0_0;
     y[s.idx_c11[0]] = cdm_1_1_0;
-    y[c.p.idx_N[c.LM(0, 0)]] = I_0_0;
-    y[c.p.idx_N[c.LM(1, 0)]] = N_1_0;
-    y[c.p.idx_N[c.LM(2, 0)]] = N_2_0;
+    y[c.idx_N[c.LM(0, 0)]] = I_0_0;
+    y[c.idx_N[c.LM(1, 0)]] = N_1_0;
+    y[c.idx_N[c.LM(2, 0)]] = N_2_0;
     double rho_monopole = bg.rho_g * I_0_0 + bg.rho_b * b_0_0_0 + bg.rho_cdm * b_0_0_0 + bg.rho_ur * I_0_0;
     y[s.idx_phip] = -Hc * psi - k_sq / (3 * Hc) * phi - a_sq * rho_monopole / (2 * Hc) + qs[s.iq_phi_prime_poisson];
   } else if (s.ic == SONG2_IC_AD_FIRST_ORDER) {
@@ -1322,16 +1423,16 @@ __device__ void initial_conditions(const K &c, double tau) {
     y[s.idx_phi] = (1 + 2 / 5. * frac_ur) * psi;
     double u0 = 0.5 * k * tau * psi;
     double I_0_0 = -2 * psi;
-    y[c.p.idx_I[c.LM(0, 0)]] = I_0_0;
-    if (!tca) y[c.p.idx_I[c.LM(1, 0)]] = 4 * u0;
+    y[c.idx_I[c.LM(0, 0)]] = I_0_0;
+    if (!tca) y[c.idx_I[c.LM(1, 0)]] = 4 * u0;
     y[s.idx_b000] = 0.75 * I_0_0;
     y[s.idx_b11[0]] = 3 * u0;
     y[s.idx_c000] = 0.75 * I_0_0;
     y[s.idx_c11[0]] = 3 * u0;
-    y[c.p.idx_N[c.LM(0, 0)]] = I_0_0;
-    y[c.p.idx_N[c.LM(1, 0)]] = 4 * u0;
+    y[c.idx_N[c.LM(0, 0)]] = I_0_0;
+    y[c.idx_N[c.LM(1, 0)]] = 4 * u0;
     /* I_20 = 10 shear, consistent with the second-order initial conditions */
-    y[c.p.idx_N[c.LM(2, 0)]] = 10 * (1 / 15. * k * k * tau * tau * psi);
+    y[c.idx_N[c.LM(2, 0)]] = 10 * (1 / 15. * k * k * tau * tau * psi);
     y[s.idx_phip] = 0.0;
   }
 }
@@ -1344,7 +1445,7 @@ __constant__ double c_alpha[5] = {-0.1850, -1.0 / 9.0, -0.0823, -0.0415, 0.0};
 /* dif[:,0..k-1] <- dif * (R(r) U): thread 0 forms R U, every thread updates its own components */
 __device__ void rescale_dif(const K &c, int k, double r) {
   double (*RU)[5] = c.sh->RU;
-  if (threadIdx.x == 0) {
+  if (c.rank == 0) {
     double Rm[5][5], U[5][5];
     for (int i = 0; i < k; ++i)
       for (int j = 0; j < k; ++j) {
@@ -1365,9 +1466,9 @@ __device__ void rescale_dif(const K &c, int k, double r) {
         RU[i][j] = sm;
       }
   }
-  __syncthreads();
+  c.sync();
   int n = c.s.n;
-  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+  for (int e = c.rank; e < n; e += c.size) {
     double tmp[5];
     for (int j = 0; j < k; ++j) {
       double sm = 0;
@@ -1376,13 +1477,13 @@ __device__ void rescale_dif(const K &c, int k, double r) {
     }
     for (int j = 0; j < k; ++j) c.dif[(size_t)j * n + e] = tmp[j];
   }
-  __syncthreads();
+  c.sync();
 }
 
 template <typename T>
 __device__ int refactor(const K &c, double hinvGak, song2_triplet_stats &st) {
-  if (threadIdx.x == 0) c.sh->lu_fail = 0;
-  __syncthreads();
+  if (c.rank == 0) c.sh->lu_fail = 0;
+  c.sync();
   form_and_factor<T>(c, hinvGak);
   st.n_lu++;
   return c.sh->lu_fail ? SONG2_E_SINGULAR : SONG2_OK;
@@ -1394,7 +1495,7 @@ __device__ void do_output(const K &c, int jout, double to) {
   rhs(c, c.sh->tca, to, c.yout, c.dyout);
   if (c.s.mode_first_order) store_first_order(c, jout, c.yout, c.dyout);
   else store_sources(c, jout, to, c.yout, c.dyout);
-  __syncthreads();
+  c.sync();
 }
 
 __device__ inline double tout_at(const K &c, int j) {
@@ -1404,7 +1505,7 @@ __device__ inline double tout_at(const K &c, int j) {
 template <typename T>
 __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0, song2_triplet_stats &st) {
   const DevSpec &s = c.s;
-  int n = s.n, tid = threadIdx.x, nt = blockDim.x;
+  int n = s.n, tid = c.rank, nt = c.size;
   int nout = s.mode_first_order ? s.fo_tau_size : s.tau_size;
   int tca = c.sh->tca;
   double rtol = s.rtol, threshold = s.threshold;
@@ -1422,7 +1523,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
     while (jout < nout && tout_at(c, jout) <= t0) {
       if (tout_at(c, jout) == t0) {
         for (int i = tid; i < n; i += nt) c.yout[i] = y[i];
-        __syncthreads();
+        c.sync();
         do_output(c, jout, t0);
       }
       ++jout;
@@ -1435,15 +1536,15 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
   int Jcurrent = 1;
   double hmin = 16 * eps * fabs(t);
   double absh = fmin(hmax, fabs(t1 - t0));
-  double v = 0;
-  for (int i = tid; i < n; i += nt) v = fmax(v, fabs(f[i]) / fmax(fabs(y[i]), threshold));
-  double rh = 1.25 * block_max(c, v) / sqrt(rtol);
+  unsigned long long vb = 0;
+  for (int i = tid; i < n; i += nt) bmax(vb, f[i] / fmax(fabs(y[i]), threshold));
+  double rh = 1.25 * block_max_bits(c, vb) / sqrt(rtol);
   if (absh * rh > 1) absh = 1.0 / rh;
   absh = fmax(absh, hmin);
   double h = absh;
   int k = 1;
   for (int e = tid; e < 7 * n; e += nt) dif[e] = 0.0;
-  __syncthreads();
+  c.sync();
   for (int i = tid; i < n; i += nt) dif[i] = h * f[i];
   double hinvGak = h * invGa[k - 1];
   int nconhk = 0;
@@ -1487,27 +1588,27 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
         tnew = t + h;
         if (done) tnew = t1;
         h = tnew - t;
-        double vm = 0;
+        unsigned long long vm = 0;
         for (int i = tid; i < n; i += nt) {
           invwt[i] = 1.0 / fmax(fmax(fabs(y[i]), fabs(ynew[i])), threshold);
-          vm = fmax(vm, fabs(ynew[i] * invwt[i]));
+          bmax(vm, ynew[i] * invwt[i]);
         }
-        double minnrm = 100 * eps * block_max(c, vm);
+        double minnrm = 100 * eps * block_max_bits(c, vm);
         double oldnrm = 0;
         prepare(c, tnew, 1);
         for (int iter = 1; iter <= maxit; ++iter) {
           rhs(c, tca, tnew, ynew, f);
           st.n_rhs++;
           for (int i = tid; i < n; i += nt) del[i] = hinvGak * f[i] - (psiv[i] + difkp1[i]);
-          __syncthreads();
+          c.sync();
           lu_solve<T>(c);
-          double vn = 0;
+          unsigned long long vn = 0;
           for (int i = tid; i < n; i += nt) {
-            vn = fmax(vn, fabs(del[i] * invwt[i]));
+            bmax(vn, del[i] * invwt[i]);
             difkp1[i] += del[i];
             ynew[i] += del[i];
           }
-          double newnrm = block_max(c, vn);
+          double newnrm = block_max_bits(c, vn);
           if (!(newnrm < INFINITY)) break;
           if (newnrm <= minnrm) { gotynew = 1; break; }
           else if (iter == 1) {
@@ -1552,13 +1653,13 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
           havrate = 0;
         }
       }
-      double ve = 0, vfin = 0;
+      unsigned long long ve = 0, vfin = 0;
       for (int i = tid; i < n; i += nt) {
-        ve = fmax(ve, fabs(difkp1[i] * invwt[i]));
-        vfin = fmax(vfin, fabs(ynew[i]));
+        bmax(ve, difkp1[i] * invwt[i]);
+        bmax(vfin, ynew[i]);
       }
-      err = block_max(c, ve) * erconst[k - 1];
-      double ymax = block_max(c, vfin);
+      err = block_max_bits(c, ve) * erconst[k - 1];
+      double ymax = block_max_bits(c, vfin);
       if (!(ymax < 1e300)) return SONG2_E_NAN;
       if (err > rtol) {
         st.n_rejected++;
@@ -1568,9 +1669,9 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
           nofailed = 0;
           double errkm1 = 0;
           if (k > 1) {
-            double vk = 0;
-            for (int i = tid; i < n; i += nt) vk = fmax(vk, fabs((dif[(size_t)(k - 1) * n + i] + difkp1[i]) * invwt[i]));
-            errkm1 = block_max(c, vk) * erconst[k - 2];
+            unsigned long long vk = 0;
+            for (int i = tid; i < n; i += nt) bmax(vk, (dif[(size_t)(k - 1) * n + i] + difkp1[i]) * invwt[i]);
+            errkm1 = block_max_bits(c, vk) * erconst[k - 2];
           }
           /* the FP64 powers are evaluated once and broadcast */
           if (tid == 0) {
@@ -1586,7 +1687,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
             c.sh->ctl[0] = hopt;
             c.sh->ctl[1] = knew;
           }
-          __syncthreads();
+          c.sync();
           double hopt = c.sh->ctl[0];
           k = (int)c.sh->ctl[1];
           absh = fmax(hmin, hopt);
@@ -1613,7 +1714,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
       dif[(size_t)k * n + i] = difkp1[i];
       for (int j = k - 1; j >= 0; --j) dif[(size_t)j * n + i] += dif[(size_t)(j + 1) * n + i];
     }
-    __syncthreads();
+    c.sync();
     while (jout < nout && tout_at(c, jout) <= tnew) {
       double to = tout_at(c, jout);
       if (to > t || (include_t0 && to == t)) {
@@ -1627,7 +1728,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
             }
           c.yout[i] = acc;
         }
-        __syncthreads();
+        c.sync();
         do_output(c, jout, to);
         st.sources_calls++;
       }
@@ -1637,12 +1738,12 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
     abshlast = absh;
     nconhk = (nconhk + 1 < maxk + 2) ? nconhk + 1 : maxk + 2;
     if (nconhk >= k + 2) {
-      double vk = 0, vp = 0;
+      unsigned long long vk = 0, vp = 0;
       for (int i = tid; i < n; i += nt) {
-        if (k > 1) vk = fmax(vk, fabs(dif[(size_t)(k - 1) * n + i] * invwt[i]));
-        if (k < maxk) vp = fmax(vp, fabs(dif[(size_t)(k + 1) * n + i] * invwt[i]));
+        if (k > 1) bmax(vk, dif[(size_t)(k - 1) * n + i] * invwt[i]);
+        if (k < maxk) bmax(vp, dif[(size_t)(k + 1) * n + i] * invwt[i]);
       }
-      double errkm1 = block_max(c, vk), errkp1 = block_max(c, vp);
+      double errkm1 = block_max_bits(c, vk), errkp1 = block_max_bits(c, vp);
       if (tid == 0) {
         double temp = 1.2 * pow(err / rtol, 1.0 / (k + 1));
         double hopt = (temp > 0.1) ? absh / temp : 10 * absh;
@@ -1662,7 +1763,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
         c.sh->ctl[0] = hopt;
         c.sh->ctl[1] = kopt;
       }
-      __syncthreads();
+      c.sync();
       double hopt = c.sh->ctl[0];
       int kopt = (int)c.sh->ctl[1];
       if (hopt > absh) {
@@ -1672,7 +1773,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
     }
     t = tnew;
     for (int i = tid; i < n; i += nt) y[i] = ynew[i];
-    __syncthreads();
+    c.sync();
     Jcurrent = 0;
   }
   return SONG2_OK;
@@ -1682,10 +1783,10 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
 
 template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_stats &st) {
   const DevSpec &s = c.s;
-  int tid = threadIdx.x;
+  int tid = c.rank;
   if (geometry(c)) return SONG2_E_CONFIG;
   if (tid == 0) c.sh->lu_fail = intervals(c);
-  __syncthreads();
+  c.sync();
   if (c.sh->lu_fail) return SONG2_E_CONFIG;
   Tri &t = c.sh->tri;
   int jout = 0;
@@ -1694,10 +1795,10 @@ template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_sta
     double tb = (iv == 0 && t.nint == 2) ? t.tau_switch : t.tau_end;
     if (iv == 0) {
       if (tid == 0) c.sh->tca = t.tca0;
-      __syncthreads();
+      c.sync();
       prepare(c, ta, 1);
       if (tid == 0) initial_conditions(c, ta);
-      __syncthreads();
+      c.sync();
     } else {
       /* TCA -> full remap (perturbations2.c:7233-7285): the frozen moments take the
          TCA values at the switching time; everything else carries over */
@@ -1706,18 +1807,18 @@ template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_sta
         YVec yv{c.y};
         compute_ws(c, 1, yv, 0, c.sh->ws);
         WS &w = c.sh->ws;
-        for (int im = 0; im <= s.index_m_max[1]; ++im) c.y[c.p.idx_I[c.LM(1, s.m[im])]] = w.I_1m_tca1[s.m[im]];
+        for (int im = 0; im <= s.index_m_max[1]; ++im) c.y[c.idx_I[c.LM(1, s.m[im])]] = w.I_1m_tca1[s.m[im]];
         for (int im = 0; im <= s.index_m_max[2]; ++im) {
           int m = s.m[im];
-          c.y[c.p.idx_I[c.LM(2, m)]] = w.I_2m_tca1[m];
+          c.y[c.idx_I[c.LM(2, m)]] = w.I_2m_tca1[m];
           if (s.has_pol) {
-            c.y[c.p.idx_E[c.LM(2, m)]] = w.E_2m_tca1[m];
-            if (m != 0) c.y[c.p.idx_B[c.LM(2, m)]] = w.B_2m_tca1[m];
+            c.y[c.idx_E[c.LM(2, m)]] = w.E_2m_tca1[m];
+            if (m != 0) c.y[c.idx_B[c.LM(2, m)]] = w.B_2m_tca1[m];
           }
         }
         c.sh->tca = 0;
       }
-      __syncthreads();
+      c.sync();
     }
     int stc = ndf15<T>(c, ta, tb, jout, iv == 0, st);
     if (stc != SONG2_OK) return stc;
@@ -1727,16 +1828,19 @@ template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_sta
   return SONG2_OK;
 }
 
-template <typename T> __global__ void __launch_bounds__(256) evolver_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
+template <typename T, int WARP_TEAM>
+__global__ void __launch_bounds__(256) evolver_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
   extern __shared__ __align__(16) char smem[];
-  K c(s, p, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64);
+  K c(s, p, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64, WARP_TEAM);
+  c.load_tables();
+  c.sync();
   for (int guard = 0; guard < s.n_items + 1; ++guard) {
-    if (threadIdx.x == 0) c.sh->item = atomicAdd(p.queue, 1);
-    __syncthreads();
+    if (c.rank == 0) c.sh->item = atomicAdd(p.queue, 1);
+    c.sync();
     int item = c.sh->item;
     if (item >= s.n_items) break;
     WorkItem wi = p.items[item];
-    if (threadIdx.x == 0) {
+    if (c.rank == 0) {
       Tri &t = c.sh->tri;
       t.i1 = wi.i1; t.i2 = wi.i2; t.i3 = wi.i3; t.pair = wi.pair; t.item = item;
       t.k1 = p.k[wi.i1];
@@ -1745,14 +1849,14 @@ template <typename T> __global__ void __launch_bounds__(256) evolver_kernel(cons
       t.k = p.k3[p.k3_off[wi.pair] + wi.i3];
       t.pair_off = p.pair_off[wi.pair];
     }
-    __syncthreads();
+    c.sync();
     song2_triplet_stats st;
     st.status = 0; st.n_steps = 0; st.n_rejected = 0; st.n_rhs = 0; st.n_jac = 0; st.n_lu = 0; st.n_newton_fail = 0;
     st.sources_calls = 0;
     int stc = solve_triplet<T>(c, st);
     st.status = stc;
-    if (threadIdx.x == 0) p.stats[item] = st;
-    __syncthreads();
+    if (c.rank == 0) p.stats[item] = st;
+    c.sync();
   }
 }
 
@@ -1763,27 +1867,29 @@ size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in
   return make_plan(spec, precision, lu_in_smem).total;
 }
 
-int song2_max_ctas_per_sm(int precision, int block, size_t smem) {
+namespace {
+template <typename T, int W> void *kernel_ptr() { return (void *)evolver_kernel<T, W>; }
+void *pick_kernel(int precision, int warp_team) {
+  if (precision == SONG2_PREC_MIXED) return warp_team ? kernel_ptr<float, 1>() : kernel_ptr<float, 0>();
+  return warp_team ? kernel_ptr<double, 1>() : kernel_ptr<double, 0>();
+}
+} // namespace
+
+int song2_max_ctas_per_sm(int precision, int warp_team, int block, size_t smem) {
   int nb = 0;
-  cudaError_t e;
-  if (precision == SONG2_PREC_MIXED) {
-    cudaFuncSetAttribute(evolver_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, evolver_kernel<float>, block, smem);
-  } else {
-    cudaFuncSetAttribute(evolver_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, evolver_kernel<double>, block, smem);
-  }
+  const void *f = pick_kernel(precision, warp_team);
+  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, block, smem);
   return e == cudaSuccess ? nb : 0;
 }
 
-int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int grid, int block, size_t smem,
-                         cudaStream_t stream) {
-  if (precision == SONG2_PREC_MIXED) {
-    cudaFuncSetAttribute(evolver_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    evolver_kernel<float><<<grid, block, smem, stream>>>(spec, ptrs);
-  } else {
-    cudaFuncSetAttribute(evolver_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    evolver_kernel<double><<<grid, block, smem, stream>>>(spec, ptrs);
-  }
-  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int warp_team, int grid, int block,
+                         size_t smem, cudaStream_t stream) {
+  const void *f = pick_kernel(precision, warp_team);
+  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  DevSpec sp = spec;
+  DevPtrs pp = ptrs;
+  void *args[] = {(void *)&sp, (void *)&pp};
+  cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, stream);
+  return e == cudaSuccess ? 0 : 1;
 }

@@ -67,7 +67,7 @@ def test_against_tight_oracle(lib, tiny):
 @pytest.mark.parametrize("kw", [
     dict(m=(0,), has_polarization2=0, sources="T"),
     dict(tight_coupling=0, sources="TEBD", l_max=5),
-    dict(l_max=3, m=(0, 2)),
+    dict(l_max=4, m=(0, 2)),
     dict(m=(0, 1, 2, 3, 4), l_max=6, sources="TEB"),
     dict(k_size=2, k3_size=1),
     dict(los="all", sources="TEB"),
@@ -80,6 +80,34 @@ def test_edge_cases(lib, olib, kw):
         src, st, _ = gpu_run(lib, p, precision)
         assert np.all(st["status"] == capi.SONG2_OK)
         assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+
+
+def test_closure_limit_is_rejected(lib):
+    """l_max_pol = 3 with m = 2 makes the reference's polarisation closure imaginary:
+    the C ABI refuses the spec with a message instead of producing NaNs."""
+    p = problem(l_max=3, m=(0, 2))
+    p.set_first_order(np.zeros(p.fo_shape()))
+    c = C.c_void_p()
+    err = capi.errbuf()
+    assert lib.song2_ctx_create(C.byref(p.spec), C.byref(p.tables), capi.SONG2_PREC_FP64, C.byref(c), err) == 1
+    assert b"closure" in err.value
+
+
+@pytest.mark.parametrize("launch", [(1, 2, 32, 0), (1, 8, 32, 0), (1, 4, 32, 1), (0, 1, 128, 1), (0, 1, 256, 0)])
+def test_launch_configurations_agree(lib, tiny, launch):
+    """Every launch configuration the autotuner may pick computes the same numbers."""
+    p, _, _ = tiny
+    base, _, _ = gpu_run(lib, p, capi.SONG2_PREC_MIXED)
+    L = capi.Launch(*launch)
+    c = C.c_void_p()
+    err = capi.errbuf()
+    assert lib.song2_ctx_create_ex(C.byref(p.spec), C.byref(p.tables), capi.SONG2_PREC_MIXED, C.byref(L), 0, 1,
+                                   C.byref(c), err) == 0, err.value
+    assert lib.song2_ctx_run(c, None, err) == 0, err.value
+    src = np.zeros_like(base)
+    lib.song2_ctx_download(c, capi.dptr(src), None, err)
+    lib.song2_ctx_destroy(c)
+    assert np.array_equal(src, base)
 
 
 def test_give_up_path_returns_status(lib, tiny):
