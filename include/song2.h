@@ -260,6 +260,30 @@ int song2_gpu_evolve(const song2_spec *spec, const song2_tables *tab, int precis
                      double ****sources_out, song2_triplet_stats *per_triplet,
                      char *err);
 
+/* Allocation-free evolver, for callers that cannot allocate device memory:
+   code running inside a CUDA stream capture that must not add allocation nodes,
+   applications whose device memory is owned by a fixed-size pool or another
+   runtime, or hosts that forbid cudaMalloc after start-up.  It has no
+   counterpart in the reference.  It performs no cudaMalloc, cudaFree or other
+   device allocation: all its device-side scratch (layout tables, work list,
+   work-queue counter, Jacobian and LU blocks) lives in one 64 MiB array
+   compiled into this library, which every GPU that loads the library holds
+   until the process exits.  Problems whose tables do not fit are rejected with
+   an error; the number of resident triplets is reduced to fit the
+   iteration-matrix blocks.  The caller passes the inputs and outputs on the
+   device: tab_dev is a song2_tables whose bg, bg_dd, fo and fo_dd point to
+   device memory (spec and its k/k3/tau grids stay in host memory);
+   sources_dev holds tp2_size * song2_sources_per_type() doubles (cleared by the
+   call) and stats_dev song2_n_triplets() entries, in the evolver's internal
+   (cost-sorted) triplet order.  Work is enqueued on `stream` (NULL = legacy
+   default stream) and the outputs are valid once it has completed.  The first
+   call on a device resolves the scratch address with that device current; make
+   that first call before any stream capture.  Calls share the scratch: two
+   calls that overlap on the GPU race and corrupt each other's results. */
+int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tables *tab_dev, int precision,
+                             double *sources_dev, song2_triplet_stats *stats_dev, void *stream,
+                             char *err);
+
 /* First-order provider: evolves SONG's own equations in first-order mode
    (quadratic sources off, has_ad_first_order initial conditions, m = 0)
    for every k of spec->k and fills the first-order table fo[k][tau][q] on the

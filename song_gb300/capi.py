@@ -138,6 +138,8 @@ SIGNATURES = {
     "song2_ctx_last_launches": (_I, [_P]),
     "song2_gpu_evolve": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _P, C.POINTER(TripletStats),
                               C.c_char_p]),
+    "song2_gpu_evolve_noalloc": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_char_p]),
     "song2_gpu_first_order": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _D, _D, _PD, C.c_char_p]),
 }
 

@@ -808,3 +808,161 @@ int song2_gpu_first_order(const song2_spec *spec2, const song2_tables *bg_only, 
 }
 
 } /* extern "C" */
+
+/* ------------------------------------------------------------ allocation-free entry */
+/* Scratch of song2_gpu_evolve_noalloc: every GPU that loads this library holds
+   these SONG2_NOALLOC_BYTES until the process exits.  Host code must not use the
+   name as an address; the device address comes from cudaGetSymbolAddress. */
+#define SONG2_NOALLOC_BYTES ((size_t)64 << 20)
+static __device__ __align__(256) unsigned char song2_noalloc_scratch[SONG2_NOALLOC_BYTES];
+
+#define SONG2_NOALLOC_MAX_DEVICES 64
+static void *g_noalloc_addr[SONG2_NOALLOC_MAX_DEVICES];
+
+static size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tables *tab_dev, int precision,
+                                        double *sources_dev, song2_triplet_stats *stats_dev, void *stream,
+                                        char *err) {
+  if (precision != SONG2_PREC_FP64 && precision != SONG2_PREC_MIXED) {
+    snprintf(err, SONG2_ERRLEN, "unknown precision %d", precision);
+    return 1;
+  }
+  if (!sources_dev || !stats_dev) {
+    snprintf(err, SONG2_ERRLEN, "sources_dev and stats_dev must be device buffers");
+    return 1;
+  }
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= SONG2_NOALLOC_MAX_DEVICES) {
+    snprintf(err, SONG2_ERRLEN, "device %d beyond the %d supported", dev, SONG2_NOALLOC_MAX_DEVICES);
+    return 1;
+  }
+  /* first call on this device (which must be current): resolve the scratch address */
+  if (!g_noalloc_addr[dev]) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, song2_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) {
+      snprintf(err, SONG2_ERRLEN, "cudaGetSymbolAddress of the scratch failed: %s", cudaGetErrorString(e));
+      return 1;
+    }
+    g_noalloc_addr[dev] = ptr;
+  }
+  char *base = (char *)g_noalloc_addr[dev];
+  cudaStream_t st = (cudaStream_t)stream;
+
+  HostLayout H;
+  if (build_layout(spec, tab_dev, 0, H, err)) return 1;
+  DevSpec s = H.s;
+  std::vector<int> k3_off, k3_size;
+  std::vector<int64_t> pair_off;
+  pair_tables(spec, k3_off, k3_size, pair_off);
+  int n3tot = k3_off.empty() ? 0 : k3_off.back() + k3_size.back();
+  std::vector<double> k3(spec->k3, spec->k3 + n3tot);
+  std::vector<WorkItem> items;
+  std::vector<int64_t> ref;
+  sorted_items(spec, k3, k3_off, k3_size, items, ref);
+  s.n_items = (int)items.size();
+  s.per_type = song2_sources_per_type(spec);
+
+  /* carve the scratch: small tables first, then the per-team Jacobian blocks */
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off = na_align(off + std::max<size_t>(bytes, 1)); return o; };
+  size_t o_k = take(sizeof(double) * spec->k_size), o_k3 = take(sizeof(double) * k3.size());
+  size_t o_tau = take(sizeof(double) * spec->tau_size);
+  size_t o_k3off = take(sizeof(int) * k3_off.size()), o_k3sz = take(sizeof(int) * k3_size.size());
+  size_t o_poff = take(sizeof(int64_t) * pair_off.size());
+  size_t nc = H.cmin.size() * sizeof(double);
+  size_t o_cm = take(nc), o_cp = take(nc), o_dm = take(nc), o_dp = take(nc), o_dz = take(nc);
+  size_t ne = sizeof(short) * H.eq_sp.size(), ni = sizeof(short) * H.idx_I.size(), nq = sizeof(short) * H.qs_sp.size();
+  size_t o_esp = take(ne), o_el = take(ne), o_em = take(ne);
+  size_t o_iI = take(ni), o_iE = take(ni), o_iB = take(ni), o_iN = take(ni);
+  size_t o_qsp = take(nq), o_ql = take(nq), o_qm = take(nq);
+  size_t o_items = take(sizeof(WorkItem) * items.size());
+  size_t o_queue = take(sizeof(int));
+  size_t fixed = off;
+  if (fixed > SONG2_NOALLOC_BYTES) {
+    snprintf(err, SONG2_ERRLEN, "problem tables need %zu B, more than the %zu B scratch", fixed,
+             (size_t)SONG2_NOALLOC_BYTES);
+    return 1;
+  }
+  int nsm = 0, smem_optin = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  size_t stack = 0;
+  CK(cudaDeviceGetLimit(&stack, cudaLimitStackSize));
+  if (stack < 4096) CK(cudaDeviceSetLimit(cudaLimitStackSize, 4096));
+  int block = 256;
+  s.lu_in_smem = song2_smem_bytes(s, precision, block, 1) <= (size_t)smem_optin ? 1 : 0;
+  size_t smem = song2_smem_bytes(s, precision, block, s.lu_in_smem);
+  if (smem > (size_t)smem_optin) {
+    snprintf(err, SONG2_ERRLEN, "shared-memory plan %zu B exceeds the %d B limit", smem, smem_optin);
+    return 1;
+  }
+  size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
+  size_t per_team = na_align((size_t)s.lu_elems * sizeof(double)) + (s.lu_in_smem ? 0 : na_align((size_t)s.lu_elems * ts));
+  size_t teams_fit = (SONG2_NOALLOC_BYTES - fixed) / per_team;
+  if (teams_fit < 1) {
+    snprintf(err, SONG2_ERRLEN, "iteration-matrix scratch of %zu B per triplet does not fit in the %zu B scratch",
+             per_team, (size_t)SONG2_NOALLOC_BYTES - fixed);
+    return 1;
+  }
+  int per_sm = song2_max_ctas_per_sm(precision, 0, block, smem);
+  if (per_sm < 1) {
+    snprintf(err, SONG2_ERRLEN, "launch configuration does not fit on an SM");
+    return 1;
+  }
+  int grid = std::max(1, std::min(s.n_items, nsm * per_sm));
+  grid = (int)std::min<size_t>((size_t)grid, teams_fit);
+  size_t o_jac = take((size_t)grid * s.lu_elems * sizeof(double));
+  size_t o_lu = s.lu_in_smem ? 0 : take((size_t)grid * s.lu_elems * ts);
+
+  auto put = [&](size_t o, const void *src, size_t bytes) -> cudaError_t {
+    return bytes ? cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
+  };
+  CK(put(o_k, spec->k, sizeof(double) * spec->k_size));
+  CK(put(o_k3, k3.data(), sizeof(double) * k3.size()));
+  CK(put(o_tau, spec->tau, sizeof(double) * spec->tau_size));
+  CK(put(o_k3off, k3_off.data(), sizeof(int) * k3_off.size()));
+  CK(put(o_k3sz, k3_size.data(), sizeof(int) * k3_size.size()));
+  CK(put(o_poff, pair_off.data(), sizeof(int64_t) * pair_off.size()));
+  CK(put(o_cm, H.cmin.data(), nc)); CK(put(o_cp, H.cplu.data(), nc)); CK(put(o_dm, H.dmin.data(), nc));
+  CK(put(o_dp, H.dplu.data(), nc)); CK(put(o_dz, H.dzer.data(), nc));
+  CK(put(o_esp, H.eq_sp.data(), ne)); CK(put(o_el, H.eq_l.data(), ne)); CK(put(o_em, H.eq_m.data(), ne));
+  CK(put(o_iI, H.idx_I.data(), ni)); CK(put(o_iE, H.idx_E.data(), ni)); CK(put(o_iB, H.idx_B.data(), ni));
+  CK(put(o_iN, H.idx_N.data(), ni));
+  CK(put(o_qsp, H.qs_sp.data(), nq)); CK(put(o_ql, H.qs_l.data(), nq)); CK(put(o_qm, H.qs_m.data(), nq));
+  CK(put(o_items, items.data(), sizeof(WorkItem) * items.size()));
+  /* the scratch keeps the previous call's contents: the work-queue counter and the
+     outputs (entries the sources never write, e.g. E with l < 2) must start at zero */
+  CK(cudaMemsetAsync(base + o_queue, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(sources_dev, 0, sizeof(double) * (size_t)s.tp2_size * s.per_type, st));
+
+  DevPtrs p;
+  memset(&p, 0, sizeof(p));
+  p.k = (const double *)(base + o_k);
+  p.k3 = (const double *)(base + o_k3);
+  p.tau = (const double *)(base + o_tau);
+  p.k3_off = (const int *)(base + o_k3off);
+  p.k3_size = (const int *)(base + o_k3sz);
+  p.pair_off = (const int64_t *)(base + o_poff);
+  p.bg = tab_dev->bg; p.bg_dd = tab_dev->bg_dd; p.fo = tab_dev->fo; p.fo_dd = tab_dev->fo_dd;
+  p.cmin = (const double *)(base + o_cm); p.cplu = (const double *)(base + o_cp);
+  p.dmin = (const double *)(base + o_dm); p.dplu = (const double *)(base + o_dp);
+  p.dzer = (const double *)(base + o_dz);
+  p.eq_sp = (const short *)(base + o_esp); p.eq_l = (const short *)(base + o_el); p.eq_m = (const short *)(base + o_em);
+  p.idx_I = (const short *)(base + o_iI); p.idx_E = (const short *)(base + o_iE);
+  p.idx_B = (const short *)(base + o_iB); p.idx_N = (const short *)(base + o_iN);
+  p.qs_sp = (const short *)(base + o_qsp); p.qs_l = (const short *)(base + o_ql); p.qs_m = (const short *)(base + o_qm);
+  p.items = (const WorkItem *)(base + o_items);
+  p.sources = sources_dev;
+  p.stats = stats_dev;
+  p.jac = (double *)(base + o_jac);
+  p.lu_global = s.lu_in_smem ? nullptr : (void *)(base + o_lu);
+  p.queue = (int *)(base + o_queue);
+  if (song2_launch_evolver(s, p, precision, 0, grid, block, smem, st)) {
+    snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return 1;
+  }
+  return 0;
+}
