@@ -334,7 +334,13 @@ typedef struct {
   int qs2_size, iq_g, iq_E, iq_B, iq_ur, iq_b, iq_cdm;
   int iq_psi, iq_psi_prime, iq_phi_prime_poisson, iq_phi_prime_longitudinal, iq_phi_prime_prime;
   int iq_omega_m1_prime, iq_gamma_m2_prime_prime, iq_vv_g, iq_vv_ur, iq_dd_b, iq_vv_b, iq_vv_cdm;
+  int iq_vvp_b, iq_vvp_cdm;
   double *qs, *qc;
+  /* quadratic-source table of the triplet on the first-order time nodes j0..j0+qt_n-1
+     (perturb2_quadratic_sources_for_k1k2k, perturbations2.c:10407-10606):
+     qtab[node][2][qs2_size] = values, spline second derivatives in ln tau */
+  double *qtab, *qt_c;
+  int qt_j0, qt_n, qt_ready;
   /* shared variables (perturb2_workspace_at_tau) */
   double I_00, N_00, N_1m[3], I_1m[3], I_2m[3], E_2m[3], B_2m[3], C_1m[3], b_200, b_22m[3], cdm_200, cdm_22m[3];
   double I_1m_tca1[3], I_2m_tca1[3], E_2m_tca1[3], B_2m_tca1[3], C_1m_tca1[3], Pi_tca1[3];
@@ -391,9 +397,15 @@ static ws_t *ws_alloc(cfg_t *c) {
   w->iq_psi = q++; w->iq_psi_prime = q++; w->iq_phi_prime_poisson = q++; w->iq_phi_prime_longitudinal = q++;
   w->iq_phi_prime_prime = q++; w->iq_omega_m1_prime = q++; w->iq_gamma_m2_prime_prime = q++;
   w->iq_vv_g = q++; w->iq_vv_ur = q++; w->iq_dd_b = q++; w->iq_vv_b = q++; w->iq_vv_cdm = q++;
+  w->iq_vvp_b = q++; w->iq_vvp_cdm = q++;
   w->qs2_size = q;
   w->qs = (double *)calloc((size_t)q, sizeof(double));
   w->qc = (double *)calloc((size_t)q, sizeof(double));
+  {
+    int nn = c->t ? (c->t->fo_tau_size > 2 ? c->t->fo_tau_size : 2) : 2;
+    w->qtab = (double *)calloc((size_t)nn * 2 * q, sizeof(double));
+    w->qt_c = (double *)calloc((size_t)nn, sizeof(double));
+  }
   int nmax = 4 * size_l_indexm(c, c->L_big) + 2 * nlm_hier_b(c) + 8;
   w->nmax = nmax;
   w->J = (double *)calloc((size_t)nmax * nmax, sizeof(double));
@@ -417,7 +429,7 @@ static void ws_free(ws_t *w) {
 #define F1(x) free(w->x);
   RLIST(F1) CLIST(F1)
 #undef F1
-  free(w->fo1); free(w->fo2); free(w->qs); free(w->qc);
+  free(w->fo1); free(w->fo2); free(w->qs); free(w->qc); free(w->qtab); free(w->qt_c);
   free(w->J); free(w->M); free(w->dif); free(w->ytmp); free(w->dytmp); free(w->rhs); free(w->del);
   free(w->invwt); free(w->psiv); free(w->difkp1); free(w->ynew); free(w->ylin); free(w->dylin); free(w->piv);
   free(w);
@@ -906,12 +918,17 @@ static void quadratic_sources(ws_t *w, int what) {
       if (what == QS_WHAT_TOTAL) w->qs[q] += w->qc[q];
     }
   }
-  /* products needed later (perturbations2.c:11795-11809) */
-  w->qs[w->iq_vv_g] = fo1[SONG2_FO_V_G] * fo2[SONG2_FO_V_G];
-  w->qs[w->iq_vv_ur] = fo1[SONG2_FO_V_UR] * fo2[SONG2_FO_V_UR];
-  w->qs[w->iq_dd_b] = delta_b_1 * delta_b_2;
-  w->qs[w->iq_vv_b] = vpot_b_1 * vpot_b_2;
-  w->qs[w->iq_vv_cdm] = vpot_cdm_1 * vpot_cdm_2;
+  /* products needed later (perturbations2.c:11795-11809), and the time derivatives
+     of the velocity products used by psi' (perturbations2.c:10312-10340) */
+  if (what == QS_WHAT_TOTAL) {
+    w->qs[w->iq_vv_g] = fo1[SONG2_FO_V_G] * fo2[SONG2_FO_V_G];
+    w->qs[w->iq_vv_ur] = fo1[SONG2_FO_V_UR] * fo2[SONG2_FO_V_UR];
+    w->qs[w->iq_dd_b] = delta_b_1 * delta_b_2;
+    w->qs[w->iq_vv_b] = vpot_b_1 * vpot_b_2;
+    w->qs[w->iq_vv_cdm] = vpot_cdm_1 * vpot_cdm_2;
+    w->qs[w->iq_vvp_b] = fo1[SONG2_FO_V_B_P] * vpot_b_2 + vpot_b_1 * fo2[SONG2_FO_V_B_P];
+    w->qs[w->iq_vvp_cdm] = fo1[SONG2_FO_V_CDM_P] * vpot_cdm_2 + vpot_cdm_1 * fo2[SONG2_FO_V_CDM_P];
+  }
 }
 
 /* ======================================================= workspace at tau */
@@ -1107,11 +1124,10 @@ static double compute_psi_prime(ws_t *w, const double *y, const double *dy) {
     rho_quadrupole_prime = rho_g * dI_20;
   }
   rho_plus_3p_quadrupole += rho_b * w->b_22m[0];
-  double db_220 = 15 * w->k1_ten_k2[2] * (fo1[SONG2_FO_V_B_P] * fo2[SONG2_FO_V_B] + fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B_P]);
+  double db_220 = 15 * w->k1_ten_k2[2] * w->qs[w->iq_vvp_b];
   rho_quadrupole_prime += rho_b * db_220;
   rho_plus_3p_quadrupole += rho_cdm * w->cdm_22m[0];
-  double dcdm_220 =
-      15 * w->k1_ten_k2[2] * (fo1[SONG2_FO_V_CDM_P] * fo2[SONG2_FO_V_CDM] + fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM_P]);
+  double dcdm_220 = 15 * w->k1_ten_k2[2] * w->qs[w->iq_vvp_cdm];
   rho_quadrupole_prime += rho_cdm * dcdm_220;
   rho_plus_3p_quadrupole += 2 * rho_ur * N(2, 0);
   rho_quadrupole_prime += rho_ur * dN(2, 0);
@@ -1130,6 +1146,106 @@ static void prepare_tau(ws_t *w, double tau) {
   background_at_tau(w, tau);
   first_order_at_tau(w, tau);
   quadratic_sources(w, QS_WHAT_TOTAL);
+}
+
+/* The reference's derivs path (perturb2_quadratic_sources_at_tau,
+   perturbations2.c:14366-14688): quadratic sources by cubic-spline interpolation
+   of the triplet's table; during tight coupling the collision terms are computed
+   directly from the interpolated first-order quantities, as perturb2_tca_variables
+   does (perturbations2.c:9440-9456). */
+static void prepare_tau_table(ws_t *w, double tau) {
+  cfg_t *c = w->c;
+  const song2_tables *t = c->t;
+  background_at_tau(w, tau);
+  if (w->linear_only || c->first_order_mode || !c->s->has_quadratic_sources || !w->qt_ready) {
+    memset(w->qs, 0, sizeof(double) * w->qs2_size);
+    memset(w->qc, 0, sizeof(double) * w->qs2_size);
+    memset(w->fo1, 0, sizeof(double) * c->nfo);
+    memset(w->fo2, 0, sizeof(double) * c->nfo);
+    return;
+  }
+  double x = log(tau), dx = t->fo_dlntau;
+  double u = (x - t->fo_lntau0) / dx;
+  int i = (int)floor(u);
+  if (i < w->qt_j0) i = w->qt_j0;
+  if (i > w->qt_j0 + w->qt_n - 2) i = w->qt_j0 + w->qt_n - 2;
+  double b = u - i, a = 1.0 - b;
+  double ca = (a * a * a - a) * (dx * dx) / 6.0, cb = (b * b * b - b) * (dx * dx) / 6.0;
+  int nq = w->qs2_size;
+  const double *r0 = w->qtab + (size_t)(i - w->qt_j0) * 2 * nq, *r1 = r0 + 2 * nq;
+  for (int q = 0; q < nq; ++q) w->qs[q] = a * r0[q] + b * r1[q] + ca * r0[nq + q] + cb * r1[nq + q];
+  if (w->pv.tca) {
+    first_order_at_tau(w, tau);
+    quadratic_sources(w, QS_WHAT_COLLISION);
+  } else {
+    memset(w->qc, 0, sizeof(double) * w->qs2_size);
+  }
+}
+
+/* Quadratic sources of the triplet at the first-order nodes covering
+   [tau_ini, tau_end] (exact first-order values at the nodes, background by
+   spline), then natural cubic splines in ln tau (perturbations2.c:10407-10606). */
+static void build_qs_table(ws_t *w, double tau_ini, double tau_end) {
+  cfg_t *c = w->c;
+  const song2_tables *t = c->t;
+  w->qt_ready = 0;
+  if (c->first_order_mode || !c->s->has_quadratic_sources) return;
+  int N = t->fo_tau_size;
+  double x0 = t->fo_lntau0, dx = t->fo_dlntau;
+  int j0 = (int)floor((log(tau_ini) - x0) / dx);
+  int j1 = (int)ceil((log(tau_end) - x0) / dx);
+  if (j0 < 0) j0 = 0;
+  if (j0 > N - 2) j0 = N - 2;
+  if (j1 > N - 1) j1 = N - 1;
+  if (j1 < j0 + 1) j1 = j0 + 1;
+  int M = j1 - j0 + 1, nq = w->qs2_size;
+  w->qt_j0 = j0;
+  w->qt_n = M;
+  size_t stride = (size_t)t->fo_tau_size * t->fo_size;
+  const double *v1 = t->fo + stride * w->index_k1, *v2 = t->fo + stride * w->index_k2;
+  for (int j = 0; j < M; ++j) {
+    double x = x0 + (j0 + j) * dx;
+    /* background at the node */
+    double tau = exp(x);
+#define BGX(qq) spl(t->bg_size, SONG2_BG_SIZE, t->bg_lntau0, t->bg_dlntau, t->bg, t->bg_dd, (qq), x)
+    w->a = exp(BGX(SONG2_BG_LN_A));
+    w->a_sq = w->a * w->a;
+    w->Hc = exp(BGX(SONG2_BG_LN_HC));
+    w->Hc_prime = BGX(SONG2_BG_HC_PRIME_TAU2) / (tau * tau);
+    w->rho_g = exp(BGX(SONG2_BG_LN_RHO_G));
+    w->rho_b = exp(BGX(SONG2_BG_LN_RHO_B));
+    w->rho_cdm = exp(BGX(SONG2_BG_LN_RHO_CDM));
+    w->rho_ur = exp(BGX(SONG2_BG_LN_RHO_UR));
+    w->kappa_dot = exp(BGX(SONG2_BG_LN_KAPPA_DOT));
+    w->exp_m_kappa = exp(-BGX(SONG2_BG_KAPPA));
+#undef BGX
+    w->g = w->kappa_dot * w->exp_m_kappa;
+    w->r = w->rho_g / w->rho_b;
+    memcpy(w->fo1, v1 + (size_t)(j0 + j) * t->fo_size, sizeof(double) * c->nfo);
+    memcpy(w->fo2, v2 + (size_t)(j0 + j) * t->fo_size, sizeof(double) * c->nfo);
+    quadratic_sources(w, QS_WHAT_TOTAL);
+    memcpy(w->qtab + (size_t)j * 2 * nq, w->qs, sizeof(double) * nq);
+  }
+  /* natural spline, column by column (same recurrence as song2_spline_uniform) */
+  for (int q = 0; q < nq; ++q) {
+    double prev = 0.0, cprev = 0.0;
+    w->qtab[nq + q] = 0.0;
+    for (int j = 1; j < M - 1; ++j) {
+      double ym = w->qtab[(size_t)(j - 1) * 2 * nq + q], y0 = w->qtab[(size_t)j * 2 * nq + q];
+      double yp = w->qtab[(size_t)(j + 1) * 2 * nq + q];
+      double r = 6.0 * (yp - 2.0 * y0 + ym) / (dx * dx);
+      double bb = 4.0 - cprev;
+      double ci = 1.0 / bb;
+      prev = (r - prev) / bb;
+      w->qtab[(size_t)j * 2 * nq + nq + q] = prev;
+      w->qt_c[j] = ci;
+      cprev = ci;
+    }
+    w->qtab[(size_t)(M - 1) * 2 * nq + nq + q] = 0.0;
+    for (int j = M - 2; j >= 1; --j)
+      w->qtab[(size_t)j * 2 * nq + nq + q] -= w->qt_c[j] * w->qtab[(size_t)(j + 1) * 2 * nq + nq + q];
+  }
+  w->qt_ready = 1;
 }
 
 static void derivs_prepared(ws_t *w, double tau, const double *y, double *dy) {
@@ -1288,7 +1404,7 @@ static void derivs_prepared(ws_t *w, double tau, const double *y, double *dy) {
 }
 
 static void derivs(ws_t *w, double tau, const double *y, double *dy) {
-  prepare_tau(w, tau);
+  prepare_tau_table(w, tau);
   derivs_prepared(w, tau, y, dy);
 }
 
@@ -1985,6 +2101,7 @@ static int solve_triplet(ws_t *w, const double *tout, int nout, output_fn out, d
   } else {
     lim[1] = tau_end;
   }
+  build_qs_table(w, tau_ini, tau_end);
   int jout = 0;
   for (int iv = 0; iv < nint; ++iv) {
     int tca = (iv == 0) ? tca0 : 0;
@@ -1996,8 +2113,9 @@ static int solve_triplet(ws_t *w, const double *tout, int nout, output_fn out, d
       pv_t old = w->pv;
       double *yold = w->ytmp;
       memcpy(yold, ybuf, sizeof(double) * old.n);
-      /* TCA quantities at the switching time, from the old vector */
-      prepare_tau(w, lim[iv]);
+      /* TCA quantities at the switching time, from the old vector, evaluated as in
+         derivs (the reference takes them from the last derivs call) */
+      prepare_tau_table(w, lim[iv]);
       workspace_at_tau(w, yold);
       double I1[3], I2[3], E2[3], B2[3];
       memcpy(I1, w->I_1m_tca1, sizeof(I1));

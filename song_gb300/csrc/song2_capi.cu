@@ -185,6 +185,8 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   s.iq_dd_b = q; push_q(SP_METRIC, 0, 0);
   s.iq_vv_b = q; push_q(SP_METRIC, 0, 0);
   s.iq_vv_cdm = q; push_q(SP_METRIC, 0, 0);
+  s.iq_vvp_b = q; push_q(SP_METRIC, 0, 0);
+  s.iq_vvp_cdm = q; push_q(SP_METRIC, 0, 0);
   s.qs2_size = q;
 
   /* state vector, grouped in m blocks */
@@ -472,6 +474,21 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
      blocks when they do not fit in shared memory. */
   if (alloc_dev(c, (size_t)c->n_teams * s.lu_elems * sizeof(double), &tmp, err)) return 1;
   p.jac = (double *)tmp;
+  /* quadratic-source tables of the resident triplets, and the spline recurrence */
+  if (s.has_qs) {
+    if (alloc_dev(c, (size_t)c->n_teams * s.fo_tau_size * 2 * s.qs2_size * sizeof(double), &tmp, err)) return 1;
+    p.qtab = (double *)tmp;
+  }
+  {
+    std::vector<double> cs(std::max(2, s.fo_tau_size + 1), 0.0);
+    double cprev = 0.0;
+    for (size_t j = 1; j < cs.size(); ++j) {
+      double bb = 4.0 - cprev;
+      cs[j] = 1.0 / bb;
+      cprev = cs[j];
+    }
+    if (upload(c, cs, &p.spl_c, st, err)) return 1;
+  }
   if (!s.lu_in_smem) {
     size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
     if (alloc_dev(c, (size_t)c->n_teams * s.lu_elems * ts, &tmp, err)) return 1;
@@ -880,6 +897,9 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   size_t o_qsp = take(nq), o_ql = take(nq), o_qm = take(nq);
   size_t o_items = take(sizeof(WorkItem) * items.size());
   size_t o_queue = take(sizeof(int));
+  std::vector<double> cs(std::max(2, s.fo_tau_size + 1), 0.0);
+  for (size_t j = 1; j < cs.size(); ++j) cs[j] = 1.0 / (4.0 - cs[j - 1]);
+  size_t o_splc = take(sizeof(double) * cs.size());
   size_t fixed = off;
   if (fixed > SONG2_NOALLOC_BYTES) {
     snprintf(err, SONG2_ERRLEN, "problem tables need %zu B, more than the %zu B scratch", fixed,
@@ -900,10 +920,12 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
     return 1;
   }
   size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
-  size_t per_team = na_align((size_t)s.lu_elems * sizeof(double)) + (s.lu_in_smem ? 0 : na_align((size_t)s.lu_elems * ts));
+  size_t qtab_team = s.has_qs ? (size_t)s.fo_tau_size * 2 * s.qs2_size * sizeof(double) : 0;
+  size_t per_team = na_align((size_t)s.lu_elems * sizeof(double)) + (s.lu_in_smem ? 0 : na_align((size_t)s.lu_elems * ts)) +
+                    na_align(qtab_team);
   size_t teams_fit = (SONG2_NOALLOC_BYTES - fixed) / per_team;
   if (teams_fit < 1) {
-    snprintf(err, SONG2_ERRLEN, "iteration-matrix scratch of %zu B per triplet does not fit in the %zu B scratch",
+    snprintf(err, SONG2_ERRLEN, "per-triplet scratch of %zu B (iteration matrices, source table) does not fit in the %zu B scratch",
              per_team, (size_t)SONG2_NOALLOC_BYTES - fixed);
     return 1;
   }
@@ -916,6 +938,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   grid = (int)std::min<size_t>((size_t)grid, teams_fit);
   size_t o_jac = take((size_t)grid * s.lu_elems * sizeof(double));
   size_t o_lu = s.lu_in_smem ? 0 : take((size_t)grid * s.lu_elems * ts);
+  size_t o_qtab = s.has_qs ? take((size_t)grid * qtab_team) : 0;
 
   auto put = [&](size_t o, const void *src, size_t bytes) -> cudaError_t {
     return bytes ? cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
@@ -933,6 +956,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   CK(put(o_iN, H.idx_N.data(), ni));
   CK(put(o_qsp, H.qs_sp.data(), nq)); CK(put(o_ql, H.qs_l.data(), nq)); CK(put(o_qm, H.qs_m.data(), nq));
   CK(put(o_items, items.data(), sizeof(WorkItem) * items.size()));
+  CK(put(o_splc, cs.data(), sizeof(double) * cs.size()));
   /* the scratch keeps the previous call's contents: the work-queue counter and the
      outputs (entries the sources never write, e.g. E with l < 2) must start at zero */
   CK(cudaMemsetAsync(base + o_queue, 0, sizeof(int), st));
@@ -959,6 +983,8 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   p.stats = stats_dev;
   p.jac = (double *)(base + o_jac);
   p.lu_global = s.lu_in_smem ? nullptr : (void *)(base + o_lu);
+  p.qtab = s.has_qs ? (double *)(base + o_qtab) : nullptr;
+  p.spl_c = (const double *)(base + o_splc);
   p.queue = (int *)(base + o_queue);
   if (song2_launch_evolver(s, p, precision, 0, grid, block, smem, st)) {
     snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));

@@ -45,6 +45,7 @@ struct DevSpec {
   int qs2_size, iq_g, iq_E, iq_B, iq_ur, iq_b, iq_cdm;
   int iq_psi, iq_psi_prime, iq_phi_prime_poisson, iq_phi_prime_longitudinal, iq_phi_prime_prime;
   int iq_omega_m1_prime, iq_gamma_m2_prime_prime, iq_vv_g, iq_vv_ur, iq_dd_b, iq_vv_b, iq_vv_cdm;
+  int iq_vvp_b, iq_vvp_cdm;        /* d/dtau of the velocity products (psi') */
   short iq_b11[2], iq_c11[2], iq_b000, iq_c000;
   /* state layout (grouped by m blocks) */
   int n;
@@ -88,7 +89,9 @@ struct DevPtrs {
   double *sources;                 /* [tp2][per_type] */
   double *fo_out;                  /* first-order mode: [k][tau][q] */
   song2_triplet_stats *stats;      /* [n_items] */
-  double *jac;                     /* per-CTA scratch: sum blk^2 doubles each */
+  double *jac;                     /* per-team scratch: sum blk^2 doubles each */
+  double *qtab;                    /* per-team quadratic-source table: fo_tau_size x 2 x qs2_size doubles */
+  const double *spl_c;             /* Thomas recurrence of the natural spline on a uniform grid */
   void *lu_global;                 /* per-CTA LU scratch when not in smem */
   int *queue;                      /* work-queue counter */
 };

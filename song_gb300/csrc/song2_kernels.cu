@@ -63,6 +63,7 @@ struct Shared {
   WS ws;
   double psi_prime;
   double lntau;
+  int qt_j0, qt_n;
   double red[32];
   double RU[5][5];
   double ctl[4];
@@ -131,6 +132,7 @@ struct K {
   int *piv;
   void *lu;
   double *jac;
+  double *qtab;
   __device__ K(const DevSpec &s_, const DevPtrs &p_, char *smem_all, int prec, int warp_team_) : s(s_), p(p_) {
     warp_team = warp_team_;
     Plan pl = make_plan(s_, prec, s_.lu_in_smem);
@@ -172,6 +174,7 @@ struct K {
     if (s_.lu_in_smem) lu = smem + pl.lu;
     else lu = (char *)p_.lu_global + (size_t)team * s_.lu_elems * ts;
     jac = p_.jac + (size_t)team * s_.lu_elems;
+    qtab = p_.qtab ? p_.qtab + (size_t)team * s_.fo_tau_size * 2 * s_.qs2_size : nullptr;
   }
   __device__ void sync() const {
     if (warp_team) __syncwarp();
@@ -503,6 +506,8 @@ __device__ void qs_metric(const K &c, const BgV &bg) {
   qs[s.iq_dd_b] = fo1[SONG2_FO_DELTA_B] * fo2[SONG2_FO_DELTA_B];
   qs[s.iq_vv_b] = fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B];
   qs[s.iq_vv_cdm] = fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM];
+  qs[s.iq_vvp_b] = fo1[SONG2_FO_V_B_P] * fo2[SONG2_FO_V_B] + fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B_P];
+  qs[s.iq_vvp_cdm] = fo1[SONG2_FO_V_CDM_P] * fo2[SONG2_FO_V_CDM] + fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM_P];
 }
 
 /* One entry of the quadratic-source vector: total (qs) and collisional (qc) part. */
@@ -554,6 +559,22 @@ __device__ void qs_entry(const K &c, const BgV &bg, int q) {
   c.qc[q] = cv;
 }
 
+/* Collision part only, the quantities perturb2_tca_variables takes directly
+   from the interpolated first-order solution (perturbations2.c:9440-9456). */
+__device__ void qc_entry(const K &c, const BgV &bg, int q) {
+  const DevSpec &s = c.s;
+  int sp = c.qs_sp[q], l = c.qs_l[q], m = c.qs_m[q];
+  double cv = 0.0;
+  if (s.has_coll) {
+    if (sp == SP_I) cv = coll_I(c, bg, l, m) * bg.kappa_dot;
+    else if (sp == SP_E && l >= 2) cv = coll_E(c, l, m) * bg.kappa_dot;
+    else if (sp == SP_B && l >= 2) cv = coll_B(c, l, m) * bg.kappa_dot;
+    else if (sp == SP_B000) cv = -bg.r * coll_I(c, bg, 0, 0) * bg.kappa_dot;
+    else if (sp == SP_B11) cv = -bg.r * coll_I(c, bg, 1, m) * bg.kappa_dot;
+  }
+  c.qc[q] = cv;
+}
+
 /* ------------------------------------------------------------------ prepare(tau) */
 
 /* Background, first-order quantities and quadratic sources at tau, block-wide.
@@ -590,6 +611,120 @@ __device__ void prepare(const K &c, double tau, int with_sources) {
   if (use_fo) {
     const BgV &bg = c.sh->bg;
     for (int q = tid; q < s.qs2_size; q += nt) qs_entry(c, bg, q);
+  }
+  c.sync();
+}
+
+/* The derivs path of the reference (perturb2_quadratic_sources_at_tau,
+   perturbations2.c:14366-14688): background by spline, quadratic sources by
+   cubic-spline interpolation of the triplet's table; in tight coupling also the
+   first-order quantities and the direct collision terms.  Ends with a barrier. */
+__device__ void prepare_table(const K &c, double tau, int tca) {
+  const DevSpec &s = c.s;
+  const Tri &t = c.sh->tri;
+  int tid = c.rank, nt = c.size;
+  if (tid == 0) c.sh->lntau = log(tau);
+  c.sync();
+  double x = c.sh->lntau;
+  if (tid < SONG2_BG_SIZE)
+    c.bgraw[tid] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, tid, x);
+  int use = s.has_qs && !s.mode_first_order && c.qtab;
+  if (use) {
+    double dx = s.fo_dlntau, u = (x - s.fo_lntau0) / dx;
+    int j0 = c.sh->qt_j0, n = c.sh->qt_n;
+    int i = (int)floor(u);
+    if (i < j0) i = j0;
+    if (i > j0 + n - 2) i = j0 + n - 2;
+    double b = u - i, a = 1.0 - b;
+    double ca = (a * a * a - a) * (dx * dx) / 6.0, cb = (b * b * b - b) * (dx * dx) / 6.0;
+    int nq = s.qs2_size;
+    const double *r0 = c.qtab + (size_t)(i - j0) * 2 * nq, *r1 = r0 + 2 * nq;
+    for (int q = tid; q < nq; q += nt) c.qs[q] = a * r0[q] + b * r1[q] + ca * r0[nq + q] + cb * r1[nq + q];
+    if (tca) {
+      size_t stride = (size_t)s.fo_tau_size * s.nfo;
+      for (int q = tid; q < 2 * s.nfo; q += nt) {
+        int which = q >= s.nfo, qq = which ? q - s.nfo : q;
+        int ik = which ? t.i2 : t.i1;
+        (which ? c.fo2 : c.fo1)[qq] =
+            spl(c.p.fo + stride * ik, c.p.fo_dd + stride * ik, s.fo_tau_size, s.nfo, s.fo_lntau0, s.fo_dlntau, qq, x);
+      }
+    }
+  } else {
+    for (int q = tid; q < s.qs2_size; q += nt) c.qs[q] = 0.0;
+  }
+  if (!(use && tca))
+    for (int q = tid; q < s.qs2_size; q += nt) c.qc[q] = 0.0;
+  c.sync();
+  if (tid == 0) bg_derive(c.bgraw, tau, c.sh->bg);
+  c.sync();
+  if (use && tca) {
+    const BgV &bg = c.sh->bg;
+    for (int q = tid; q < s.qs2_size; q += nt) qc_entry(c, bg, q);
+    c.sync();
+  }
+}
+
+/* Quadratic sources of the triplet at the first-order time nodes covering
+   [tau_ini, tau_end] (exact first-order values at the nodes, background by
+   spline) and their natural cubic splines in ln tau: the per-triplet table of
+   perturb2_quadratic_sources_for_k1k2k (perturbations2.c:10407-10606). */
+__device__ void build_qs_table(const K &c) {
+  const DevSpec &s = c.s;
+  Tri &t = c.sh->tri;
+  int tid = c.rank, nt = c.size;
+  if (!s.has_qs || s.mode_first_order || !c.qtab) return;
+  int N = s.fo_tau_size, nq = s.qs2_size;
+  double x0 = s.fo_lntau0, dx = s.fo_dlntau;
+  if (tid == 0) {
+    int j0 = (int)floor((log(t.tau_ini) - x0) / dx);
+    int j1 = (int)ceil((log(t.tau_end) - x0) / dx);
+    if (j0 < 0) j0 = 0;
+    if (j0 > N - 2) j0 = N - 2;
+    if (j1 > N - 1) j1 = N - 1;
+    if (j1 < j0 + 1) j1 = j0 + 1;
+    c.sh->qt_j0 = j0;
+    c.sh->qt_n = j1 - j0 + 1;
+  }
+  c.sync();
+  int j0 = c.sh->qt_j0, M = c.sh->qt_n;
+  size_t stride = (size_t)s.fo_tau_size * s.nfo;
+  const double *v1 = c.p.fo + stride * t.i1, *v2 = c.p.fo + stride * t.i2;
+  for (int j = 0; j < M; ++j) {
+    double x = x0 + (j0 + j) * dx;
+    if (tid < SONG2_BG_SIZE)
+      c.bgraw[tid] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, tid, x);
+    for (int q = tid; q < 2 * s.nfo; q += nt) {
+      int which = q >= s.nfo, qq = which ? q - s.nfo : q;
+      (which ? c.fo2 : c.fo1)[qq] = __ldg((which ? v2 : v1) + (size_t)(j0 + j) * s.nfo + qq);
+    }
+    c.sync();
+    if (tid == 0) bg_derive(c.bgraw, exp(x), c.sh->bg);
+    c.sync();
+    {
+      const BgV &bg = c.sh->bg;
+      for (int q = tid; q < nq; q += nt) qs_entry(c, bg, q);
+    }
+    c.sync();
+    double *row = c.qtab + (size_t)j * 2 * nq;
+    for (int q = tid; q < nq; q += nt) row[q] = c.qs[q];
+  }
+  c.sync();
+  /* natural spline per entry: Thomas sweeps along the nodes (same recurrence as
+     song2_spline_uniform; spl_c[j] = 1/(4 - spl_c[j-1])) */
+  for (int q = tid; q < nq; q += nt) {
+    double prev = 0.0;
+    c.qtab[nq + q] = 0.0;
+    for (int j = 1; j < M - 1; ++j) {
+      double ym = c.qtab[(size_t)(j - 1) * 2 * nq + q], y0 = c.qtab[(size_t)j * 2 * nq + q];
+      double yp = c.qtab[(size_t)(j + 1) * 2 * nq + q];
+      double r = 6.0 * (yp - 2.0 * y0 + ym) / (dx * dx);
+      double bb = 4.0 - __ldg(c.p.spl_c + j - 1);
+      prev = (r - prev) / bb;
+      c.qtab[(size_t)j * 2 * nq + nq + q] = prev;
+    }
+    c.qtab[(size_t)(M - 1) * 2 * nq + nq + q] = 0.0;
+    for (int j = M - 2; j >= 1; --j)
+      c.qtab[(size_t)j * 2 * nq + nq + q] -= __ldg(c.p.spl_c + j) * c.qtab[(size_t)(j + 1) * 2 * nq + nq + q];
   }
   c.sync();
 }
@@ -861,33 +996,36 @@ __device__ double row_h(const K &c, int tca, int i, const Y &y, const WS &w, int
 }
 
 
-/* Row i of dy = f(tau, y).  The phi' row is phi'' = (Einstein part) - Hc psi',
-   where psi' (perturb2_compute_psi_prime, perturbations2.c:10188-10383) needs the
-   I_20 and N_20 rows. */
+/* psi' given the time derivatives of the photon and neutrino quadrupoles
+   (perturb2_compute_psi_prime, perturbations2.c:10188-10383); in tight coupling
+   the photon quadrupole derivative is the TCA one. */
 template <class Y>
-__device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
+__device__ double psi_prime_of(const K &c, int tca, const Y &y, const WS &w, int lin, double dI20, double dN20) {
   const DevSpec &s = c.s;
-  if (c.eq_sp[i] != SP_PHIP) return row_h(c, tca, i, y, w, lin, tau);
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
   double k = t.k, kd = bg.kappa_dot, Hc = bg.Hc;
   int use_qs = !lin && s.has_qs;
-    /* phi'' = (einstein part) - Hc psi' (perturb2_compute_psi_prime, perturbations2.c:10188-10383) */
-    double dI20;
-    if (!tca) dI20 = row_h(c, tca, c.idx_I[c.LM(2, 0)], y, w, lin, tau);
-    else dI20 = 2 / 3. * k * w.I_1m_tca1[0] - kd * (w.I_2m_tca1[0] - w.Pi_tca1[0]) + (use_qs ? c.qs[s.iq_g + c.LM(2, 0)] : 0.0);
-    double dN20 = row_h(c, tca, c.idx_N[c.LM(2, 0)], y, w, lin, tau);
-    double rqp = bg.rho_g * dI20 + bg.rho_ur * dN20;
-    if (!lin) {
-      const double *fo1 = c.fo1, *fo2 = c.fo2;
-      rqp += bg.rho_b * 15 * t.k1_ten_k2[2] * (fo1[SONG2_FO_V_B_P] * fo2[SONG2_FO_V_B] + fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B_P]);
-      rqp += bg.rho_cdm * 15 * t.k1_ten_k2[2] *
-             (fo1[SONG2_FO_V_CDM_P] * fo2[SONG2_FO_V_CDM] + fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM_P]);
-    }
-    double psi_prime = w.phi_prime - 2 * Hc * (w.psi - y(s.idx_phi)) -
-                       3 / 5. * (bg.a_sq / t.k_sq) * (rqp + Hc * bg.rho_b * w.b_22m[0] + Hc * bg.rho_cdm * w.cdm_22m[0]) +
-                       (lin ? 0.0 : c.qs[s.iq_psi_prime]);
-    return w.phi_pp - Hc * psi_prime;
+  if (tca)
+    dI20 = 2 / 3. * k * w.I_1m_tca1[0] - kd * (w.I_2m_tca1[0] - w.Pi_tca1[0]) + (use_qs ? c.qs[s.iq_g + c.LM(2, 0)] : 0.0);
+  double rqp = bg.rho_g * dI20 + bg.rho_ur * dN20;
+  if (!lin) {
+    rqp += bg.rho_b * 15 * t.k1_ten_k2[2] * c.qs[s.iq_vvp_b];
+    rqp += bg.rho_cdm * 15 * t.k1_ten_k2[2] * c.qs[s.iq_vvp_cdm];
+  }
+  return w.phi_prime - 2 * Hc * (w.psi - y(s.idx_phi)) -
+         3 / 5. * (bg.a_sq / t.k_sq) * (rqp + Hc * bg.rho_b * w.b_22m[0] + Hc * bg.rho_cdm * w.cdm_22m[0]) +
+         (lin ? 0.0 : c.qs[s.iq_psi_prime]);
+}
+
+/* Row i of dy = f(tau, y).  The phi' row is phi'' = (Einstein part) - Hc psi',
+   where psi' needs the I_20 and N_20 rows. */
+template <class Y>
+__device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
+  if (c.eq_sp[i] != SP_PHIP) return row_h(c, tca, i, y, w, lin, tau);
+  double dI20 = tca ? 0.0 : row_h(c, tca, c.idx_I[c.LM(2, 0)], y, w, lin, tau);
+  double dN20 = row_h(c, tca, c.idx_N[c.LM(2, 0)], y, w, lin, tau);
+  return w.phi_pp - c.sh->bg.Hc * psi_prime_of(c, tca, y, w, lin, dI20, dN20);
 }
 
 /* dy = f(tau, y): block-wide; prepare(tau) must have run.  Ends with a barrier. */
@@ -1079,9 +1217,12 @@ __device__ void store_sources(const K &c, int index_tau, double tau, const doubl
   YVec yv{y};
   /* psi' from the phi' row: psi' = (phi_pp - dy[phi']) / Hc */
   if (c.rank == 0) {
-    const WS &w = c.sh->ws;
     double psi_prime = 0.0;
-    if (s.compute_m[0]) psi_prime = (w.phi_pp - dy[s.idx_phip]) / c.sh->bg.Hc;
+    if (s.compute_m[0]) {
+      int tca = c.sh->tca;
+      double dI20 = tca ? 0.0 : dy[c.idx_I[c.LM(2, 0)]], dN20 = dy[c.idx_N[c.LM(2, 0)]];
+      psi_prime = psi_prime_of(c, tca, yv, c.sh->ws, 0, dI20, dN20);
+    }
     c.sh->psi_prime = psi_prime;
   }
   c.sync();
@@ -1489,10 +1630,17 @@ __device__ int refactor(const K &c, double hinvGak, song2_triplet_stats &st) {
   return c.sh->lu_fail ? SONG2_E_SINGULAR : SONG2_OK;
 }
 
-/* output of one sampling time: y interpolated in c.yout */
+/* output of one sampling time: y interpolated in c.yout.  As in the reference,
+   dy comes from derivs (tabulated quadratic sources, perturbations2.c:7702-7718)
+   and the source functions from quadratic sources and workspace recomputed at
+   tau (perturb2_sources, perturbations2.c:11956-12030). */
 __device__ void do_output(const K &c, int jout, double to) {
+  int tca = c.sh->tca;
+  prepare_table(c, to, tca);
+  rhs(c, tca, to, c.yout, c.dyout);
   prepare(c, to, 1);
-  rhs(c, c.sh->tca, to, c.yout, c.dyout);
+  if (c.rank == 0) compute_ws(c, tca, YVec{c.yout}, 0, c.sh->ws);
+  c.sync();
   if (c.s.mode_first_order) store_first_order(c, jout, c.yout, c.dyout);
   else store_sources(c, jout, to, c.yout, c.dyout);
   c.sync();
@@ -1528,7 +1676,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
       }
       ++jout;
     }
-  prepare(c, t, 1);
+  prepare_table(c, t, tca);
   rhs(c, tca, t, y, f);
   st.n_rhs++;
   jacobian(c, tca, t);
@@ -1595,7 +1743,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
         }
         double minnrm = 100 * eps * block_max_bits(c, vm);
         double oldnrm = 0;
-        prepare(c, tnew, 1);
+        prepare_table(c, tnew, tca);
         for (int iter = 1; iter <= maxit; ++iter) {
           rhs(c, tca, tnew, ynew, f);
           st.n_rhs++;
@@ -1789,6 +1937,7 @@ template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_sta
   c.sync();
   if (c.sh->lu_fail) return SONG2_E_CONFIG;
   Tri &t = c.sh->tri;
+  build_qs_table(c);
   int jout = 0;
   for (int iv = 0; iv < t.nint; ++iv) {
     double ta = iv == 0 ? t.tau_ini : t.tau_switch;
@@ -1801,8 +1950,9 @@ template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_sta
       c.sync();
     } else {
       /* TCA -> full remap (perturbations2.c:7233-7285): the frozen moments take the
-         TCA values at the switching time; everything else carries over */
-      prepare(c, ta, 1);
+         TCA values at the switching time, evaluated as derivs does; everything
+         else carries over */
+      prepare_table(c, ta, 1);
       if (tid == 0) {
         YVec yv{c.y};
         compute_ws(c, 1, yv, 0, c.sh->ws);
