@@ -151,10 +151,13 @@ typedef struct {
 typedef struct song2_ctx song2_ctx;
 
 /* Launch configuration of the persistent evolver.  A "team" evolves one
-   triplet: one CTA of threads_per_team threads (warp_team = 0) or one warp
-   (warp_team = 1, teams_per_cta warps per CTA).  lu_in_smem keeps the
-   iteration-matrix blocks in shared memory instead of an L2-resident global
-   scratch.  Zeros everywhere mean "choose automatically". */
+   triplet: one CTA of threads_per_team threads (warp_team = 0), one warp
+   (warp_team = 1, teams_per_cta warps per CTA), or threads_per_team lanes of a
+   warp (warp_team = 2: 1, 2, 4, ... 32 lanes, the 32/threads_per_team teams of a
+   warp interleaved in global memory so that they advance side by side;
+   teams_per_cta is rounded to whole warps, at most four).  lu_in_smem keeps the
+   iteration-matrix blocks in shared memory instead of a global scratch (modes 0
+   and 1).  Zeros everywhere mean "choose automatically". */
 typedef struct {
   int warp_team;
   int teams_per_cta;

@@ -59,7 +59,7 @@ int size_l_indexm(int l_max, const int *m, int m_size) {
 
 struct HostLayout {
   DevSpec s;
-  std::vector<short> eq_sp, eq_l, eq_m, idx_I, idx_E, idx_B, idx_N, qs_sp, qs_l, qs_m;
+  std::vector<short> eq_sp, eq_l, eq_m, idx_I, idx_E, idx_B, idx_N, qs_sp, qs_l, qs_m, row_slot, qs_slot;
   std::vector<double> cmin, cplu, dmin, dplu, dzer;
 };
 
@@ -233,6 +233,29 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   }
   s.lu_elems = off;
 
+  /* evaluation order of the rows and of the quadratic-source entries: grouped by
+     species (I, E, B, N, the rest), each group padded to whole warps, so that the
+     threads of a warp run one code path */
+  auto slots = [](const std::vector<short> &sp_of, std::vector<short> &out) {
+    const int cls_sp[4] = {SP_I, SP_E, SP_B, SP_N};
+    out.clear();
+    for (int g = 0; g < 5; ++g) {
+      size_t start = out.size();
+      for (size_t i = 0; i < sp_of.size(); ++i) {
+        int sp_ = sp_of[i];
+        int cls = 4;
+        for (int u = 0; u < 4; ++u)
+          if (sp_ == cls_sp[u]) cls = u;
+        if (cls == g) out.push_back((short)i);
+      }
+      while ((out.size() - start) % 32) out.push_back(-1);
+    }
+  };
+  slots(H.eq_sp, H.row_slot);
+  slots(H.qs_sp, H.qs_slot);
+  s.n_row_slots = (int)H.row_slot.size();
+  s.n_qs_slots = (int)H.qs_slot.size();
+
   /* coupling tables for l <= Lq */
   H.cmin.assign((size_t)s.n_lm * 3, 0.0); H.cplu = H.cmin; H.dmin = H.cmin; H.dplu = H.cmin; H.dzer = H.cmin;
   for (int l = 0; l <= s.Lq; ++l)
@@ -384,7 +407,19 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     L.threads_per_team = 256;
     L.lu_in_smem = 0;
   }
-  if (L.warp_team) {
+  if (L.warp_team == 2) {
+    /* G lanes per triplet: G a power of two up to 32, whole warps per CTA, at most
+       four warps per CTA */
+    int G = 1;
+    while (G < L.threads_per_team && G < 32) G <<= 1;
+    L.threads_per_team = G;
+    int per_warp = 32 / G;
+    int warps = (L.teams_per_cta + per_warp - 1) / per_warp;
+    warps = std::max(1, std::min(4, warps));
+    L.teams_per_cta = warps * per_warp;
+    L.lu_in_smem = 0;
+    c->block = 32 * warps;
+  } else if (L.warp_team) {
     if (L.teams_per_cta < 1) L.teams_per_cta = 4;
     if (L.teams_per_cta > 8) L.teams_per_cta = 8;
     L.threads_per_team = 32;
@@ -398,7 +433,9 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   size_t with_lu = song2_smem_bytes(s, precision, c->block, 1) * L.teams_per_cta;
   if (L.lu_in_smem && with_lu > (size_t)smem_optin) L.lu_in_smem = 0;
   s.lu_in_smem = L.lu_in_smem;
-  c->smem = song2_smem_bytes(s, precision, c->block, s.lu_in_smem) * L.teams_per_cta;
+  s.team_lanes = L.warp_team == 2 ? L.threads_per_team : 0;
+  if (L.warp_team == 2) c->smem = song2_team_smem_bytes(s, L.teams_per_cta);
+  else c->smem = song2_smem_bytes(s, precision, c->block, s.lu_in_smem) * L.teams_per_cta;
   if (c->smem > (size_t)smem_optin) {
     snprintf(err, SONG2_ERRLEN, "shared-memory plan %zu B exceeds the %d B limit", c->smem, smem_optin);
     return 1;
@@ -454,6 +491,7 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     return 1;
   if (upload(c, H.qs_sp, &p.qs_sp, st, err) || upload(c, H.qs_l, &p.qs_l, st, err) || upload(c, H.qs_m, &p.qs_m, st, err))
     return 1;
+  if (upload(c, H.row_slot, &p.row_slot, st, err) || upload(c, H.qs_slot, &p.qs_slot, st, err)) return 1;
   if (upload(c, items, &p.items, st, err)) return 1;
   if (!first_order_mode) {
     c->sources_len = (size_t)s.tp2_size * per_type;
@@ -493,6 +531,16 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
     if (alloc_dev(c, (size_t)c->n_teams * s.lu_elems * ts, &tmp, err)) return 1;
     p.lu_global = tmp;
+  }
+  if (L.warp_team == 2) {
+    /* team kernel: vectors, solve vectors and pivots of every resident team */
+    size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
+    if (alloc_dev(c, (size_t)c->n_teams * song2_team_slab_doubles(s) * sizeof(double), &tmp, err)) return 1;
+    p.tslab = (double *)tmp;
+    if (alloc_dev(c, (size_t)c->n_teams * s.n * ts, &tmp, err)) return 1;
+    p.txsol = tmp;
+    if (alloc_dev(c, (size_t)c->n_teams * s.n * sizeof(int), &tmp, err)) return 1;
+    p.tpiv = (int *)tmp;
   }
   if (alloc_dev(c, sizeof(int), &tmp, err)) return 1;
   c->d_queue = (int *)tmp;
@@ -895,6 +943,8 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   size_t o_esp = take(ne), o_el = take(ne), o_em = take(ne);
   size_t o_iI = take(ni), o_iE = take(ni), o_iB = take(ni), o_iN = take(ni);
   size_t o_qsp = take(nq), o_ql = take(nq), o_qm = take(nq);
+  size_t nrs = sizeof(short) * H.row_slot.size(), nqs = sizeof(short) * H.qs_slot.size();
+  size_t o_rsl = take(nrs), o_qsl = take(nqs);
   size_t o_items = take(sizeof(WorkItem) * items.size());
   size_t o_queue = take(sizeof(int));
   std::vector<double> cs(std::max(2, s.fo_tau_size + 1), 0.0);
@@ -955,6 +1005,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   CK(put(o_iI, H.idx_I.data(), ni)); CK(put(o_iE, H.idx_E.data(), ni)); CK(put(o_iB, H.idx_B.data(), ni));
   CK(put(o_iN, H.idx_N.data(), ni));
   CK(put(o_qsp, H.qs_sp.data(), nq)); CK(put(o_ql, H.qs_l.data(), nq)); CK(put(o_qm, H.qs_m.data(), nq));
+  CK(put(o_rsl, H.row_slot.data(), nrs)); CK(put(o_qsl, H.qs_slot.data(), nqs));
   CK(put(o_items, items.data(), sizeof(WorkItem) * items.size()));
   CK(put(o_splc, cs.data(), sizeof(double) * cs.size()));
   /* the scratch keeps the previous call's contents: the work-queue counter and the
@@ -978,6 +1029,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   p.idx_I = (const short *)(base + o_iI); p.idx_E = (const short *)(base + o_iE);
   p.idx_B = (const short *)(base + o_iB); p.idx_N = (const short *)(base + o_iN);
   p.qs_sp = (const short *)(base + o_qsp); p.qs_l = (const short *)(base + o_ql); p.qs_m = (const short *)(base + o_qm);
+  p.row_slot = (const short *)(base + o_rsl); p.qs_slot = (const short *)(base + o_qsl);
   p.items = (const WorkItem *)(base + o_items);
   p.sources = sources_dev;
   p.stats = stats_dev;

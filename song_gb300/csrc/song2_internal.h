@@ -46,6 +46,7 @@ struct DevSpec {
   int iq_psi, iq_psi_prime, iq_phi_prime_poisson, iq_phi_prime_longitudinal, iq_phi_prime_prime;
   int iq_omega_m1_prime, iq_gamma_m2_prime_prime, iq_vv_g, iq_vv_ur, iq_dd_b, iq_vv_b, iq_vv_cdm;
   int iq_vvp_b, iq_vvp_cdm;        /* d/dtau of the velocity products (psi') */
+  int n_row_slots, n_qs_slots;     /* species-grouped, warp-padded evaluation orders */
   short iq_b11[2], iq_c11[2], iq_b000, iq_c000;
   /* state layout (grouped by m blocks) */
   int n;
@@ -64,6 +65,8 @@ struct DevSpec {
   int64_t per_type;
   int k_size;
   int n_items;
+  /* launch: lanes per triplet of the team kernel (1..32) */
+  int team_lanes;
   /* shared-memory plan */
   int lu_in_smem;
   int lu_elems;                    /* sum of blk_size^2 */
@@ -85,6 +88,7 @@ struct DevPtrs {
   const short *eq_sp, *eq_l, *eq_m;                  /* [n] */
   const short *idx_I, *idx_E, *idx_B, *idx_N;        /* [n_lm] -> state index or -1 */
   const short *qs_sp, *qs_l, *qs_m;                  /* [qs2_size] */
+  const short *row_slot, *qs_slot;                   /* [n_row_slots], [n_qs_slots]: index or -1 */
   const WorkItem *items;
   double *sources;                 /* [tp2][per_type] */
   double *fo_out;                  /* first-order mode: [k][tau][q] */
@@ -92,16 +96,23 @@ struct DevPtrs {
   double *jac;                     /* per-team scratch: sum blk^2 doubles each */
   double *qtab;                    /* per-team quadratic-source table: fo_tau_size x 2 x qs2_size doubles */
   const double *spl_c;             /* Thomas recurrence of the natural spline on a uniform grid */
-  void *lu_global;                 /* per-CTA LU scratch when not in smem */
+  void *lu_global;                 /* per-team LU scratch when not in smem */
+  double *tslab;                   /* team kernel: per-team vectors, 32/G teams interleaved per warp */
+  void *txsol;                     /* team kernel: solve vectors (iteration-matrix precision) */
+  int *tpiv;                       /* team kernel: pivots */
   int *queue;                      /* work-queue counter */
 };
 
-/* host-side launcher implemented in song2_kernels.cu */
-/* warp_team = 1: one warp per triplet (several per CTA); 0: one CTA per triplet */
-int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int warp_team, int grid, int block,
+/* host-side launcher implemented in song2_kernels.cu.  mode 0: one CTA per
+   triplet; 1: one warp per triplet (several per CTA); 2: spec.team_lanes lanes per
+   triplet, arrays in global slabs (tslab, txsol, tpiv, jac, lu_global, qtab). */
+int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int mode, int grid, int block,
                          size_t smem, cudaStream_t stream);
 /* shared memory of one team (one CTA in block mode, one warp in warp mode) */
 size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in_smem);
-int song2_max_ctas_per_sm(int precision, int warp_team, int block, size_t smem);
+/* shared memory of a team-kernel CTA, and the doubles of one team's slab */
+size_t song2_team_smem_bytes(const DevSpec &spec, int teams_per_cta);
+int song2_team_slab_doubles(const DevSpec &spec);
+int song2_max_ctas_per_sm(int precision, int mode, int block, size_t smem);
 
 #endif

@@ -65,10 +65,11 @@ struct Shared {
   double lntau;
   int qt_j0, qt_n;
   double red[32];
-  double RU[5][5];
+  double RU[5][5], Rm[5][5];
   double ctl[4];
   int item;
   int lu_fail;
+  float gjp[S2_MAXBLK];    /* Gauss-Jordan: reciprocal pivot of each block */
   int tca;
 };
 
@@ -108,7 +109,7 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
      loops index them per thread, which the constant bank would serialise */
   p.tab = o;
   o = al(o + sizeof(short) * ((size_t)(s.Lq + 1) * (SONG2_MAX_M + SONG2_MAX_M + 2) + SONG2_MAX_M + 3 * n +
-                              4 * (size_t)s.n_lm + 3 * (size_t)s.qs2_size));
+                              4 * (size_t)s.n_lm + 3 * (size_t)s.qs2_size + s.n_row_slots + s.n_qs_slots));
   size_t ts = prec == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
   p.xsol = o; o = al(o + n * ts);
   p.piv = o; o = al(o + n * sizeof(int));
@@ -120,83 +121,194 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
 
 /* ------------------------------------------------------------------ context */
 
-struct K {
+/* A team solves one triplet.  MODE_BLOCK: the CTA; MODE_WARP: one warp; MODE_TEAM:
+   G lanes of a warp (G = 1, 2, 4, ... 32), the 32/G teams of a warp interleaved in
+   global slabs so that the same element of every team is one coalesced access. */
+enum { MODE_BLOCK = 0, MODE_WARP = 1, MODE_TEAM = 2 };
+
+/* per-team array: element i at p[i] (the team owns the array) or p[i * T] (T teams
+   interleaved) */
+template <typename E, int STRIDED> struct View;
+template <typename E> struct View<E, 0> {
+  E *p;
+  __device__ E &operator[](int i) const { return p[i]; }
+  __device__ View operator+(int o) const { return View{p + o}; }
+};
+template <typename E> struct View<E, 1> {
+  E *p;
+  int T;
+  __device__ E &operator[](int i) const { return p[(long)i * T]; }
+  __device__ View operator+(int o) const { return View{p + (long)o * T, T}; }
+};
+
+/* Element offsets (in doubles) of one team's arrays in the global slab of MODE_TEAM. */
+struct TeamPlan {
+  int y, f, ynew, difkp1, psiv, del, invwt, yout, dyout, dif, fo1, fo2, qs, qc, rot1, rot2, sc, bgraw, total;
+};
+
+__host__ __device__ inline TeamPlan make_team_plan(const DevSpec &s) {
+  TeamPlan t;
+  int o = 0, n = s.n;
+  t.y = o; o += n;
+  t.f = o; o += n;
+  t.ynew = o; o += n;
+  t.difkp1 = o; o += n;
+  t.psiv = o; o += n;
+  t.del = o; o += n;
+  t.invwt = o; o += n;
+  t.yout = t.psiv;
+  t.dyout = t.del;
+  t.dif = o; o += 7 * n;
+  t.fo1 = o; o += s.nfo;
+  t.fo2 = o; o += s.nfo;
+  t.qs = o; o += s.qs2_size;
+  t.qc = o; o += s.qs2_size;
+  t.rot1 = o; o += s.n_lmq;
+  t.rot2 = o; o += s.n_lmq;
+  t.sc = o; o += 20 * s.n_lm;
+  t.bgraw = o; o += 16;
+  t.total = o;
+  return t;
+}
+
+/* shared memory of MODE_TEAM: the index tables once per CTA, then one Shared per team */
+__host__ __device__ inline size_t team_tables_bytes(const DevSpec &s) {
+  return al(sizeof(short) * ((size_t)(s.Lq + 1) * (SONG2_MAX_M + SONG2_MAX_M + 2) + SONG2_MAX_M + 3 * (size_t)s.n +
+                             4 * (size_t)s.n_lm + 3 * (size_t)s.qs2_size + s.n_row_slots + s.n_qs_slots));
+}
+
+template <int MODE> struct KX {
+  static constexpr int STR = MODE == MODE_TEAM ? 1 : 0;
+  using DA = View<double, STR>;
   const DevSpec &s;
   const DevPtrs &p;
-  int rank, size, warp_team, team;   /* team = one CTA (block mode) or one warp (warp mode) */
-  double *y, *f, *ynew, *difkp1, *psiv, *del, *invwt, *yout, *dyout, *dif, *fo1, *fo2, *qs, *qc, *rot1, *rot2, *sc,
-      *bgraw;
+  int rank, size;          /* this thread's rank in its team, team size */
+  long team;               /* global team index (per-team global scratch) */
+  unsigned tmask;          /* lanes of the team (MODE_TEAM) */
+  int nt;                  /* teams interleaved in the slabs (MODE_TEAM), else 1 */
+  DA y, f, ynew, difkp1, psiv, del, invwt, yout, dyout, dif, fo1, fo2, qs, qc, rot1, rot2, sc, bgraw;
   Shared *sh;
-  short *lm_s, *lmq_s, *im_s, *eq_sp, *eq_l, *eq_m, *idx_I, *idx_E, *idx_B, *idx_N, *qs_sp, *qs_l, *qs_m;
-  void *xsol;
-  int *piv;
-  void *lu;
-  double *jac;
-  double *qtab;
-  __device__ K(const DevSpec &s_, const DevPtrs &p_, char *smem_all, int prec, int warp_team_) : s(s_), p(p_) {
-    warp_team = warp_team_;
-    Plan pl = make_plan(s_, prec, s_.lu_in_smem);
-    char *smem = smem_all;
-    if (warp_team) {
-      rank = threadIdx.x & 31;
-      size = 32;
-      team = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-      smem = smem_all + (size_t)(threadIdx.x >> 5) * pl.total;
-    } else {
-      rank = threadIdx.x;
-      size = blockDim.x;
-      team = blockIdx.x;
-    }
-    y = (double *)(smem + pl.y); f = (double *)(smem + pl.f); ynew = (double *)(smem + pl.ynew);
-    difkp1 = (double *)(smem + pl.difkp1); psiv = (double *)(smem + pl.psiv); del = (double *)(smem + pl.del);
-    invwt = (double *)(smem + pl.invwt); yout = (double *)(smem + pl.yout); dyout = (double *)(smem + pl.dyout);
-    dif = (double *)(smem + pl.dif); fo1 = (double *)(smem + pl.fo1); fo2 = (double *)(smem + pl.fo2);
-    qs = (double *)(smem + pl.qs); qc = (double *)(smem + pl.qc); rot1 = (double *)(smem + pl.rot1);
-    rot2 = (double *)(smem + pl.rot2); sc = (double *)(smem + pl.sc); bgraw = (double *)(smem + pl.bgraw);
-    sh = (Shared *)(smem + pl.shared);
-    short *tb = (short *)(smem + pl.tab);
-    lm_s = tb; tb += (s_.Lq + 1) * SONG2_MAX_M;
-    lmq_s = tb; tb += (s_.Lq + 1) * (SONG2_MAX_M + 2);
+  short *lm_s, *lmq_s, *im_s, *eq_sp, *eq_l, *eq_m, *idx_I, *idx_E, *idx_B, *idx_N, *qs_sp, *qs_l, *qs_m, *row_slot,
+      *qs_slot;
+  char *xsol_b, *lu_b;     /* element 0 of this team's solve vector and LU blocks */
+  View<int, STR> piv;
+  DA jac, qtab;
+
+  template <typename E> __device__ View<E, STR> mk(char *b) const {
+    if constexpr (STR) return View<E, 1>{(E *)b, nt};
+    else return View<E, 0>{(E *)b};
+  }
+  __device__ DA da(double *b) const {
+    if constexpr (STR) return DA{b, nt};
+    else return DA{b};
+  }
+  template <typename E> __device__ View<E, STR> xsol() const { return mk<E>(xsol_b); }
+  template <typename E> __device__ View<E, STR> lu() const { return mk<E>(lu_b); }
+  /* the Jacobian blocks, stored in the iteration-matrix precision */
+  template <typename E> __device__ View<E, STR> jacv() const { return mk<E>((char *)jac.p); }
+
+  __device__ void set_tables(short *tb) {
+    lm_s = tb; tb += (s.Lq + 1) * SONG2_MAX_M;
+    lmq_s = tb; tb += (s.Lq + 1) * (SONG2_MAX_M + 2);
     im_s = tb; tb += SONG2_MAX_M;
-    eq_sp = tb; tb += s_.n;
-    eq_l = tb; tb += s_.n;
-    eq_m = tb; tb += s_.n;
-    idx_I = tb; tb += s_.n_lm;
-    idx_E = tb; tb += s_.n_lm;
-    idx_B = tb; tb += s_.n_lm;
-    idx_N = tb; tb += s_.n_lm;
-    qs_sp = tb; tb += s_.qs2_size;
-    qs_l = tb; tb += s_.qs2_size;
-    qs_m = tb;
-    xsol = smem + pl.xsol;
-    piv = (int *)(smem + pl.piv);
+    eq_sp = tb; tb += s.n;
+    eq_l = tb; tb += s.n;
+    eq_m = tb; tb += s.n;
+    idx_I = tb; tb += s.n_lm;
+    idx_E = tb; tb += s.n_lm;
+    idx_B = tb; tb += s.n_lm;
+    idx_N = tb; tb += s.n_lm;
+    qs_sp = tb; tb += s.qs2_size;
+    qs_l = tb; tb += s.qs2_size;
+    qs_m = tb; tb += s.qs2_size;
+    row_slot = tb; tb += s.n_row_slots;
+    qs_slot = tb;
+  }
+
+  __device__ KX(const DevSpec &s_, const DevPtrs &p_, char *smem_all, int prec) : s(s_), p(p_) {
     size_t ts = prec == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
-    if (s_.lu_in_smem) lu = smem + pl.lu;
-    else lu = (char *)p_.lu_global + (size_t)team * s_.lu_elems * ts;
-    jac = p_.jac + (size_t)team * s_.lu_elems;
-    qtab = p_.qtab ? p_.qtab + (size_t)team * s_.fo_tau_size * 2 * s_.qs2_size : nullptr;
+    if constexpr (MODE == MODE_TEAM) {
+      int G = s_.team_lanes, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
+      nt = 32 / G;
+      int tiw = lane / G;
+      rank = lane % G;
+      size = G;
+      tmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (tiw * G));
+      long gw = (long)blockIdx.x * wpc + warp;
+      team = gw * nt + tiw;
+      TeamPlan tp = make_team_plan(s_);
+      double *base = p_.tslab + gw * (long)tp.total * nt + tiw;
+      y = da(base + (long)tp.y * nt); f = da(base + (long)tp.f * nt); ynew = da(base + (long)tp.ynew * nt);
+      difkp1 = da(base + (long)tp.difkp1 * nt); psiv = da(base + (long)tp.psiv * nt); del = da(base + (long)tp.del * nt);
+      invwt = da(base + (long)tp.invwt * nt); yout = da(base + (long)tp.yout * nt); dyout = da(base + (long)tp.dyout * nt);
+      dif = da(base + (long)tp.dif * nt); fo1 = da(base + (long)tp.fo1 * nt); fo2 = da(base + (long)tp.fo2 * nt);
+      qs = da(base + (long)tp.qs * nt); qc = da(base + (long)tp.qc * nt); rot1 = da(base + (long)tp.rot1 * nt);
+      rot2 = da(base + (long)tp.rot2 * nt); sc = da(base + (long)tp.sc * nt); bgraw = da(base + (long)tp.bgraw * nt);
+      set_tables((short *)smem_all);
+      sh = (Shared *)(smem_all + team_tables_bytes(s_)) + (long)warp * nt + tiw;
+      xsol_b = (char *)p_.txsol + (gw * (long)s_.n * nt + tiw) * ts;
+      piv = View<int, STR>{p_.tpiv + gw * (long)s_.n * nt + tiw, nt};
+      lu_b = (char *)p_.lu_global + (gw * (long)s_.lu_elems * nt + tiw) * ts;
+      jac = da(p_.jac + gw * (long)s_.lu_elems * nt + tiw);
+      qtab = da(p_.qtab ? p_.qtab + gw * (long)s_.fo_tau_size * 2 * s_.qs2_size * nt + tiw : nullptr);
+    } else {
+      Plan pl = make_plan(s_, prec, s_.lu_in_smem);
+      char *smem = smem_all;
+      nt = 1;
+      tmask = 0xffffffffu;
+      if constexpr (MODE == MODE_WARP) {
+        rank = threadIdx.x & 31;
+        size = 32;
+        team = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        smem = smem_all + (size_t)(threadIdx.x >> 5) * pl.total;
+      } else {
+        rank = threadIdx.x;
+        size = blockDim.x;
+        team = blockIdx.x;
+      }
+      y = da((double *)(smem + pl.y)); f = da((double *)(smem + pl.f)); ynew = da((double *)(smem + pl.ynew));
+      difkp1 = da((double *)(smem + pl.difkp1)); psiv = da((double *)(smem + pl.psiv)); del = da((double *)(smem + pl.del));
+      invwt = da((double *)(smem + pl.invwt)); yout = da((double *)(smem + pl.yout)); dyout = da((double *)(smem + pl.dyout));
+      dif = da((double *)(smem + pl.dif)); fo1 = da((double *)(smem + pl.fo1)); fo2 = da((double *)(smem + pl.fo2));
+      qs = da((double *)(smem + pl.qs)); qc = da((double *)(smem + pl.qc)); rot1 = da((double *)(smem + pl.rot1));
+      rot2 = da((double *)(smem + pl.rot2)); sc = da((double *)(smem + pl.sc)); bgraw = da((double *)(smem + pl.bgraw));
+      sh = (Shared *)(smem + pl.shared);
+      set_tables((short *)(smem + pl.tab));
+      xsol_b = smem + pl.xsol;
+      piv = View<int, STR>{(int *)(smem + pl.piv)};
+      if (s_.lu_in_smem) lu_b = smem + pl.lu;
+      else lu_b = (char *)p_.lu_global + (size_t)team * s_.lu_elems * ts;
+      jac = da(p_.jac + (size_t)team * s_.lu_elems);
+      qtab = da(p_.qtab ? p_.qtab + (size_t)team * s_.fo_tau_size * 2 * s_.qs2_size : nullptr);
+    }
   }
   __device__ void sync() const {
-    if (warp_team) __syncwarp();
-    else __syncthreads();
+    if constexpr (MODE == MODE_BLOCK) __syncthreads();
+    else if constexpr (MODE == MODE_WARP) __syncwarp();
+    else __syncwarp(tmask);
   }
   __device__ int LM(int l, int m) const { return lm_s[l * SONG2_MAX_M + im_s[m]]; }
   __device__ int LMQ(int l, int m) const { return lmq_s[l * (SONG2_MAX_M + 2) + m]; }
-  /* copy the index tables into the team's shared workspace (once per kernel) */
+  /* copy the index tables into shared memory (once per kernel; by the CTA in
+     MODE_TEAM, by the team otherwise) */
   __device__ void load_tables() const {
-    for (int e = rank; e < (s.Lq + 1) * SONG2_MAX_M; e += size) lm_s[e] = s.lm_array[e / SONG2_MAX_M][e % SONG2_MAX_M];
-    for (int e = rank; e < (s.Lq + 1) * (SONG2_MAX_M + 2); e += size)
+    int r = rank, z = size;
+    if constexpr (MODE == MODE_TEAM) { r = threadIdx.x; z = blockDim.x; }
+    for (int e = r; e < (s.Lq + 1) * SONG2_MAX_M; e += z) lm_s[e] = s.lm_array[e / SONG2_MAX_M][e % SONG2_MAX_M];
+    for (int e = r; e < (s.Lq + 1) * (SONG2_MAX_M + 2); e += z)
       lmq_s[e] = s.lmq[e / (SONG2_MAX_M + 2)][e % (SONG2_MAX_M + 2)];
-    for (int e = rank; e < SONG2_MAX_M; e += size) im_s[e] = (short)s.index_m[e];
-    for (int e = rank; e < s.n; e += size) {
+    for (int e = r; e < SONG2_MAX_M; e += z) im_s[e] = (short)s.index_m[e];
+    for (int e = r; e < s.n; e += z) {
       eq_sp[e] = p.eq_sp[e]; eq_l[e] = p.eq_l[e]; eq_m[e] = p.eq_m[e];
     }
-    for (int e = rank; e < s.n_lm; e += size) {
+    for (int e = r; e < s.n_lm; e += z) {
       idx_I[e] = p.idx_I[e]; idx_E[e] = p.idx_E[e]; idx_B[e] = p.idx_B[e]; idx_N[e] = p.idx_N[e];
     }
-    for (int e = rank; e < s.qs2_size; e += size) {
+    for (int e = r; e < s.qs2_size; e += z) {
       qs_sp[e] = p.qs_sp[e]; qs_l[e] = p.qs_l[e]; qs_m[e] = p.qs_m[e];
     }
+    for (int e = r; e < s.n_row_slots; e += z) row_slot[e] = p.row_slot[e];
+    for (int e = r; e < s.n_qs_slots; e += z) qs_slot[e] = p.qs_slot[e];
   }
   /* summed couplings, index X in 0..19 */
   __device__ double S(int X, int l, int m) const { return sc[X * s.n_lm + LM(l, m)]; }
@@ -228,37 +340,38 @@ enum { CM12 = 0, CM21, CP12, CP21, CM11, CM22, CP11, CP22, DM12, DM21, DP12, DP2
 
 /* ------------------------------------------------------------------ state accessors */
 
-struct YVec {
-  const double *v;
+template <class A> struct YVec {
+  A v;
   __device__ double operator()(int i) const { return i < 0 ? 0.0 : v[i]; }
 };
+template <class A> __device__ inline YVec<A> yvec(const A &a) { return YVec<A>{a}; }
 struct YUnit {
   int j;
   __device__ double operator()(int i) const { return (i >= 0 && i == j) ? 1.0 : 0.0; }
 };
 
-template <class Y> __device__ inline double getI(const K &c, int tca, const Y &y, int l, int m) {
+template <class Y, class C> __device__ inline double getI(const C &c, int tca, const Y &y, int l, int m) {
   if (l < 0 || m < 0 || m > l || l > c.s.l_max_g || (tca && l >= 1)) return 0.0;
   return y(c.idx_I[c.LM(l, m)]);
 }
-template <class Y> __device__ inline double getE(const K &c, int tca, const Y &y, int l, int m) {
+template <class Y, class C> __device__ inline double getE(const C &c, int tca, const Y &y, int l, int m) {
   if (!c.s.has_pol || tca || l < 2 || m < 0 || m > l || l > c.s.l_max_pol) return 0.0;
   return y(c.idx_E[c.LM(l, m)]);
 }
-template <class Y> __device__ inline double getB(const K &c, int tca, const Y &y, int l, int m) {
+template <class Y, class C> __device__ inline double getB(const C &c, int tca, const Y &y, int l, int m) {
   if (!c.s.has_pol || tca || l < 2 || m <= 0 || m > l || l > c.s.l_max_pol) return 0.0;
   return y(c.idx_B[c.LM(l, m)]);
 }
-template <class Y> __device__ inline double getN(const K &c, const Y &y, int l, int m) {
+template <class Y, class C> __device__ inline double getN(const C &c, const Y &y, int l, int m) {
   if (l < 0 || m < 0 || m > l || l > c.s.l_max_ur) return 0.0;
   return y(c.idx_N[c.LM(l, m)]);
 }
-template <class Y> __device__ inline double getb(const K &c, const Y &y, int n, int m) {
+template <class Y, class C> __device__ inline double getb(const C &c, const Y &y, int n, int m) {
   /* n = 0: b000 ; n = 1: b11m */
   if (n == 0) return y(c.s.idx_b000);
   return (m <= 1) ? y(c.s.idx_b11[m]) : 0.0;
 }
-template <class Y> __device__ inline double getc(const K &c, const Y &y, int n, int m) {
+template <class Y, class C> __device__ inline double getc(const C &c, const Y &y, int n, int m) {
   if (n == 0) return y(c.s.idx_c000);
   return (m <= 1) ? y(c.s.idx_c11[m]) : 0.0;
 }
@@ -276,36 +389,47 @@ __device__ inline double spl(const double *yv, const double *dd, int n, int ncol
          ((a * a * a - a) * __ldg(d0 + q) + (b * b * b - b) * __ldg(d0 + ncol + q)) * (dx * dx) / 6.0;
 }
 
-__device__ inline double bg_col(const K &c, int q, double tau) {
+template <class C> __device__ inline double bg_col(const C &c, int q, double tau) {
   return spl(c.p.bg, c.p.bg_dd, c.s.bg_size, SONG2_BG_SIZE, c.s.bg_lntau0, c.s.bg_dlntau, q, log(tau));
 }
 
-__device__ inline void bg_derive(const double *raw, double tau, BgV &b) {
-  b.a = exp(raw[SONG2_BG_LN_A]);
+/* Background column q at ln tau = x in linear form (exp of the logarithmic
+   columns, Hc' from Hc' tau^2), one column per thread. */
+__device__ inline double bg_value(const double *bg, const double *bg_dd, int bg_size, double x0, double dx, int q, double x,
+                                  double tau) {
+  double v = spl(bg, bg_dd, bg_size, SONG2_BG_SIZE, x0, dx, q, x);
+  if (q == SONG2_BG_HC_PRIME_TAU2) return v / (tau * tau);
+  if (q == SONG2_BG_KAPPA) return exp(-v);
+  return exp(v);
+}
+
+/* BgV from the linear columns */
+template <class A> __device__ inline void bg_derive(const A &lin, BgV &b) {
+  b.a = lin[SONG2_BG_LN_A];
   b.a_sq = b.a * b.a;
-  b.Hc = exp(raw[SONG2_BG_LN_HC]);
-  b.Hc_prime = raw[SONG2_BG_HC_PRIME_TAU2] / (tau * tau);
-  b.rho_g = exp(raw[SONG2_BG_LN_RHO_G]);
-  b.rho_b = exp(raw[SONG2_BG_LN_RHO_B]);
-  b.rho_cdm = exp(raw[SONG2_BG_LN_RHO_CDM]);
-  b.rho_ur = exp(raw[SONG2_BG_LN_RHO_UR]);
-  b.kappa_dot = exp(raw[SONG2_BG_LN_KAPPA_DOT]);
-  b.exp_m_kappa = exp(-raw[SONG2_BG_KAPPA]);
+  b.Hc = lin[SONG2_BG_LN_HC];
+  b.Hc_prime = lin[SONG2_BG_HC_PRIME_TAU2];
+  b.rho_g = lin[SONG2_BG_LN_RHO_G];
+  b.rho_b = lin[SONG2_BG_LN_RHO_B];
+  b.rho_cdm = lin[SONG2_BG_LN_RHO_CDM];
+  b.rho_ur = lin[SONG2_BG_LN_RHO_UR];
+  b.kappa_dot = lin[SONG2_BG_LN_KAPPA_DOT];
+  b.exp_m_kappa = lin[SONG2_BG_KAPPA];
   b.g = b.kappa_dot * b.exp_m_kappa;
   b.r = b.rho_g / b.rho_b;
 }
 
 /* Hc and kappa_dot only (start time, TCA trigger) */
-__device__ inline void bg_hk(const K &c, double tau, double &Hc, double &kd) {
+template <class C> __device__ inline void bg_hk(const C &c, double tau, double &Hc, double &kd) {
   Hc = exp(bg_col(c, SONG2_BG_LN_HC, tau));
   kd = exp(bg_col(c, SONG2_BG_LN_KAPPA_DOT, tau));
 }
 
 /* ------------------------------------------------------------------ quadratic sources */
 
-__device__ double coll_I(const K &c, const BgV &bg, int l, int m) {
+template <class C> __device__ double coll_I(const C &c, const BgV &bg, int l, int m) {
   const Tri &t = c.sh->tri;
-  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  auto fo1 = c.fo1, fo2 = c.fo2;
   double vb1 = fo1[SONG2_FO_V_B], vb2 = fo2[SONG2_FO_V_B], db1 = fo1[SONG2_FO_DELTA_B], db2 = fo2[SONG2_FO_DELTA_B];
   if (l == 0) {
     double vg1 = fo1[SONG2_FO_V_G], vg2 = fo2[SONG2_FO_V_G];
@@ -340,9 +464,9 @@ __device__ double coll_I(const K &c, const BgV &bg, int l, int m) {
   return spec + loss;
 }
 
-__device__ double coll_E(const K &c, int l, int m) {
+template <class C> __device__ double coll_E(const C &c, int l, int m) {
   const Tri &t = c.sh->tri;
-  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  auto fo1 = c.fo1, fo2 = c.fo2;
   double vb1 = fo1[SONG2_FO_V_B], vb2 = fo2[SONG2_FO_V_B], db1 = fo1[SONG2_FO_DELTA_B], db2 = fo2[SONG2_FO_DELTA_B];
   double v01 = -t.k1 * vb1, v02 = -t.k2 * vb2;
   double A1 = fo1[SONG2_FO_PSI], A2 = fo2[SONG2_FO_PSI];
@@ -369,7 +493,7 @@ __device__ double coll_E(const K &c, int l, int m) {
   return spec + loss;
 }
 
-__device__ double coll_B(const K &c, int l, int m) {
+template <class C> __device__ double coll_B(const C &c, int l, int m) {
   const Tri &t = c.sh->tri;
   double v01 = -t.k1 * c.fo1[SONG2_FO_V_B], v02 = -t.k2 * c.fo2[SONG2_FO_V_B];
   double v = 0;
@@ -380,9 +504,9 @@ __device__ double coll_B(const K &c, int l, int m) {
 }
 
 /* Liouville part of the photon / neutrino intensity hierarchy (before the sign flip) */
-__device__ double liou_IN(const K &c, int nu, int l, int m) {
+template <class C> __device__ double liou_IN(const C &c, int nu, int l, int m) {
   const Tri &t = c.sh->tri;
-  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  auto fo1 = c.fo1, fo2 = c.fo2;
   double phi1 = fo1[SONG2_FO_PHI], phi2 = fo2[SONG2_FO_PHI], psi1 = fo1[SONG2_FO_PSI], psi2 = fo2[SONG2_FO_PSI];
   double php1 = fo1[SONG2_FO_PHI_P], php2 = fo2[SONG2_FO_PHI_P];
   double k1 = t.k1, k2 = t.k2;
@@ -404,9 +528,9 @@ __device__ double liou_IN(const K &c, int nu, int l, int m) {
   return v;
 }
 
-template <int WANT_B> __device__ double liou_EB(const K &c, int l, int m) {
+template <int WANT_B, class C> __device__ double liou_EB(const C &c, int l, int m) {
   const Tri &t = c.sh->tri;
-  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  auto fo1 = c.fo1, fo2 = c.fo2;
   double phi1 = fo1[SONG2_FO_PHI], phi2 = fo2[SONG2_FO_PHI], psi1 = fo1[SONG2_FO_PSI], psi2 = fo2[SONG2_FO_PSI];
   double php1 = fo1[SONG2_FO_PHI_P], php2 = fo2[SONG2_FO_PHI_P];
   double k1 = t.k1, k2 = t.k2;
@@ -426,9 +550,9 @@ template <int WANT_B> __device__ double liou_EB(const K &c, int l, int m) {
       c.E1r(l - 1) * (km21 * k2 * (phi2 + psi2) + dm11 * k1 * (phi2 + psi2) + 4 * dm21 * k2 * psi2);
 }
 
-__device__ double liou_matter(const K &c, int cdm, int n, int m) {
+template <class C> __device__ double liou_matter(const C &c, int cdm, int n, int m) {
   const Tri &t = c.sh->tri;
-  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  auto fo1 = c.fo1, fo2 = c.fo2;
   double phi1 = fo1[SONG2_FO_PHI], phi2 = fo2[SONG2_FO_PHI], psi1 = fo1[SONG2_FO_PSI], psi2 = fo2[SONG2_FO_PSI];
   double php1 = fo1[SONG2_FO_PHI_P], php2 = fo2[SONG2_FO_PHI_P];
   double d1 = fo1[cdm ? SONG2_FO_DELTA_CDM : SONG2_FO_DELTA_B], d2 = fo2[cdm ? SONG2_FO_DELTA_CDM : SONG2_FO_DELTA_B];
@@ -442,11 +566,11 @@ __device__ double liou_matter(const K &c, int cdm, int n, int m) {
 }
 
 /* Einstein-tensor quadratic terms (perturbations2.c:10905-11060) into qs */
-__device__ void qs_metric(const K &c, const BgV &bg) {
+template <class C> __device__ void qs_metric(const C &c, const BgV &bg) {
   const Tri &t = c.sh->tri;
   const DevSpec &s = c.s;
-  const double *fo1 = c.fo1, *fo2 = c.fo2;
-  double *qs = c.qs;
+  auto fo1 = c.fo1, fo2 = c.fo2;
+  auto qs = c.qs;
   double phi_1 = fo1[SONG2_FO_PHI], phi_2 = fo2[SONG2_FO_PHI], psi_1 = fo1[SONG2_FO_PSI], psi_2 = fo2[SONG2_FO_PSI];
   double psi_prime_1 = fo1[SONG2_FO_PSI_P], psi_prime_2 = fo2[SONG2_FO_PSI_P];
   double phi_prime_1 = fo1[SONG2_FO_PHI_P], phi_prime_2 = fo2[SONG2_FO_PHI_P];
@@ -511,7 +635,7 @@ __device__ void qs_metric(const K &c, const BgV &bg) {
 }
 
 /* One entry of the quadratic-source vector: total (qs) and collisional (qc) part. */
-__device__ void qs_entry(const K &c, const BgV &bg, int q) {
+template <class C> __device__ void qs_entry(const C &c, const BgV &bg, int q) {
   const DevSpec &s = c.s;
   int sp = c.qs_sp[q], l = c.qs_l[q], m = c.qs_m[q];
   double lv = 0, cv = 0;
@@ -561,7 +685,7 @@ __device__ void qs_entry(const K &c, const BgV &bg, int q) {
 
 /* Collision part only, the quantities perturb2_tca_variables takes directly
    from the interpolated first-order solution (perturbations2.c:9440-9456). */
-__device__ void qc_entry(const K &c, const BgV &bg, int q) {
+template <class C> __device__ void qc_entry(const C &c, const BgV &bg, int q) {
   const DevSpec &s = c.s;
   int sp = c.qs_sp[q], l = c.qs_l[q], m = c.qs_m[q];
   double cv = 0.0;
@@ -579,7 +703,7 @@ __device__ void qc_entry(const K &c, const BgV &bg, int q) {
 
 /* Background, first-order quantities and quadratic sources at tau, block-wide.
    Leaves sh->bg and the qs/qc/fo arrays ready; ends with a barrier. */
-__device__ void prepare(const K &c, double tau, int with_sources) {
+template <class C> __device__ void prepare(const C &c, double tau, int with_sources) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   int tid = c.rank, nt = c.size;
@@ -587,8 +711,8 @@ __device__ void prepare(const K &c, double tau, int with_sources) {
   if (tid == 0) c.sh->lntau = log(tau);
   c.sync();
   double x = c.sh->lntau;
-  if (tid < SONG2_BG_SIZE)
-    c.bgraw[tid] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, tid, x);
+  for (int q = tid; q < SONG2_BG_SIZE; q += nt)
+    c.bgraw[q] = bg_value(c.p.bg, c.p.bg_dd, s.bg_size, s.bg_lntau0, s.bg_dlntau, q, x, tau);
   int use_fo = with_sources && s.has_qs && !s.mode_first_order;
   for (int q = tid; q < 2 * s.nfo; q += nt) {
     int which = q >= s.nfo, qq = which ? q - s.nfo : q;
@@ -602,7 +726,7 @@ __device__ void prepare(const K &c, double tau, int with_sources) {
   }
   c.sync();
   /* FP64 transcendental work is done once, not once per thread */
-  if (tid == 0) bg_derive(c.bgraw, tau, c.sh->bg);
+  if (tid == 0) bg_derive(c.bgraw, c.sh->bg);
   for (int q = tid; q < s.qs2_size; q += nt) {
     c.qs[q] = 0.0;
     c.qc[q] = 0.0;
@@ -610,7 +734,10 @@ __device__ void prepare(const K &c, double tau, int with_sources) {
   c.sync();
   if (use_fo) {
     const BgV &bg = c.sh->bg;
-    for (int q = tid; q < s.qs2_size; q += nt) qs_entry(c, bg, q);
+    for (int e = tid; e < s.n_qs_slots; e += nt) {
+      int q = c.qs_slot[e];
+      if (q >= 0) qs_entry(c, bg, q);
+    }
   }
   c.sync();
 }
@@ -619,16 +746,16 @@ __device__ void prepare(const K &c, double tau, int with_sources) {
    perturbations2.c:14366-14688): background by spline, quadratic sources by
    cubic-spline interpolation of the triplet's table; in tight coupling also the
    first-order quantities and the direct collision terms.  Ends with a barrier. */
-__device__ void prepare_table(const K &c, double tau, int tca) {
+template <class C> __device__ void prepare_table(const C &c, double tau, int tca) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   int tid = c.rank, nt = c.size;
   if (tid == 0) c.sh->lntau = log(tau);
   c.sync();
   double x = c.sh->lntau;
-  if (tid < SONG2_BG_SIZE)
-    c.bgraw[tid] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, tid, x);
-  int use = s.has_qs && !s.mode_first_order && c.qtab;
+  for (int q = tid; q < SONG2_BG_SIZE; q += nt)
+    c.bgraw[q] = bg_value(c.p.bg, c.p.bg_dd, s.bg_size, s.bg_lntau0, s.bg_dlntau, q, x, tau);
+  int use = s.has_qs && !s.mode_first_order && c.qtab.p != nullptr;
   if (use) {
     double dx = s.fo_dlntau, u = (x - s.fo_lntau0) / dx;
     int j0 = c.sh->qt_j0, n = c.sh->qt_n;
@@ -638,7 +765,7 @@ __device__ void prepare_table(const K &c, double tau, int tca) {
     double b = u - i, a = 1.0 - b;
     double ca = (a * a * a - a) * (dx * dx) / 6.0, cb = (b * b * b - b) * (dx * dx) / 6.0;
     int nq = s.qs2_size;
-    const double *r0 = c.qtab + (size_t)(i - j0) * 2 * nq, *r1 = r0 + 2 * nq;
+    auto r0 = c.qtab + (i - j0) * 2 * nq, r1 = r0 + 2 * nq;
     for (int q = tid; q < nq; q += nt) c.qs[q] = a * r0[q] + b * r1[q] + ca * r0[nq + q] + cb * r1[nq + q];
     if (tca) {
       size_t stride = (size_t)s.fo_tau_size * s.nfo;
@@ -655,11 +782,14 @@ __device__ void prepare_table(const K &c, double tau, int tca) {
   if (!(use && tca))
     for (int q = tid; q < s.qs2_size; q += nt) c.qc[q] = 0.0;
   c.sync();
-  if (tid == 0) bg_derive(c.bgraw, tau, c.sh->bg);
+  if (tid == 0) bg_derive(c.bgraw, c.sh->bg);
   c.sync();
   if (use && tca) {
     const BgV &bg = c.sh->bg;
-    for (int q = tid; q < s.qs2_size; q += nt) qc_entry(c, bg, q);
+    for (int e = tid; e < s.n_qs_slots; e += nt) {
+      int q = c.qs_slot[e];
+      if (q >= 0) qc_entry(c, bg, q);
+    }
     c.sync();
   }
 }
@@ -668,11 +798,11 @@ __device__ void prepare_table(const K &c, double tau, int tca) {
    [tau_ini, tau_end] (exact first-order values at the nodes, background by
    spline) and their natural cubic splines in ln tau: the per-triplet table of
    perturb2_quadratic_sources_for_k1k2k (perturbations2.c:10407-10606). */
-__device__ void build_qs_table(const K &c) {
+template <class C> __device__ void build_qs_table(const C &c) {
   const DevSpec &s = c.s;
   Tri &t = c.sh->tri;
   int tid = c.rank, nt = c.size;
-  if (!s.has_qs || s.mode_first_order || !c.qtab) return;
+  if (!s.has_qs || s.mode_first_order || c.qtab.p == nullptr) return;
   int N = s.fo_tau_size, nq = s.qs2_size;
   double x0 = s.fo_lntau0, dx = s.fo_dlntau;
   if (tid == 0) {
@@ -691,21 +821,24 @@ __device__ void build_qs_table(const K &c) {
   const double *v1 = c.p.fo + stride * t.i1, *v2 = c.p.fo + stride * t.i2;
   for (int j = 0; j < M; ++j) {
     double x = x0 + (j0 + j) * dx;
-    if (tid < SONG2_BG_SIZE)
-      c.bgraw[tid] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, tid, x);
+    for (int q = tid; q < SONG2_BG_SIZE; q += nt)
+      c.bgraw[q] = bg_value(c.p.bg, c.p.bg_dd, s.bg_size, s.bg_lntau0, s.bg_dlntau, q, x, exp(x));
     for (int q = tid; q < 2 * s.nfo; q += nt) {
       int which = q >= s.nfo, qq = which ? q - s.nfo : q;
       (which ? c.fo2 : c.fo1)[qq] = __ldg((which ? v2 : v1) + (size_t)(j0 + j) * s.nfo + qq);
     }
     c.sync();
-    if (tid == 0) bg_derive(c.bgraw, exp(x), c.sh->bg);
+    if (tid == 0) bg_derive(c.bgraw, c.sh->bg);
     c.sync();
     {
       const BgV &bg = c.sh->bg;
-      for (int q = tid; q < nq; q += nt) qs_entry(c, bg, q);
+      for (int e = tid; e < s.n_qs_slots; e += nt) {
+        int q = c.qs_slot[e];
+        if (q >= 0) qs_entry(c, bg, q);
+      }
     }
     c.sync();
-    double *row = c.qtab + (size_t)j * 2 * nq;
+    auto row = c.qtab + j * 2 * nq;
     for (int q = tid; q < nq; q += nt) row[q] = c.qs[q];
   }
   c.sync();
@@ -715,74 +848,77 @@ __device__ void build_qs_table(const K &c) {
     double prev = 0.0;
     c.qtab[nq + q] = 0.0;
     for (int j = 1; j < M - 1; ++j) {
-      double ym = c.qtab[(size_t)(j - 1) * 2 * nq + q], y0 = c.qtab[(size_t)j * 2 * nq + q];
-      double yp = c.qtab[(size_t)(j + 1) * 2 * nq + q];
+      double ym = c.qtab[(j - 1) * 2 * nq + q], y0 = c.qtab[j * 2 * nq + q];
+      double yp = c.qtab[(j + 1) * 2 * nq + q];
       double r = 6.0 * (yp - 2.0 * y0 + ym) / (dx * dx);
       double bb = 4.0 - __ldg(c.p.spl_c + j - 1);
       prev = (r - prev) / bb;
-      c.qtab[(size_t)j * 2 * nq + nq + q] = prev;
+      c.qtab[j * 2 * nq + nq + q] = prev;
     }
-    c.qtab[(size_t)(M - 1) * 2 * nq + nq + q] = 0.0;
+    c.qtab[(M - 1) * 2 * nq + nq + q] = 0.0;
     for (int j = M - 2; j >= 1; --j)
-      c.qtab[(size_t)j * 2 * nq + nq + q] -= __ldg(c.p.spl_c + j) * c.qtab[(size_t)(j + 1) * 2 * nq + nq + q];
+      c.qtab[j * 2 * nq + nq + q] -= __ldg(c.p.spl_c + j) * c.qtab[(j + 1) * 2 * nq + nq + q];
   }
   c.sync();
 }
 
 /* ------------------------------------------------------------------ workspace */
 
-template <class Y> __device__ void compute_ws(const K &c, int tca, const Y &y, int lin, WS &w) {
+/* The workspace of perturb2_workspace_at_tau / perturb2_tca_variables /
+   perturb2_einstein for one azimuthal number m in {0, 1, 2}: every field of WS
+   belongs to exactly one m, so the three parts can be evaluated side by side. */
+template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, const Y &y, int lin, WS &w, int m) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
-  const double *qs = c.qs, *qc = c.qc, *fo1 = c.fo1, *fo2 = c.fo2;
+  auto qs = c.qs, qc = c.qc, fo1 = c.fo1, fo2 = c.fo2;
   double k = t.k, Hc = bg.Hc, kd = bg.kappa_dot, r = bg.r;
-  for (int mm = 0; mm < 3; ++mm) {
-    w.N_1m[mm] = w.I_1m[mm] = w.I_2m[mm] = w.E_2m[mm] = w.B_2m[mm] = w.C_1m[mm] = 0;
-    w.b_22m[mm] = w.cdm_22m[mm] = 0;
-    w.I_1m_tca1[mm] = w.I_2m_tca1[mm] = w.E_2m_tca1[mm] = w.B_2m_tca1[mm] = w.Pi_tca1[mm] = 0;
+  w.N_1m[m] = w.I_1m[m] = w.I_2m[m] = w.E_2m[m] = w.B_2m[m] = w.C_1m[m] = 0;
+  w.b_22m[m] = w.cdm_22m[m] = 0;
+  w.I_1m_tca1[m] = w.I_2m_tca1[m] = w.E_2m_tca1[m] = w.B_2m_tca1[m] = w.Pi_tca1[m] = 0;
+  if (m == 0) {
+    w.I_00 = w.N_00 = 0;
+    w.b_200 = w.cdm_200 = 0;
+    w.psi = w.phi_prime = w.phi_pp = 0;
   }
-  w.I_00 = w.N_00 = 0;
-  if (s.compute_m[0]) {
+  if (m == 1) w.omega_m1_prime = 0;
+  if (m == 2) w.gamma_m2_pp = 0;
+  if (!s.compute_m[m]) return;
+  if (m == 0) {
     w.I_00 = getI(c, tca, y, 0, 0);
     w.N_00 = getN(c, y, 0, 0);
   }
-  for (int im = 0; im <= s.index_m_max[1]; ++im) {
-    int m = s.m[im];
+  if (m <= 1) {
     w.I_1m[m] = getI(c, tca, y, 1, m);
     w.N_1m[m] = getN(c, y, 1, m);
     w.C_1m[m] = kd * (FOUR_THIRDS * getb(c, y, 1, m) - getI(c, tca, y, 1, m));
   }
-  for (int im = 0; im <= s.index_m_max[2]; ++im) {
-    int m = s.m[im];
-    w.I_2m[m] = getI(c, tca, y, 2, m);
-    w.E_2m[m] = getE(c, tca, y, 2, m);
-    w.B_2m[m] = getB(c, tca, y, 2, m);
-  }
+  w.I_2m[m] = getI(c, tca, y, 2, m);
+  w.E_2m[m] = getE(c, tca, y, 2, m);
+  w.B_2m[m] = getB(c, tca, y, 2, m);
   double vv_b = lin ? 0.0 : qs[s.iq_vv_b], vv_cdm = lin ? 0.0 : qs[s.iq_vv_cdm];
-  w.b_200 = -2 * t.k1_dot_k2 * vv_b;
-  w.cdm_200 = -2 * t.k1_dot_k2 * vv_cdm;
-  for (int im = 0; im <= s.index_m_max[2]; ++im) {
-    int m = s.m[im];
-    w.b_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_b;
-    w.cdm_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_cdm;
+  if (m == 0) {
+    w.b_200 = -2 * t.k1_dot_k2 * vv_b;
+    w.cdm_200 = -2 * t.k1_dot_k2 * vv_cdm;
   }
+  w.b_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_b;
+  w.cdm_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_cdm;
   if (tca) {
     /* perturb2_tca_variables (perturbations2.c:9374-9738) */
     double tau_c = 1.0 / kd;
-    double f1[SONG2_FO_I], f2[SONG2_FO_I];
-    for (int q = 0; q < SONG2_FO_I; ++q) { f1[q] = lin ? 0.0 : fo1[q]; f2[q] = lin ? 0.0 : fo2[q]; }
-    double vpot_g_1 = f1[SONG2_FO_V_G], vpot_g_2 = f2[SONG2_FO_V_G];
-    double delta_g_1 = f1[SONG2_FO_DELTA_G], delta_g_2 = f2[SONG2_FO_DELTA_G];
-    double v_dot_v_g = -t.k1_dot_k2 * vpot_g_1 * vpot_g_2;
-    double delta_g = w.I_00 - 8 / 3. * v_dot_v_g;
-    double vpot_b_1 = f1[SONG2_FO_V_B], vpot_b_2 = f2[SONG2_FO_V_B];
-    double vpot_b_1_prime = f1[SONG2_FO_V_B_P], vpot_b_2_prime = f2[SONG2_FO_V_B_P];
-    double delta_b_1 = f1[SONG2_FO_DELTA_B], delta_b_2 = f2[SONG2_FO_DELTA_B];
-    double delta_b_1_prime = f1[SONG2_FO_DELTA_B_P], delta_b_2_prime = f2[SONG2_FO_DELTA_B_P];
-    double c1tca[3] = {0.0, 0.0, 0.0};
-    for (int im = 0; im <= s.index_m_max[1]; ++im) {
-      int m = s.m[im];
+    double vpot_g_1 = lin ? 0.0 : fo1[SONG2_FO_V_G], vpot_g_2 = lin ? 0.0 : fo2[SONG2_FO_V_G];
+    double delta_g_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_G], delta_g_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_G];
+    double vpot_b_1 = lin ? 0.0 : fo1[SONG2_FO_V_B], vpot_b_2 = lin ? 0.0 : fo2[SONG2_FO_V_B];
+    double vpot_b_1_prime = lin ? 0.0 : fo1[SONG2_FO_V_B_P], vpot_b_2_prime = lin ? 0.0 : fo2[SONG2_FO_V_B_P];
+    double c1tca = 0.0;
+    if (m <= 1) {
+      double delta_b_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_B], delta_b_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_B];
+      double delta_b_1_prime = lin ? 0.0 : fo1[SONG2_FO_DELTA_B_P], delta_b_2_prime = lin ? 0.0 : fo2[SONG2_FO_DELTA_B_P];
+      double delta_g = 0.0;
+      if (m == 0) {
+        double v_dot_v_g = -t.k1_dot_k2 * vpot_g_1 * vpot_g_2;
+        delta_g = w.I_00 - 8 / 3. * v_dot_v_g;
+      }
       double u_g_1 = -t.k1_m[m + 1] * vpot_g_1, u_g_2 = -t.k2_m[m + 1] * vpot_g_2;
       double u_b_1 = -t.k1_m[m + 1] * vpot_b_1, u_b_2 = -t.k2_m[m + 1] * vpot_b_2;
       double u_b_1_prime = -t.k1_m[m + 1] * vpot_b_1_prime, u_b_2_prime = -t.k2_m[m + 1] * vpot_b_2_prime;
@@ -800,12 +936,11 @@ template <class Y> __device__ void compute_ws(const K &c, int tca, const Y &y, i
       double om = (m == 1) ? y(s.idx_omega) : 0.0;
       double core = Hc * (u_b + om) + k / 4 * (m == 0 ? delta_g : 0) + quadL_diff;
       double U_slip = -quadC_u_g_m - R / (1 + R) * tau_c * core;
-      c1tca[m] = -qcI1 - 4 * R / (1 + R) * core;
+      c1tca = -qcI1 - 4 * R / (1 + R) * core;
       double u_g_tca1 = u_b - U_slip;
       w.I_1m_tca1[m] = 4 * (u_g_tca1 + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
     }
-    for (int im = 0; im <= s.index_m_max[2]; ++im) {
-      int m = s.m[im];
+    {
       double v_ten_v_g = -t.k1_ten_k2[m + 2] * vpot_g_1 * vpot_g_2;
       double v_ten_v_b_prime = -t.k1_ten_k2[m + 2] * (vpot_b_1 * vpot_b_2_prime + vpot_b_2 * vpot_b_1_prime);
       double gp = (m == 2) ? y(s.idx_gammap) : 0.0;
@@ -834,22 +969,19 @@ template <class Y> __device__ void compute_ws(const K &c, int tca, const Y &y, i
       }
     }
     /* the TCA values replace the evolved ones only now (perturbations2.c:8999-9020) */
-    for (int im = 0; im <= s.index_m_max[1]; ++im) {
-      w.I_1m[s.m[im]] = w.I_1m_tca1[s.m[im]];
-      w.C_1m[s.m[im]] = c1tca[s.m[im]];
+    if (m <= 1) {
+      w.I_1m[m] = w.I_1m_tca1[m];
+      w.C_1m[m] = c1tca;
     }
-    for (int im = 0; im <= s.index_m_max[2]; ++im) {
-      int m = s.m[im];
-      w.I_2m[m] = w.I_2m_tca1[m];
-      if (s.has_pol) {
-        w.E_2m[m] = w.E_2m_tca1[m];
-        w.B_2m[m] = (m != 0 ? w.B_2m_tca1[m] : 0.0);
-      }
+    w.I_2m[m] = w.I_2m_tca1[m];
+    if (s.has_pol) {
+      w.E_2m[m] = w.E_2m_tca1[m];
+      w.B_2m[m] = (m != 0 ? w.B_2m_tca1[m] : 0.0);
     }
   }
   /* perturb2_einstein (perturbations2.c:8484-8814), Newtonian gauge, phi_eq = huang */
   double a_sq = bg.a_sq, k_sq = t.k_sq;
-  if (s.compute_m[0]) {
+  if (m == 0) {
     double rho_quadrupole = bg.rho_g * w.I_2m[0] + bg.rho_b * w.b_22m[0] + bg.rho_cdm * w.cdm_22m[0] + bg.rho_ur * getN(c, y, 2, 0);
     double rho_mono_b = bg.rho_b * getb(c, y, 0, 0), rho_mono_c = bg.rho_cdm * getc(c, y, 0, 0);
     double phi = y(s.idx_phi);
@@ -857,27 +989,36 @@ template <class Y> __device__ void compute_ws(const K &c, int tca, const Y &y, i
     w.phi_prime = y(s.idx_phip);
     w.phi_pp = k_sq / 3 * (w.psi - 2 * phi) - Hc * (3 * w.phi_prime) - 2 * w.psi * (Hc * Hc + bg.Hc_prime) -
                a_sq / 2 * (rho_mono_b + rho_mono_c) + (lin ? 0.0 : qs[s.iq_phi_prime_prime]);
-  } else {
-    w.psi = w.phi_prime = w.phi_pp = 0;
-  }
-  w.omega_m1_prime = 0;
-  if (s.compute_m[1]) {
+  } else if (m == 1) {
     double rq1 = bg.rho_g * w.I_2m[1] + bg.rho_b * w.b_22m[1] + bg.rho_cdm * w.cdm_22m[1] + bg.rho_ur * getN(c, y, 2, 1);
     w.omega_m1_prime = -2 * Hc * y(s.idx_omega) + 2 * SQRT_3 / (5. * k) * a_sq * rq1 + (lin ? 0.0 : qs[s.iq_omega_m1_prime]);
-  }
-  w.gamma_m2_pp = 0;
-  if (s.compute_m[2]) {
+  } else {
     double rq2 = bg.rho_g * w.I_2m[2] + bg.rho_b * w.b_22m[2] + bg.rho_cdm * w.cdm_22m[2] + bg.rho_ur * getN(c, y, 2, 2);
     w.gamma_m2_pp = -2 * Hc * y(s.idx_gammap) - k_sq * y(s.idx_gamma) - 2 / 5. * a_sq * rq2 +
                     (lin ? 0.0 : qs[s.iq_gamma_m2_prime_prime]);
   }
 }
 
+/* the whole workspace, one thread */
+template <class Y, class C> __device__ void compute_ws(const C &c, int tca, const Y &y, int lin, WS &w) {
+  for (int m = 0; m < 3; ++m) compute_ws_m(c, tca, y, lin, w, m);
+}
+
+/* the workspace into sh->ws, the three m parts on three threads of the team */
+template <class Y, class C> __device__ void compute_ws_team(const C &c, int tca, const Y &y) {
+  if (c.size >= 96) {
+    /* lane 0 of warps 0, 1, 2: the three parts run on different schedulers */
+    if ((c.rank & 31) == 0 && c.rank < 96) compute_ws_m(c, tca, y, 0, c.sh->ws, c.rank >> 5);
+  } else {
+    for (int m = c.rank; m < 3; m += c.size) compute_ws_m(c, tca, y, 0, c.sh->ws, m);
+  }
+}
+
 /* ------------------------------------------------------------------ derivs rows */
 
 /* every row except phi' (which needs two other rows, see row() below) */
-template <class Y>
-__device__ double row_h(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
+template <class Y, class C>
+__device__ double row_h(const C &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
@@ -999,8 +1140,8 @@ __device__ double row_h(const K &c, int tca, int i, const Y &y, const WS &w, int
 /* psi' given the time derivatives of the photon and neutrino quadrupoles
    (perturb2_compute_psi_prime, perturbations2.c:10188-10383); in tight coupling
    the photon quadrupole derivative is the TCA one. */
-template <class Y>
-__device__ double psi_prime_of(const K &c, int tca, const Y &y, const WS &w, int lin, double dI20, double dN20) {
+template <class Y, class C>
+__device__ double psi_prime_of(const C &c, int tca, const Y &y, const WS &w, int lin, double dI20, double dN20) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
@@ -1020,8 +1161,8 @@ __device__ double psi_prime_of(const K &c, int tca, const Y &y, const WS &w, int
 
 /* Row i of dy = f(tau, y).  The phi' row is phi'' = (Einstein part) - Hc psi',
    where psi' needs the I_20 and N_20 rows. */
-template <class Y>
-__device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
+template <class Y, class C>
+__device__ double row(const C &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
   if (c.eq_sp[i] != SP_PHIP) return row_h(c, tca, i, y, w, lin, tau);
   double dI20 = tca ? 0.0 : row_h(c, tca, c.idx_I[c.LM(2, 0)], y, w, lin, tau);
   double dN20 = row_h(c, tca, c.idx_N[c.LM(2, 0)], y, w, lin, tau);
@@ -1029,19 +1170,23 @@ __device__ double row(const K &c, int tca, int i, const Y &y, const WS &w, int l
 }
 
 /* dy = f(tau, y): block-wide; prepare(tau) must have run.  Ends with a barrier. */
-__device__ void rhs(const K &c, int tca, double tau, const double *y, double *dy) {
+template <class C, class A, class B> __device__ void rhs(const C &c, int tca, double tau, A y, B dy) {
   const DevSpec &s = c.s;
-  YVec yv{y};
-  if (c.rank == 0) compute_ws(c, tca, yv, 0, c.sh->ws);
+  auto yv = yvec(y);
+  compute_ws_team(c, tca, yv);
   c.sync();
-  for (int i = c.rank; i < s.n; i += c.size) dy[i] = row(c, tca, i, yv, c.sh->ws, 0, tau);
+  for (int e = c.rank; e < s.n_row_slots; e += c.size) {
+    int i = c.row_slot[e];
+    if (i >= 0) dy[i] = row(c, tca, i, yv, c.sh->ws, 0, tau);
+  }
   c.sync();
 }
 
 /* Exact Jacobian of the affine system at tau (prepare(tau) must have run):
    J[:, j] = A e_j, one thread per column; stored per m block in global scratch. */
-__device__ void jacobian(const K &c, int tca, double tau) {
+template <typename T, class C> __device__ void jacobian(const C &c, int tca, double tau) {
   const DevSpec &s = c.s;
+  auto J0 = c.template jacv<T>();
   for (int j = c.rank; j < s.n; j += c.size) {
     int b = 0;
     while (b + 1 < s.nblk && j >= s.blk_start[b + 1]) ++b;
@@ -1049,8 +1194,8 @@ __device__ void jacobian(const K &c, int tca, double tau) {
     YUnit yu{j};
     WS w;
     compute_ws(c, tca, yu, 1, w);
-    double *J = c.jac + s.lu_off[b];
-    for (int i = b0; i < b0 + nb; ++i) J[(size_t)(i - b0) * nb + (j - b0)] = row(c, tca, i, yu, w, 1, tau);
+    auto J = J0 + s.lu_off[b];
+    for (int i = b0; i < b0 + nb; ++i) J[(i - b0) * nb + (j - b0)] = (T)row(c, tca, i, yu, w, 1, tau);
   }
   c.sync();
 }
@@ -1059,113 +1204,291 @@ __device__ void jacobian(const K &c, int tca, double tau) {
 
 template <typename T> __device__ inline T tabs(T x) { return x < T(0) ? -x : x; }
 
-/* one m block, factorised by one warp: partial pivoting, row-major in place */
-template <typename T> __device__ void warp_lu(const K &c, int b, int lane) {
+/* One m block, factorised by a group of W lanes (a warp, or a team of MODE_TEAM):
+   partial pivoting, row-major in place. */
+template <typename T, class C>
+__device__ void group_lu(const C &c, int b, int lane, int W, unsigned mask) {
   const DevSpec &s = c.s;
-  T *A = (T *)c.lu + s.lu_off[b];
+  auto A = c.template lu<T>() + s.lu_off[b];
   int nb = s.blk_size[b];
-  int *pv = c.piv + s.blk_start[b];
+  auto pv = c.piv + s.blk_start[b];
   for (int kk = 0; kk < nb; ++kk) {
     T best = T(-1);
     int bi = kk;
-    for (int i = kk + lane; i < nb; i += 32) {
+    for (int i = kk + lane; i < nb; i += W) {
       T v = tabs(A[i * nb + kk]);
       if (v > best) { best = v; bi = i; }
     }
-    for (int off = 16; off > 0; off >>= 1) {
-      T ob = __shfl_xor_sync(0xffffffffu, best, off);
-      int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+    for (int off = W >> 1; off > 0; off >>= 1) {
+      T ob = __shfl_xor_sync(mask, best, off);
+      int oi = __shfl_xor_sync(mask, bi, off);
       if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
     }
     if (lane == 0) pv[kk] = bi;
     if (!(best > T(0))) {
-      if (lane == 0) c.sh->lu_fail = 1;
-      A[kk * nb + kk] = T(1);
-      __syncwarp();
+      if (lane == 0) {
+        c.sh->lu_fail = 1;
+        A[kk * nb + kk] = T(1);
+      }
+      __syncwarp(mask);
       continue;
     }
     if (bi != kk)
-      for (int j = lane; j < nb; j += 32) {
+      for (int j = lane; j < nb; j += W) {
         T tmp = A[kk * nb + j];
         A[kk * nb + j] = A[bi * nb + j];
         A[bi * nb + j] = tmp;
       }
-    __syncwarp();
+    __syncwarp(mask);
     T inv = T(1) / A[kk * nb + kk];
-    for (int i = kk + 1 + lane; i < nb; i += 32) A[i * nb + kk] *= inv;
-    __syncwarp();
+    for (int i = kk + 1 + lane; i < nb; i += W) A[i * nb + kk] *= inv;
+    __syncwarp(mask);
     for (int i = kk + 1; i < nb; ++i) {
       T lik = A[i * nb + kk];
       if (lik != T(0))
-        for (int j = kk + 1 + lane; j < nb; j += 32) A[i * nb + j] -= lik * A[kk * nb + j];
+        for (int j = kk + 1 + lane; j < nb; j += W) A[i * nb + j] -= lik * A[kk * nb + j];
     }
-    __syncwarp();
+    __syncwarp(mask);
   }
 }
 
-template <typename T> __device__ void form_and_factor(const K &c, double hinvGak) {
+template <typename T, class C> __device__ void form_and_factor(const C &c, double hinvGak) {
   const DevSpec &s = c.s;
-  T *LU = (T *)c.lu;
+  auto LU = c.template lu<T>();
+  auto J = c.template jacv<T>();
   for (int e = c.rank; e < s.lu_elems; e += c.size) {
     int b = 0;
     while (b + 1 < s.nblk && e >= s.lu_off[b + 1]) ++b;
     int nb = s.blk_size[b], r = (e - s.lu_off[b]) / nb, col = (e - s.lu_off[b]) % nb;
-    double v = -hinvGak * c.jac[e];
+    double v = -hinvGak * J[e];
     if (r == col) v += 1.0;
     LU[e] = (T)v;
   }
   c.sync();
-  if (c.warp_team) {
-    for (int b = 0; b < s.nblk; ++b) warp_lu<T>(c, b, c.rank);
+  if constexpr (C::STR) {
+    for (int b = 0; b < s.nblk; ++b) group_lu<T>(c, b, c.rank, c.size, c.tmask);
+  } else if (c.size == 32) {
+    for (int b = 0; b < s.nblk; ++b) group_lu<T>(c, b, c.rank, 32, 0xffffffffu);
   } else {
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int b = warp; b < s.nblk; b += nw) warp_lu<T>(c, b, lane);
+    for (int b = warp; b < s.nblk; b += nw) group_lu<T>(c, b, lane, 32, 0xffffffffu);
   }
   c.sync();
 }
 
-/* one m block, solved by one warp */
-template <typename T> __device__ void warp_solve(const K &c, int b, int lane) {
+/* one m block, solved by a group of W lanes */
+template <typename T, class C>
+__device__ void group_solve(const C &c, int b, int lane, int W, unsigned mask) {
   const DevSpec &s = c.s;
-  T *x = (T *)c.xsol;
   int nb = s.blk_size[b];
-  const T *A = (const T *)c.lu + s.lu_off[b];
-  const int *pv = c.piv + s.blk_start[b];
-  T *xb = x + s.blk_start[b];
+  auto A = c.template lu<T>() + s.lu_off[b];
+  auto pv = c.piv + s.blk_start[b];
+  auto xb = c.template xsol<T>() + s.blk_start[b];
   if (lane == 0)
     for (int kk = 0; kk < nb; ++kk) {
-      int p = pv[kk];
-      if (p != kk) { T tmp = xb[kk]; xb[kk] = xb[p]; xb[p] = tmp; }
+      int q = pv[kk];
+      if (q != kk) { T tmp = xb[kk]; xb[kk] = xb[q]; xb[q] = tmp; }
     }
-  __syncwarp();
+  __syncwarp(mask);
   for (int j = 0; j < nb; ++j) {
     T xj = xb[j];
-    for (int i = j + 1 + lane; i < nb; i += 32) xb[i] -= A[i * nb + j] * xj;
-    __syncwarp();
+    for (int i = j + 1 + lane; i < nb; i += W) xb[i] -= A[i * nb + j] * xj;
+    __syncwarp(mask);
   }
   for (int j = nb - 1; j >= 0; --j) {
     if (lane == 0) xb[j] /= A[j * nb + j];
-    __syncwarp();
+    __syncwarp(mask);
     T xj = xb[j];
-    for (int i = lane; i < j; i += 32) xb[i] -= A[i * nb + j] * xj;
-    __syncwarp();
+    for (int i = lane; i < j; i += W) xb[i] -= A[i * nb + j] * xj;
+    __syncwarp(mask);
   }
 }
 
 /* del <- M^{-1} rhs (rhs given in c.del, result written back to c.del) */
-template <typename T> __device__ void lu_solve(const K &c) {
+template <typename T, class C> __device__ void lu_solve(const C &c) {
   const DevSpec &s = c.s;
-  T *x = (T *)c.xsol;
+  auto x = c.template xsol<T>();
   for (int i = c.rank; i < s.n; i += c.size) x[i] = (T)c.del[i];
   c.sync();
-  if (c.warp_team) {
-    for (int b = 0; b < s.nblk; ++b) warp_solve<T>(c, b, c.rank);
+  if constexpr (C::STR) {
+    for (int b = 0; b < s.nblk; ++b) group_solve<T>(c, b, c.rank, c.size, c.tmask);
+  } else if (c.size == 32) {
+    for (int b = 0; b < s.nblk; ++b) group_solve<T>(c, b, c.rank, 32, 0xffffffffu);
   } else {
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int b = warp; b < s.nblk; b += nw) warp_solve<T>(c, b, lane);
+    for (int b = warp; b < s.nblk; b += nw) group_solve<T>(c, b, lane, 32, 0xffffffffu);
   }
   c.sync();
   for (int i = c.rank; i < s.n; i += c.size) c.del[i] = (double)x[i];
+  c.sync();
+}
+
+/* ------------------------------------------------------------------ explicit inverse (mixed form) */
+
+/* In the mixed form the FP32 iteration matrix is inverted in place, every m block
+   at once across the team (Gauss-Jordan elimination with partial pivoting), so
+   that a Newton solve is one matrix-vector product instead of serial triangular
+   sweeps: FP32 arithmetic is cheap on this GPU, the sweeps' latency is not.  The
+   simplified Newton iteration corrects the FP32 rounding as it does for an FP32
+   LU solve. */
+
+/* Column kk of block b, by one group: pivot search, row interchange, scaling of
+   the pivot row (its diagonal becomes the reciprocal pivot) and a copy of column kk
+   for the elimination. */
+template <typename T, class C>
+__device__ void gj_pivot(const C &c, int b, int kk, int lane, int W, unsigned mask) {
+  const DevSpec &s = c.s;
+  int nb = s.blk_size[b];
+  if (kk >= nb) return;
+  auto A = c.template lu<T>() + s.lu_off[b];
+  auto col = c.template xsol<T>() + s.blk_start[b];
+  T best = T(-1);
+  int bi = kk;
+  for (int i = kk + lane; i < nb; i += W) {
+    T v = tabs(A[i * nb + kk]);
+    if (v > best) { best = v; bi = i; }
+  }
+  for (int off = W >> 1; off > 0; off >>= 1) {
+    T ob = __shfl_xor_sync(mask, best, off);
+    int oi = __shfl_xor_sync(mask, bi, off);
+    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+  }
+  if (bi != kk)
+    for (int j = lane; j < nb; j += W) {
+      T tmp = A[kk * nb + j];
+      A[kk * nb + j] = A[bi * nb + j];
+      A[bi * nb + j] = tmp;
+    }
+  __syncwarp(mask);
+  T inv = T(1);
+  if (best > T(0)) inv = T(1) / A[kk * nb + kk];
+  for (int i = lane; i < nb; i += W) col[i] = (i == kk) ? T(0) : A[i * nb + kk];
+  __syncwarp(mask);
+  for (int j = lane; j < nb; j += W) A[kk * nb + j] = (j == kk) ? inv : A[kk * nb + j] * inv;
+  if (lane == 0) {
+    c.piv[s.blk_start[b] + kk] = bi;
+    c.sh->gjp[b] = (float)inv;
+    if (!(best > T(0))) c.sh->lu_fail = 1;
+  }
+  __syncwarp(mask);
+}
+
+/* undo the row interchanges on the columns of the inverse of block b */
+template <typename T, class C> __device__ void gj_unpermute(const C &c, int b, int lane, int W, unsigned mask) {
+  const DevSpec &s = c.s;
+  int nb = s.blk_size[b];
+  auto A = c.template lu<T>() + s.lu_off[b];
+  for (int k = nb - 1; k >= 0; --k) {
+    int q = c.piv[s.blk_start[b] + k];
+    if (q != k)
+      for (int i = lane; i < nb; i += W) {
+        T tmp = A[i * nb + k];
+        A[i * nb + k] = A[i * nb + q];
+        A[i * nb + q] = tmp;
+      }
+    __syncwarp(mask);
+  }
+}
+
+/* run f(b, lane, W, mask) for every block: a warp per block (CTA teams), the team
+   itself otherwise */
+template <class C, class F> __device__ void per_block_group(const C &c, F f) {
+  const DevSpec &s = c.s;
+  if constexpr (C::STR) {
+    for (int b = 0; b < s.nblk; ++b) f(b, c.rank, c.size, c.tmask);
+  } else if (c.size == 32) {
+    for (int b = 0; b < s.nblk; ++b) f(b, c.rank, 32, 0xffffffffu);
+  } else {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int b = warp; b < s.nblk; b += nw) f(b, lane, 32, 0xffffffffu);
+  }
+}
+
+template <class C> __device__ inline int block_of(const C &c, int i) {
+  int b = 0;
+  while (b + 1 < c.s.nblk && i >= c.s.blk_start[b + 1]) ++b;
+  return b;
+}
+
+template <typename T, class C> __device__ void form_and_invert(const C &c, double hinvGak) {
+  const DevSpec &s = c.s;
+  auto A = c.template lu<T>();
+  auto J = c.template jacv<T>();
+  auto col = c.template xsol<T>();
+  T hg = (T)hinvGak;
+  for (int e = c.rank; e < s.lu_elems; e += c.size) {
+    int b = 0;
+    while (b + 1 < s.nblk && e >= s.lu_off[b + 1]) ++b;
+    int nb = s.blk_size[b], r = (e - s.lu_off[b]) / nb, cc = (e - s.lu_off[b]) % nb;
+    A[e] = (r == cc ? T(1) : T(0)) - hg * J[e];
+  }
+  /* elimination work of this thread per block: columns cc (and row groups rg of
+     R rows each) in steps of the team size; the first item is precomputed */
+  int Rb[S2_MAXBLK], cb[S2_MAXBLK], rb[S2_MAXBLK];
+  int maxnb = 0;
+#pragma unroll
+  for (int b = 0; b < S2_MAXBLK; ++b) {
+    int nb = b < s.nblk ? s.blk_size[b] : 1;
+    Rb[b] = max(1, c.size / nb);
+    cb[b] = c.rank % nb;
+    rb[b] = c.rank / nb;
+    if (b < s.nblk) maxnb = max(maxnb, nb);
+  }
+  c.sync();
+  for (int kk = 0; kk < maxnb; ++kk) {
+    per_block_group(c, [&](int b, int lane, int W, unsigned mask) { gj_pivot<T>(c, b, kk, lane, W, mask); });
+    c.sync();
+#pragma unroll
+    for (int b = 0; b < S2_MAXBLK; ++b) {
+      if (b >= s.nblk) break;
+      int nb = s.blk_size[b];
+      if (kk >= nb) continue;
+      int R = Rb[b];
+      auto Ab = A + s.lu_off[b];
+      auto colb = col + s.blk_start[b];
+      T inv = (T)c.sh->gjp[b];
+      for (int item = c.rank; item < nb * R; item += c.size) {
+        int cc = item == c.rank ? cb[b] : item % nb, rg = item == c.rank ? rb[b] : item / nb;
+        /* column kk becomes -col * inv; the others lose col * (scaled pivot row) */
+        T pr = cc == kk ? T(0) : Ab[kk * nb + cc];
+        T sa = cc == kk ? T(0) : T(1), sb = cc == kk ? -inv : -pr;
+        /* eight rows at a time: all loads issued before the stores */
+        for (int r0 = rg; r0 < nb; r0 += 8 * R) {
+          T cv[8], av[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            int r = r0 + u * R;
+            cv[u] = r < nb ? colb[r] : T(0);
+            av[u] = r < nb ? Ab[r * nb + cc] : T(0);
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            int r = r0 + u * R;
+            if (r < nb && r != kk) Ab[r * nb + cc] = sa * av[u] + sb * cv[u];
+          }
+        }
+      }
+    }
+    c.sync();
+  }
+  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { gj_unpermute<T>(c, b, lane, W, mask); });
+  c.sync();
+}
+
+/* del <- M^{-1} del with the explicit inverse: one row per thread */
+template <typename T, class C> __device__ void inv_solve(const C &c) {
+  const DevSpec &s = c.s;
+  auto x = c.template xsol<T>();
+  for (int i = c.rank; i < s.n; i += c.size) x[i] = (T)c.del[i];
+  c.sync();
+  auto A = c.template lu<T>();
+  for (int i = c.rank; i < s.n; i += c.size) {
+    int b = block_of(c, i), nb = s.blk_size[b], b0 = s.blk_start[b];
+    auto row = A + s.lu_off[b] + (i - b0) * nb;
+    T acc = T(0);
+    for (int j = 0; j < nb; ++j) acc += row[j] * x[b0 + j];
+    c.del[i] = (double)acc;
+  }
   c.sync();
 }
 
@@ -1176,21 +1499,28 @@ template <typename T> __device__ void lu_solve(const K &c) {
    a NaN compares above +inf, so no FP64 instruction is spent on it. */
 __device__ inline unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
 
-__device__ double block_max_bits(const K &c, unsigned long long v) {
-  for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
-    v = o > v ? o : v;
-  }
-  if (!c.warp_team) {
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0) ((unsigned long long *)c.sh->red)[warp] = v;
-    __syncthreads();
-    int nw = (blockDim.x + 31) >> 5;
-    v = 0;
-    for (int i = 0; i < nw; ++i) {
-      unsigned long long o = ((unsigned long long *)c.sh->red)[i];
+template <class C> __device__ double block_max_bits(const C &c, unsigned long long v) {
+  if constexpr (C::STR) {
+    for (int off = c.size >> 1; off > 0; off >>= 1) {
+      unsigned long long o = __shfl_xor_sync(c.tmask, v, off);
       v = o > v ? o : v;
+    }
+  } else {
+    for (int off = 16; off > 0; off >>= 1) {
+      unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
+      v = o > v ? o : v;
+    }
+    if (c.size > 32) {
+      int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      __syncthreads();
+      if (lane == 0) ((unsigned long long *)c.sh->red)[warp] = v;
+      __syncthreads();
+      int nw = (blockDim.x + 31) >> 5;
+      v = 0;
+      for (int i = 0; i < nw; ++i) {
+        unsigned long long o = ((unsigned long long *)c.sh->red)[i];
+        v = o > v ? o : v;
+      }
     }
   }
   /* any NaN maps to +inf, so callers test a single "< inf" */
@@ -1204,17 +1534,14 @@ __device__ inline void bmax(unsigned long long &acc, double x) {
   acc = b > acc ? b : acc;
 }
 
-__device__ double block_max(const K &c, double v) {
-  unsigned long long b = dbits(v) & 0x7fffffffffffffffull;
-  return block_max_bits(c, b);
-}
 
 /* ------------------------------------------------------------------ outputs */
 
-__device__ void store_sources(const K &c, int index_tau, double tau, const double *y, const double *dy) {
+template <class C, class A, class B>
+__device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
-  YVec yv{y};
+  auto yv = yvec(y);
   /* psi' from the phi' row: psi' = (phi_pp - dy[phi']) / Hc */
   if (c.rank == 0) {
     double psi_prime = 0.0;
@@ -1228,7 +1555,7 @@ __device__ void store_sources(const K &c, int index_tau, double tau, const doubl
   c.sync();
   const WS &w = c.sh->ws;
   const BgV &bg = c.sh->bg;
-  const double *fo1 = c.fo1, *fo2 = c.fo2;
+  auto fo1 = c.fo1, fo2 = c.fo2;
   double k1 = t.k1, k2 = t.k2, k = t.k;
   double psi_1 = fo1[SONG2_FO_PSI], psi_2 = fo2[SONG2_FO_PSI], phi_1 = fo1[SONG2_FO_PHI], phi_2 = fo2[SONG2_FO_PHI];
   double phi_prime_1 = fo1[SONG2_FO_PHI_P], phi_prime_2 = fo2[SONG2_FO_PHI_P];
@@ -1321,11 +1648,11 @@ __device__ void store_sources(const K &c, int index_tau, double tau, const doubl
   }
 }
 
-__device__ void store_first_order(const K &c, int index_tau, const double *y, const double *dy) {
+template <class C, class A, class B> __device__ void store_first_order(const C &c, int index_tau, A y, B dy) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   int tca = c.sh->tca;
-  YVec yv{y};
+  auto yv = yvec(y);
   const WS &w = c.sh->ws;
   const BgV &bg = c.sh->bg;
   double k = t.k;
@@ -1384,7 +1711,7 @@ __device__ double legendre_norm(int l, int m, double x) {
   return q1;
 }
 
-__device__ int geometry(const K &c) {
+template <class C> __device__ int geometry(const C &c) {
   const DevSpec &s = c.s;
   Tri &t = c.sh->tri;
   int tid = c.rank, nt = c.size;
@@ -1456,7 +1783,7 @@ __device__ int geometry(const K &c) {
 }
 
 /* start time (perturbations2.c:3388-3524) and TCA interval (perturbations2.c:4854-5403), thread 0 */
-__device__ int intervals(const K &c) {
+template <class C> __device__ int intervals(const C &c) {
   const DevSpec &s = c.s;
   Tri &t = c.sh->tri;
   double kmax = fmax(t.k, fmax(t.k1, t.k2));
@@ -1498,18 +1825,18 @@ __device__ int intervals(const K &c) {
 
 /* ------------------------------------------------------------------ initial conditions (thread 0) */
 
-__device__ void initial_conditions(const K &c, double tau) {
+template <class C> __device__ void initial_conditions(const C &c, double tau) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
-  double *y = c.y;
+  auto y = c.y;
   for (int i = 0; i < s.n; ++i) y[i] = 0.0;
   if (s.ic == SONG2_IC_ZERO || !s.compute_m[0]) return;
   int tca = c.sh->tca;
   double k = t.k, k_sq = t.k_sq, Hc = bg.Hc, Hc_sq = Hc * Hc, a_sq = bg.a_sq;
   double rho_r = bg.rho_g + bg.rho_ur, frac_ur = bg.rho_ur / rho_r, frac_g = 1 - frac_ur;
   double rho_tot = Hc_sq / a_sq, Omega_m = (bg.rho_b + bg.rho_cdm) / rho_tot, Omega_r = rho_r / rho_tot;
-  const double *fo1 = c.fo1, *fo2 = c.fo2, *qs = c.qs;
+  auto fo1 = c.fo1, fo2 = c.fo2, qs = c.qs;
   if (s.ic == SONG2_IC_AD) {
     double k1_0 = t.k1_m[1], k2_0 = t.k2_m[1];
     double delta_g_1 = fo1[SONG2_FO_DELTA_G], delta_g_2 = fo2[SONG2_FO_DELTA_G];
@@ -1582,30 +1909,26 @@ __device__ void initial_conditions(const K &c, double tau) {
 
 __constant__ double c_G[5] = {1.0, 1.5, 11.0 / 6.0, 25.0 / 12.0, 137.0 / 60.0};
 __constant__ double c_alpha[5] = {-0.1850, -1.0 / 9.0, -0.0823, -0.0415, 0.0};
+/* U(i, j) = (-1)^(i+1) binom(j+1, i+1) (zero below the diagonal) */
+__constant__ double c_U[5][5] = {{-1, -2, -3, -4, -5}, {0, 1, 3, 6, 10}, {0, 0, -1, -4, -10}, {0, 0, 0, 1, 5}, {0, 0, 0, 0, -1}};
 
 /* dif[:,0..k-1] <- dif * (R(r) U): thread 0 forms R U, every thread updates its own components */
-__device__ void rescale_dif(const K &c, int k, double r) {
-  double (*RU)[5] = c.sh->RU;
-  if (c.rank == 0) {
-    double Rm[5][5], U[5][5];
-    for (int i = 0; i < k; ++i)
-      for (int j = 0; j < k; ++j) {
-        double prod = 1.0;
-        for (int p = 1; p <= i + 1; ++p) prod *= ((p - 1) - (j + 1) * r) / p;
-        Rm[i][j] = prod;
-        double binom = 0.0;
-        if (j >= i) {
-          binom = 1.0;
-          for (int p = 1; p <= i + 1; ++p) binom = binom * (j + 1 - (i + 1) + p) / p;
-        }
-        U[i][j] = ((i + 1) % 2 ? -binom : binom);
-      }
-    for (int i = 0; i < k; ++i)
-      for (int j = 0; j < k; ++j) {
-        double sm = 0;
-        for (int p = 0; p < k; ++p) sm += Rm[i][p] * U[p][j];
-        RU[i][j] = sm;
-      }
+template <class C> __device__ void rescale_dif(const C &c, int k, double r) {
+  double (*RU)[5] = c.sh->RU, (*Rm)[5] = c.sh->Rm;
+  /* R(r) entry (i, j) = prod_{p=1..i+1} ((p-1) - (j+1) r) / p, one entry per thread */
+  for (int e = c.rank; e < k * k; e += c.size) {
+    int i = e / k, j = e % k;
+    double prod = 1.0;
+    for (int p = 1; p <= i + 1; ++p) prod *= ((p - 1) - (j + 1) * r) / p;
+    Rm[i][j] = prod;
+  }
+  c.sync();
+  /* RU = R U with U(i, j) = (-1)^(i+1) binom(j+1, i+1) for j >= i */
+  for (int e = c.rank; e < k * k; e += c.size) {
+    int i = e / k, j = e % k;
+    double sm = 0;
+    for (int p = 0; p <= j; ++p) sm += Rm[i][p] * c_U[p][j];
+    RU[i][j] = sm;
   }
   c.sync();
   int n = c.s.n;
@@ -1613,19 +1936,20 @@ __device__ void rescale_dif(const K &c, int k, double r) {
     double tmp[5];
     for (int j = 0; j < k; ++j) {
       double sm = 0;
-      for (int i = 0; i < k; ++i) sm += c.dif[(size_t)i * n + e] * RU[i][j];
+      for (int i = 0; i < k; ++i) sm += c.dif[i * n + e] * RU[i][j];
       tmp[j] = sm;
     }
-    for (int j = 0; j < k; ++j) c.dif[(size_t)j * n + e] = tmp[j];
+    for (int j = 0; j < k; ++j) c.dif[j * n + e] = tmp[j];
   }
   c.sync();
 }
 
-template <typename T>
-__device__ int refactor(const K &c, double hinvGak, song2_triplet_stats &st) {
+template <typename T, class C>
+__device__ int refactor(const C &c, double hinvGak, song2_triplet_stats &st) {
   if (c.rank == 0) c.sh->lu_fail = 0;
   c.sync();
-  form_and_factor<T>(c, hinvGak);
+  if constexpr (sizeof(T) == sizeof(float)) form_and_invert<T>(c, hinvGak);
+  else form_and_factor<T>(c, hinvGak);
   st.n_lu++;
   return c.sh->lu_fail ? SONG2_E_SINGULAR : SONG2_OK;
 }
@@ -1634,24 +1958,24 @@ __device__ int refactor(const K &c, double hinvGak, song2_triplet_stats &st) {
    dy comes from derivs (tabulated quadratic sources, perturbations2.c:7702-7718)
    and the source functions from quadratic sources and workspace recomputed at
    tau (perturb2_sources, perturbations2.c:11956-12030). */
-__device__ void do_output(const K &c, int jout, double to) {
+template <class C> __device__ void do_output(const C &c, int jout, double to) {
   int tca = c.sh->tca;
   prepare_table(c, to, tca);
   rhs(c, tca, to, c.yout, c.dyout);
   prepare(c, to, 1);
-  if (c.rank == 0) compute_ws(c, tca, YVec{c.yout}, 0, c.sh->ws);
+  compute_ws_team(c, tca, yvec(c.yout));
   c.sync();
   if (c.s.mode_first_order) store_first_order(c, jout, c.yout, c.dyout);
   else store_sources(c, jout, to, c.yout, c.dyout);
   c.sync();
 }
 
-__device__ inline double tout_at(const K &c, int j) {
+template <class C> __device__ inline double tout_at(const C &c, int j) {
   return c.s.mode_first_order ? exp(c.s.fo_lntau0 + j * c.s.fo_dlntau) : c.p.tau[j];
 }
 
-template <typename T>
-__device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0, song2_triplet_stats &st) {
+template <typename T, class C>
+__device__ int ndf15(const C &c, double t0, double t1, int &jout, int include_t0, song2_triplet_stats &st) {
   const DevSpec &s = c.s;
   int n = s.n, tid = c.rank, nt = c.size;
   int nout = s.mode_first_order ? s.fo_tau_size : s.tau_size;
@@ -1664,8 +1988,8 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
     invGa[i] = 1.0 / (c_G[i] * (1.0 - c_alpha[i]));
     erconst[i] = c_alpha[i] * c_G[i] + 1.0 / (i + 2);
   }
-  double *y = c.y, *f = c.f, *ynew = c.ynew, *difkp1 = c.difkp1, *psiv = c.psiv, *del = c.del, *invwt = c.invwt;
-  double *dif = c.dif;
+  auto y = c.y, f = c.f, ynew = c.ynew, difkp1 = c.difkp1, psiv = c.psiv, del = c.del, invwt = c.invwt;
+  auto dif = c.dif;
   double t = t0, hmax = 0.1 * fabs(t1 - t0);
   if (include_t0)
     while (jout < nout && tout_at(c, jout) <= t0) {
@@ -1679,7 +2003,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
   prepare_table(c, t, tca);
   rhs(c, tca, t, y, f);
   st.n_rhs++;
-  jacobian(c, tca, t);
+  jacobian<T>(c, tca, t);
   st.n_jac++;
   int Jcurrent = 1;
   double hmin = 16 * eps * fabs(t);
@@ -1749,7 +2073,8 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
           st.n_rhs++;
           for (int i = tid; i < n; i += nt) del[i] = hinvGak * f[i] - (psiv[i] + difkp1[i]);
           c.sync();
-          lu_solve<T>(c);
+          if constexpr (sizeof(T) == sizeof(float)) inv_solve<T>(c);
+          else lu_solve<T>(c);
           unsigned long long vn = 0;
           for (int i = tid; i < n; i += nt) {
             bmax(vn, del[i] * invwt[i]);
@@ -1793,7 +2118,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
             nconhk = 0;
           } else {
             prepare(c, t, 0);
-            jacobian(c, tca, t);
+            jacobian<T>(c, tca, t);
             st.n_jac++;
             Jcurrent = 1;
           }
@@ -1821,23 +2146,21 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
             for (int i = tid; i < n; i += nt) bmax(vk, (dif[(size_t)(k - 1) * n + i] + difkp1[i]) * invwt[i]);
             errkm1 = block_max_bits(c, vk) * erconst[k - 2];
           }
-          /* the FP64 powers are evaluated once and broadcast */
-          if (tid == 0) {
-            double hopt = absh * fmax(0.1, 0.833 * pow(rtol / err, 1.0 / (k + 1)));
-            int knew = k;
-            if (k > 1) {
-              double hkm1 = absh * fmax(0.1, 0.769 * pow(rtol / errkm1, 1.0 / k));
-              if (hkm1 > hopt) {
-                hopt = fmin(absh, hkm1);
-                knew = k - 1;
-              }
-            }
-            c.sh->ctl[0] = hopt;
-            c.sh->ctl[1] = knew;
+          /* the FP64 powers are evaluated side by side and shared */
+          for (int q = tid; q < 2; q += nt) {
+            if (q == 0) c.sh->ctl[0] = absh * fmax(0.1, 0.833 * pow(rtol / err, 1.0 / (k + 1)));
+            else if (k > 1) c.sh->ctl[1] = absh * fmax(0.1, 0.769 * pow(rtol / errkm1, 1.0 / k));
           }
           c.sync();
           double hopt = c.sh->ctl[0];
-          k = (int)c.sh->ctl[1];
+          if (k > 1) {
+            double hkm1 = c.sh->ctl[1];
+            if (hkm1 > hopt) {
+              hopt = fmin(absh, hkm1);
+              k = k - 1;
+            }
+          }
+          c.sync();
           absh = fmax(hmin, hopt);
         } else {
           absh = fmax(hmin, 0.5 * absh);
@@ -1892,28 +2215,27 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
         if (k < maxk) bmax(vp, dif[(size_t)(k + 1) * n + i] * invwt[i]);
       }
       double errkm1 = block_max_bits(c, vk), errkp1 = block_max_bits(c, vp);
-      if (tid == 0) {
-        double temp = 1.2 * pow(err / rtol, 1.0 / (k + 1));
-        double hopt = (temp > 0.1) ? absh / temp : 10 * absh;
-        int kopt = k;
-        if (k > 1) {
-          errkm1 *= erconst[k - 2];
-          temp = 1.3 * pow(errkm1 / rtol, 1.0 / k);
-          double hkm1 = (temp > 0.1) ? absh / temp : 10 * absh;
-          if (hkm1 > hopt) { hopt = hkm1; kopt = k - 1; }
+      /* the three candidate step sizes, side by side */
+      for (int q = tid; q < 3; q += nt) {
+        double temp, hq = 0.0;
+        if (q == 0) {
+          temp = 1.2 * pow(err / rtol, 1.0 / (k + 1));
+          hq = (temp > 0.1) ? absh / temp : 10 * absh;
+        } else if (q == 1 && k > 1) {
+          temp = 1.3 * pow(errkm1 * erconst[k - 2] / rtol, 1.0 / k);
+          hq = (temp > 0.1) ? absh / temp : 10 * absh;
+        } else if (q == 2 && k < maxk) {
+          temp = 1.4 * pow(errkp1 * erconst[k] / rtol, 1.0 / (k + 2));
+          hq = (temp > 0.1) ? absh / temp : 10 * absh;
         }
-        if (k < maxk) {
-          errkp1 *= erconst[k];
-          temp = 1.4 * pow(errkp1 / rtol, 1.0 / (k + 2));
-          double hkp1 = (temp > 0.1) ? absh / temp : 10 * absh;
-          if (hkp1 > hopt) { hopt = hkp1; kopt = k + 1; }
-        }
-        c.sh->ctl[0] = hopt;
-        c.sh->ctl[1] = kopt;
+        c.sh->ctl[q] = hq;
       }
       c.sync();
       double hopt = c.sh->ctl[0];
-      int kopt = (int)c.sh->ctl[1];
+      int kopt = k;
+      if (k > 1 && c.sh->ctl[1] > hopt) { hopt = c.sh->ctl[1]; kopt = k - 1; }
+      if (k < maxk && c.sh->ctl[2] > hopt) { hopt = c.sh->ctl[2]; kopt = k + 1; }
+      c.sync();
       if (hopt > absh) {
         absh = hopt;
         if (k != kopt) k = kopt;
@@ -1929,7 +2251,7 @@ __device__ int ndf15(const K &c, double t0, double t1, int &jout, int include_t0
 
 /* ------------------------------------------------------------------ one triplet */
 
-template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_stats &st) {
+template <typename T, class C> __device__ int solve_triplet(const C &c, song2_triplet_stats &st) {
   const DevSpec &s = c.s;
   int tid = c.rank;
   if (geometry(c)) return SONG2_E_CONFIG;
@@ -1954,7 +2276,7 @@ template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_sta
          else carries over */
       prepare_table(c, ta, 1);
       if (tid == 0) {
-        YVec yv{c.y};
+        auto yv = yvec(c.y);
         compute_ws(c, 1, yv, 0, c.sh->ws);
         WS &w = c.sh->ws;
         for (int im = 0; im <= s.index_m_max[1]; ++im) c.y[c.idx_I[c.LM(1, s.m[im])]] = w.I_1m_tca1[s.m[im]];
@@ -1978,10 +2300,38 @@ template <typename T> __device__ int solve_triplet(const K &c, song2_triplet_sta
   return SONG2_OK;
 }
 
-template <typename T, int WARP_TEAM>
+/* set up the team's triplet from its work item (rank 0) */
+template <class C> __device__ void begin_item(const C &c, int item) {
+  const DevPtrs &p = c.p;
+  WorkItem wi = p.items[item];
+  if (c.rank == 0) {
+    Tri &t = c.sh->tri;
+    t.i1 = wi.i1; t.i2 = wi.i2; t.i3 = wi.i3; t.pair = wi.pair; t.item = item;
+    t.k1 = p.k[wi.i1];
+    t.k2 = p.k[wi.i2];
+    t.k3_size = p.k3_size[wi.pair];
+    t.k = p.k3[p.k3_off[wi.pair] + wi.i3];
+    t.pair_off = p.pair_off[wi.pair];
+  }
+  c.sync();
+}
+
+template <typename T, class C> __device__ void run_item(const C &c, int item) {
+  begin_item(c, item);
+  song2_triplet_stats st;
+  st.status = 0; st.n_steps = 0; st.n_rejected = 0; st.n_rhs = 0; st.n_jac = 0; st.n_lu = 0; st.n_newton_fail = 0;
+  st.sources_calls = 0;
+  int stc = solve_triplet<T>(c, st);
+  st.status = stc;
+  if (c.rank == 0) c.p.stats[item] = st;
+  c.sync();
+}
+
+/* CTA or warp per triplet: persistent, one item at a time from the queue */
+template <typename T, int MODE>
 __global__ void __launch_bounds__(256) evolver_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
   extern __shared__ __align__(16) char smem[];
-  K c(s, p, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64, WARP_TEAM);
+  KX<MODE> c(s, p, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64);
   c.load_tables();
   c.sync();
   for (int guard = 0; guard < s.n_items + 1; ++guard) {
@@ -1989,24 +2339,27 @@ __global__ void __launch_bounds__(256) evolver_kernel(const __grid_constant__ De
     c.sync();
     int item = c.sh->item;
     if (item >= s.n_items) break;
-    WorkItem wi = p.items[item];
-    if (c.rank == 0) {
-      Tri &t = c.sh->tri;
-      t.i1 = wi.i1; t.i2 = wi.i2; t.i3 = wi.i3; t.pair = wi.pair; t.item = item;
-      t.k1 = p.k[wi.i1];
-      t.k2 = p.k[wi.i2];
-      t.k3_size = p.k3_size[wi.pair];
-      t.k = p.k3[p.k3_off[wi.pair] + wi.i3];
-      t.pair_off = p.pair_off[wi.pair];
-    }
-    c.sync();
-    song2_triplet_stats st;
-    st.status = 0; st.n_steps = 0; st.n_rejected = 0; st.n_rhs = 0; st.n_jac = 0; st.n_lu = 0; st.n_newton_fail = 0;
-    st.sources_calls = 0;
-    int stc = solve_triplet<T>(c, st);
-    st.status = stc;
-    if (c.rank == 0) p.stats[item] = st;
-    c.sync();
+    run_item<T>(c, item);
+  }
+}
+
+/* G lanes per triplet: each warp takes the next 32/G items of the cost-sorted
+   queue at once, so that its teams advance through similar triplets side by side. */
+template <typename T>
+__global__ void __launch_bounds__(128) team_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
+  extern __shared__ __align__(16) char smem[];
+  KX<MODE_TEAM> c(s, p, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64);
+  c.load_tables();
+  __syncthreads();
+  int lane = threadIdx.x & 31, tiw = lane / s.team_lanes;
+  for (int guard = 0; guard < s.n_items + 1; ++guard) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(p.queue, c.nt);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= s.n_items) break;
+    int item = base + tiw;
+    if (item < s.n_items) run_item<T>(c, item);
+    __syncwarp();
   }
 }
 
@@ -2017,25 +2370,32 @@ size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in
   return make_plan(spec, precision, lu_in_smem).total;
 }
 
+size_t song2_team_smem_bytes(const DevSpec &spec, int teams_per_cta) {
+  return team_tables_bytes(spec) + sizeof(Shared) * (size_t)teams_per_cta;
+}
+
+int song2_team_slab_doubles(const DevSpec &spec) { return make_team_plan(spec).total; }
+
 namespace {
 template <typename T, int W> void *kernel_ptr() { return (void *)evolver_kernel<T, W>; }
-void *pick_kernel(int precision, int warp_team) {
-  if (precision == SONG2_PREC_MIXED) return warp_team ? kernel_ptr<float, 1>() : kernel_ptr<float, 0>();
-  return warp_team ? kernel_ptr<double, 1>() : kernel_ptr<double, 0>();
+void *pick_kernel(int precision, int mode) {
+  if (mode == 2) return precision == SONG2_PREC_MIXED ? (void *)team_kernel<float> : (void *)team_kernel<double>;
+  if (precision == SONG2_PREC_MIXED) return mode ? kernel_ptr<float, MODE_WARP>() : kernel_ptr<float, MODE_BLOCK>();
+  return mode ? kernel_ptr<double, MODE_WARP>() : kernel_ptr<double, MODE_BLOCK>();
 }
 } // namespace
 
-int song2_max_ctas_per_sm(int precision, int warp_team, int block, size_t smem) {
+int song2_max_ctas_per_sm(int precision, int mode, int block, size_t smem) {
   int nb = 0;
-  const void *f = pick_kernel(precision, warp_team);
+  const void *f = pick_kernel(precision, mode);
   cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, block, smem);
   return e == cudaSuccess ? nb : 0;
 }
 
-int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int warp_team, int grid, int block,
+int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int mode, int grid, int block,
                          size_t smem, cudaStream_t stream) {
-  const void *f = pick_kernel(precision, warp_team);
+  const void *f = pick_kernel(precision, mode);
   cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   DevSpec sp = spec;
   DevPtrs pp = ptrs;

@@ -93,10 +93,14 @@ def test_closure_limit_is_rejected(lib):
     assert b"closure" in err.value
 
 
-@pytest.mark.parametrize("launch", [(1, 2, 32, 0), (1, 8, 32, 0), (1, 4, 32, 1), (0, 1, 128, 1), (0, 1, 256, 0)])
+@pytest.mark.parametrize("launch", [(1, 2, 32, 0), (1, 8, 32, 0), (1, 4, 32, 1), (0, 1, 128, 1), (0, 1, 256, 0),
+                                    (2, 32, 1, 0), (2, 64, 2, 0), (2, 32, 4, 0), (2, 16, 8, 0), (2, 4, 32, 0)])
 def test_launch_configurations_agree(lib, tiny, launch):
-    """Every launch configuration the autotuner may pick computes the same numbers."""
-    p, _, _ = tiny
+    """Every launch configuration the autotuner may pick computes the same numbers:
+    bit for bit among the CTA- and warp-per-triplet kernels (same instruction
+    stream per row); the lane-team kernel is compiled separately, so its floating
+    point contractions may differ and it is held to the solver tolerance."""
+    p, ref, _ = tiny
     base, _, _ = gpu_run(lib, p, capi.SONG2_PREC_MIXED)
     L = capi.Launch(*launch)
     c = C.c_void_p()
@@ -105,9 +109,15 @@ def test_launch_configurations_agree(lib, tiny, launch):
                                    C.byref(c), err) == 0, err.value
     assert lib.song2_ctx_run(c, None, err) == 0, err.value
     src = np.zeros_like(base)
-    lib.song2_ctx_download(c, capi.dptr(src), None, err)
+    st = (capi.TripletStats * p.n_triplets)()
+    lib.song2_ctx_download(c, capi.dptr(src), st, err)
     lib.song2_ctx_destroy(c)
-    assert np.array_equal(src, base)
+    assert np.all(np.frombuffer(st, dtype=capi.STATS_DTYPE)["status"] == capi.SONG2_OK)
+    if launch[0] == 2:
+        assert np.max(floored_errors(src, base, p)) < 10 * p.spec.rtol
+        assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+    else:
+        assert np.array_equal(src, base)
 
 
 def test_give_up_path_returns_status(lib, tiny):
