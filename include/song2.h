@@ -121,6 +121,19 @@ typedef struct {
   const double *k3;                        /* concatenated k3 grids of the pairs, pair order */
   int tau_size;
   const double *tau;                       /* [tau_size] ascending */
+  /* Uneven batches (no counterpart in the reference, whose hierarchy sizes are
+     run-wide).  n_classes > 0 gives every triplet a class; triplets are numbered
+     in pair order (k1 ascending, k2 <= k1, k3 ascending: the order of the
+     concatenated k3 grids).  A class sets l_max of the photon intensity,
+     polarisation and neutrino hierarchies and evolves the modes m = 0..m_max.
+     The run-wide l_max and mode list above must cover every class: they fix the
+     source types (a class's sources for modes it does not evolve are zero) and
+     the first-order tables.  n_classes = 0: every triplet uses the run-wide
+     hierarchy. */
+  int n_classes;
+  const int *class_l_max;                  /* [n_classes] */
+  const int *class_m_max;                  /* [n_classes] */
+  const int *triplet_class;                /* [n_triplets], pair order */
 } song2_spec;
 
 /* Background/thermo and first-order interpolation tables, owned by the caller

@@ -118,7 +118,7 @@ double song2_oracle_coupling(int kind, int l, int m1, int m) {
 
 /* ======================================================= configuration */
 
-typedef struct {
+typedef struct cfg_s {
   const song2_spec *s;
   const song2_tables *t;
   int m_size, m[SONG2_MAX_M];
@@ -136,10 +136,15 @@ typedef struct {
   int first_order_mode;
   int tp2_size, index_tp2_T, index_tp2_E, index_tp2_B, index_tp2_delta_cdm;
   int64_t n_triplets;
+  /* the run-wide configuration, which fixes the source types (itself, except for
+     the hierarchy classes of an uneven batch) */
+  const struct cfg_s *run;
 } cfg_t;
 
 #define LM(l, m) (c->lm_array[(l)][c->index_m[(m)]])
 #define LMQ(l, m) (c->lm_quad[(l)][(m)])
+/* source-type index of (l, m) in the run-wide layout */
+#define RLM(l, m) (c->run->lm_array[(l)][c->run->index_m[(m)]])
 
 static int size_l_indexm(const cfg_t *c, int l_max) {
   int n = 0;
@@ -152,6 +157,7 @@ static int size_l_indexm(const cfg_t *c, int l_max) {
 static int cfg_init(cfg_t *c, const song2_spec *s, const song2_tables *t, int fo_l_max, char *err) {
   memset(c, 0, sizeof(*c));
   c->s = s; c->t = t;
+  c->run = c;
   c->m_size = s->m_size;
   for (int i = 0; i < SONG2_MAX_M; ++i) c->index_m[i] = -1;
   for (int i = 0; i < s->m_size; ++i) {
@@ -1629,7 +1635,7 @@ static void store_sources(ws_t *w, int index_tau, double tau, const double *y, c
           src -= I_2_raw(l + 1) * r_plus_12(l, m) * k1 * (phi_1 + psi_1) - I_2_raw(l - 1) * r_minus_12(l, m) * k1 * (phi_1 + psi_1) +
                  I_1_raw(l + 1) * r_plus_21(l, m) * k2 * (phi_2 + psi_2) - I_1_raw(l - 1) * r_minus_21(l, m) * k2 * (phi_2 + psi_2);
         src *= exp_m_kappa;
-        base[(int64_t)(c->index_tp2_T + LM(l, m)) * w->per_type] = src;
+        base[(int64_t)(c->run->index_tp2_T + RLM(l, m)) * w->per_type] = src;
       }
   }
   if (s->has_source_E) {
@@ -1650,7 +1656,7 @@ static void store_sources(ws_t *w, int index_tau, double tau, const double *y, c
           src -= E_2_raw(l + 1) * k_plus_12(l, m) * k1 * (phi_1 + psi_1) - E_2_raw(l - 1) * k_minus_12(l, m) * k1 * (phi_1 + psi_1) +
                  E_1_raw(l + 1) * k_plus_21(l, m) * k2 * (phi_2 + psi_2) - E_1_raw(l - 1) * k_minus_21(l, m) * k2 * (phi_2 + psi_2);
         src *= exp_m_kappa;
-        base[(int64_t)(c->index_tp2_E + LM(l, m)) * w->per_type] = src;
+        base[(int64_t)(c->run->index_tp2_E + RLM(l, m)) * w->per_type] = src;
       }
   }
   if (s->has_source_B) {
@@ -1664,12 +1670,12 @@ static void store_sources(ws_t *w, int index_tau, double tau, const double *y, c
         if (s->has_redshift_in_los) src -= -E_2_raw(l) * 4 * d_zero_12(l, m) * k1 * psi_1 - E_1_raw(l) * 4 * d_zero_21(l, m) * k2 * psi_2;
         if (s->has_lensing_in_los) src -= -E_2_raw(l) * k_zero_12(l, m) * k1 * (phi_1 + psi_1) - E_1_raw(l) * k_zero_21(l, m) * k2 * (phi_2 + psi_2);
         src *= exp_m_kappa;
-        base[(int64_t)(c->index_tp2_B + LM(l, m)) * w->per_type] = src;
+        base[(int64_t)(c->run->index_tp2_B + RLM(l, m)) * w->per_type] = src;
       }
   }
   if (s->has_source_delta_cdm && c->compute_m[0]) {
     double v_dot_v_cdm = -w->k1_dot_k2 * fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM];
-    base[(int64_t)c->index_tp2_delta_cdm * w->per_type] = 0.5 * (cdm(0, 0, 0) - 2 * v_dot_v_cdm);
+    base[(int64_t)c->run->index_tp2_delta_cdm * w->per_type] = 0.5 * (cdm(0, 0, 0) - 2 * v_dot_v_cdm);
   }
 }
 
@@ -2157,7 +2163,7 @@ static int solve_triplet(ws_t *w, const double *tout, int nout, output_fn out, d
 
 /* ======================================================= drivers */
 
-typedef struct { int i1, i2, i3; double *k3row; int k3_size; int64_t pair_off; } trip_t;
+typedef struct { int i1, i2, i3; double *k3row; int k3_size; int64_t pair_off, porder; } trip_t;
 
 static int64_t build_work(const song2_spec *s, trip_t *list) {
   /* k3 grids are concatenated in pair order (i1 ascending, i2 <= i1 ascending) */
@@ -2178,6 +2184,7 @@ static int64_t build_work(const song2_spec *s, trip_t *list) {
           list[n].k3row = (double *)(s->k3 + k3off[i1 * s->k_size + i2]);
           list[n].k3_size = nk3;
           list[n].pair_off = po;
+          list[n].porder = k3off[i1 * s->k_size + i2] + i3;
         }
         ++n;
       }
@@ -2204,28 +2211,75 @@ static int evolve_impl(const song2_spec *s, const song2_tables *t, double *src, 
   cfg_t c;
   if (cfg_init(&c, s, t, t->fo_l_max, err)) return 1;
   if (t->fo_l_max < c.L_big + 1) { snprintf(err, SONG2_ERRLEN, "first-order table l_max too small"); cfg_free(&c); return 1; }
+  /* hierarchy classes of an uneven batch: the run-wide spec with the class's l_max
+     and modes 0..m_max; the source types stay the run-wide ones */
+  int ncls = s->n_classes > 0 ? s->n_classes : 0;
+  song2_spec *cspec = NULL;
+  cfg_t *ccfg = NULL;
+  if (ncls) {
+    if (!s->class_l_max || !s->class_m_max || !s->triplet_class) {
+      snprintf(err, SONG2_ERRLEN, "n_classes > 0 needs class_l_max, class_m_max and triplet_class");
+      cfg_free(&c);
+      return 1;
+    }
+    cspec = (song2_spec *)calloc(ncls, sizeof(song2_spec));
+    ccfg = (cfg_t *)calloc(ncls, sizeof(cfg_t));
+    for (int k = 0; k < ncls; ++k) {
+      int L = s->class_l_max[k], mm = s->class_m_max[k];
+      int bad = L < 2 || L > s->l_max_g || L > s->l_max_ur || (s->has_polarization2 && L > s->l_max_pol_g) || mm < 0 ||
+                mm >= SONG2_MAX_M;
+      for (int m = 0; !bad && m <= mm; ++m) bad = !c.compute_m[m];
+      cspec[k] = *s;
+      cspec[k].n_classes = 0;
+      cspec[k].l_max_g = cspec[k].l_max_ur = L;
+      if (s->has_polarization2) cspec[k].l_max_pol_g = L;
+      cspec[k].m_size = mm + 1;
+      for (int m = 0; m <= mm; ++m) cspec[k].m[m] = m;
+      if (bad || cfg_init(&ccfg[k], &cspec[k], t, t->fo_l_max, err)) {
+        if (bad) snprintf(err, SONG2_ERRLEN, "class %d: l_max or m_max not covered by the run-wide spec", k);
+        for (int q = 0; q < k; ++q) cfg_free(&ccfg[q]);
+        free(ccfg); free(cspec); cfg_free(&c);
+        return 1;
+      }
+      ccfg[k].run = &c;
+    }
+  }
   int64_t n = build_work(s, NULL);
   trip_t *list = (trip_t *)malloc(sizeof(trip_t) * (n > 0 ? n : 1));
   build_work(s, list);
+  int failed = 0;
   if (first < 0) first = 0;
   if (!sel && first + count > n) count = n - first;
   if (sel)
     for (int64_t i = 0; i < count; ++i)
-      if (sel[i] < 0 || sel[i] >= n) { snprintf(err, SONG2_ERRLEN, "bad item"); free(list); cfg_free(&c); return 1; }
+      if (sel[i] < 0 || sel[i] >= n) { snprintf(err, SONG2_ERRLEN, "bad item"); failed = -1; }
+  if (ncls)
+    for (int64_t i = 0; i < n; ++i) {
+      int k = s->triplet_class[list[i].porder];
+      if (k < 0 || k >= ncls) { snprintf(err, SONG2_ERRLEN, "triplet_class entry out of range"); failed = -1; }
+    }
   int64_t per_type = (int64_t)s->tau_size * o_n_triplets(s);
-  int failed = 0;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
-#pragma omp parallel
+#pragma omp parallel if (failed == 0)
   {
-    ws_t *w = ws_alloc(&c);
-    double *ybuf = (double *)calloc(w->nmax, sizeof(double));
+    ws_t *w = NULL;
+    cfg_t *wc = NULL;
+    double *ybuf = NULL;
     char lerr[SONG2_ERRLEN];
 #pragma omp for schedule(dynamic)
     for (int64_t jt = first; jt < first + count; ++jt) {
+      if (failed < 0) continue;
       int64_t it = sel ? sel[jt] : jt;
       trip_t *tr = &list[it];
+      cfg_t *tc = ncls ? &ccfg[s->triplet_class[tr->porder]] : &c;
+      if (tc != wc) {
+        if (w) { ws_free(w); free(ybuf); }
+        w = ws_alloc(tc);
+        ybuf = (double *)calloc(w->nmax, sizeof(double));
+        wc = tc;
+      }
       memset(&w->st, 0, sizeof(w->st));
       w->src_flat = src;
       w->per_type = per_type;
@@ -2241,11 +2295,14 @@ static int evolve_impl(const song2_spec *s, const song2_tables *t, double *src, 
         failed++;
       }
     }
-    free(ybuf);
-    ws_free(w);
+    if (w) { ws_free(w); free(ybuf); }
   }
   free(list);
+  for (int k = 0; k < ncls; ++k) cfg_free(&ccfg[k]);
+  free(ccfg);
+  free(cspec);
   cfg_free(&c);
+  if (failed < 0) return 1;
   if (failed) { snprintf(err, SONG2_ERRLEN, "%d triplets failed", failed); return 1; }
   return 0;
 }

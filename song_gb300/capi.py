@@ -68,6 +68,8 @@ class Spec(C.Structure):
         ("k_size", C.c_int), ("k", C.POINTER(C.c_double)),
         ("k3_size", C.POINTER(C.c_int)), ("k3", C.POINTER(C.c_double)),
         ("tau_size", C.c_int), ("tau", C.POINTER(C.c_double)),
+        ("n_classes", C.c_int), ("class_l_max", C.POINTER(C.c_int)), ("class_m_max", C.POINTER(C.c_int)),
+        ("triplet_class", C.POINTER(C.c_int)),
     ]
 
 

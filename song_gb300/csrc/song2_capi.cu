@@ -319,6 +319,48 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   s.fo_E = SONG2_FO_I + (s.fo_l_max + 1);
   s.fo_N = SONG2_FO_I + 2 * (s.fo_l_max + 1);
   s.fo_CG = SONG2_FO_I + 3 * (s.fo_l_max + 1);
+  s.lu_stride = s.lu_elems;
+  s.qtab_stride = (long)s.fo_tau_size * 2 * s.qs2_size;
+  return 0;
+}
+
+/* Layouts of the hierarchy classes of an uneven batch: the run-wide spec with the
+   class's l_max and modes 0..m_max; the source types stay the run-wide ones. */
+int build_class_layouts(const song2_spec *sp, const song2_tables *tab, const DevSpec &run, std::vector<HostLayout> &HC,
+                        char *err) {
+  if (!sp->class_l_max || !sp->class_m_max || !sp->triplet_class) {
+    snprintf(err, SONG2_ERRLEN, "n_classes > 0 needs class_l_max, class_m_max and triplet_class");
+    return 1;
+  }
+  HC.resize(sp->n_classes);
+  for (int k = 0; k < sp->n_classes; ++k) {
+    int L = sp->class_l_max[k], mm = sp->class_m_max[k];
+    if (L < 2 || L > sp->l_max_g || L > sp->l_max_ur || (sp->has_polarization2 && L > sp->l_max_pol_g)) {
+      snprintf(err, SONG2_ERRLEN, "class %d: l_max %d outside 2..run-wide l_max", k, L);
+      return 1;
+    }
+    if (mm < 0 || mm >= SONG2_MAX_M) {
+      snprintf(err, SONG2_ERRLEN, "class %d: m_max %d outside 0..%d", k, mm, SONG2_MAX_M - 1);
+      return 1;
+    }
+    for (int m = 0; m <= mm; ++m)
+      if (!run.compute_m[m]) {
+        snprintf(err, SONG2_ERRLEN, "class %d: mode %d is not in the run-wide mode list", k, m);
+        return 1;
+      }
+    song2_spec sc = *sp;
+    sc.n_classes = 0;
+    sc.l_max_g = sc.l_max_ur = L;
+    if (sp->has_polarization2) sc.l_max_pol_g = L;
+    sc.m_size = mm + 1;
+    for (int m = 0; m <= mm; ++m) sc.m[m] = m;
+    if (build_layout(&sc, tab, 0, HC[k], err)) return 1;
+    DevSpec &d = HC[k].s;
+    d.tp2_size = run.tp2_size;
+    memcpy(d.tp_kind, run.tp_kind, sizeof(d.tp_kind));
+    memcpy(d.tp_l, run.tp_l, sizeof(d.tp_l));
+    memcpy(d.tp_m, run.tp_m, sizeof(d.tp_m));
+  }
   return 0;
 }
 
@@ -361,6 +403,22 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   }
   if (build_layout(sp, tab, first_order_mode, H, err)) return 1;
   DevSpec &s = H.s;
+  std::vector<HostLayout> HC;
+  int classes = !first_order_mode && sp->n_classes > 0;
+  if (classes && build_class_layouts(sp, tab, s, HC, err)) return 1;
+  if (classes)
+    for (const WorkItem &w : items)
+      if (w.cls < 0 || w.cls >= sp->n_classes) {
+        snprintf(err, SONG2_ERRLEN, "triplet_class entry %d outside 0..%d", w.cls, sp->n_classes - 1);
+        return 1;
+      }
+  if (classes) {
+    /* scratch strides of the largest class */
+    for (auto &hc : HC) {
+      s.lu_stride = std::max(s.lu_stride, hc.s.lu_elems);
+      s.qtab_stride = std::max(s.qtab_stride, hc.s.qtab_stride);
+    }
+  }
   if (first_order_mode) {
     s.fo_l_max = fo_l_max;
     s.nfo = song2_fo_size(fo_l_max);
@@ -389,8 +447,7 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   if (stack < 4096) CK(cudaDeviceSetLimit(cudaLimitStackSize, 4096));
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  /* launch configuration: explicit, or the default (one warp per triplet, four per
-     CTA, iteration matrices in the L2-resident scratch) */
+  /* launch configuration: explicit, or the default below */
   song2_launch L = c->launch;
   /* SONG2_LAUNCH="warp_team,teams_per_cta,threads_per_team,lu_in_smem" overrides the
      automatic choice (used to pin a configuration in profiling commands) */
@@ -401,11 +458,20 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
       L.warp_team = a; L.teams_per_cta = b; L.threads_per_team = t; L.lu_in_smem = d;
     }
   }
-  if (L.teams_per_cta <= 0 && L.threads_per_team <= 0 && !L.warp_team) {
+  if (classes) {
+    /* uneven batches run one CTA per triplet */
     L.warp_team = 0;
     L.teams_per_cta = 1;
-    L.threads_per_team = 256;
-    L.lu_in_smem = 0;
+    if (L.threads_per_team <= 0) L.threads_per_team = 256;
+  }
+  if (L.teams_per_cta <= 0 && L.threads_per_team <= 0 && !L.warp_team) {
+    /* measured on config-2-sized problems: the mixed form is fastest with 256
+       threads and the FP32 inverse in shared memory (two CTAs per SM), the FP64
+       form with 128 threads and its LU blocks in global scratch (four per SM) */
+    L.warp_team = 0;
+    L.teams_per_cta = 1;
+    L.threads_per_team = precision == SONG2_PREC_MIXED ? 256 : 128;
+    L.lu_in_smem = precision == SONG2_PREC_MIXED ? 1 : 0;
   }
   if (L.warp_team == 2) {
     /* G lanes per triplet: G a power of two up to 32, whole warps per CTA, at most
@@ -430,18 +496,25 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     L.threads_per_team = std::min(256, (L.threads_per_team / 32) * 32);
     c->block = L.threads_per_team;
   }
-  size_t with_lu = song2_smem_bytes(s, precision, c->block, 1) * L.teams_per_cta;
-  if (L.lu_in_smem && with_lu > (size_t)smem_optin) L.lu_in_smem = 0;
+  /* shared memory of a CTA: the team plans (the largest class in uneven batches,
+     after the copy of the class spec) */
+  auto plan_bytes = [&](int lu) -> size_t {
+    if (!classes) return song2_smem_bytes(s, precision, c->block, lu) * L.teams_per_cta;
+    size_t mx = 0;
+    for (auto &hc : HC) mx = std::max(mx, song2_smem_bytes(hc.s, precision, c->block, lu));
+    return song2_class_spec_bytes() + mx;
+  };
+  if (L.lu_in_smem && plan_bytes(1) > (size_t)smem_optin) L.lu_in_smem = 0;
   s.lu_in_smem = L.lu_in_smem;
   s.team_lanes = L.warp_team == 2 ? L.threads_per_team : 0;
   if (L.warp_team == 2) c->smem = song2_team_smem_bytes(s, L.teams_per_cta);
-  else c->smem = song2_smem_bytes(s, precision, c->block, s.lu_in_smem) * L.teams_per_cta;
+  else c->smem = plan_bytes(s.lu_in_smem);
   if (c->smem > (size_t)smem_optin) {
     snprintf(err, SONG2_ERRLEN, "shared-memory plan %zu B exceeds the %d B limit", c->smem, smem_optin);
     return 1;
   }
   c->launch = L;
-  int per_sm = song2_max_ctas_per_sm(precision, L.warp_team, c->block, c->smem);
+  int per_sm = song2_max_ctas_per_sm(precision, classes ? 3 : L.warp_team, c->block, c->smem);
   if (per_sm < 1) {
     snprintf(err, SONG2_ERRLEN, "launch configuration does not fit on an SM");
     return 1;
@@ -481,18 +554,47 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   } else {
     p.fo = p.fo_dd = p.bg;  /* never read in first-order mode */
   }
-  if (upload(c, H.cmin, &p.cmin, st, err) || upload(c, H.cplu, &p.cplu, st, err) || upload(c, H.dmin, &p.dmin, st, err) ||
-      upload(c, H.dplu, &p.dplu, st, err) || upload(c, H.dzer, &p.dzer, st, err))
+  if (upload(c, H.cmin, &p.tabs.cmin, st, err) || upload(c, H.cplu, &p.tabs.cplu, st, err) || upload(c, H.dmin, &p.tabs.dmin, st, err) ||
+      upload(c, H.dplu, &p.tabs.dplu, st, err) || upload(c, H.dzer, &p.tabs.dzer, st, err))
     return 1;
-  if (upload(c, H.eq_sp, &p.eq_sp, st, err) || upload(c, H.eq_l, &p.eq_l, st, err) || upload(c, H.eq_m, &p.eq_m, st, err))
+  if (upload(c, H.eq_sp, &p.tabs.eq_sp, st, err) || upload(c, H.eq_l, &p.tabs.eq_l, st, err) || upload(c, H.eq_m, &p.tabs.eq_m, st, err))
     return 1;
-  if (upload(c, H.idx_I, &p.idx_I, st, err) || upload(c, H.idx_E, &p.idx_E, st, err) ||
-      upload(c, H.idx_B, &p.idx_B, st, err) || upload(c, H.idx_N, &p.idx_N, st, err))
+  if (upload(c, H.idx_I, &p.tabs.idx_I, st, err) || upload(c, H.idx_E, &p.tabs.idx_E, st, err) ||
+      upload(c, H.idx_B, &p.tabs.idx_B, st, err) || upload(c, H.idx_N, &p.tabs.idx_N, st, err))
     return 1;
-  if (upload(c, H.qs_sp, &p.qs_sp, st, err) || upload(c, H.qs_l, &p.qs_l, st, err) || upload(c, H.qs_m, &p.qs_m, st, err))
+  if (upload(c, H.qs_sp, &p.tabs.qs_sp, st, err) || upload(c, H.qs_l, &p.tabs.qs_l, st, err) || upload(c, H.qs_m, &p.tabs.qs_m, st, err))
     return 1;
-  if (upload(c, H.row_slot, &p.row_slot, st, err) || upload(c, H.qs_slot, &p.qs_slot, st, err)) return 1;
+  if (upload(c, H.row_slot, &p.tabs.row_slot, st, err) || upload(c, H.qs_slot, &p.tabs.qs_slot, st, err)) return 1;
   if (upload(c, items, &p.items, st, err)) return 1;
+  if (classes) {
+    /* per-class specs (run-level fields from the run-wide spec) and tables */
+    std::vector<DevSpec> cspec;
+    std::vector<ClassTabs> ctabs;
+    for (auto &hc : HC) {
+      DevSpec d = hc.s;
+      d.n_items = s.n_items;
+      d.per_type = s.per_type;
+      d.lu_in_smem = s.lu_in_smem;
+      d.team_lanes = 0;
+      d.lu_stride = s.lu_stride;
+      d.qtab_stride = s.qtab_stride;
+      cspec.push_back(d);
+      ClassTabs t;
+      memset(&t, 0, sizeof(t));
+      if (upload(c, hc.cmin, &t.cmin, st, err) || upload(c, hc.cplu, &t.cplu, st, err) ||
+          upload(c, hc.dmin, &t.dmin, st, err) || upload(c, hc.dplu, &t.dplu, st, err) ||
+          upload(c, hc.dzer, &t.dzer, st, err) || upload(c, hc.eq_sp, &t.eq_sp, st, err) ||
+          upload(c, hc.eq_l, &t.eq_l, st, err) || upload(c, hc.eq_m, &t.eq_m, st, err) ||
+          upload(c, hc.idx_I, &t.idx_I, st, err) || upload(c, hc.idx_E, &t.idx_E, st, err) ||
+          upload(c, hc.idx_B, &t.idx_B, st, err) || upload(c, hc.idx_N, &t.idx_N, st, err) ||
+          upload(c, hc.qs_sp, &t.qs_sp, st, err) || upload(c, hc.qs_l, &t.qs_l, st, err) ||
+          upload(c, hc.qs_m, &t.qs_m, st, err) || upload(c, hc.row_slot, &t.row_slot, st, err) ||
+          upload(c, hc.qs_slot, &t.qs_slot, st, err))
+        return 1;
+      ctabs.push_back(t);
+    }
+    if (upload(c, cspec, &p.class_spec, st, err) || upload(c, ctabs, &p.class_tabs, st, err)) return 1;
+  }
   if (!first_order_mode) {
     c->sources_len = (size_t)s.tp2_size * per_type;
     if (alloc_dev(c, std::max<size_t>(1, c->sources_len) * sizeof(double), &tmp, err)) return 1;
@@ -510,11 +612,11 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   p.stats = c->d_stats;
   /* Evolver scratch: the Jacobian blocks of each resident CTA, and the LU
      blocks when they do not fit in shared memory. */
-  if (alloc_dev(c, (size_t)c->n_teams * s.lu_elems * sizeof(double), &tmp, err)) return 1;
+  if (alloc_dev(c, (size_t)c->n_teams * s.lu_stride * sizeof(double), &tmp, err)) return 1;
   p.jac = (double *)tmp;
   /* quadratic-source tables of the resident triplets, and the spline recurrence */
   if (s.has_qs) {
-    if (alloc_dev(c, (size_t)c->n_teams * s.fo_tau_size * 2 * s.qs2_size * sizeof(double), &tmp, err)) return 1;
+    if (alloc_dev(c, (size_t)c->n_teams * s.qtab_stride * sizeof(double), &tmp, err)) return 1;
     p.qtab = (double *)tmp;
   }
   {
@@ -529,7 +631,7 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   }
   if (!s.lu_in_smem) {
     size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
-    if (alloc_dev(c, (size_t)c->n_teams * s.lu_elems * ts, &tmp, err)) return 1;
+    if (alloc_dev(c, (size_t)c->n_teams * s.lu_stride * ts, &tmp, err)) return 1;
     p.lu_global = tmp;
   }
   if (L.warp_team == 2) {
@@ -579,8 +681,14 @@ static void sorted_items(const song2_spec *spec, const std::vector<double> &k3, 
   for (int i1 = 0; i1 < spec->k_size; ++i1)
     for (int i2 = 0; i2 <= i1; ++i2, ++pair)
       for (int i3 = 0; i3 < k3_size[pair]; ++i3) {
-        items.push_back(WorkItem{i1, i2, i3, pair});
+        /* hierarchy class of an uneven batch (triplets numbered in pair order) */
+        int has_cls = spec->n_classes > 0 && spec->triplet_class && spec->class_l_max && spec->class_m_max;
+        int cls = has_cls ? spec->triplet_class[k3_off[pair] + i3] : 0;
+        items.push_back(WorkItem{i1, i2, i3, pair, cls});
         double kk = std::max(spec->k[i1], std::max(spec->k[i2], k3[k3_off[pair] + i3]));
+        /* cost: steps grow with k; per-step work with the class's hierarchy size */
+        if (has_cls && cls >= 0 && cls < spec->n_classes)
+          kk *= (spec->class_l_max[cls] + 1.0) * (spec->class_m_max[cls] + 1.0);
         cost.push_back(kk);
       }
   /* reference order start of every pair */
@@ -696,7 +804,7 @@ int song2_autotune(const song2_spec *spec, const song2_tables *tab, int precisio
   size_t stride = std::max<size_t>(1, sorted.size() / (size_t)sample);
   for (size_t i = 0; i < sorted.size() && (int)pick.size() < sample; i += stride) pick.push_back(sorted[i]);
   const song2_launch cands[] = {
-      {1, 2, 32, 0}, {1, 4, 32, 0}, {1, 8, 32, 0}, {1, 4, 32, 1}, {0, 1, 128, 1}, {0, 1, 256, 1}, {0, 1, 256, 0},
+      {1, 4, 32, 0}, {1, 8, 32, 0}, {0, 1, 128, 0}, {0, 1, 128, 1}, {0, 1, 256, 1}, {0, 1, 256, 0}, {2, 16, 8, 0},
   };
   double bestv = 1e300;
   int found = 0;
@@ -916,6 +1024,10 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   char *base = (char *)g_noalloc_addr[dev];
   cudaStream_t st = (cudaStream_t)stream;
 
+  if (spec->n_classes > 0) {
+    snprintf(err, SONG2_ERRLEN, "hierarchy classes are not supported by the allocation-free entry");
+    return 1;
+  }
   HostLayout H;
   if (build_layout(spec, tab_dev, 0, H, err)) return 1;
   DevSpec s = H.s;
@@ -1022,14 +1134,14 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   p.k3_size = (const int *)(base + o_k3sz);
   p.pair_off = (const int64_t *)(base + o_poff);
   p.bg = tab_dev->bg; p.bg_dd = tab_dev->bg_dd; p.fo = tab_dev->fo; p.fo_dd = tab_dev->fo_dd;
-  p.cmin = (const double *)(base + o_cm); p.cplu = (const double *)(base + o_cp);
-  p.dmin = (const double *)(base + o_dm); p.dplu = (const double *)(base + o_dp);
-  p.dzer = (const double *)(base + o_dz);
-  p.eq_sp = (const short *)(base + o_esp); p.eq_l = (const short *)(base + o_el); p.eq_m = (const short *)(base + o_em);
-  p.idx_I = (const short *)(base + o_iI); p.idx_E = (const short *)(base + o_iE);
-  p.idx_B = (const short *)(base + o_iB); p.idx_N = (const short *)(base + o_iN);
-  p.qs_sp = (const short *)(base + o_qsp); p.qs_l = (const short *)(base + o_ql); p.qs_m = (const short *)(base + o_qm);
-  p.row_slot = (const short *)(base + o_rsl); p.qs_slot = (const short *)(base + o_qsl);
+  p.tabs.cmin = (const double *)(base + o_cm); p.tabs.cplu = (const double *)(base + o_cp);
+  p.tabs.dmin = (const double *)(base + o_dm); p.tabs.dplu = (const double *)(base + o_dp);
+  p.tabs.dzer = (const double *)(base + o_dz);
+  p.tabs.eq_sp = (const short *)(base + o_esp); p.tabs.eq_l = (const short *)(base + o_el); p.tabs.eq_m = (const short *)(base + o_em);
+  p.tabs.idx_I = (const short *)(base + o_iI); p.tabs.idx_E = (const short *)(base + o_iE);
+  p.tabs.idx_B = (const short *)(base + o_iB); p.tabs.idx_N = (const short *)(base + o_iN);
+  p.tabs.qs_sp = (const short *)(base + o_qsp); p.tabs.qs_l = (const short *)(base + o_ql); p.tabs.qs_m = (const short *)(base + o_qm);
+  p.tabs.row_slot = (const short *)(base + o_rsl); p.tabs.qs_slot = (const short *)(base + o_qsl);
   p.items = (const WorkItem *)(base + o_items);
   p.sources = sources_dev;
   p.stats = stats_dev;

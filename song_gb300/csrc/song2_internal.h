@@ -70,12 +70,24 @@ struct DevSpec {
   /* shared-memory plan */
   int lu_in_smem;
   int lu_elems;                    /* sum of blk_size^2 */
+  int lu_stride;                   /* per-team Jacobian/LU scratch (>= lu_elems; the largest class) */
+  long qtab_stride;                /* per-team quadratic-source table (doubles) */
   int lu_off[S2_MAXBLK];
 };
 
 /* Per-triplet work item: indices and where its sources go. */
 struct WorkItem {
   int i1, i2, i3, pair;            /* pair = index of (i1,i2) in pair order */
+  int cls;                         /* hierarchy class (uneven batches), else 0 */
+};
+
+/* Tables that depend on the hierarchy layout (one set per class in uneven batches). */
+struct ClassTabs {
+  const double *cmin, *cplu, *dmin, *dplu, *dzer;   /* [n_lm][3] */
+  const short *eq_sp, *eq_l, *eq_m;                  /* [n] */
+  const short *idx_I, *idx_E, *idx_B, *idx_N;        /* [n_lm] -> state index or -1 */
+  const short *qs_sp, *qs_l, *qs_m;                  /* [qs2_size] */
+  const short *row_slot, *qs_slot;                   /* [n_row_slots], [n_qs_slots]: index or -1 */
 };
 
 /* Device pointers of a run. */
@@ -84,11 +96,9 @@ struct DevPtrs {
   const int *k3_off, *k3_size;     /* per pair */
   const int64_t *pair_off;         /* per pair, in doubles, within one source type */
   const double *bg, *bg_dd, *fo, *fo_dd;
-  const double *cmin, *cplu, *dmin, *dplu, *dzer;   /* [n_lm][3] */
-  const short *eq_sp, *eq_l, *eq_m;                  /* [n] */
-  const short *idx_I, *idx_E, *idx_B, *idx_N;        /* [n_lm] -> state index or -1 */
-  const short *qs_sp, *qs_l, *qs_m;                  /* [qs2_size] */
-  const short *row_slot, *qs_slot;                   /* [n_row_slots], [n_qs_slots]: index or -1 */
+  ClassTabs tabs;                  /* uniform runs */
+  const DevSpec *class_spec;       /* uneven batches: per class, else null */
+  const ClassTabs *class_tabs;
   const WorkItem *items;
   double *sources;                 /* [tp2][per_type] */
   double *fo_out;                  /* first-order mode: [k][tau][q] */
@@ -105,13 +115,17 @@ struct DevPtrs {
 
 /* host-side launcher implemented in song2_kernels.cu.  mode 0: one CTA per
    triplet; 1: one warp per triplet (several per CTA); 2: spec.team_lanes lanes per
-   triplet, arrays in global slabs (tslab, txsol, tpiv, jac, lu_global, qtab). */
+   triplet, arrays in global slabs (tslab, txsol, tpiv, jac, lu_global, qtab);
+   3: one CTA per triplet with hierarchy classes (ptrs.class_spec set; the dynamic
+   shared memory starts with song2_class_spec_bytes() for the class spec copy).
+   Mode 0 with ptrs.class_spec set launches mode 3. */
 int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int mode, int grid, int block,
                          size_t smem, cudaStream_t stream);
 /* shared memory of one team (one CTA in block mode, one warp in warp mode) */
 size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in_smem);
 /* shared memory of a team-kernel CTA, and the doubles of one team's slab */
 size_t song2_team_smem_bytes(const DevSpec &spec, int teams_per_cta);
+size_t song2_class_spec_bytes();
 int song2_team_slab_doubles(const DevSpec &spec);
 int song2_max_ctas_per_sm(int precision, int mode, int block, size_t smem);
 

@@ -182,6 +182,7 @@ template <int MODE> struct KX {
   using DA = View<double, STR>;
   const DevSpec &s;
   const DevPtrs &p;
+  const ClassTabs &ct;
   int rank, size;          /* this thread's rank in its team, team size */
   long team;               /* global team index (per-team global scratch) */
   unsigned tmask;          /* lanes of the team (MODE_TEAM) */
@@ -225,7 +226,8 @@ template <int MODE> struct KX {
     qs_slot = tb;
   }
 
-  __device__ KX(const DevSpec &s_, const DevPtrs &p_, char *smem_all, int prec) : s(s_), p(p_) {
+  __device__ KX(const DevSpec &s_, const DevPtrs &p_, const ClassTabs &ct_, char *smem_all, int prec)
+      : s(s_), p(p_), ct(ct_) {
     size_t ts = prec == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
     if constexpr (MODE == MODE_TEAM) {
       int G = s_.team_lanes, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
@@ -248,9 +250,9 @@ template <int MODE> struct KX {
       sh = (Shared *)(smem_all + team_tables_bytes(s_)) + (long)warp * nt + tiw;
       xsol_b = (char *)p_.txsol + (gw * (long)s_.n * nt + tiw) * ts;
       piv = View<int, STR>{p_.tpiv + gw * (long)s_.n * nt + tiw, nt};
-      lu_b = (char *)p_.lu_global + (gw * (long)s_.lu_elems * nt + tiw) * ts;
-      jac = da(p_.jac + gw * (long)s_.lu_elems * nt + tiw);
-      qtab = da(p_.qtab ? p_.qtab + gw * (long)s_.fo_tau_size * 2 * s_.qs2_size * nt + tiw : nullptr);
+      lu_b = (char *)p_.lu_global + (gw * (long)s_.lu_stride * nt + tiw) * ts;
+      jac = da(p_.jac + gw * (long)s_.lu_stride * nt + tiw);
+      qtab = da(p_.qtab ? p_.qtab + gw * s_.qtab_stride * nt + tiw : nullptr);
     } else {
       Plan pl = make_plan(s_, prec, s_.lu_in_smem);
       char *smem = smem_all;
@@ -277,9 +279,9 @@ template <int MODE> struct KX {
       xsol_b = smem + pl.xsol;
       piv = View<int, STR>{(int *)(smem + pl.piv)};
       if (s_.lu_in_smem) lu_b = smem + pl.lu;
-      else lu_b = (char *)p_.lu_global + (size_t)team * s_.lu_elems * ts;
-      jac = da(p_.jac + (size_t)team * s_.lu_elems);
-      qtab = da(p_.qtab ? p_.qtab + (size_t)team * s_.fo_tau_size * 2 * s_.qs2_size : nullptr);
+      else lu_b = (char *)p_.lu_global + (size_t)team * s_.lu_stride * ts;
+      jac = da(p_.jac + (size_t)team * s_.lu_stride);
+      qtab = da(p_.qtab ? p_.qtab + (size_t)team * s_.qtab_stride : nullptr);
     }
   }
   __device__ void sync() const {
@@ -299,24 +301,24 @@ template <int MODE> struct KX {
       lmq_s[e] = s.lmq[e / (SONG2_MAX_M + 2)][e % (SONG2_MAX_M + 2)];
     for (int e = r; e < SONG2_MAX_M; e += z) im_s[e] = (short)s.index_m[e];
     for (int e = r; e < s.n; e += z) {
-      eq_sp[e] = p.eq_sp[e]; eq_l[e] = p.eq_l[e]; eq_m[e] = p.eq_m[e];
+      eq_sp[e] = ct.eq_sp[e]; eq_l[e] = ct.eq_l[e]; eq_m[e] = ct.eq_m[e];
     }
     for (int e = r; e < s.n_lm; e += z) {
-      idx_I[e] = p.idx_I[e]; idx_E[e] = p.idx_E[e]; idx_B[e] = p.idx_B[e]; idx_N[e] = p.idx_N[e];
+      idx_I[e] = ct.idx_I[e]; idx_E[e] = ct.idx_E[e]; idx_B[e] = ct.idx_B[e]; idx_N[e] = ct.idx_N[e];
     }
     for (int e = r; e < s.qs2_size; e += z) {
-      qs_sp[e] = p.qs_sp[e]; qs_l[e] = p.qs_l[e]; qs_m[e] = p.qs_m[e];
+      qs_sp[e] = ct.qs_sp[e]; qs_l[e] = ct.qs_l[e]; qs_m[e] = ct.qs_m[e];
     }
-    for (int e = r; e < s.n_row_slots; e += z) row_slot[e] = p.row_slot[e];
-    for (int e = r; e < s.n_qs_slots; e += z) qs_slot[e] = p.qs_slot[e];
+    for (int e = r; e < s.n_row_slots; e += z) row_slot[e] = ct.row_slot[e];
+    for (int e = r; e < s.n_qs_slots; e += z) qs_slot[e] = ct.qs_slot[e];
   }
   /* summed couplings, index X in 0..19 */
   __device__ double S(int X, int l, int m) const { return sc[X * s.n_lm + LM(l, m)]; }
-  __device__ double cmin(int l, int m1, int m) const { return __ldg(p.cmin + LM(l, m) * 3 + m - m1 + 1); }
-  __device__ double cplu(int l, int m1, int m) const { return __ldg(p.cplu + LM(l, m) * 3 + m - m1 + 1); }
-  __device__ double dmin(int l, int m1, int m) const { return __ldg(p.dmin + LM(l, m) * 3 + m - m1 + 1); }
-  __device__ double dplu(int l, int m1, int m) const { return __ldg(p.dplu + LM(l, m) * 3 + m - m1 + 1); }
-  __device__ double dzer(int l, int m1, int m) const { return __ldg(p.dzer + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double cmin(int l, int m1, int m) const { return __ldg(ct.cmin + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double cplu(int l, int m1, int m) const { return __ldg(ct.cplu + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double dmin(int l, int m1, int m) const { return __ldg(ct.dmin + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double dplu(int l, int m1, int m) const { return __ldg(ct.dplu + LM(l, m) * 3 + m - m1 + 1); }
+  __device__ double dzer(int l, int m1, int m) const { return __ldg(ct.dzer + LM(l, m) * 3 + m - m1 + 1); }
   __device__ double rot_1(int l, int m) const {
     if (l < 0 || abs(m) > l) return 0.0;
     double v = rot1[LMQ(l, abs(m))];
@@ -1572,6 +1574,11 @@ __device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) 
   for (int tp = c.rank; tp < s.tp2_size; tp += c.size) {
     int kind = s.tp_kind[tp], l = s.tp_l[tp], m = s.tp_m[tp];
     double src = 0.0;
+    if (!s.compute_m[m]) {
+      /* a mode this triplet's hierarchy class does not evolve */
+      c.p.sources[(int64_t)tp * s.per_type + col] = 0.0;
+      continue;
+    }
     if (kind == TP_T) {
       if (l == 0) {
         src += kd * w.I_00;
@@ -1764,9 +1771,9 @@ template <class C> __device__ int geometry(const C &c) {
     for (int X = 0; X < 20; ++X) a[X] = 0.0;
     for (int m2 = -1; m2 <= 1; ++m2) {
       int m1 = m - m2;
-      double cm = __ldg(c.p.cmin + lm * 3 + m - m1 + 1), cp = __ldg(c.p.cplu + lm * 3 + m - m1 + 1);
-      double dm = __ldg(c.p.dmin + lm * 3 + m - m1 + 1), dp = __ldg(c.p.dplu + lm * 3 + m - m1 + 1);
-      double dz = __ldg(c.p.dzer + lm * 3 + m - m1 + 1);
+      double cm = __ldg(c.ct.cmin + lm * 3 + m - m1 + 1), cp = __ldg(c.ct.cplu + lm * 3 + m - m1 + 1);
+      double dm = __ldg(c.ct.dmin + lm * 3 + m - m1 + 1), dp = __ldg(c.ct.dplu + lm * 3 + m - m1 + 1);
+      double dz = __ldg(c.ct.dzer + lm * 3 + m - m1 + 1);
       double r11 = c.rot_1(1, m2), r21 = c.rot_2(1, m2);
       double r1m = c.rot_1(l - 1, m1), r2m = c.rot_2(l - 1, m1), r1p = c.rot_1(l + 1, m1), r2p = c.rot_2(l + 1, m1);
       double r10 = c.rot_1(l, m1), r20 = c.rot_2(l, m1);
@@ -2327,19 +2334,47 @@ template <typename T, class C> __device__ void run_item(const C &c, int item) {
   c.sync();
 }
 
-/* CTA or warp per triplet: persistent, one item at a time from the queue */
-template <typename T, int MODE>
+/* CTA or warp per triplet: persistent, one item at a time from the queue.  With
+   hierarchy classes (uneven batches, CTA teams only) the item's class spec is
+   copied into shared memory and the team's context is rebuilt for it. */
+template <typename T, int MODE, int CLASSES>
 __global__ void __launch_bounds__(256) evolver_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
   extern __shared__ __align__(16) char smem[];
-  KX<MODE> c(s, p, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64);
-  c.load_tables();
-  c.sync();
-  for (int guard = 0; guard < s.n_items + 1; ++guard) {
-    if (c.rank == 0) c.sh->item = atomicAdd(p.queue, 1);
+  __shared__ int s_item[8];
+  const int prec = sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64;
+  if constexpr (!CLASSES) {
+    KX<MODE> c(s, p, p.tabs, smem, prec);
+    int slot = MODE == MODE_WARP ? (threadIdx.x >> 5) : 0;
+    c.load_tables();
     c.sync();
-    int item = c.sh->item;
-    if (item >= s.n_items) break;
-    run_item<T>(c, item);
+    for (int guard = 0; guard < s.n_items + 1; ++guard) {
+      if (c.rank == 0) s_item[slot] = atomicAdd(p.queue, 1);
+      c.sync();
+      int item = s_item[slot];
+      c.sync();
+      if (item >= s.n_items) break;
+      run_item<T>(c, item);
+    }
+  } else {
+    DevSpec *cs = (DevSpec *)smem;
+    char *rest = smem + al(sizeof(DevSpec));
+    for (int guard = 0; guard < s.n_items + 1; ++guard) {
+      if (threadIdx.x == 0) s_item[0] = atomicAdd(p.queue, 1);
+      __syncthreads();
+      int item = s_item[0];
+      __syncthreads();
+      if (item >= s.n_items) break;
+      int cls = p.items[item].cls;
+      static_assert(sizeof(DevSpec) % sizeof(long long) == 0, "DevSpec copy granularity");
+      const long long *src = (const long long *)(p.class_spec + cls);
+      long long *dst = (long long *)cs;
+      for (int e = threadIdx.x; e < (int)(sizeof(DevSpec) / sizeof(long long)); e += blockDim.x) dst[e] = src[e];
+      __syncthreads();
+      KX<MODE> c(*cs, p, p.class_tabs[cls], rest, prec);
+      c.load_tables();
+      c.sync();
+      run_item<T>(c, item);
+    }
   }
 }
 
@@ -2348,7 +2383,7 @@ __global__ void __launch_bounds__(256) evolver_kernel(const __grid_constant__ De
 template <typename T>
 __global__ void __launch_bounds__(128) team_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
   extern __shared__ __align__(16) char smem[];
-  KX<MODE_TEAM> c(s, p, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64);
+  KX<MODE_TEAM> c(s, p, p.tabs, smem, sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64);
   c.load_tables();
   __syncthreads();
   int lane = threadIdx.x & 31, tiw = lane / s.team_lanes;
@@ -2370,6 +2405,8 @@ size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in
   return make_plan(spec, precision, lu_in_smem).total;
 }
 
+size_t song2_class_spec_bytes() { return al(sizeof(DevSpec)); }
+
 size_t song2_team_smem_bytes(const DevSpec &spec, int teams_per_cta) {
   return team_tables_bytes(spec) + sizeof(Shared) * (size_t)teams_per_cta;
 }
@@ -2377,11 +2414,14 @@ size_t song2_team_smem_bytes(const DevSpec &spec, int teams_per_cta) {
 int song2_team_slab_doubles(const DevSpec &spec) { return make_team_plan(spec).total; }
 
 namespace {
-template <typename T, int W> void *kernel_ptr() { return (void *)evolver_kernel<T, W>; }
+template <typename T, int W, int CL> void *kernel_ptr() { return (void *)evolver_kernel<T, W, CL>; }
+/* mode 3: CTA per triplet with hierarchy classes */
 void *pick_kernel(int precision, int mode) {
   if (mode == 2) return precision == SONG2_PREC_MIXED ? (void *)team_kernel<float> : (void *)team_kernel<double>;
-  if (precision == SONG2_PREC_MIXED) return mode ? kernel_ptr<float, MODE_WARP>() : kernel_ptr<float, MODE_BLOCK>();
-  return mode ? kernel_ptr<double, MODE_WARP>() : kernel_ptr<double, MODE_BLOCK>();
+  if (mode == 3)
+    return precision == SONG2_PREC_MIXED ? kernel_ptr<float, MODE_BLOCK, 1>() : kernel_ptr<double, MODE_BLOCK, 1>();
+  if (precision == SONG2_PREC_MIXED) return mode ? kernel_ptr<float, MODE_WARP, 0>() : kernel_ptr<float, MODE_BLOCK, 0>();
+  return mode ? kernel_ptr<double, MODE_WARP, 0>() : kernel_ptr<double, MODE_BLOCK, 0>();
 }
 } // namespace
 
@@ -2395,6 +2435,7 @@ int song2_max_ctas_per_sm(int precision, int mode, int block, size_t smem) {
 
 int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int mode, int grid, int block,
                          size_t smem, cudaStream_t stream) {
+  if (ptrs.class_spec && mode == 0) mode = 3;
   const void *f = pick_kernel(precision, mode);
   cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   DevSpec sp = spec;

@@ -26,9 +26,15 @@ CONFIGS = {
             m=(0, 1, 2), rtol=1e-4, tau_size=200, sources="TE"),
     3: dict(name="config3_mixed_16.4k", k_min=1e-5, k_max=0.3, k_size=40, k3_size=20, l_max=20,
             m=(0, 1, 2), rtol=1e-4, tau_size=200, sources="TE"),
+    4: dict(name="config4_uneven_30k", k_min=1e-5, k_max=0.3, k_size=50, k3_size=24, l_max=40,
+            m=(0, 1, 2, 3, 4), rtol=1e-4, tau_size=200, sources="TEB", uneven=dict(seed=20261203)),
     5: dict(name="config5_production_97k", k_min=1e-5, k_max=0.4, k_size=80, k3_size=30, l_max=25,
             m=(0, 1, 2), rtol=1e-5, tau_size=400, sources="TE"),
 }
+
+# Uneven batches: l_max = min(L_CAP, L_BASE + ceil(k tau_rec / 2)) with k = max(k1, k2, k3),
+# m_max drawn from M_MAX_CHOICES per triplet (pair order).
+L_BASE, L_CAP, M_MAX_CHOICES = 8, 40, (0, 2, 4)
 
 TAU_START_SOURCES = 200.0   # Mpc, just before recombination (tau_rec ~ 280 Mpc)
 
@@ -39,7 +45,7 @@ class Problem:
     def __init__(self, k_min, k_max, k_size, k3_size, l_max, m=(0,), rtol=1e-4, tau_size=50,
                  tau_ini=TAU_START_SOURCES, tau_end=None, sources="TE", cosmo=None, bg_size=6000,
                  k_log=True, k3_log=False, tau_log=False, los="intrinsic", threshold=1e-6,
-                 fo_dlntau=0.01, lib=None, **spec_overrides):
+                 fo_dlntau=0.01, lib=None, uneven=None, **spec_overrides):
         self.lib = lib or capi.load()
         lib = self.lib
         err = capi.errbuf()
@@ -113,6 +119,9 @@ class Problem:
         t.bg_dd = capi.dptr(self.bg_dd)
         self.tables = t
         self.fo_l_max = max(l_max, s.l_max_los_t, s.l_max_los_p) + 1
+        self.classes = None
+        if uneven:
+            self.set_uneven(**uneven)
         # first-order time grid: uniform in ln tau from before the earliest start time to tau0
         kmax_all = 2.0 * float(self.k[-1])
         tau_ini_min = C.c_double()
@@ -124,6 +133,64 @@ class Problem:
         self.fo_lntau0 = lo
         self.fo_dlntau = (hi - lo) / (self.fo_tau_size - 1)
         self.fo = None
+
+    # ------------------------------------------------------------------ uneven batches
+    def tau_rec(self):
+        """Conformal time of the visibility peak (kappa' e^-kappa) on the background grid."""
+        lnkd = self.bg[:, capi.BG_LN_KAPPA_DOT]
+        kap = self.bg[:, capi.BG_KAPPA]
+        i = int(np.argmax(lnkd - kap))
+        return float(np.exp(self.tables.bg_lntau0 + i * self.tables.bg_dlntau))
+
+    def set_uneven(self, seed=20261203, l_base=None, l_cap=None, m_choices=None, l_max_fn=None):
+        """Give every triplet (pair order) its hierarchy class: l_max from its largest
+        wavenumber, m_max drawn from the choices with a seeded generator."""
+        l_base = L_BASE if l_base is None else l_base
+        l_cap = L_CAP if l_cap is None else l_cap
+        m_choices = M_MAX_CHOICES if m_choices is None else m_choices
+        trec = self.tau_rec()
+        n = len(self.k)
+        kmax = []
+        off = 0
+        for i1 in range(n):
+            for i2 in range(i1 + 1):
+                nk3 = int(self.k3_size[i1 * n + i2])
+                for i3 in range(nk3):
+                    kmax.append(max(self.k[i1], self.k[i2], self.k3[off + i3]))
+                off += nk3
+        kmax = np.array(kmax)
+        if l_max_fn is None:
+            lmax = np.minimum(l_cap, l_base + np.ceil(kmax * trec / 2.0)).astype(int)
+        else:
+            lmax = np.array([l_max_fn(k) for k in kmax], dtype=int)
+        lmax = np.minimum(lmax, self.spec.l_max_g)
+        rng = np.random.default_rng(seed)
+        mmax = rng.choice(np.array(m_choices), size=len(kmax))
+        mmax = np.minimum(mmax, max(self.spec.m[i] for i in range(self.spec.m_size)))
+        pairs = sorted(set(zip(lmax.tolist(), mmax.tolist())))
+        index = {pq: i for i, pq in enumerate(pairs)}
+        self.class_l_max = np.array([a for a, _ in pairs], dtype=np.int32)
+        self.class_m_max = np.array([b for _, b in pairs], dtype=np.int32)
+        self.triplet_class = np.array([index[(a, b)] for a, b in zip(lmax.tolist(), mmax.tolist())], dtype=np.int32)
+        self.classes = pairs
+        s = self.spec
+        s.n_classes = len(pairs)
+        s.class_l_max = capi.iptr(self.class_l_max)
+        s.class_m_max = capi.iptr(self.class_m_max)
+        s.triplet_class = capi.iptr(self.triplet_class)
+
+    def class_sizes(self):
+        """Number of equations (outside tight coupling) of every triplet's class."""
+        if self.classes is None:
+            return None
+        out = []
+        for L, mm in self.classes:
+            nh = sum(1 for l in range(L + 1) for m in range(mm + 1) if m <= l)
+            ne = sum(1 for l in range(2, L + 1) for m in range(mm + 1) if m <= l)
+            nb = sum(1 for l in range(2, L + 1) for m in range(1, mm + 1) if m <= l)
+            extra = 4 + (3 if mm >= 1 else 0) + (2 if mm >= 2 else 0)
+            out.append(2 * nh + ne + nb + extra)
+        return np.array(out)[self.triplet_class]
 
     # ------------------------------------------------------------------ sizes
     @property
