@@ -69,7 +69,7 @@ struct Shared {
   double ctl[4];
   int item;
   int lu_fail;
-  float gjp[S2_MAXBLK];    /* Gauss-Jordan: reciprocal pivot of each block */
+  int kl[S2_MAXBLK], ku[S2_MAXBLK];   /* band of each block's Jacobian */
   int tca;
 };
 
@@ -205,8 +205,11 @@ template <int MODE> struct KX {
   }
   template <typename E> __device__ View<E, STR> xsol() const { return mk<E>(xsol_b); }
   template <typename E> __device__ View<E, STR> lu() const { return mk<E>(lu_b); }
-  /* the Jacobian blocks, stored in the iteration-matrix precision */
-  template <typename E> __device__ View<E, STR> jacv() const { return mk<E>((char *)jac.p); }
+  /* the Jacobian blocks, stored in the iteration-matrix precision: element offset
+     jac_eoff counted in elements of that precision, so the teams' regions stay
+     disjoint whatever the element size */
+  long jac_eoff;
+  template <typename E> __device__ View<E, STR> jacv() const { return mk<E>((char *)((E *)p.jac + jac_eoff)); }
 
   __device__ void set_tables(short *tb) {
     lm_s = tb; tb += (s.Lq + 1) * SONG2_MAX_M;
@@ -251,7 +254,8 @@ template <int MODE> struct KX {
       xsol_b = (char *)p_.txsol + (gw * (long)s_.n * nt + tiw) * ts;
       piv = View<int, STR>{p_.tpiv + gw * (long)s_.n * nt + tiw, nt};
       lu_b = (char *)p_.lu_global + (gw * (long)s_.lu_stride * nt + tiw) * ts;
-      jac = da(p_.jac + gw * (long)s_.lu_stride * nt + tiw);
+      jac_eoff = gw * (long)s_.lu_stride * nt + tiw;
+      jac = da(p_.jac + jac_eoff);
       qtab = da(p_.qtab ? p_.qtab + gw * s_.qtab_stride * nt + tiw : nullptr);
     } else {
       Plan pl = make_plan(s_, prec, s_.lu_in_smem);
@@ -280,7 +284,8 @@ template <int MODE> struct KX {
       piv = View<int, STR>{(int *)(smem + pl.piv)};
       if (s_.lu_in_smem) lu_b = smem + pl.lu;
       else lu_b = (char *)p_.lu_global + (size_t)team * s_.lu_stride * ts;
-      jac = da(p_.jac + (size_t)team * s_.lu_stride);
+      jac_eoff = (long)team * s_.lu_stride;
+      jac = da(p_.jac + jac_eoff);
       qtab = da(p_.qtab ? p_.qtab + (size_t)team * s_.qtab_stride : nullptr);
     }
   }
@@ -1189,6 +1194,8 @@ template <class C, class A, class B> __device__ void rhs(const C &c, int tca, do
 template <typename T, class C> __device__ void jacobian(const C &c, int tca, double tau) {
   const DevSpec &s = c.s;
   auto J0 = c.template jacv<T>();
+  for (int b = c.rank; b < s.nblk; b += c.size) c.sh->kl[b] = c.sh->ku[b] = 0;
+  c.sync();
   for (int j = c.rank; j < s.n; j += c.size) {
     int b = 0;
     while (b + 1 < s.nblk && j >= s.blk_start[b + 1]) ++b;
@@ -1197,200 +1204,33 @@ template <typename T, class C> __device__ void jacobian(const C &c, int tca, dou
     WS w;
     compute_ws(c, tca, yu, 1, w);
     auto J = J0 + s.lu_off[b];
-    for (int i = b0; i < b0 + nb; ++i) J[(i - b0) * nb + (j - b0)] = (T)row(c, tca, i, yu, w, 1, tau);
+    int lo = 0, up = 0;
+    for (int i = b0; i < b0 + nb; ++i) {
+      T v = (T)row(c, tca, i, yu, w, 1, tau);
+      J[(i - b0) * nb + (j - b0)] = v;
+      if (v != T(0)) {
+        if (i > j) lo = max(lo, i - j);
+        else up = max(up, j - i);
+      }
+    }
+    atomicMax(&c.sh->kl[b], lo);
+    atomicMax(&c.sh->ku[b], up);
   }
   c.sync();
 }
 
-/* ------------------------------------------------------------------ block LU per m (one warp each) */
+/* ------------------------------------------------------------------ banded LU per m block */
+
+/* Within an m block the state is ordered l-major (metric and matter first, then
+   I_l, E_l, B_l, N_l for increasing l), so the iteration matrix of each block is
+   banded: free streaming couples l to l +- 1, Thomson scattering and the closure
+   stay within an l, and the Einstein and fluid equations couple the lowest
+   multipoles.  The band (kl below, ku above the diagonal) is measured on every
+   new Jacobian; the factorisation and the solves touch the band only, so their
+   cost is O(n kl (kl + ku)) and O(n (kl + ku)) per block instead of O(n^3) and
+   O(n^2).  The blocks keep their dense row-major storage. */
 
 template <typename T> __device__ inline T tabs(T x) { return x < T(0) ? -x : x; }
-
-/* One m block, factorised by a group of W lanes (a warp, or a team of MODE_TEAM):
-   partial pivoting, row-major in place. */
-template <typename T, class C>
-__device__ void group_lu(const C &c, int b, int lane, int W, unsigned mask) {
-  const DevSpec &s = c.s;
-  auto A = c.template lu<T>() + s.lu_off[b];
-  int nb = s.blk_size[b];
-  auto pv = c.piv + s.blk_start[b];
-  for (int kk = 0; kk < nb; ++kk) {
-    T best = T(-1);
-    int bi = kk;
-    for (int i = kk + lane; i < nb; i += W) {
-      T v = tabs(A[i * nb + kk]);
-      if (v > best) { best = v; bi = i; }
-    }
-    for (int off = W >> 1; off > 0; off >>= 1) {
-      T ob = __shfl_xor_sync(mask, best, off);
-      int oi = __shfl_xor_sync(mask, bi, off);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-    }
-    if (lane == 0) pv[kk] = bi;
-    if (!(best > T(0))) {
-      if (lane == 0) {
-        c.sh->lu_fail = 1;
-        A[kk * nb + kk] = T(1);
-      }
-      __syncwarp(mask);
-      continue;
-    }
-    if (bi != kk)
-      for (int j = lane; j < nb; j += W) {
-        T tmp = A[kk * nb + j];
-        A[kk * nb + j] = A[bi * nb + j];
-        A[bi * nb + j] = tmp;
-      }
-    __syncwarp(mask);
-    T inv = T(1) / A[kk * nb + kk];
-    for (int i = kk + 1 + lane; i < nb; i += W) A[i * nb + kk] *= inv;
-    __syncwarp(mask);
-    for (int i = kk + 1; i < nb; ++i) {
-      T lik = A[i * nb + kk];
-      if (lik != T(0))
-        for (int j = kk + 1 + lane; j < nb; j += W) A[i * nb + j] -= lik * A[kk * nb + j];
-    }
-    __syncwarp(mask);
-  }
-}
-
-template <typename T, class C> __device__ void form_and_factor(const C &c, double hinvGak) {
-  const DevSpec &s = c.s;
-  auto LU = c.template lu<T>();
-  auto J = c.template jacv<T>();
-  for (int e = c.rank; e < s.lu_elems; e += c.size) {
-    int b = 0;
-    while (b + 1 < s.nblk && e >= s.lu_off[b + 1]) ++b;
-    int nb = s.blk_size[b], r = (e - s.lu_off[b]) / nb, col = (e - s.lu_off[b]) % nb;
-    double v = -hinvGak * J[e];
-    if (r == col) v += 1.0;
-    LU[e] = (T)v;
-  }
-  c.sync();
-  if constexpr (C::STR) {
-    for (int b = 0; b < s.nblk; ++b) group_lu<T>(c, b, c.rank, c.size, c.tmask);
-  } else if (c.size == 32) {
-    for (int b = 0; b < s.nblk; ++b) group_lu<T>(c, b, c.rank, 32, 0xffffffffu);
-  } else {
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int b = warp; b < s.nblk; b += nw) group_lu<T>(c, b, lane, 32, 0xffffffffu);
-  }
-  c.sync();
-}
-
-/* one m block, solved by a group of W lanes */
-template <typename T, class C>
-__device__ void group_solve(const C &c, int b, int lane, int W, unsigned mask) {
-  const DevSpec &s = c.s;
-  int nb = s.blk_size[b];
-  auto A = c.template lu<T>() + s.lu_off[b];
-  auto pv = c.piv + s.blk_start[b];
-  auto xb = c.template xsol<T>() + s.blk_start[b];
-  if (lane == 0)
-    for (int kk = 0; kk < nb; ++kk) {
-      int q = pv[kk];
-      if (q != kk) { T tmp = xb[kk]; xb[kk] = xb[q]; xb[q] = tmp; }
-    }
-  __syncwarp(mask);
-  for (int j = 0; j < nb; ++j) {
-    T xj = xb[j];
-    for (int i = j + 1 + lane; i < nb; i += W) xb[i] -= A[i * nb + j] * xj;
-    __syncwarp(mask);
-  }
-  for (int j = nb - 1; j >= 0; --j) {
-    if (lane == 0) xb[j] /= A[j * nb + j];
-    __syncwarp(mask);
-    T xj = xb[j];
-    for (int i = lane; i < j; i += W) xb[i] -= A[i * nb + j] * xj;
-    __syncwarp(mask);
-  }
-}
-
-/* del <- M^{-1} rhs (rhs given in c.del, result written back to c.del) */
-template <typename T, class C> __device__ void lu_solve(const C &c) {
-  const DevSpec &s = c.s;
-  auto x = c.template xsol<T>();
-  for (int i = c.rank; i < s.n; i += c.size) x[i] = (T)c.del[i];
-  c.sync();
-  if constexpr (C::STR) {
-    for (int b = 0; b < s.nblk; ++b) group_solve<T>(c, b, c.rank, c.size, c.tmask);
-  } else if (c.size == 32) {
-    for (int b = 0; b < s.nblk; ++b) group_solve<T>(c, b, c.rank, 32, 0xffffffffu);
-  } else {
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int b = warp; b < s.nblk; b += nw) group_solve<T>(c, b, lane, 32, 0xffffffffu);
-  }
-  c.sync();
-  for (int i = c.rank; i < s.n; i += c.size) c.del[i] = (double)x[i];
-  c.sync();
-}
-
-/* ------------------------------------------------------------------ explicit inverse (mixed form) */
-
-/* In the mixed form the FP32 iteration matrix is inverted in place, every m block
-   at once across the team (Gauss-Jordan elimination with partial pivoting), so
-   that a Newton solve is one matrix-vector product instead of serial triangular
-   sweeps: FP32 arithmetic is cheap on this GPU, the sweeps' latency is not.  The
-   simplified Newton iteration corrects the FP32 rounding as it does for an FP32
-   LU solve. */
-
-/* Column kk of block b, by one group: pivot search, row interchange, scaling of
-   the pivot row (its diagonal becomes the reciprocal pivot) and a copy of column kk
-   for the elimination. */
-template <typename T, class C>
-__device__ void gj_pivot(const C &c, int b, int kk, int lane, int W, unsigned mask) {
-  const DevSpec &s = c.s;
-  int nb = s.blk_size[b];
-  if (kk >= nb) return;
-  auto A = c.template lu<T>() + s.lu_off[b];
-  auto col = c.template xsol<T>() + s.blk_start[b];
-  T best = T(-1);
-  int bi = kk;
-  for (int i = kk + lane; i < nb; i += W) {
-    T v = tabs(A[i * nb + kk]);
-    if (v > best) { best = v; bi = i; }
-  }
-  for (int off = W >> 1; off > 0; off >>= 1) {
-    T ob = __shfl_xor_sync(mask, best, off);
-    int oi = __shfl_xor_sync(mask, bi, off);
-    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-  }
-  if (bi != kk)
-    for (int j = lane; j < nb; j += W) {
-      T tmp = A[kk * nb + j];
-      A[kk * nb + j] = A[bi * nb + j];
-      A[bi * nb + j] = tmp;
-    }
-  __syncwarp(mask);
-  T inv = T(1);
-  if (best > T(0)) inv = T(1) / A[kk * nb + kk];
-  for (int i = lane; i < nb; i += W) col[i] = (i == kk) ? T(0) : A[i * nb + kk];
-  __syncwarp(mask);
-  for (int j = lane; j < nb; j += W) A[kk * nb + j] = (j == kk) ? inv : A[kk * nb + j] * inv;
-  if (lane == 0) {
-    c.piv[s.blk_start[b] + kk] = bi;
-    c.sh->gjp[b] = (float)inv;
-    if (!(best > T(0))) c.sh->lu_fail = 1;
-  }
-  __syncwarp(mask);
-}
-
-/* undo the row interchanges on the columns of the inverse of block b */
-template <typename T, class C> __device__ void gj_unpermute(const C &c, int b, int lane, int W, unsigned mask) {
-  const DevSpec &s = c.s;
-  int nb = s.blk_size[b];
-  auto A = c.template lu<T>() + s.lu_off[b];
-  for (int k = nb - 1; k >= 0; --k) {
-    int q = c.piv[s.blk_start[b] + k];
-    if (q != k)
-      for (int i = lane; i < nb; i += W) {
-        T tmp = A[i * nb + k];
-        A[i * nb + k] = A[i * nb + q];
-        A[i * nb + q] = tmp;
-      }
-    __syncwarp(mask);
-  }
-}
 
 /* run f(b, lane, W, mask) for every block: a warp per block (CTA teams), the team
    itself otherwise */
@@ -1406,91 +1246,115 @@ template <class C, class F> __device__ void per_block_group(const C &c, F f) {
   }
 }
 
-template <class C> __device__ inline int block_of(const C &c, int i) {
-  int b = 0;
-  while (b + 1 < c.s.nblk && i >= c.s.blk_start[b + 1]) ++b;
-  return b;
+/* One m block, factorised by a group of W lanes: partial pivoting within the band
+   with the row interchanges applied to the trailing columns only (the multipliers
+   stay where they were computed, as in LINPACK's banded factorisation), so U has
+   kl + ku superdiagonals.  The diagonal keeps the reciprocal pivot for the solves. */
+template <typename T, class C>
+__device__ void band_lu(const C &c, int b, int lane, int W, unsigned mask) {
+  const DevSpec &s = c.s;
+  auto A = c.template lu<T>() + s.lu_off[b];
+  int nb = s.blk_size[b], kl = c.sh->kl[b], kw = kl + c.sh->ku[b];
+  auto pv = c.piv + s.blk_start[b];
+  for (int k = 0; k < nb; ++k) {
+    int last = min(nb - 1, k + kl), cend = min(nb - 1, k + kw);
+    T best = T(-1);
+    int bi = k;
+    for (int i = k + lane; i <= last; i += W) {
+      T v = tabs(A[i * nb + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+    for (int off = W >> 1; off > 0; off >>= 1) {
+      T ob = __shfl_xor_sync(mask, best, off);
+      int oi = __shfl_xor_sync(mask, bi, off);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (bi != k)
+      for (int j = k + lane; j <= cend; j += W) {
+        T tmp = A[k * nb + j];
+        A[k * nb + j] = A[bi * nb + j];
+        A[bi * nb + j] = tmp;
+      }
+    __syncwarp(mask);
+    T inv = T(1);
+    if (best > T(0)) inv = T(1) / A[k * nb + k];
+    for (int i = k + 1 + lane; i <= last; i += W) A[i * nb + k] *= inv;
+    __syncwarp(mask);
+    /* rank-1 update of the band below and right of the pivot, a column per lane */
+    for (int j = k + 1 + lane; j <= cend; j += W) {
+      T akj = A[k * nb + j];
+      if (akj != T(0))
+        for (int i = k + 1; i <= last; ++i) A[i * nb + j] -= A[i * nb + k] * akj;
+    }
+    if (lane == 0) {
+      pv[k] = bi;
+      A[k * nb + k] = inv;
+      if (!(best > T(0))) c.sh->lu_fail = 1;
+    }
+    __syncwarp(mask);
+  }
 }
 
-template <typename T, class C> __device__ void form_and_invert(const C &c, double hinvGak) {
+template <typename T, class C> __device__ void form_and_factor(const C &c, double hinvGak) {
   const DevSpec &s = c.s;
-  auto A = c.template lu<T>();
+  auto LU = c.template lu<T>();
   auto J = c.template jacv<T>();
-  auto col = c.template xsol<T>();
-  T hg = (T)hinvGak;
   for (int e = c.rank; e < s.lu_elems; e += c.size) {
     int b = 0;
     while (b + 1 < s.nblk && e >= s.lu_off[b + 1]) ++b;
-    int nb = s.blk_size[b], r = (e - s.lu_off[b]) / nb, cc = (e - s.lu_off[b]) % nb;
-    A[e] = (r == cc ? T(1) : T(0)) - hg * J[e];
-  }
-  /* elimination work of this thread per block: columns cc (and row groups rg of
-     R rows each) in steps of the team size; the first item is precomputed */
-  int Rb[S2_MAXBLK], cb[S2_MAXBLK], rb[S2_MAXBLK];
-  int maxnb = 0;
-#pragma unroll
-  for (int b = 0; b < S2_MAXBLK; ++b) {
-    int nb = b < s.nblk ? s.blk_size[b] : 1;
-    Rb[b] = max(1, c.size / nb);
-    cb[b] = c.rank % nb;
-    rb[b] = c.rank / nb;
-    if (b < s.nblk) maxnb = max(maxnb, nb);
+    int nb = s.blk_size[b], r = (e - s.lu_off[b]) / nb, col = (e - s.lu_off[b]) % nb;
+    if constexpr (sizeof(T) == sizeof(float)) {
+      LU[e] = (r == col ? 1.0f : 0.0f) - (float)hinvGak * J[e];
+    } else {
+      double v = -hinvGak * J[e];
+      if (r == col) v += 1.0;
+      LU[e] = v;
+    }
   }
   c.sync();
-  for (int kk = 0; kk < maxnb; ++kk) {
-    per_block_group(c, [&](int b, int lane, int W, unsigned mask) { gj_pivot<T>(c, b, kk, lane, W, mask); });
-    c.sync();
-#pragma unroll
-    for (int b = 0; b < S2_MAXBLK; ++b) {
-      if (b >= s.nblk) break;
-      int nb = s.blk_size[b];
-      if (kk >= nb) continue;
-      int R = Rb[b];
-      auto Ab = A + s.lu_off[b];
-      auto colb = col + s.blk_start[b];
-      T inv = (T)c.sh->gjp[b];
-      for (int item = c.rank; item < nb * R; item += c.size) {
-        int cc = item == c.rank ? cb[b] : item % nb, rg = item == c.rank ? rb[b] : item / nb;
-        /* column kk becomes -col * inv; the others lose col * (scaled pivot row) */
-        T pr = cc == kk ? T(0) : Ab[kk * nb + cc];
-        T sa = cc == kk ? T(0) : T(1), sb = cc == kk ? -inv : -pr;
-        /* eight rows at a time: all loads issued before the stores */
-        for (int r0 = rg; r0 < nb; r0 += 8 * R) {
-          T cv[8], av[8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            int r = r0 + u * R;
-            cv[u] = r < nb ? colb[r] : T(0);
-            av[u] = r < nb ? Ab[r * nb + cc] : T(0);
-          }
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            int r = r0 + u * R;
-            if (r < nb && r != kk) Ab[r * nb + cc] = sa * av[u] + sb * cv[u];
-          }
-        }
-      }
-    }
-    c.sync();
-  }
-  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { gj_unpermute<T>(c, b, lane, W, mask); });
+  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { band_lu<T>(c, b, lane, W, mask); });
   c.sync();
 }
 
-/* del <- M^{-1} del with the explicit inverse: one row per thread */
-template <typename T, class C> __device__ void inv_solve(const C &c) {
+/* one m block, solved by a group of W lanes: interchange and eliminate column by
+   column, then back substitution with the reciprocal pivots */
+template <typename T, class C>
+__device__ void band_solve(const C &c, int b, int lane, int W, unsigned mask) {
+  const DevSpec &s = c.s;
+  int nb = s.blk_size[b], kl = c.sh->kl[b], kw = kl + c.sh->ku[b];
+  auto A = c.template lu<T>() + s.lu_off[b];
+  auto pv = c.piv + s.blk_start[b];
+  auto x = c.template xsol<T>() + s.blk_start[b];
+  for (int k = 0; k < nb; ++k) {
+    int q = pv[k];
+    T xk = x[q];
+    if (q != k) {
+      __syncwarp(mask);
+      if (lane == 0) { x[q] = x[k]; x[k] = xk; }
+    }
+    __syncwarp(mask);
+    int last = min(nb - 1, k + kl);
+    for (int i = k + 1 + lane; i <= last; i += W) x[i] -= A[i * nb + k] * xk;
+    __syncwarp(mask);
+  }
+  for (int j = nb - 1; j >= 0; --j) {
+    T xj = x[j] * A[j * nb + j];
+    __syncwarp(mask);
+    if (lane == 0) x[j] = xj;
+    for (int i = max(0, j - kw) + lane; i < j; i += W) x[i] -= A[i * nb + j] * xj;
+    __syncwarp(mask);
+  }
+}
+
+/* del <- M^{-1} del (the right-hand side in c.del, the result written back) */
+template <typename T, class C> __device__ void lu_solve(const C &c) {
   const DevSpec &s = c.s;
   auto x = c.template xsol<T>();
   for (int i = c.rank; i < s.n; i += c.size) x[i] = (T)c.del[i];
   c.sync();
-  auto A = c.template lu<T>();
-  for (int i = c.rank; i < s.n; i += c.size) {
-    int b = block_of(c, i), nb = s.blk_size[b], b0 = s.blk_start[b];
-    auto row = A + s.lu_off[b] + (i - b0) * nb;
-    T acc = T(0);
-    for (int j = 0; j < nb; ++j) acc += row[j] * x[b0 + j];
-    c.del[i] = (double)acc;
-  }
+  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { band_solve<T>(c, b, lane, W, mask); });
+  c.sync();
+  for (int i = c.rank; i < s.n; i += c.size) c.del[i] = (double)x[i];
   c.sync();
 }
 
@@ -1955,8 +1819,7 @@ template <typename T, class C>
 __device__ int refactor(const C &c, double hinvGak, song2_triplet_stats &st) {
   if (c.rank == 0) c.sh->lu_fail = 0;
   c.sync();
-  if constexpr (sizeof(T) == sizeof(float)) form_and_invert<T>(c, hinvGak);
-  else form_and_factor<T>(c, hinvGak);
+  form_and_factor<T>(c, hinvGak);
   st.n_lu++;
   return c.sh->lu_fail ? SONG2_E_SINGULAR : SONG2_OK;
 }
@@ -2080,8 +1943,7 @@ __device__ int ndf15(const C &c, double t0, double t1, int &jout, int include_t0
           st.n_rhs++;
           for (int i = tid; i < n; i += nt) del[i] = hinvGak * f[i] - (psiv[i] + difkp1[i]);
           c.sync();
-          if constexpr (sizeof(T) == sizeof(float)) inv_solve<T>(c);
-          else lu_solve<T>(c);
+          lu_solve<T>(c);
           unsigned long long vn = 0;
           for (int i = tid; i < n; i += nt) {
             bmax(vn, del[i] * invwt[i]);
