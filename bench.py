@@ -10,9 +10,10 @@ project's own provider (the CLASS tables the reference would use are not
 available).
 
   value        triplets/s of the mixed form (FP64 RHS/residual/error control,
-               FP32 block LU), tables resident in HBM, CUDA events around each
-               persistent-kernel launch; L2 is flushed between steps.
-  plain_fp64   the same for the plain FP64 form (FP64 LU), for the
+               FP32 banded LU of the per-m iteration-matrix blocks), tables
+               resident in HBM, CUDA events around each persistent-kernel
+               launch; L2 is flushed between steps.
+  plain_fp64   the same for the plain FP64 form (FP64 banded LU), for the
                mixed-vs-plain ratio the metric asks for.
   e2e          triplets/s through song2_gpu_evolve (the drop-in C ABI): host
                tables uploaded and the host ppt2->sources slabs filled inside
@@ -40,6 +41,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "2nd-order k-triplets/s at rtol 1e-4: mixed+batched vs plain FP64 GPU; err vs FP64"
 WORKLOAD = 2
+# FP64 work of the mixed-form evolver per NDF step (ncu, reduced config 2) and the
+# FP64 issue rate of a GB300 SM (DFMA probe); see profiles/
+FP64_FLOPS_PER_STEP = 47.1e3
+FP64_WARP_INSTR_PER_STEP = 2.68e3
+FP64_WARP_INSTR_PER_SM_CYCLE = 0.0526
 
 
 def parse():
@@ -347,11 +353,26 @@ def main():
                 "note": "the evolver is bound by the FP64 pipe (RHS, residual, error control), not by HBM; "
                         "bytes = first-order rows of every (k1,k2) pair + background + source writes"}
     steps_tot = st_mixed["n_steps"].sum()
+    # FP64 pipe: algorithmic FP64 work per NDF step and the SM's FP64 issue rate,
+    # both measured on this kernel/GPU (profiles/evolver_fp64_counters.md,
+    # profiles/fp64_pipe_probe.md); the run supplies the step count and the time
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    fp64_flops = steps_tot * FP64_FLOPS_PER_STEP / (ms_step / 1e3)
+    fp64_peak = FP64_WARP_INSTR_PER_SM_CYCLE * 32 * 2 * sm_mhz * 1e6 * nsm
+    fp64_slots = steps_tot * FP64_WARP_INSTR_PER_STEP / (ms_step / 1e3)
+    slot_peak = FP64_WARP_INSTR_PER_SM_CYCLE * sm_mhz * 1e6 * nsm
+    roofline_fp64 = {"bound": "fp64", "achieved": fp64_flops / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": fp64_flops / fp64_peak, "issue_slots_frac": fp64_slots / slot_peak,
+                     "note": "FP64 flops (FMA = 2) per NDF step from the ncu counters of this kernel; peak from "
+                             "the DFMA probe (one FP64 warp instruction per ~19 SM cycles, any lane count); "
+                             "issue_slots_frac counts FP64 warp instructions against that rate"}
     line = {"metric": METRIC, "value": value, "unit": "triplets/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 (FP32 block LU)",
+            "vs_baseline": None, "dtype": "f64 (FP32 banded LU)",
             "data": "synthetic (own background/recombination and first-order provider)", "config": config,
-            "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "roofline_fp64": roofline_fp64,
+            "e2e": e2e,
             "status_ok": bool(np.all(st_mixed["status"] == 0)),
             "counters": {"ndf_steps": int(steps_tot), "rhs": int(st_mixed["n_rhs"].sum()),
                          "jacobians": int(st_mixed["n_jac"].sum()), "lu": int(st_mixed["n_lu"].sum())}}
