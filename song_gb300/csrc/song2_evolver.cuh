@@ -1,20 +1,26 @@
 /*
- * song2_kernels.cu - the GB300 evolver of SONG's second-order system.
+ * song2_evolver.cuh - the GB300 evolver of SONG's second-order system: device
+ * code of the persistent kernels for every team layout.  Each song2_k_*.cu
+ * translation unit instantiates one kernel from it, so the kernels compile in
+ * parallel; song2_launch.cu holds the host-side launcher.
  *
- * One CTA evolves one (k1,k2,k3) triplet at a time and pulls the next one from
- * a device work queue (persistent kernel).  Inside a CTA:
+ * A team (a CTA by default) evolves one (k1,k2,k3) triplet at a time and pulls
+ * the next one from a device work queue (persistent kernel).  Inside a team:
  *   - background/thermo and first-order interpolation (cubic splines in ln tau)
- *     and the quadratic sources (perturbations2.c:10643-11813) are computed
- *     thread-parallel into shared memory;
+ *     and the quadratic sources (perturbations2.c:10643-11813), tabulated per
+ *     triplet on the first-order nodes and splined (perturbations2.c:10407-10606),
+ *     are held in shared memory;
  *   - the right-hand side of perturb2_derivs (perturbations2.c:7636-8451) is
- *     evaluated by a per-equation row function, one thread per equation, after
- *     thread 0 has formed the shared "workspace" scalars (workspace_at_tau,
- *     tca_variables, einstein: perturbations2.c:8484-9738);
+ *     evaluated by a per-equation row function, one thread per equation, in a
+ *     species-grouped order, after three warps have formed the workspace scalars
+ *     of the three azimuthal numbers (workspace_at_tau, tca_variables, einstein:
+ *     perturbations2.c:8484-9738);
  *   - the system is affine, dy = A(tau) y + s(tau), so the Jacobian is exact:
  *     column j is the row function applied to the unit vector e_j, one thread
  *     per column, with the sources switched off;
- *   - azimuthal modes never couple, so the NDF iteration matrix I - h*gamma*J is
- *     block diagonal in m; every m block is LU-factorised (partial pivoting) and
+ *   - azimuthal modes never couple and the state is l-major within a mode, so the
+ *     NDF iteration matrix I - h*gamma*J is block diagonal in m with banded
+ *     blocks; every block is factorised (partial pivoting within the band) and
  *     solved by one warp, in FP64 (plain form) or FP32 (mixed form: the Newton
  *     residual, error estimate and step control stay FP64, the simplified Newton
  *     iteration doubles as iterative refinement);
@@ -23,6 +29,9 @@
  * Every loop is bounded (max_steps, 4 Newton iterations, 200 bisection steps);
  * a triplet that breaches a bound retires with a status code.  No kernel spins.
  */
+#ifndef SONG2_EVOLVER_CUH
+#define SONG2_EVOLVER_CUH
+
 #include <math.h>
 #include <stdio.h>
 
@@ -1757,8 +1766,8 @@ template <class C> __device__ void initial_conditions(const C &c, double tau) {
     double rho_monopole = bg.rho_g * I_0_0 + bg.rho_b * b_0_0_0 + bg.rho_cdm * b_0_0_0 + bg.rho_ur * I_0_0;
     y[s.idx_phip] = -Hc * psi - k_sq / (3 * Hc) * phi - a_sq * rho_monopole / (2 * Hc) + qs[s.iq_phi_prime_poisson];
   } else if (s.ic == SONG2_IC_AD_FIRST_ORDER) {
-    double C = 0.5 * (2 * (-(3 / 5. * s.fnl)));
-    double psi = 20 * C / (15 + 4 * frac_ur);
+    double c_zeta = 0.5 * (2 * (-(3 / 5. * s.fnl)));
+    double psi = 20 * c_zeta / (15 + 4 * frac_ur);
     y[s.idx_phi] = (1 + 2 / 5. * frac_ur) * psi;
     double u0 = 0.5 * k * tau * psi;
     double I_0_0 = -2 * psi;
@@ -2262,47 +2271,4 @@ __global__ void __launch_bounds__(128) team_kernel(const __grid_constant__ DevSp
 
 } // namespace
 
-size_t song2_smem_bytes(const DevSpec &spec, int precision, int block, int lu_in_smem) {
-  (void)block;
-  return make_plan(spec, precision, lu_in_smem).total;
-}
-
-size_t song2_class_spec_bytes() { return al(sizeof(DevSpec)); }
-
-size_t song2_team_smem_bytes(const DevSpec &spec, int teams_per_cta) {
-  return team_tables_bytes(spec) + sizeof(Shared) * (size_t)teams_per_cta;
-}
-
-int song2_team_slab_doubles(const DevSpec &spec) { return make_team_plan(spec).total; }
-
-namespace {
-template <typename T, int W, int CL> void *kernel_ptr() { return (void *)evolver_kernel<T, W, CL>; }
-/* mode 3: CTA per triplet with hierarchy classes */
-void *pick_kernel(int precision, int mode) {
-  if (mode == 2) return precision == SONG2_PREC_MIXED ? (void *)team_kernel<float> : (void *)team_kernel<double>;
-  if (mode == 3)
-    return precision == SONG2_PREC_MIXED ? kernel_ptr<float, MODE_BLOCK, 1>() : kernel_ptr<double, MODE_BLOCK, 1>();
-  if (precision == SONG2_PREC_MIXED) return mode ? kernel_ptr<float, MODE_WARP, 0>() : kernel_ptr<float, MODE_BLOCK, 0>();
-  return mode ? kernel_ptr<double, MODE_WARP, 0>() : kernel_ptr<double, MODE_BLOCK, 0>();
-}
-} // namespace
-
-int song2_max_ctas_per_sm(int precision, int mode, int block, size_t smem) {
-  int nb = 0;
-  const void *f = pick_kernel(precision, mode);
-  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, block, smem);
-  return e == cudaSuccess ? nb : 0;
-}
-
-int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int mode, int grid, int block,
-                         size_t smem, cudaStream_t stream) {
-  if (ptrs.class_spec && mode == 0) mode = 3;
-  const void *f = pick_kernel(precision, mode);
-  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  DevSpec sp = spec;
-  DevPtrs pp = ptrs;
-  void *args[] = {(void *)&sp, (void *)&pp};
-  cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, stream);
-  return e == cudaSuccess ? 0 : 1;
-}
+#endif

@@ -1,6 +1,6 @@
 /*
  * song2_internal.h - device-side data layout shared by the evolver kernel
- * (song2_kernels.cu) and the C ABI host code (song2_capi.cu).
+ * (song2_evolver.cuh, song2_launch.cu) and the C ABI host code (song2_capi.cu).
  */
 #ifndef SONG2_INTERNAL_H
 #define SONG2_INTERNAL_H
@@ -113,7 +113,7 @@ struct DevPtrs {
   int *queue;                      /* work-queue counter */
 };
 
-/* host-side launcher implemented in song2_kernels.cu.  mode 0: one CTA per
+/* host-side launcher implemented in song2_launch.cu.  mode 0: one CTA per
    triplet; 1: one warp per triplet (several per CTA); 2: spec.team_lanes lanes per
    triplet, arrays in global slabs (tslab, txsol, tpiv, jac, lu_global, qtab);
    3: one CTA per triplet with hierarchy classes (ptrs.class_spec set; the dynamic
