@@ -233,26 +233,55 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   }
   s.lu_elems = off;
 
-  /* evaluation order of the rows and of the quadratic-source entries: grouped by
-     species (I, E, B, N, the rest), each group padded to whole warps, so that the
-     threads of a warp run one code path */
-  auto slots = [](const std::vector<short> &sp_of, std::vector<short> &out) {
+  /* evaluation order of the rows and of the quadratic-source entries: the
+     hierarchy entries grouped by species (I, E, B, N), each group padded to whole
+     warps, so that the threads of a warp run one code path; the few other entries
+     (metric, matter, and the seven entries that carry the metric parts of the
+     quadratic sources, heaviest first) go one per warp into free slots, so that
+     their different code paths run side by side on different warps */
+  auto slots = [](const std::vector<short> &sp_of, const std::vector<int> &first, std::vector<short> &out) {
     const int cls_sp[4] = {SP_I, SP_E, SP_B, SP_N};
     out.clear();
-    for (int g = 0; g < 5; ++g) {
+    std::vector<int> rest;
+    for (int f : first)
+      if (f >= 0) rest.push_back(f);
+    for (size_t i = 0; i < sp_of.size(); ++i) {
+      int sp_ = sp_of[i];
+      bool hier = false;
+      for (int u = 0; u < 4; ++u) hier |= sp_ == cls_sp[u];
+      bool listed = false;
+      for (int f : first) listed |= f == (int)i;
+      if (!hier && !listed) rest.push_back((int)i);
+    }
+    for (int g = 0; g < 4; ++g) {
       size_t start = out.size();
-      for (size_t i = 0; i < sp_of.size(); ++i) {
-        int sp_ = sp_of[i];
-        int cls = 4;
-        for (int u = 0; u < 4; ++u)
-          if (sp_ == cls_sp[u]) cls = u;
-        if (cls == g) out.push_back((short)i);
-      }
+      for (size_t i = 0; i < sp_of.size(); ++i)
+        if (sp_of[i] == cls_sp[g]) out.push_back((short)i);
       while ((out.size() - start) % 32) out.push_back(-1);
     }
+    int nw = (int)out.size() / 32;
+    std::vector<int> used(nw, 0);
+    for (int e : rest) {
+      int best = -1, bestscore = 0;
+      for (int w = 0; w < nw; ++w) {
+        int fr = 0;
+        for (int u = 0; u < 32; ++u) fr += out[w * 32 + u] < 0;
+        int score = fr - 64 * used[w];
+        if (fr > 0 && (best < 0 || score > bestscore)) { best = w; bestscore = score; }
+      }
+      if (best < 0) {
+        out.resize(out.size() + 32, -1);
+        used.push_back(0);
+        best = nw++;
+      }
+      for (int u = 31; u >= 0; --u)
+        if (out[best * 32 + u] < 0) { out[best * 32 + u] = (short)e; break; }
+      used[best]++;
+    }
   };
-  slots(H.eq_sp, H.row_slot);
-  slots(H.qs_sp, H.qs_slot);
+  slots(H.eq_sp, {s.idx_phip}, H.row_slot);
+  slots(H.qs_sp, {s.iq_psi, s.iq_phi_prime_prime, s.iq_phi_prime_longitudinal, s.iq_phi_prime_poisson,
+                  s.iq_omega_m1_prime, s.iq_gamma_m2_prime_prime, s.iq_vv_g}, H.qs_slot);
   s.n_row_slots = (int)H.row_slot.size();
   s.n_qs_slots = (int)H.qs_slot.size();
 

@@ -582,7 +582,11 @@ template <class C> __device__ double liou_matter(const C &c, int cdm, int n, int
 }
 
 /* Einstein-tensor quadratic terms (perturbations2.c:10905-11060) into qs */
-template <class C> __device__ void qs_metric(const C &c, const BgV &bg) {
+/* Quadratic metric sources (perturbations2.c:10937-11029) and the first-order
+   products kept for later (:11795-11809), in seven independent parts so that
+   they can run on different warps: 0 phi' (Poisson), 1 phi' (longitudinal),
+   2 psi and psi', 3 phi'', 4 omega' (m = 1), 5 gamma'' (m = 2), 6 products. */
+template <class C> __device__ void qs_metric_part(const C &c, const BgV &bg, int part) {
   const Tri &t = c.sh->tri;
   const DevSpec &s = c.s;
   auto fo1 = c.fo1, fo2 = c.fo2;
@@ -590,64 +594,85 @@ template <class C> __device__ void qs_metric(const C &c, const BgV &bg) {
   double phi_1 = fo1[SONG2_FO_PHI], phi_2 = fo2[SONG2_FO_PHI], psi_1 = fo1[SONG2_FO_PSI], psi_2 = fo2[SONG2_FO_PSI];
   double psi_prime_1 = fo1[SONG2_FO_PSI_P], psi_prime_2 = fo2[SONG2_FO_PSI_P];
   double phi_prime_1 = fo1[SONG2_FO_PHI_P], phi_prime_2 = fo2[SONG2_FO_PHI_P];
-  double phi_prime_prime_1 = fo1[SONG2_FO_PHI_PP], phi_prime_prime_2 = fo2[SONG2_FO_PHI_PP];
   double k1 = t.k1, k2 = t.k2, k = t.k, k_sq = t.k_sq, k1_sq = k1 * k1, k2_sq = k2 * k2, k1_dot_k2 = t.k1_dot_k2;
   const double *k1_m = t.k1_m, *k2_m = t.k2_m, *k1_ten_k2 = t.k1_ten_k2, *k1_ten_k1 = t.k1_ten_k1,
                *k2_ten_k2 = t.k2_ten_k2;
   double Hc = bg.Hc, Hc_sq = Hc * Hc, Hc_prime = bg.Hc_prime, a_sq = bg.a_sq;
-  if (s.compute_m[0]) {
-    double rho_dipole_1 = bg.rho_g * c.I1r(1) + bg.rho_b * fo1[SONG2_FO_DIPOLE_B] + bg.rho_cdm * fo1[SONG2_FO_DIPOLE_CDM] +
-                          bg.rho_ur * c.N1r(1);
-    double rho_dipole_2 = bg.rho_g * c.I2r(1) + bg.rho_b * fo2[SONG2_FO_DIPOLE_B] + bg.rho_cdm * fo2[SONG2_FO_DIPOLE_CDM] +
-                          bg.rho_ur * c.N2r(1);
-    double Q_TT = -12 * psi_1 * psi_2 * Hc_sq + phi_1 * phi_2 * (3 * k1_dot_k2 + 4 * k1_sq + 4 * k2_sq) +
-                  6 * phi_prime_2 * (phi_1 - psi_1) * Hc + 6 * phi_prime_1 * (phi_2 - psi_2) * Hc -
-                  3 * phi_prime_1 * phi_prime_2;
-    double Q_ST = +2 * psi_1 * psi_2 * Hc * (k1_m[1] + k2_m[1]) - 2 * psi_1 * phi_2 * Hc * (k1_m[1]) -
-                  2 * psi_2 * phi_1 * Hc * (+k2_m[1]) - 2 * phi_1 * phi_prime_2 * (k1_m[1] + 2 * k2_m[1]) -
-                  2 * phi_2 * phi_prime_1 * (2 * k1_m[1] + k2_m[1]) + psi_1 * phi_prime_2 * (k1_m[1]) +
-                  psi_2 * phi_prime_1 * (k2_m[1]) +
-                  0.5 * a_sq * (k1_m[1] / k1 * rho_dipole_1 * (psi_2 + phi_2) + k2_m[1] / k2 * rho_dipole_2 * (psi_1 + phi_1));
-    double Q_TR = -12 * psi_1 * psi_2 * (Hc * Hc + 2 * Hc_prime) + psi_1 * psi_2 * (k_sq + k1_sq + k2_sq) +
-                  phi_1 * phi_2 * (3 * k1_dot_k2 + 4 * k1_sq + 4 * k2_sq) + phi_1 * psi_2 * (k1_dot_k2 - 2 * k2_sq) +
-                  phi_2 * psi_1 * (k1_dot_k2 - 2 * k1_sq) + 6 * (phi_prime_prime_2 + 2 * Hc * phi_prime_2) * (phi_1 - psi_1) +
-                  6 * (phi_prime_prime_1 + 2 * Hc * phi_prime_1) * (phi_2 - psi_2) -
-                  3 * psi_prime_2 * (4 * Hc * psi_1 + phi_prime_1) - 3 * psi_prime_1 * (4 * Hc * psi_2 + phi_prime_2) +
-                  3 * phi_prime_1 * phi_prime_2;
-    double Q_SS = phi_1 * phi_2 * (-3 * k1_ten_k2[2] - 2 * k1_ten_k1[2] - 2 * k2_ten_k2[2]) +
-                  psi_1 * psi_2 * (-k1_ten_k2[2] - k1_ten_k1[2] - k2_ten_k2[2]) +
-                  psi_1 * phi_2 * (k1_ten_k2[2] + k1_ten_k1[2]) + psi_2 * phi_1 * (k1_ten_k2[2] + k2_ten_k2[2]);
-    double Q_SS_prime =
-        (phi_prime_1 * phi_2 + phi_1 * phi_prime_2) * (-3 * k1_ten_k2[2] - 2 * k1_ten_k1[2] - 2 * k2_ten_k2[2]) +
-        (psi_prime_1 * psi_2 + psi_1 * psi_prime_2) * (-k1_ten_k2[2] - k1_ten_k1[2] - k2_ten_k2[2]) +
-        (psi_prime_1 * phi_2 + psi_1 * phi_prime_2) * (k1_ten_k2[2] + k1_ten_k1[2]) +
-        (psi_prime_2 * phi_1 + psi_2 * phi_prime_1) * (k1_ten_k2[2] + k2_ten_k2[2]);
-    Q_TT *= 2; Q_ST *= 2; Q_TR *= 2; Q_SS *= 2; Q_SS_prime *= 2;
-    qs[s.iq_phi_prime_poisson] = -Q_TT / (6 * Hc);
-    qs[s.iq_phi_prime_longitudinal] = Q_ST / (2 * k);
-    qs[s.iq_psi] = -Q_SS * 3 / (2 * k_sq);
-    qs[s.iq_psi_prime] = -Q_SS_prime * 3 / (2 * k_sq) - Q_SS * 3 * Hc / k_sq;
-    qs[s.iq_phi_prime_prime] = -(Q_TR + Q_TT) / 6;
+  auto q_tt = [&]() {
+    return -12 * psi_1 * psi_2 * Hc_sq + phi_1 * phi_2 * (3 * k1_dot_k2 + 4 * k1_sq + 4 * k2_sq) +
+           6 * phi_prime_2 * (phi_1 - psi_1) * Hc + 6 * phi_prime_1 * (phi_2 - psi_2) * Hc - 3 * phi_prime_1 * phi_prime_2;
+  };
+  auto q_ss = [&](int i) {
+    return phi_1 * phi_2 * (-3 * k1_ten_k2[i] - 2 * k1_ten_k1[i] - 2 * k2_ten_k2[i]) +
+           psi_1 * psi_2 * (-k1_ten_k2[i] - k1_ten_k1[i] - k2_ten_k2[i]) + psi_1 * phi_2 * (k1_ten_k2[i] + k1_ten_k1[i]) +
+           psi_2 * phi_1 * (k1_ten_k2[i] + k2_ten_k2[i]);
+  };
+  switch (part) {
+  case 0:
+    if (s.compute_m[0]) {
+      double Q_TT = 2 * q_tt();
+      qs[s.iq_phi_prime_poisson] = -Q_TT / (6 * Hc);
+    }
+    break;
+  case 1:
+    if (s.compute_m[0]) {
+      double rho_dipole_1 = bg.rho_g * c.I1r(1) + bg.rho_b * fo1[SONG2_FO_DIPOLE_B] + bg.rho_cdm * fo1[SONG2_FO_DIPOLE_CDM] +
+                            bg.rho_ur * c.N1r(1);
+      double rho_dipole_2 = bg.rho_g * c.I2r(1) + bg.rho_b * fo2[SONG2_FO_DIPOLE_B] + bg.rho_cdm * fo2[SONG2_FO_DIPOLE_CDM] +
+                            bg.rho_ur * c.N2r(1);
+      double Q_ST = +2 * psi_1 * psi_2 * Hc * (k1_m[1] + k2_m[1]) - 2 * psi_1 * phi_2 * Hc * (k1_m[1]) -
+                    2 * psi_2 * phi_1 * Hc * (+k2_m[1]) - 2 * phi_1 * phi_prime_2 * (k1_m[1] + 2 * k2_m[1]) -
+                    2 * phi_2 * phi_prime_1 * (2 * k1_m[1] + k2_m[1]) + psi_1 * phi_prime_2 * (k1_m[1]) +
+                    psi_2 * phi_prime_1 * (k2_m[1]) +
+                    0.5 * a_sq * (k1_m[1] / k1 * rho_dipole_1 * (psi_2 + phi_2) + k2_m[1] / k2 * rho_dipole_2 * (psi_1 + phi_1));
+      Q_ST *= 2;
+      qs[s.iq_phi_prime_longitudinal] = Q_ST / (2 * k);
+    }
+    break;
+  case 2:
+    if (s.compute_m[0]) {
+      double Q_SS = q_ss(2);
+      double Q_SS_prime =
+          (phi_prime_1 * phi_2 + phi_1 * phi_prime_2) * (-3 * k1_ten_k2[2] - 2 * k1_ten_k1[2] - 2 * k2_ten_k2[2]) +
+          (psi_prime_1 * psi_2 + psi_1 * psi_prime_2) * (-k1_ten_k2[2] - k1_ten_k1[2] - k2_ten_k2[2]) +
+          (psi_prime_1 * phi_2 + psi_1 * phi_prime_2) * (k1_ten_k2[2] + k1_ten_k1[2]) +
+          (psi_prime_2 * phi_1 + psi_2 * phi_prime_1) * (k1_ten_k2[2] + k2_ten_k2[2]);
+      Q_SS *= 2;
+      Q_SS_prime *= 2;
+      qs[s.iq_psi] = -Q_SS * 3 / (2 * k_sq);
+      qs[s.iq_psi_prime] = -Q_SS_prime * 3 / (2 * k_sq) - Q_SS * 3 * Hc / k_sq;
+    }
+    break;
+  case 3:
+    if (s.compute_m[0]) {
+      double phi_prime_prime_1 = fo1[SONG2_FO_PHI_PP], phi_prime_prime_2 = fo2[SONG2_FO_PHI_PP];
+      double Q_TT = q_tt();
+      double Q_TR = -12 * psi_1 * psi_2 * (Hc * Hc + 2 * Hc_prime) + psi_1 * psi_2 * (k_sq + k1_sq + k2_sq) +
+                    phi_1 * phi_2 * (3 * k1_dot_k2 + 4 * k1_sq + 4 * k2_sq) + phi_1 * psi_2 * (k1_dot_k2 - 2 * k2_sq) +
+                    phi_2 * psi_1 * (k1_dot_k2 - 2 * k1_sq) + 6 * (phi_prime_prime_2 + 2 * Hc * phi_prime_2) * (phi_1 - psi_1) +
+                    6 * (phi_prime_prime_1 + 2 * Hc * phi_prime_1) * (phi_2 - psi_2) -
+                    3 * psi_prime_2 * (4 * Hc * psi_1 + phi_prime_1) - 3 * psi_prime_1 * (4 * Hc * psi_2 + phi_prime_2) +
+                    3 * phi_prime_1 * phi_prime_2;
+      Q_TT *= 2;
+      Q_TR *= 2;
+      qs[s.iq_phi_prime_prime] = -(Q_TR + Q_TT) / 6;
+    }
+    break;
+  case 4:
+    if (s.compute_m[1]) qs[s.iq_omega_m1_prime] = SQRT_3 / k * 2 * q_ss(3);
+    break;
+  case 5:
+    if (s.compute_m[2]) qs[s.iq_gamma_m2_prime_prime] = -2 * q_ss(4);
+    break;
+  default:
+    qs[s.iq_vv_g] = fo1[SONG2_FO_V_G] * fo2[SONG2_FO_V_G];
+    qs[s.iq_vv_ur] = fo1[SONG2_FO_V_UR] * fo2[SONG2_FO_V_UR];
+    qs[s.iq_dd_b] = fo1[SONG2_FO_DELTA_B] * fo2[SONG2_FO_DELTA_B];
+    qs[s.iq_vv_b] = fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B];
+    qs[s.iq_vv_cdm] = fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM];
+    qs[s.iq_vvp_b] = fo1[SONG2_FO_V_B_P] * fo2[SONG2_FO_V_B] + fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B_P];
+    qs[s.iq_vvp_cdm] = fo1[SONG2_FO_V_CDM_P] * fo2[SONG2_FO_V_CDM] + fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM_P];
   }
-  if (s.compute_m[1]) {
-    double Q_SS = phi_1 * phi_2 * (-3 * k1_ten_k2[3] - 2 * k1_ten_k1[3] - 2 * k2_ten_k2[3]) +
-                  psi_1 * psi_2 * (-k1_ten_k2[3] - k1_ten_k1[3] - k2_ten_k2[3]) +
-                  psi_1 * phi_2 * (k1_ten_k2[3] + k1_ten_k1[3]) + psi_2 * phi_1 * (k1_ten_k2[3] + k2_ten_k2[3]);
-    qs[s.iq_omega_m1_prime] = SQRT_3 / k * 2 * Q_SS;
-  }
-  if (s.compute_m[2]) {
-    double Q_SS = phi_1 * phi_2 * (-3 * k1_ten_k2[4] - 2 * k1_ten_k1[4] - 2 * k2_ten_k2[4]) +
-                  psi_1 * psi_2 * (-k1_ten_k2[4] - k1_ten_k1[4] - k2_ten_k2[4]) +
-                  psi_1 * phi_2 * (k1_ten_k2[4] + k1_ten_k1[4]) + psi_2 * phi_1 * (k1_ten_k2[4] + k2_ten_k2[4]);
-    qs[s.iq_gamma_m2_prime_prime] = -2 * Q_SS;
-  }
-  qs[s.iq_vv_g] = fo1[SONG2_FO_V_G] * fo2[SONG2_FO_V_G];
-  qs[s.iq_vv_ur] = fo1[SONG2_FO_V_UR] * fo2[SONG2_FO_V_UR];
-  qs[s.iq_dd_b] = fo1[SONG2_FO_DELTA_B] * fo2[SONG2_FO_DELTA_B];
-  qs[s.iq_vv_b] = fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B];
-  qs[s.iq_vv_cdm] = fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM];
-  qs[s.iq_vvp_b] = fo1[SONG2_FO_V_B_P] * fo2[SONG2_FO_V_B] + fo1[SONG2_FO_V_B] * fo2[SONG2_FO_V_B_P];
-  qs[s.iq_vvp_cdm] = fo1[SONG2_FO_V_CDM_P] * fo2[SONG2_FO_V_CDM] + fo1[SONG2_FO_V_CDM] * fo2[SONG2_FO_V_CDM_P];
 }
 
 /* One entry of the quadratic-source vector: total (qs) and collisional (qc) part. */
@@ -689,9 +714,14 @@ template <class C> __device__ void qs_entry(const C &c, const BgV &bg, int q) {
   case SP_C11:
     if (s.has_liou) lv = liou_matter(c, 1, 1, m);
     break;
-  case SP_METRIC:
-    if (q == s.iq_psi) qs_metric(c, bg);
+  case SP_METRIC: {
+    /* the metric part carried by this entry (none for the entries it fills) */
+    int part = q == s.iq_phi_prime_poisson ? 0 : q == s.iq_phi_prime_longitudinal ? 1 : q == s.iq_psi ? 2
+             : q == s.iq_phi_prime_prime ? 3 : q == s.iq_omega_m1_prime ? 4 : q == s.iq_gamma_m2_prime_prime ? 5
+             : q == s.iq_vv_g ? 6 : -1;
+    if (part >= 0) qs_metric_part(c, bg, part);
     return;
+  }
   default:
     return;
   }
