@@ -36,6 +36,14 @@ struct song2_ctx {
   int last_launches;
   song2_launch launch;
   int n_teams;
+  /* uneven batches: consecutive item ranges launched one after the other, the
+     classes with large shared-memory plans first, so that the small ones run
+     several CTAs per SM */
+  struct Group {
+    int first, count, grid;
+    size_t smem;
+  };
+  std::vector<Group> groups;
 };
 
 namespace {
@@ -551,6 +559,45 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   int ctas_needed = (s.n_items + L.teams_per_cta - 1) / L.teams_per_cta;
   c->grid = std::max(1, std::min(ctas_needed, nsm * per_sm));
   c->n_teams = c->grid * L.teams_per_cta;
+  std::vector<WorkItem> gitems(items.begin(), items.end());
+  c->groups.clear();
+  if (classes) {
+    int smem_sm = 0;
+    CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    size_t half = (size_t)smem_sm / 2 > 1024 ? (size_t)smem_sm / 2 - 1024 : 0;
+    /* SONG2_CLASS_SPLIT_BYTES overrides the plan size that separates the groups */
+    const char *split = getenv("SONG2_CLASS_SPLIT_BYTES");
+    if (split && atol(split) > 0) half = (size_t)atol(split);
+    std::vector<size_t> pb(HC.size());
+    for (size_t k = 0; k < HC.size(); ++k)
+      pb[k] = song2_class_spec_bytes() + song2_smem_bytes(HC[k].s, precision, c->block, s.lu_in_smem);
+    std::vector<WorkItem> big, small;
+    size_t smem_big = 0, smem_small = 0;
+    for (const WorkItem &w : gitems) {
+      if (pb[w.cls] > half) { big.push_back(w); smem_big = std::max(smem_big, pb[w.cls]); }
+      else { small.push_back(w); smem_small = std::max(smem_small, pb[w.cls]); }
+    }
+    if (!big.empty() && !small.empty()) {
+      gitems = big;
+      gitems.insert(gitems.end(), small.begin(), small.end());
+      int nt = 0;
+      for (int g = 0; g < 2; ++g) {
+        song2_ctx::Group G;
+        G.first = g == 0 ? 0 : (int)big.size();
+        G.count = g == 0 ? (int)big.size() : (int)small.size();
+        G.smem = g == 0 ? smem_big : smem_small;
+        int ps = song2_max_ctas_per_sm(precision, 3, c->block, G.smem);
+        if (ps < 1) {
+          snprintf(err, SONG2_ERRLEN, "launch configuration does not fit on an SM");
+          return 1;
+        }
+        G.grid = std::max(1, std::min(G.count, nsm * ps));
+        nt = std::max(nt, G.grid);
+        c->groups.push_back(G);
+      }
+      c->n_teams = nt;
+    }
+  }
 
   cudaStream_t st = 0;
   DevPtrs &p = c->ptrs;
@@ -594,7 +641,7 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   if (upload(c, H.qs_sp, &p.tabs.qs_sp, st, err) || upload(c, H.qs_l, &p.tabs.qs_l, st, err) || upload(c, H.qs_m, &p.tabs.qs_m, st, err))
     return 1;
   if (upload(c, H.row_slot, &p.tabs.row_slot, st, err) || upload(c, H.qs_slot, &p.tabs.qs_slot, st, err)) return 1;
-  if (upload(c, items, &p.items, st, err)) return 1;
+  if (upload(c, gitems, &p.items, st, err)) return 1;
   if (classes) {
     /* per-class specs (run-level fields from the run-wide spec) and tables */
     std::vector<DevSpec> cspec;
@@ -876,14 +923,30 @@ int song2_ctx_run(song2_ctx *c, void *stream, char *err) {
   cudaStream_t st = (cudaStream_t)stream;
   CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
   CK(cudaEventRecord(c->ev0, st));
-  if (song2_launch_evolver(c->spec, c->ptrs, c->precision, c->launch.warp_team, c->grid, c->block, c->smem, st)) {
-    snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-    return 1;
+  if (c->groups.empty()) {
+    if (song2_launch_evolver(c->spec, c->ptrs, c->precision, c->launch.warp_team, c->grid, c->block, c->smem, st)) {
+      snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return 1;
+    }
+    c->last_launches = 1;
+  } else {
+    for (const song2_ctx::Group &G : c->groups) {
+      DevSpec sg = c->spec;
+      sg.n_items = G.count;
+      DevPtrs pg = c->ptrs;
+      pg.items = c->ptrs.items + G.first;
+      pg.stats = c->ptrs.stats + G.first;
+      if (G.first > 0) CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
+      if (song2_launch_evolver(sg, pg, c->precision, c->launch.warp_team, G.grid, c->block, G.smem, st)) {
+        snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        return 1;
+      }
+    }
+    c->last_launches = (int)c->groups.size();
   }
   CK(cudaEventRecord(c->ev1, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
-  c->last_launches = 1;
   return 0;
 }
 

@@ -96,3 +96,16 @@ def test_gpu_uneven_matches_oracle(lib, uneven, precision):
     src, st, _ = gpu_run(lib, p, precision)
     assert np.all(st["status"] == 0)
     assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+
+
+@pytest.mark.gpu
+def test_gpu_uneven_launch_groups_match_single_launch(lib, uneven, monkeypatch):
+    """Splitting an uneven batch into launch groups by class size (large plans
+    first) computes the same sources as one launch."""
+    from helpers import gpu_run
+    p, _, _ = uneven
+    one, _, _ = gpu_run(lib, p, 1)
+    monkeypatch.setenv("SONG2_CLASS_SPLIT_BYTES", "20000")
+    two, st, _ = gpu_run(lib, p, 1)
+    assert np.all(st["status"] == 0)
+    assert np.array_equal(one, two)
