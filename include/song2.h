@@ -189,6 +189,15 @@ int song2_tp2_size(const song2_spec *spec);
    source buffer, and the length of one source type. */
 int64_t song2_pair_offset(const song2_spec *spec, int index_k1, int index_k2);
 int64_t song2_sources_per_type(const song2_spec *spec);
+/* The reference's raw source files (store_sources = yes): <dir>/sources_%03d.dat
+   holds, for one k1, every source type and every k2 <= k1 the tau_size*k3_size
+   doubles of ppt2->sources[tp][k1][k2] in native byte order, no header.  Writes /
+   reads the k1 slab of the flat buffer.  Replace perturb2_store_sources_to_disk
+   (perturbations2.c:15347-15387, with perturb2_store_sources_k3_tau :15397-15419,
+   path :1062) and perturb2_load_sources_from_disk (:521-563, with
+   perturb2_load_sources_k3_tau :575-602), so transfer2 reads the files unchanged. */
+int song2_store_sources(const song2_spec *spec, const double *flat, const char *dir, int index_k1, char *err);
+int song2_load_sources(const song2_spec *spec, double *flat, const char *dir, int index_k1, char *err);
 /* Default spec values from source/input2.c:2027-2371 (pointers left NULL). */
 void song2_spec_defaults(song2_spec *spec);
 

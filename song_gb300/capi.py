@@ -112,6 +112,8 @@ SIGNATURES = {
     "song2_tp2_size": (_I, [C.POINTER(Spec)]),
     "song2_pair_offset": (C.c_int64, [C.POINTER(Spec), _I, _I]),
     "song2_sources_per_type": (C.c_int64, [C.POINTER(Spec)]),
+    "song2_store_sources": (_I, [C.POINTER(Spec), C.POINTER(C.c_double), C.c_char_p, _I, C.c_char_p]),
+    "song2_load_sources": (_I, [C.POINTER(Spec), C.POINTER(C.c_double), C.c_char_p, _I, C.c_char_p]),
     "song2_spec_defaults": (None, [C.POINTER(Spec)]),
     "song2_background_compute": (_I, [C.POINTER(Cosmo), _I, _PD, _PD, _PD, _PD, _PD, _PD, C.c_char_p]),
     "song2_spline_uniform": (None, [_I, _I, _D, _PD, _PD]),

@@ -74,6 +74,65 @@ int64_t song2_sources_per_type(const song2_spec *s) {
   return (int64_t)s->tau_size * song2_n_triplets(s);
 }
 
+/* Bytes of the k1 slab of every source type in the flat buffer: the pairs
+   (k1, k2 <= k1) are consecutive, so it is one contiguous run per type. */
+static int64_t k1_run(const song2_spec *s, int index_k1) {
+  int64_t n = 0;
+  for (int i2 = 0; i2 <= index_k1; ++i2) n += (int64_t)s->tau_size * s->k3_size[index_k1 * s->k_size + i2];
+  return n;
+}
+
+int song2_store_sources(const song2_spec *s, const double *flat, const char *dir, int index_k1, char *err) {
+  if (index_k1 < 0 || index_k1 >= s->k_size) {
+    snprintf(err, SONG2_ERRLEN, "index_k1 %d outside 0..%d", index_k1, s->k_size - 1);
+    return 1;
+  }
+  char path[4096];
+  snprintf(path, sizeof(path), "%s/sources_%03d.dat", dir, index_k1);
+  FILE *f = fopen(path, "wb");
+  if (!f) {
+    snprintf(err, SONG2_ERRLEN, "cannot open %.900s for writing", path);
+    return 1;
+  }
+  int tp2 = song2_tp2_size(s);
+  int64_t per_type = song2_sources_per_type(s), off = song2_pair_offset(s, index_k1, 0), n = k1_run(s, index_k1);
+  for (int tp = 0; tp < tp2; ++tp)
+    if (n > 0 && fwrite(flat + (int64_t)tp * per_type + off, sizeof(double), (size_t)n, f) != (size_t)n) {
+      fclose(f);
+      snprintf(err, SONG2_ERRLEN, "short write to %.900s", path);
+      return 1;
+    }
+  if (fclose(f)) {
+    snprintf(err, SONG2_ERRLEN, "error closing %.900s", path);
+    return 1;
+  }
+  return 0;
+}
+
+int song2_load_sources(const song2_spec *s, double *flat, const char *dir, int index_k1, char *err) {
+  if (index_k1 < 0 || index_k1 >= s->k_size) {
+    snprintf(err, SONG2_ERRLEN, "index_k1 %d outside 0..%d", index_k1, s->k_size - 1);
+    return 1;
+  }
+  char path[4096];
+  snprintf(path, sizeof(path), "%s/sources_%03d.dat", dir, index_k1);
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    snprintf(err, SONG2_ERRLEN, "cannot open %.900s for reading", path);
+    return 1;
+  }
+  int tp2 = song2_tp2_size(s);
+  int64_t per_type = song2_sources_per_type(s), off = song2_pair_offset(s, index_k1, 0), n = k1_run(s, index_k1);
+  for (int tp = 0; tp < tp2; ++tp)
+    if (n > 0 && fread(flat + (int64_t)tp * per_type + off, sizeof(double), (size_t)n, f) != (size_t)n) {
+      fclose(f);
+      snprintf(err, SONG2_ERRLEN, "Error reading from %.900s: fewer entries than tau_size*k3_size per (type, k2)", path);
+      return 1;
+    }
+  fclose(f);
+  return 0;
+}
+
 void song2_spec_defaults(song2_spec *s) {
   memset(s, 0, sizeof(*s));
   s->l_max_g = s->l_max_pol_g = s->l_max_ur = 8;         /* input2.c:2257-2259 */
