@@ -496,10 +496,14 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     }
   }
   if (classes) {
-    /* uneven batches run one CTA per triplet */
+    /* uneven batches run one CTA per triplet; automatic: 256 threads, iteration
+       matrices in shared memory where they fit */
     L.warp_team = 0;
     L.teams_per_cta = 1;
-    if (L.threads_per_team <= 0) L.threads_per_team = 256;
+    if (L.threads_per_team <= 0) {
+      L.threads_per_team = 256;
+      L.lu_in_smem = 1;
+    }
   }
   if (L.teams_per_cta <= 0 && L.threads_per_team <= 0 && !L.warp_team) {
     /* measured on config-2-sized problems: the mixed form is fastest with 256
@@ -541,10 +545,36 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     for (auto &hc : HC) mx = std::max(mx, song2_smem_bytes(hc.s, precision, c->block, lu));
     return song2_class_spec_bytes() + mx;
   };
-  if (L.lu_in_smem && plan_bytes(1) > (size_t)smem_optin) L.lu_in_smem = 0;
-  s.lu_in_smem = L.lu_in_smem;
+  /* uneven batches: per class, the iteration matrices go to shared memory when
+     they fit the class's launch group (two CTAs per SM for the classes whose plan
+     without them fits half an SM, one CTA per SM for the others) */
+  int smem_sm = 0;
+  CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  size_t half = (size_t)smem_sm / 2 > 1024 ? (size_t)smem_sm / 2 - 1024 : 0;
+  /* SONG2_CLASS_SPLIT_BYTES overrides the plan size that separates the groups */
+  const char *split = getenv("SONG2_CLASS_SPLIT_BYTES");
+  if (split && atol(split) > 0) half = (size_t)atol(split);
+  std::vector<size_t> pb(HC.size());
+  std::vector<int> small_cls(HC.size(), 0);
+  int any_global_lu = 0;
+  for (size_t k = 0; k < HC.size(); ++k) {
+    size_t p0 = song2_class_spec_bytes() + song2_smem_bytes(HC[k].s, precision, c->block, 0);
+    size_t p1 = song2_class_spec_bytes() + song2_smem_bytes(HC[k].s, precision, c->block, 1);
+    small_cls[k] = p0 <= half;
+    size_t room = small_cls[k] ? half : (size_t)smem_optin;
+    HC[k].s.lu_in_smem = L.lu_in_smem && p1 <= room;
+    pb[k] = HC[k].s.lu_in_smem ? p1 : p0;
+    any_global_lu |= !HC[k].s.lu_in_smem;
+  }
+  if (classes) {
+    s.lu_in_smem = !any_global_lu;
+  } else {
+    if (L.lu_in_smem && plan_bytes(1) > (size_t)smem_optin) L.lu_in_smem = 0;
+    s.lu_in_smem = L.lu_in_smem;
+  }
   s.team_lanes = L.warp_team == 2 ? L.threads_per_team : 0;
   if (L.warp_team == 2) c->smem = song2_team_smem_bytes(s, L.teams_per_cta);
+  else if (classes) c->smem = *std::max_element(pb.begin(), pb.end());
   else c->smem = plan_bytes(s.lu_in_smem);
   if (c->smem > (size_t)smem_optin) {
     snprintf(err, SONG2_ERRLEN, "shared-memory plan %zu B exceeds the %d B limit", c->smem, smem_optin);
@@ -562,19 +592,10 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   std::vector<WorkItem> gitems(items.begin(), items.end());
   c->groups.clear();
   if (classes) {
-    int smem_sm = 0;
-    CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
-    size_t half = (size_t)smem_sm / 2 > 1024 ? (size_t)smem_sm / 2 - 1024 : 0;
-    /* SONG2_CLASS_SPLIT_BYTES overrides the plan size that separates the groups */
-    const char *split = getenv("SONG2_CLASS_SPLIT_BYTES");
-    if (split && atol(split) > 0) half = (size_t)atol(split);
-    std::vector<size_t> pb(HC.size());
-    for (size_t k = 0; k < HC.size(); ++k)
-      pb[k] = song2_class_spec_bytes() + song2_smem_bytes(HC[k].s, precision, c->block, s.lu_in_smem);
     std::vector<WorkItem> big, small;
     size_t smem_big = 0, smem_small = 0;
     for (const WorkItem &w : gitems) {
-      if (pb[w.cls] > half) { big.push_back(w); smem_big = std::max(smem_big, pb[w.cls]); }
+      if (!small_cls[w.cls]) { big.push_back(w); smem_big = std::max(smem_big, pb[w.cls]); }
       else { small.push_back(w); smem_small = std::max(smem_small, pb[w.cls]); }
     }
     if (!big.empty() && !small.empty()) {
@@ -650,7 +671,6 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
       DevSpec d = hc.s;
       d.n_items = s.n_items;
       d.per_type = s.per_type;
-      d.lu_in_smem = s.lu_in_smem;
       d.team_lanes = 0;
       d.lu_stride = s.lu_stride;
       d.qtab_stride = s.qtab_stride;
@@ -709,6 +729,11 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
     if (alloc_dev(c, (size_t)c->n_teams * s.lu_stride * ts, &tmp, err)) return 1;
     p.lu_global = tmp;
+    if (precision == SONG2_PREC_MIXED && L.warp_team != 2) {
+      /* the explicit inverse of the FP32 blocks */
+      if (alloc_dev(c, (size_t)c->n_teams * s.lu_stride * sizeof(float), &tmp, err)) return 1;
+      p.minv_global = (float *)tmp;
+    }
   }
   if (L.warp_team == 2) {
     /* team kernel: vectors, solve vectors and pivots of every resident team */
@@ -1176,6 +1201,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
   size_t qtab_team = s.has_qs ? (size_t)s.fo_tau_size * 2 * s.qs2_size * sizeof(double) : 0;
   size_t per_team = na_align((size_t)s.lu_elems * sizeof(double)) + (s.lu_in_smem ? 0 : na_align((size_t)s.lu_elems * ts)) +
+                    ((s.lu_in_smem || precision != SONG2_PREC_MIXED) ? 0 : na_align((size_t)s.lu_elems * sizeof(float))) +
                     na_align(qtab_team);
   size_t teams_fit = (SONG2_NOALLOC_BYTES - fixed) / per_team;
   if (teams_fit < 1) {
@@ -1192,6 +1218,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   grid = (int)std::min<size_t>((size_t)grid, teams_fit);
   size_t o_jac = take((size_t)grid * s.lu_elems * sizeof(double));
   size_t o_lu = s.lu_in_smem ? 0 : take((size_t)grid * s.lu_elems * ts);
+  size_t o_minv = (s.lu_in_smem || precision != SONG2_PREC_MIXED) ? 0 : take((size_t)grid * s.lu_elems * sizeof(float));
   size_t o_qtab = s.has_qs ? take((size_t)grid * qtab_team) : 0;
 
   auto put = [&](size_t o, const void *src, size_t bytes) -> cudaError_t {
@@ -1239,6 +1266,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   p.stats = stats_dev;
   p.jac = (double *)(base + o_jac);
   p.lu_global = s.lu_in_smem ? nullptr : (void *)(base + o_lu);
+  p.minv_global = (s.lu_in_smem || precision != SONG2_PREC_MIXED) ? nullptr : (float *)(base + o_minv);
   p.qtab = s.has_qs ? (double *)(base + o_qtab) : nullptr;
   p.spl_c = (const double *)(base + o_splc);
   p.queue = (int *)(base + o_queue);

@@ -85,7 +85,7 @@ struct Shared {
 /* Offsets (in bytes) of the dynamic shared-memory plan. */
 struct Plan {
   size_t y, f, ynew, difkp1, psiv, del, invwt, yout, dyout, dif, fo1, fo2, qs, qc, rot1, rot2, sc, bgraw, shared,
-      tab, xsol, piv, lu, total;
+      tab, xsol, piv, lu, minv, total;
 };
 
 __host__ __device__ inline size_t al(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -124,6 +124,9 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
   p.piv = o; o = al(o + n * sizeof(int));
   p.lu = o;
   if (lu_in_smem) o = al(o + (size_t)s.lu_elems * ts);
+  /* mixed form: the explicit inverse of the factorised blocks, beside them */
+  p.minv = o;
+  if (lu_in_smem && prec == SONG2_PREC_MIXED) o = al(o + (size_t)s.lu_elems * sizeof(float));
   p.total = o;
   return p;
 }
@@ -201,6 +204,7 @@ template <int MODE> struct KX {
   short *lm_s, *lmq_s, *im_s, *eq_sp, *eq_l, *eq_m, *idx_I, *idx_E, *idx_B, *idx_N, *qs_sp, *qs_l, *qs_m, *row_slot,
       *qs_slot;
   char *xsol_b, *lu_b;     /* element 0 of this team's solve vector and LU blocks */
+  float *minv_b;           /* mixed form, CTA/warp teams: the inverse of the LU blocks */
   View<int, STR> piv;
   DA jac, qtab;
 
@@ -263,6 +267,7 @@ template <int MODE> struct KX {
       xsol_b = (char *)p_.txsol + (gw * (long)s_.n * nt + tiw) * ts;
       piv = View<int, STR>{p_.tpiv + gw * (long)s_.n * nt + tiw, nt};
       lu_b = (char *)p_.lu_global + (gw * (long)s_.lu_stride * nt + tiw) * ts;
+      minv_b = nullptr;
       jac_eoff = gw * (long)s_.lu_stride * nt + tiw;
       jac = da(p_.jac + jac_eoff);
       qtab = da(p_.qtab ? p_.qtab + gw * s_.qtab_stride * nt + tiw : nullptr);
@@ -293,6 +298,12 @@ template <int MODE> struct KX {
       piv = View<int, STR>{(int *)(smem + pl.piv)};
       if (s_.lu_in_smem) lu_b = smem + pl.lu;
       else lu_b = (char *)p_.lu_global + (size_t)team * s_.lu_stride * ts;
+      /* the inverse lives beside the LU blocks in shared memory, or in global
+         scratch for small blocks (its column sweeps are latency bound there) */
+      int maxnb = 0;
+      for (int bb = 0; bb < s_.nblk; ++bb) maxnb = max(maxnb, s_.blk_size[bb]);
+      if (s_.lu_in_smem) minv_b = (float *)(smem + pl.minv);
+      else minv_b = p_.minv_global && maxnb <= 64 ? p_.minv_global + (size_t)team * s_.lu_stride : nullptr;
       jac_eoff = (long)team * s_.lu_stride;
       jac = da(p_.jac + jac_eoff);
       qtab = da(p_.qtab ? p_.qtab + (size_t)team * s_.qtab_stride : nullptr);
@@ -1228,6 +1239,26 @@ template <class C, class A, class B> __device__ void rhs(const C &c, int tca, do
   c.sync();
 }
 
+/* One simplified-Newton right-hand side: rows of f(tau, y) as in rhs(), each
+   thread turning its row straight into the residual del = h/(gamma) f - (psi +
+   dif_{k+1}) and the solve vector in the iteration-matrix precision.  Ends with a
+   barrier. */
+template <typename T, class C, class A> __device__ void newton_rhs(const C &c, int tca, double tau, A y, double hinvGak) {
+  const DevSpec &s = c.s;
+  auto yv = yvec(y);
+  compute_ws_team(c, tca, yv);
+  c.sync();
+  auto x = c.template xsol<T>();
+  for (int e = c.rank; e < s.n_row_slots; e += c.size) {
+    int i = c.row_slot[e];
+    if (i >= 0) {
+      double fi = row(c, tca, i, yv, c.sh->ws, 0, tau);
+      x[i] = (T)(hinvGak * fi - (c.psiv[i] + c.difkp1[i]));
+    }
+  }
+  c.sync();
+}
+
 /* Exact Jacobian of the affine system at tau (prepare(tau) must have run):
    J[:, j] = A e_j, one thread per column; stored per m block in global scratch. */
 template <typename T, class C> __device__ void jacobian(const C &c, int tca, double tau) {
@@ -1334,6 +1365,72 @@ __device__ void band_lu(const C &c, int b, int lane, int W, unsigned mask) {
   }
 }
 
+/* Mixed form: the inverse of every factorised block, column by column.  Lane j of
+   a warp solves M x = e_(col0+j) with the band factors in its own column of the
+   inverse (row-major, so the lanes' entries are adjacent), with no exchange
+   between lanes; the warps of the team share the 32-column tasks.  A Newton solve
+   is then one matrix-vector product per block instead of two serial sweeps. */
+template <class C> __device__ void band_inverse(const C &c) {
+  const DevSpec &s = c.s;
+  auto LUv = c.template lu<float>();
+  float *Mi = c.minv_b;
+  int warp = 0, lane = c.rank, nw = 1;
+  if (c.size > 32) {
+    warp = threadIdx.x >> 5;
+    lane = threadIdx.x & 31;
+    nw = blockDim.x >> 5;
+  }
+  int task = 0;
+  for (int b = 0; b < s.nblk; ++b) {
+    int nb = s.blk_size[b], kl = c.sh->kl[b], kw = kl + c.sh->ku[b];
+    auto A = LUv + s.lu_off[b];
+    float *X = Mi + s.lu_off[b];
+    auto pv = c.piv + s.blk_start[b];
+    for (int col0 = 0; col0 < nb; col0 += 32, ++task) {
+      int col = col0 + lane;
+      if (task % nw != warp || col >= nb) continue;
+      for (int i = 0; i < nb; ++i) X[i * nb + col] = i == col ? 1.0f : 0.0f;
+      for (int k = 0; k < nb; ++k) {
+        int q = pv[k];
+        float xk = X[q * nb + col];
+        if (q != k) {
+          X[q * nb + col] = X[k * nb + col];
+          X[k * nb + col] = xk;
+        }
+        int last = min(nb - 1, k + kl);
+        for (int i = k + 1; i <= last; ++i) X[i * nb + col] -= A[i * nb + k] * xk;
+      }
+      for (int j = nb - 1; j >= 0; --j) {
+        float xj = X[j * nb + col] * A[j * nb + j];
+        X[j * nb + col] = xj;
+        for (int i = max(0, j - kw); i < j; ++i) X[i * nb + col] -= A[i * nb + j] * xj;
+      }
+    }
+  }
+}
+
+/* del <- M^{-1} xsol with the inverse blocks, one row per thread */
+template <class C> __device__ void inv_solve(const C &c) {
+  const DevSpec &s = c.s;
+  auto x = c.template xsol<float>();
+  for (int i = c.rank; i < s.n; i += c.size) {
+    int b = 0;
+    while (b + 1 < s.nblk && i >= s.blk_start[b + 1]) ++b;
+    int nb = s.blk_size[b], b0 = s.blk_start[b];
+    const float *row = c.minv_b + s.lu_off[b] + (i - b0) * nb;
+    float acc = 0.0f;
+    for (int j = 0; j < nb; ++j) acc += row[j] * x[b0 + j];
+    c.del[i] = (double)acc;
+  }
+  c.sync();
+}
+
+/* whether this team solves with the explicit inverse (mixed form, CTA or warp teams) */
+template <typename T, class C> __device__ inline bool use_inverse(const C &c) {
+  if constexpr (sizeof(T) == sizeof(float) && !C::STR) return c.minv_b != nullptr;
+  else return false;
+}
+
 template <typename T, class C> __device__ void form_and_factor(const C &c, double hinvGak) {
   const DevSpec &s = c.s;
   auto LU = c.template lu<T>();
@@ -1353,6 +1450,10 @@ template <typename T, class C> __device__ void form_and_factor(const C &c, doubl
   c.sync();
   per_block_group(c, [&](int b, int lane, int W, unsigned mask) { band_lu<T>(c, b, lane, W, mask); });
   c.sync();
+  if (use_inverse<T>(c)) {
+    band_inverse(c);
+    c.sync();
+  }
 }
 
 /* one m block, solved by a group of W lanes: interchange and eliminate column by
@@ -1385,15 +1486,9 @@ __device__ void band_solve(const C &c, int b, int lane, int W, unsigned mask) {
   }
 }
 
-/* del <- M^{-1} del (the right-hand side in c.del, the result written back) */
+/* xsol <- M^{-1} xsol (the right-hand side already in the solve vector) */
 template <typename T, class C> __device__ void lu_solve(const C &c) {
-  const DevSpec &s = c.s;
-  auto x = c.template xsol<T>();
-  for (int i = c.rank; i < s.n; i += c.size) x[i] = (T)c.del[i];
-  c.sync();
   per_block_group(c, [&](int b, int lane, int W, unsigned mask) { band_solve<T>(c, b, lane, W, mask); });
-  c.sync();
-  for (int i = c.rank; i < s.n; i += c.size) c.del[i] = (double)x[i];
   c.sync();
 }
 
@@ -1955,8 +2050,10 @@ __device__ int ndf15(const C &c, double t0, double t1, int &jout, int include_t0
       int gotynew = 0;
       while (!gotynew) {
         if (++attempts > s.max_steps) return SONG2_E_MAXSTEPS;
+        /* predictor, its error weights and norm in one pass */
+        unsigned long long vm = 0;
         for (int i = tid; i < n; i += nt) {
-          double ps = 0, pr = y[i];
+          double ps = 0, yi = y[i], pr = yi;
           for (int j = 0; j < k; ++j) {
             double dj = dif[(size_t)j * n + i];
             ps += dj * c_G[j];
@@ -1965,29 +2062,29 @@ __device__ int ndf15(const C &c, double t0, double t1, int &jout, int include_t0
           psiv[i] = ps * invGa[k - 1];
           ynew[i] = pr;
           difkp1[i] = 0.0;
+          double iw = 1.0 / fmax(fmax(fabs(yi), fabs(pr)), threshold);
+          invwt[i] = iw;
+          bmax(vm, pr * iw);
         }
         tnew = t + h;
         if (done) tnew = t1;
         h = tnew - t;
-        unsigned long long vm = 0;
-        for (int i = tid; i < n; i += nt) {
-          invwt[i] = 1.0 / fmax(fmax(fabs(y[i]), fabs(ynew[i])), threshold);
-          bmax(vm, ynew[i] * invwt[i]);
-        }
         double minnrm = 100 * eps * block_max_bits(c, vm);
         double oldnrm = 0;
         prepare_table(c, tnew, tca);
         for (int iter = 1; iter <= maxit; ++iter) {
-          rhs(c, tca, tnew, ynew, f);
+          newton_rhs<T>(c, tca, tnew, ynew, hinvGak);
           st.n_rhs++;
-          for (int i = tid; i < n; i += nt) del[i] = hinvGak * f[i] - (psiv[i] + difkp1[i]);
-          c.sync();
-          lu_solve<T>(c);
+          bool inv = use_inverse<T>(c);
+          if (inv) inv_solve(c);
+          else lu_solve<T>(c);
           unsigned long long vn = 0;
+          auto xs = c.template xsol<T>();
           for (int i = tid; i < n; i += nt) {
-            bmax(vn, del[i] * invwt[i]);
-            difkp1[i] += del[i];
-            ynew[i] += del[i];
+            double d = inv ? del[i] : (double)xs[i];
+            bmax(vn, d * invwt[i]);
+            difkp1[i] += d;
+            ynew[i] += d;
           }
           double newnrm = block_max_bits(c, vn);
           if (!(newnrm < INFINITY)) break;

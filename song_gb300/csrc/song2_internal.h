@@ -107,6 +107,7 @@ struct DevPtrs {
   double *qtab;                    /* per-team quadratic-source table: fo_tau_size x 2 x qs2_size doubles */
   const double *spl_c;             /* Thomas recurrence of the natural spline on a uniform grid */
   void *lu_global;                 /* per-team LU scratch when not in smem */
+  float *minv_global;              /* mixed form: per-team inverse of the LU blocks when not in smem */
   double *tslab;                   /* team kernel: per-team vectors, 32/G teams interleaved per warp */
   void *txsol;                     /* team kernel: solve vectors (iteration-matrix precision) */
   int *tpiv;                       /* team kernel: pivots */
