@@ -43,8 +43,8 @@ METRIC = "2nd-order k-triplets/s at rtol 1e-4: mixed+batched vs plain FP64 GPU; 
 WORKLOAD = 2
 # FP64 work of the mixed-form evolver per NDF step (ncu, reduced config 2) and the
 # FP64 issue rate of a GB300 SM (DFMA probe); see profiles/
-FP64_FLOPS_PER_STEP = 47.1e3
-FP64_WARP_INSTR_PER_STEP = 2.68e3
+FP64_FLOPS_PER_STEP = 47.0e3
+FP64_WARP_INSTR_PER_STEP = 2.74e3
 FP64_WARP_INSTR_PER_SM_CYCLE = 0.0526
 
 

@@ -506,13 +506,12 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     }
   }
   if (L.teams_per_cta <= 0 && L.threads_per_team <= 0 && !L.warp_team) {
-    /* measured on config-2-sized problems: the mixed form is fastest with 256
-       threads and the FP32 inverse in shared memory (two CTAs per SM), the FP64
-       form with 128 threads and its LU blocks in global scratch (four per SM) */
+    /* measured on config-2-sized problems: both forms are fastest with 256
+       threads and their iteration matrices in shared memory (two CTAs per SM) */
     L.warp_team = 0;
     L.teams_per_cta = 1;
-    L.threads_per_team = precision == SONG2_PREC_MIXED ? 256 : 128;
-    L.lu_in_smem = precision == SONG2_PREC_MIXED ? 1 : 0;
+    L.threads_per_team = 256;
+    L.lu_in_smem = 1;
   }
   if (L.warp_team == 2) {
     /* G lanes per triplet: G a power of two up to 32, whole warps per CTA, at most
