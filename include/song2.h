@@ -267,6 +267,10 @@ int song2_ctx_destroy(song2_ctx *ctx);
 /* Evolve every triplet on the device and leave the sources in device memory.
    stream may be NULL (legacy default stream).  Blocking on return. */
 int song2_ctx_run(song2_ctx *ctx, void *stream, char *err);
+/* As song2_ctx_run, with the run's stream work (queue resets and the evolver
+   launches of every launch group) captured into a CUDA graph on the first call
+   and replayed on the later ones (no counterpart in the reference). */
+int song2_ctx_run_graph(song2_ctx *ctx, void *stream, char *err);
 /* Device pointer of the flat source buffer and of the per-triplet stats. */
 double *song2_ctx_device_sources(song2_ctx *ctx);
 song2_triplet_stats *song2_ctx_device_stats(song2_ctx *ctx);

@@ -135,6 +135,7 @@ SIGNATURES = {
     "song2_autotune": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, C.c_void_p, _PD, C.c_char_p]),
     "song2_ctx_destroy": (_I, [_P]),
     "song2_ctx_run": (_I, [_P, _P, C.c_char_p]),
+    "song2_ctx_run_graph": (_I, [_P, _P, C.c_char_p]),
     "song2_ctx_device_sources": (_P, [_P]),
     "song2_ctx_device_stats": (_P, [_P]),
     "song2_ctx_download": (_I, [_P, _PD, C.POINTER(TripletStats), C.c_char_p]),

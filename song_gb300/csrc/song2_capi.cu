@@ -44,6 +44,10 @@ struct song2_ctx {
     size_t smem;
   };
   std::vector<Group> groups;
+  /* song2_ctx_run_graph: the run's memsets and launches captured once */
+  cudaStream_t cap_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
 };
 
 namespace {
@@ -936,6 +940,9 @@ int song2_autotune(const song2_spec *spec, const song2_tables *tab, int precisio
 
 int song2_ctx_destroy(song2_ctx *c) {
   if (!c) return 0;
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
   for (void *p : c->allocs) cudaFree(p);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -943,10 +950,9 @@ int song2_ctx_destroy(song2_ctx *c) {
   return 0;
 }
 
-int song2_ctx_run(song2_ctx *c, void *stream, char *err) {
-  cudaStream_t st = (cudaStream_t)stream;
+/* the stream work of one run: queue resets and the evolver launch(es) */
+static int enqueue_run(song2_ctx *c, cudaStream_t st, char *err) {
   CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
-  CK(cudaEventRecord(c->ev0, st));
   if (c->groups.empty()) {
     if (song2_launch_evolver(c->spec, c->ptrs, c->precision, c->launch.warp_team, c->grid, c->block, c->smem, st)) {
       snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -968,6 +974,35 @@ int song2_ctx_run(song2_ctx *c, void *stream, char *err) {
     }
     c->last_launches = (int)c->groups.size();
   }
+  return 0;
+}
+
+int song2_ctx_run(song2_ctx *c, void *stream, char *err) {
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(cudaEventRecord(c->ev0, st));
+  if (enqueue_run(c, st, err)) return 1;
+  CK(cudaEventRecord(c->ev1, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  return 0;
+}
+
+int song2_ctx_run_graph(song2_ctx *c, void *stream, char *err) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!c->graph_exec) {
+    if (!c->cap_stream) CK(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+    if (enqueue_run(c, c->cap_stream, err)) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(c->cap_stream, &g);
+      if (g) cudaGraphDestroy(g);
+      return 1;
+    }
+    CK(cudaStreamEndCapture(c->cap_stream, &c->graph));
+    CK(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+  }
+  CK(cudaEventRecord(c->ev0, st));
+  CK(cudaGraphLaunch(c->graph_exec, st));
   CK(cudaEventRecord(c->ev1, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));

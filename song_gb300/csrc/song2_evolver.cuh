@@ -425,9 +425,12 @@ template <class C> __device__ inline double bg_col(const C &c, int q, double tau
 __device__ inline double bg_value(const double *bg, const double *bg_dd, int bg_size, double x0, double dx, int q, double x,
                                   double tau) {
   double v = spl(bg, bg_dd, bg_size, SONG2_BG_SIZE, x0, dx, q, x);
-  if (q == SONG2_BG_HC_PRIME_TAU2) return v / (tau * tau);
-  if (q == SONG2_BG_KAPPA) return exp(-v);
-  return exp(v);
+  /* one exponential on every lane of the warp: exp(v), exp(-kappa), and
+     1/tau^2 = exp(-2 ln tau) for Hc' */
+  (void)tau;
+  double arg = q == SONG2_BG_HC_PRIME_TAU2 ? -2.0 * x : (q == SONG2_BG_KAPPA ? -v : v);
+  double e = exp(arg);
+  return q == SONG2_BG_HC_PRIME_TAU2 ? v * e : e;
 }
 
 /* BgV from the linear columns */

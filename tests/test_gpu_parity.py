@@ -71,6 +71,7 @@ def test_against_tight_oracle(lib, tiny):
     dict(m=(0, 1, 2, 3, 4), l_max=6, sources="TEB"),
     dict(k_size=2, k3_size=1),
     dict(los="all", sources="TEB"),
+    dict(l_max=20, k_size=2, k3_size=2),
 ])
 def test_edge_cases(lib, olib, kw):
     p = problem(**kw)
@@ -196,3 +197,43 @@ def test_gpu_matches_golden_fixture(lib):
         for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
             src, st, _ = gpu_run(lib, p, precision)
             assert np.max(floored_errors(src, g["sources"], p)) < 10 * p.spec.rtol, name
+
+
+def test_large_blocks_in_global_scratch(lib, olib):
+    """l_max = 20 (m blocks of 67-81 rows) with the iteration matrices in global
+    scratch: the mixed form falls back from the explicit inverse to the band sweeps;
+    both forms agree with the oracle."""
+    p = problem(l_max=20, k_size=2, k3_size=2)
+    p.set_first_order(oracle.first_order(p, nthreads=8))
+    ref, _ = oracle.evolve(p, nthreads=8)
+    for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+        L = capi.Launch(0, 1, 256, 0)
+        c = C.c_void_p()
+        err = capi.errbuf()
+        assert lib.song2_ctx_create_ex(C.byref(p.spec), C.byref(p.tables), precision, C.byref(L), 0, 1, C.byref(c),
+                                       err) == 0, err.value
+        assert lib.song2_ctx_run(c, None, err) == 0, err.value
+        src = np.zeros(p.tp2_size * p.per_type)
+        st = (capi.TripletStats * p.n_triplets)()
+        lib.song2_ctx_download(c, capi.dptr(src), st, err)
+        lib.song2_ctx_destroy(c)
+        assert np.all(np.frombuffer(st, dtype=capi.STATS_DTYPE)["status"] == capi.SONG2_OK)
+        assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+
+
+def test_graph_replay_matches_direct_run(lib, tiny):
+    """song2_ctx_run_graph (captured once, replayed) computes what song2_ctx_run does."""
+    p, _, _ = tiny
+    c = C.c_void_p()
+    err = capi.errbuf()
+    assert lib.song2_ctx_create(C.byref(p.spec), C.byref(p.tables), capi.SONG2_PREC_MIXED, C.byref(c), err) == 0
+    try:
+        out = []
+        for run in (lib.song2_ctx_run, lib.song2_ctx_run_graph, lib.song2_ctx_run_graph):
+            assert run(c, None, err) == 0, err.value
+            src = np.zeros(p.tp2_size * p.per_type)
+            lib.song2_ctx_download(c, capi.dptr(src), None, err)
+            out.append(src)
+    finally:
+        lib.song2_ctx_destroy(c)
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
