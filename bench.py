@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", type=int, default=WORKLOAD)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    ap.add_argument("--accuracy-sample", type=int, default=32,
+                    help="triplets checked against the FP64 oracle at rtol 1e-8 (0: skip)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--k-size", type=int, default=None, help="override the k grid size (small profiling cases)")
@@ -247,6 +249,32 @@ def cpu_baseline(p, budget_s, threads):
     return len(pick) / dt, len(pick), dt
 
 
+def accuracy_sample(p, results, n, threads, rtol=1e-8, floor=1e-10):
+    """Max relative error of GPU sources against the FP64 oracle at rtol = 1e-8 on an
+    evenly spread sample of n triplets: per (source type, triplet) max_tau |S - S_ref| /
+    max_tau |S_ref|, the denominator floored at `floor` times the triplet's largest
+    source (odd-m sources vanish by symmetry when k1 = k2)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    work = p.work_order()
+    pick = list(range(0, len(work), max(1, len(work) // n)))[:n]
+    ref, _ = oracle.evolve(p, nthreads=threads, items=np.array(pick), rtol=rtol)
+    b = ref.reshape(p.tp2_size, p.per_type)
+    out = {}
+    for name, flat in results.items():
+        a = flat.reshape(p.tp2_size, p.per_type)
+        worst = 0.0
+        for it in pick:
+            i1, i2, i3 = work[it]
+            ta, tb = p.triplet_view(a, i1, i2, i3), p.triplet_view(b, i1, i2, i3)
+            den = np.max(np.abs(tb), axis=1)
+            den = np.maximum(den, floor * max(den.max(), 1e-300))
+            worst = max(worst, float(np.max(np.max(np.abs(ta - tb), axis=1) / den)))
+        out[name] = worst
+    return out, len(pick)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -387,6 +415,17 @@ def main():
         b = src_plain.reshape(p.tp2_size, p.per_type)
         den = np.max(np.abs(b)) + 1e-300
         line["mixed_vs_plain_max_abs_over_max"] = float(np.max(np.abs(a - b)) / den)
+    if rank == 0 and world == 1 and args.accuracy_sample > 0:
+        try:
+            res = {"mixed": src_mixed}
+            if ms_plain is not None:
+                res["plain_fp64"] = src_plain
+            errs, npick = accuracy_sample(p, res, args.accuracy_sample, os.cpu_count())
+            line["err_vs_fp64_oracle"] = dict(errs, sample_triplets=npick, oracle_rtol=1e-8,
+                                              metric="max over source types and sampled triplets of "
+                                                     "max_tau|S - S_ref| / max_tau|S_ref|")
+        except Exception as e:  # noqa: BLE001
+            line["err_vs_fp64_oracle"] = {"error": str(e)[:200]}
     if rank == 0 and world == 1:
         try:
             v, n, dt = cpu_baseline(p, args.cpu_sample_s, os.cpu_count())
