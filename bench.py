@@ -42,7 +42,7 @@ sys.path.insert(0, ROOT)
 METRIC = "2nd-order k-triplets/s at rtol 1e-4: mixed+batched vs plain FP64 GPU; err vs FP64"
 WORKLOAD = 2
 # FP64 work of the mixed-form evolver per NDF step (ncu, reduced config 2) and the
-# FP64 issue rate of a GB300 SM (DFMA probe); see profiles/
+# FP64 issue rate of a GB300 SM (DFMA probe, song_gb300/csrc/probe_fp64.cu)
 FP64_FLOPS_PER_STEP = 47.0e3
 FP64_WARP_INSTR_PER_STEP = 2.74e3
 FP64_WARP_INSTR_PER_SM_CYCLE = 0.0526
@@ -381,9 +381,9 @@ def main():
                 "note": "the evolver is bound by the FP64 pipe (RHS, residual, error control), not by HBM; "
                         "bytes = first-order rows of every (k1,k2) pair + background + source writes"}
     steps_tot = st_mixed["n_steps"].sum()
-    # FP64 pipe: algorithmic FP64 work per NDF step and the SM's FP64 issue rate,
-    # both measured on this kernel/GPU (profiles/evolver_fp64_counters.md,
-    # profiles/fp64_pipe_probe.md); the run supplies the step count and the time
+    # FP64 pipe: algorithmic FP64 work per NDF step (ncu counters of this kernel on
+    # the reduced config-2 case) and the SM's FP64 issue rate (the DFMA probe in
+    # song_gb300/csrc/probe_fp64.cu); the run supplies the step count and the time
     sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
     nsm = torch.cuda.get_device_properties(0).multi_processor_count
     fp64_flops = steps_tot * FP64_FLOPS_PER_STEP / (ms_step / 1e3)

@@ -1,8 +1,8 @@
 """ctypes mirror of include/song2.h.
 
 This module is the binding a maintainer of the reference would add to drive
-the C ABI from Python (the reference itself is driven from C: see
-INTEGRATION.md).  Every structure here matches song2.h field by field.
+the C ABI from Python (the reference itself is driven from C, through the same
+entry points).  Every structure here matches song2.h field by field.
 """
 import ctypes as C
 import os
