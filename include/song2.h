@@ -134,6 +134,19 @@ typedef struct {
   const int *class_l_max;                  /* [n_classes] */
   const int *class_m_max;                  /* [n_classes] */
   const int *triplet_class;                /* [n_triplets], pair order */
+  /* delta-tilde line-of-sight sources (use_delta_tilde_in_los, input2.c:680-683;
+     incompatible with has_redshift_in_los, input2.c:742-744): the T, E, B sources
+     gain -2 kappa' (delta*delta/2 + delta*collision), perturbations2.c:12339-12398,
+     12509-12561, 12658-12710, summed over first-order multipoles
+     l1, l2 <= l_max_los_quadratic_t (T) or l_max_los_quadratic_p (E, B);
+     input2.c:1788-1789, defaults 2 (input2.c:2265-2266). */
+  int use_delta_tilde_in_los;
+  int l_max_los_quadratic_t, l_max_los_quadratic_p;
+  /* rotation coefficients divided by sin(theta_k1)^m (ppt2->rescale_cmb_sources,
+     perturbations2.c:5635-5652; on in the reference's bispectrum runs with m > 0,
+     input2.c:1962-1971): every m-multipole of the second-order solution and of the
+     sources is multiplied by sin(theta_k1)^-m. */
+  int rescale_cmb_sources;
 } song2_spec;
 
 /* Background/thermo and first-order interpolation tables, owned by the caller
@@ -220,6 +233,15 @@ double song2_coupling_c_plus(int l, int m1, int m);
 double song2_coupling_d_minus(int l, int m1, int m);
 double song2_coupling_d_plus(int l, int m1, int m);
 double song2_coupling_d_zero(int l, int m1, int m);
+
+/* Coupling coefficient of the delta-tilde sources, the value the reference stores
+   in ppt2->coupling_coefficients[index_pf][lm(l,m)][l1][m1+l1_max][l2]
+   (perturbations2.c:1285-1527): field 0 (T, spin F = 0, prefactor 1/2),
+   1 (E) or 2 (B) (F = 2, prefactor 1), with m2 = m - m1 and L = l - l1 - l2,
+     prefactor * i^L (T, E; L even) or i^(L-1) (B; L odd)
+       * (-1)^m (2l+1) (l1 l2 l; 0 F -F) (l1 l2 l; m1 m2 -m),
+   zero for the other parity and for l2 < F or l < F. */
+double song2_delta_tilde_coupling(int field, int l, int m, int l1, int m1, int l2);
 
 /* Grids: lin/log k sampling (sources2_k_sampling = lin/log), per-pair k3 grids
    with the reference's clipping (sources2_k3_sampling = lin/log), custom tau

@@ -43,6 +43,8 @@ def load():
                                                  C.c_char_p]
         lib.song2_oracle_coupling.restype = C.c_double
         lib.song2_oracle_coupling.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
+        lib.song2_oracle_delta_tilde_coupling.restype = C.c_double
+        lib.song2_oracle_delta_tilde_coupling.argtypes = [C.c_int] * 6
         lib.song2_oracle_rhs.restype = C.c_int
         lib.song2_oracle_rhs.argtypes = [C.POINTER(capi.Spec), C.POINTER(capi.Tables), C.c_int, C.c_int, C.c_int,
                                          C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double),

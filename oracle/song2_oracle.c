@@ -116,6 +116,23 @@ double song2_oracle_coupling(int kind, int l, int m1, int m) {
   return 0.0;
 }
 
+/* delta-tilde coupling, perturb2_get_lm_lists (perturbations2.c:1380-1490): the
+   3j products of coupling_general (song_tools, absent from the reference tree),
+   as its call site defines them (:1439-1446), with the field's prefactor
+   (:1386-1400) and the sign i^L or i^(L-1) (:1466-1476). */
+double song2_oracle_delta_tilde_coupling(int field, int l, int m, int l1, int m1, int l2) {
+  int F = (field == 0) ? 0 : 2;
+  double prefactor = (field == 0) ? 0.5 : 1.0;
+  if (l2 < F || l < F) return 0.0;
+  int L = l - l1 - l2;
+  int even = (field != 2);
+  if ((abs(L) % 2 == 0) != even) return 0.0;
+  double sign = even ? ((abs(L) / 2) % 2 ? -1.0 : 1.0) : ((abs(L - 1) / 2) % 2 ? -1.0 : 1.0);
+  int m2 = m - m1;
+  double v = (m % 2 ? -1.0 : 1.0) * (2.0 * l + 1) * wigner3j(l1, l2, l, 0, F, -F) * wigner3j(l1, l2, l, m1, m2, -m);
+  return prefactor * sign * v;
+}
+
 /* ======================================================= configuration */
 
 typedef struct cfg_s {
@@ -136,6 +153,9 @@ typedef struct cfg_s {
   int first_order_mode;
   int tp2_size, index_tp2_T, index_tp2_E, index_tp2_B, index_tp2_delta_cdm;
   int64_t n_triplets;
+  /* ppt2->coupling_coefficients[field][l][m][l1][m1 + dt_Q][l2], l <= dt_L */
+  double *dtc;
+  int dt_Q, dt_L;
   /* the run-wide configuration, which fixes the source types (itself, except for
      the hierarchy classes of an uneven batch) */
   const struct cfg_s *run;
@@ -143,6 +163,10 @@ typedef struct cfg_s {
 
 #define LM(l, m) (c->lm_array[(l)][c->index_m[(m)]])
 #define LMQ(l, m) (c->lm_quad[(l)][(m)])
+#define DTC_SIZE(c) (3 * ((c)->dt_L + 1) * SONG2_MAX_M * ((c)->dt_Q + 1) * (2 * (c)->dt_Q + 1) * ((c)->dt_Q + 1))
+#define DTC(c, f, l, m, l1, m1, l2)                                                                                    \
+  ((c)->dtc[(((((f) * ((c)->dt_L + 1) + (l)) * SONG2_MAX_M + (m)) * ((c)->dt_Q + 1) + (l1)) * (2 * (c)->dt_Q + 1) +      \
+             (m1) + (c)->dt_Q) * ((c)->dt_Q + 1) + (l2)])
 /* source-type index of (l, m) in the run-wide layout */
 #define RLM(l, m) (c->run->lm_array[(l)][c->run->index_m[(m)]])
 
@@ -238,11 +262,33 @@ static int cfg_init(cfg_t *c, const song2_spec *s, const song2_tables *t, int fo
   if (s->has_source_delta_cdm) c->index_tp2_delta_cdm = tp++;
   c->tp2_size = tp;
   c->n_triplets = o_n_triplets(s);
+  if (s->use_delta_tilde_in_los && !c->first_order_mode) {
+    /* input2.c:742-744 */
+    if (s->has_redshift_in_los) {
+      snprintf(err, SONG2_ERRLEN, "use_delta_tilde_in_los excludes has_redshift_in_los");
+      return 1;
+    }
+    int Q = s->l_max_los_quadratic_t > s->l_max_los_quadratic_p ? s->l_max_los_quadratic_t : s->l_max_los_quadratic_p;
+    if (s->l_max_los_quadratic_t < 0 || s->l_max_los_quadratic_p < 0 || Q > L || Q > SONG2_MAX_M + 1) {
+      snprintf(err, SONG2_ERRLEN, "l_max_los_quadratic_t/p out of range");
+      return 1;
+    }
+    c->dt_Q = Q;
+    c->dt_L = s->l_max_los_t > s->l_max_los_p ? s->l_max_los_t : s->l_max_los_p;
+    c->dtc = (double *)calloc((size_t)DTC_SIZE(c), sizeof(double));
+    for (int f = 0; f < 3; ++f)
+      for (int l = 0; l <= c->dt_L; ++l)
+        for (int m = 0; m <= l && m < SONG2_MAX_M; ++m)
+          for (int l1 = 0; l1 <= Q; ++l1)
+            for (int m1 = -l1; m1 <= l1; ++m1)
+              for (int l2 = 0; l2 <= Q; ++l2)
+                DTC(c, f, l, m, l1, m1, l2) = song2_oracle_delta_tilde_coupling(f, l, m, l1, m1, l2);
+  }
   return 0;
 }
 
 static void cfg_free(cfg_t *c) {
-  free(c->cmin); free(c->cplu); free(c->dmin); free(c->dplu); free(c->dzer);
+  free(c->cmin); free(c->cplu); free(c->dmin); free(c->dplu); free(c->dzer); free(c->dtc);
 }
 
 /* ======================================================= interpolation */
@@ -527,9 +573,11 @@ static void ws_free(ws_t *w) {
 /* sqrt((l-m)!/(l+m)!) P_l^m(x) with the Condon-Shortley phase, computed from the
    unnormalised upward recurrence and a log-factorial normalisation (an
    independent route from the device's normalised recurrence). */
-static double legendre_norm(int l, int m, double x) {
+static double legendre_norm_r(int l, int m, double x, int rescaled) {
   double s = sqrt(fmax(0.0, 1.0 - x * x));
-  /* P_m^m = (-1)^m (2m-1)!! s^m, kept in log form with sign */
+  /* P_m^m = (-1)^m (2m-1)!! s^m, kept in log form with sign; rescaled: without s^m
+     (plegendre_lm_rescaled, perturbations2.c:5641) */
+  if (rescaled) s = 1.0;
   double logpmm = 0.0;
   for (int i = 1; i <= m; ++i) logpmm += log(2.0 * i - 1.0);
   double norm = 0.5 * (lfact(l - m) - lfact(l + m));
@@ -548,6 +596,8 @@ static double legendre_norm(int l, int m, double x) {
   return (m % 2 ? -v : v);
 }
 
+static double legendre_norm(int l, int m, double x) { return legendre_norm_r(l, m, x, 0); }
+
 static int geometrical_corner(ws_t *w, int index_k1, int index_k2, int index_k3, const double *k3row) {
   cfg_t *c = w->c;
   const song2_spec *s = c->s;
@@ -561,14 +611,27 @@ static int geometrical_corner(ws_t *w, int index_k1, int index_k2, int index_k3,
   double cosk2k = w->cosk2k = (k2 + k1 * cosk1k2) / k;
   if (fabs(cosk1k2) > 1 || fabs(cosk1k) > 1 || fabs(cosk2k) > 1) return 1;
   w->k1_dot_k2 = k1 * k2 * cosk1k2;
+  int rescale = s->rescale_cmb_sources && !c->first_order_mode;
+  double sin1 = sqrt(fmax(0.0, 1.0 - cosk1k * cosk1k)), sin2 = sqrt(fmax(0.0, 1.0 - cosk2k * cosk2k));
   for (int l = 0; l <= c->Lq; ++l)
     for (int m = 0; m <= l; ++m) {
-      double r1 = legendre_norm(l, m, cosk1k);
-      double r2 = (m % 2 ? -1.0 : 1.0) * legendre_norm(l, m, cosk2k);
-      w->rot1[LMQ(l, m)] = r1;
-      w->rot2[LMQ(l, m)] = r2;
-      w->rot1m[LMQ(l, m)] = (m % 2 ? -1.0 : 1.0) * r1;
-      w->rot2m[LMQ(l, m)] = (m % 2 ? -1.0 : 1.0) * r2;
+      double sg = (m % 2 ? -1.0 : 1.0);
+      if (!rescale) {
+        /* perturbations2.c:5604-5622 */
+        double r1 = legendre_norm(l, m, cosk1k);
+        double r2 = sg * legendre_norm(l, m, cosk2k);
+        w->rot1[LMQ(l, m)] = r1;
+        w->rot2[LMQ(l, m)] = r2;
+        w->rot1m[LMQ(l, m)] = sg * r1;
+        w->rot2m[LMQ(l, m)] = sg * r2;
+      } else {
+        /* perturbations2.c:5635-5652: P_lm / sin^m for m >= 0, (-1)^m P_lm sin^m for -m;
+           (k1/k2)^(+-m) on the k2 side */
+        w->rot1[LMQ(l, m)] = legendre_norm_r(l, m, cosk1k, 1);
+        w->rot2[LMQ(l, m)] = sg * legendre_norm_r(l, m, cosk2k, 1) * pow(k1 / k2, m);
+        w->rot1m[LMQ(l, m)] = sg * legendre_norm(l, m, cosk1k) * pow(sin1, m);
+        w->rot2m[LMQ(l, m)] = sg * (sg * legendre_norm(l, m, cosk2k) * pow(sin2, m)) * pow(k1 / k2, -m);
+      }
     }
   double k1_M1 = w->k1_m[0] = k1 * rot_1(1, -1);
   double k1_0 = w->k1_m[1] = k1 * rot_1(1, 0);
@@ -1557,6 +1620,52 @@ static void initial_conditions(ws_t *w, double tau, double *y) {
 
 /* ======================================================= outputs */
 
+/* First-order collision terms over kappa' (ppt->index_qs_monopole_collision_g and
+   _E of the first-order module): the photon one is a column of the first-order
+   table; the E one is the linear E collision term, -E_l - sqrt6/10 Pi delta_l2. */
+static double coll_g_raw(const cfg_t *c, const double *fo, int l) { return (l < 0) ? 0.0 : fo[c->fo_CG + l]; }
+static double coll_E_raw(const cfg_t *c, const double *fo, int l) {
+  if (l < 2) return 0.0;
+  double v = -fo[c->fo_E + l];
+  if (l == 2) v += -SQRT_6 * 0.1 * (fo[SONG2_FO_I + 2] - SQRT_6 * fo[c->fo_E + 2]);
+  return v;
+}
+
+/* delta-tilde terms of the (l,m) source of field 0/1/2 = T/E/B
+   (perturbations2.c:12339-12398, 12509-12561, 12658-12710) */
+static double delta_tilde_source(ws_t *w, int field, int l, int m) {
+  cfg_t *c = w->c;
+  const song2_spec *s = c->s;
+  const double *fo1 = w->fo1, *fo2 = w->fo2;
+  double delta_delta_lm = 0, delta_collision_lm = 0;
+  int lq = (field == 0) ? s->l_max_los_quadratic_t : s->l_max_los_quadratic_p;
+  for (int l1 = 0; l1 <= lq; ++l1)
+    for (int l2 = abs(l1 - l); l2 <= (l1 + l < lq ? l1 + l : lq); ++l2) {
+      if (field != 2 && (l1 + l2 + l) % 2 != 0) continue;
+      if (field == 2 && (l1 + l2 + l) % 2 == 0) continue;
+      for (int m1 = -l1; m1 <= l1; ++m1) {
+        int m2 = m - m1;
+        double coupling = (abs(m2) > l2) ? 0.0 : DTC(c, field, l, m, l1, m1, l2);
+        if (field == 0) {
+          double c_1 = rot_1(l2, m2) * coll_g_raw(c, fo1, l2);
+          double c_2 = rot_2(l2, m2) * coll_g_raw(c, fo2, l2);
+          delta_delta_lm += coupling * 2 * I_1(l1, m1) * I_2(l2, m2);
+          delta_collision_lm += coupling * 2 * 0.5 * (I_1(l1, m1) * c_2 + I_2(l1, m1) * c_1);
+        } else {
+          double c_I_k1_l1 = rot_1(l1, m1) * coll_g_raw(c, fo1, l1);
+          double c_I_k2_l1 = rot_2(l1, m1) * coll_g_raw(c, fo2, l1);
+          double c_E_k1_l2 = rot_1(l2, m2) * coll_E_raw(c, fo1, l2);
+          double c_E_k2_l2 = rot_2(l2, m2) * coll_E_raw(c, fo2, l2);
+          delta_delta_lm += coupling * 2 * 0.5 * (I_1(l1, m1) * E_2(l2, m2) + I_2(l1, m1) * E_1(l2, m2));
+          delta_collision_lm += coupling * 0.5 *
+                                (I_1(l1, m1) * c_E_k2_l2 + c_I_k1_l1 * E_2(l2, m2) + I_2(l1, m1) * c_E_k1_l2 +
+                                 c_I_k2_l1 * E_1(l2, m2));
+        }
+      }
+    }
+  return -QUAD_COEFF * w->kappa_dot * 0.5 * delta_delta_lm - QUAD_COEFF * w->kappa_dot * delta_collision_lm;
+}
+
 static void store_sources(ws_t *w, int index_tau, double tau, const double *y, const double *dy) {
   cfg_t *c = w->c;
   const song2_spec *s = c->s;
@@ -1590,6 +1699,7 @@ static void store_sources(ws_t *w, int index_tau, double tau, const double *y, c
   if (c->compute_m[2]) gamma_m2_prime = y[PV->idx_gamma_p];
   int64_t col = (int64_t)index_tau * w->k3_size + w->index_k3;
   double *base = w->src_flat + w->pair_off + col;
+  int dtilde = s->use_delta_tilde_in_los && s->has_quadratic_sources;
   if (s->has_source_T) {
     int switch_sw = s->has_sw ? 1 : 0, switch_isw = s->has_isw ? 1 : 0;
     for (int l = 0; l <= s->l_max_los_t; ++l)
@@ -1634,6 +1744,7 @@ static void store_sources(ws_t *w, int index_tau, double tau, const double *y, c
         if (s->has_lensing_in_los)
           src -= I_2_raw(l + 1) * r_plus_12(l, m) * k1 * (phi_1 + psi_1) - I_2_raw(l - 1) * r_minus_12(l, m) * k1 * (phi_1 + psi_1) +
                  I_1_raw(l + 1) * r_plus_21(l, m) * k2 * (phi_2 + psi_2) - I_1_raw(l - 1) * r_minus_21(l, m) * k2 * (phi_2 + psi_2);
+        if (dtilde) src += delta_tilde_source(w, 0, l, m);
         src *= exp_m_kappa;
         base[(int64_t)(c->run->index_tp2_T + RLM(l, m)) * w->per_type] = src;
       }
@@ -1655,6 +1766,7 @@ static void store_sources(ws_t *w, int index_tau, double tau, const double *y, c
         if (s->has_lensing_in_los)
           src -= E_2_raw(l + 1) * k_plus_12(l, m) * k1 * (phi_1 + psi_1) - E_2_raw(l - 1) * k_minus_12(l, m) * k1 * (phi_1 + psi_1) +
                  E_1_raw(l + 1) * k_plus_21(l, m) * k2 * (phi_2 + psi_2) - E_1_raw(l - 1) * k_minus_21(l, m) * k2 * (phi_2 + psi_2);
+        if (dtilde) src += delta_tilde_source(w, 1, l, m);
         src *= exp_m_kappa;
         base[(int64_t)(c->run->index_tp2_E + RLM(l, m)) * w->per_type] = src;
       }
@@ -1669,6 +1781,7 @@ static void store_sources(ws_t *w, int index_tau, double tau, const double *y, c
         if (s->has_time_delay_in_los) src -= -k2 * E_2_raw(l) * d_zero_22(l, m) * (phi_1 + psi_1) - k1 * E_1_raw(l) * d_zero_11(l, m) * (phi_2 + psi_2);
         if (s->has_redshift_in_los) src -= -E_2_raw(l) * 4 * d_zero_12(l, m) * k1 * psi_1 - E_1_raw(l) * 4 * d_zero_21(l, m) * k2 * psi_2;
         if (s->has_lensing_in_los) src -= -E_2_raw(l) * k_zero_12(l, m) * k1 * (phi_1 + psi_1) - E_1_raw(l) * k_zero_21(l, m) * k2 * (phi_2 + psi_2);
+        if (dtilde) src += delta_tilde_source(w, 2, l, m);
         src *= exp_m_kappa;
         base[(int64_t)(c->run->index_tp2_B + RLM(l, m)) * w->per_type] = src;
       }
@@ -2415,7 +2528,29 @@ int song2_oracle_geometry_checks(const song2_spec *s, int i1, int i2, int i3, do
     CHK((k - (kz1 + kz2)) / k, 1e-12);
     CHK((kx1 + kx2) / k, 1e-8);
     CHK(1 - kz1 / w->k1_m[1], 1e-12);
-    if (fabs(kx1) > 1e-6 * k1) CHK(1 - (-kx1 / SQRT_2) / w->k1_m[2], 1e-8);
+    CHK(1 - kz2 / w->k2_m[1], 1e-12);
+    /* the l = 1 rotation coefficients are the spherical components of the unit
+       vectors, divided by sin(theta_k1) when rescaled (:5953-5970) */
+    int resc = s->rescale_cmb_sources;
+    double k1_P1_cart = -kx1 / SQRT_2, k2_P1_cart = -kx2 / SQRT_2;
+    if (resc) { k1_P1_cart /= sink1k; k2_P1_cart = k2_P1_cart / sink2k * k1 / k2; }
+    /* sin(theta) from 1 - cos^2 loses digits as 1/sin^2: near-collinear triangles
+       are checked to that conditioning */
+    double cond = 1.0 / fmin(1.0, 1e4 * sink1k * sink1k);
+    if (fabs(kx1) > 1e-6 * k1) {
+      CHK(1 - k1_P1_cart / w->k1_m[2], 1e-8 * cond);
+      CHK(1 - k2_P1_cart / w->k2_m[2], 1e-8 * cond);
+    }
+    if (resc && fabs(kx1) > 1e-6 * k1) {
+      /* rescaled k1 (x) k2 times sin^m equals the Cartesian, unrescaled one (:6025-6064) */
+      double u1M = kx1 / SQRT_2, u1P = -u1M, u2M = kx2 / SQRT_2, u2P = -u2M;
+      double t[3] = {kz1 * kz2 - w->k1_dot_k2 / 3., (u1P * kz2 + u2P * kz1) / SQRT_3, SQRT_2 / SQRT_3 * u1P * u2P};
+      (void)u1M; (void)u2M;
+      for (int m = 0; m <= 2; ++m) {
+        double un = w->k1_ten_k2[m + 2] * pow(sink1k, m);
+        if (fabs(un) > 1e-30) CHK((t[m] - un) / (k1 * k2), 1e-8 * cond);
+      }
+    }
     double k1k2s = w->k1_m[1] * w->k2_m[1] - w->k1_m[0] * w->k2_m[2] - w->k1_m[2] * w->k2_m[0];
     CHK((k1k2s - w->k1_dot_k2) / (k1 * k2), 1e-8);
     CHK(w->rot1[0] - 1.0, 1e-14);

@@ -49,6 +49,10 @@ int song2_oracle_first_order(const song2_spec *spec, const song2_tables *bg_only
    0 c_minus, 1 c_plus, 2 d_minus, 3 d_plus, 4 d_zero. */
 double song2_oracle_coupling(int kind, int l, int m1, int m);
 
+/* delta-tilde coupling ppt2->coupling_coefficients of field 0/1/2 = T/E/B at
+   (l, m, l1, m1, l2) (perturbations2.c:1380-1490), from the same 3j symbols. */
+double song2_oracle_delta_tilde_coupling(int field, int l, int m, int l1, int m1, int l2);
+
 /* Right-hand side of one triplet at (tau, y) for tests: layout of the full
    (no approximation) vector unless tca != 0.  Returns n or -1. */
 int song2_oracle_rhs(const song2_spec *spec, const song2_tables *tab, int index_k1, int index_k2,

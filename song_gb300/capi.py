@@ -70,6 +70,9 @@ class Spec(C.Structure):
         ("tau_size", C.c_int), ("tau", C.POINTER(C.c_double)),
         ("n_classes", C.c_int), ("class_l_max", C.POINTER(C.c_int)), ("class_m_max", C.POINTER(C.c_int)),
         ("triplet_class", C.POINTER(C.c_int)),
+        ("use_delta_tilde_in_los", C.c_int),
+        ("l_max_los_quadratic_t", C.c_int), ("l_max_los_quadratic_p", C.c_int),
+        ("rescale_cmb_sources", C.c_int),
     ]
 
 
@@ -122,6 +125,7 @@ SIGNATURES = {
     "song2_coupling_d_minus": (_D, [_I, _I, _I]),
     "song2_coupling_d_plus": (_D, [_I, _I, _I]),
     "song2_coupling_d_zero": (_D, [_I, _I, _I]),
+    "song2_delta_tilde_coupling": (_D, [_I, _I, _I, _I, _I, _I]),
     "song2_k_grid": (_I, [_I, _D, _D, _I, _PD]),
     "song2_k3_grids": (_I, [_PD, _I, _I, _I, _PI, _PD, C.c_char_p]),
     "song2_tau_grid": (_I, [_I, _D, _D, _I, _PD]),

@@ -119,6 +119,26 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   s.L_big = L;
   s.Lq = L + 1;
   s.mq_max = std::min(m_max + 1, s.Lq);
+  /* delta-tilde sources (perturb2_get_lm_lists, perturbations2.c:1285-1300; the
+     flag check of input2.c:742-744): the couplings reach |m1|, |m2| <= the
+     quadratic cut, so the rotation coefficients are needed up to that m */
+  if (sp->use_delta_tilde_in_los && !first_order_mode) {
+    if (sp->has_redshift_in_los) {
+      snprintf(err, SONG2_ERRLEN, "use_delta_tilde_in_los excludes has_redshift_in_los");
+      return 1;
+    }
+    int qt = sp->l_max_los_quadratic_t, qp = sp->l_max_los_quadratic_p;
+    int Q = std::max(qt, qp);
+    if (qt < 0 || qp < 0 || Q > L || Q > SONG2_MAX_M + 1) {
+      snprintf(err, SONG2_ERRLEN, "l_max_los_quadratic_t/p must lie in 0..min(%d, l_max)", SONG2_MAX_M + 1);
+      return 1;
+    }
+    s.dtilde = sp->has_quadratic_sources ? 1 : 0;
+    s.dt_qt = qt; s.dt_qp = qp; s.dt_Q = Q;
+    s.dt_L = std::max(sp->l_max_los_t, sp->l_max_los_p);
+    s.mq_max = std::max(s.mq_max, Q);
+  }
+  s.rescale = sp->rescale_cmb_sources && !first_order_mode;
   for (int l = 0; l < S2_LMAXP; ++l) {
     s.index_m_max[l] = -1;
     for (int i = 0; i < s.m_size; ++i)
@@ -403,6 +423,22 @@ int build_class_layouts(const song2_spec *sp, const song2_tables *tab, const Dev
     memcpy(d.tp_m, run.tp_m, sizeof(d.tp_m));
   }
   return 0;
+}
+
+/* ppt2->coupling_coefficients of the three fields in the dt_index() layout */
+static std::vector<double> dt_table(const DevSpec &s) {
+  std::vector<double> t;
+  if (!s.dtilde) return t;
+  t.assign(dt_table_size(s), 0.0);
+  int Q = s.dt_Q;
+  for (int f = 0; f < 3; ++f)
+    for (int l = 0; l <= s.dt_L; ++l)
+      for (int m = 0; m <= std::min(l, SONG2_MAX_M - 1); ++m)
+        for (int l1 = 0; l1 <= Q; ++l1)
+          for (int m1 = -l1; m1 <= l1; ++m1)
+            for (int l2 = 0; l2 <= Q; ++l2)
+              t[dt_index(s, f, l, m, l1, m1, l2)] = song2_delta_tilde_coupling(f, l, m, l1, m1, l2);
+  return t;
 }
 
 template <typename V> int upload(song2_ctx *c, const V &v, const typename V::value_type **dst, cudaStream_t st, char *err) {
@@ -728,6 +764,7 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     }
     if (upload(c, cs, &p.spl_c, st, err)) return 1;
   }
+  if (s.dtilde && upload(c, dt_table(s), &p.dt_coup, st, err)) return 1;
   if (!s.lu_in_smem) {
     size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
     if (alloc_dev(c, (size_t)c->n_teams * s.lu_stride * ts, &tmp, err)) return 1;
@@ -1213,6 +1250,8 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   std::vector<double> cs(std::max(2, s.fo_tau_size + 1), 0.0);
   for (size_t j = 1; j < cs.size(); ++j) cs[j] = 1.0 / (4.0 - cs[j - 1]);
   size_t o_splc = take(sizeof(double) * cs.size());
+  std::vector<double> dtc = dt_table(s);
+  size_t o_dt = take(sizeof(double) * dtc.size());
   size_t fixed = off;
   if (fixed > SONG2_NOALLOC_BYTES) {
     snprintf(err, SONG2_ERRLEN, "problem tables need %zu B, more than the %zu B scratch", fixed,
@@ -1273,6 +1312,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   CK(put(o_rsl, H.row_slot.data(), nrs)); CK(put(o_qsl, H.qs_slot.data(), nqs));
   CK(put(o_items, items.data(), sizeof(WorkItem) * items.size()));
   CK(put(o_splc, cs.data(), sizeof(double) * cs.size()));
+  CK(put(o_dt, dtc.data(), sizeof(double) * dtc.size()));
   /* the scratch keeps the previous call's contents: the work-queue counter and the
      outputs (entries the sources never write, e.g. E with l < 2) must start at zero */
   CK(cudaMemsetAsync(base + o_queue, 0, sizeof(int), st));
@@ -1303,6 +1343,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   p.minv_global = (s.lu_in_smem || precision != SONG2_PREC_MIXED) ? nullptr : (float *)(base + o_minv);
   p.qtab = s.has_qs ? (double *)(base + o_qtab) : nullptr;
   p.spl_c = (const double *)(base + o_splc);
+  p.dt_coup = s.dtilde ? (const double *)(base + o_dt) : nullptr;
   p.queue = (int *)(base + o_queue);
   if (song2_launch_evolver(s, p, precision, 0, grid, block, smem, st)) {
     snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));

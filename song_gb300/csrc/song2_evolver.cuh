@@ -53,6 +53,7 @@ struct BgV {
 struct Tri {
   double k1, k2, k, k_sq, cosk1k2, cosk1k, cosk2k, k1_dot_k2;
   double k1_m[3], k2_m[3], k1_ten_k2[5], k1_ten_k1[5], k2_ten_k2[5];
+  double mfac[SONG2_MAX_M + 3];    /* rot(l,-m) = (-1)^m rot(l,m) mfac[m]: sin(theta_k1)^2m if rescaled, else 1 */
   double tau_ini, tau_switch, tau_end;
   int i1, i2, i3, pair, item, tca0, nint, k3_size;
   int64_t pair_off;
@@ -347,11 +348,13 @@ template <int MODE> struct KX {
   __device__ double rot_1(int l, int m) const {
     if (l < 0 || abs(m) > l) return 0.0;
     double v = rot1[LMQ(l, abs(m))];
+    if (m < 0) v *= sh->tri.mfac[-m];
     return (m < 0 && (m & 1)) ? -v : v;
   }
   __device__ double rot_2(int l, int m) const {
     if (l < 0 || abs(m) > l) return 0.0;
     double v = rot2[LMQ(l, abs(m))];
+    if (m < 0) v *= sh->tri.mfac[-m];
     return (m < 0 && (m & 1)) ? -v : v;
   }
   __device__ double I1r(int l) const { return l < 0 ? 0.0 : fo1[SONG2_FO_I + l]; }
@@ -1540,6 +1543,50 @@ __device__ inline void bmax(unsigned long long &acc, double x) {
 
 /* ------------------------------------------------------------------ outputs */
 
+/* First-order collision terms over kappa' of the photon intensity (stored in the
+   first-order table) and of the E polarisation (its linear collision term,
+   -E_l - sqrt6/10 Pi delta_l2, Pi = I_2 - sqrt6 E_2), unrotated. */
+template <class V> __device__ double fo_coll_I(const V &fo, const DevSpec &s, int l) { return fo[s.fo_CG + l]; }
+template <class V> __device__ double fo_coll_E(const V &fo, const DevSpec &s, int l) {
+  if (l < 2) return 0.0;
+  double v = -fo[s.fo_E + l];
+  if (l == 2) v -= SQRT_6 * 0.1 * (fo[SONG2_FO_I + 2] - SQRT_6 * fo[s.fo_E + 2]);
+  return v;
+}
+
+/* delta-tilde part of the (l,m) source of field 0 (T), 1 (E) or 2 (B):
+   -2 kappa' (delta*delta/2 + delta*collision), perturbations2.c:12339-12398 (T),
+   12509-12561 (E), 12658-12710 (B). */
+template <class C> __device__ double delta_tilde_source(const C &c, int field, int l, int m, double kappa_dot) {
+  const DevSpec &s = c.s;
+  auto fo1 = c.fo1, fo2 = c.fo2;
+  int Q = field == 0 ? s.dt_qt : s.dt_qp;
+  double dd = 0.0, dc = 0.0;
+  for (int l1 = 0; l1 <= Q; ++l1)
+    for (int l2 = abs(l1 - l); l2 <= min(l1 + l, Q); ++l2) {
+      if (((l1 + l2 + l) & 1) != (field == 2 ? 1 : 0)) continue;
+      for (int m1 = -l1; m1 <= l1; ++m1) {
+        int m2 = m - m1;
+        if (abs(m2) > l2) continue;
+        double cpl = __ldg(c.p.dt_coup + dt_index(s, field, l, m, l1, m1, l2));
+        double r11 = c.rot_1(l1, m1), r21 = c.rot_2(l1, m1), r12 = c.rot_1(l2, m2), r22 = c.rot_2(l2, m2);
+        double I_1 = r11 * c.I1r(l1), I_2 = r21 * c.I2r(l1);
+        if (field == 0) {
+          double c_1 = r12 * fo_coll_I(fo1, s, l2), c_2 = r22 * fo_coll_I(fo2, s, l2);
+          dd += cpl * 2 * I_1 * (r22 * c.I2r(l2));
+          dc += cpl * 2 * 0.5 * (I_1 * c_2 + I_2 * c_1);
+        } else {
+          double E_1 = r12 * c.E1r(l2), E_2 = r22 * c.E2r(l2);
+          double cI_1 = r11 * fo_coll_I(fo1, s, l1), cI_2 = r21 * fo_coll_I(fo2, s, l1);
+          double cE_1 = r12 * fo_coll_E(fo1, s, l2), cE_2 = r22 * fo_coll_E(fo2, s, l2);
+          dd += cpl * 2 * 0.5 * (I_1 * E_2 + I_2 * E_1);
+          dc += cpl * 0.5 * (I_1 * cE_2 + cI_1 * E_2 + I_2 * cE_1 + cI_2 * E_1);
+        }
+      }
+    }
+  return -2 * kappa_dot * 0.5 * dd - 2 * kappa_dot * dc;
+}
+
 template <class C, class A, class B>
 __device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) {
   const DevSpec &s = c.s;
@@ -1617,6 +1664,7 @@ __device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) 
                c.I2r(l - 1) * ((l - 1) * c.S(CM12, l, m)) * k1 * (phi_1 + psi_1) +
                c.I1r(l + 1) * (-(l + 2) * c.S(CP21, l, m)) * k2 * (phi_2 + psi_2) -
                c.I1r(l - 1) * ((l - 1) * c.S(CM21, l, m)) * k2 * (phi_2 + psi_2);
+      if (s.dtilde) src += delta_tilde_source(c, 0, l, m, kd);
     } else if (kind == TP_E) {
       if (l >= 2) {
         if (l == 2 && s.los_pure_scat) src += -SQRT_6 * kd * 0.1 * (w.I_2m[m] - SQRT_6 * w.E_2m[m]);
@@ -1633,6 +1681,7 @@ __device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) 
                  c.E2r(l - 1) * ((l - 1) * c.S(DM12, l, m)) * k1 * (phi_1 + psi_1) +
                  c.E1r(l + 1) * (-(l + 2) * c.S(DP21, l, m)) * k2 * (phi_2 + psi_2) -
                  c.E1r(l - 1) * ((l - 1) * c.S(DM21, l, m)) * k2 * (phi_2 + psi_2);
+        if (s.dtilde) src += delta_tilde_source(c, 1, l, m, kd);
       }
     } else if (kind == TP_B) {
       if (l >= 2 && m != 0) {
@@ -1643,6 +1692,7 @@ __device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) 
           src -= -c.E2r(l) * 4 * c.S(DZ12, l, m) * k1 * psi_1 - c.E1r(l) * 4 * c.S(DZ21, l, m) * k2 * psi_2;
         if (s.los_lensing)
           src -= -c.E2r(l) * (-c.S(DZ12, l, m)) * k1 * (phi_1 + psi_1) - c.E1r(l) * (-c.S(DZ21, l, m)) * k2 * (phi_2 + psi_2);
+        if (s.dtilde) src += delta_tilde_source(c, 2, l, m, kd);
       }
     } else if (kind == TP_D) {
       if (s.compute_m[0]) {
@@ -1704,9 +1754,11 @@ template <class C, class A, class B> __device__ void store_first_order(const C &
 
 /* ------------------------------------------------------------------ geometry */
 
-/* sqrt((l-m)!/(l+m)!) P_l^m(x), Condon-Shortley phase, normalised recurrence */
-__device__ double legendre_norm(int l, int m, double x) {
-  double sx = sqrt(fmax(0.0, 1.0 - x * x));
+/* sqrt((l-m)!/(l+m)!) P_l^m(x), Condon-Shortley phase, normalised recurrence;
+   rescaled: divided by (1-x^2)^(m/2), by leaving that factor out of P_m^m (the
+   form of plegendre_lm_rescaled, which stays finite as x -> 1) */
+__device__ double legendre_norm(int l, int m, double x, int rescaled) {
+  double sx = rescaled ? 1.0 : sqrt(fmax(0.0, 1.0 - x * x));
   double q = 1.0;
   for (int i = 1; i <= m; ++i) q *= -sqrt((2.0 * i - 1.0) / (2.0 * i)) * sx;
   if (l == m) return q;
@@ -1730,14 +1782,23 @@ template <class C> __device__ int geometry(const C &c) {
     t.cosk1k = (k1 + k2 * t.cosk1k2) / k;
     t.cosk2k = (k2 + k1 * t.cosk1k2) / k;
     t.k1_dot_k2 = k1 * k2 * t.cosk1k2;
+    /* perturbations2.c:5604-5652: with rescaling, rot(l,m) = rescaled P_lm (times
+       (k1/k2)^m for k2) and rot(l,-m) = (-1)^m P_lm sin^m, i.e. (-1)^m rot(l,m) sin^2m */
+    double s2 = fmax(0.0, 1.0 - t.cosk1k * t.cosk1k), f = 1.0;
+    for (int m = 0; m < SONG2_MAX_M + 3; ++m) {
+      t.mfac[m] = s.rescale ? f : 1.0;
+      f *= s2;
+    }
   }
   c.sync();
   if (fabs(t.cosk1k2) > 1 || fabs(t.cosk1k) > 1 || fabs(t.cosk2k) > 1) return 1;
   for (int e = tid; e < (s.Lq + 1) * (s.mq_max + 1); e += nt) {
     int l = e / (s.mq_max + 1), m = e % (s.mq_max + 1);
     if (m > l) continue;
-    double r1 = legendre_norm(l, m, t.cosk1k), r2 = legendre_norm(l, m, t.cosk2k);
+    double r1 = legendre_norm(l, m, t.cosk1k, s.rescale), r2 = legendre_norm(l, m, t.cosk2k, s.rescale);
     if (m & 1) r2 = -r2;
+    if (s.rescale)
+      for (int i = 0; i < m; ++i) r2 *= t.k1 / t.k2;
     c.rot1[c.LMQ(l, m)] = r1;
     c.rot2[c.LMQ(l, m)] = r2;
   }

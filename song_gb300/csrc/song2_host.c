@@ -137,6 +137,7 @@ void song2_spec_defaults(song2_spec *s) {
   memset(s, 0, sizeof(*s));
   s->l_max_g = s->l_max_pol_g = s->l_max_ur = 8;         /* input2.c:2257-2259 */
   s->l_max_los_t = s->l_max_los_p = 2;                   /* input2.c:2265-2266 */
+  s->l_max_los_quadratic_t = s->l_max_los_quadratic_p = 2;
   s->m_size = 1; s->m[0] = 0;                            /* input2.c:2268-2270 */
   s->has_polarization2 = 1;
   s->has_quadratic_sources = 1;
@@ -448,6 +449,48 @@ double song2_coupling_d_zero(int l, int m1, int m) {
   if (m1 == m - 1) return -pre * sqrt((L + m) * (L - m + 1) / 2.0);
   if (m1 == m + 1) return pre * sqrt((L - m) * (L + m + 1) / 2.0);
   return 0.0;
+}
+
+/* Wigner 3j symbol (j1 j2 j3; m1 m2 m3) by the Racah sum, with the factorials as
+   plain doubles (exact up to 22!, and the arguments stay below 40 for the
+   delta-tilde couplings, whose l, l1, l2 are bounded by twice the quadratic
+   LOS multipole cut). */
+static double threej(int j1, int j2, int j3, int m1, int m2, int m3) {
+  if (m1 + m2 + m3 != 0 || j3 < abs(j1 - j2) || j3 > j1 + j2) return 0.0;
+  if (abs(m1) > j1 || abs(m2) > j2 || abs(m3) > j3 || j1 + j2 + j3 + 1 > 170) return 0.0;
+  double f[171];
+  f[0] = 1.0;
+  for (int i = 1; i <= j1 + j2 + j3 + 1; ++i) f[i] = f[i - 1] * (double)i;
+  double tri = f[j1 + j2 - j3] * f[j1 - j2 + j3] * f[-j1 + j2 + j3] / f[j1 + j2 + j3 + 1];
+  double ms = f[j1 + m1] * f[j1 - m1] * f[j2 + m2] * f[j2 - m2] * f[j3 + m3] * f[j3 - m3];
+  int kmin = 0, kmax = j1 + j2 - j3;
+  if (j2 - j3 - m1 > kmin) kmin = j2 - j3 - m1;
+  if (j1 - j3 + m2 > kmin) kmin = j1 - j3 + m2;
+  if (j1 - m1 < kmax) kmax = j1 - m1;
+  if (j2 + m2 < kmax) kmax = j2 + m2;
+  double sum = 0.0;
+  for (int k = kmin; k <= kmax; ++k) {
+    double d = f[k] * f[j3 - j2 + k + m1] * f[j3 - j1 + k - m2] * f[j1 + j2 - j3 - k] * f[j1 - k - m1] * f[j2 - k + m2];
+    sum += (k & 1) ? -1.0 / d : 1.0 / d;
+  }
+  double v = sqrt(tri * ms) * sum;
+  return ((j1 - j2 - m3) & 1) ? -v : v;
+}
+
+double song2_delta_tilde_coupling(int field, int l, int m, int l1, int m1, int l2) {
+  if (field < 0 || field > 2 || l < 0 || l1 < 0 || l2 < 0) return 0.0;
+  int F = field == 0 ? 0 : 2;
+  double pre = field == 0 ? 0.5 : 1.0;
+  if (l2 < F || l < F) return 0.0;
+  int L = l - l1 - l2;
+  int odd_field = field == 2;
+  if ((abs(L) % 2 != 0) != odd_field) return 0.0;
+  int e = odd_field ? abs(L - 1) / 2 : abs(L) / 2;
+  double sign = (e & 1) ? -1.0 : 1.0;
+  int m2 = m - m1;
+  double v = threej(l1, l2, l, 0, F, -F) * threej(l1, l2, l, m1, m2, -m);
+  if (v == 0.0) return 0.0;
+  return pre * sign * ((m & 1) ? -1.0 : 1.0) * (2.0 * l + 1) * v;
 }
 
 /* ------------------------------------------------------------ start time */

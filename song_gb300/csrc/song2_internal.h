@@ -33,6 +33,8 @@ struct DevSpec {
   double fnl;
   int los_pure_scat, los_quad_scat, los_pure_metric, los_quad_metric, los_time_delay, los_redshift, los_lensing;
   int los_sw, los_isw, los_exp_pot;
+  int dtilde, dt_qt, dt_qp, dt_Q, dt_L;  /* delta-tilde sources: l1, l2 cuts of T and E/B, table extents */
+  int rescale;                     /* rotation coefficients / sin(theta_k1)^m */
   double rtol, threshold;
   int max_steps;
   double start_h, start_k, tol_tau;
@@ -106,6 +108,7 @@ struct DevPtrs {
   double *jac;                     /* per-team scratch: sum blk^2 doubles each */
   double *qtab;                    /* per-team quadratic-source table: fo_tau_size x 2 x qs2_size doubles */
   const double *spl_c;             /* Thomas recurrence of the natural spline on a uniform grid */
+  const double *dt_coup;           /* delta-tilde couplings, see dt_index() */
   void *lu_global;                 /* per-team LU scratch when not in smem */
   float *minv_global;              /* mixed form: per-team inverse of the LU blocks when not in smem */
   double *tslab;                   /* team kernel: per-team vectors, 32/G teams interleaved per warp */
@@ -113,6 +116,15 @@ struct DevPtrs {
   int *tpiv;                       /* team kernel: pivots */
   int *queue;                      /* work-queue counter */
 };
+
+/* Position of the delta-tilde coupling of (field, l, m, l1, m1, l2) in
+   DevPtrs::dt_coup: field 0..2 (T, E, B), l <= dt_L, 0 <= m < SONG2_MAX_M,
+   l1, l2 <= dt_Q, |m1| <= dt_Q. */
+__host__ __device__ inline int dt_index(const DevSpec &s, int field, int l, int m, int l1, int m1, int l2) {
+  return ((((field * (s.dt_L + 1) + l) * SONG2_MAX_M + m) * (s.dt_Q + 1) + l1) * (2 * s.dt_Q + 1) + m1 + s.dt_Q) *
+             (s.dt_Q + 1) + l2;
+}
+inline int dt_table_size(const DevSpec &s) { return 3 * (s.dt_L + 1) * SONG2_MAX_M * (s.dt_Q + 1) * (2 * s.dt_Q + 1) * (s.dt_Q + 1); }
 
 /* host-side launcher implemented in song2_launch.cu.  mode 0: one CTA per
    triplet; 1: one warp per triplet (several per CTA); 2: spec.team_lanes lanes per

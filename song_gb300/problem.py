@@ -270,6 +270,31 @@ class Problem:
         flat = flat.reshape(self.tp2_size, self.per_type)
         return flat[:, off + i3: off + len(self.tau) * nk3: nk3]
 
+    def tp_list(self):
+        """(kind, l, m) of every source type in the reference order: T, E, B by
+        lm(l, m) up to l_max_los_t / l_max_los_p, then delta_cdm (kind 'D', -1, 0)."""
+        s = self.spec
+        ms = [s.m[i] for i in range(s.m_size)]
+        out = []
+        for kind, flag, lmax in (("T", s.has_source_T, s.l_max_los_t), ("E", s.has_source_E, s.l_max_los_p),
+                                 ("B", s.has_source_B, s.l_max_los_p)):
+            if flag:
+                out += [(kind, l, m) for l in range(lmax + 1) for m in ms if m <= l]
+        if s.has_source_delta_cdm:
+            out.append(("D", -1, 0))
+        return out
+
+    def triplet_k(self, i1, i2, i3):
+        """(k1, k2, k) of one triplet."""
+        n = len(self.k)
+        off = 0
+        for j1 in range(n):
+            for j2 in range(j1 + 1):
+                if (j1, j2) == (i1, i2):
+                    return self.k[i1], self.k[i2], self.k3[off + i3]
+                off += int(self.k3_size[j1 * n + j2])
+        raise IndexError((i1, i2, i3))
+
     def to_nested(self, flat):
         """The reference layout sources[tp2][k1][k2<=k1] -> array (tau*k3_size + k3)."""
         flat = flat.reshape(self.tp2_size, self.per_type)

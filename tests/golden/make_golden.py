@@ -27,10 +27,16 @@ CASES = {
     "tiny_m012": dict(),
     "tiny_m0_nopol": dict(m=(0,), has_polarization2=0, sources="T"),
     "tiny_tca_off_TEB": dict(tight_coupling=0, sources="TEBD", l_max=5),
+    # delta-tilde LOS sources with rescaled rotation coefficients (the reference's
+    # intrinsic-bispectrum settings, ini/intrinsic.ini)
+    "tiny_dtilde_rescaled": dict(sources="TEB", l_max=5, use_delta_tilde_in_los=1, rescale_cmb_sources=1),
 }
 
 if __name__ == "__main__":
+    # with names as arguments only those fixtures are (re)made
     for name, kw in CASES.items():
+        if len(sys.argv) > 1 and name not in sys.argv[1:]:
+            continue
         p = problem(**kw)
         fo = oracle.first_order(p, nthreads=8)
         p.set_first_order(fo)

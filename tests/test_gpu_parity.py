@@ -237,3 +237,47 @@ def test_graph_replay_matches_direct_run(lib, tiny):
     finally:
         lib.song2_ctx_destroy(c)
     assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+
+
+@pytest.mark.parametrize("kw", [
+    dict(sources="TEB", l_max=5, use_delta_tilde_in_los=1, rescale_cmb_sources=1),
+    dict(sources="TEB", l_max=6, l_max_los_t=4, l_max_los_p=4, use_delta_tilde_in_los=1,
+         l_max_los_quadratic_t=3, l_max_los_quadratic_p=4),
+    dict(m=(0,), sources="TE", use_delta_tilde_in_los=1),
+    dict(m=(0, 1, 2, 3, 4), l_max=6, sources="TEB", rescale_cmb_sources=1),
+])
+def test_delta_tilde_and_rescaling_match_oracle(lib, olib, kw):
+    """delta-tilde LOS sources (couplings up to |m1|, |m2| = the quadratic cut, past
+    the modes the hierarchy evolves) and rescaled rotation coefficients agree with
+    the oracle in both precisions."""
+    p = problem(**kw)
+    p.set_first_order(oracle.first_order(p, nthreads=8))
+    ref, _ = oracle.evolve(p, nthreads=8)
+    for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+        src, st, _ = gpu_run(lib, p, precision)
+        assert np.all(st["status"] == capi.SONG2_OK)
+        assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+    # the warp-per-triplet and lane-team kernels carry the same source terms
+    for launch in ((1, 4, 32, 0), (2, 16, 8, 0)) if p.spec.l_max_g <= 5 else ():
+        L = capi.Launch(*launch)
+        c = C.c_void_p()
+        err = capi.errbuf()
+        assert lib.song2_ctx_create_ex(C.byref(p.spec), C.byref(p.tables), capi.SONG2_PREC_MIXED, C.byref(L), 0, 1,
+                                       C.byref(c), err) == 0, err.value
+        assert lib.song2_ctx_run(c, None, err) == 0, err.value
+        src = np.zeros(p.tp2_size * p.per_type)
+        st = (capi.TripletStats * p.n_triplets)()
+        lib.song2_ctx_download(c, capi.dptr(src), st, err)
+        lib.song2_ctx_destroy(c)
+        assert np.all(np.frombuffer(st, dtype=capi.STATS_DTYPE)["status"] == capi.SONG2_OK)
+        assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+
+
+def test_delta_tilde_excludes_redshift_term(lib):
+    """input2.c:742-744: use_delta_tilde_in_los with has_redshift_in_los is refused."""
+    p = problem(use_delta_tilde_in_los=1, has_redshift_in_los=1)
+    p.set_first_order(np.zeros(p.fo_shape()))
+    c = C.c_void_p()
+    err = capi.errbuf()
+    assert lib.song2_ctx_create(C.byref(p.spec), C.byref(p.tables), capi.SONG2_PREC_FP64, C.byref(c), err) == 1
+    assert b"redshift" in err.value

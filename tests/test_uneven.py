@@ -109,3 +109,17 @@ def test_gpu_uneven_launch_groups_match_single_launch(lib, uneven, monkeypatch):
     two, st, _ = gpu_run(lib, p, 1)
     assert np.all(st["status"] == 0)
     assert np.array_equal(one, two)
+
+
+@pytest.mark.gpu
+def test_gpu_uneven_delta_tilde_rescaled_matches_oracle(lib):
+    """Hierarchy classes with delta-tilde sources and rescaled rotation coefficients
+    (an m_max = 0 class still needs the rotation coefficients up to m = 2)."""
+    from helpers import floored_errors, gpu_run
+    p = problem(**UNEVEN, use_delta_tilde_in_los=1, rescale_cmb_sources=1)
+    p.set_uneven(**CLASSES)
+    p.set_first_order(oracle.first_order(p, nthreads=8))
+    ref, _ = oracle.evolve(p, nthreads=8)
+    src, st, _ = gpu_run(lib, p, 1)
+    assert np.all(st["status"] == 0)
+    assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
