@@ -19,13 +19,15 @@
  *   perturb2_tca_variables                   :9374-9738      -> tca_variables
  *   perturb2_compute_psi_prime               :10188-10383    -> compute_psi_prime
  *   perturb2_quadratic_sources               :10643-11813    -> quadratic_sources
- *   perturb2_sources                         :11869-12823    -> sources
+ *   perturb2_sources                         :11869-12823    -> store_sources
+ *     (delta-tilde terms                     :12339-12710    -> delta_tilde_source)
  *   evolver_ndf15 [CLASS, absent]           called :6517-6536 -> ndf15
  *
  * Deliberate, documented choices (same in the GPU evolver):
- *  - quadratic sources are computed directly from the interpolated first-order
- *    quantities at every derivs call, the reference's own alternative path
- *    (perturbations2.c:7713-7731), instead of a per-triplet spline table;
+ *  - quadratic sources in derivs come from a per-triplet table on the
+ *    first-order time nodes, splined in ln tau (perturbations2.c:10407-10606,
+ *    14366-14688), as the reference's default path; tight coupling, initial
+ *    conditions and the source functions compute them directly;
  *  - perfect baryons and CDM (reference default, input2.c:2087-2088), Newtonian
  *    gauge, phi equation = huang (input2.c:2152); no RSA/NRA intervals;
  *  - NDF15 written from Shampine & Reichelt, SIAM J. Sci. Comput. 18 (1997):
