@@ -147,7 +147,19 @@ typedef struct {
      input2.c:1962-1971): every m-multipole of the second-order solution and of the
      sources is multiplied by sin(theta_k1)^-m. */
   int rescale_cmb_sources;
+  /* radiation-streaming approximation (radiation_streaming_approximation_song,
+     input2.c:824-829; reference default rsa2_MD with triggers 90 and 10,
+     input2.c:2139-2141): SONG2_RSA_NONE or SONG2_RSA_MD.  After photon
+     decoupling (tau > tables.tau_free_streaming) and once k tau exceeds
+     radiation_streaming_trigger_tau_over_tau_k, the photon and neutrino
+     hierarchies are no longer evolved and their monopoles and dipoles follow the
+     algebraic RSA solution (perturbations2.c:5309-5321, 6778-6796, 8777-8809,
+     9773-10164). */
+  int radiation_streaming_approximation;
+  double radiation_streaming_trigger_tau_over_tau_k;
 } song2_spec;
+
+enum { SONG2_RSA_NONE = 0, SONG2_RSA_MD = 1 };
 
 /* Background/thermo and first-order interpolation tables, owned by the caller
    (the replacement for CLASS's pba/pth/ppt->quadsources). */
@@ -165,6 +177,11 @@ typedef struct {
   int fo_size;                             /* quantities per node = song2_fo_size(fo_l_max) */
   const double *fo;                        /* [k][tau][q] values */
   const double *fo_dd;                     /* [k][tau][q] spline d2/dx2 */
+  /* start of photon free streaming (CLASS pth->tau_free_streaming): the time
+     after recombination at which tau_c/tau exceeds
+     radiation_streaming_trigger_tau_c_over_tau; needed by the RSA only, see
+     song2_free_streaming_time() */
+  double tau_free_streaming;
 } song2_tables;
 
 /* Per-triplet diagnostics (the reference's per-workspace counters,
@@ -233,6 +250,12 @@ double song2_coupling_c_plus(int l, int m1, int m);
 double song2_coupling_d_minus(int l, int m1, int m);
 double song2_coupling_d_plus(int l, int m1, int m);
 double song2_coupling_d_zero(int l, int m1, int m);
+
+/* Conformal time at which tau_c/tau = 1/(kappa' tau) first exceeds trigger
+   (radiation_streaming_trigger_tau_c_over_tau, 10 by default, input2.c:2141)
+   on the background table of tab (bisection in ln tau; without reionisation
+   tau_c/tau - trigger changes sign once).  Returns tab->tau0 if it never does. */
+double song2_free_streaming_time(const song2_tables *tab, double trigger);
 
 /* Coupling coefficient of the delta-tilde sources, the value the reference stores
    in ppt2->coupling_coefficients[index_pf][lm(l,m)][l1][m1+l1_max][l2]

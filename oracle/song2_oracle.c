@@ -264,6 +264,16 @@ static int cfg_init(cfg_t *c, const song2_spec *s, const song2_tables *t, int fo
   if (s->has_source_delta_cdm) c->index_tp2_delta_cdm = tp++;
   c->tp2_size = tp;
   c->n_triplets = o_n_triplets(s);
+  if (s->radiation_streaming_approximation != SONG2_RSA_NONE && !c->first_order_mode) {
+    if (s->radiation_streaming_approximation != SONG2_RSA_MD) {
+      snprintf(err, SONG2_ERRLEN, "radiation_streaming_approximation: only none and MD");
+      return 1;
+    }
+    if (!(t->tau_free_streaming > 0) || !(s->radiation_streaming_trigger_tau_over_tau_k > 0)) {
+      snprintf(err, SONG2_ERRLEN, "the RSA needs tau_free_streaming > 0 and a positive k tau trigger");
+      return 1;
+    }
+  }
   if (s->use_delta_tilde_in_los && !c->first_order_mode) {
     /* input2.c:742-744 */
     if (s->has_redshift_in_los) {
@@ -364,7 +374,7 @@ typedef struct {
   int idx_g, idx_E, idx_B, idx_ur, idx_b, idx_cdm;
   int idx_phi, idx_phi_p, idx_omega, idx_gamma, idx_gamma_p;
   int n;
-  int tca;
+  int tca, rsa;
 } pv_t;
 
 enum { QS_WHAT_TOTAL = 0, QS_WHAT_COLLISION = 1 };
@@ -1140,6 +1150,58 @@ static void workspace_at_tau(ws_t *w, const double *y) {
   }
 }
 
+/* perturb2_rsa_variables (perturbations2.c:9773-10164) for rsa2_MD with
+   compute_quadsources_derivatives = no (input2.c defaults), and its use at the
+   end of perturb2_einstein (:8777-8809): the photon and neutrino monopoles and
+   dipoles from the RSA solution, the photon collision dipole from the RSA dipole.
+   The m = 1 dipoles are zero (:10094-10098, a documented limitation). */
+static void rsa_variables(ws_t *w, const double *y) {
+  cfg_t *c = w->c;
+  const double *fo1 = w->fo1, *fo2 = w->fo2;
+  double k = w->k, Hc = w->Hc, kappa_dot = w->kappa_dot;
+  double *k1_m = w->k1_m, *k2_m = w->k2_m;
+  /* perturb2_fluid_variables (:9108-9338) */
+  double vpot_g_1 = fo1[SONG2_FO_V_G], vpot_g_2 = fo2[SONG2_FO_V_G];
+  double delta_g_1 = fo1[SONG2_FO_DELTA_G], delta_g_2 = fo2[SONG2_FO_DELTA_G];
+  double v_dot_v_g = -w->k1_dot_k2 * vpot_g_1 * vpot_g_2;
+  double vpot_ur_1 = fo1[SONG2_FO_V_UR], vpot_ur_2 = fo2[SONG2_FO_V_UR];
+  double delta_ur_1 = fo1[SONG2_FO_DELTA_UR], delta_ur_2 = fo2[SONG2_FO_DELTA_UR];
+  double v_dot_v_ur = -w->k1_dot_k2 * vpot_ur_1 * vpot_ur_2;
+  if (c->compute_m[0]) {
+    double psi = w->psi;
+    double quadL_I_10 = -(dI_qs2(1, 0) - dI_qc2(1, 0));
+    double delta_g_rsa = -4 * psi + quadL_I_10 / k;
+    w->I_00 = delta_g_rsa + 8 * v_dot_v_g / 3;
+    double quadL_N_10 = -dN_qs2(1, 0);
+    double delta_ur_rsa = -4 * psi + quadL_N_10 / k;
+    w->N_00 = delta_ur_rsa + 8 * v_dot_v_ur / 3;
+  }
+  for (int im = 0; im <= c->index_m_max[1]; ++im) {
+    int m = c->m[im];
+    double I_1m_rsa = 0, N_1m_rsa = 0;
+    if (m == 0) {
+      double phi_prime = w->phi_prime;
+      double psi_prime_quad = w->qs[w->iq_psi_prime] - 2 * Hc * w->qs[w->iq_psi];
+      double psi_prime = phi_prime + psi_prime_quad;
+      double u_g_1 = -k1_m[1] * vpot_g_1, u_g_2 = -k2_m[1] * vpot_g_2;
+      double u_g_rsa = 3 / k * (phi_prime + psi_prime);
+      double quadL_I_00 = -(dI_qs2(0, 0) - dI_qc2(0, 0));
+      double u_delta_g = u_g_1 * delta_g_2 + u_g_2 * delta_g_1;
+      u_g_rsa += -u_delta_g - 3 / (4 * k) * quadL_I_00;
+      I_1m_rsa = 4 * (u_g_rsa + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
+      double u_ur_1 = -k1_m[1] * vpot_ur_1, u_ur_2 = -k2_m[1] * vpot_ur_2;
+      double u_ur_rsa = 3 / k * (phi_prime + psi_prime);
+      double quadL_N_00 = -dN_qs2(0, 0);
+      double u_delta_ur = u_ur_1 * delta_ur_2 + u_ur_2 * delta_ur_1;
+      u_ur_rsa += -u_delta_ur - 3 / (4 * k) * quadL_N_00;
+      N_1m_rsa = 4 * (u_ur_rsa + delta_ur_1 * u_ur_2 + delta_ur_2 * u_ur_1);
+    }
+    w->I_1m[m] = I_1m_rsa;
+    w->C_1m[m] = kappa_dot * (FOUR_THIRDS * b(1, 1, m) - I_1m_rsa);
+    w->N_1m[m] = N_1m_rsa;
+  }
+}
+
 static void einstein(ws_t *w, const double *y) {
   cfg_t *c = w->c;
   double rho_monopole = 0, rho_quadrupole = 0, rho_quadrupole_m1 = 0, rho_quadrupole_m2 = 0, rho_dipole = 0;
@@ -1179,6 +1241,7 @@ static void einstein(ws_t *w, const double *y) {
   if (c->compute_m[2])
     w->gamma_m2_prime_prime = -2 * Hc * y[PV->idx_gamma_p] - k_sq * y[PV->idx_gamma] - 2 / 5. * a_sq * rho_quadrupole_m2 +
                               w->qs[w->iq_gamma_m2_prime_prime];
+  if (PV->rsa) rsa_variables(w, y);
 }
 
 static double compute_psi_prime(ws_t *w, const double *y, const double *dy) {
@@ -1245,7 +1308,7 @@ static void prepare_tau_table(ws_t *w, double tau) {
   int nq = w->qs2_size;
   const double *r0 = w->qtab + (size_t)(i - w->qt_j0) * 2 * nq, *r1 = r0 + 2 * nq;
   for (int q = 0; q < nq; ++q) w->qs[q] = a * r0[q] + b * r1[q] + ca * r0[nq + q] + cb * r1[nq + q];
-  if (w->pv.tca) {
+  if (w->pv.tca || w->pv.rsa) {
     first_order_at_tau(w, tau);
     quadratic_sources(w, QS_WHAT_COLLISION);
   } else {
@@ -1498,18 +1561,26 @@ static void jacobian(ws_t *w, double tau) {
 
 /* ======================================================= vector layout */
 
-static void vector_layout(ws_t *w, int tca) {
+/* approximation: 0 none, 1 tight coupling, 2 radiation streaming */
+static void vector_layout(ws_t *w, int approx) {
   cfg_t *c = w->c;
   const song2_spec *s = c->s;
   pv_t *p = PV;
-  p->tca = tca;
+  p->tca = approx == 1;
+  p->rsa = approx == 2;
   p->use_closure_g = p->use_closure_pol_g = p->use_closure_ur = 1;
   p->l_max_g = s->l_max_g;
   p->l_max_pol_g = s->has_polarization2 ? s->l_max_pol_g : -1;
   p->l_max_ur = s->l_max_ur;
-  if (tca) {
+  if (p->tca) {
     p->l_max_g = 0; p->use_closure_g = 0;
     p->l_max_pol_g = -1; p->use_closure_pol_g = 0;
+  }
+  if (p->rsa) {
+    /* perturbations2.c:6778-6796: no massless hierarchies; their start indices
+       all fall on the baryon block, as in the reference */
+    p->l_max_g = p->l_max_pol_g = p->l_max_ur = -1;
+    p->use_closure_g = p->use_closure_pol_g = p->use_closure_ur = 0;
   }
   if (!s->has_polarization2) p->use_closure_pol_g = 0;
   p->n_max_b = p->l_max_b = p->n_max_cdm = p->l_max_cdm = 1;
@@ -2183,6 +2254,13 @@ static int ndf15(ws_t *w, double t0, double t1, double *y, const double *tout, i
 
 /* ======================================================= per-triplet solve */
 
+/* RSA trigger (perturbations2.c:5309-5321) */
+static int rsa_is_on(ws_t *w, double tau) {
+  const song2_spec *s = w->c->s;
+  if (s->radiation_streaming_approximation == SONG2_RSA_NONE || w->c->first_order_mode) return 0;
+  return (tau * w->k > s->radiation_streaming_trigger_tau_over_tau_k) && (tau > w->c->t->tau_free_streaming);
+}
+
 static int tca_is_on(ws_t *w, double tau) {
   const song2_spec *s = w->c->s;
   if (!s->tight_coupling) return 0;
@@ -2204,31 +2282,62 @@ static int solve_triplet(ws_t *w, const double *tout, int nout, output_fn out, d
   double tau_ini;
   if (o_start_time(s, c->t, kmax, tout[0], &tau_ini, err)) return SONG2_E_CONFIG;
   double tau_end = tout[nout - 1];
-  /* approximation intervals: TCA on at the start, switched off once */
-  double lim[3];
-  int nint = 1, tca0 = tca_is_on(w, tau_ini);
-  lim[0] = tau_ini;
-  if (tca0 && tca_is_on(w, tau_end)) {
-    lim[1] = tau_end;
-  } else if (tca0) {
-    double lo = tau_ini, hi = tau_end;
-    while ((hi - lo) / lo > s->tol_tau_approx) {
-      double mid = 0.5 * (lo + hi);
-      if (tca_is_on(w, mid)) lo = mid; else hi = mid;
+  /* approximation intervals (perturb2_find_approximation_switches,
+     perturbations2.c:4854-5209): TCA from the start until it switches off, then
+     the full system, then the RSA once it switches on */
+  int tca0 = tca_is_on(w, tau_ini);
+  double t_tca = tau_ini;
+  if (tca0) {
+    if (tca_is_on(w, tau_end)) t_tca = tau_end;
+    else {
+      double lo = tau_ini, hi = tau_end;
+      while ((hi - lo) / lo > s->tol_tau_approx) {
+        double mid = 0.5 * (lo + hi);
+        if (tca_is_on(w, mid)) lo = mid; else hi = mid;
+      }
+      t_tca = 0.5 * (lo + hi);
     }
-    lim[1] = 0.5 * (lo + hi);
-    lim[2] = tau_end;
-    nint = 2;
-  } else {
-    lim[1] = tau_end;
   }
+  double t_rsa = tau_end;
+  if (t_tca < tau_end && rsa_is_on(w, tau_end)) {
+    if (rsa_is_on(w, t_tca)) t_rsa = t_tca;
+    else {
+      double lo = t_tca, hi = tau_end;
+      while ((hi - lo) / lo > s->tol_tau_approx) {
+        double mid = 0.5 * (lo + hi);
+        if (rsa_is_on(w, mid)) hi = mid; else lo = mid;
+      }
+      t_rsa = 0.5 * (lo + hi);
+    }
+  }
+  double lim[4];
+  int ap[3], nint = 0;
+  lim[0] = tau_ini;
+  if (tca0) { ap[nint] = 1; lim[++nint] = t_tca; }
+  if (lim[nint] < t_rsa) { ap[nint] = 0; lim[++nint] = t_rsa; }
+  if (t_rsa < tau_end) { ap[nint] = 2; lim[++nint] = tau_end; }
   build_qs_table(w, tau_ini, tau_end);
   int jout = 0;
   for (int iv = 0; iv < nint; ++iv) {
-    int tca = (iv == 0) ? tca0 : 0;
     if (iv == 0) {
-      vector_layout(w, tca);
+      vector_layout(w, ap[0]);
       initial_conditions(w, lim[0], ybuf);
+    } else if (ap[iv] == 2) {
+      /* RSA on: the massless hierarchies are dropped, matter and metric carry
+         over (perturbations2.c:7105-7300) */
+      pv_t old = w->pv;
+      double *yold = w->ytmp;
+      memcpy(yold, ybuf, sizeof(double) * old.n);
+      vector_layout(w, 2);
+      pv_t *p = PV;
+      memset(ybuf, 0, sizeof(double) * p->n);
+      for (int i = 0; i < nlm_hier_b(c); ++i) {
+        ybuf[p->idx_b + i] = yold[old.idx_b + i];
+        ybuf[p->idx_cdm + i] = yold[old.idx_cdm + i];
+      }
+      if (c->compute_m[0]) { ybuf[p->idx_phi] = yold[old.idx_phi]; ybuf[p->idx_phi_p] = yold[old.idx_phi_p]; }
+      if (c->compute_m[1]) ybuf[p->idx_omega] = yold[old.idx_omega];
+      if (c->compute_m[2]) { ybuf[p->idx_gamma] = yold[old.idx_gamma]; ybuf[p->idx_gamma_p] = yold[old.idx_gamma_p]; }
     } else {
       /* TCA -> full remap (perturbations2.c:7233-7285) */
       pv_t old = w->pv;

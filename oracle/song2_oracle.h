@@ -53,8 +53,9 @@ double song2_oracle_coupling(int kind, int l, int m1, int m);
    (l, m, l1, m1, l2) (perturbations2.c:1380-1490), from the same 3j symbols. */
 double song2_oracle_delta_tilde_coupling(int field, int l, int m, int l1, int m1, int l2);
 
-/* Right-hand side of one triplet at (tau, y) for tests: layout of the full
-   (no approximation) vector unless tca != 0.  Returns n or -1. */
+/* Right-hand side of one triplet at (tau, y) for tests, in the vector layout of
+   tca = 0 (no approximation), 1 (tight coupling) or 2 (radiation streaming).
+   Returns n or -1. */
 int song2_oracle_rhs(const song2_spec *spec, const song2_tables *tab, int index_k1, int index_k2,
                      int index_k3, int tca, double tau, const double *y, double *dy, char *err);
 

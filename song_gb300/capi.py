@@ -23,6 +23,10 @@ SONG2_OK, SONG2_E_MAXSTEPS, SONG2_E_HMIN, SONG2_E_NAN, SONG2_E_NEWTON, SONG2_E_S
 SONG2_IC_AD, SONG2_IC_AD_FIRST_ORDER, SONG2_IC_ZERO = range(3)
 # precision
 SONG2_PREC_FP64, SONG2_PREC_MIXED = 0, 1
+# radiation-streaming approximation
+SONG2_RSA_NONE, SONG2_RSA_MD = 0, 1
+# tau_c/tau at which photons free-stream (radiation_streaming_trigger_tau_c_over_tau_song)
+RSA_TRIGGER_TAU_C_OVER_TAU = 10.0
 
 # background columns
 (BG_LN_A, BG_LN_HC, BG_HC_PRIME_TAU2, BG_LN_RHO_G, BG_LN_RHO_B, BG_LN_RHO_CDM, BG_LN_RHO_UR,
@@ -73,6 +77,8 @@ class Spec(C.Structure):
         ("use_delta_tilde_in_los", C.c_int),
         ("l_max_los_quadratic_t", C.c_int), ("l_max_los_quadratic_p", C.c_int),
         ("rescale_cmb_sources", C.c_int),
+        ("radiation_streaming_approximation", C.c_int),
+        ("radiation_streaming_trigger_tau_over_tau_k", C.c_double),
     ]
 
 
@@ -85,6 +91,7 @@ class Tables(C.Structure):
         ("fo_lntau0", C.c_double), ("fo_dlntau", C.c_double),
         ("fo_l_max", C.c_int), ("fo_size", C.c_int),
         ("fo", C.POINTER(C.c_double)), ("fo_dd", C.POINTER(C.c_double)),
+        ("tau_free_streaming", C.c_double),
     ]
 
 
@@ -126,6 +133,7 @@ SIGNATURES = {
     "song2_coupling_d_plus": (_D, [_I, _I, _I]),
     "song2_coupling_d_zero": (_D, [_I, _I, _I]),
     "song2_delta_tilde_coupling": (_D, [_I, _I, _I, _I, _I, _I]),
+    "song2_free_streaming_time": (_D, [C.POINTER(Tables), _D]),
     "song2_k_grid": (_I, [_I, _D, _D, _I, _PD]),
     "song2_k3_grids": (_I, [_PD, _I, _I, _I, _PI, _PD, C.c_char_p]),
     "song2_tau_grid": (_I, [_I, _D, _D, _I, _PD]),

@@ -139,6 +139,21 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
     s.mq_max = std::max(s.mq_max, Q);
   }
   s.rescale = sp->rescale_cmb_sources && !first_order_mode;
+  /* radiation-streaming approximation (perturbations2.c:5309-5321; rsa2_MD only) */
+  if (sp->radiation_streaming_approximation != SONG2_RSA_NONE && !first_order_mode) {
+    if (sp->radiation_streaming_approximation != SONG2_RSA_MD) {
+      snprintf(err, SONG2_ERRLEN, "radiation_streaming_approximation %d: only none (0) and MD (1) are built",
+               sp->radiation_streaming_approximation);
+      return 1;
+    }
+    if (!(tab && tab->tau_free_streaming > 0) || !(sp->radiation_streaming_trigger_tau_over_tau_k > 0)) {
+      snprintf(err, SONG2_ERRLEN, "the RSA needs tables.tau_free_streaming > 0 and a positive k tau trigger");
+      return 1;
+    }
+    s.rsa = 1;
+    s.rsa_k = sp->radiation_streaming_trigger_tau_over_tau_k;
+    s.tau_fs = tab->tau_free_streaming;
+  }
   for (int l = 0; l < S2_LMAXP; ++l) {
     s.index_m_max[l] = -1;
     for (int i = 0; i < s.m_size; ++i)

@@ -54,8 +54,10 @@ struct Tri {
   double k1, k2, k, k_sq, cosk1k2, cosk1k, cosk2k, k1_dot_k2;
   double k1_m[3], k2_m[3], k1_ten_k2[5], k1_ten_k1[5], k2_ten_k2[5];
   double mfac[SONG2_MAX_M + 3];    /* rot(l,-m) = (-1)^m rot(l,m) mfac[m]: sin(theta_k1)^2m if rescaled, else 1 */
-  double tau_ini, tau_switch, tau_end;
-  int i1, i2, i3, pair, item, tca0, nint, k3_size;
+  double tau_ini, tau_end;
+  double ivb[4];                   /* interval limits */
+  int ivk[3];                      /* approximation of each interval (AP_*) */
+  int i1, i2, i3, pair, item, nint, k3_size;
   int64_t pair_off;
 };
 
@@ -138,6 +140,9 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
    G lanes of a warp (G = 1, 2, 4, ... 32), the 32/G teams of a warp interleaved in
    global slabs so that the same element of every team is one coalesced access. */
 enum { MODE_BLOCK = 0, MODE_WARP = 1, MODE_TEAM = 2 };
+/* approximation of an integration interval (Shared::tca, the `tca` arguments):
+   none, tight coupling, radiation streaming */
+enum { AP_NONE = 0, AP_TCA = 1, AP_RSA = 2 };
 
 /* per-team array: element i at p[i] (the team owns the array) or p[i * T] (T teams
    interleaved) */
@@ -381,7 +386,7 @@ struct YUnit {
 };
 
 template <class Y, class C> __device__ inline double getI(const C &c, int tca, const Y &y, int l, int m) {
-  if (l < 0 || m < 0 || m > l || l > c.s.l_max_g || (tca && l >= 1)) return 0.0;
+  if (l < 0 || m < 0 || m > l || l > c.s.l_max_g || (tca && l >= 1) || tca == AP_RSA) return 0.0;
   return y(c.idx_I[c.LM(l, m)]);
 }
 template <class Y, class C> __device__ inline double getE(const C &c, int tca, const Y &y, int l, int m) {
@@ -947,13 +952,15 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, co
   if (m == 1) w.omega_m1_prime = 0;
   if (m == 2) w.gamma_m2_pp = 0;
   if (!s.compute_m[m]) return;
+  const int rsa = tca == AP_RSA;
+  auto gN = [&](int l_, int m_) { return rsa ? 0.0 : getN(c, y, l_, m_); };
   if (m == 0) {
     w.I_00 = getI(c, tca, y, 0, 0);
-    w.N_00 = getN(c, y, 0, 0);
+    w.N_00 = gN(0, 0);
   }
   if (m <= 1) {
     w.I_1m[m] = getI(c, tca, y, 1, m);
-    w.N_1m[m] = getN(c, y, 1, m);
+    w.N_1m[m] = gN(1, m);
     w.C_1m[m] = kd * (FOUR_THIRDS * getb(c, y, 1, m) - getI(c, tca, y, 1, m));
   }
   w.I_2m[m] = getI(c, tca, y, 2, m);
@@ -966,7 +973,7 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, co
   }
   w.b_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_b;
   w.cdm_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_cdm;
-  if (tca) {
+  if (tca == AP_TCA) {
     /* perturb2_tca_variables (perturbations2.c:9374-9738) */
     double tau_c = 1.0 / kd;
     double vpot_g_1 = lin ? 0.0 : fo1[SONG2_FO_V_G], vpot_g_2 = lin ? 0.0 : fo2[SONG2_FO_V_G];
@@ -1045,7 +1052,7 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, co
   /* perturb2_einstein (perturbations2.c:8484-8814), Newtonian gauge, phi_eq = huang */
   double a_sq = bg.a_sq, k_sq = t.k_sq;
   if (m == 0) {
-    double rho_quadrupole = bg.rho_g * w.I_2m[0] + bg.rho_b * w.b_22m[0] + bg.rho_cdm * w.cdm_22m[0] + bg.rho_ur * getN(c, y, 2, 0);
+    double rho_quadrupole = bg.rho_g * w.I_2m[0] + bg.rho_b * w.b_22m[0] + bg.rho_cdm * w.cdm_22m[0] + bg.rho_ur * gN(2, 0);
     double rho_mono_b = bg.rho_b * getb(c, y, 0, 0), rho_mono_c = bg.rho_cdm * getc(c, y, 0, 0);
     double phi = y(s.idx_phi);
     w.psi = phi - 3 / 5. * (a_sq / k_sq) * rho_quadrupole + (lin ? 0.0 : qs[s.iq_psi]);
@@ -1053,12 +1060,50 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, co
     w.phi_pp = k_sq / 3 * (w.psi - 2 * phi) - Hc * (3 * w.phi_prime) - 2 * w.psi * (Hc * Hc + bg.Hc_prime) -
                a_sq / 2 * (rho_mono_b + rho_mono_c) + (lin ? 0.0 : qs[s.iq_phi_prime_prime]);
   } else if (m == 1) {
-    double rq1 = bg.rho_g * w.I_2m[1] + bg.rho_b * w.b_22m[1] + bg.rho_cdm * w.cdm_22m[1] + bg.rho_ur * getN(c, y, 2, 1);
+    double rq1 = bg.rho_g * w.I_2m[1] + bg.rho_b * w.b_22m[1] + bg.rho_cdm * w.cdm_22m[1] + bg.rho_ur * gN(2, 1);
     w.omega_m1_prime = -2 * Hc * y(s.idx_omega) + 2 * SQRT_3 / (5. * k) * a_sq * rq1 + (lin ? 0.0 : qs[s.iq_omega_m1_prime]);
   } else {
-    double rq2 = bg.rho_g * w.I_2m[2] + bg.rho_b * w.b_22m[2] + bg.rho_cdm * w.cdm_22m[2] + bg.rho_ur * getN(c, y, 2, 2);
+    double rq2 = bg.rho_g * w.I_2m[2] + bg.rho_b * w.b_22m[2] + bg.rho_cdm * w.cdm_22m[2] + bg.rho_ur * gN(2, 2);
     w.gamma_m2_pp = -2 * Hc * y(s.idx_gammap) - k_sq * y(s.idx_gamma) - 2 / 5. * a_sq * rq2 +
                     (lin ? 0.0 : qs[s.iq_gamma_m2_prime_prime]);
+  }
+  if (rsa && m <= 1) {
+    /* perturb2_rsa_variables (perturbations2.c:9773-10164), rsa2_MD without the
+       quadratic-source derivative terms (compute_quadsources_derivatives = no),
+       applied after the Einstein equations as perturbations2.c:8777-8809 does:
+       the photon and neutrino monopoles and dipoles, and the photon collision
+       dipole of the baryon equation.  The m = 1 dipoles are zero (:10094-10098). */
+    double I1 = 0.0, N1 = 0.0;
+    double vpot_g_1 = lin ? 0.0 : fo1[SONG2_FO_V_G], vpot_g_2 = lin ? 0.0 : fo2[SONG2_FO_V_G];
+    double delta_g_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_G], delta_g_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_G];
+    double vpot_ur_1 = lin ? 0.0 : fo1[SONG2_FO_V_UR], vpot_ur_2 = lin ? 0.0 : fo2[SONG2_FO_V_UR];
+    double delta_ur_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_UR], delta_ur_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_UR];
+    if (m == 0) {
+      double v_dot_v_g = -t.k1_dot_k2 * vpot_g_1 * vpot_g_2, v_dot_v_ur = -t.k1_dot_k2 * vpot_ur_1 * vpot_ur_2;
+      int lm00 = c.LM(0, 0), lm10 = c.LM(1, 0);
+      double qsI00 = lin ? 0.0 : qs[s.iq_g + lm00], qcI00 = lin ? 0.0 : qc[s.iq_g + lm00];
+      double qsI10 = lin ? 0.0 : qs[s.iq_g + lm10], qcI10 = lin ? 0.0 : qc[s.iq_g + lm10];
+      double qsN00 = lin ? 0.0 : qs[s.iq_ur + lm00], qsN10 = lin ? 0.0 : qs[s.iq_ur + lm10];
+      double quadL_I_10 = -(qsI10 - qcI10), quadL_N_10 = -qsN10;
+      double delta_g_rsa = -4 * w.psi + quadL_I_10 / k;
+      w.I_00 = delta_g_rsa + 8 * v_dot_v_g / 3;
+      double delta_ur_rsa = -4 * w.psi + quadL_N_10 / k;
+      w.N_00 = delta_ur_rsa + 8 * v_dot_v_ur / 3;
+      double psi_prime_quad = lin ? 0.0 : qs[s.iq_psi_prime] - 2 * Hc * qs[s.iq_psi];
+      double psi_prime = w.phi_prime + psi_prime_quad;
+      double u_g_1 = -t.k1_m[1] * vpot_g_1, u_g_2 = -t.k2_m[1] * vpot_g_2;
+      double u_ur_1 = -t.k1_m[1] * vpot_ur_1, u_ur_2 = -t.k2_m[1] * vpot_ur_2;
+      double quadL_I_00 = -(qsI00 - qcI00), quadL_N_00 = -qsN00;
+      double u_g = 3 / k * (w.phi_prime + psi_prime);
+      u_g += -(u_g_1 * delta_g_2 + u_g_2 * delta_g_1) - 3 / (4 * k) * quadL_I_00;
+      I1 = 4 * (u_g + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
+      double u_ur = 3 / k * (w.phi_prime + psi_prime);
+      u_ur += -(u_ur_1 * delta_ur_2 + u_ur_2 * delta_ur_1) - 3 / (4 * k) * quadL_N_00;
+      N1 = 4 * (u_ur + delta_ur_1 * u_ur_2 + delta_ur_2 * u_ur_1);
+    }
+    w.I_1m[m] = I1;
+    w.C_1m[m] = kd * (FOUR_THIRDS * getb(c, y, 1, m) - I1);
+    w.N_1m[m] = N1;
   }
 }
 
@@ -1092,6 +1137,7 @@ __device__ double row_h(const C &c, int tca, int i, const Y &y, const WS &w, int
   double gp = s.compute_m[2] ? y(s.idx_gammap) : 0.0;
   int use_qs = !lin && s.has_qs;
   double d = 0.0;
+  if (tca == AP_RSA && sp <= SP_N) return 0.0;
   switch (sp) {
   case SP_I: {
     if (tca && l >= 1) return 0.0;
@@ -1210,7 +1256,7 @@ __device__ double psi_prime_of(const C &c, int tca, const Y &y, const WS &w, int
   const BgV &bg = c.sh->bg;
   double k = t.k, kd = bg.kappa_dot, Hc = bg.Hc;
   int use_qs = !lin && s.has_qs;
-  if (tca)
+  if (tca == AP_TCA)
     dI20 = 2 / 3. * k * w.I_1m_tca1[0] - kd * (w.I_2m_tca1[0] - w.Pi_tca1[0]) + (use_qs ? c.qs[s.iq_g + c.LM(2, 0)] : 0.0);
   double rqp = bg.rho_g * dI20 + bg.rho_ur * dN20;
   if (!lin) {
@@ -1227,8 +1273,11 @@ __device__ double psi_prime_of(const C &c, int tca, const Y &y, const WS &w, int
 template <class Y, class C>
 __device__ double row(const C &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
   if (c.eq_sp[i] != SP_PHIP) return row_h(c, tca, i, y, w, lin, tau);
-  double dI20 = tca ? 0.0 : row_h(c, tca, c.idx_I[c.LM(2, 0)], y, w, lin, tau);
-  double dN20 = row_h(c, tca, c.idx_N[c.LM(2, 0)], y, w, lin, tau);
+  /* in RSA the reference's dI(2,0) and dN(2,0) index the photon and neutrino
+     blocks, which are empty then, at lm(2,0) = the size of the baryon block: both
+     read the CDM density row (perturbations2.c:6853-6891, 10253, 10304) */
+  double dI20 = tca == AP_TCA ? 0.0 : row_h(c, tca, tca == AP_RSA ? c.s.idx_c000 : c.idx_I[c.LM(2, 0)], y, w, lin, tau);
+  double dN20 = row_h(c, tca, tca == AP_RSA ? c.s.idx_c000 : c.idx_N[c.LM(2, 0)], y, w, lin, tau);
   return w.phi_pp - c.sh->bg.Hc * psi_prime_of(c, tca, y, w, lin, dI20, dN20);
 }
 
@@ -1597,7 +1646,8 @@ __device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) 
     double psi_prime = 0.0;
     if (s.compute_m[0]) {
       int tca = c.sh->tca;
-      double dI20 = tca ? 0.0 : dy[c.idx_I[c.LM(2, 0)]], dN20 = dy[c.idx_N[c.LM(2, 0)]];
+      double dI20 = tca == AP_TCA ? 0.0 : dy[tca == AP_RSA ? c.s.idx_c000 : c.idx_I[c.LM(2, 0)]];
+      double dN20 = dy[tca == AP_RSA ? c.s.idx_c000 : c.idx_N[c.LM(2, 0)]];
       psi_prime = psi_prime_of(c, tca, yv, c.sh->ws, 0, dI20, dN20);
     }
     c.sh->psi_prime = psi_prime;
@@ -1877,18 +1927,41 @@ template <class C> __device__ int intervals(const C &c) {
     bg_hk(c, tau, h, kk);
     return s.tca_on && ((1.0 / kk) / (1.0 / h) < s.tca_h) && ((1.0 / kk) * kmax < s.tca_k);
   };
-  t.tca0 = tca_on(t.tau_ini);
-  t.nint = 1;
-  t.tau_switch = t.tau_end;
-  if (t.tca0 && !tca_on(t.tau_end)) {
-    double lo = t.tau_ini, hi = t.tau_end;
-    for (int it = 0; it < 200 && (hi - lo) / lo > s.tol_tau; ++it) {
-      double mid = 0.5 * (lo + hi);
-      if (tca_on(mid)) lo = mid; else hi = mid;
+  /* RSA trigger (perturbations2.c:5309-5321): k tau above the trigger, after free streaming */
+  auto rsa_on = [&](double tau) {
+    return s.rsa && tau * t.k > s.rsa_k && tau > s.tau_fs;
+  };
+  int tca0 = tca_on(t.tau_ini);
+  double t_tca = t.tau_ini;
+  if (tca0) {
+    if (tca_on(t.tau_end)) t_tca = t.tau_end;
+    else {
+      double lo = t.tau_ini, hi = t.tau_end;
+      for (int it = 0; it < 200 && (hi - lo) / lo > s.tol_tau; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (tca_on(mid)) lo = mid; else hi = mid;
+      }
+      t_tca = 0.5 * (lo + hi);
     }
-    t.tau_switch = 0.5 * (lo + hi);
-    t.nint = 2;
   }
+  double t_rsa = t.tau_end;
+  if (t_tca < t.tau_end && rsa_on(t.tau_end)) {
+    if (rsa_on(t_tca)) t_rsa = t_tca;
+    else {
+      double lo = t_tca, hi = t.tau_end;
+      for (int it = 0; it < 200 && (hi - lo) / lo > s.tol_tau; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (rsa_on(mid)) hi = mid; else lo = mid;
+      }
+      t_rsa = 0.5 * (lo + hi);
+    }
+  }
+  int n = 0;
+  t.ivb[0] = t.tau_ini;
+  if (tca0) { t.ivk[n] = AP_TCA; t.ivb[++n] = t_tca; }
+  if (t.ivb[n] < t_rsa) { t.ivk[n] = AP_NONE; t.ivb[++n] = t_rsa; }
+  if (t_rsa < t.tau_end) { t.ivk[n] = AP_RSA; t.ivb[++n] = t.tau_end; }
+  t.nint = n;
   return 0;
 }
 
@@ -2331,13 +2404,17 @@ template <typename T, class C> __device__ int solve_triplet(const C &c, song2_tr
   build_qs_table(c);
   int jout = 0;
   for (int iv = 0; iv < t.nint; ++iv) {
-    double ta = iv == 0 ? t.tau_ini : t.tau_switch;
-    double tb = (iv == 0 && t.nint == 2) ? t.tau_switch : t.tau_end;
+    double ta = t.ivb[iv], tb = t.ivb[iv + 1];
     if (iv == 0) {
-      if (tid == 0) c.sh->tca = t.tca0;
+      if (tid == 0) c.sh->tca = t.ivk[0];
       c.sync();
       prepare(c, ta, 1);
       if (tid == 0) initial_conditions(c, ta);
+      c.sync();
+    } else if (t.ivk[iv] == AP_RSA) {
+      /* switching the RSA on drops the massless hierarchies: nothing to remap
+         (perturbations2.c:7295-7300); their entries stay in y, unevolved */
+      if (tid == 0) c.sh->tca = AP_RSA;
       c.sync();
     } else {
       /* TCA -> full remap (perturbations2.c:7233-7285): the frozen moments take the

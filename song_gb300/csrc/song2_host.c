@@ -138,6 +138,7 @@ void song2_spec_defaults(song2_spec *s) {
   s->l_max_g = s->l_max_pol_g = s->l_max_ur = 8;         /* input2.c:2257-2259 */
   s->l_max_los_t = s->l_max_los_p = 2;                   /* input2.c:2265-2266 */
   s->l_max_los_quadratic_t = s->l_max_los_quadratic_p = 2;
+  s->radiation_streaming_trigger_tau_over_tau_k = 90;    /* input2.c:2140 */
   s->m_size = 1; s->m[0] = 0;                            /* input2.c:2268-2270 */
   s->has_polarization2 = 1;
   s->has_quadratic_sources = 1;
@@ -491,6 +492,23 @@ double song2_delta_tilde_coupling(int field, int l, int m, int l1, int m1, int l
   double v = threej(l1, l2, l, 0, F, -F) * threej(l1, l2, l, m1, m2, -m);
   if (v == 0.0) return 0.0;
   return pre * sign * ((m & 1) ? -1.0 : 1.0) * (2.0 * l + 1) * v;
+}
+
+double song2_free_streaming_time(const song2_tables *tab, double trigger) {
+  /* g(x) = ln(tau_c/tau) - ln(trigger) = -ln kappa'(tau) - x - ln(trigger), x = ln tau:
+     negative until photon decoupling, positive after (no reionisation) */
+  double lo = tab->bg_lntau0, hi = tab->bg_lntau0 + (tab->bg_size - 1) * tab->bg_dlntau;
+  double lt = log(trigger);
+#define G(x) (-spline_eval_uniform(tab->bg_size, SONG2_BG_SIZE, tab->bg_lntau0, tab->bg_dlntau, tab->bg, tab->bg_dd, \
+                                   SONG2_BG_LN_KAPPA_DOT, (x)) - (x) - lt)
+  if (G(hi) <= 0) return tab->tau0;
+  if (G(lo) > 0) return exp(lo);
+  for (int it = 0; it < 200 && hi - lo > 1e-13; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (G(mid) > 0) hi = mid; else lo = mid;
+  }
+#undef G
+  return exp(0.5 * (lo + hi));
 }
 
 /* ------------------------------------------------------------ start time */

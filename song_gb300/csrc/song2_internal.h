@@ -35,6 +35,8 @@ struct DevSpec {
   int los_sw, los_isw, los_exp_pot;
   int dtilde, dt_qt, dt_qp, dt_Q, dt_L;  /* delta-tilde sources: l1, l2 cuts of T and E/B, table extents */
   int rescale;                     /* rotation coefficients / sin(theta_k1)^m */
+  int rsa;                         /* radiation-streaming approximation on */
+  double rsa_k, tau_fs;            /* its k tau trigger and the start of free streaming */
   double rtol, threshold;
   int max_steps;
   double start_h, start_k, tol_tau;

@@ -117,6 +117,7 @@ class Problem:
         t.bg_dlntau = dlt.value
         t.bg = capi.dptr(self.bg)
         t.bg_dd = capi.dptr(self.bg_dd)
+        t.tau_free_streaming = lib.song2_free_streaming_time(C.byref(t), capi.RSA_TRIGGER_TAU_C_OVER_TAU)
         self.tables = t
         self.fo_l_max = max(l_max, s.l_max_los_t, s.l_max_los_p) + 1
         self.classes = None

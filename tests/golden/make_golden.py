@@ -30,6 +30,8 @@ CASES = {
     # delta-tilde LOS sources with rescaled rotation coefficients (the reference's
     # intrinsic-bispectrum settings, ini/intrinsic.ini)
     "tiny_dtilde_rescaled": dict(sources="TEB", l_max=5, use_delta_tilde_in_los=1, rescale_cmb_sources=1),
+    # radiation-streaming approximation (the reference's default, rsa2_MD)
+    "tiny_rsa": dict(sources="TEB", l_max=5, radiation_streaming_approximation=1),
 }
 
 if __name__ == "__main__":

@@ -250,6 +250,23 @@ def test_delta_tilde_and_rescaling_match_oracle(lib, olib, kw):
     """delta-tilde LOS sources (couplings up to |m1|, |m2| = the quadratic cut, past
     the modes the hierarchy evolves) and rescaled rotation coefficients agree with
     the oracle in both precisions."""
+    _check_options_against_oracle(lib, kw)
+
+
+@pytest.mark.parametrize("kw", [
+    dict(sources="TEB", l_max=5, radiation_streaming_approximation=1),
+    dict(sources="TEB", l_max=5, radiation_streaming_approximation=1, use_delta_tilde_in_los=1, rescale_cmb_sources=1),
+    dict(m=(0,), sources="T", has_polarization2=0, radiation_streaming_approximation=1),
+    dict(tight_coupling=0, sources="TEBD", l_max=5, radiation_streaming_approximation=1),
+])
+def test_rsa_matches_oracle(lib, olib, kw):
+    """The radiation-streaming interval (massless hierarchies frozen, RSA monopoles
+    and dipoles) agrees with the oracle's reduced vector in both precisions and in
+    the warp and lane-team kernels."""
+    _check_options_against_oracle(lib, kw)
+
+
+def _check_options_against_oracle(lib, kw):
     p = problem(**kw)
     p.set_first_order(oracle.first_order(p, nthreads=8))
     ref, _ = oracle.evolve(p, nthreads=8)

@@ -112,11 +112,11 @@ def test_gpu_uneven_launch_groups_match_single_launch(lib, uneven, monkeypatch):
 
 
 @pytest.mark.gpu
-def test_gpu_uneven_delta_tilde_rescaled_matches_oracle(lib):
-    """Hierarchy classes with delta-tilde sources and rescaled rotation coefficients
-    (an m_max = 0 class still needs the rotation coefficients up to m = 2)."""
+def test_gpu_uneven_with_los_options_and_rsa_matches_oracle(lib):
+    """Hierarchy classes with delta-tilde sources, rescaled rotation coefficients and
+    the RSA (an m_max = 0 class still needs the rotation coefficients up to m = 2)."""
     from helpers import floored_errors, gpu_run
-    p = problem(**UNEVEN, use_delta_tilde_in_los=1, rescale_cmb_sources=1)
+    p = problem(**UNEVEN, use_delta_tilde_in_los=1, rescale_cmb_sources=1, radiation_streaming_approximation=1)
     p.set_uneven(**CLASSES)
     p.set_first_order(oracle.first_order(p, nthreads=8))
     ref, _ = oracle.evolve(p, nthreads=8)
