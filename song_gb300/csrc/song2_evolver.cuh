@@ -932,6 +932,52 @@ template <class C> __device__ void build_qs_table(const C &c) {
 
 /* ------------------------------------------------------------------ workspace */
 
+/* perturb2_rsa_variables (perturbations2.c:9773-10164), rsa2_MD without the
+   quadratic-source derivative terms (compute_quadsources_derivatives = no),
+   applied after the Einstein equations as perturbations2.c:8777-8809 does: the
+   photon and neutrino monopoles and dipoles, and the photon collision dipole of
+   the baryon equation; the m = 1 dipoles are zero (:10094-10098).  Kept out of
+   line: the RSA interval is the rare path, and inlining it into every
+   right-hand-side evaluation costs registers in the NDF loop. */
+template <class Y, class C> __device__ __noinline__ void rsa_moments(const C &c, const Y &y, int lin, WS &w, int m) {
+  const DevSpec &s = c.s;
+  const Tri &t = c.sh->tri;
+  const BgV &bg = c.sh->bg;
+  auto qs = c.qs, qc = c.qc, fo1 = c.fo1, fo2 = c.fo2;
+  double k = t.k, Hc = bg.Hc, kd = bg.kappa_dot;
+  double I1 = 0.0, N1 = 0.0;
+  double vpot_g_1 = lin ? 0.0 : fo1[SONG2_FO_V_G], vpot_g_2 = lin ? 0.0 : fo2[SONG2_FO_V_G];
+  double delta_g_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_G], delta_g_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_G];
+  double vpot_ur_1 = lin ? 0.0 : fo1[SONG2_FO_V_UR], vpot_ur_2 = lin ? 0.0 : fo2[SONG2_FO_V_UR];
+  double delta_ur_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_UR], delta_ur_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_UR];
+  if (m == 0) {
+    double v_dot_v_g = -t.k1_dot_k2 * vpot_g_1 * vpot_g_2, v_dot_v_ur = -t.k1_dot_k2 * vpot_ur_1 * vpot_ur_2;
+    int lm00 = c.LM(0, 0), lm10 = c.LM(1, 0);
+    double qsI00 = lin ? 0.0 : qs[s.iq_g + lm00], qcI00 = lin ? 0.0 : qc[s.iq_g + lm00];
+    double qsI10 = lin ? 0.0 : qs[s.iq_g + lm10], qcI10 = lin ? 0.0 : qc[s.iq_g + lm10];
+    double qsN00 = lin ? 0.0 : qs[s.iq_ur + lm00], qsN10 = lin ? 0.0 : qs[s.iq_ur + lm10];
+    double quadL_I_10 = -(qsI10 - qcI10), quadL_N_10 = -qsN10;
+    double delta_g_rsa = -4 * w.psi + quadL_I_10 / k;
+    w.I_00 = delta_g_rsa + 8 * v_dot_v_g / 3;
+    double delta_ur_rsa = -4 * w.psi + quadL_N_10 / k;
+    w.N_00 = delta_ur_rsa + 8 * v_dot_v_ur / 3;
+    double psi_prime_quad = lin ? 0.0 : qs[s.iq_psi_prime] - 2 * Hc * qs[s.iq_psi];
+    double psi_prime = w.phi_prime + psi_prime_quad;
+    double u_g_1 = -t.k1_m[1] * vpot_g_1, u_g_2 = -t.k2_m[1] * vpot_g_2;
+    double u_ur_1 = -t.k1_m[1] * vpot_ur_1, u_ur_2 = -t.k2_m[1] * vpot_ur_2;
+    double quadL_I_00 = -(qsI00 - qcI00), quadL_N_00 = -qsN00;
+    double u_g = 3 / k * (w.phi_prime + psi_prime);
+    u_g += -(u_g_1 * delta_g_2 + u_g_2 * delta_g_1) - 3 / (4 * k) * quadL_I_00;
+    I1 = 4 * (u_g + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
+    double u_ur = 3 / k * (w.phi_prime + psi_prime);
+    u_ur += -(u_ur_1 * delta_ur_2 + u_ur_2 * delta_ur_1) - 3 / (4 * k) * quadL_N_00;
+    N1 = 4 * (u_ur + delta_ur_1 * u_ur_2 + delta_ur_2 * u_ur_1);
+  }
+  w.I_1m[m] = I1;
+  w.C_1m[m] = kd * (FOUR_THIRDS * getb(c, y, 1, m) - I1);
+  w.N_1m[m] = N1;
+}
+
 /* The workspace of perturb2_workspace_at_tau / perturb2_tca_variables /
    perturb2_einstein for one azimuthal number m in {0, 1, 2}: every field of WS
    belongs to exactly one m, so the three parts can be evaluated side by side. */
@@ -1067,44 +1113,7 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, co
     w.gamma_m2_pp = -2 * Hc * y(s.idx_gammap) - k_sq * y(s.idx_gamma) - 2 / 5. * a_sq * rq2 +
                     (lin ? 0.0 : qs[s.iq_gamma_m2_prime_prime]);
   }
-  if (rsa && m <= 1) {
-    /* perturb2_rsa_variables (perturbations2.c:9773-10164), rsa2_MD without the
-       quadratic-source derivative terms (compute_quadsources_derivatives = no),
-       applied after the Einstein equations as perturbations2.c:8777-8809 does:
-       the photon and neutrino monopoles and dipoles, and the photon collision
-       dipole of the baryon equation.  The m = 1 dipoles are zero (:10094-10098). */
-    double I1 = 0.0, N1 = 0.0;
-    double vpot_g_1 = lin ? 0.0 : fo1[SONG2_FO_V_G], vpot_g_2 = lin ? 0.0 : fo2[SONG2_FO_V_G];
-    double delta_g_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_G], delta_g_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_G];
-    double vpot_ur_1 = lin ? 0.0 : fo1[SONG2_FO_V_UR], vpot_ur_2 = lin ? 0.0 : fo2[SONG2_FO_V_UR];
-    double delta_ur_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_UR], delta_ur_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_UR];
-    if (m == 0) {
-      double v_dot_v_g = -t.k1_dot_k2 * vpot_g_1 * vpot_g_2, v_dot_v_ur = -t.k1_dot_k2 * vpot_ur_1 * vpot_ur_2;
-      int lm00 = c.LM(0, 0), lm10 = c.LM(1, 0);
-      double qsI00 = lin ? 0.0 : qs[s.iq_g + lm00], qcI00 = lin ? 0.0 : qc[s.iq_g + lm00];
-      double qsI10 = lin ? 0.0 : qs[s.iq_g + lm10], qcI10 = lin ? 0.0 : qc[s.iq_g + lm10];
-      double qsN00 = lin ? 0.0 : qs[s.iq_ur + lm00], qsN10 = lin ? 0.0 : qs[s.iq_ur + lm10];
-      double quadL_I_10 = -(qsI10 - qcI10), quadL_N_10 = -qsN10;
-      double delta_g_rsa = -4 * w.psi + quadL_I_10 / k;
-      w.I_00 = delta_g_rsa + 8 * v_dot_v_g / 3;
-      double delta_ur_rsa = -4 * w.psi + quadL_N_10 / k;
-      w.N_00 = delta_ur_rsa + 8 * v_dot_v_ur / 3;
-      double psi_prime_quad = lin ? 0.0 : qs[s.iq_psi_prime] - 2 * Hc * qs[s.iq_psi];
-      double psi_prime = w.phi_prime + psi_prime_quad;
-      double u_g_1 = -t.k1_m[1] * vpot_g_1, u_g_2 = -t.k2_m[1] * vpot_g_2;
-      double u_ur_1 = -t.k1_m[1] * vpot_ur_1, u_ur_2 = -t.k2_m[1] * vpot_ur_2;
-      double quadL_I_00 = -(qsI00 - qcI00), quadL_N_00 = -qsN00;
-      double u_g = 3 / k * (w.phi_prime + psi_prime);
-      u_g += -(u_g_1 * delta_g_2 + u_g_2 * delta_g_1) - 3 / (4 * k) * quadL_I_00;
-      I1 = 4 * (u_g + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
-      double u_ur = 3 / k * (w.phi_prime + psi_prime);
-      u_ur += -(u_ur_1 * delta_ur_2 + u_ur_2 * delta_ur_1) - 3 / (4 * k) * quadL_N_00;
-      N1 = 4 * (u_ur + delta_ur_1 * u_ur_2 + delta_ur_2 * u_ur_1);
-    }
-    w.I_1m[m] = I1;
-    w.C_1m[m] = kd * (FOUR_THIRDS * getb(c, y, 1, m) - I1);
-    w.N_1m[m] = N1;
-  }
+  if (rsa && m <= 1) rsa_moments(c, y, lin, w, m);
 }
 
 /* the whole workspace, one thread */
@@ -1316,7 +1325,7 @@ template <typename T, class C, class A> __device__ void newton_rhs(const C &c, i
 
 /* Exact Jacobian of the affine system at tau (prepare(tau) must have run):
    J[:, j] = A e_j, one thread per column; stored per m block in global scratch. */
-template <typename T, class C> __device__ void jacobian(const C &c, int tca, double tau) {
+template <typename T, class C> __device__ __forceinline__ void jacobian(const C &c, int tca, double tau) {
   const DevSpec &s = c.s;
   auto J0 = c.template jacv<T>();
   for (int b = c.rank; b < s.nblk; b += c.size) c.sh->kl[b] = c.sh->ku[b] = 0;
@@ -1606,7 +1615,7 @@ template <class V> __device__ double fo_coll_E(const V &fo, const DevSpec &s, in
 /* delta-tilde part of the (l,m) source of field 0 (T), 1 (E) or 2 (B):
    -2 kappa' (delta*delta/2 + delta*collision), perturbations2.c:12339-12398 (T),
    12509-12561 (E), 12658-12710 (B). */
-template <class C> __device__ double delta_tilde_source(const C &c, int field, int l, int m, double kappa_dot) {
+template <class C> __device__ __noinline__ double delta_tilde_source(const C &c, int field, int l, int m, double kappa_dot) {
   const DevSpec &s = c.s;
   auto fo1 = c.fo1, fo2 = c.fo2;
   int Q = field == 0 ? s.dt_qt : s.dt_qp;
@@ -2116,7 +2125,7 @@ template <class C> __device__ inline double tout_at(const C &c, int j) {
 }
 
 template <typename T, class C>
-__device__ int ndf15(const C &c, double t0, double t1, int &jout, int include_t0, song2_triplet_stats &st) {
+__device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout, int include_t0, song2_triplet_stats &st) {
   const DevSpec &s = c.s;
   int n = s.n, tid = c.rank, nt = c.size;
   int nout = s.mode_first_order ? s.fo_tau_size : s.tau_size;
@@ -2393,7 +2402,7 @@ __device__ int ndf15(const C &c, double t0, double t1, int &jout, int include_t0
 
 /* ------------------------------------------------------------------ one triplet */
 
-template <typename T, class C> __device__ int solve_triplet(const C &c, song2_triplet_stats &st) {
+template <typename T, class C> __device__ __forceinline__ int solve_triplet(const C &c, song2_triplet_stats &st) {
   const DevSpec &s = c.s;
   int tid = c.rank;
   if (geometry(c)) return SONG2_E_CONFIG;
@@ -2462,7 +2471,7 @@ template <class C> __device__ void begin_item(const C &c, int item) {
   c.sync();
 }
 
-template <typename T, class C> __device__ void run_item(const C &c, int item) {
+template <typename T, class C> __device__ __forceinline__ void run_item(const C &c, int item) {
   begin_item(c, item);
   song2_triplet_stats st;
   st.status = 0; st.n_steps = 0; st.n_rejected = 0; st.n_rhs = 0; st.n_jac = 0; st.n_lu = 0; st.n_newton_fail = 0;

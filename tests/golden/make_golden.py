@@ -34,6 +34,13 @@ CASES = {
     "tiny_rsa": dict(sources="TEB", l_max=5, radiation_streaming_approximation=1),
 }
 
+# Bound of a GPU run against a fixture, in units of rtol.  With the RSA the T
+# monopole source is a difference of large terms (kappa' I_00 + 4 kappa' psi with
+# I_00 = -4 psi + ..., and the ISW term through psi'), so the oracle's own
+# rtol-level error is ~10 rtol there (rtol 1e-4 against 1e-6: 1.1e-3); the GPU is
+# held to three times that.
+GPU_TOL_RTOL = {"tiny_rsa": 30}
+
 if __name__ == "__main__":
     # with names as arguments only those fixtures are (re)made
     for name, kw in CASES.items():

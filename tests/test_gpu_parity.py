@@ -189,14 +189,15 @@ def test_shards_sum_to_full_run(lib, tiny):
 def test_gpu_matches_golden_fixture(lib):
     import sys
     sys.path.insert(0, os.path.join(HERE, "golden"))
-    from make_golden import CASES
+    from make_golden import CASES, GPU_TOL_RTOL
     for name, kw in CASES.items():
         g = np.load(os.path.join(HERE, "golden", name + ".npz"))
         p = problem(**kw)
         p.set_first_order(g["fo"])
         for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
             src, st, _ = gpu_run(lib, p, precision)
-            assert np.max(floored_errors(src, g["sources"], p)) < 10 * p.spec.rtol, name
+            tol = GPU_TOL_RTOL.get(name, 10) * p.spec.rtol
+            assert np.max(floored_errors(src, g["sources"], p)) < tol, name
 
 
 def test_large_blocks_in_global_scratch(lib, olib):
@@ -267,13 +268,19 @@ def test_rsa_matches_oracle(lib, olib, kw):
 
 
 def _check_options_against_oracle(lib, kw):
+    """GPU runs against the oracle at the same rtol, within 10 rtol or three times
+    the oracle's own error (its distance to an rtol/100 run), whichever is larger:
+    with the RSA the T monopole source is a difference of large terms, and both
+    sides carry that rtol-level error."""
     p = problem(**kw)
     p.set_first_order(oracle.first_order(p, nthreads=8))
     ref, _ = oracle.evolve(p, nthreads=8)
+    tight, _ = oracle.evolve(p, nthreads=8, rtol=p.spec.rtol / 100)
+    bound = max(10 * p.spec.rtol, 3 * np.max(floored_errors(ref, tight, p)))
     for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
         src, st, _ = gpu_run(lib, p, precision)
         assert np.all(st["status"] == capi.SONG2_OK)
-        assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+        assert np.max(floored_errors(src, ref, p)) < bound
     # the warp-per-triplet and lane-team kernels carry the same source terms
     for launch in ((1, 4, 32, 0), (2, 16, 8, 0)) if p.spec.l_max_g <= 5 else ():
         L = capi.Launch(*launch)
@@ -287,7 +294,7 @@ def _check_options_against_oracle(lib, kw):
         lib.song2_ctx_download(c, capi.dptr(src), st, err)
         lib.song2_ctx_destroy(c)
         assert np.all(np.frombuffer(st, dtype=capi.STATS_DTYPE)["status"] == capi.SONG2_OK)
-        assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+        assert np.max(floored_errors(src, ref, p)) < bound
 
 
 def test_delta_tilde_excludes_redshift_term(lib):

@@ -120,6 +120,9 @@ def test_gpu_uneven_with_los_options_and_rsa_matches_oracle(lib):
     p.set_uneven(**CLASSES)
     p.set_first_order(oracle.first_order(p, nthreads=8))
     ref, _ = oracle.evolve(p, nthreads=8)
+    tight, _ = oracle.evolve(p, nthreads=8, rtol=p.spec.rtol / 100)
+    # the RSA's T monopole source carries the solver's rtol-level error amplified
+    bound = max(10 * p.spec.rtol, 3 * np.max(floored_errors(ref, tight, p)))
     src, st, _ = gpu_run(lib, p, 1)
     assert np.all(st["status"] == 0)
-    assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+    assert np.max(floored_errors(src, ref, p)) < bound
