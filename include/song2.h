@@ -149,7 +149,10 @@ typedef struct {
   int rescale_cmb_sources;
   /* radiation-streaming approximation (radiation_streaming_approximation_song,
      input2.c:824-829; reference default rsa2_MD with triggers 90 and 10,
-     input2.c:2139-2141): SONG2_RSA_NONE or SONG2_RSA_MD.  After photon
+     input2.c:2139-2141; the precision files shipped in pre/ use MD_with_reio
+     with triggers 45 and 5): SONG2_RSA_NONE, SONG2_RSA_MD or
+     SONG2_RSA_MD_WITH_REIO, which adds the first-order collision terms in tau_c
+     (perturbations2.c:9929-9953, 10064-10084).  After photon
      decoupling (tau > tables.tau_free_streaming) and once k tau exceeds
      radiation_streaming_trigger_tau_over_tau_k, the photon and neutrino
      hierarchies are no longer evolved and their monopoles and dipoles follow the
@@ -159,7 +162,7 @@ typedef struct {
   double radiation_streaming_trigger_tau_over_tau_k;
 } song2_spec;
 
-enum { SONG2_RSA_NONE = 0, SONG2_RSA_MD = 1 };
+enum { SONG2_RSA_NONE = 0, SONG2_RSA_MD = 1, SONG2_RSA_MD_WITH_REIO = 2 };
 
 /* Background/thermo and first-order interpolation tables, owned by the caller
    (the replacement for CLASS's pba/pth/ppt->quadsources). */

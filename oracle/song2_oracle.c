@@ -265,8 +265,9 @@ static int cfg_init(cfg_t *c, const song2_spec *s, const song2_tables *t, int fo
   c->tp2_size = tp;
   c->n_triplets = o_n_triplets(s);
   if (s->radiation_streaming_approximation != SONG2_RSA_NONE && !c->first_order_mode) {
-    if (s->radiation_streaming_approximation != SONG2_RSA_MD) {
-      snprintf(err, SONG2_ERRLEN, "radiation_streaming_approximation: only none and MD");
+    if (s->radiation_streaming_approximation != SONG2_RSA_MD &&
+        s->radiation_streaming_approximation != SONG2_RSA_MD_WITH_REIO) {
+      snprintf(err, SONG2_ERRLEN, "radiation_streaming_approximation: none, MD or MD_with_reio");
       return 1;
     }
     if (!(t->tau_free_streaming > 0) || !(s->radiation_streaming_trigger_tau_over_tau_k > 0)) {
@@ -315,6 +316,16 @@ static double spl(int n, int ncol, double x0, double dx, const double *y, const 
   return a * y0[q] + b * y0[ncol + q] + ((a * a * a - a) * d0[q] + (b * b * b - b) * d0[ncol + q]) * (dx * dx) / 6.0;
 }
 
+/* d/dx of the same spline */
+static double spl_dx(int n, int ncol, double x0, double dx, const double *y, const double *dd, int q, double x) {
+  double u = (x - x0) / dx;
+  int i = (int)floor(u);
+  if (i < 0) i = 0;
+  if (i > n - 2) i = n - 2;
+  double b = u - i, a = 1.0 - b;
+  const double *y0 = y + (size_t)i * ncol, *d0 = dd + (size_t)i * ncol;
+  return (y0[ncol + q] - y0[q]) / dx + ((1 - 3 * a * a) * d0[q] + (3 * b * b - 1) * d0[ncol + q]) * dx / 6.0;
+}
 
 /* ======================================================= layout helpers
    (restated here so that the oracle links against nothing of the product) */
@@ -392,7 +403,7 @@ typedef struct {
   /* full (no approximation) hierarchy sizes, used by the quadratic sources */
   int l_max_g, l_max_pol_g, l_max_ur;
   /* background at tau */
-  double a, a_sq, Hc, Hc_prime, rho_g, rho_b, rho_cdm, rho_ur, kappa_dot, exp_m_kappa, g, r;
+  double tau, a, a_sq, Hc, Hc_prime, rho_g, rho_b, rho_cdm, rho_ur, kappa_dot, exp_m_kappa, g, r;
   double *fo1, *fo2;
   int linear_only;
   int qs2_size, iq_g, iq_E, iq_B, iq_ur, iq_b, iq_cdm;
@@ -712,6 +723,7 @@ static int geometrical_corner(ws_t *w, int index_k1, int index_k2, int index_k3,
 static void background_at_tau(ws_t *w, double tau) {
   const song2_tables *t = w->c->t;
   double x = log(tau);
+  w->tau = tau;
 #define BG(q) spl(t->bg_size, SONG2_BG_SIZE, t->bg_lntau0, t->bg_dlntau, t->bg, t->bg_dd, (q), x)
   w->a = exp(BG(SONG2_BG_LN_A));
   w->a_sq = w->a * w->a;
@@ -1150,15 +1162,28 @@ static void workspace_at_tau(ws_t *w, const double *y) {
   }
 }
 
-/* perturb2_rsa_variables (perturbations2.c:9773-10164) for rsa2_MD with
-   compute_quadsources_derivatives = no (input2.c defaults), and its use at the
+/* perturb2_rsa_variables (perturbations2.c:9773-10164) for rsa2_MD and
+   rsa2_MD_with_reio with compute_quadsources_derivatives = no (input2.c
+   defaults), and its use at the
    end of perturb2_einstein (:8777-8809): the photon and neutrino monopoles and
    dipoles from the RSA solution, the photon collision dipole from the RSA dipole.
    The m = 1 dipoles are zero (:10094-10098, a documented limitation). */
-static void rsa_variables(ws_t *w, const double *y) {
+static void rsa_variables(ws_t *w, const double *y, double tau) {
   cfg_t *c = w->c;
+  const song2_tables *tab = c->t;
   const double *fo1 = w->fo1, *fo2 = w->fo2;
   double k = w->k, Hc = w->Hc, kappa_dot = w->kappa_dot;
+  /* rsa2_MD_with_reio (:9929-9953, 10064-10084): tau_c = 1/kappa' and its
+     derivative tau_c' = -kappa'' tau_c^2, kappa'' from the background spline of
+     ln kappa' (CLASS's pth->ddkappa is the derivative of its own table) */
+  int reio = c->s->radiation_streaming_approximation == SONG2_RSA_MD_WITH_REIO;
+  double tau_c = 1 / kappa_dot, tau_c_dot = 0;
+  if (reio) {
+    double dlnkd = spl_dx(tab->bg_size, SONG2_BG_SIZE, tab->bg_lntau0, tab->bg_dlntau, tab->bg, tab->bg_dd,
+                          SONG2_BG_LN_KAPPA_DOT, log(tau));
+    double kappa_dot_dot = kappa_dot * dlnkd / tau;
+    tau_c_dot = -kappa_dot_dot * tau_c * tau_c;
+  }
   double *k1_m = w->k1_m, *k2_m = w->k2_m;
   /* perturb2_fluid_variables (:9108-9338) */
   double vpot_g_1 = fo1[SONG2_FO_V_G], vpot_g_2 = fo2[SONG2_FO_V_G];
@@ -1171,6 +1196,11 @@ static void rsa_variables(ws_t *w, const double *y) {
     double psi = w->psi;
     double quadL_I_10 = -(dI_qs2(1, 0) - dI_qc2(1, 0));
     double delta_g_rsa = -4 * psi + quadL_I_10 / k;
+    if (reio) {
+      delta_g_rsa += -FOUR_THIRDS * b(1, 1, 0) / (k * tau_c);
+      double quadC_I_10 = dI_qc2(1, 0) / kappa_dot;
+      delta_g_rsa += -quadC_I_10 / (k * tau_c);
+    }
     w->I_00 = delta_g_rsa + 8 * v_dot_v_g / 3;
     double quadL_N_10 = -dN_qs2(1, 0);
     double delta_ur_rsa = -4 * psi + quadL_N_10 / k;
@@ -1188,6 +1218,11 @@ static void rsa_variables(ws_t *w, const double *y) {
       double quadL_I_00 = -(dI_qs2(0, 0) - dI_qc2(0, 0));
       double u_delta_g = u_g_1 * delta_g_2 + u_g_2 * delta_g_1;
       u_g_rsa += -u_delta_g - 3 / (4 * k) * quadL_I_00;
+      if (reio) {
+        double quadC_I_00 = dI_qc2(0, 0) / kappa_dot, quadC_I_10 = dI_qc2(1, 0) / kappa_dot;
+        u_g_rsa += 1 / (k * tau_c) * (-(3 * Hc + tau_c_dot / tau_c) / k * b(1, 1, m) + 9 * w->psi +
+                                      3 / 4. * quadC_I_00 - 3 * tau_c_dot * quadC_I_10 / (4 * k * tau_c));
+      }
       I_1m_rsa = 4 * (u_g_rsa + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
       double u_ur_1 = -k1_m[1] * vpot_ur_1, u_ur_2 = -k2_m[1] * vpot_ur_2;
       double u_ur_rsa = 3 / k * (phi_prime + psi_prime);
@@ -1241,7 +1276,7 @@ static void einstein(ws_t *w, const double *y) {
   if (c->compute_m[2])
     w->gamma_m2_prime_prime = -2 * Hc * y[PV->idx_gamma_p] - k_sq * y[PV->idx_gamma] - 2 / 5. * a_sq * rho_quadrupole_m2 +
                               w->qs[w->iq_gamma_m2_prime_prime];
-  if (PV->rsa) rsa_variables(w, y);
+  if (PV->rsa) rsa_variables(w, y, w->tau);
 }
 
 static double compute_psi_prime(ws_t *w, const double *y, const double *dy) {

@@ -24,7 +24,7 @@ SONG2_IC_AD, SONG2_IC_AD_FIRST_ORDER, SONG2_IC_ZERO = range(3)
 # precision
 SONG2_PREC_FP64, SONG2_PREC_MIXED = 0, 1
 # radiation-streaming approximation
-SONG2_RSA_NONE, SONG2_RSA_MD = 0, 1
+SONG2_RSA_NONE, SONG2_RSA_MD, SONG2_RSA_MD_WITH_REIO = 0, 1, 2
 # tau_c/tau at which photons free-stream (radiation_streaming_trigger_tau_c_over_tau_song)
 RSA_TRIGGER_TAU_C_OVER_TAU = 10.0
 

@@ -139,10 +139,11 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
     s.mq_max = std::max(s.mq_max, Q);
   }
   s.rescale = sp->rescale_cmb_sources && !first_order_mode;
-  /* radiation-streaming approximation (perturbations2.c:5309-5321; rsa2_MD only) */
+  /* radiation-streaming approximation (perturbations2.c:5309-5321) */
   if (sp->radiation_streaming_approximation != SONG2_RSA_NONE && !first_order_mode) {
-    if (sp->radiation_streaming_approximation != SONG2_RSA_MD) {
-      snprintf(err, SONG2_ERRLEN, "radiation_streaming_approximation %d: only none (0) and MD (1) are built",
+    if (sp->radiation_streaming_approximation != SONG2_RSA_MD &&
+        sp->radiation_streaming_approximation != SONG2_RSA_MD_WITH_REIO) {
+      snprintf(err, SONG2_ERRLEN, "radiation_streaming_approximation %d: none (0), MD (1) or MD_with_reio (2)",
                sp->radiation_streaming_approximation);
       return 1;
     }
@@ -150,7 +151,7 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
       snprintf(err, SONG2_ERRLEN, "the RSA needs tables.tau_free_streaming > 0 and a positive k tau trigger");
       return 1;
     }
-    s.rsa = 1;
+    s.rsa = sp->radiation_streaming_approximation;
     s.rsa_k = sp->radiation_streaming_trigger_tau_over_tau_k;
     s.tau_fs = tab->tau_free_streaming;
   }

@@ -424,6 +424,18 @@ __device__ inline double spl(const double *yv, const double *dd, int n, int ncol
          ((a * a * a - a) * __ldg(d0 + q) + (b * b * b - b) * __ldg(d0 + ncol + q)) * (dx * dx) / 6.0;
 }
 
+/* d/dx of the same spline */
+__device__ inline double spl_dx(const double *yv, const double *dd, int n, int ncol, double x0, double dx, int q,
+                                double x) {
+  double u = (x - x0) / dx;
+  int i = (int)floor(u);
+  i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+  double b = u - i, a = 1.0 - b;
+  const double *y0 = yv + (size_t)i * ncol, *d0 = dd + (size_t)i * ncol;
+  return (__ldg(y0 + ncol + q) - __ldg(y0 + q)) / dx +
+         ((1.0 - 3 * a * a) * __ldg(d0 + q) + (3 * b * b - 1.0) * __ldg(d0 + ncol + q)) * dx / 6.0;
+}
+
 template <class C> __device__ inline double bg_col(const C &c, int q, double tau) {
   return spl(c.p.bg, c.p.bg_dd, c.s.bg_size, SONG2_BG_SIZE, c.s.bg_lntau0, c.s.bg_dlntau, q, log(tau));
 }
@@ -946,6 +958,14 @@ template <class Y, class C> __device__ __noinline__ void rsa_moments(const C &c,
   auto qs = c.qs, qc = c.qc, fo1 = c.fo1, fo2 = c.fo2;
   double k = t.k, Hc = bg.Hc, kd = bg.kappa_dot;
   double I1 = 0.0, N1 = 0.0;
+  /* MD_with_reio: tau_c = 1/kappa', tau_c'/tau_c = -kappa''/kappa' = -(d ln kappa'/d ln tau)/tau */
+  const int reio = s.rsa == SONG2_RSA_MD_WITH_REIO;
+  double tau_c = 1.0 / kd, tcd_over_tc = 0.0;
+  if (reio) {
+    double x = c.sh->lntau;
+    tcd_over_tc = -spl_dx(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau,
+                          SONG2_BG_LN_KAPPA_DOT, x) / exp(x);
+  }
   double vpot_g_1 = lin ? 0.0 : fo1[SONG2_FO_V_G], vpot_g_2 = lin ? 0.0 : fo2[SONG2_FO_V_G];
   double delta_g_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_G], delta_g_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_G];
   double vpot_ur_1 = lin ? 0.0 : fo1[SONG2_FO_V_UR], vpot_ur_2 = lin ? 0.0 : fo2[SONG2_FO_V_UR];
@@ -958,6 +978,10 @@ template <class Y, class C> __device__ __noinline__ void rsa_moments(const C &c,
     double qsN00 = lin ? 0.0 : qs[s.iq_ur + lm00], qsN10 = lin ? 0.0 : qs[s.iq_ur + lm10];
     double quadL_I_10 = -(qsI10 - qcI10), quadL_N_10 = -qsN10;
     double delta_g_rsa = -4 * w.psi + quadL_I_10 / k;
+    if (reio) {
+      delta_g_rsa += -FOUR_THIRDS * getb(c, y, 1, 0) / (k * tau_c);
+      delta_g_rsa += -(qcI10 / kd) / (k * tau_c);
+    }
     w.I_00 = delta_g_rsa + 8 * v_dot_v_g / 3;
     double delta_ur_rsa = -4 * w.psi + quadL_N_10 / k;
     w.N_00 = delta_ur_rsa + 8 * v_dot_v_ur / 3;
@@ -968,6 +992,12 @@ template <class Y, class C> __device__ __noinline__ void rsa_moments(const C &c,
     double quadL_I_00 = -(qsI00 - qcI00), quadL_N_00 = -qsN00;
     double u_g = 3 / k * (w.phi_prime + psi_prime);
     u_g += -(u_g_1 * delta_g_2 + u_g_2 * delta_g_1) - 3 / (4 * k) * quadL_I_00;
+    if (reio) {
+      double quadC_I_00 = qcI00 / kd, quadC_I_10 = qcI10 / kd, tau_c_dot = tcd_over_tc * tau_c;
+      u_g += 1 / (k * tau_c) *
+             (-(3 * Hc + tcd_over_tc) / k * getb(c, y, 1, 0) + 9 * w.psi + 3 / 4. * quadC_I_00 -
+              3 * tau_c_dot * quadC_I_10 / (4 * k * tau_c));
+    }
     I1 = 4 * (u_g + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
     double u_ur = 3 / k * (w.phi_prime + psi_prime);
     u_ur += -(u_ur_1 * delta_ur_2 + u_ur_2 * delta_ur_1) - 3 / (4 * k) * quadL_N_00;

@@ -35,7 +35,7 @@ struct DevSpec {
   int los_sw, los_isw, los_exp_pot;
   int dtilde, dt_qt, dt_qp, dt_Q, dt_L;  /* delta-tilde sources: l1, l2 cuts of T and E/B, table extents */
   int rescale;                     /* rotation coefficients / sin(theta_k1)^m */
-  int rsa;                         /* radiation-streaming approximation on */
+  int rsa;                         /* radiation-streaming approximation: 0 off, 1 MD, 2 MD with reionisation */
   double rsa_k, tau_fs;            /* its k tau trigger and the start of free streaming */
   double rtol, threshold;
   int max_steps;

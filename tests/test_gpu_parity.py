@@ -259,6 +259,9 @@ def test_delta_tilde_and_rescaling_match_oracle(lib, olib, kw):
     dict(sources="TEB", l_max=5, radiation_streaming_approximation=1, use_delta_tilde_in_los=1, rescale_cmb_sources=1),
     dict(m=(0,), sources="T", has_polarization2=0, radiation_streaming_approximation=1),
     dict(tight_coupling=0, sources="TEBD", l_max=5, radiation_streaming_approximation=1),
+    # MD_with_reio with an early switch (free streaming from 300 Mpc, k tau > 10)
+    dict(sources="TEB", l_max=5, radiation_streaming_approximation=2, radiation_streaming_trigger_tau_over_tau_k=10,
+         rtol=1e-6, tau_free_streaming=300.0),
 ])
 def test_rsa_matches_oracle(lib, olib, kw):
     """The radiation-streaming interval (massless hierarchies frozen, RSA monopoles
@@ -272,7 +275,11 @@ def _check_options_against_oracle(lib, kw):
     the oracle's own error (its distance to an rtol/100 run), whichever is larger:
     with the RSA the T monopole source is a difference of large terms, and both
     sides carry that rtol-level error."""
+    kw = dict(kw)
+    tau_fs = kw.pop("tau_free_streaming", None)
     p = problem(**kw)
+    if tau_fs is not None:
+        p.tables.tau_free_streaming = tau_fs
     p.set_first_order(oracle.first_order(p, nthreads=8))
     ref, _ = oracle.evolve(p, nthreads=8)
     tight, _ = oracle.evolve(p, nthreads=8, rtol=p.spec.rtol / 100)

@@ -69,10 +69,20 @@ def test_rsa_switch_gating(rsa_problem):
     assert np.array_equal(full, same)
 
 
+def test_reio_terms_are_small_without_reionisation(rsa_problem):
+    """rsa2_MD_with_reio adds collision terms of order tau_c (perturbations2.c:9929-9953,
+    10064-10084); the synthetic cosmology has no reionisation, so once photons
+    free-stream they change the sources by far less than the integration error."""
+    p = rsa_problem
+    md, _ = _run(p, radiation_streaming_approximation=capi.SONG2_RSA_MD)
+    reio, _ = _run(p, radiation_streaming_approximation=capi.SONG2_RSA_MD_WITH_REIO)
+    assert 0 < np.max(floored_errors(reio, md, p)) < 1e-6
+
+
 def test_rsa_options_are_checked(rsa_problem):
     p = rsa_problem
-    with pytest.raises(RuntimeError, match="only none and MD"):
-        _run(p, radiation_streaming_approximation=2)
+    with pytest.raises(RuntimeError, match="none, MD or MD_with_reio"):
+        _run(p, radiation_streaming_approximation=3)
     t = p.tables
     old = t.tau_free_streaming
     t.tau_free_streaming = 0.0
