@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--k-size", type=int, default=None, help="override the k grid size (small profiling cases)")
     ap.add_argument("--k3-size", type=int, default=None, help="override the k3 grid size (small profiling cases)")
+    ap.add_argument("--rsa", type=int, default=0, choices=[0, 1, 2],
+                    help="radiation-streaming approximation of both arms: 0 none (default), 1 MD, 2 MD with reio")
     return ap.parse_args()
 
 
@@ -287,10 +289,13 @@ def main():
     if args.k3_size:
         overrides["k3_size"] = cfg["k3_size"] = args.k3_size
     cfg_name = cfg["name"] + ("" if not overrides else "_reduced")
+    if args.rsa:
+        overrides["radiation_streaming_approximation"] = args.rsa
+        cfg_name += "_rsa%d" % args.rsa
     config = {"workload": cfg_name, "triplets_per_gpu": None, "k_min": cfg["k_min"], "k_max": cfg["k_max"],
               "k_size": cfg["k_size"], "k3_size": cfg["k3_size"], "l_max": cfg["l_max"], "m": list(cfg["m"]),
               "rtol": cfg["rtol"], "tau_size": cfg["tau_size"], "sources": cfg["sources"],
-              "l2": "flushed between steps (256 MiB write)"}
+              "l2": "flushed between steps (256 MiB write)", "rsa": args.rsa}
 
     if args.impl == "reference":
         if rank != 0:
