@@ -82,7 +82,7 @@ struct Shared {
   int item;
   int lu_fail;
   int kl[S2_MAXBLK], ku[S2_MAXBLK];   /* band of each block's Jacobian */
-  int tca;
+  int ap;
 };
 
 /* Offsets (in bytes) of the dynamic shared-memory plan. */
@@ -140,7 +140,7 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
    G lanes of a warp (G = 1, 2, 4, ... 32), the 32/G teams of a warp interleaved in
    global slabs so that the same element of every team is one coalesced access. */
 enum { MODE_BLOCK = 0, MODE_WARP = 1, MODE_TEAM = 2 };
-/* approximation of an integration interval (Shared::tca, the `tca` arguments):
+/* approximation of an integration interval (Shared::ap, the `ap` arguments):
    none, tight coupling, radiation streaming */
 enum { AP_NONE = 0, AP_TCA = 1, AP_RSA = 2 };
 
@@ -385,16 +385,16 @@ struct YUnit {
   __device__ double operator()(int i) const { return (i >= 0 && i == j) ? 1.0 : 0.0; }
 };
 
-template <class Y, class C> __device__ inline double getI(const C &c, int tca, const Y &y, int l, int m) {
-  if (l < 0 || m < 0 || m > l || l > c.s.l_max_g || (tca && l >= 1) || tca == AP_RSA) return 0.0;
+template <class Y, class C> __device__ inline double getI(const C &c, int ap, const Y &y, int l, int m) {
+  if (l < 0 || m < 0 || m > l || l > c.s.l_max_g || (ap == AP_TCA && l >= 1) || ap == AP_RSA) return 0.0;
   return y(c.idx_I[c.LM(l, m)]);
 }
-template <class Y, class C> __device__ inline double getE(const C &c, int tca, const Y &y, int l, int m) {
-  if (!c.s.has_pol || tca || l < 2 || m < 0 || m > l || l > c.s.l_max_pol) return 0.0;
+template <class Y, class C> __device__ inline double getE(const C &c, int ap, const Y &y, int l, int m) {
+  if (!c.s.has_pol || ap || l < 2 || m < 0 || m > l || l > c.s.l_max_pol) return 0.0;
   return y(c.idx_E[c.LM(l, m)]);
 }
-template <class Y, class C> __device__ inline double getB(const C &c, int tca, const Y &y, int l, int m) {
-  if (!c.s.has_pol || tca || l < 2 || m <= 0 || m > l || l > c.s.l_max_pol) return 0.0;
+template <class Y, class C> __device__ inline double getB(const C &c, int ap, const Y &y, int l, int m) {
+  if (!c.s.has_pol || ap || l < 2 || m <= 0 || m > l || l > c.s.l_max_pol) return 0.0;
   return y(c.idx_B[c.LM(l, m)]);
 }
 template <class Y, class C> __device__ inline double getN(const C &c, const Y &y, int l, int m) {
@@ -826,7 +826,9 @@ template <class C> __device__ void prepare(const C &c, double tau, int with_sour
    perturbations2.c:14366-14688): background by spline, quadratic sources by
    cubic-spline interpolation of the triplet's table; in tight coupling also the
    first-order quantities and the direct collision terms.  Ends with a barrier. */
-template <class C> __device__ void prepare_table(const C &c, double tau, int tca) {
+template <class C> __device__ void prepare_table(const C &c, double tau, int ap) {
+  /* ap != AP_NONE (TCA or RSA): first-order values and collision terms computed
+     directly, as perturb2_tca_variables and perturb2_rsa_variables do */
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   int tid = c.rank, nt = c.size;
@@ -847,7 +849,7 @@ template <class C> __device__ void prepare_table(const C &c, double tau, int tca
     int nq = s.qs2_size;
     auto r0 = c.qtab + (i - j0) * 2 * nq, r1 = r0 + 2 * nq;
     for (int q = tid; q < nq; q += nt) c.qs[q] = a * r0[q] + b * r1[q] + ca * r0[nq + q] + cb * r1[nq + q];
-    if (tca) {
+    if (ap) {
       size_t stride = (size_t)s.fo_tau_size * s.nfo;
       for (int q = tid; q < 2 * s.nfo; q += nt) {
         int which = q >= s.nfo, qq = which ? q - s.nfo : q;
@@ -859,12 +861,12 @@ template <class C> __device__ void prepare_table(const C &c, double tau, int tca
   } else {
     for (int q = tid; q < s.qs2_size; q += nt) c.qs[q] = 0.0;
   }
-  if (!(use && tca))
+  if (!(use && ap))
     for (int q = tid; q < s.qs2_size; q += nt) c.qc[q] = 0.0;
   c.sync();
   if (tid == 0) bg_derive(c.bgraw, c.sh->bg);
   c.sync();
-  if (use && tca) {
+  if (use && ap) {
     const BgV &bg = c.sh->bg;
     for (int e = tid; e < s.n_qs_slots; e += nt) {
       int q = c.qs_slot[e];
@@ -1011,7 +1013,7 @@ template <class Y, class C> __device__ __noinline__ void rsa_moments(const C &c,
 /* The workspace of perturb2_workspace_at_tau / perturb2_tca_variables /
    perturb2_einstein for one azimuthal number m in {0, 1, 2}: every field of WS
    belongs to exactly one m, so the three parts can be evaluated side by side. */
-template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, const Y &y, int lin, WS &w, int m) {
+template <class Y, class C> __device__ void compute_ws_m(const C &c, int ap, const Y &y, int lin, WS &w, int m) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
@@ -1028,20 +1030,20 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, co
   if (m == 1) w.omega_m1_prime = 0;
   if (m == 2) w.gamma_m2_pp = 0;
   if (!s.compute_m[m]) return;
-  const int rsa = tca == AP_RSA;
+  const int rsa = ap == AP_RSA;
   auto gN = [&](int l_, int m_) { return rsa ? 0.0 : getN(c, y, l_, m_); };
   if (m == 0) {
-    w.I_00 = getI(c, tca, y, 0, 0);
+    w.I_00 = getI(c, ap, y, 0, 0);
     w.N_00 = gN(0, 0);
   }
   if (m <= 1) {
-    w.I_1m[m] = getI(c, tca, y, 1, m);
+    w.I_1m[m] = getI(c, ap, y, 1, m);
     w.N_1m[m] = gN(1, m);
-    w.C_1m[m] = kd * (FOUR_THIRDS * getb(c, y, 1, m) - getI(c, tca, y, 1, m));
+    w.C_1m[m] = kd * (FOUR_THIRDS * getb(c, y, 1, m) - getI(c, ap, y, 1, m));
   }
-  w.I_2m[m] = getI(c, tca, y, 2, m);
-  w.E_2m[m] = getE(c, tca, y, 2, m);
-  w.B_2m[m] = getB(c, tca, y, 2, m);
+  w.I_2m[m] = getI(c, ap, y, 2, m);
+  w.E_2m[m] = getE(c, ap, y, 2, m);
+  w.B_2m[m] = getB(c, ap, y, 2, m);
   double vv_b = lin ? 0.0 : qs[s.iq_vv_b], vv_cdm = lin ? 0.0 : qs[s.iq_vv_cdm];
   if (m == 0) {
     w.b_200 = -2 * t.k1_dot_k2 * vv_b;
@@ -1049,7 +1051,7 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, co
   }
   w.b_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_b;
   w.cdm_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_cdm;
-  if (tca == AP_TCA) {
+  if (ap == AP_TCA) {
     /* perturb2_tca_variables (perturbations2.c:9374-9738) */
     double tau_c = 1.0 / kd;
     double vpot_g_1 = lin ? 0.0 : fo1[SONG2_FO_V_G], vpot_g_2 = lin ? 0.0 : fo2[SONG2_FO_V_G];
@@ -1147,17 +1149,17 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int tca, co
 }
 
 /* the whole workspace, one thread */
-template <class Y, class C> __device__ void compute_ws(const C &c, int tca, const Y &y, int lin, WS &w) {
-  for (int m = 0; m < 3; ++m) compute_ws_m(c, tca, y, lin, w, m);
+template <class Y, class C> __device__ void compute_ws(const C &c, int ap, const Y &y, int lin, WS &w) {
+  for (int m = 0; m < 3; ++m) compute_ws_m(c, ap, y, lin, w, m);
 }
 
 /* the workspace into sh->ws, the three m parts on three threads of the team */
-template <class Y, class C> __device__ void compute_ws_team(const C &c, int tca, const Y &y) {
+template <class Y, class C> __device__ void compute_ws_team(const C &c, int ap, const Y &y) {
   if (c.size >= 96) {
     /* lane 0 of warps 0, 1, 2: the three parts run on different schedulers */
-    if ((c.rank & 31) == 0 && c.rank < 96) compute_ws_m(c, tca, y, 0, c.sh->ws, c.rank >> 5);
+    if ((c.rank & 31) == 0 && c.rank < 96) compute_ws_m(c, ap, y, 0, c.sh->ws, c.rank >> 5);
   } else {
-    for (int m = c.rank; m < 3; m += c.size) compute_ws_m(c, tca, y, 0, c.sh->ws, m);
+    for (int m = c.rank; m < 3; m += c.size) compute_ws_m(c, ap, y, 0, c.sh->ws, m);
   }
 }
 
@@ -1165,7 +1167,7 @@ template <class Y, class C> __device__ void compute_ws_team(const C &c, int tca,
 
 /* every row except phi' (which needs two other rows, see row() below) */
 template <class Y, class C>
-__device__ double row_h(const C &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
+__device__ double row_h(const C &c, int ap, int i, const Y &y, const WS &w, int lin, double tau) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
@@ -1176,14 +1178,14 @@ __device__ double row_h(const C &c, int tca, int i, const Y &y, const WS &w, int
   double gp = s.compute_m[2] ? y(s.idx_gammap) : 0.0;
   int use_qs = !lin && s.has_qs;
   double d = 0.0;
-  if (tca == AP_RSA && sp <= SP_N) return 0.0;
+  if (ap == AP_RSA && sp <= SP_N) return 0.0;
   switch (sp) {
   case SP_I: {
-    if (tca && l >= 1) return 0.0;
-    if (!tca && l == s.l_max_g) {
+    if (ap == AP_TCA && l >= 1) return 0.0;
+    if (ap == AP_NONE && l == s.l_max_g) {
       double c_pre = (m == 0 ? (2 * l + 1) / (2 * l - 1.) : sqrt((double)(l + m) / (l - m)) * (2 * l + 1) / (2 * l - 1.));
       double cc = (l + 1 + m) / (k * tau);
-      d = k * (c_pre * getI(c, tca, y, l - 1, m) - cc * getI(c, tca, y, l, m)) - kd * getI(c, tca, y, l, m);
+      d = k * (c_pre * getI(c, ap, y, l - 1, m) - cc * getI(c, ap, y, l, m)) - kd * getI(c, ap, y, l, m);
     } else if (l == 0) {
       d = -FOUR_THIRDS * (k * w.I_1m[0] / 4 + mc);
     } else if (l == 1) {
@@ -1192,44 +1194,44 @@ __device__ double row_h(const C &c, int tca, int i, const Y &y, const WS &w, int
       if (m == 1) d += -4 * omp;
     } else if (l == 2) {
       double Pi = 0.1 * (w.I_2m[m] - SQRT_6 * w.E_2m[m]);
-      d = k * (c.cmin(2, m, m) * w.I_1m[m] - c.cplu(2, m, m) * getI(c, tca, y, 3, m)) - kd * (w.I_2m[m] - Pi);
+      d = k * (c.cmin(2, m, m) * w.I_1m[m] - c.cplu(2, m, m) * getI(c, ap, y, 3, m)) - kd * (w.I_2m[m] - Pi);
       if (m == 2) d += 4 * gp;
     } else {
-      d = k * (c.cmin(l, m, m) * getI(c, tca, y, l - 1, m) - c.cplu(l, m, m) * getI(c, tca, y, l + 1, m)) -
-          kd * getI(c, tca, y, l, m);
+      d = k * (c.cmin(l, m, m) * getI(c, ap, y, l - 1, m) - c.cplu(l, m, m) * getI(c, ap, y, l + 1, m)) -
+          kd * getI(c, ap, y, l, m);
     }
     if (use_qs) d += c.qs[s.iq_g + c.LM(l, m)];
     return d;
   }
   case SP_E: {
-    if (tca) return 0.0;
+    if (ap != AP_NONE) return 0.0;
     if (l == s.l_max_pol) {
       double c_pre = sqrt(1 - ((double)m * m) / (l * l) * (l + 2) / (l - 2.)) * (2 * l + 1) / (2 * l - 1.);
       double cc = (l + 3) / (k * tau), cmix = (double)m / l;
-      d = k * (c_pre * getE(c, tca, y, l - 1, m) - cc * getE(c, tca, y, l, m) - cmix * getB(c, tca, y, l, m)) -
-          kd * getE(c, tca, y, l, m);
+      d = k * (c_pre * getE(c, ap, y, l - 1, m) - cc * getE(c, ap, y, l, m) - cmix * getB(c, ap, y, l, m)) -
+          kd * getE(c, ap, y, l, m);
     } else if (l == 2) {
       double Pi = 0.1 * (w.I_2m[m] - SQRT_6 * w.E_2m[m]);
-      d = k * (-c.dplu(2, m, m) * getE(c, tca, y, 3, m) - c.dzer(2, m, m) * w.B_2m[m]) - kd * (w.E_2m[m] + SQRT_6 * Pi);
+      d = k * (-c.dplu(2, m, m) * getE(c, ap, y, 3, m) - c.dzer(2, m, m) * w.B_2m[m]) - kd * (w.E_2m[m] + SQRT_6 * Pi);
     } else {
-      d = k * (c.dmin(l, m, m) * getE(c, tca, y, l - 1, m) - c.dplu(l, m, m) * getE(c, tca, y, l + 1, m) -
-               c.dzer(l, m, m) * getB(c, tca, y, l, m)) -
-          kd * getE(c, tca, y, l, m);
+      d = k * (c.dmin(l, m, m) * getE(c, ap, y, l - 1, m) - c.dplu(l, m, m) * getE(c, ap, y, l + 1, m) -
+               c.dzer(l, m, m) * getB(c, ap, y, l, m)) -
+          kd * getE(c, ap, y, l, m);
     }
     if (use_qs) d += c.qs[s.iq_E + c.LM(l, m)];
     return d;
   }
   case SP_B: {
-    if (tca) return 0.0;
+    if (ap != AP_NONE) return 0.0;
     if (l == s.l_max_pol) {
       double c_pre = sqrt(1 - ((double)m * m) / (l * l) * (l + 2) / (l - 2.)) * (2 * l + 1) / (2 * l - 1.);
       double cc = (l + 3) / (k * tau), cmix = (double)m / l;
-      d = k * (c_pre * getB(c, tca, y, l - 1, m) - cc * getB(c, tca, y, l, m) + cmix * getE(c, tca, y, l, m)) -
-          kd * getB(c, tca, y, l, m);
+      d = k * (c_pre * getB(c, ap, y, l - 1, m) - cc * getB(c, ap, y, l, m) + cmix * getE(c, ap, y, l, m)) -
+          kd * getB(c, ap, y, l, m);
     } else {
-      d = k * (c.dmin(l, m, m) * getB(c, tca, y, l - 1, m) - c.dplu(l, m, m) * getB(c, tca, y, l + 1, m) +
-               c.dzer(l, m, m) * getE(c, tca, y, l, m)) -
-          kd * getB(c, tca, y, l, m);
+      d = k * (c.dmin(l, m, m) * getB(c, ap, y, l - 1, m) - c.dplu(l, m, m) * getB(c, ap, y, l + 1, m) +
+               c.dzer(l, m, m) * getE(c, ap, y, l, m)) -
+          kd * getB(c, ap, y, l, m);
     }
     if (use_qs) d += c.qs[s.iq_B + c.LM(l, m)];
     return d;
@@ -1289,13 +1291,13 @@ __device__ double row_h(const C &c, int tca, int i, const Y &y, const WS &w, int
    (perturb2_compute_psi_prime, perturbations2.c:10188-10383); in tight coupling
    the photon quadrupole derivative is the TCA one. */
 template <class Y, class C>
-__device__ double psi_prime_of(const C &c, int tca, const Y &y, const WS &w, int lin, double dI20, double dN20) {
+__device__ double psi_prime_of(const C &c, int ap, const Y &y, const WS &w, int lin, double dI20, double dN20) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
   const BgV &bg = c.sh->bg;
   double k = t.k, kd = bg.kappa_dot, Hc = bg.Hc;
   int use_qs = !lin && s.has_qs;
-  if (tca == AP_TCA)
+  if (ap == AP_TCA)
     dI20 = 2 / 3. * k * w.I_1m_tca1[0] - kd * (w.I_2m_tca1[0] - w.Pi_tca1[0]) + (use_qs ? c.qs[s.iq_g + c.LM(2, 0)] : 0.0);
   double rqp = bg.rho_g * dI20 + bg.rho_ur * dN20;
   if (!lin) {
@@ -1310,25 +1312,25 @@ __device__ double psi_prime_of(const C &c, int tca, const Y &y, const WS &w, int
 /* Row i of dy = f(tau, y).  The phi' row is phi'' = (Einstein part) - Hc psi',
    where psi' needs the I_20 and N_20 rows. */
 template <class Y, class C>
-__device__ double row(const C &c, int tca, int i, const Y &y, const WS &w, int lin, double tau) {
-  if (c.eq_sp[i] != SP_PHIP) return row_h(c, tca, i, y, w, lin, tau);
+__device__ double row(const C &c, int ap, int i, const Y &y, const WS &w, int lin, double tau) {
+  if (c.eq_sp[i] != SP_PHIP) return row_h(c, ap, i, y, w, lin, tau);
   /* in RSA the reference's dI(2,0) and dN(2,0) index the photon and neutrino
      blocks, which are empty then, at lm(2,0) = the size of the baryon block: both
      read the CDM density row (perturbations2.c:6853-6891, 10253, 10304) */
-  double dI20 = tca == AP_TCA ? 0.0 : row_h(c, tca, tca == AP_RSA ? c.s.idx_c000 : c.idx_I[c.LM(2, 0)], y, w, lin, tau);
-  double dN20 = row_h(c, tca, tca == AP_RSA ? c.s.idx_c000 : c.idx_N[c.LM(2, 0)], y, w, lin, tau);
-  return w.phi_pp - c.sh->bg.Hc * psi_prime_of(c, tca, y, w, lin, dI20, dN20);
+  double dI20 = ap == AP_TCA ? 0.0 : row_h(c, ap, ap == AP_RSA ? c.s.idx_c000 : c.idx_I[c.LM(2, 0)], y, w, lin, tau);
+  double dN20 = row_h(c, ap, ap == AP_RSA ? c.s.idx_c000 : c.idx_N[c.LM(2, 0)], y, w, lin, tau);
+  return w.phi_pp - c.sh->bg.Hc * psi_prime_of(c, ap, y, w, lin, dI20, dN20);
 }
 
 /* dy = f(tau, y): block-wide; prepare(tau) must have run.  Ends with a barrier. */
-template <class C, class A, class B> __device__ void rhs(const C &c, int tca, double tau, A y, B dy) {
+template <class C, class A, class B> __device__ void rhs(const C &c, int ap, double tau, A y, B dy) {
   const DevSpec &s = c.s;
   auto yv = yvec(y);
-  compute_ws_team(c, tca, yv);
+  compute_ws_team(c, ap, yv);
   c.sync();
   for (int e = c.rank; e < s.n_row_slots; e += c.size) {
     int i = c.row_slot[e];
-    if (i >= 0) dy[i] = row(c, tca, i, yv, c.sh->ws, 0, tau);
+    if (i >= 0) dy[i] = row(c, ap, i, yv, c.sh->ws, 0, tau);
   }
   c.sync();
 }
@@ -1337,16 +1339,16 @@ template <class C, class A, class B> __device__ void rhs(const C &c, int tca, do
    thread turning its row straight into the residual del = h/(gamma) f - (psi +
    dif_{k+1}) and the solve vector in the iteration-matrix precision.  Ends with a
    barrier. */
-template <typename T, class C, class A> __device__ void newton_rhs(const C &c, int tca, double tau, A y, double hinvGak) {
+template <typename T, class C, class A> __device__ void newton_rhs(const C &c, int ap, double tau, A y, double hinvGak) {
   const DevSpec &s = c.s;
   auto yv = yvec(y);
-  compute_ws_team(c, tca, yv);
+  compute_ws_team(c, ap, yv);
   c.sync();
   auto x = c.template xsol<T>();
   for (int e = c.rank; e < s.n_row_slots; e += c.size) {
     int i = c.row_slot[e];
     if (i >= 0) {
-      double fi = row(c, tca, i, yv, c.sh->ws, 0, tau);
+      double fi = row(c, ap, i, yv, c.sh->ws, 0, tau);
       x[i] = (T)(hinvGak * fi - (c.psiv[i] + c.difkp1[i]));
     }
   }
@@ -1355,7 +1357,7 @@ template <typename T, class C, class A> __device__ void newton_rhs(const C &c, i
 
 /* Exact Jacobian of the affine system at tau (prepare(tau) must have run):
    J[:, j] = A e_j, one thread per column; stored per m block in global scratch. */
-template <typename T, class C> __device__ __forceinline__ void jacobian(const C &c, int tca, double tau) {
+template <typename T, class C> __device__ __forceinline__ void jacobian(const C &c, int ap, double tau) {
   const DevSpec &s = c.s;
   auto J0 = c.template jacv<T>();
   for (int b = c.rank; b < s.nblk; b += c.size) c.sh->kl[b] = c.sh->ku[b] = 0;
@@ -1366,11 +1368,11 @@ template <typename T, class C> __device__ __forceinline__ void jacobian(const C 
     int b0 = s.blk_start[b], nb = s.blk_size[b];
     YUnit yu{j};
     WS w;
-    compute_ws(c, tca, yu, 1, w);
+    compute_ws(c, ap, yu, 1, w);
     auto J = J0 + s.lu_off[b];
     int lo = 0, up = 0;
     for (int i = b0; i < b0 + nb; ++i) {
-      T v = (T)row(c, tca, i, yu, w, 1, tau);
+      T v = (T)row(c, ap, i, yu, w, 1, tau);
       J[(i - b0) * nb + (j - b0)] = v;
       if (v != T(0)) {
         if (i > j) lo = max(lo, i - j);
@@ -1684,10 +1686,10 @@ __device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) 
   if (c.rank == 0) {
     double psi_prime = 0.0;
     if (s.compute_m[0]) {
-      int tca = c.sh->tca;
-      double dI20 = tca == AP_TCA ? 0.0 : dy[tca == AP_RSA ? c.s.idx_c000 : c.idx_I[c.LM(2, 0)]];
-      double dN20 = dy[tca == AP_RSA ? c.s.idx_c000 : c.idx_N[c.LM(2, 0)]];
-      psi_prime = psi_prime_of(c, tca, yv, c.sh->ws, 0, dI20, dN20);
+      int ap = c.sh->ap;
+      double dI20 = ap == AP_TCA ? 0.0 : dy[ap == AP_RSA ? c.s.idx_c000 : c.idx_I[c.LM(2, 0)]];
+      double dN20 = dy[ap == AP_RSA ? c.s.idx_c000 : c.idx_N[c.LM(2, 0)]];
+      psi_prime = psi_prime_of(c, ap, yv, c.sh->ws, 0, dI20, dN20);
     }
     c.sh->psi_prime = psi_prime;
   }
@@ -1798,7 +1800,7 @@ __device__ void store_sources(const C &c, int index_tau, double tau, A y, B dy) 
 template <class C, class A, class B> __device__ void store_first_order(const C &c, int index_tau, A y, B dy) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
-  int tca = c.sh->tca;
+  int ap = c.sh->ap;
   auto yv = yvec(y);
   const WS &w = c.sh->ws;
   const BgV &bg = c.sh->bg;
@@ -1830,12 +1832,12 @@ template <class C, class A, class B> __device__ void store_first_order(const C &
       }
     } else {
       int blk = (q - SONG2_FO_I) / L1, l = (q - SONG2_FO_I) % L1;
-      if (blk == 0) v = (l == 0) ? w.I_00 : (l == 1) ? w.I_1m[0] : (l == 2) ? w.I_2m[0] : getI(c, tca, yv, l, 0);
-      else if (blk == 1) v = (l < 2) ? 0.0 : (l == 2) ? w.E_2m[0] : getE(c, tca, yv, l, 0);
+      if (blk == 0) v = (l == 0) ? w.I_00 : (l == 1) ? w.I_1m[0] : (l == 2) ? w.I_2m[0] : getI(c, ap, yv, l, 0);
+      else if (blk == 1) v = (l < 2) ? 0.0 : (l == 2) ? w.E_2m[0] : getE(c, ap, yv, l, 0);
       else if (blk == 2) v = (l == 0) ? w.N_00 : (l == 1) ? w.N_1m[0] : getN(c, yv, l, 0);
       else
         v = (l == 0) ? 0.0 : (l == 1) ? w.C_1m[0] / bg.kappa_dot
-          : (l == 2) ? -w.I_2m[0] + 0.1 * (w.I_2m[0] - SQRT_6 * w.E_2m[0]) : -getI(c, tca, yv, l, 0);
+          : (l == 2) ? -w.I_2m[0] + 0.1 * (w.I_2m[0] - SQRT_6 * w.E_2m[0]) : -getI(c, ap, yv, l, 0);
     }
     o[q] = v;
   }
@@ -2013,7 +2015,7 @@ template <class C> __device__ void initial_conditions(const C &c, double tau) {
   auto y = c.y;
   for (int i = 0; i < s.n; ++i) y[i] = 0.0;
   if (s.ic == SONG2_IC_ZERO || !s.compute_m[0]) return;
-  int tca = c.sh->tca;
+  int ap = c.sh->ap;
   double k = t.k, k_sq = t.k_sq, Hc = bg.Hc, Hc_sq = Hc * Hc, a_sq = bg.a_sq;
   double rho_r = bg.rho_g + bg.rho_ur, frac_ur = bg.rho_ur / rho_r, frac_g = 1 - frac_ur;
   double rho_tot = Hc_sq / a_sq, Omega_m = (bg.rho_b + bg.rho_cdm) / rho_tot, Omega_r = rho_r / rho_tot;
@@ -2053,7 +2055,7 @@ template <class C> __device__ void initial_conditions(const C &c, double tau) {
     double b_0_0_0 = 3 * (I_0_0 / 4 - delta_g_1 * delta_g_2 / 16);
     y[s.idx_phi] = phi;
     y[c.idx_I[c.LM(0, 0)]] = I_0_0;
-    if (!tca) {
+    if (!ap) {
       y[c.idx_I[c.LM(1, 0)]] = I_1_0;
       y[c.idx_I[c.LM(2, 0)]] = I_2_0;
     }
@@ -2073,7 +2075,7 @@ template <class C> __device__ void initial_conditions(const C &c, double tau) {
     double u0 = 0.5 * k * tau * psi;
     double I_0_0 = -2 * psi;
     y[c.idx_I[c.LM(0, 0)]] = I_0_0;
-    if (!tca) y[c.idx_I[c.LM(1, 0)]] = 4 * u0;
+    if (!ap) y[c.idx_I[c.LM(1, 0)]] = 4 * u0;
     y[s.idx_b000] = 0.75 * I_0_0;
     y[s.idx_b11[0]] = 3 * u0;
     y[s.idx_c000] = 0.75 * I_0_0;
@@ -2139,11 +2141,11 @@ __device__ int refactor(const C &c, double hinvGak, song2_triplet_stats &st) {
    and the source functions from quadratic sources and workspace recomputed at
    tau (perturb2_sources, perturbations2.c:11956-12030). */
 template <class C> __device__ void do_output(const C &c, int jout, double to) {
-  int tca = c.sh->tca;
-  prepare_table(c, to, tca);
-  rhs(c, tca, to, c.yout, c.dyout);
+  int ap = c.sh->ap;
+  prepare_table(c, to, ap);
+  rhs(c, ap, to, c.yout, c.dyout);
   prepare(c, to, 1);
-  compute_ws_team(c, tca, yvec(c.yout));
+  compute_ws_team(c, ap, yvec(c.yout));
   c.sync();
   if (c.s.mode_first_order) store_first_order(c, jout, c.yout, c.dyout);
   else store_sources(c, jout, to, c.yout, c.dyout);
@@ -2159,7 +2161,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
   const DevSpec &s = c.s;
   int n = s.n, tid = c.rank, nt = c.size;
   int nout = s.mode_first_order ? s.fo_tau_size : s.tau_size;
-  int tca = c.sh->tca;
+  int ap = c.sh->ap;
   double rtol = s.rtol, threshold = s.threshold;
   const double eps = 2.220446049250313e-16;
   const int maxk = 5, maxit = 4;
@@ -2180,10 +2182,10 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
       }
       ++jout;
     }
-  prepare_table(c, t, tca);
-  rhs(c, tca, t, y, f);
+  prepare_table(c, t, ap);
+  rhs(c, ap, t, y, f);
   st.n_rhs++;
-  jacobian<T>(c, tca, t);
+  jacobian<T>(c, ap, t);
   st.n_jac++;
   int Jcurrent = 1;
   double hmin = 16 * eps * fabs(t);
@@ -2247,9 +2249,9 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
         h = tnew - t;
         double minnrm = 100 * eps * block_max_bits(c, vm);
         double oldnrm = 0;
-        prepare_table(c, tnew, tca);
+        prepare_table(c, tnew, ap);
         for (int iter = 1; iter <= maxit; ++iter) {
-          newton_rhs<T>(c, tca, tnew, ynew, hinvGak);
+          newton_rhs<T>(c, ap, tnew, ynew, hinvGak);
           st.n_rhs++;
           bool inv = use_inverse<T>(c);
           if (inv) inv_solve(c);
@@ -2299,7 +2301,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
             nconhk = 0;
           } else {
             prepare(c, t, 0);
-            jacobian<T>(c, tca, t);
+            jacobian<T>(c, ap, t);
             st.n_jac++;
             Jcurrent = 1;
           }
@@ -2445,7 +2447,7 @@ template <typename T, class C> __device__ __forceinline__ int solve_triplet(cons
   for (int iv = 0; iv < t.nint; ++iv) {
     double ta = t.ivb[iv], tb = t.ivb[iv + 1];
     if (iv == 0) {
-      if (tid == 0) c.sh->tca = t.ivk[0];
+      if (tid == 0) c.sh->ap = t.ivk[0];
       c.sync();
       prepare(c, ta, 1);
       if (tid == 0) initial_conditions(c, ta);
@@ -2453,7 +2455,7 @@ template <typename T, class C> __device__ __forceinline__ int solve_triplet(cons
     } else if (t.ivk[iv] == AP_RSA) {
       /* switching the RSA on drops the massless hierarchies: nothing to remap
          (perturbations2.c:7295-7300); their entries stay in y, unevolved */
-      if (tid == 0) c.sh->tca = AP_RSA;
+      if (tid == 0) c.sh->ap = AP_RSA;
       c.sync();
     } else {
       /* TCA -> full remap (perturbations2.c:7233-7285): the frozen moments take the
@@ -2473,7 +2475,7 @@ template <typename T, class C> __device__ __forceinline__ int solve_triplet(cons
             if (m != 0) c.y[c.idx_B[c.LM(2, m)]] = w.B_2m_tca1[m];
           }
         }
-        c.sh->tca = 0;
+        c.sh->ap = 0;
       }
       c.sync();
     }
