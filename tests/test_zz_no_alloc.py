@@ -21,10 +21,15 @@ from helpers import floored_errors, gpu_run, problem
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_matches_regular_entry_twice(lib):
+@pytest.mark.parametrize("kw", [
+    dict(),
+    # the delta-tilde coupling table is carved from the scratch too
+    dict(sources="TEB", l_max=5, use_delta_tilde_in_los=1, rescale_cmb_sources=1, radiation_streaming_approximation=1),
+])
+def test_noalloc_matches_regular_entry_twice(lib, kw):
     torch = pytest.importorskip("torch")
     import oracle
-    p = problem()
+    p = problem(**kw)
     p.set_first_order(oracle.first_order(p, nthreads=4))
     ref, st_ref, _ = gpu_run(lib, p, capi.SONG2_PREC_MIXED)
     # device copies of the tables (the caller's own buffers)
