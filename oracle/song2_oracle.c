@@ -17,6 +17,7 @@
  *   perturb2_workspace_at_tau                :8839-9027      -> workspace_at_tau
  *   perturb2_fluid_variables                 :9108-9338      -> (inlined in tca_variables)
  *   perturb2_tca_variables                   :9374-9738      -> tca_variables
+ *   perturb2_rsa_variables                   :9773-10164     -> rsa_variables
  *   perturb2_compute_psi_prime               :10188-10383    -> compute_psi_prime
  *   perturb2_quadratic_sources               :10643-11813    -> quadratic_sources
  *   perturb2_sources                         :11869-12823    -> store_sources
@@ -29,7 +30,8 @@
  *    14366-14688), as the reference's default path; tight coupling, initial
  *    conditions and the source functions compute them directly;
  *  - perfect baryons and CDM (reference default, input2.c:2087-2088), Newtonian
- *    gauge, phi equation = huang (input2.c:2152); no RSA/NRA intervals;
+ *    gauge, phi equation = huang (input2.c:2152); RSA intervals when the spec
+ *    asks for them, no NRA/UFA;
  *  - NDF15 written from Shampine & Reichelt, SIAM J. Sci. Comput. 18 (1997):
  *    orders 1-5, kappa = (-0.185,-1/9,-0.0823,-0.0415,0), simplified Newton,
  *    max-norm error control, backward-difference step change, dense output.
