@@ -25,7 +25,13 @@
  *     residual, error estimate and step control stay FP64, the simplified Newton
  *     iteration doubles as iterative refinement);
  *   - the integrator is the variable-order NDF method of Shampine & Reichelt
- *     (1997), the same algorithm as the CPU restatement in oracle/.
+ *     (1997), the same algorithm as the CPU restatement in oracle/;
+ *   - a triplet's time range splits into up to three intervals (tight coupling,
+ *     full system, radiation streaming: perturbations2.c:4854-5403); the state
+ *     keeps every equation, and the ones an approximation drops have zero rows;
+ *   - the source writer (perturb2_sources, perturbations2.c:11869-12823) adds the
+ *     delta-tilde terms when asked; rescaled rotation coefficients
+ *     (perturbations2.c:5635-5652) change only the geometry step.
  * Every loop is bounded (max_steps, 4 Newton iterations, 200 bisection steps);
  * a triplet that breaches a bound retires with a status code.  No kernel spins.
  */
