@@ -107,3 +107,11 @@ def test_rsa_vector_drops_massless_hierarchies(olib, rsa_problem):
     # baryons and CDM: (0,0,0) and (1,1,m) for m <= 1 in the list; metric phi, phi', omega, gamma, gamma'
     assert n_rsa == 2 * 3 + 5
     assert n_full > n_rsa
+
+
+def test_free_streaming_time_edges(lib, rsa_problem):
+    """A trigger never reached gives tau0; one met from the first node gives the
+    start of the table."""
+    t = rsa_problem.tables
+    assert lib.song2_free_streaming_time(C.byref(t), 1e30) == t.tau0
+    assert abs(lib.song2_free_streaming_time(C.byref(t), 1e-30) - np.exp(t.bg_lntau0)) < 1e-12 * np.exp(t.bg_lntau0)
