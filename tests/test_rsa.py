@@ -115,3 +115,35 @@ def test_free_streaming_time_edges(lib, rsa_problem):
     t = rsa_problem.tables
     assert lib.song2_free_streaming_time(C.byref(t), 1e30) == t.tau0
     assert abs(lib.song2_free_streaming_time(C.byref(t), 1e-30) - np.exp(t.bg_lntau0)) < 1e-12 * np.exp(t.bg_lntau0)
+
+
+def test_rsa_dipole_enters_the_baryon_equation(olib, rsa_problem):
+    """With the quadratic sources off, the RSA photon dipole is I_10 = 4*3/k (phi' + psi')
+    with psi' = phi' (perturbations2.c:10033-10090); the baryon dipole equation in
+    the RSA vector must then equal the full-vector one evaluated with that I_10
+    (perturbations2.c:8802-8804: C_1m from the RSA dipole)."""
+    p = rsa_problem
+    spec = capi.Spec.from_buffer_copy(p.spec)
+    spec.radiation_streaming_approximation = capi.SONG2_RSA_MD
+    spec.has_quadratic_sources = 0
+    i1, i2, i3 = 2, 1, 0
+    k = p.triplet_k(i1, i2, i3)[2]
+    err = capi.errbuf()
+    y = np.zeros(4096)
+    dy = np.zeros(4096)
+    n_rsa = olib.song2_oracle_rhs(C.byref(spec), C.byref(p.tables), i1, i2, i3, 2, 3000.0, capi.dptr(y), capi.dptr(dy), err)
+    n_full = olib.song2_oracle_rhs(C.byref(spec), C.byref(p.tables), i1, i2, i3, 0, 3000.0, capi.dptr(y), capi.dptr(dy), err)
+    assert n_rsa == 11 and n_full > n_rsa
+    rng = np.random.default_rng(7)
+    tail = rng.normal(size=11)          # b000 b110 b111 c000 c110 c111 phi phi' omega gamma gamma'
+    y_rsa = np.zeros(4096)
+    y_rsa[:11] = tail
+    y_full = np.zeros(4096)
+    y_full[n_full - 11:n_full] = tail
+    y_full[1] = 24 * tail[7] / k        # I(1,0): lm(1,0) = 1 in the photon block at the start of the vector
+    d_rsa = np.zeros(4096)
+    d_full = np.zeros(4096)
+    olib.song2_oracle_rhs(C.byref(spec), C.byref(p.tables), i1, i2, i3, 2, 3000.0, capi.dptr(y_rsa), capi.dptr(d_rsa), err)
+    olib.song2_oracle_rhs(C.byref(spec), C.byref(p.tables), i1, i2, i3, 0, 3000.0, capi.dptr(y_full), capi.dptr(d_full), err)
+    for j in (1, 2):                    # b110, b111 (I(1,1) = 0 in both)
+        assert abs(d_rsa[j] - d_full[n_full - 11 + j]) <= 1e-12 * max(abs(d_rsa[j]), 1e-30), j
