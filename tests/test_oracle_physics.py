@@ -7,7 +7,11 @@ vectors and cannot be built here, so these are the checks it documents):
 - with no quadratic sources the m=0 second-order solution depends on k3 only,
   not on k1 and k2 (the same debug mode);
 - the second-order result is converged: rtol 1e-6 and 1e-8 runs agree well
-  within 1e-4 (the tolerance contract of the benchmark).
+  within 1e-4 (the tolerance contract of the benchmark);
+- today's second-order CDM density on subhorizon scales is the Newtonian
+  2 F2(k1,k2) delta_1 delta_2 (the comparison of test/print_kernel.c:205-216);
+- the sources obey S(k2,k1,k3) = (-1)^m S(k1,k2,k3) (perturbations2.h:382-388),
+  so odd-m sources vanish when k1 = k2, and B has no m = 0 part.
 """
 import numpy as np
 
@@ -59,3 +63,46 @@ def test_convergence_in_rtol(lib, olib):
     b, _ = oracle.evolve(p, nthreads=4, rtol=1e-8)
     e = floored_errors(a, b, p)
     assert np.max(e) < 1e-4
+
+
+def test_late_cdm_density_follows_the_f2_kernel(lib, olib):
+    """delta_cdm^(2)(tau0) = 2 F2 delta_1 delta_2 with
+    F2 = 5/7 + (k1.k2)/2 (1/k1^2 + 1/k2^2) + 2/7 (k1.k2)^2/(k1^2 k2^2); the stored
+    source is delta^(2)/2 (perturbations2.c:12778).  Lambda, baryons and the
+    relativistic terms keep the ratio within a few per cent at 0.02 <= k <= 0.1."""
+    p = problem(k_min=0.02, k_max=0.1, k_size=3, k3_size=3, l_max=6, m=(0,), sources="TD", tau_size=10)
+    p.set_first_order(oracle.first_order(p, nthreads=8))
+    src, st = oracle.evolve(p, nthreads=8)
+    assert np.all(st["status"] == 0)
+    tp_d = [i for i, (kind, _, _) in enumerate(p.tp_list()) if kind == "D"][0]
+    assert abs(p.tau[-1] / p.fo_tau_grid()[-1] - 1) < 1e-12
+    ratios = []
+    for (i1, i2, i3) in p.work_order():
+        k1, k2, k = p.triplet_k(i1, i2, i3)
+        s_d = p.triplet_view(src, i1, i2, i3)[tp_d][-1]
+        d1, d2 = p.fo[i1, -1, capi.FO_DELTA_CDM], p.fo[i2, -1, capi.FO_DELTA_CDM]
+        kk = (k * k - k1 * k1 - k2 * k2) / 2
+        f2 = 5 / 7 + 0.5 * kk * (1 / k1 ** 2 + 1 / k2 ** 2) + 2 / 7 * kk * kk / (k1 ** 2 * k2 ** 2)
+        ratios.append(s_d / (f2 * d1 * d2))
+    ratios = np.array(ratios)
+    assert np.all(np.abs(ratios - 1) < 0.03), ratios
+
+
+def test_source_symmetries(lib, olib):
+    p = problem(sources="TEB", l_max=5)
+    p.set_first_order(oracle.first_order(p, nthreads=8))
+    src, st = oracle.evolve(p, nthreads=8)
+    assert np.all(st["status"] == 0)
+    kinds = p.tp_list()
+    odd = [i for i, (kind, _, m) in enumerate(kinds) if m % 2 == 1]
+    even = [i for i, (kind, _, m) in enumerate(kinds) if m % 2 == 0 and kind != "B"]
+    b0 = [i for i, (kind, _, m) in enumerate(kinds) if kind == "B" and m == 0]
+    assert odd and even and b0
+    n_diag = 0
+    for (i1, i2, i3) in p.work_order():
+        v = p.triplet_view(src, i1, i2, i3)
+        assert not np.any(v[b0])
+        if i1 == i2:
+            n_diag += 1
+            assert np.abs(v[odd]).max() <= 1e-9 * np.abs(v[even]).max()
+    assert n_diag > 0
