@@ -1,37 +1,50 @@
 """Benchmark of the GB300 second-order evolver.
 
-A "step" evolves every (k1,k2,k3) triplet of the workload once and fills the
-ppt2->sources layout.  The default workload is the plain-vs-reference
-configuration of the benchmark set: flat LCDM, k1,k2 on 25 log points in
-[1e-5, 0.1]/Mpc, 15 k3 per pair (4875 triplets), T+E sources with l_max = 12,
-m in {0,1,2}, rtol 1e-4, 200 source times from 200 Mpc to tau0.  Inputs are
-synthetic: the background/recombination and first-order tables come from this
-project's own provider (the CLASS tables the reference would use are not
-available).
+A "step" is one pass of the evolver over one part of the workload.  The default
+workload is the uneven batch of the benchmark set (config 4): flat LCDM, k1, k2
+on 50 log points in [1e-5, 0.3]/Mpc, 24 k3 per pair (30,600 triplets), T+E+B
+sources, l_max = min(40, 8 + ceil(k tau_rec / 2)) and m_max drawn from {0, 2, 4}
+per triplet (96 hierarchy classes, 32 to 744 equations), rtol 1e-4, 200 source
+times from 200 Mpc to tau0.  The triplets are dealt into K = --steps
+cost-balanced parts (song2_ctx_run_part: round-robin over each launch group's
+cost-sorted work list), so the K timed steps evolve every triplet exactly once.
+Inputs are synthetic: the background/recombination and first-order tables come
+from this project's own provider (the CLASS tables the reference would use are
+not available).
 
-  value        triplets/s of the mixed form (FP64 RHS/residual/error control,
-               FP32 banded LU of the per-m iteration-matrix blocks), tables
-               resident in HBM, CUDA events around each persistent-kernel
-               launch; L2 is flushed between steps.
-  plain_fp64   the same for the plain FP64 form (FP64 banded LU), for the
-               mixed-vs-plain ratio the metric asks for.
-  e2e          triplets/s through song2_gpu_evolve (the drop-in C ABI): host
-               tables uploaded and the host ppt2->sources slabs filled inside
-               the timed region.
+  value        triplets/s of the mixed form (FP64 right-hand side, Newton residual
+               and error control; FP32 factorisation of the structured iteration
+               matrix), tables resident in HBM, CUDA events around each part's
+               launches; L2 flushed (256 MiB write) before every step.
+  plain_fp64   the plain FP64 form on the first --plain-parts parts, and the
+               mixed form's time on the same parts (mixed_over_plain).
+  e2e          triplets/s through song2_gpu_evolve (the drop-in C ABI) over the
+               whole workload: host tables uploaded and the host ppt2->sources
+               slabs filled inside the timed region.
   cpu_baseline the CPU restatement (oracle/) on this machine's host cores, on a
-               bounded sample of the same triplets.
+               bounded cost-stratified sample of the same triplets.
+  err_vs_fp64_oracle
+               per (source type, triplet) max_tau |S - S_ref| / max_tau |S_ref| of
+               the GPU sources against the oracle at rtol 1e-8, on triplets spread
+               over every hierarchy size and m_max; computed in a spawned CPU
+               process while the GPU arms run.
 
 --impl reference runs the reference arm: the reference (coccoinomane/song)
 cannot be built (its CLASS submodule is empty), so the arm times the CPU
-restatement of its algorithm with all host threads.
+restatement of its algorithm with all host threads, building its inputs with
+the oracle library alone (no product library is loaded).  Each of its steps is
+a cost-stratified sample of the workload; ms_per_step is the measured wall time
+of a step.
 """
 import argparse
 import ctypes as C
 import json
+import multiprocessing as mp
 import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -40,9 +53,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "2nd-order k-triplets/s at rtol 1e-4: mixed+batched vs plain FP64 GPU; err vs FP64"
-WORKLOAD = 2
-# FP64 work of the mixed-form evolver per NDF step (ncu, reduced config 2) and the
-# FP64 issue rate of a GB300 SM (DFMA probe, song_gb300/csrc/probe_fp64.cu)
+WORKLOAD = 4
+ERR_BOUND = 1e-4
+# FP64 work of the mixed-form evolver per NDF step and FP64 warp instructions per
+# NDF step (ncu counters of this kernel on the reduced config-4 case, see
+# profiles/), and the FP64 issue rate of a GB300 SM (one FP64 warp instruction per
+# ~19 SM cycles whatever the number of active lanes; DFMA probe, see profiles/)
 FP64_FLOPS_PER_STEP = 47.0e3
 FP64_WARP_INSTR_PER_STEP = 2.74e3
 FP64_WARP_INSTR_PER_SM_CYCLE = 0.0526
@@ -55,9 +71,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", type=int, default=WORKLOAD)
-    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
-    ap.add_argument("--accuracy-sample", type=int, default=32,
+    ap.add_argument("--parts", type=int, default=0, help="parts of the workload (default: --steps)")
+    ap.add_argument("--cpu-sample", type=int, default=256,
+                    help="triplets of the CPU-baseline sample (every n/N-th of the cost-sorted workload)")
+    ap.add_argument("--ref-step-items", type=int, default=192, help="triplets per reference-arm step")
+    ap.add_argument("--accuracy-sample", type=int, default=16,
                     help="triplets checked against the FP64 oracle at rtol 1e-8 (0: skip)")
+    ap.add_argument("--plain-parts", type=int, default=0, help="parts timed in plain FP64 (default: steps/4)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--k-size", type=int, default=None, help="override the k grid size (small profiling cases)")
@@ -75,15 +95,16 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region
+    (written to a temporary file)."""
 
     def __init__(self, gpu):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu}.csv")
+        fd, self.path = tempfile.mkstemp(prefix=f"song2_clocks_gpu{gpu}_", suffix=".csv")
+        os.close(fd)
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -109,6 +130,11 @@ class Clocks:
             lines = [l.strip() for l in open(self.path) if l.strip() and not l.startswith("index")]
         except OSError:
             return None
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for l in lines:
@@ -136,11 +162,17 @@ def measured_peaks():
         return {}
 
 
-def build_problem(cfg, overrides):
-    from song_gb300.problem import config_problem
-    p = config_problem(cfg, **overrides)
-    p.first_order_gpu()          # first-order tables from the GPU first-order mode (untimed set-up)
-    return p
+def workload_overrides(args, cfg):
+    overrides = {}
+    if args.k_size:
+        overrides["k_size"] = cfg["k_size"] = args.k_size
+    if args.k3_size:
+        overrides["k3_size"] = cfg["k3_size"] = args.k3_size
+    name = cfg["name"] + ("" if not overrides else "_reduced")
+    if args.rsa:
+        overrides["radiation_streaming_approximation"] = args.rsa
+        name += "_rsa%d" % args.rsa
+    return overrides, name
 
 
 def table_bytes(p):
@@ -148,57 +180,206 @@ def table_bytes(p):
 
 
 def algorithmic_bytes(p):
-    """Bytes a step must move: the two first-order rows of every triplet's (k1,k2)
-    pair over its time range (read once per pair and reused from L2 by the other k3
-    of the pair), the background table, and the source writes."""
-    per_pair_rows = 2 * p.fo.shape[1] * p.fo.shape[2] * 8 * 2   # values + spline d2 of two k rows
+    """Bytes a full pass must move: the two first-order rows of every (k1,k2) pair
+    over the table's time range (values and spline coefficients, read once per pair
+    and reused from L2 by the pair's other k3), the background table, and the source
+    writes."""
+    per_pair_rows = 2 * p.fo.shape[1] * p.fo.shape[2] * 8 * 2
     n = len(p.k)
     n_pairs = n * (n + 1) // 2
     return int(n_pairs * per_pair_rows + 2 * p.bg.nbytes + p.tp2_size * p.per_type * 8)
 
 
-def flush_l2(torch, buf):
-    buf.zero_()
+# ---------------------------------------------------------------- workload bookkeeping
+
+def pair_order_classes(p):
+    """Class (l_max, m_max) of every triplet in work order, or None for uniform runs."""
+    if p.classes is None:
+        return None
+    n = len(p.k)
+    start, off = {}, 0
+    for i1 in range(n):
+        for i2 in range(i1 + 1):
+            start[(i1, i2)] = off
+            off += int(p.k3_size[i1 * n + i2])
+    out = []
+    for (i1, i2, i3) in p.work_order():
+        out.append(p.classes[int(p.triplet_class[start[(i1, i2)] + i3])])
+    return out
 
 
-def run_device(lib, p, precision, steps, warmup, torch, rank, world):
+def cost_order(p):
+    """Work-order indices sorted by decreasing cost estimate (the GPU work list's
+    order: max(k1, k2, k3), times (l_max + 1)(m_max + 1) for hierarchy classes)."""
+    work = p.work_order()
+    cls = pair_order_classes(p)
+    n = len(p.k)
+    kk = np.empty(len(work))
+    off = {}
+    acc = 0
+    for i1 in range(n):
+        for i2 in range(i1 + 1):
+            off[(i1, i2)] = acc
+            acc += int(p.k3_size[i1 * n + i2])
+    for t, (i1, i2, i3) in enumerate(work):
+        kk[t] = max(p.k[i1], p.k[i2], p.k3[off[(i1, i2)] + i3])
+        if cls is not None:
+            kk[t] *= (cls[t][0] + 1.0) * (cls[t][1] + 1.0)
+    return np.argsort(-kk, kind="stable"), kk
+
+
+def triplet_entries(p, items):
+    """Flat indices (within one source type) of every (tau) entry of the given
+    work-order triplets: array [len(items), tau_size]."""
+    work = p.work_order()
+    n = len(p.k)
+    rows = []
+    ntau = len(p.tau)
+    for it in items:
+        i1, i2, i3 = work[int(it)]
+        nk3 = int(p.k3_size[i1 * n + i2])
+        off = p.pair_offset(i1, i2)
+        rows.append(off + i3 + nk3 * np.arange(ntau))
+    return np.array(rows, dtype=np.int64)
+
+
+def source_error(p, test, ref, items, floor=1e-10):
+    """max over (source type, triplet) of max_tau |S - S_ref| / max_tau |S_ref| (the
+    denominator floored at `floor` times the triplet's largest source: odd-m sources
+    vanish by symmetry when k1 = k2) and the worst (source type, work-order index)."""
+    a = test.reshape(p.tp2_size, p.per_type)
+    b = ref.reshape(p.tp2_size, p.per_type)
+    idx = triplet_entries(p, items)
+    ta, tb = a[:, idx], b[:, idx]                     # [tp, triplet, tau]
+    den = np.max(np.abs(tb), axis=2)
+    den = np.maximum(den, floor * np.maximum(den.max(axis=0, keepdims=True), 1e-300))
+    e = np.max(np.abs(ta - tb), axis=2) / den
+    w = np.unravel_index(int(np.argmax(e)), e.shape)
+    return float(e.max()), (int(w[0]), int(items[w[1]]))
+
+
+def accuracy_items(p, n):
+    """Work-order indices of n triplets spread over every hierarchy size and m_max:
+    for each m_max, the cheapest triplet of the smallest, a middle and the largest
+    l_max class, then triplets evenly spread over the cost-sorted order (without
+    its most expensive tenth, whose rtol-1e-8 runs take minutes on a CPU core)."""
+    order, kk = cost_order(p)
+    cls = pair_order_classes(p)
+    pick = []
+    if cls is not None:
+        ms = sorted({c[1] for c in cls})
+        for m in ms:
+            ls = sorted({c[0] for c in cls if c[1] == m})
+            for L in (ls[0], ls[len(ls) // 2], ls[-1]):
+                cand = [t for t in range(len(cls)) if cls[t] == (L, m)]
+                pick.append(min(cand, key=lambda t: kk[t]))
+    rest = max(0, n - len(pick))
+    lo = len(order) // 10
+    if rest:
+        for q in np.linspace(lo, len(order) - 1, rest).astype(int):
+            pick.append(int(order[q]))
+    out = []
+    for t in pick:
+        if int(t) not in out:
+            out.append(int(t))
+    return np.array(out, dtype=np.int64)
+
+
+# ---------------------------------------------------------------- oracle side (CPU)
+
+def oracle_problem(cfg, overrides, fo=None, threads=None):
+    """The workload built with the oracle library alone (its input provider is the
+    same C source as the product's), first-order tables from the oracle or given."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
     from song_gb300 import capi
-    import torch.distributed as dist
+    from song_gb300.problem import config_problem
+    oracle.build()
+    oracle.load()
+    host = capi.bind(C.CDLL(oracle.LIB), host_only=True)
+    p = config_problem(cfg, lib=host, **overrides)
+    if fo is None:
+        fo = oracle.first_order(p, nthreads=threads or os.cpu_count())
+    p.set_first_order(fo)
+    return p
+
+
+def accuracy_worker(cfg, overrides, fo_path, items_path, out_path, threads):
+    """Spawned process: the oracle at rtol 1e-8 on the sample triplets."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    p = oracle_problem(cfg, overrides, fo=np.load(fo_path))
+    items = np.load(items_path)
+    t0 = time.perf_counter()
+    ref, st = oracle.evolve(p, nthreads=threads, items=items, rtol=1e-8)
+    np.savez(out_path, ref=ref, status=st["status"], seconds=time.perf_counter() - t0)
+
+
+def stratified(order, m, offset):
+    """m triplets, every (n/m)-th of the cost-sorted order starting at offset (mod the
+    stride), most expensive first: the sample carries the workload's cost
+    distribution, and the dynamic schedule starts its longest triplets first."""
+    n = len(order)
+    stride = max(1, n // max(1, m))
+    return order[(offset % stride)::stride][:m], stride
+
+
+def cpu_sample(p, m, threads, offset=0):
+    """The oracle on a cost-stratified sample of m triplets of the workload.
+    Returns (triplets/s, items, seconds, stride)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    order, _ = cost_order(p)
+    pick, stride = stratified(order, m, offset)
+    t0 = time.perf_counter()
+    oracle.evolve(p, nthreads=threads, items=pick)
+    dt = time.perf_counter() - t0
+    return len(pick) / dt, len(pick), dt, stride
+
+
+# ---------------------------------------------------------------- GPU side
+
+def ctx_create(lib, p, precision):
+    from song_gb300 import capi
     c = C.c_void_p()
     err = capi.errbuf()
     if lib.song2_ctx_create(C.byref(p.spec), C.byref(p.tables), precision, C.byref(c), err):
         raise RuntimeError(err.value.decode())
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    try:
-        for _ in range(warmup):
-            if lib.song2_ctx_run(c, None, err):
-                raise RuntimeError(err.value.decode())
-        ms = []
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        for _ in range(steps):
-            flush_l2(torch, flush)
+    return c
+
+
+def run_parts(lib, c, parts, n_parts, torch, flush):
+    """Run the given parts one per step, L2 flushed before each; device ms per part
+    and launches in the timed region."""
+    from song_gb300 import capi
+    err = capi.errbuf()
+    ms, launches = [], 0
+    torch.cuda.synchronize()
+    for q in parts:
+        if flush is not None:
+            flush.zero_()
             torch.cuda.synchronize()
-            if lib.song2_ctx_run(c, None, err):      # CUDA events on the launching stream inside
-                raise RuntimeError(err.value.decode())
-            ms.append(lib.song2_ctx_last_kernel_ms(c))
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        stats = (capi.TripletStats * p.n_triplets)()
-        src = np.zeros(p.tp2_size * p.per_type)
-        lib.song2_ctx_download(c, capi.dptr(src), stats, err)
-        st = np.frombuffer(stats, dtype=capi.STATS_DTYPE).copy()
-        launches = lib.song2_ctx_last_launches(c) * steps
-    finally:
-        lib.song2_ctx_destroy(c)
-    return ms, st, src, launches
+        if lib.song2_ctx_run_part(c, int(q), n_parts, None, err):
+            raise RuntimeError(err.value.decode())
+        ms.append(lib.song2_ctx_last_kernel_ms(c))
+        launches += lib.song2_ctx_last_launches(c)
+    torch.cuda.synchronize()
+    return ms, launches
 
 
-def run_e2e(lib, p, precision, steps, warmup):
-    """song2_gpu_evolve with host tables and host nested slabs, wall time on the host
-    around a synchronous call (the call returns after its D2H copies)."""
+def download(lib, c, p):
+    from song_gb300 import capi
+    err = capi.errbuf()
+    stats = (capi.TripletStats * p.n_triplets)()
+    src = np.zeros(p.tp2_size * p.per_type)
+    if lib.song2_ctx_download(c, capi.dptr(src), stats, err):
+        raise RuntimeError(err.value.decode())
+    return src, np.frombuffer(stats, dtype=capi.STATS_DTYPE).copy()
+
+
+def run_e2e(lib, p, precision):
+    """song2_gpu_evolve with host tables and host nested slabs: wall time on the host
+    around the synchronous call (it returns after its D2H copies and the scatter)."""
     from song_gb300 import capi
     n = len(p.k)
     keep = []
@@ -219,114 +400,73 @@ def run_e2e(lib, p, precision, steps, warmup):
         tp_level[tp] = k1_level
     st = (capi.TripletStats * p.n_triplets)()
     err = capi.errbuf()
-    times = []
-    for i in range(warmup + steps):
+    t0 = time.perf_counter()
+    if lib.song2_gpu_evolve(C.byref(p.spec), C.byref(p.tables), precision, C.cast(tp_level, C.c_void_p), st, err):
+        raise RuntimeError(err.value.decode())
+    return time.perf_counter() - t0, table_bytes(p), d2h
+
+
+# ---------------------------------------------------------------- arms
+
+def reference_arm(args, cfg_num, overrides, config):
+    """The CPU restatement with all host threads: each step a cost-stratified sample
+    of the workload (ms_per_step = the steps' measured wall time)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count()
+    p = oracle_problem(cfg_num, overrides, threads=threads)
+    config["triplets_per_gpu"] = p.n_triplets
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    order, _ = cost_order(p)
+    n = len(order)
+    m = min(n, args.ref_step_items)
+    stride = max(1, n // m)
+    # warm-up steps: one cheap triplet each (untimed)
+    for w in range(args.warmup):
+        oracle.evolve(p, nthreads=threads, items=order[-1 - w:][:1])
+    walls, counts = [], []
+    for j in range(args.steps):
+        # a different stratified sample per step: the offsets walk through the strata
+        items, _ = stratified(order, m, (j * stride) // max(1, args.steps) + j)
         t0 = time.perf_counter()
-        if lib.song2_gpu_evolve(C.byref(p.spec), C.byref(p.tables), precision, C.cast(tp_level, C.c_void_p), st,
-                                err):
-            raise RuntimeError(err.value.decode())
-        if i >= warmup:
-            times.append(time.perf_counter() - t0)
-    return times, table_bytes(p), d2h
-
-
-def cpu_baseline(p, budget_s, threads):
-    """The oracle on a bounded, evenly spread sample of the same triplets."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    oracle.build()
-    order = np.arange(p.n_triplets)
-    # calibrate with a small sample, then size the sample to the budget
-    n0 = min(p.n_triplets, max(threads, 8))
-    pick = order[:: max(1, p.n_triplets // n0)][:n0]
-    t0 = time.perf_counter()
-    oracle.evolve(p, nthreads=threads, items=pick)
-    dt = time.perf_counter() - t0
-    per = dt / len(pick)
-    n1 = int(min(p.n_triplets, max(len(pick), budget_s / max(per, 1e-6))))
-    pick = order[:: max(1, p.n_triplets // n1)][:n1]
-    t0 = time.perf_counter()
-    oracle.evolve(p, nthreads=threads, items=pick)
-    dt = time.perf_counter() - t0
-    return len(pick) / dt, len(pick), dt
-
-
-def accuracy_sample(p, results, n, threads, rtol=1e-8, floor=1e-10):
-    """Max relative error of GPU sources against the FP64 oracle at rtol = 1e-8 on an
-    evenly spread sample of n triplets: per (source type, triplet) max_tau |S - S_ref| /
-    max_tau |S_ref|, the denominator floored at `floor` times the triplet's largest
-    source (odd-m sources vanish by symmetry when k1 = k2)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    oracle.build()
-    work = p.work_order()
-    pick = list(range(0, len(work), max(1, len(work) // n)))[:n]
-    ref, _ = oracle.evolve(p, nthreads=threads, items=np.array(pick), rtol=rtol)
-    b = ref.reshape(p.tp2_size, p.per_type)
-    out = {}
-    for name, flat in results.items():
-        a = flat.reshape(p.tp2_size, p.per_type)
-        worst = 0.0
-        for it in pick:
-            i1, i2, i3 = work[it]
-            ta, tb = p.triplet_view(a, i1, i2, i3), p.triplet_view(b, i1, i2, i3)
-            den = np.max(np.abs(tb), axis=1)
-            den = np.maximum(den, floor * max(den.max(), 1e-300))
-            worst = max(worst, float(np.max(np.max(np.abs(ta - tb), axis=1) / den)))
-        out[name] = worst
-    return out, len(pick)
+        oracle.evolve(p, nthreads=threads, items=items)
+        walls.append(time.perf_counter() - t0)
+        counts.append(len(items))
+    v = sum(counts) / sum(walls)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "triplets/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(walls) / len(walls),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (own background/recombination and first-order provider)", "config": config,
+            "cpu_baseline": {"value": v, "unit": "triplets/s", "cores": threads, "kind": "port",
+                             "sample": f"each step every {stride}-th triplet of the cost-sorted "
+                                       f"{n}-triplet workload ({m} triplets, {statistics.mean(walls):.1f} s), "
+                                       f"most expensive first, offsets differ per step"},
+            "e2e": {"value": v, "unit": "triplets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference (coccoinomane/song) does not build: its CLASS submodule class.git is empty; "
+                    "this arm times the CPU restatement of its algorithm (oracle/) with all host threads, "
+                    "inputs built by the oracle library alone"}
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def main():
     args = parse()
     rank, world, local = dist_env()
-    cfg_name = None
     from song_gb300.problem import CONFIGS
     cfg = dict(CONFIGS[args.config])
-    overrides = {}
-    if args.k_size:
-        overrides["k_size"] = cfg["k_size"] = args.k_size
-    if args.k3_size:
-        overrides["k3_size"] = cfg["k3_size"] = args.k3_size
-    cfg_name = cfg["name"] + ("" if not overrides else "_reduced")
-    if args.rsa:
-        overrides["radiation_streaming_approximation"] = args.rsa
-        cfg_name += "_rsa%d" % args.rsa
+    overrides, cfg_name = workload_overrides(args, cfg)
+    n_parts = args.parts or args.steps
     config = {"workload": cfg_name, "triplets_per_gpu": None, "k_min": cfg["k_min"], "k_max": cfg["k_max"],
               "k_size": cfg["k_size"], "k3_size": cfg["k3_size"], "l_max": cfg["l_max"], "m": list(cfg["m"]),
               "rtol": cfg["rtol"], "tau_size": cfg["tau_size"], "sources": cfg["sources"],
               "l2": "flushed between steps (256 MiB write)", "rsa": args.rsa}
+    if cfg.get("uneven"):
+        config["uneven"] = "l_max = min(40, 8 + ceil(k tau_rec/2)), m_max from {0,2,4} (seeded), 96 classes"
 
     if args.impl == "reference":
-        if rank != 0:
-            return 0
-        from song_gb300 import build
-        build.build()
-        from song_gb300.problem import config_problem
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle
-        p = config_problem(args.config, **overrides)
-        p.set_first_order(oracle.first_order(p, nthreads=os.cpu_count()))
-        threads = os.cpu_count()
-        vals = []
-        for i in range(args.warmup + args.steps):
-            v, n, dt = cpu_baseline(p, args.cpu_sample_s / max(1, args.steps), threads)
-            if i >= args.warmup:
-                vals.append((v, n, dt))
-        v = statistics.median([x[0] for x in vals])
-        config["triplets_per_gpu"] = p.n_triplets
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "triplets/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * p.n_triplets / v,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (own background/recombination and first-order provider)", "config": config,
-                "cpu_baseline": {"value": v, "unit": "triplets/s", "cores": threads, "kind": "port",
-                                 "sample": f"{vals[-1][1]} triplets spread over the {p.n_triplets}-triplet "
-                                           f"workload per step ({vals[-1][2]:.1f} s)"},
-                "e2e": {"value": v, "unit": "triplets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "note": "reference (coccoinomane/song) does not build: its CLASS submodule class.git is empty; "
-                        "this arm times the CPU restatement of its algorithm (oracle/) with all host threads"}
-        print(json.dumps(line), flush=True)
-        return 0
+        return reference_arm(args, args.config, overrides, config)
 
     import torch
     import torch.distributed as dist
@@ -336,39 +476,88 @@ def main():
     else:
         torch.cuda.set_device(0)
     from song_gb300 import build, capi
+    from song_gb300.problem import config_problem
     if rank == 0:
         build.build()
     if world > 1:
         dist.barrier()
     lib = capi.load()
-    p = build_problem(args.config, overrides)
+    p = config_problem(args.config, **overrides)
+    p.first_order_gpu()          # first-order tables from the GPU first-order mode (untimed set-up)
     n_trip = p.n_triplets
     config["triplets_per_gpu"] = n_trip
+    config["parts"] = f"{n_parts} cost-balanced parts, one per step (song2_ctx_run_part)"
 
-    with Clocks(local) as clk:
-        ms_mixed, st_mixed, src_mixed, launches = run_device(lib, p, capi.SONG2_PREC_MIXED, args.steps,
-                                                             args.warmup, torch, rank, world)
+    # the rtol-1e-8 oracle check runs in a spawned CPU process during the GPU arms
+    acc = None
+    if rank == 0 and world == 1 and args.accuracy_sample > 0:
+        tmp = tempfile.mkdtemp(prefix="song2_bench_")
+        items = accuracy_items(p, args.accuracy_sample)
+        np.save(os.path.join(tmp, "fo.npy"), p.fo)
+        np.save(os.path.join(tmp, "items.npy"), items)
+        out = os.path.join(tmp, "ref.npz")
+        proc = mp.get_context("spawn").Process(
+            target=accuracy_worker,
+            args=(args.config, overrides, os.path.join(tmp, "fo.npy"), os.path.join(tmp, "items.npy"), out,
+                  max(1, os.cpu_count() - 2)))
+        proc.start()
+        acc = (proc, items, out, time.perf_counter())
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    c = ctx_create(lib, p, capi.SONG2_PREC_MIXED)
+    try:
+        run_parts(lib, c, [w % n_parts for w in range(args.warmup)], n_parts, torch, None)
+        if world > 1:
+            dist.barrier()
+        with Clocks(local) as clk:
+            ms_mixed, launches = run_parts(lib, c, [s % n_parts for s in range(args.steps)], n_parts, torch, flush)
+        if world > 1:
+            dist.barrier()
+        src_mixed, st_mixed = download(lib, c, p)
+    finally:
+        lib.song2_ctx_destroy(c)
     clocks = clk.summary()
-    ms_plain = None
-    if not args.no_plain:
-        ms_plain, st_plain, src_plain, _ = run_device(lib, p, capi.SONG2_PREC_FP64, max(1, args.steps),
-                                                      max(1, min(args.warmup, 1)), torch, rank, world)
-    # max over ranks of the timed device time
     t_mixed = sum(ms_mixed) / 1e3
     tt = torch.tensor([t_mixed], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
     t_mixed = float(tt.item())
-    value = world * n_trip * args.steps / t_mixed
+    trip_timed = n_trip * args.steps / n_parts
+    value = world * trip_timed / t_mixed
+
+    plain = None
+    if not args.no_plain:
+        pp = args.plain_parts or max(1, args.steps // 4)
+        pp = min(pp, n_parts)
+        c = ctx_create(lib, p, capi.SONG2_PREC_FP64)
+        warm = n_parts - 1 if n_parts - 1 >= pp else None
+        try:
+            if warm is not None:
+                run_parts(lib, c, [warm], n_parts, torch, None)
+                _, st_warm = download(lib, c, p)
+            ms_plain, _ = run_parts(lib, c, list(range(pp)), n_parts, torch, flush)
+            src_plain, st_plain = download(lib, c, p)
+        finally:
+            lib.song2_ctx_destroy(c)
+        # the triplets of the timed parts (without the untimed warm-up part)
+        timed = st_plain["n_steps"] > 0
+        if warm is not None:
+            timed &= st_warm["n_steps"] == 0
+        ran = np.nonzero(timed)[0]
+        ms_m = sum(ms_mixed[q] for q in range(pp)) if pp <= args.steps else None
+        plain = {"parts": pp, "ms": ms_plain, "ms_mixed_same_parts": ms_m, "src": src_plain, "st": st_plain,
+                 "ran": ran}
 
     e2e = None
     if not args.no_e2e:
-        times, h2d, d2h = run_e2e(lib, p, capi.SONG2_PREC_MIXED, max(1, args.steps), 1)
-        te = torch.tensor([sum(times)], dtype=torch.float64, device="cuda")
+        te, h2d, d2h = run_e2e(lib, p, capi.SONG2_PREC_MIXED)
+        tt = torch.tensor([te], dtype=torch.float64, device="cuda")
         if world > 1:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        e2e = {"value": world * n_trip * len(times) / float(te.item()), "unit": "triplets/s",
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e = {"value": world * n_trip / float(tt.item()), "unit": "triplets/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "note": "whole workload through song2_gpu_evolve (one call: set-up, upload, evolve, download, "
+                       "scatter into the nested host slabs)"}
 
     if rank != 0:
         if world > 1:
@@ -377,23 +566,21 @@ def main():
 
     peaks = measured_peaks()
     ms_step = 1e3 * t_mixed / args.steps
-    alg = algorithmic_bytes(p)
+    # roofline of the dominant kernel: algorithmic bytes of one step (a part) over its time
+    alg = algorithmic_bytes(p) * (trip_timed / n_trip) / args.steps
     hbm_peak = peaks.get("hbm_gbs")
     achieved = alg / (ms_step / 1e3) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": (achieved / hbm_peak) if hbm_peak else None, "traffic": None,
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak or 6800.0, "unit": "GB/s",
+                "frac": achieved / (hbm_peak or 6800.0), "traffic": None,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else "fallback 6800",
-                "note": "the evolver is bound by the FP64 pipe (RHS, residual, error control), not by HBM; "
+                "note": "the evolver is bound by the latency of its FP64 chains and the FP64 pipe, not by HBM; "
                         "bytes = first-order rows of every (k1,k2) pair + background + source writes"}
-    steps_tot = st_mixed["n_steps"].sum()
-    # FP64 pipe: algorithmic FP64 work per NDF step (ncu counters of this kernel on
-    # the reduced config-2 case) and the SM's FP64 issue rate (the DFMA probe in
-    # song_gb300/csrc/probe_fp64.cu); the run supplies the step count and the time
+    steps_tot = int(st_mixed["n_steps"].sum())
     sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
     nsm = torch.cuda.get_device_properties(0).multi_processor_count
-    fp64_flops = steps_tot * FP64_FLOPS_PER_STEP / (ms_step / 1e3)
+    fp64_flops = steps_tot * FP64_FLOPS_PER_STEP / t_mixed * (args.steps / n_parts)
     fp64_peak = FP64_WARP_INSTR_PER_SM_CYCLE * 32 * 2 * sm_mhz * 1e6 * nsm
-    fp64_slots = steps_tot * FP64_WARP_INSTR_PER_STEP / (ms_step / 1e3)
+    fp64_slots = steps_tot * FP64_WARP_INSTR_PER_STEP / t_mixed * (args.steps / n_parts)
     slot_peak = FP64_WARP_INSTR_PER_SM_CYCLE * sm_mhz * 1e6 * nsm
     roofline_fp64 = {"bound": "fp64", "achieved": fp64_flops / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
                      "frac": fp64_flops / fp64_peak, "issue_slots_frac": fp64_slots / slot_peak,
@@ -402,44 +589,64 @@ def main():
                              "issue_slots_frac counts FP64 warp instructions against that rate"}
     line = {"metric": METRIC, "value": value, "unit": "triplets/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 (FP32 banded LU)",
+            "vs_baseline": None, "dtype": "f64 (FP32 iteration-matrix factors)",
             "data": "synthetic (own background/recombination and first-order provider)", "config": config,
             "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "roofline_fp64": roofline_fp64,
             "e2e": e2e,
             "status_ok": bool(np.all(st_mixed["status"] == 0)),
-            "counters": {"ndf_steps": int(steps_tot), "rhs": int(st_mixed["n_rhs"].sum()),
-                         "jacobians": int(st_mixed["n_jac"].sum()), "lu": int(st_mixed["n_lu"].sum())}}
-    if ms_plain is not None:
-        t_plain = sum(ms_plain) / 1e3
-        v_plain = n_trip * len(ms_plain) / t_plain
-        line["plain_fp64"] = {"value": world * v_plain, "unit": "triplets/s", "ms_per_step": 1e3 * t_plain / len(ms_plain),
-                              "status_ok": bool(np.all(st_plain["status"] == 0))}
-        line["mixed_over_plain"] = value / (world * v_plain)
-        from song_gb300.problem import source_errors  # noqa: F401
-        a = src_mixed.reshape(p.tp2_size, p.per_type)
-        b = src_plain.reshape(p.tp2_size, p.per_type)
-        den = np.max(np.abs(b)) + 1e-300
-        line["mixed_vs_plain_max_abs_over_max"] = float(np.max(np.abs(a - b)) / den)
+            "counters": {"ndf_steps": steps_tot, "rhs": int(st_mixed["n_rhs"].sum()),
+                         "jacobians": int(st_mixed["n_jac"].sum()), "factorisations": int(st_mixed["n_lu"].sum()),
+                         "rejected": int(st_mixed["n_rejected"].sum())}}
+    if plain is not None:
+        t_plain = sum(plain["ms"]) / 1e3
+        n_pl = len(plain["ran"])
+        line["plain_fp64"] = {"value": world * n_pl / t_plain, "unit": "triplets/s",
+                              "ms_per_step": 1e3 * t_plain / len(plain["ms"]),
+                              "parts": f"{plain['parts']} of {n_parts} ({n_pl} triplets)",
+                              "status_ok": bool(np.all(plain["st"]["status"][plain["ran"]] == 0))}
+        if plain["ms_mixed_same_parts"]:
+            line["mixed_over_plain"] = t_plain / (plain["ms_mixed_same_parts"] / 1e3)
+        if n_pl:
+            e, _ = source_error(p, src_mixed, plain["src"], plain["ran"], floor=1e-10)
+            line["mixed_vs_plain_max_rel"] = e
     if rank == 0 and world == 1:
-        # the CPU leg: the oracle timed on a bounded sample, and used as the checker
-        # of the GPU sources against its FP64 run at rtol 1e-8
-        try:
-            v, n, dt = cpu_baseline(p, args.cpu_sample_s, os.cpu_count())
-            line["cpu_baseline"] = {"value": v, "unit": "triplets/s", "cores": os.cpu_count(), "kind": "port",
-                                    "sample": f"{n} triplets spread over the {n_trip}-triplet workload ({dt:.1f} s)"}
-        except Exception as e:  # noqa: BLE001
-            line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
-        if args.accuracy_sample > 0:
+        # the CPU leg: the oracle timed on a bounded sample (after the accuracy worker)
+        if acc is not None:
+            proc, items, out, t_start = acc
+            proc.join()
             try:
-                res = {"mixed": src_mixed}
-                if ms_plain is not None:
-                    res["plain_fp64"] = src_plain
-                errs, npick = accuracy_sample(p, res, args.accuracy_sample, os.cpu_count())
-                line["err_vs_fp64_oracle"] = dict(errs, sample_triplets=npick, oracle_rtol=1e-8,
-                                                  metric="max over source types and sampled triplets of "
-                                                         "max_tau|S - S_ref| / max_tau|S_ref|")
-            except Exception as e:  # noqa: BLE001
-                line["err_vs_fp64_oracle"] = {"error": str(e)[:200]}
+                r = np.load(out)
+                ref, stat = r["ref"], r["status"]
+                worst = {}
+                errs = {}
+                e, w = source_error(p, src_mixed, ref, items)
+                errs["mixed"], worst["mixed"] = e, w
+                if plain is not None:
+                    both = np.intersect1d(items, plain["ran"])
+                    if len(both):
+                        e, w = source_error(p, plain["src"], ref, both)
+                        errs["plain_fp64"], worst["plain_fp64"] = e, w
+                work = p.work_order()
+                tp = p.tp_list()
+                line["err_vs_fp64_oracle"] = dict(
+                    errs, sample_triplets=len(items), oracle_rtol=1e-8, bound=ERR_BOUND,
+                    within_bound=bool(errs["mixed"] <= ERR_BOUND and errs.get("plain_fp64", 0.0) <= ERR_BOUND),
+                    worst={k: {"source": list(tp[v[0]]), "triplet": list(work[v[1]])} for k, v in worst.items()},
+                    oracle_status_ok=bool(np.all(stat == 0)), oracle_seconds=float(r["seconds"]),
+                    metric="max over source types and sampled triplets of max_tau|S - S_ref| / max_tau|S_ref|",
+                    sample="for each m_max the cheapest triplet of the smallest, a middle and the largest l_max "
+                           "class, then triplets spread over the cost-sorted order without its top tenth")
+                if not line["err_vs_fp64_oracle"]["within_bound"]:
+                    line["status_ok"] = False
+            except (OSError, KeyError, ValueError) as ex:
+                line["err_vs_fp64_oracle"] = {"error": str(ex)[:200]}
+        try:
+            v, n, dt, stride = cpu_sample(p, args.cpu_sample, os.cpu_count())
+            line["cpu_baseline"] = {"value": v, "unit": "triplets/s", "cores": os.cpu_count(), "kind": "port",
+                                    "sample": f"{n} triplets, every {stride}-th of the cost-sorted "
+                                              f"{n_trip}-triplet workload, most expensive first ({dt:.1f} s)"}
+        except Exception as ex:  # noqa: BLE001
+            line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -192,6 +192,8 @@ typedef struct {
 typedef struct {
   int32_t status;
   int32_t n_steps, n_rejected, n_rhs, n_jac, n_lu, n_newton_fail, sources_calls;
+  int32_t retried;        /* song2_gpu_evolve: the triplet failed its first pass and was
+                             re-run in plain FP64 (the counters are the re-run's) */
 } song2_triplet_stats;
 
 typedef struct song2_ctx song2_ctx;
@@ -241,6 +243,43 @@ int song2_background_compute(const song2_cosmo *cosmo, int bg_size,
                              double *bg, double *bg_dd,
                              double *lntau0, double *dlntau,
                              double *tau0, double *a_eq, char *err);
+
+/* Table providers: the adapter from the caller's own first-order and background
+   modules (CLASS in the reference) to song2_tables.
+
+   A first-order provider has the shape of CLASS's perturb_song_sources_at_tau_and_k
+   as the reference calls it (perturbations2.c:9133-9163, 10217-10248,
+   10727-10762): it writes the first-order quantities of wavenumber k =
+   spec->k[index_k] at conformal time tau into out[0 .. n_provided - 1] in its own
+   order (CLASS: ppt->index_qs_*), interpolating its own time sampling
+   (ppt->tau_sampling_quadsources) as it does for the reference, and returns 0 on
+   success.  song2_first_order_from_provider samples it on the uniform ln(tau)
+   grid of fo_tau_size nodes from fo_lntau0 (step fo_dlntau), stores out[qs_map[q]]
+   as quantity q of enum song2_fo_index (qs_map has song2_fo_size(fo_l_max)
+   entries; -1 stores zero, for quantities the run never reads), computes the
+   spline second derivatives, and points tab's first-order fields at fo_out and
+   fo_dd_out (k_size * fo_tau_size * song2_fo_size(fo_l_max) doubles each).  For
+   CLASS, the map sends SONG2_FO_PHI to ppt->index_qs_phi, SONG2_FO_I + l to
+   ppt->index_qs_monopole_g + l, and so on; the grid should reach from before the
+   earliest start time (song2_start_time at the largest k) to tau0 with a step of
+   about 0.01 in ln tau.
+
+   A background provider writes the SONG2_BG_SIZE columns of enum song2_bg_column
+   at conformal time tau (from CLASS: background_at_tau and thermodynamics_at_z;
+   ln a, ln of the conformal Hubble rate a H, (aH)' tau^2, the logarithms of the
+   densities in CLASS units, ln kappa', and kappa = -ln(exp_m_kappa)).
+   song2_background_from_provider samples it on bg_size nodes uniform in ln tau
+   and points tab's background fields at bg_out and bg_dd_out
+   (bg_size * SONG2_BG_SIZE doubles each); the caller sets tab->tau0, a_eq and
+   tau_free_streaming.  Both return 0, or 1 with a message. */
+typedef int (*song2_fo_provider)(void *user, int index_k, double k, double tau, double *out);
+typedef int (*song2_bg_provider)(void *user, double tau, double *columns);
+int song2_first_order_from_provider(const song2_spec *spec, int fo_l_max, int fo_tau_size, double fo_lntau0,
+                                    double fo_dlntau, song2_fo_provider provider, void *user, int n_provided,
+                                    const int *qs_map, double *fo_out, double *fo_dd_out, song2_tables *tab,
+                                    char *err);
+int song2_background_from_provider(int bg_size, double bg_lntau0, double bg_dlntau, song2_bg_provider provider,
+                                   void *user, double *bg_out, double *bg_dd_out, song2_tables *tab, char *err);
 
 /* Natural cubic spline second derivatives in x on a uniform grid, column-wise:
    y[n][ncol] -> dd[n][ncol]. */
@@ -306,6 +345,13 @@ void song2_ctx_get_launch(song2_ctx *ctx, song2_launch *out, int *grid, int *blo
    expensive triplets (largest max(k1,k2,k3)) and returns the fastest. */
 int song2_autotune(const song2_spec *spec, const song2_tables *tab, int precision, int sample,
                    song2_launch *best, double *best_ms, char *err);
+/* Same, restricted to the given triplets (indices in the reference work order:
+   k1 descending, k2 <= k1, k3 ascending); spec may differ from the run's in its
+   integrator fields (rtol, max_steps).  The flat source buffer keeps the full
+   layout; the entries of the other triplets stay 0.  No counterpart in the
+   reference (its re-runs go through what_if_ndf15_fails, perturbations2.c:12877-12957). */
+int song2_ctx_create_list(const song2_spec *spec, const song2_tables *tab, int precision, const int64_t *items,
+                          int64_t n_items, song2_ctx **out, char *err);
 /* Same, restricted to the triplets of song2_shard_items(spec, shard, n_shards);
    the flat source buffer keeps the full layout, entries of other shards stay 0. */
 int song2_ctx_create_shard(const song2_spec *spec, const song2_tables *tab, int precision,
@@ -315,6 +361,15 @@ int song2_ctx_destroy(song2_ctx *ctx);
 /* Evolve every triplet on the device and leave the sources in device memory.
    stream may be NULL (legacy default stream).  Blocking on return. */
 int song2_ctx_run(song2_ctx *ctx, void *stream, char *err);
+/* Evolve only part `part` of n_parts of the context's triplets: every launch
+   group's cost-sorted work list is dealt round-robin into n_parts parts, so the
+   parts carry similar work.  The sources of the part's triplets are written into
+   the context's flat buffer (the other entries keep their values), so n_parts
+   calls with part = 0..n_parts-1 fill the whole buffer.  The first call with a
+   new n_parts regroups the device work list and clears the per-triplet stats.
+   Blocking on return; song2_ctx_last_kernel_ms() gives the part's device time.
+   No counterpart in the reference (its OpenMP loop runs every triplet at once). */
+int song2_ctx_run_part(song2_ctx *ctx, int part, int n_parts, void *stream, char *err);
 /* As song2_ctx_run, with the run's stream work (queue resets and the evolver
    launches of every launch group) captured into a CUDA graph on the first call
    and replayed on the later ones (no counterpart in the reference). */
@@ -330,33 +385,48 @@ int song2_ctx_download(song2_ctx *ctx, double *flat_sources_host,
 double song2_ctx_last_kernel_ms(song2_ctx *ctx);
 int song2_ctx_last_launches(song2_ctx *ctx);
 
+/* Diagnostics of builds compiled with -DSONG2_PHASE_TIMERS (no counterpart in
+   the reference): the SM clock cycles and the number of visits of each evolver
+   phase, summed over the runs of the context so far, as out[2*phase] and
+   out[2*phase+1] (out holds n >= 48 entries).  Returns the number of phases, or
+   0 for a build without the timers. */
+int song2_ctx_phase_cycles(song2_ctx *ctx, unsigned long long *out, int n);
+
 /* One-shot drop-in for the reference's triplet loop: creates a context,
    evolves every triplet and scatters the result into the caller-allocated
-   ppt2->sources slabs sources[tp2][k1][k2][tau*k3_size+k3]. */
+   ppt2->sources slabs sources[tp2][k1][k2][tau*k3_size+k3].  Triplets whose
+   first pass retires with an error status are evolved again, in plain FP64 with
+   eight times spec.max_steps (the exit strategy of what_if_ndf15_fails,
+   perturbations2.c:12877-12957, which re-integrates a failed triplet with another
+   evolver and stops the run if that fails too); their stats carry retried = 1.
+   Returns 1 if a triplet still fails, with its index and status in err. */
 int song2_gpu_evolve(const song2_spec *spec, const song2_tables *tab, int precision,
                      double ****sources_out, song2_triplet_stats *per_triplet,
                      char *err);
 
 /* Allocation-free evolver, for callers that cannot allocate device memory:
-   code running inside a CUDA stream capture that must not add allocation nodes,
-   applications whose device memory is owned by a fixed-size pool or another
-   runtime, or hosts that forbid cudaMalloc after start-up.  It has no
-   counterpart in the reference.  It performs no cudaMalloc, cudaFree or other
-   device allocation: all its device-side scratch (layout tables, work list,
-   work-queue counter, Jacobian and LU blocks) lives in one 64 MiB array
-   compiled into this library, which every GPU that loads the library holds
-   until the process exits.  Problems whose tables do not fit are rejected with
-   an error; the number of resident triplets is reduced to fit the
-   iteration-matrix blocks.  The caller passes the inputs and outputs on the
-   device: tab_dev is a song2_tables whose bg, bg_dd, fo and fo_dd point to
-   device memory (spec and its k/k3/tau grids stay in host memory);
+   applications whose device memory is owned by a fixed-size pool or by another
+   runtime (a framework's caching allocator, a solver that reserves the GPU's
+   memory at start-up), or hosts that forbid cudaMalloc after initialisation.  It
+   has no counterpart in the reference.  It calls no cudaMalloc, cudaFree or other
+   allocating routine: its device scratch (layout tables, work list, work-queue
+   counter, the per-triplet Jacobians and quadratic-source tables) lives in one
+   64 MiB array compiled into this library, which every GPU that loads the library
+   holds until the process exits.  (As for any kernel, the CUDA driver may reserve
+   local memory for the evolver's stack frame at its first launch on a device.)
+   Problems whose tables do not fit are rejected with an error, and fewer
+   triplets run at once when their per-triplet scratch does not all fit.  The
+   caller passes the inputs and outputs on the device: tab_dev is a song2_tables
+   whose bg, bg_dd, fo and fo_dd point to device memory (spec and its k/k3/tau
+   grids stay in host memory and may be freed when the call returns);
    sources_dev holds tp2_size * song2_sources_per_type() doubles (cleared by the
-   call) and stats_dev song2_n_triplets() entries, in the evolver's internal
-   (cost-sorted) triplet order.  Work is enqueued on `stream` (NULL = legacy
-   default stream) and the outputs are valid once it has completed.  The first
-   call on a device resolves the scratch address with that device current; make
-   that first call before any stream capture.  Calls share the scratch: two
-   calls that overlap on the GPU race and corrupt each other's results. */
+   call) and stats_dev song2_n_triplets() entries in the reference work order (k1
+   descending, k2 <= k1, k3 ascending).  Work is enqueued on `stream` (NULL =
+   legacy default stream) and the outputs are valid once it has completed.  The
+   first call on a device resolves the scratch address with that device current.
+   Calls share the scratch and find the previous call's contents in it (each call
+   clears what must start at zero): two calls that overlap on the GPU race and
+   corrupt each other's results. */
 int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tables *tab_dev, int precision,
                              double *sources_dev, song2_triplet_stats *stats_dev, void *stream,
                              char *err);

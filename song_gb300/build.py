@@ -23,6 +23,7 @@ CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall"]
 
 C_SOURCES = ["song2_host.c"]
 CU_SOURCES = ["song2_k_block_f.cu", "song2_k_block_d.cu", "song2_k_class_f.cu", "song2_k_class_d.cu",
+              "song2_k_class2_f.cu", "song2_k_class2_d.cu",
               "song2_k_warp_f.cu", "song2_k_warp_d.cu", "song2_k_team_f.cu", "song2_k_team_d.cu",
               "song2_launch.cu", "song2_capi.cu"]
 
@@ -42,41 +43,48 @@ def _run(cmd, log):
     return p.stdout
 
 
-def sources_newer_than_lib():
-    if not os.path.exists(LIB):
+# Diagnostic variant: the same library with the evolver's per-phase cycle
+# counters compiled in (song2_ctx_phase_cycles), built into its own directory.
+PHASE_OUT = os.path.join(HERE, "_build_phase")
+
+
+def sources_newer_than_lib(lib=LIB):
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INC, "song2.h")]
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False):
-    if not force and not sources_newer_than_lib():
-        return LIB
-    os.makedirs(OUT, exist_ok=True)
+def build(force=False, verbose=False, phase_timers=False):
+    out = PHASE_OUT if phase_timers else OUT
+    lib = os.path.join(out, "libsong2.so")
+    if not force and not sources_newer_than_lib(lib):
+        return lib
+    os.makedirs(out, exist_ok=True)
+    extra = ["-DSONG2_PHASE_TIMERS"] if phase_timers else []
     nvcc = _nvcc()
     jobs = []
     objs = []
     for f in C_SOURCES:
-        o = os.path.join(OUT, f + ".o")
+        o = os.path.join(out, f + ".o")
         objs.append(o)
         jobs.append((["gcc", *CC_FLAGS, "-I", INC, "-c", os.path.join(CSRC, f), "-o", o], o + ".log"))
     for f in CU_SOURCES:
-        o = os.path.join(OUT, f + ".o")
+        o = os.path.join(out, f + ".o")
         objs.append(o)
-        jobs.append(([nvcc, *ARCH, *NVCC_FLAGS, "-I", INC, "-I", CSRC, "-c", os.path.join(CSRC, f), "-o", o],
-                     o + ".log"))
+        jobs.append(([nvcc, *ARCH, *NVCC_FLAGS, *extra, "-I", INC, "-I", CSRC, "-c", os.path.join(CSRC, f),
+                      "-o", o], o + ".log"))
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         outs = list(ex.map(lambda j: _run(*j), jobs))
     if verbose:
         for o in outs:
             print(o)
-    tmp = LIB + ".tmp"
-    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lm"], os.path.join(OUT, "link.log"))
-    os.replace(tmp, LIB)
-    return LIB
+    tmp = lib + ".tmp"
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lm"], os.path.join(out, "link.log"))
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
-    print(LIB)
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, phase_timers="--phase-timers" in sys.argv))

@@ -103,12 +103,12 @@ class Launch(C.Structure):
 class TripletStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("n_steps", C.c_int32), ("n_rejected", C.c_int32),
                 ("n_rhs", C.c_int32), ("n_jac", C.c_int32), ("n_lu", C.c_int32),
-                ("n_newton_fail", C.c_int32), ("sources_calls", C.c_int32)]
+                ("n_newton_fail", C.c_int32), ("sources_calls", C.c_int32), ("retried", C.c_int32)]
 
 
 STATS_DTYPE = np.dtype([("status", np.int32), ("n_steps", np.int32), ("n_rejected", np.int32),
                         ("n_rhs", np.int32), ("n_jac", np.int32), ("n_lu", np.int32),
-                        ("n_newton_fail", np.int32), ("sources_calls", np.int32)])
+                        ("n_newton_fail", np.int32), ("sources_calls", np.int32), ("retried", np.int32)])
 
 # Every extern "C" symbol declared in include/song2.h, with its ctypes signature.
 _P = C.c_void_p
@@ -127,6 +127,10 @@ SIGNATURES = {
     "song2_spec_defaults": (None, [C.POINTER(Spec)]),
     "song2_background_compute": (_I, [C.POINTER(Cosmo), _I, _PD, _PD, _PD, _PD, _PD, _PD, C.c_char_p]),
     "song2_spline_uniform": (None, [_I, _I, _D, _PD, _PD]),
+    "song2_first_order_from_provider": (_I, [C.POINTER(Spec), _I, _I, _D, _D, C.c_void_p, C.c_void_p, _I, _PI,
+                                             _PD, _PD, C.POINTER(Tables), C.c_char_p]),
+    "song2_background_from_provider": (_I, [_I, _D, _D, C.c_void_p, C.c_void_p, _PD, _PD, C.POINTER(Tables),
+                                            C.c_char_p]),
     "song2_coupling_c_minus": (_D, [_I, _I, _I]),
     "song2_coupling_c_plus": (_D, [_I, _I, _I]),
     "song2_coupling_d_minus": (_D, [_I, _I, _I]),
@@ -141,6 +145,8 @@ SIGNATURES = {
     "song2_shard_items": (C.c_int64, [C.POINTER(Spec), _I, _I, C.POINTER(C.c_int64)]),
     "song2_ctx_create": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.POINTER(_P), C.c_char_p]),
     "song2_ctx_create_shard": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _I, C.POINTER(_P), C.c_char_p]),
+    "song2_ctx_create_list": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.POINTER(C.c_int64), C.c_int64,
+                                   C.POINTER(_P), C.c_char_p]),
     "song2_ctx_create_ex": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.c_void_p, _I, _I, C.POINTER(_P),
                                  C.c_char_p]),
     "song2_ctx_get_launch": (None, [_P, C.c_void_p, C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_size_t)]),
@@ -148,11 +154,13 @@ SIGNATURES = {
     "song2_ctx_destroy": (_I, [_P]),
     "song2_ctx_run": (_I, [_P, _P, C.c_char_p]),
     "song2_ctx_run_graph": (_I, [_P, _P, C.c_char_p]),
+    "song2_ctx_run_part": (_I, [_P, _I, _I, _P, C.c_char_p]),
     "song2_ctx_device_sources": (_P, [_P]),
     "song2_ctx_device_stats": (_P, [_P]),
     "song2_ctx_download": (_I, [_P, _PD, C.POINTER(TripletStats), C.c_char_p]),
     "song2_ctx_last_kernel_ms": (_D, [_P]),
     "song2_ctx_last_launches": (_I, [_P]),
+    "song2_ctx_phase_cycles": (_I, [_P, C.POINTER(C.c_uint64), _I]),
     "song2_gpu_evolve": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _P, C.POINTER(TripletStats),
                               C.c_char_p]),
     "song2_gpu_evolve_noalloc": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -161,9 +169,24 @@ SIGNATURES = {
 }
 
 
-def bind(lib):
+# callback types of the table providers (song2_fo_provider, song2_bg_provider)
+FO_PROVIDER = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double))
+BG_PROVIDER = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, C.POINTER(C.c_double))
+
+
+def bind(lib, host_only=False):
+    """Set the ctypes signatures of the entry points; host_only binds just the
+    host-side functions that a library exports (a CPU-only build of the input
+    provider, which carries no GPU entry points)."""
     for name, (res, args) in SIGNATURES.items():
-        f = getattr(lib, name)
+        if host_only and ("_ctx_" in name or "_gpu_" in name or name == "song2_autotune"):
+            continue
+        try:
+            f = getattr(lib, name)
+        except AttributeError:
+            if host_only:
+                continue
+            raise
         f.restype = res
         f.argtypes = args
     return lib
@@ -172,9 +195,13 @@ def bind(lib):
 _lib = None
 
 
-def load(path=LIB_PATH):
-    """Load the in-tree product library (build it with song_gb300.build.build())."""
+def load(path=None):
+    """Load the in-tree product library (build it with song_gb300.build.build()).
+    SONG2_LIB names another build of the same library (the phase-timer build of
+    song_gb300.build, for instance)."""
     global _lib
+    if path is None:
+        path = os.environ.get("SONG2_LIB") or LIB_PATH
     if _lib is None:
         if not os.path.exists(path):
             raise RuntimeError(f"song2 library not built: {path} is missing (run song_gb300.build.build())")

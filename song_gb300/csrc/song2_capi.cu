@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "song2_internal.h"
@@ -42,8 +43,15 @@ struct song2_ctx {
   struct Group {
     int first, count, grid;
     size_t smem;
+    int mode;   /* kernel of the group (song2_launch_evolver's mode) */
   };
   std::vector<Group> groups;
+  /* host copy of the device work list (launch-group order) and, after
+     song2_ctx_run_part, its split into parts: part q of group g is the range
+     part_first[g * parts + q], part_count[...] */
+  std::vector<WorkItem> h_items;
+  int parts = 0;
+  std::vector<int> part_first, part_count;
   /* song2_ctx_run_graph: the run's memsets and launches captured once */
   cudaStream_t cap_stream = nullptr;
   cudaGraph_t graph = nullptr;
@@ -71,7 +79,8 @@ int size_l_indexm(int l_max, const int *m, int m_size) {
 
 struct HostLayout {
   DevSpec s;
-  std::vector<short> eq_sp, eq_l, eq_m, idx_I, idx_E, idx_B, idx_N, qs_sp, qs_l, qs_m, row_slot, qs_slot;
+  std::vector<short> eq_sp, eq_l, eq_m, idx_I, idx_E, idx_B, idx_N, qs_sp, qs_l, qs_m, row_slot, qs_slot, qo_slot, mx_idx,
+      mx_pos;
   std::vector<double> cmin, cplu, dmin, dplu, dzer;
 };
 
@@ -155,6 +164,20 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
     s.rsa_k = sp->radiation_streaming_trigger_tau_over_tau_k;
     s.tau_fs = tab->tau_free_streaming;
   }
+  /* closure coefficients at l_max (the same expressions as the closure rows of
+     perturb2_derivs, evaluated once per hierarchy class instead of per right-hand side) */
+  for (int mm = 0; mm < SONG2_MAX_M; ++mm) {
+    auto c_in = [&](int l) {
+      return l <= mm ? 0.0 : (mm == 0 ? (2.0 * l + 1) / (2.0 * l - 1) : sqrt((double)(l + mm) / (l - mm)) * (2.0 * l + 1) / (2.0 * l - 1));
+    };
+    s.cl_I[mm] = c_in(s.l_max_g);
+    s.cl_N[mm] = c_in(s.l_max_ur);
+    int lp = s.l_max_pol;
+    s.cl_P[mm] = lp > 2 ? sqrt(std::max(0.0, 1 - ((double)mm * mm) / ((double)lp * lp) * (lp + 2) / (lp - 2.0))) *
+                              (2.0 * lp + 1) / (2.0 * lp - 1)
+                        : 0.0;
+    s.cmix_P[mm] = lp > 0 ? (double)mm / lp : 0.0;
+  }
   for (int l = 0; l < S2_LMAXP; ++l) {
     s.index_m_max[l] = -1;
     for (int i = 0; i < s.m_size; ++i)
@@ -194,6 +217,10 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   s.los_exp_pot = sp->use_exponential_potentials;
   s.rtol = sp->rtol;
   s.threshold = sp->threshold;
+  if (!(sp->threshold >= 1e-30 && sp->threshold <= 1e30) || !(sp->rtol > 0)) {
+    snprintf(err, SONG2_ERRLEN, "rtol must be positive and threshold in [1e-30, 1e30]");
+    return 1;
+  }
   s.max_steps = sp->max_steps;
   s.start_h = sp->start_small_k_at_tau_c_over_tau_h;
   s.start_k = sp->start_large_k_at_tau_h_over_tau_k;
@@ -274,11 +301,81 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   }
   s.n = ni;
   if (s.n > 32767) { snprintf(err, SONG2_ERRLEN, "system too large"); return 1; }
+  /* structured iteration matrix of every block: the core (every entry that is not
+     a hierarchy moment with l >= 3) and the moment chains I, E (paired with B where
+     the block has B) and N over l >= 3.  A moment with l >= 3 couples only to the
+     same species at l - 1, l, l + 1 (and E to B at the same l), so each chain is
+     block tridiagonal, and its first node couples to the core's l = 2 moments. */
+  H.mx_idx.clear();
+  H.mx_pos.assign(s.n, 0);
   int off = 0;
   for (int b = 0; b < s.nblk; ++b) {
-    s.lu_off[b] = off;
-    off += s.blk_size[b] * s.blk_size[b];
+    int b0 = s.blk_start[b], nb = s.blk_size[b];
+    std::vector<int> core;
+    /* chain 0: I, 1: E/B, 2: N; per chain the state indices of (l, component) */
+    std::vector<std::vector<std::pair<int, int>>> chain(3);
+    for (int i = b0; i < b0 + nb; ++i) {
+      int sp_ = H.eq_sp[i], l = H.eq_l[i];
+      int ch = sp_ == SP_I ? 0 : (sp_ == SP_E || sp_ == SP_B) ? 1 : sp_ == SP_N ? 2 : -1;
+      if (ch < 0 || l <= 2) core.push_back(i);
+      else chain[ch].push_back({l, i});
+    }
+    if ((int)core.size() > S2_MAXCORE) {
+      snprintf(err, SONG2_ERRLEN, "core of block m=%d has %d entries (max %d)", s.m[b], (int)core.size(), S2_MAXCORE);
+      return 1;
+    }
+    s.core_n[b] = (int)core.size();
+    s.core_idx[b] = (int)H.mx_idx.size();
+    for (size_t p = 0; p < core.size(); ++p) {
+      H.mx_idx.push_back((short)core[p]);
+      H.mx_pos[core[p]] = (short)p;
+    }
+    int nch = 0;
+    for (int ch = 0; ch < 3; ++ch) {
+      if (chain[ch].empty()) continue;
+      auto &v = chain[ch];
+      int lfirst = v.front().first, llast = v.back().first;
+      int len = llast - lfirst + 1;
+      int d = (int)v.size() / len;
+      if ((d != 1 && d != 2) || (int)v.size() != d * len) {
+        snprintf(err, SONG2_ERRLEN, "moment chain %d of block m=%d is not regular", ch, s.m[b]);
+        return 1;
+      }
+      s.ch_d[b][nch] = d;
+      s.ch_len[b][nch] = len;
+      s.ch_idx[b][nch] = (int)H.mx_idx.size();
+      /* node k holds l = lfirst + k; component 0 is I, E or N, component 1 is B */
+      std::vector<short> nodes((size_t)len * d, -1);
+      for (auto &e : v) {
+        int k = e.first - lfirst, comp = H.eq_sp[e.second] == SP_B ? 1 : 0;
+        nodes[(size_t)k * d + comp] = (short)e.second;
+        H.mx_pos[e.second] = (short)(((nch + 1) << 8) | (comp << 7) | k);
+      }
+      for (short x : nodes) {
+        if (x < 0) {
+          snprintf(err, SONG2_ERRLEN, "moment chain %d of block m=%d has a gap", ch, s.m[b]);
+          return 1;
+        }
+        H.mx_idx.push_back(x);
+      }
+      s.ch_off[b][nch] = off;
+      off += 3 * d * d * len + 2 * d * s.core_n[b];
+      ++nch;
+    }
+    s.ch_n[b] = nch;
+    s.core_off[b] = off;
+    off += s.core_n[b] * s.core_n[b];
   }
+  if ((int)H.mx_idx.size() != s.n) {
+    snprintf(err, SONG2_ERRLEN, "iteration-matrix structure does not cover the state");
+    return 1;
+  }
+  s.n_ch1 = s.n_ch2 = 0;
+  for (int b = 0; b < s.nblk; ++b)
+    for (int ch = 0; ch < s.ch_n[b]; ++ch) {
+      if (s.ch_d[b][ch] == 1) s.ch1[s.n_ch1++] = (short)(b << 4 | ch);
+      else s.ch2[s.n_ch2++] = (short)(b << 4 | ch);
+    }
   s.lu_elems = off;
 
   /* evaluation order of the rows and of the quadratic-source entries: the
@@ -295,6 +392,7 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
       if (f >= 0) rest.push_back(f);
     for (size_t i = 0; i < sp_of.size(); ++i) {
       int sp_ = sp_of[i];
+      if (sp_ == SP_NONE) continue;
       bool hier = false;
       for (int u = 0; u < 4; ++u) hier |= sp_ == cls_sp[u];
       bool listed = false;
@@ -330,8 +428,22 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   slots(H.eq_sp, {s.idx_phip}, H.row_slot);
   slots(H.qs_sp, {s.iq_psi, s.iq_phi_prime_prime, s.iq_phi_prime_longitudinal, s.iq_phi_prime_poisson,
                   s.iq_omega_m1_prime, s.iq_gamma_m2_prime_prime, s.iq_vv_g}, H.qs_slot);
+  /* the entries the source functions and the workspace read at an output time:
+     the hierarchy moments up to l = max(2, l_max_los_t, l_max_los_p), the matter and
+     the metric entries (perturb2_sources recomputes only what it uses) */
+  {
+    int lo = std::max(2, std::max(sp->l_max_los_t, sp->l_max_los_p));
+    std::vector<short> sp_out(H.qs_sp);
+    for (size_t i = 0; i < sp_out.size(); ++i) {
+      int sp_ = sp_out[i];
+      if ((sp_ == SP_I || sp_ == SP_E || sp_ == SP_B || sp_ == SP_N) && H.qs_l[i] > lo) sp_out[i] = SP_NONE;
+    }
+    slots(sp_out, {s.iq_psi, s.iq_phi_prime_prime, s.iq_phi_prime_longitudinal, s.iq_phi_prime_poisson,
+                   s.iq_omega_m1_prime, s.iq_gamma_m2_prime_prime, s.iq_vv_g}, H.qo_slot);
+  }
   s.n_row_slots = (int)H.row_slot.size();
   s.n_qs_slots = (int)H.qs_slot.size();
+  s.n_qo_slots = (int)H.qo_slot.size();
 
   /* coupling tables for l <= Lq */
   H.cmin.assign((size_t)s.n_lm * 3, 0.0); H.cplu = H.cmin; H.dmin = H.cmin; H.dplu = H.cmin; H.dzer = H.cmin;
@@ -636,7 +748,7 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     return 1;
   }
   c->launch = L;
-  int per_sm = song2_max_ctas_per_sm(precision, classes ? 3 : L.warp_team, c->block, c->smem);
+  int per_sm = song2_max_ctas_per_sm(precision, classes ? 4 : L.warp_team, c->block, c->smem);
   if (per_sm < 1) {
     snprintf(err, SONG2_ERRLEN, "launch configuration does not fit on an SM");
     return 1;
@@ -653,26 +765,29 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
       if (!small_cls[w.cls]) { big.push_back(w); smem_big = std::max(smem_big, pb[w.cls]); }
       else { small.push_back(w); smem_small = std::max(smem_small, pb[w.cls]); }
     }
-    if (!big.empty() && !small.empty()) {
-      gitems = big;
-      gitems.insert(gitems.end(), small.begin(), small.end());
-      int nt = 0;
-      for (int g = 0; g < 2; ++g) {
-        song2_ctx::Group G;
-        G.first = g == 0 ? 0 : (int)big.size();
-        G.count = g == 0 ? (int)big.size() : (int)small.size();
-        G.smem = g == 0 ? smem_big : smem_small;
-        int ps = song2_max_ctas_per_sm(precision, 3, c->block, G.smem);
-        if (ps < 1) {
-          snprintf(err, SONG2_ERRLEN, "launch configuration does not fit on an SM");
-          return 1;
-        }
-        G.grid = std::max(1, std::min(G.count, nsm * ps));
-        nt = std::max(nt, G.grid);
-        c->groups.push_back(G);
+    /* the classes with large plans first (one CTA per SM, the kernel with the
+       registers of a full SM), then the small ones (two CTAs per SM, the kernel
+       whose registers allow two) */
+    gitems = big;
+    gitems.insert(gitems.end(), small.begin(), small.end());
+    int nt = 0;
+    for (int g = 0; g < 2; ++g) {
+      song2_ctx::Group G;
+      G.first = g == 0 ? 0 : (int)big.size();
+      G.count = g == 0 ? (int)big.size() : (int)small.size();
+      if (G.count == 0) continue;
+      G.smem = g == 0 ? smem_big : smem_small;
+      G.mode = g == 0 ? 3 : 4;
+      int ps = song2_max_ctas_per_sm(precision, G.mode, c->block, G.smem);
+      if (ps < 1) {
+        snprintf(err, SONG2_ERRLEN, "launch configuration does not fit on an SM");
+        return 1;
       }
-      c->n_teams = nt;
+      G.grid = std::max(1, std::min(G.count, nsm * ps));
+      nt = std::max(nt, G.grid);
+      c->groups.push_back(G);
     }
+    c->n_teams = nt;
   }
 
   cudaStream_t st = 0;
@@ -717,7 +832,10 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   if (upload(c, H.qs_sp, &p.tabs.qs_sp, st, err) || upload(c, H.qs_l, &p.tabs.qs_l, st, err) || upload(c, H.qs_m, &p.tabs.qs_m, st, err))
     return 1;
   if (upload(c, H.row_slot, &p.tabs.row_slot, st, err) || upload(c, H.qs_slot, &p.tabs.qs_slot, st, err)) return 1;
+  if (upload(c, H.mx_idx, &p.tabs.mx_idx, st, err) || upload(c, H.mx_pos, &p.tabs.mx_pos, st, err)) return 1;
+  if (upload(c, H.qo_slot, &p.tabs.qo_slot, st, err)) return 1;
   if (upload(c, gitems, &p.items, st, err)) return 1;
+  c->h_items = gitems;
   if (classes) {
     /* per-class specs (run-level fields from the run-wide spec) and tables */
     std::vector<DevSpec> cspec;
@@ -740,7 +858,8 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
           upload(c, hc.idx_B, &t.idx_B, st, err) || upload(c, hc.idx_N, &t.idx_N, st, err) ||
           upload(c, hc.qs_sp, &t.qs_sp, st, err) || upload(c, hc.qs_l, &t.qs_l, st, err) ||
           upload(c, hc.qs_m, &t.qs_m, st, err) || upload(c, hc.row_slot, &t.row_slot, st, err) ||
-          upload(c, hc.qs_slot, &t.qs_slot, st, err))
+          upload(c, hc.qs_slot, &t.qs_slot, st, err) || upload(c, hc.mx_idx, &t.mx_idx, st, err) ||
+          upload(c, hc.mx_pos, &t.mx_pos, st, err) || upload(c, hc.qo_slot, &t.qo_slot, st, err))
         return 1;
       ctabs.push_back(t);
     }
@@ -785,11 +904,6 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
     if (alloc_dev(c, (size_t)c->n_teams * s.lu_stride * ts, &tmp, err)) return 1;
     p.lu_global = tmp;
-    if (precision == SONG2_PREC_MIXED && L.warp_team != 2) {
-      /* the explicit inverse of the FP32 blocks */
-      if (alloc_dev(c, (size_t)c->n_teams * s.lu_stride * sizeof(float), &tmp, err)) return 1;
-      p.minv_global = (float *)tmp;
-    }
   }
   if (L.warp_team == 2) {
     /* team kernel: vectors, solve vectors and pivots of every resident team */
@@ -798,12 +912,15 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     p.tslab = (double *)tmp;
     if (alloc_dev(c, (size_t)c->n_teams * s.n * ts, &tmp, err)) return 1;
     p.txsol = tmp;
-    if (alloc_dev(c, (size_t)c->n_teams * s.n * sizeof(int), &tmp, err)) return 1;
-    p.tpiv = (int *)tmp;
   }
   if (alloc_dev(c, sizeof(int), &tmp, err)) return 1;
   c->d_queue = (int *)tmp;
   p.queue = c->d_queue;
+#ifdef SONG2_PHASE_TIMERS
+  if (alloc_dev(c, 2 * S2_NPHASE * sizeof(unsigned long long), &tmp, err)) return 1;
+  CK(cudaMemsetAsync(tmp, 0, 2 * S2_NPHASE * sizeof(unsigned long long), st));
+  p.phase = (unsigned long long *)tmp;
+#endif
   CK(cudaStreamSynchronize(st));
   c->spec = s;
   CK(cudaEventCreate(&c->ev0));
@@ -841,7 +958,7 @@ static void sorted_items(const song2_spec *spec, const std::vector<double> &k3, 
         /* hierarchy class of an uneven batch (triplets numbered in pair order) */
         int has_cls = spec->n_classes > 0 && spec->triplet_class && spec->class_l_max && spec->class_m_max;
         int cls = has_cls ? spec->triplet_class[k3_off[pair] + i3] : 0;
-        items.push_back(WorkItem{i1, i2, i3, pair, cls});
+        items.push_back(WorkItem{i1, i2, i3, pair, cls, 0});
         double kk = std::max(spec->k[i1], std::max(spec->k[i2], k3[k3_off[pair] + i3]));
         /* cost: steps grow with k; per-step work with the class's hierarchy size */
         if (has_cls && cls >= 0 && cls < spec->n_classes)
@@ -866,6 +983,7 @@ static void sorted_items(const song2_spec *spec, const std::vector<double> &k3, 
   for (size_t i = 0; i < order.size(); ++i) {
     sorted[i] = items[order[i]];
     ref_index[i] = start[sorted[i].pair] + sorted[i].i3;
+    sorted[i].ref = (int)ref_index[i];
   }
 }
 
@@ -890,7 +1008,8 @@ int64_t song2_shard_items(const song2_spec *spec, int shard, int n_shards, int64
 }
 
 static int ctx_create_impl(const song2_spec *spec, const song2_tables *tab, int precision, const song2_launch *launch,
-                           int shard, int n_shards, song2_ctx **out, char *err) {
+                           int shard, int n_shards, song2_ctx **out, char *err, const int64_t *list = nullptr,
+                           int64_t n_list = -1) {
   *out = nullptr;
   if (n_shards < 1 || shard < 0 || shard >= n_shards) {
     snprintf(err, SONG2_ERRLEN, "bad shard %d of %d", shard, n_shards);
@@ -910,7 +1029,25 @@ static int ctx_create_impl(const song2_spec *spec, const song2_tables *tab, int 
   std::vector<WorkItem> sorted, mine;
   std::vector<int64_t> ref;
   sorted_items(spec, k3, k3_off, k3_size, sorted, ref);
-  for (size_t i = shard; i < sorted.size(); i += n_shards) mine.push_back(sorted[i]);
+  if (list) {
+    /* an explicit list of reference work-order indices, kept in cost order */
+    std::vector<char> want(sorted.size(), 0);
+    for (int64_t i = 0; i < n_list; ++i) {
+      if (list[i] < 0 || list[i] >= (int64_t)sorted.size()) {
+        snprintf(err, SONG2_ERRLEN, "triplet index %lld outside 0..%zu", (long long)list[i], sorted.size() - 1);
+        return 1;
+      }
+      want[list[i]] = 1;
+    }
+    for (size_t i = 0; i < sorted.size(); ++i)
+      if (want[ref[i]]) mine.push_back(sorted[i]);
+    if (mine.empty()) {
+      snprintf(err, SONG2_ERRLEN, "empty triplet list");
+      return 1;
+    }
+  } else {
+    for (size_t i = shard; i < sorted.size(); i += n_shards) mine.push_back(sorted[i]);
+  }
   song2_ctx *c = new song2_ctx();
   memset((void *)&c->spec, 0, sizeof(c->spec));
   if (launch) c->launch = *launch;
@@ -929,6 +1066,15 @@ int song2_ctx_create(const song2_spec *spec, const song2_tables *tab, int precis
 int song2_ctx_create_shard(const song2_spec *spec, const song2_tables *tab, int precision, int shard, int n_shards,
                            song2_ctx **out, char *err) {
   return ctx_create_impl(spec, tab, precision, nullptr, shard, n_shards, out, err);
+}
+
+int song2_ctx_create_list(const song2_spec *spec, const song2_tables *tab, int precision, const int64_t *items,
+                          int64_t n_items, song2_ctx **out, char *err) {
+  if (!items || n_items < 1) {
+    snprintf(err, SONG2_ERRLEN, "empty triplet list");
+    return 1;
+  }
+  return ctx_create_impl(spec, tab, precision, nullptr, 0, 1, out, err, items, n_items);
 }
 
 int song2_ctx_create_ex(const song2_spec *spec, const song2_tables *tab, int precision, const song2_launch *launch,
@@ -1003,6 +1149,34 @@ int song2_ctx_destroy(song2_ctx *c) {
   return 0;
 }
 
+/* the stream work of a part of a run: for every launch group, the items
+   [first, first + count) of the work list, one launch each */
+static int enqueue_part(song2_ctx *c, int part, cudaStream_t st, char *err) {
+  int ng = c->groups.empty() ? 1 : (int)c->groups.size();
+  c->last_launches = 0;
+  for (int g = 0; g < ng; ++g) {
+    int first = c->part_first[g * c->parts + part], count = c->part_count[g * c->parts + part];
+    if (count == 0) continue;
+    int grid = c->groups.empty() ? c->grid : c->groups[g].grid;
+    size_t smem = c->groups.empty() ? c->smem : c->groups[g].smem;
+    int per_cta = c->groups.empty() ? c->launch.teams_per_cta : 1;
+    int mode = c->groups.empty() ? c->launch.warp_team : c->groups[g].mode;
+    grid = std::max(1, std::min(grid, (count + per_cta - 1) / per_cta));
+    DevSpec sg = c->spec;
+    sg.n_items = count;
+    DevPtrs pg = c->ptrs;
+    pg.items = c->ptrs.items + first;
+    pg.stats = c->ptrs.stats + first;
+    CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
+    if (song2_launch_evolver(sg, pg, c->precision, mode, grid, c->block, smem, st)) {
+      snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return 1;
+    }
+    c->last_launches++;
+  }
+  return 0;
+}
+
 /* the stream work of one run: queue resets and the evolver launch(es) */
 static int enqueue_run(song2_ctx *c, cudaStream_t st, char *err) {
   CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
@@ -1020,7 +1194,7 @@ static int enqueue_run(song2_ctx *c, cudaStream_t st, char *err) {
       pg.items = c->ptrs.items + G.first;
       pg.stats = c->ptrs.stats + G.first;
       if (G.first > 0) CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
-      if (song2_launch_evolver(sg, pg, c->precision, c->launch.warp_team, G.grid, c->block, G.smem, st)) {
+      if (song2_launch_evolver(sg, pg, c->precision, G.mode, G.grid, c->block, G.smem, st)) {
         snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
         return 1;
       }
@@ -1034,6 +1208,43 @@ int song2_ctx_run(song2_ctx *c, void *stream, char *err) {
   cudaStream_t st = (cudaStream_t)stream;
   CK(cudaEventRecord(c->ev0, st));
   if (enqueue_run(c, st, err)) return 1;
+  CK(cudaEventRecord(c->ev1, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  return 0;
+}
+
+int song2_ctx_run_part(song2_ctx *c, int part, int n_parts, void *stream, char *err) {
+  if (n_parts < 1 || part < 0 || part >= n_parts) {
+    snprintf(err, SONG2_ERRLEN, "bad part %d of %d", part, n_parts);
+    return 1;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (c->parts != n_parts) {
+    /* regroup the work list part-major within every launch group: part q takes
+       every n_parts-th item of the group's cost-sorted list, from position q */
+    int ng = c->groups.empty() ? 1 : (int)c->groups.size();
+    std::vector<WorkItem> reo;
+    reo.reserve(c->h_items.size());
+    c->part_first.assign((size_t)ng * n_parts, 0);
+    c->part_count.assign((size_t)ng * n_parts, 0);
+    for (int g = 0; g < ng; ++g) {
+      int gf = c->groups.empty() ? 0 : c->groups[g].first;
+      int gc = c->groups.empty() ? c->n_items : c->groups[g].count;
+      for (int q = 0; q < n_parts; ++q) {
+        c->part_first[(size_t)g * n_parts + q] = (int)reo.size();
+        for (int i = gf + q; i < gf + gc; i += n_parts) reo.push_back(c->h_items[i]);
+        c->part_count[(size_t)g * n_parts + q] = (int)reo.size() - c->part_first[(size_t)g * n_parts + q];
+      }
+    }
+    c->h_items = reo;
+    c->parts = n_parts;
+    CK(cudaMemcpyAsync((void *)c->ptrs.items, reo.data(), sizeof(WorkItem) * reo.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(c->d_stats, 0, sizeof(song2_triplet_stats) * std::max(1, c->n_items), st));
+    CK(cudaStreamSynchronize(st));
+  }
+  CK(cudaEventRecord(c->ev0, st));
+  if (enqueue_part(c, part, st, err)) return 1;
   CK(cudaEventRecord(c->ev1, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
@@ -1060,6 +1271,18 @@ int song2_ctx_run_graph(song2_ctx *c, void *stream, char *err) {
   CK(cudaStreamSynchronize(st));
   CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
   return 0;
+}
+
+int song2_ctx_phase_cycles(song2_ctx *c, unsigned long long *out, int n) {
+#ifdef SONG2_PHASE_TIMERS
+  if (!c->ptrs.phase || n < 2 * S2_NPHASE) return 0;
+  if (cudaMemcpy(out, c->ptrs.phase, 2 * S2_NPHASE * sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return 0;
+  return S2_NPHASE;
+#else
+  (void)c; (void)out; (void)n;
+  return 0;
+#endif
 }
 
 double *song2_ctx_device_sources(song2_ctx *c) { return c->d_sources; }
@@ -1098,16 +1321,66 @@ int song2_ctx_download(song2_ctx *c, double *flat, song2_triplet_stats *stats, c
   return 0;
 }
 
+/* reference work-order index -> (k1, k2, k3) indices */
+static void work_order_triplets(const song2_spec *spec, std::vector<int> &i1s, std::vector<int> &i2s,
+                                std::vector<int> &i3s) {
+  i1s.clear(); i2s.clear(); i3s.clear();
+  for (int i1 = spec->k_size - 1; i1 >= 0; --i1)
+    for (int i2 = 0; i2 <= i1; ++i2)
+      for (int i3 = 0; i3 < spec->k3_size[i1 * spec->k_size + i2]; ++i3) {
+        i1s.push_back(i1); i2s.push_back(i2); i3s.push_back(i3);
+      }
+}
+
 int song2_gpu_evolve(const song2_spec *spec, const song2_tables *tab, int precision, double ****sources_out,
                      song2_triplet_stats *per_triplet, char *err) {
   song2_ctx *c = nullptr;
   if (song2_ctx_create(spec, tab, precision, &c, err)) return 1;
   int rc = song2_ctx_run(c, nullptr, err);
   std::vector<double> flat;
+  int64_t nt = song2_n_triplets(spec);
+  std::vector<song2_triplet_stats> stv(nt);
   if (!rc) {
     flat.resize(c->sources_len);
-    rc = song2_ctx_download(c, flat.data(), per_triplet, err);
+    rc = song2_ctx_download(c, flat.data(), stv.data(), err);
   }
+  if (!rc) {
+    /* exit strategy for the triplets that failed: evolve them again in plain FP64
+       with a larger step budget, and take their sources and stats from that run */
+    std::vector<int64_t> failed;
+    for (int64_t i = 0; i < nt; ++i)
+      if (stv[i].status != SONG2_OK) failed.push_back(i);
+    if (!failed.empty()) {
+      song2_spec rs = *spec;
+      rs.max_steps = spec->max_steps > (1 << 27) ? (1 << 30) : spec->max_steps * 8;
+      song2_ctx *r = nullptr;
+      rc = song2_ctx_create_list(&rs, tab, SONG2_PREC_FP64, failed.data(), (int64_t)failed.size(), &r, err);
+      if (!rc) rc = song2_ctx_run(r, nullptr, err);
+      std::vector<double> flat2;
+      std::vector<song2_triplet_stats> st2(nt);
+      if (!rc) {
+        flat2.resize(r->sources_len);
+        rc = song2_ctx_download(r, flat2.data(), st2.data(), err);
+      }
+      if (!rc) {
+        std::vector<int> i1s, i2s, i3s;
+        work_order_triplets(spec, i1s, i2s, i3s);
+        for (int64_t i : failed) {
+          int nk3 = spec->k3_size[i1s[i] * spec->k_size + i2s[i]];
+          int64_t off = song2_pair_offset(spec, i1s[i], i2s[i]) + i3s[i];
+          for (int tp = 0; tp < c->tp2_size; ++tp)
+            for (int j = 0; j < spec->tau_size; ++j) {
+              size_t e = (size_t)tp * c->per_type + off + (size_t)j * nk3;
+              flat[e] = flat2[e];
+            }
+          stv[i] = st2[i];
+          stv[i].retried = 1;
+        }
+      }
+      song2_ctx_destroy(r);
+    }
+  }
+  if (!rc && per_triplet) memcpy(per_triplet, stv.data(), sizeof(song2_triplet_stats) * nt);
   if (!rc && sources_out) {
     for (int tp = 0; tp < c->tp2_size; ++tp)
       for (int i1 = 0; i1 < spec->k_size; ++i1)
@@ -1117,15 +1390,14 @@ int song2_gpu_evolve(const song2_spec *spec, const song2_tables *tab, int precis
           memcpy(sources_out[tp][i1][i2], flat.data() + (size_t)tp * c->per_type + off, sizeof(double) * len);
         }
   }
-  if (!rc && per_triplet) {
-    int64_t nt = song2_n_triplets(spec);
+  if (!rc)
     for (int64_t i = 0; i < nt; ++i)
-      if (per_triplet[i].status != SONG2_OK) {
-        snprintf(err, SONG2_ERRLEN, "triplet %lld failed with status %d", (long long)i, per_triplet[i].status);
+      if (stv[i].status != SONG2_OK) {
+        snprintf(err, SONG2_ERRLEN, "triplet %lld failed with status %d, also on its plain-FP64 re-run", (long long)i,
+                 stv[i].status);
         rc = 1;
         break;
       }
-  }
   song2_ctx_destroy(c);
   return rc;
 }
@@ -1150,7 +1422,7 @@ int song2_gpu_first_order(const song2_spec *spec2, const song2_tables *bg_only, 
   std::vector<int> k3_off, k3_size;
   std::vector<int64_t> pair_off;
   for (int ik = 0; ik < s.k_size; ++ik) {
-    items.push_back(WorkItem{ik, ik, 0, ik});
+    items.push_back(WorkItem{ik, ik, 0, ik, 0, ik});
     k3.push_back(s.k[ik]);
     k3_off.push_back(ik);
     k3_size.push_back(1);
@@ -1195,6 +1467,7 @@ static __device__ __align__(256) unsigned char song2_noalloc_scratch[SONG2_NOALL
 
 #define SONG2_NOALLOC_MAX_DEVICES 64
 static void *g_noalloc_addr[SONG2_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mutex;   /* guards the lazy resolve of g_noalloc_addr */
 
 static size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -1216,16 +1489,20 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
     return 1;
   }
   /* first call on this device (which must be current): resolve the scratch address */
-  if (!g_noalloc_addr[dev]) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, song2_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) {
-      snprintf(err, SONG2_ERRLEN, "cudaGetSymbolAddress of the scratch failed: %s", cudaGetErrorString(e));
-      return 1;
+  char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+      void *ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, song2_noalloc_scratch);
+      if (e != cudaSuccess || !ptr) {
+        snprintf(err, SONG2_ERRLEN, "cudaGetSymbolAddress of the scratch failed: %s", cudaGetErrorString(e));
+        return 1;
+      }
+      g_noalloc_addr[dev] = ptr;
     }
-    g_noalloc_addr[dev] = ptr;
+    base = (char *)g_noalloc_addr[dev];
   }
-  char *base = (char *)g_noalloc_addr[dev];
   cudaStream_t st = (cudaStream_t)stream;
 
   if (spec->n_classes > 0) {
@@ -1261,6 +1538,8 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   size_t o_qsp = take(nq), o_ql = take(nq), o_qm = take(nq);
   size_t nrs = sizeof(short) * H.row_slot.size(), nqs = sizeof(short) * H.qs_slot.size();
   size_t o_rsl = take(nrs), o_qsl = take(nqs);
+  size_t nmx = sizeof(short) * H.mx_idx.size(), nqo = sizeof(short) * H.qo_slot.size();
+  size_t o_mxi = take(nmx), o_mxp = take(nmx), o_qo = take(nqo);
   size_t o_items = take(sizeof(WorkItem) * items.size());
   size_t o_queue = take(sizeof(int));
   std::vector<double> cs(std::max(2, s.fo_tau_size + 1), 0.0);
@@ -1277,9 +1556,6 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   int nsm = 0, smem_optin = 0;
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  size_t stack = 0;
-  CK(cudaDeviceGetLimit(&stack, cudaLimitStackSize));
-  if (stack < 4096) CK(cudaDeviceSetLimit(cudaLimitStackSize, 4096));
   int block = 256;
   s.lu_in_smem = song2_smem_bytes(s, precision, block, 1) <= (size_t)smem_optin ? 1 : 0;
   size_t smem = song2_smem_bytes(s, precision, block, s.lu_in_smem);
@@ -1290,7 +1566,6 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   size_t ts = precision == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
   size_t qtab_team = s.has_qs ? (size_t)s.fo_tau_size * 2 * s.qs2_size * sizeof(double) : 0;
   size_t per_team = na_align((size_t)s.lu_elems * sizeof(double)) + (s.lu_in_smem ? 0 : na_align((size_t)s.lu_elems * ts)) +
-                    ((s.lu_in_smem || precision != SONG2_PREC_MIXED) ? 0 : na_align((size_t)s.lu_elems * sizeof(float))) +
                     na_align(qtab_team);
   size_t teams_fit = (SONG2_NOALLOC_BYTES - fixed) / per_team;
   if (teams_fit < 1) {
@@ -1307,8 +1582,11 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   grid = (int)std::min<size_t>((size_t)grid, teams_fit);
   size_t o_jac = take((size_t)grid * s.lu_elems * sizeof(double));
   size_t o_lu = s.lu_in_smem ? 0 : take((size_t)grid * s.lu_elems * ts);
-  size_t o_minv = (s.lu_in_smem || precision != SONG2_PREC_MIXED) ? 0 : take((size_t)grid * s.lu_elems * sizeof(float));
   size_t o_qtab = s.has_qs ? take((size_t)grid * qtab_team) : 0;
+  if (off > SONG2_NOALLOC_BYTES) {
+    snprintf(err, SONG2_ERRLEN, "scratch plan of %zu B exceeds the %zu B scratch", off, (size_t)SONG2_NOALLOC_BYTES);
+    return 1;
+  }
 
   auto put = [&](size_t o, const void *src, size_t bytes) -> cudaError_t {
     return bytes ? cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
@@ -1326,6 +1604,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   CK(put(o_iN, H.idx_N.data(), ni));
   CK(put(o_qsp, H.qs_sp.data(), nq)); CK(put(o_ql, H.qs_l.data(), nq)); CK(put(o_qm, H.qs_m.data(), nq));
   CK(put(o_rsl, H.row_slot.data(), nrs)); CK(put(o_qsl, H.qs_slot.data(), nqs));
+  CK(put(o_mxi, H.mx_idx.data(), nmx)); CK(put(o_mxp, H.mx_pos.data(), nmx)); CK(put(o_qo, H.qo_slot.data(), nqo));
   CK(put(o_items, items.data(), sizeof(WorkItem) * items.size()));
   CK(put(o_splc, cs.data(), sizeof(double) * cs.size()));
   CK(put(o_dt, dtc.data(), sizeof(double) * dtc.size()));
@@ -1351,12 +1630,14 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   p.tabs.idx_B = (const short *)(base + o_iB); p.tabs.idx_N = (const short *)(base + o_iN);
   p.tabs.qs_sp = (const short *)(base + o_qsp); p.tabs.qs_l = (const short *)(base + o_ql); p.tabs.qs_m = (const short *)(base + o_qm);
   p.tabs.row_slot = (const short *)(base + o_rsl); p.tabs.qs_slot = (const short *)(base + o_qsl);
+  p.tabs.mx_idx = (const short *)(base + o_mxi); p.tabs.mx_pos = (const short *)(base + o_mxp);
+  p.tabs.qo_slot = (const short *)(base + o_qo);
   p.items = (const WorkItem *)(base + o_items);
   p.sources = sources_dev;
   p.stats = stats_dev;
+  p.stats_by_ref = 1;
   p.jac = (double *)(base + o_jac);
   p.lu_global = s.lu_in_smem ? nullptr : (void *)(base + o_lu);
-  p.minv_global = (s.lu_in_smem || precision != SONG2_PREC_MIXED) ? nullptr : (float *)(base + o_minv);
   p.qtab = s.has_qs ? (double *)(base + o_qtab) : nullptr;
   p.spl_c = (const double *)(base + o_splc);
   p.dt_coup = s.dtilde ? (const double *)(base + o_dt) : nullptr;

@@ -47,17 +47,26 @@
 #define SQRT_3 1.7320508075688772935
 #define SQRT_6 2.4494897427831780982
 #define FOUR_THIRDS (4.0 / 3.0)
+#define ONE_THIRD (1.0 / 3.0)
 
 namespace {
 
 /* ------------------------------------------------------------------ smem */
 
+/* Background and thermodynamics at one time, with the reciprocals the
+   right-hand side needs (no FP64 division on the hot path).  Field q is
+   bg_field(q); the order below is that of bg_field. */
 struct BgV {
   double a, a_sq, Hc, Hc_prime, rho_g, rho_b, rho_cdm, rho_ur, kappa_dot, exp_m_kappa, g, r;
+  double inv_kd;     /* 1 / kappa' = tau_c */
+  double a2_k2;      /* a^2 / k^2 */
+  double inv_ktau;   /* 1 / (k tau), the closure of the hierarchies */
 };
+#define S2_NBGV 15
 
 struct Tri {
   double k1, k2, k, k_sq, cosk1k2, cosk1k, cosk2k, k1_dot_k2;
+  double inv_k, inv_k_sq, lnk;
   double k1_m[3], k2_m[3], k1_ten_k2[5], k1_ten_k1[5], k2_ten_k2[5];
   double mfac[SONG2_MAX_M + 3];    /* rot(l,-m) = (-1)^m rot(l,m) mfac[m]: sin(theta_k1)^2m if rescaled, else 1 */
   double tau_ini, tau_end;
@@ -87,14 +96,45 @@ struct Shared {
   double ctl[4];
   int item;
   int lu_fail;
-  int kl[S2_MAXBLK], ku[S2_MAXBLK];   /* band of each block's Jacobian */
+  int mx_bad;                          /* a Jacobian entry outside the structured layout */
   int ap;
+  long long ph_t, ph_item;             /* phase-timer marks (SONG2_PHASE_TIMERS builds) */
 };
+
+/* Per-phase cycle counters: PH_MARK(c, id) charges the cycles since the team's
+   previous mark to phase id (thread 0 of the team, fire-and-forget atomics).
+   Compiled in only with -DSONG2_PHASE_TIMERS; otherwise they vanish. */
+#ifdef SONG2_PHASE_TIMERS
+#define PH_RESET(c)                                                     \
+  do {                                                                  \
+    if ((c).rank == 0) (c).sh->ph_t = (c).sh->ph_item = clock64();      \
+  } while (0)
+#define PH_MARK(c, id)                                                              \
+  do {                                                                              \
+    if ((c).rank == 0 && (c).p.phase) {                                             \
+      long long now_ = clock64();                                                   \
+      atomicAdd((c).p.phase + 2 * (id), (unsigned long long)(now_ - (c).sh->ph_t)); \
+      atomicAdd((c).p.phase + 2 * (id) + 1, 1ull);                                  \
+      (c).sh->ph_t = now_;                                                          \
+    }                                                                               \
+  } while (0)
+#define PH_ITEM_END(c)                                                                          \
+  do {                                                                                          \
+    if ((c).rank == 0 && (c).p.phase) {                                                         \
+      atomicAdd((c).p.phase + 2 * PH_ITEM, (unsigned long long)(clock64() - (c).sh->ph_item)); \
+      atomicAdd((c).p.phase + 2 * PH_ITEM + 1, 1ull);                                           \
+    }                                                                                           \
+  } while (0)
+#else
+#define PH_RESET(c) do {} while (0)
+#define PH_MARK(c, id) do {} while (0)
+#define PH_ITEM_END(c) do {} while (0)
+#endif
 
 /* Offsets (in bytes) of the dynamic shared-memory plan. */
 struct Plan {
   size_t y, f, ynew, difkp1, psiv, del, invwt, yout, dyout, dif, fo1, fo2, qs, qc, rot1, rot2, sc, bgraw, shared,
-      tab, xsol, piv, lu, minv, total;
+      tab, xsol, lu, jac, total;
 };
 
 __host__ __device__ inline size_t al(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -126,16 +166,17 @@ __host__ __device__ inline Plan make_plan(const DevSpec &s, int prec, int lu_in_
   /* index tables copied from the launch parameters / global memory: the hot
      loops index them per thread, which the constant bank would serialise */
   p.tab = o;
-  o = al(o + sizeof(short) * ((size_t)(s.Lq + 1) * (SONG2_MAX_M + SONG2_MAX_M + 2) + SONG2_MAX_M + 3 * n +
-                              4 * (size_t)s.n_lm + 3 * (size_t)s.qs2_size + s.n_row_slots + s.n_qs_slots));
+  o = al(o + sizeof(short) * ((size_t)(s.Lq + 1) * (SONG2_MAX_M + SONG2_MAX_M + 2) + SONG2_MAX_M + 4 * n +
+                              4 * (size_t)s.n_lm + 3 * (size_t)s.qs2_size + s.n_row_slots + s.n_qs_slots +
+                              s.n_qo_slots));
   size_t ts = prec == SONG2_PREC_MIXED ? sizeof(float) : sizeof(double);
   p.xsol = o; o = al(o + n * ts);
-  p.piv = o; o = al(o + n * sizeof(int));
+  /* the structured Jacobian and the factors of the iteration matrix (O(n)
+     elements each) */
   p.lu = o;
   if (lu_in_smem) o = al(o + (size_t)s.lu_elems * ts);
-  /* mixed form: the explicit inverse of the factorised blocks, beside them */
-  p.minv = o;
-  if (lu_in_smem && prec == SONG2_PREC_MIXED) o = al(o + (size_t)s.lu_elems * sizeof(float));
+  p.jac = o;
+  if (lu_in_smem) o = al(o + (size_t)s.lu_elems * ts);
   p.total = o;
   return p;
 }
@@ -197,8 +238,9 @@ __host__ __device__ inline TeamPlan make_team_plan(const DevSpec &s) {
 
 /* shared memory of MODE_TEAM: the index tables once per CTA, then one Shared per team */
 __host__ __device__ inline size_t team_tables_bytes(const DevSpec &s) {
-  return al(sizeof(short) * ((size_t)(s.Lq + 1) * (SONG2_MAX_M + SONG2_MAX_M + 2) + SONG2_MAX_M + 3 * (size_t)s.n +
-                             4 * (size_t)s.n_lm + 3 * (size_t)s.qs2_size + s.n_row_slots + s.n_qs_slots));
+  return al(sizeof(short) * ((size_t)(s.Lq + 1) * (SONG2_MAX_M + SONG2_MAX_M + 2) + SONG2_MAX_M + 4 * (size_t)s.n +
+                             4 * (size_t)s.n_lm + 3 * (size_t)s.qs2_size + s.n_row_slots + s.n_qs_slots +
+                             s.n_qo_slots));
 }
 
 template <int MODE> struct KX {
@@ -214,11 +256,10 @@ template <int MODE> struct KX {
   DA y, f, ynew, difkp1, psiv, del, invwt, yout, dyout, dif, fo1, fo2, qs, qc, rot1, rot2, sc, bgraw;
   Shared *sh;
   short *lm_s, *lmq_s, *im_s, *eq_sp, *eq_l, *eq_m, *idx_I, *idx_E, *idx_B, *idx_N, *qs_sp, *qs_l, *qs_m, *row_slot,
-      *qs_slot;
-  char *xsol_b, *lu_b;     /* element 0 of this team's solve vector and LU blocks */
-  float *minv_b;           /* mixed form, CTA/warp teams: the inverse of the LU blocks */
-  View<int, STR> piv;
-  DA jac, qtab;
+      *qs_slot, *qo_slot, *mx_s;
+  char *xsol_b, *lu_b;     /* element 0 of this team's solve vector and iteration-matrix factors */
+  char *jac_b;             /* element 0 of this team's structured Jacobian */
+  DA qtab;
 
   template <typename E> __device__ View<E, STR> mk(char *b) const {
     if constexpr (STR) return View<E, 1>{(E *)b, nt};
@@ -230,11 +271,11 @@ template <int MODE> struct KX {
   }
   template <typename E> __device__ View<E, STR> xsol() const { return mk<E>(xsol_b); }
   template <typename E> __device__ View<E, STR> lu() const { return mk<E>(lu_b); }
-  /* the Jacobian blocks, stored in the iteration-matrix precision: element offset
-     jac_eoff counted in elements of that precision, so the teams' regions stay
-     disjoint whatever the element size */
-  long jac_eoff;
-  template <typename E> __device__ View<E, STR> jacv() const { return mk<E>((char *)((E *)p.jac + jac_eoff)); }
+  /* the structured Jacobian, stored in the iteration-matrix precision: in shared
+     memory beside the factors, or in global scratch at an element offset counted in
+     elements of that precision, so the teams' regions stay disjoint whatever the
+     element size */
+  template <typename E> __device__ View<E, STR> jacv() const { return mk<E>(jac_b); }
 
   __device__ void set_tables(short *tb) {
     lm_s = tb; tb += (s.Lq + 1) * SONG2_MAX_M;
@@ -251,7 +292,9 @@ template <int MODE> struct KX {
     qs_l = tb; tb += s.qs2_size;
     qs_m = tb; tb += s.qs2_size;
     row_slot = tb; tb += s.n_row_slots;
-    qs_slot = tb;
+    qs_slot = tb; tb += s.n_qs_slots;
+    qo_slot = tb; tb += s.n_qo_slots;
+    mx_s = tb;
   }
 
   __device__ KX(const DevSpec &s_, const DevPtrs &p_, const ClassTabs &ct_, char *smem_all, int prec)
@@ -277,11 +320,8 @@ template <int MODE> struct KX {
       set_tables((short *)smem_all);
       sh = (Shared *)(smem_all + team_tables_bytes(s_)) + (long)warp * nt + tiw;
       xsol_b = (char *)p_.txsol + (gw * (long)s_.n * nt + tiw) * ts;
-      piv = View<int, STR>{p_.tpiv + gw * (long)s_.n * nt + tiw, nt};
       lu_b = (char *)p_.lu_global + (gw * (long)s_.lu_stride * nt + tiw) * ts;
-      minv_b = nullptr;
-      jac_eoff = gw * (long)s_.lu_stride * nt + tiw;
-      jac = da(p_.jac + jac_eoff);
+      jac_b = (char *)p_.jac + (gw * (long)s_.lu_stride * nt + tiw) * ts;
       qtab = da(p_.qtab ? p_.qtab + gw * s_.qtab_stride * nt + tiw : nullptr);
     } else {
       Plan pl = make_plan(s_, prec, s_.lu_in_smem);
@@ -307,17 +347,10 @@ template <int MODE> struct KX {
       sh = (Shared *)(smem + pl.shared);
       set_tables((short *)(smem + pl.tab));
       xsol_b = smem + pl.xsol;
-      piv = View<int, STR>{(int *)(smem + pl.piv)};
       if (s_.lu_in_smem) lu_b = smem + pl.lu;
       else lu_b = (char *)p_.lu_global + (size_t)team * s_.lu_stride * ts;
-      /* the inverse lives beside the LU blocks in shared memory, or in global
-         scratch for small blocks (its column sweeps are latency bound there) */
-      int maxnb = 0;
-      for (int bb = 0; bb < s_.nblk; ++bb) maxnb = max(maxnb, s_.blk_size[bb]);
-      if (s_.lu_in_smem) minv_b = (float *)(smem + pl.minv);
-      else minv_b = p_.minv_global && maxnb <= 64 ? p_.minv_global + (size_t)team * s_.lu_stride : nullptr;
-      jac_eoff = (long)team * s_.lu_stride;
-      jac = da(p_.jac + jac_eoff);
+      if (s_.lu_in_smem) jac_b = smem + pl.jac;
+      else jac_b = (char *)p_.jac + (size_t)team * s_.lu_stride * ts;
       qtab = da(p_.qtab ? p_.qtab + (size_t)team * s_.qtab_stride : nullptr);
     }
   }
@@ -348,6 +381,8 @@ template <int MODE> struct KX {
     }
     for (int e = r; e < s.n_row_slots; e += z) row_slot[e] = ct.row_slot[e];
     for (int e = r; e < s.n_qs_slots; e += z) qs_slot[e] = ct.qs_slot[e];
+    for (int e = r; e < s.n_qo_slots; e += z) qo_slot[e] = ct.qo_slot[e];
+    for (int e = r; e < s.n; e += z) mx_s[e] = ct.mx_idx[e];
   }
   /* summed couplings, index X in 0..19 */
   __device__ double S(int X, int l, int m) const { return sc[X * s.n_lm + LM(l, m)]; }
@@ -446,33 +481,40 @@ template <class C> __device__ inline double bg_col(const C &c, int q, double tau
   return spl(c.p.bg, c.p.bg_dd, c.s.bg_size, SONG2_BG_SIZE, c.s.bg_lntau0, c.s.bg_dlntau, q, log(tau));
 }
 
-/* Background column q at ln tau = x in linear form (exp of the logarithmic
-   columns, Hc' from Hc' tau^2), one column per thread. */
-__device__ inline double bg_value(const double *bg, const double *bg_dd, int bg_size, double x0, double dx, int q, double x,
-                                  double tau) {
-  double v = spl(bg, bg_dd, bg_size, SONG2_BG_SIZE, x0, dx, q, x);
-  /* one exponential on every lane of the warp: exp(v), exp(-kappa), and
-     1/tau^2 = exp(-2 ln tau) for Hc' */
-  (void)tau;
-  double arg = q == SONG2_BG_HC_PRIME_TAU2 ? -2.0 * x : (q == SONG2_BG_KAPPA ? -v : v);
-  double e = exp(arg);
-  return q == SONG2_BG_HC_PRIME_TAU2 ? v * e : e;
+/* Field q of BgV from the spline values v[] of the background columns at
+   x = ln tau: every field is exp(c1 v[i1] + c2 v[i2] + cx x + ck ln k), except
+   Hc' = v[Hc' tau^2] exp(-2x), so the fields run on separate lanes along one
+   code path (one exponential each, no division). */
+template <class A> __device__ inline double bg_field(const A &v, int q, double x, double lnk) {
+  int i1 = 0, i2 = 0;
+  double c1 = 0.0, c2 = 0.0, cx = 0.0, ck = 0.0;
+  switch (q) {
+  case 0: i1 = SONG2_BG_LN_A; c1 = 1; break;                                           /* a */
+  case 1: i1 = SONG2_BG_LN_A; c1 = 2; break;                                           /* a^2 */
+  case 2: i1 = SONG2_BG_LN_HC; c1 = 1; break;                                          /* Hc */
+  case 3: cx = -2; break;                                                              /* Hc' */
+  case 4: i1 = SONG2_BG_LN_RHO_G; c1 = 1; break;
+  case 5: i1 = SONG2_BG_LN_RHO_B; c1 = 1; break;
+  case 6: i1 = SONG2_BG_LN_RHO_CDM; c1 = 1; break;
+  case 7: i1 = SONG2_BG_LN_RHO_UR; c1 = 1; break;
+  case 8: i1 = SONG2_BG_LN_KAPPA_DOT; c1 = 1; break;                                   /* kappa' */
+  case 9: i1 = SONG2_BG_KAPPA; c1 = -1; break;                                         /* e^-kappa */
+  case 10: i1 = SONG2_BG_LN_KAPPA_DOT; c1 = 1; i2 = SONG2_BG_KAPPA; c2 = -1; break;    /* g */
+  case 11: i1 = SONG2_BG_LN_RHO_G; c1 = 1; i2 = SONG2_BG_LN_RHO_B; c2 = -1; break;     /* r */
+  case 12: i1 = SONG2_BG_LN_KAPPA_DOT; c1 = -1; break;                                 /* 1/kappa' */
+  case 13: i1 = SONG2_BG_LN_A; c1 = 2; ck = -2; break;                                 /* a^2/k^2 */
+  default: cx = -1; ck = -1; break;                                                    /* 1/(k tau) */
+  }
+  double e = exp(c1 * v[i1] + c2 * v[i2] + cx * x + ck * lnk);
+  return q == 3 ? v[SONG2_BG_HC_PRIME_TAU2] * e : e;
 }
 
-/* BgV from the linear columns */
-template <class A> __device__ inline void bg_derive(const A &lin, BgV &b) {
-  b.a = lin[SONG2_BG_LN_A];
-  b.a_sq = b.a * b.a;
-  b.Hc = lin[SONG2_BG_LN_HC];
-  b.Hc_prime = lin[SONG2_BG_HC_PRIME_TAU2];
-  b.rho_g = lin[SONG2_BG_LN_RHO_G];
-  b.rho_b = lin[SONG2_BG_LN_RHO_B];
-  b.rho_cdm = lin[SONG2_BG_LN_RHO_CDM];
-  b.rho_ur = lin[SONG2_BG_LN_RHO_UR];
-  b.kappa_dot = lin[SONG2_BG_LN_KAPPA_DOT];
-  b.exp_m_kappa = lin[SONG2_BG_KAPPA];
-  b.g = b.kappa_dot * b.exp_m_kappa;
-  b.r = b.rho_g / b.rho_b;
+/* sh->bg at x = ln tau from the spline values in c.bgraw (the team's threads
+   share the fields); the caller separates this from the spline step and from
+   the readers of sh->bg by barriers */
+template <class C> __device__ inline void bg_fields(const C &c, double x) {
+  double *b = (double *)&c.sh->bg;
+  for (int q = c.rank; q < S2_NBGV; q += c.size) b[q] = bg_field(c.bgraw, q, x, c.sh->tri.lnk);
 }
 
 /* Hc and kappa_dot only (start time, TCA trigger) */
@@ -787,8 +829,10 @@ template <class C> __device__ void qc_entry(const C &c, const BgV &bg, int q) {
 
 /* ------------------------------------------------------------------ prepare(tau) */
 
-/* Background, first-order quantities and quadratic sources at tau, block-wide.
-   Leaves sh->bg and the qs/qc/fo arrays ready; ends with a barrier. */
+/* Background, first-order quantities and quadratic sources at tau, block-wide:
+   the entries an output time or an interval start reads (qo_slot: moments up to
+   the line-of-sight l, matter, metric; the others are left at zero).  Leaves
+   sh->bg and the qs/qc/fo arrays ready; ends with a barrier. */
 template <class C> __device__ void prepare(const C &c, double tau, int with_sources) {
   const DevSpec &s = c.s;
   const Tri &t = c.sh->tri;
@@ -798,7 +842,7 @@ template <class C> __device__ void prepare(const C &c, double tau, int with_sour
   c.sync();
   double x = c.sh->lntau;
   for (int q = tid; q < SONG2_BG_SIZE; q += nt)
-    c.bgraw[q] = bg_value(c.p.bg, c.p.bg_dd, s.bg_size, s.bg_lntau0, s.bg_dlntau, q, x, tau);
+    c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, q, x);
   int use_fo = with_sources && s.has_qs && !s.mode_first_order;
   for (int q = tid; q < 2 * s.nfo; q += nt) {
     int which = q >= s.nfo, qq = which ? q - s.nfo : q;
@@ -811,8 +855,7 @@ template <class C> __device__ void prepare(const C &c, double tau, int with_sour
     (which ? c.fo2 : c.fo1)[qq] = v;
   }
   c.sync();
-  /* FP64 transcendental work is done once, not once per thread */
-  if (tid == 0) bg_derive(c.bgraw, c.sh->bg);
+  bg_fields(c, x);
   for (int q = tid; q < s.qs2_size; q += nt) {
     c.qs[q] = 0.0;
     c.qc[q] = 0.0;
@@ -820,8 +863,8 @@ template <class C> __device__ void prepare(const C &c, double tau, int with_sour
   c.sync();
   if (use_fo) {
     const BgV &bg = c.sh->bg;
-    for (int e = tid; e < s.n_qs_slots; e += nt) {
-      int q = c.qs_slot[e];
+    for (int e = tid; e < s.n_qo_slots; e += nt) {
+      int q = c.qo_slot[e];
       if (q >= 0) qs_entry(c, bg, q);
     }
   }
@@ -842,7 +885,7 @@ template <class C> __device__ void prepare_table(const C &c, double tau, int ap)
   c.sync();
   double x = c.sh->lntau;
   for (int q = tid; q < SONG2_BG_SIZE; q += nt)
-    c.bgraw[q] = bg_value(c.p.bg, c.p.bg_dd, s.bg_size, s.bg_lntau0, s.bg_dlntau, q, x, tau);
+    c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, q, x);
   int use = s.has_qs && !s.mode_first_order && c.qtab.p != nullptr;
   if (use) {
     double dx = s.fo_dlntau, u = (x - s.fo_lntau0) / dx;
@@ -870,7 +913,7 @@ template <class C> __device__ void prepare_table(const C &c, double tau, int ap)
   if (!(use && ap))
     for (int q = tid; q < s.qs2_size; q += nt) c.qc[q] = 0.0;
   c.sync();
-  if (tid == 0) bg_derive(c.bgraw, c.sh->bg);
+  bg_fields(c, x);
   c.sync();
   if (use && ap) {
     const BgV &bg = c.sh->bg;
@@ -910,13 +953,13 @@ template <class C> __device__ void build_qs_table(const C &c) {
   for (int j = 0; j < M; ++j) {
     double x = x0 + (j0 + j) * dx;
     for (int q = tid; q < SONG2_BG_SIZE; q += nt)
-      c.bgraw[q] = bg_value(c.p.bg, c.p.bg_dd, s.bg_size, s.bg_lntau0, s.bg_dlntau, q, x, exp(x));
+      c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, q, x);
     for (int q = tid; q < 2 * s.nfo; q += nt) {
       int which = q >= s.nfo, qq = which ? q - s.nfo : q;
       (which ? c.fo2 : c.fo1)[qq] = __ldg((which ? v2 : v1) + (size_t)(j0 + j) * s.nfo + qq);
     }
     c.sync();
-    if (tid == 0) bg_derive(c.bgraw, c.sh->bg);
+    bg_fields(c, x);
     c.sync();
     {
       const BgV &bg = c.sh->bg;
@@ -1059,7 +1102,7 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int ap, con
   w.cdm_22m[m] = 15 * t.k1_ten_k2[m + 2] * vv_cdm;
   if (ap == AP_TCA) {
     /* perturb2_tca_variables (perturbations2.c:9374-9738) */
-    double tau_c = 1.0 / kd;
+    double tau_c = bg.inv_kd;
     double vpot_g_1 = lin ? 0.0 : fo1[SONG2_FO_V_G], vpot_g_2 = lin ? 0.0 : fo2[SONG2_FO_V_G];
     double delta_g_1 = lin ? 0.0 : fo1[SONG2_FO_DELTA_G], delta_g_2 = lin ? 0.0 : fo2[SONG2_FO_DELTA_G];
     double vpot_b_1 = lin ? 0.0 : fo1[SONG2_FO_V_B], vpot_b_2 = lin ? 0.0 : fo2[SONG2_FO_V_B];
@@ -1076,21 +1119,22 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int ap, con
       double u_g_1 = -t.k1_m[m + 1] * vpot_g_1, u_g_2 = -t.k2_m[m + 1] * vpot_g_2;
       double u_b_1 = -t.k1_m[m + 1] * vpot_b_1, u_b_2 = -t.k2_m[m + 1] * vpot_b_2;
       double u_b_1_prime = -t.k1_m[m + 1] * vpot_b_1_prime, u_b_2_prime = -t.k2_m[m + 1] * vpot_b_2_prime;
-      double u_b = getb(c, y, 1, m) / 3 - delta_b_1 * u_b_2 - delta_b_2 * u_b_1;
+      double u_b = getb(c, y, 1, m) * ONE_THIRD - delta_b_1 * u_b_2 - delta_b_2 * u_b_1;
       double qcI1 = lin ? 0.0 : qc[s.iq_g + c.LM(1, m)];
       double qsI1 = lin ? 0.0 : qs[s.iq_g + c.LM(1, m)];
       double qsb = lin ? 0.0 : qs[s.iq_b11[m]], qcb = lin ? 0.0 : qc[s.iq_b11[m]];
-      double quadC_u_g_m = qcI1 / kd / 4 + (u_b_1 * delta_b_2 + u_b_2 * delta_b_1) - (u_g_1 * delta_g_2 + u_g_2 * delta_g_1);
+      double quadC_u_g_m = qcI1 * tau_c * 0.25 + (u_b_1 * delta_b_2 + u_b_2 * delta_b_1) - (u_g_1 * delta_g_2 + u_g_2 * delta_g_1);
       double delta_u_prime_b_m = delta_b_1_prime * u_b_2 + delta_b_2_prime * u_b_1 + delta_b_1 * u_b_2_prime +
                                  delta_b_2 * u_b_1_prime;
       double quadL_b_11M = -(qsb - qcb), quadL_I_1M = -(qsI1 - qcI1);
-      double quadL_diff = quadL_b_11M / 3 - quadL_I_1M / 4 - FOUR_THIRDS * delta_u_prime_b_m / 4 +
+      double quadL_diff = quadL_b_11M * ONE_THIRD - quadL_I_1M * 0.25 - FOUR_THIRDS * delta_u_prime_b_m * 0.25 +
                           Hc * (u_b_1 * delta_b_2 + u_b_2 * delta_b_1);
-      double R = 3 / (4 * r);
+      /* R / (1 + R) with R = 3 / (4 r) */
+      double Rf = 1.0 / (1.0 + FOUR_THIRDS * r);
       double om = (m == 1) ? y(s.idx_omega) : 0.0;
-      double core = Hc * (u_b + om) + k / 4 * (m == 0 ? delta_g : 0) + quadL_diff;
-      double U_slip = -quadC_u_g_m - R / (1 + R) * tau_c * core;
-      c1tca = -qcI1 - 4 * R / (1 + R) * core;
+      double core = Hc * (u_b + om) + k * 0.25 * (m == 0 ? delta_g : 0) + quadL_diff;
+      double U_slip = -quadC_u_g_m - Rf * tau_c * core;
+      c1tca = -qcI1 - 4 * Rf * core;
       double u_g_tca1 = u_b - U_slip;
       w.I_1m_tca1[m] = 4 * (u_g_tca1 + delta_g_1 * u_g_2 + delta_g_2 * u_g_1);
     }
@@ -1100,12 +1144,12 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int ap, con
       double gp = (m == 2) ? y(s.idx_gammap) : 0.0;
       double cm2 = c.cmin(2, m, m);
       double shear = 8 / 45. * tau_c * (-k * w.I_1m_tca1[m] * cm2 - 4 * gp);
-      double quadC_I_2M = (lin ? 0.0 : qc[s.iq_g + c.LM(2, m)]) / kd;
+      double quadC_I_2M = (lin ? 0.0 : qc[s.iq_g + c.LM(2, m)]) * tau_c;
       double quadC_E_2M = 0, quadC_B_2M = 0, quadL_E_2M = 0;
       double quadL_I_2M = lin ? 0.0 : -(qs[s.iq_g + c.LM(2, m)] - qc[s.iq_g + c.LM(2, m)]);
       if (s.has_pol && !lin) {
-        quadC_E_2M = qc[s.iq_E + c.LM(2, m)] / kd;
-        quadC_B_2M = (m != 0 ? qc[s.iq_B + c.LM(2, m)] : 0.0) / kd;
+        quadC_E_2M = qc[s.iq_E + c.LM(2, m)] * tau_c;
+        quadC_B_2M = (m != 0 ? qc[s.iq_B + c.LM(2, m)] : 0.0) * tau_c;
         quadL_E_2M = -(qs[s.iq_E + c.LM(2, m)] - qc[s.iq_E + c.LM(2, m)]);
       }
       shear += 8 / 45. * (-quadC_I_2M + SQRT_6 / 4 * quadC_E_2M - 15 * v_ten_v_g);
@@ -1115,7 +1159,7 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int ap, con
                             tau_c * (-20 * v_ten_v_b_prime - k * w.I_1m[m] * cm2 - 4 * gp + quadL_I_2M));
       w.I_2m_tca1[m] = -15 / 2. * shear - 20 * v_ten_v_g;
       if (s.has_pol) {
-        w.Pi_tca1[m] = (w.I_2m_tca1[m] - SQRT_6 * (quadC_E_2M - tau_c * quadL_E_2M)) / 4;
+        w.Pi_tca1[m] = (w.I_2m_tca1[m] - SQRT_6 * (quadC_E_2M - tau_c * quadL_E_2M)) * 0.25;
         w.E_2m_tca1[m] = -SQRT_6 * w.Pi_tca1[m] + quadC_E_2M - tau_c * quadL_E_2M;
         w.B_2m_tca1[m] = (m != 0 ? quadC_B_2M : 0.0);
       } else {
@@ -1139,16 +1183,16 @@ template <class Y, class C> __device__ void compute_ws_m(const C &c, int ap, con
     double rho_quadrupole = bg.rho_g * w.I_2m[0] + bg.rho_b * w.b_22m[0] + bg.rho_cdm * w.cdm_22m[0] + bg.rho_ur * gN(2, 0);
     double rho_mono_b = bg.rho_b * getb(c, y, 0, 0), rho_mono_c = bg.rho_cdm * getc(c, y, 0, 0);
     double phi = y(s.idx_phi);
-    w.psi = phi - 3 / 5. * (a_sq / k_sq) * rho_quadrupole + (lin ? 0.0 : qs[s.iq_psi]);
+    w.psi = phi - 0.6 * bg.a2_k2 * rho_quadrupole + (lin ? 0.0 : qs[s.iq_psi]);
     w.phi_prime = y(s.idx_phip);
-    w.phi_pp = k_sq / 3 * (w.psi - 2 * phi) - Hc * (3 * w.phi_prime) - 2 * w.psi * (Hc * Hc + bg.Hc_prime) -
-               a_sq / 2 * (rho_mono_b + rho_mono_c) + (lin ? 0.0 : qs[s.iq_phi_prime_prime]);
+    w.phi_pp = k_sq * ONE_THIRD * (w.psi - 2 * phi) - Hc * (3 * w.phi_prime) - 2 * w.psi * (Hc * Hc + bg.Hc_prime) -
+               a_sq * 0.5 * (rho_mono_b + rho_mono_c) + (lin ? 0.0 : qs[s.iq_phi_prime_prime]);
   } else if (m == 1) {
     double rq1 = bg.rho_g * w.I_2m[1] + bg.rho_b * w.b_22m[1] + bg.rho_cdm * w.cdm_22m[1] + bg.rho_ur * gN(2, 1);
-    w.omega_m1_prime = -2 * Hc * y(s.idx_omega) + 2 * SQRT_3 / (5. * k) * a_sq * rq1 + (lin ? 0.0 : qs[s.iq_omega_m1_prime]);
+    w.omega_m1_prime = -2 * Hc * y(s.idx_omega) + (0.4 * SQRT_3) * t.inv_k * a_sq * rq1 + (lin ? 0.0 : qs[s.iq_omega_m1_prime]);
   } else {
     double rq2 = bg.rho_g * w.I_2m[2] + bg.rho_b * w.b_22m[2] + bg.rho_cdm * w.cdm_22m[2] + bg.rho_ur * gN(2, 2);
-    w.gamma_m2_pp = -2 * Hc * y(s.idx_gammap) - k_sq * y(s.idx_gamma) - 2 / 5. * a_sq * rq2 +
+    w.gamma_m2_pp = -2 * Hc * y(s.idx_gammap) - k_sq * y(s.idx_gamma) - 0.4 * a_sq * rq2 +
                     (lin ? 0.0 : qs[s.iq_gamma_m2_prime_prime]);
   }
   if (rsa && m <= 1) rsa_moments(c, y, lin, w, m);
@@ -1189,9 +1233,8 @@ __device__ double row_h(const C &c, int ap, int i, const Y &y, const WS &w, int 
   case SP_I: {
     if (ap == AP_TCA && l >= 1) return 0.0;
     if (ap == AP_NONE && l == s.l_max_g) {
-      double c_pre = (m == 0 ? (2 * l + 1) / (2 * l - 1.) : sqrt((double)(l + m) / (l - m)) * (2 * l + 1) / (2 * l - 1.));
-      double cc = (l + 1 + m) / (k * tau);
-      d = k * (c_pre * getI(c, ap, y, l - 1, m) - cc * getI(c, ap, y, l, m)) - kd * getI(c, ap, y, l, m);
+      double cc = (l + 1 + m) * bg.inv_ktau;
+      d = k * (s.cl_I[m] * getI(c, ap, y, l - 1, m) - cc * getI(c, ap, y, l, m)) - kd * getI(c, ap, y, l, m);
     } else if (l == 0) {
       d = -FOUR_THIRDS * (k * w.I_1m[0] / 4 + mc);
     } else if (l == 1) {
@@ -1212,9 +1255,8 @@ __device__ double row_h(const C &c, int ap, int i, const Y &y, const WS &w, int 
   case SP_E: {
     if (ap != AP_NONE) return 0.0;
     if (l == s.l_max_pol) {
-      double c_pre = sqrt(1 - ((double)m * m) / (l * l) * (l + 2) / (l - 2.)) * (2 * l + 1) / (2 * l - 1.);
-      double cc = (l + 3) / (k * tau), cmix = (double)m / l;
-      d = k * (c_pre * getE(c, ap, y, l - 1, m) - cc * getE(c, ap, y, l, m) - cmix * getB(c, ap, y, l, m)) -
+      double cc = (l + 3) * bg.inv_ktau;
+      d = k * (s.cl_P[m] * getE(c, ap, y, l - 1, m) - cc * getE(c, ap, y, l, m) - s.cmix_P[m] * getB(c, ap, y, l, m)) -
           kd * getE(c, ap, y, l, m);
     } else if (l == 2) {
       double Pi = 0.1 * (w.I_2m[m] - SQRT_6 * w.E_2m[m]);
@@ -1230,9 +1272,8 @@ __device__ double row_h(const C &c, int ap, int i, const Y &y, const WS &w, int 
   case SP_B: {
     if (ap != AP_NONE) return 0.0;
     if (l == s.l_max_pol) {
-      double c_pre = sqrt(1 - ((double)m * m) / (l * l) * (l + 2) / (l - 2.)) * (2 * l + 1) / (2 * l - 1.);
-      double cc = (l + 3) / (k * tau), cmix = (double)m / l;
-      d = k * (c_pre * getB(c, ap, y, l - 1, m) - cc * getB(c, ap, y, l, m) + cmix * getE(c, ap, y, l, m)) -
+      double cc = (l + 3) * bg.inv_ktau;
+      d = k * (s.cl_P[m] * getB(c, ap, y, l - 1, m) - cc * getB(c, ap, y, l, m) + s.cmix_P[m] * getE(c, ap, y, l, m)) -
           kd * getB(c, ap, y, l, m);
     } else {
       d = k * (c.dmin(l, m, m) * getB(c, ap, y, l - 1, m) - c.dplu(l, m, m) * getB(c, ap, y, l + 1, m) +
@@ -1244,9 +1285,8 @@ __device__ double row_h(const C &c, int ap, int i, const Y &y, const WS &w, int 
   }
   case SP_N: {
     if (l == s.l_max_ur) {
-      double c_pre = (m == 0 ? (2 * l + 1) / (2 * l - 1.) : sqrt((double)(l + m) / (l - m)) * (2 * l + 1) / (2 * l - 1.));
-      double cc = (l + 1 + m) / (k * tau);
-      d = k * (c_pre * getN(c, y, l - 1, m) - cc * getN(c, y, l, m));
+      double cc = (l + 1 + m) * bg.inv_ktau;
+      d = k * (s.cl_N[m] * getN(c, y, l - 1, m) - cc * getN(c, y, l, m));
     } else if (l == 0) {
       d = -FOUR_THIRDS * (k * w.N_1m[0] * 0.25 + mc);
     } else if (l == 1) {
@@ -1261,7 +1301,7 @@ __device__ double row_h(const C &c, int ap, int i, const Y &y, const WS &w, int 
     return d;
   }
   case SP_B000:
-    d = -(k * getb(c, y, 1, 0) / 3.0 + mc) - Hc * w.b_200;
+    d = -(k * getb(c, y, 1, 0) * ONE_THIRD + mc) - Hc * w.b_200;
     if (use_qs) d += c.qs[s.iq_b000];
     return d;
   case SP_B11:
@@ -1271,7 +1311,7 @@ __device__ double row_h(const C &c, int ap, int i, const Y &y, const WS &w, int 
     if (use_qs) d += c.qs[s.iq_b11[m]];
     return d;
   case SP_C000:
-    d = -(k * getc(c, y, 1, 0) / 3.0 + mc) - Hc * w.cdm_200;
+    d = -(k * getc(c, y, 1, 0) * ONE_THIRD + mc) - Hc * w.cdm_200;
     if (use_qs) d += c.qs[s.iq_c000];
     return d;
   case SP_C11:
@@ -1311,7 +1351,7 @@ __device__ double psi_prime_of(const C &c, int ap, const Y &y, const WS &w, int 
     rqp += bg.rho_cdm * 15 * t.k1_ten_k2[2] * c.qs[s.iq_vvp_cdm];
   }
   return w.phi_prime - 2 * Hc * (w.psi - y(s.idx_phi)) -
-         3 / 5. * (bg.a_sq / t.k_sq) * (rqp + Hc * bg.rho_b * w.b_22m[0] + Hc * bg.rho_cdm * w.cdm_22m[0]) +
+         0.6 * bg.a2_k2 * (rqp + Hc * bg.rho_b * w.b_22m[0] + Hc * bg.rho_cdm * w.cdm_22m[0]) +
          (lin ? 0.0 : c.qs[s.iq_psi_prime]);
 }
 
@@ -1350,6 +1390,7 @@ template <typename T, class C, class A> __device__ void newton_rhs(const C &c, i
   auto yv = yvec(y);
   compute_ws_team(c, ap, yv);
   c.sync();
+  PH_MARK(c, PH_WS);
   auto x = c.template xsol<T>();
   for (int e = c.rank; e < s.n_row_slots; e += c.size) {
     int i = c.row_slot[e];
@@ -1359,50 +1400,244 @@ template <typename T, class C, class A> __device__ void newton_rhs(const C &c, i
     }
   }
   c.sync();
+  PH_MARK(c, PH_ROWS);
+}
+
+/* ------------------------------------------------------------------ iteration matrix */
+
+/* The iteration matrix M = I - h gamma J of an NDF step is block diagonal in m
+   (azimuthal modes never couple).  Within an m block the state splits into a
+   dense core (metric and matter variables and the moments with l <= 2, at most
+   S2_MAXCORE entries) and up to three chains of moments with l >= 3: I, E
+   (paired with B in blocks that have B) and N.  Free streaming couples a moment
+   only to the same species at l - 1 and l + 1 (and E to B at the same l); the
+   Thomson term and the closure stay within one l; only the l = 3 node of a chain
+   couples to the core (to its l = 2 neighbours, and to psi' through the l = 2
+   rows).  So every chain is block tridiagonal with 1 x 1 or 2 x 2 blocks, and
+       M = [ C  F ]    C: core x core, T: the chains, F: the core rows on the
+           [ E  T ]    chains' first nodes, E: the first nodes' rows on the core.
+   The factorisation eliminates each chain from its last node upwards,
+       Theta_last = D_last,   Theta_k = D_k - U_k Theta_(k+1)^-1 L_(k+1),
+   with D, L, U the diagonal, lower and upper blocks of M, and inverts the core's
+   Schur complement S = C - sum over chains of F Theta_0^-1 E by Gauss-Jordan
+   elimination with partial pivoting.  A chain needs no pivoting: the coupling
+   coefficients of l -> l + 1 and of l + 1 -> l are positive and enter M with
+   opposite signs, so U_k L_(k+1) is a negative multiple of the identity (E and B
+   share their coefficients), and the Thomson and E-B terms add a positive
+   diagonal and a skew part; every Theta_k therefore keeps a positive definite
+   symmetric part, at least that of the identity.
+   The factors kept (layout in DevSpec ch_off / core_off): per chain node k
+   Q_k = U_k Theta_(k+1)^-1, Theta_k^-1 and P_k = Theta_k^-1 L_k; per chain
+   R = Theta_0^-1 E and F; the core's S^-1.  A solve is two sweeps along every
+   chain around one core matrix-vector product:
+       g_last = b_last,   g_k = b_k - Q_k g_(k+1),   h_k = Theta_k^-1 g_k,
+       x_core = S^-1 (b_core - sum F h_0),
+       x_0 = h_0 - R x_core,   x_k = h_k - P_k x_(k-1).
+   Work and storage are O(n) per block (against O(n kl (kl + ku)) for a banded
+   LU whose band must span the core), so the factors of every hierarchy class
+   fit in shared memory.  The factorisation stays out of line: inlined into the
+   NDF loop it raises the kernel to 255 registers (one CTA per SM); the solve
+   sweeps are inlined (a call saves and restores the caller's registers). */
+
+template <typename T> __device__ inline T tabs(T x) { return x < T(0) ? -x : x; }
+
+/* position of J(i, j), i and j in block b with structure codes pi and pj (mx_pos),
+   in the structured storage; -1 for an entry outside the structure */
+template <class C> __device__ inline int mx_slot(const C &c, int b, int pi, int pj) {
+  const DevSpec &s = c.s;
+  int ci = (pi >> 8) - 1, cj = (pj >> 8) - 1, cn = s.core_n[b];
+  if (ci < 0 && cj < 0) return s.core_off[b] + pi * cn + pj;
+  if (ci < 0) {
+    /* a core row on a chain column: the chain's first node only */
+    int d = s.ch_d[b][cj], kj = pj & 127, aj = (pj >> 7) & 1;
+    if (kj != 0) return -1;
+    return s.ch_off[b][cj] + 3 * d * d * s.ch_len[b][cj] + d * cn + pi * d + aj;
+  }
+  int d = s.ch_d[b][ci], ki = pi & 127, ai = (pi >> 7) & 1;
+  if (cj < 0) {
+    /* a chain row on a core column: the chain's first node only */
+    if (ki != 0) return -1;
+    return s.ch_off[b][ci] + 3 * d * d * s.ch_len[b][ci] + ai * cn + pj;
+  }
+  int kj = pj & 127, aj = (pj >> 7) & 1;
+  if (ci != cj || kj < ki - 1 || kj > ki + 1) return -1;
+  int part = kj == ki ? 0 : (kj < ki ? 1 : 2);
+  return s.ch_off[b][ci] + (3 * ki + part) * d * d + ai * d + aj;
 }
 
 /* Exact Jacobian of the affine system at tau (prepare(tau) must have run):
-   J[:, j] = A e_j, one thread per column; stored per m block in global scratch. */
-template <typename T, class C> __device__ __forceinline__ void jacobian(const C &c, int ap, double tau) {
+   J[:, j] = A e_j, one thread per column, scattered into the structured storage
+   in the iteration-matrix precision.  Every row of the column's block is
+   evaluated, so an entry outside the structure is detected (status
+   SONG2_E_CONFIG) instead of being dropped.  Ends with a barrier. */
+template <typename T, class C> __device__ __forceinline__ int jacobian(const C &c, int ap, double tau) {
   const DevSpec &s = c.s;
-  auto J0 = c.template jacv<T>();
-  for (int b = c.rank; b < s.nblk; b += c.size) c.sh->kl[b] = c.sh->ku[b] = 0;
+  auto J = c.template jacv<T>();
+  for (int e = c.rank; e < s.lu_elems; e += c.size) J[e] = T(0);
+  if (c.rank == 0) c.sh->mx_bad = 0;
   c.sync();
   for (int j = c.rank; j < s.n; j += c.size) {
     int b = 0;
     while (b + 1 < s.nblk && j >= s.blk_start[b + 1]) ++b;
     int b0 = s.blk_start[b], nb = s.blk_size[b];
+    int pj = __ldg(c.ct.mx_pos + j);
     YUnit yu{j};
     WS w;
     compute_ws(c, ap, yu, 1, w);
-    auto J = J0 + s.lu_off[b];
-    int lo = 0, up = 0;
     for (int i = b0; i < b0 + nb; ++i) {
-      T v = (T)row(c, ap, i, yu, w, 1, tau);
-      J[(i - b0) * nb + (j - b0)] = v;
-      if (v != T(0)) {
-        if (i > j) lo = max(lo, i - j);
-        else up = max(up, j - i);
+      double v = row(c, ap, i, yu, w, 1, tau);
+      if (v != 0.0) {
+        int slot = mx_slot(c, b, __ldg(c.ct.mx_pos + i), pj);
+        if (slot < 0) c.sh->mx_bad = 1;
+        else J[slot] = (T)v;
       }
     }
-    atomicMax(&c.sh->kl[b], lo);
-    atomicMax(&c.sh->ku[b], up);
   }
   c.sync();
+  return c.sh->mx_bad ? SONG2_E_CONFIG : SONG2_OK;
 }
 
-/* ------------------------------------------------------------------ banded LU per m block */
+/* d x d blocks, row major, d = 1 or 2 */
+template <typename T, int D> __device__ inline void mx_mul(const T *a, const T *b, T *r) {
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = 0; k < D; ++k) acc += a[i * D + k] * b[k * D + j];
+      r[i * D + j] = acc;
+    }
+}
+template <typename T, int D> __device__ inline bool mx_inv(const T *a, T *r) {
+  if constexpr (D == 1) {
+    r[0] = T(1) / a[0];
+    return tabs(a[0]) > T(0);
+  } else {
+    T det = a[0] * a[3] - a[1] * a[2];
+    T id = T(1) / det;
+    r[0] = a[3] * id; r[1] = -a[1] * id; r[2] = -a[2] * id; r[3] = a[0] * id;
+    return tabs(det) > T(0);
+  }
+}
 
-/* Within an m block the state is ordered l-major (metric and matter first, then
-   I_l, E_l, B_l, N_l for increasing l), so the iteration matrix of each block is
-   banded: free streaming couples l to l +- 1, Thomson scattering and the closure
-   stay within an l, and the Einstein and fluid equations couple the lowest
-   multipoles.  The band (kl below, ku above the diagonal) is measured on every
-   new Jacobian; the factorisation and the solves touch the band only, so their
-   cost is O(n kl (kl + ku)) and O(n (kl + ku)) per block instead of O(n^3) and
-   O(n^2).  The blocks keep their dense row-major storage. */
+/* one chain of block b, by one lane: Q_k, Theta_k^-1, P_k from the last node up,
+   then R = Theta_0^-1 E and the scaled F.  False on a zero pivot. */
+template <typename T, int D, class C, class VJ, class VF>
+__device__ __noinline__ bool chain_factor(const C &c, int b, int ch, T hg, const VJ &J, const VF &F) {
+  const DevSpec &s = c.s;
+  constexpr int D2 = D * D;
+  int len = s.ch_len[b][ch], cn = s.core_n[b], base = s.ch_off[b][ch];
+  T tn[D2], lnext[D2];
+  bool ok = true;
+  for (int k = len - 1; k >= 0; --k) {
+    int o = base + 3 * D2 * k;
+    T th[D2], ml[D2];
+#pragma unroll
+    for (int e = 0; e < D2; ++e) {
+      th[e] = (e % (D + 1) == 0 ? T(1) : T(0)) - hg * J[o + e];
+      ml[e] = -hg * J[o + D2 + e];
+    }
+    if (k < len - 1) {
+      T mu[D2], q[D2], ql[D2];
+#pragma unroll
+      for (int e = 0; e < D2; ++e) mu[e] = -hg * J[o + 2 * D2 + e];
+      mx_mul<T, D>(mu, tn, q);
+      mx_mul<T, D>(q, lnext, ql);
+#pragma unroll
+      for (int e = 0; e < D2; ++e) {
+        th[e] -= ql[e];
+        F[o + e] = q[e];
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < D2; ++e) F[o + e] = T(0);
+    }
+    T ti[D2], pk[D2];
+    ok &= mx_inv<T, D>(th, ti);
+    mx_mul<T, D>(ti, ml, pk);
+#pragma unroll
+    for (int e = 0; e < D2; ++e) {
+      F[o + D2 + e] = ti[e];
+      F[o + 2 * D2 + e] = pk[e];
+      tn[e] = ti[e];
+      lnext[e] = ml[e];
+    }
+  }
+  int oe = base + 3 * D2 * len;
+  for (int j = 0; j < cn; ++j)
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      T acc = T(0);
+#pragma unroll
+      for (int q = 0; q < D; ++q) acc += tn[a * D + q] * (-hg * J[oe + q * cn + j]);
+      F[oe + a * cn + j] = acc;
+    }
+  for (int e = 0; e < cn * D; ++e) F[oe + D * cn + e] = -hg * J[oe + D * cn + e];
+  return ok;
+}
 
-template <typename T> __device__ inline T tabs(T x) { return x < T(0) ? -x : x; }
+/* the core of block b, by a group of W lanes (after its chains): the Schur
+   complement and its inverse, in place, by Gauss-Jordan elimination with partial
+   pivoting (lane j updates columns j, j + W, ...).  False on a zero pivot. */
+template <typename T, class C, class VJ, class VF>
+__device__ __noinline__ bool core_factor(const C &c, int b, T hg, const VJ &J, const VF &F, int lane, int W, unsigned mask) {
+  const DevSpec &s = c.s;
+  int cn = s.core_n[b], co = s.core_off[b];
+  if (cn == 0) return true;
+  for (int e = lane; e < cn * cn; e += W) {
+    int i = e / cn, j = e % cn;
+    T v = (i == j ? T(1) : T(0)) - hg * J[co + e];
+    for (int ch = 0; ch < s.ch_n[b]; ++ch) {
+      int d = s.ch_d[b][ch], oe = s.ch_off[b][ch] + 3 * d * d * s.ch_len[b][ch];
+      for (int a = 0; a < d; ++a) v -= F[oe + d * cn + i * d + a] * F[oe + a * cn + j];
+    }
+    F[co + e] = v;
+  }
+  __syncwarp(mask);
+  bool ok = true;
+  int perm[S2_MAXCORE];
+  for (int p = 0; p < cn; ++p) {
+    int r = p;
+    T best = tabs((T)F[co + p * cn + p]);
+    for (int i = p + 1; i < cn; ++i) {
+      T v = tabs((T)F[co + i * cn + p]);
+      if (v > best) { best = v; r = i; }
+    }
+    perm[p] = r;
+    __syncwarp(mask);
+    if (r != p)
+      for (int j = lane; j < cn; j += W) {
+        T t = F[co + p * cn + j];
+        F[co + p * cn + j] = F[co + r * cn + j];
+        F[co + r * cn + j] = t;
+      }
+    __syncwarp(mask);
+    T colp[S2_MAXCORE];
+    for (int i = 0; i < cn; ++i) colp[i] = F[co + i * cn + p];
+    __syncwarp(mask);
+    T piv = colp[p];
+    if (!(tabs(piv) > T(0))) { ok = false; piv = T(1); }
+    T pinv = T(1) / piv;
+    for (int j = lane; j < cn; j += W) {
+      T apj = (j == p ? T(1) : (T)F[co + p * cn + j]) * pinv;
+      F[co + p * cn + j] = apj;
+      for (int i = 0; i < cn; ++i)
+        if (i != p) F[co + i * cn + j] = (j == p ? T(0) : (T)F[co + i * cn + j]) - apj * colp[i];
+    }
+    __syncwarp(mask);
+  }
+  /* undo the row interchanges on the inverse's columns, one row per lane */
+  for (int i = lane; i < cn; i += W)
+    for (int p = cn - 1; p >= 0; --p)
+      if (perm[p] != p) {
+        T t = F[co + i * cn + p];
+        F[co + i * cn + p] = F[co + i * cn + perm[p]];
+        F[co + i * cn + perm[p]] = t;
+      }
+  __syncwarp(mask);
+  return ok;
+}
 
 /* run f(b, lane, W, mask) for every block: a warp per block (CTA teams), the team
    itself otherwise */
@@ -1418,179 +1653,190 @@ template <class C, class F> __device__ void per_block_group(const C &c, F f) {
   }
 }
 
-/* One m block, factorised by a group of W lanes: partial pivoting within the band
-   with the row interchanges applied to the trailing columns only (the multipliers
-   stay where they were computed, as in LINPACK's banded factorisation), so U has
-   kl + ku superdiagonals.  The diagonal keeps the reciprocal pivot for the solves. */
-template <typename T, class C>
-__device__ void band_lu(const C &c, int b, int lane, int W, unsigned mask) {
+/* f1(b, ch) for every chain of node dimension 1 and f2(b, ch) for every chain of
+   dimension 2: in a CTA team the scalar chains run on the lanes of warp 0 and the
+   E/B chains on the lanes of warp 1, so that every warp follows one code path and
+   the two kinds run side by side; smaller teams take the chains in turn. */
+template <class C, class F1, class F2> __device__ void for_chains(const C &c, F1 f1, F2 f2) {
   const DevSpec &s = c.s;
-  auto A = c.template lu<T>() + s.lu_off[b];
-  int nb = s.blk_size[b], kl = c.sh->kl[b], kw = kl + c.sh->ku[b];
-  auto pv = c.piv + s.blk_start[b];
-  for (int k = 0; k < nb; ++k) {
-    int last = min(nb - 1, k + kl), cend = min(nb - 1, k + kw);
-    T best = T(-1);
-    int bi = k;
-    for (int i = k + lane; i <= last; i += W) {
-      T v = tabs(A[i * nb + k]);
-      if (v > best) { best = v; bi = i; }
+  if constexpr (!C::STR) {
+    if (c.size >= 64) {
+      int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      if (warp == 0 && lane < s.n_ch1) f1(s.ch1[lane] >> 4, s.ch1[lane] & 15);
+      if (warp == 1 && lane < s.n_ch2) f2(s.ch2[lane] >> 4, s.ch2[lane] & 15);
+      return;
     }
-    for (int off = W >> 1; off > 0; off >>= 1) {
-      T ob = __shfl_xor_sync(mask, best, off);
-      int oi = __shfl_xor_sync(mask, bi, off);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-    }
-    if (bi != k)
-      for (int j = k + lane; j <= cend; j += W) {
-        T tmp = A[k * nb + j];
-        A[k * nb + j] = A[bi * nb + j];
-        A[bi * nb + j] = tmp;
-      }
-    __syncwarp(mask);
-    T inv = T(1);
-    if (best > T(0)) inv = T(1) / A[k * nb + k];
-    for (int i = k + 1 + lane; i <= last; i += W) A[i * nb + k] *= inv;
-    __syncwarp(mask);
-    /* rank-1 update of the band below and right of the pivot, a column per lane */
-    for (int j = k + 1 + lane; j <= cend; j += W) {
-      T akj = A[k * nb + j];
-      if (akj != T(0))
-        for (int i = k + 1; i <= last; ++i) A[i * nb + j] -= A[i * nb + k] * akj;
-    }
-    if (lane == 0) {
-      pv[k] = bi;
-      A[k * nb + k] = inv;
-      if (!(best > T(0))) c.sh->lu_fail = 1;
-    }
-    __syncwarp(mask);
+  }
+  for (int t = c.rank; t < s.n_ch1 + s.n_ch2; t += c.size) {
+    if (t < s.n_ch1) f1(s.ch1[t] >> 4, s.ch1[t] & 15);
+    else f2(s.ch2[t - s.n_ch1] >> 4, s.ch2[t - s.n_ch1] & 15);
   }
 }
 
-/* Mixed form: the inverse of every factorised block, column by column.  Lane j of
-   a warp solves M x = e_(col0+j) with the band factors in its own column of the
-   inverse (row-major, so the lanes' entries are adjacent), with no exchange
-   between lanes; the warps of the team share the 32-column tasks.  A Newton solve
-   is then one matrix-vector product per block instead of two serial sweeps. */
-template <class C> __device__ void band_inverse(const C &c) {
-  const DevSpec &s = c.s;
-  auto LUv = c.template lu<float>();
-  float *Mi = c.minv_b;
-  int warp = 0, lane = c.rank, nw = 1;
-  if (c.size > 32) {
-    warp = threadIdx.x >> 5;
-    lane = threadIdx.x & 31;
-    nw = blockDim.x >> 5;
-  }
-  int task = 0;
-  for (int b = 0; b < s.nblk; ++b) {
-    int nb = s.blk_size[b], kl = c.sh->kl[b], kw = kl + c.sh->ku[b];
-    auto A = LUv + s.lu_off[b];
-    float *X = Mi + s.lu_off[b];
-    auto pv = c.piv + s.blk_start[b];
-    for (int col0 = 0; col0 < nb; col0 += 32, ++task) {
-      int col = col0 + lane;
-      if (task % nw != warp || col >= nb) continue;
-      for (int i = 0; i < nb; ++i) X[i * nb + col] = i == col ? 1.0f : 0.0f;
-      for (int k = 0; k < nb; ++k) {
-        int q = pv[k];
-        float xk = X[q * nb + col];
-        if (q != k) {
-          X[q * nb + col] = X[k * nb + col];
-          X[k * nb + col] = xk;
-        }
-        int last = min(nb - 1, k + kl);
-        for (int i = k + 1; i <= last; ++i) X[i * nb + col] -= A[i * nb + k] * xk;
-      }
-      for (int j = nb - 1; j >= 0; --j) {
-        float xj = X[j * nb + col] * A[j * nb + j];
-        X[j * nb + col] = xj;
-        for (int i = max(0, j - kw); i < j; ++i) X[i * nb + col] -= A[i * nb + j] * xj;
-      }
-    }
-  }
-}
-
-/* del <- M^{-1} xsol with the inverse blocks, one row per thread */
-template <class C> __device__ void inv_solve(const C &c) {
-  const DevSpec &s = c.s;
-  auto x = c.template xsol<float>();
-  for (int i = c.rank; i < s.n; i += c.size) {
-    int b = 0;
-    while (b + 1 < s.nblk && i >= s.blk_start[b + 1]) ++b;
-    int nb = s.blk_size[b], b0 = s.blk_start[b];
-    const float *row = c.minv_b + s.lu_off[b] + (i - b0) * nb;
-    float acc = 0.0f;
-    for (int j = 0; j < nb; ++j) acc += row[j] * x[b0 + j];
-    c.del[i] = (double)acc;
-  }
-  c.sync();
-}
-
-/* whether this team solves with the explicit inverse (mixed form, CTA or warp teams) */
-template <typename T, class C> __device__ inline bool use_inverse(const C &c) {
-  if constexpr (sizeof(T) == sizeof(float) && !C::STR) return c.minv_b != nullptr;
-  else return false;
-}
-
+/* M = I - hinvGak J factorised from the stored Jacobian: every chain on its own
+   lane, then the core of every block.  Ends with a barrier; sets sh->lu_fail on a
+   zero pivot. */
 template <typename T, class C> __device__ void form_and_factor(const C &c, double hinvGak) {
   const DevSpec &s = c.s;
-  auto LU = c.template lu<T>();
   auto J = c.template jacv<T>();
-  for (int e = c.rank; e < s.lu_elems; e += c.size) {
-    int b = 0;
-    while (b + 1 < s.nblk && e >= s.lu_off[b + 1]) ++b;
-    int nb = s.blk_size[b], r = (e - s.lu_off[b]) / nb, col = (e - s.lu_off[b]) % nb;
-    if constexpr (sizeof(T) == sizeof(float)) {
-      LU[e] = (r == col ? 1.0f : 0.0f) - (float)hinvGak * J[e];
-    } else {
-      double v = -hinvGak * J[e];
-      if (r == col) v += 1.0;
-      LU[e] = v;
-    }
-  }
+  auto F = c.template lu<T>();
+  T hg = (T)hinvGak;
+  for_chains(
+      c, [&](int b, int ch) { if (!chain_factor<T, 1>(c, b, ch, hg, J, F)) c.sh->lu_fail = 1; },
+      [&](int b, int ch) { if (!chain_factor<T, 2>(c, b, ch, hg, J, F)) c.sh->lu_fail = 1; });
   c.sync();
-  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { band_lu<T>(c, b, lane, W, mask); });
+  per_block_group(c, [&](int b, int lane, int W, unsigned mask) {
+    if (!core_factor<T>(c, b, hg, J, F, lane, W, mask)) c.sh->lu_fail = 1;
+  });
   c.sync();
-  if (use_inverse<T>(c)) {
-    band_inverse(c);
-    c.sync();
-  }
 }
 
-/* one m block, solved by a group of W lanes: interchange and eliminate column by
-   column, then back substitution with the reciprocal pivots */
-template <typename T, class C>
-__device__ void band_solve(const C &c, int b, int lane, int W, unsigned mask) {
+/* backward sweep of one chain: h_k = Theta_k^-1 g_k into the node entries of x.
+   The next node's right-hand side, state indices and factors are loaded before the
+   current node is stored, so the loop carries only the FMA chain of g. */
+template <typename T, int D, class C, class VF, class X>
+__device__ __forceinline__ void chain_back(const C &c, int b, int ch, const VF &F, const X &x) {
   const DevSpec &s = c.s;
-  int nb = s.blk_size[b], kl = c.sh->kl[b], kw = kl + c.sh->ku[b];
-  auto A = c.template lu<T>() + s.lu_off[b];
-  auto pv = c.piv + s.blk_start[b];
-  auto x = c.template xsol<T>() + s.blk_start[b];
-  for (int k = 0; k < nb; ++k) {
-    int q = pv[k];
-    T xk = x[q];
-    if (q != k) {
-      __syncwarp(mask);
-      if (lane == 0) { x[q] = x[k]; x[k] = xk; }
+  constexpr int D2 = D * D;
+  int len = s.ch_len[b][ch], base = s.ch_off[b][ch];
+  const short *ix = c.mx_s + s.ch_idx[b][ch];
+  T g[D], bn[D], qn[D2], tn[D2];
+  int in[D];
+  int k = len - 1;
+#pragma unroll
+  for (int a = 0; a < D; ++a) { in[a] = ix[k * D + a]; bn[a] = x[in[a]]; }
+#pragma unroll
+  for (int e = 0; e < D2; ++e) { qn[e] = F[base + 3 * D2 * k + e]; tn[e] = F[base + 3 * D2 * k + D2 + e]; }
+  for (; k >= 0; --k) {
+    T bk[D], q[D2], t[D2];
+    int ik[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) { bk[a] = bn[a]; ik[a] = in[a]; }
+#pragma unroll
+    for (int e = 0; e < D2; ++e) { q[e] = qn[e]; t[e] = tn[e]; }
+    if (k > 0) {
+      int o = base + 3 * D2 * (k - 1);
+#pragma unroll
+      for (int a = 0; a < D; ++a) { in[a] = ix[(k - 1) * D + a]; bn[a] = x[in[a]]; }
+#pragma unroll
+      for (int e = 0; e < D2; ++e) { qn[e] = F[o + e]; tn[e] = F[o + D2 + e]; }
     }
-    __syncwarp(mask);
-    int last = min(nb - 1, k + kl);
-    for (int i = k + 1 + lane; i <= last; i += W) x[i] -= A[i * nb + k] * xk;
-    __syncwarp(mask);
-  }
-  for (int j = nb - 1; j >= 0; --j) {
-    T xj = x[j] * A[j * nb + j];
-    __syncwarp(mask);
-    if (lane == 0) x[j] = xj;
-    for (int i = max(0, j - kw) + lane; i < j; i += W) x[i] -= A[i * nb + j] * xj;
-    __syncwarp(mask);
+    if (k < len - 1)
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int r = 0; r < D; ++r) bk[a] -= q[a * D + r] * g[r];
+#pragma unroll
+    for (int a = 0; a < D; ++a) g[a] = bk[a];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      T h = T(0);
+#pragma unroll
+      for (int r = 0; r < D; ++r) h += t[a * D + r] * g[r];
+      x[ik[a]] = h;
+    }
   }
 }
 
-/* xsol <- M^{-1} xsol (the right-hand side already in the solve vector) */
+/* forward sweep of one chain: x_0 = h_0 - R x_core, x_k = h_k - P_k x_(k-1), with
+   the next node's h, indices and P loaded ahead */
+template <typename T, int D, class C, class VF, class X>
+__device__ __forceinline__ void chain_fwd(const C &c, int b, int ch, const VF &F, const X &x) {
+  const DevSpec &s = c.s;
+  constexpr int D2 = D * D;
+  int len = s.ch_len[b][ch], base = s.ch_off[b][ch], cn = s.core_n[b];
+  const short *ix = c.mx_s + s.ch_idx[b][ch], *cx = c.mx_s + s.core_idx[b];
+  int oe = base + 3 * D2 * len;
+  T prev[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    T v = x[ix[a]];
+    for (int j = 0; j < cn; ++j) v -= F[oe + a * cn + j] * (T)x[cx[j]];
+    prev[a] = v;
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[ix[a]] = prev[a];
+  if (len < 2) return;
+  T hn[D], pn[D2];
+  int in[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) { in[a] = ix[D + a]; hn[a] = x[in[a]]; }
+#pragma unroll
+  for (int e = 0; e < D2; ++e) pn[e] = F[base + 3 * D2 + 2 * D2 + e];
+  for (int k = 1; k < len; ++k) {
+    T h[D], pk[D2];
+    int ik[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) { h[a] = hn[a]; ik[a] = in[a]; }
+#pragma unroll
+    for (int e = 0; e < D2; ++e) pk[e] = pn[e];
+    if (k + 1 < len) {
+      int o = base + 3 * D2 * (k + 1) + 2 * D2;
+#pragma unroll
+      for (int a = 0; a < D; ++a) { in[a] = ix[(k + 1) * D + a]; hn[a] = x[in[a]]; }
+#pragma unroll
+      for (int e = 0; e < D2; ++e) pn[e] = F[o + e];
+    }
+    T v[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      v[a] = h[a];
+#pragma unroll
+      for (int r = 0; r < D; ++r) v[a] -= pk[a * D + r] * prev[r];
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      x[ik[a]] = v[a];
+      prev[a] = v[a];
+    }
+  }
+}
+
+/* the core of block b in M x = xsol: x_core = S^-1 (b_core - sum F h_0), by a group
+   of W lanes, after the chains' backward sweeps */
+template <typename T, class C> __device__ void core_solve(const C &c, int b, int lane, int W, unsigned mask) {
+  const DevSpec &s = c.s;
+  auto F = c.template lu<T>();
+  auto x = c.template xsol<T>();
+  int nch = s.ch_n[b], cn = s.core_n[b];
+  if (cn == 0) return;
+  const short *cx = c.mx_s + s.core_idx[b];
+  for (int i = lane; i < cn; i += W) {
+    T r = x[cx[i]];
+    for (int ch = 0; ch < nch; ++ch) {
+      int d = s.ch_d[b][ch], oe = s.ch_off[b][ch] + 3 * d * d * s.ch_len[b][ch];
+      const short *ix = c.mx_s + s.ch_idx[b][ch];
+      for (int a = 0; a < d; ++a) r -= F[oe + d * cn + i * d + a] * (T)x[ix[a]];
+    }
+    x[cx[i]] = r;
+  }
+  __syncwarp(mask);
+  T out[S2_MAXCORE];
+  int cnt = 0;
+  int co = s.core_off[b];
+  for (int i = lane; i < cn; i += W) {
+    T acc = T(0);
+    for (int j = 0; j < cn; ++j) acc += F[co + i * cn + j] * (T)x[cx[j]];
+    out[cnt++] = acc;
+  }
+  __syncwarp(mask);
+  cnt = 0;
+  for (int i = lane; i < cn; i += W) x[cx[i]] = out[cnt++];
+}
+
+/* xsol <- M^{-1} xsol (the right-hand side already in the solve vector): the
+   backward sweeps of every chain, the cores, the forward sweeps, separated by
+   barriers.  Ends with a barrier. */
 template <typename T, class C> __device__ void lu_solve(const C &c) {
-  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { band_solve<T>(c, b, lane, W, mask); });
+  auto F = c.template lu<T>();
+  auto x = c.template xsol<T>();
+  for_chains(c, [&](int b, int ch) { chain_back<T, 1>(c, b, ch, F, x); },
+             [&](int b, int ch) { chain_back<T, 2>(c, b, ch, F, x); });
+  c.sync();
+  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { core_solve<T>(c, b, lane, W, mask); });
+  c.sync();
+  for_chains(c, [&](int b, int ch) { chain_fwd<T, 1>(c, b, ch, F, x); },
+             [&](int b, int ch) { chain_fwd<T, 2>(c, b, ch, F, x); });
   c.sync();
 }
 
@@ -1875,6 +2121,9 @@ template <class C> __device__ int geometry(const C &c) {
   if (tid == 0) {
     double k1 = t.k1, k2 = t.k2, k = t.k;
     t.k_sq = k * k;
+    t.inv_k = 1.0 / k;
+    t.inv_k_sq = t.inv_k * t.inv_k;
+    t.lnk = log(k);
     t.cosk1k2 = (t.k_sq - k1 * k1 - k2 * k2) / (2 * k1 * k2);
     t.cosk1k = (k1 + k2 * t.cosk1k2) / k;
     t.cosk2k = (k2 + k1 * t.cosk1k2) / k;
@@ -2096,6 +2345,11 @@ template <class C> __device__ void initial_conditions(const C &c, double tau) {
 
 /* ------------------------------------------------------------------ NDF15 */
 
+/* x^p for the step-size and order heuristics, in FP32: the choice needs a few
+   significant digits, and an FP64 pow costs hundreds of cycles of the SM's FP64
+   pipe on GB300.  x = 0 gives 0, x = inf gives inf, as pow does for p > 0. */
+__device__ inline double pow_ctl(double x, double p) { return (double)exp2f((float)p * log2f((float)x)); }
+
 __constant__ double c_G[5] = {1.0, 1.5, 11.0 / 6.0, 25.0 / 12.0, 137.0 / 60.0};
 __constant__ double c_alpha[5] = {-0.1850, -1.0 / 9.0, -0.0823, -0.0415, 0.0};
 /* U(i, j) = (-1)^(i+1) binom(j+1, i+1) (zero below the diagonal) */
@@ -2150,12 +2404,15 @@ template <class C> __device__ void do_output(const C &c, int jout, double to) {
   int ap = c.sh->ap;
   prepare_table(c, to, ap);
   rhs(c, ap, to, c.yout, c.dyout);
+  PH_MARK(c, PH_OUT_RHS);
   prepare(c, to, 1);
   compute_ws_team(c, ap, yvec(c.yout));
   c.sync();
+  PH_MARK(c, PH_OUT_QS);
   if (c.s.mode_first_order) store_first_order(c, jout, c.yout, c.dyout);
   else store_sources(c, jout, to, c.yout, c.dyout);
   c.sync();
+  PH_MARK(c, PH_OUT_STORE);
 }
 
 template <class C> __device__ inline double tout_at(const C &c, int j) {
@@ -2191,7 +2448,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
   prepare_table(c, t, ap);
   rhs(c, ap, t, y, f);
   st.n_rhs++;
-  jacobian<T>(c, ap, t);
+  if (jacobian<T>(c, ap, t)) return SONG2_E_CONFIG;
   st.n_jac++;
   int Jcurrent = 1;
   double hmin = 16 * eps * fabs(t);
@@ -2209,6 +2466,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
   double hinvGak = h * invGa[k - 1];
   int nconhk = 0;
   if (refactor<T>(c, hinvGak, st)) return SONG2_E_SINGULAR;
+  PH_MARK(c, PH_START);
   int havrate = 0;
   double rate = 0, abshlast = absh;
   int klast = k, done = 0, attempts = 0;
@@ -2223,9 +2481,11 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
     }
     if (absh != abshlast || k != klast) {
       rescale_dif(c, k, absh / abshlast);
+      PH_MARK(c, PH_RESCALE);
       hinvGak = h * invGa[k - 1];
       nconhk = 0;
       if (refactor<T>(c, hinvGak, st)) return SONG2_E_SINGULAR;
+      PH_MARK(c, PH_FACT);
       havrate = 0;
     }
     int nofailed = 1;
@@ -2246,7 +2506,9 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
           psiv[i] = ps * invGa[k - 1];
           ynew[i] = pr;
           difkp1[i] = 0.0;
-          double iw = 1.0 / fmax(fmax(fabs(yi), fabs(pr)), threshold);
+          /* error weight 1/max(|y|, |y_pred|, threshold): an FP32 reciprocal (the
+             norms it scales need no more than single precision) */
+          double iw = (double)__frcp_rn((float)fmax(fmax(fabs(yi), fabs(pr)), threshold));
           invwt[i] = iw;
           bmax(vm, pr * iw);
         }
@@ -2255,22 +2517,24 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
         h = tnew - t;
         double minnrm = 100 * eps * block_max_bits(c, vm);
         double oldnrm = 0;
+        PH_MARK(c, PH_PRED);
         prepare_table(c, tnew, ap);
+        PH_MARK(c, PH_PREP);
         for (int iter = 1; iter <= maxit; ++iter) {
           newton_rhs<T>(c, ap, tnew, ynew, hinvGak);
           st.n_rhs++;
-          bool inv = use_inverse<T>(c);
-          if (inv) inv_solve(c);
-          else lu_solve<T>(c);
+          lu_solve<T>(c);
+          PH_MARK(c, PH_SOLVE);
           unsigned long long vn = 0;
           auto xs = c.template xsol<T>();
           for (int i = tid; i < n; i += nt) {
-            double d = inv ? del[i] : (double)xs[i];
+            double d = (double)xs[i];
             bmax(vn, d * invwt[i]);
             difkp1[i] += d;
             ynew[i] += d;
           }
           double newnrm = block_max_bits(c, vn);
+          PH_MARK(c, PH_NUPD);
           if (!(newnrm < INFINITY)) break;
           if (newnrm <= minnrm) { gotynew = 1; break; }
           else if (iter == 1) {
@@ -2293,6 +2557,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
           }
           oldnrm = newnrm;
         }
+        PH_MARK(c, PH_NUPD);
         if (!gotynew) {
           st.n_newton_fail++;
           if (absh <= hmin) return SONG2_E_NEWTON;
@@ -2307,11 +2572,13 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
             nconhk = 0;
           } else {
             prepare(c, t, 0);
-            jacobian<T>(c, ap, t);
+            if (jacobian<T>(c, ap, t)) return SONG2_E_CONFIG;
             st.n_jac++;
             Jcurrent = 1;
           }
+          PH_MARK(c, PH_JAC);
           if (refactor<T>(c, hinvGak, st)) return SONG2_E_SINGULAR;
+          PH_MARK(c, PH_FACT);
           havrate = 0;
         }
       }
@@ -2337,8 +2604,8 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
           }
           /* the FP64 powers are evaluated side by side and shared */
           for (int q = tid; q < 2; q += nt) {
-            if (q == 0) c.sh->ctl[0] = absh * fmax(0.1, 0.833 * pow(rtol / err, 1.0 / (k + 1)));
-            else if (k > 1) c.sh->ctl[1] = absh * fmax(0.1, 0.769 * pow(rtol / errkm1, 1.0 / k));
+            if (q == 0) c.sh->ctl[0] = absh * fmax(0.1, 0.833 * pow_ctl(rtol / err, 1.0 / (k + 1)));
+            else if (k > 1) c.sh->ctl[1] = absh * fmax(0.1, 0.769 * pow_ctl(rtol / errkm1, 1.0 / k));
           }
           c.sync();
           double hopt = c.sh->ctl[0];
@@ -2356,16 +2623,20 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
         }
         h = absh;
         if (absh < abshl) done = 0;
+        PH_MARK(c, PH_ERR);
         rescale_dif(c, k, absh / abshl);
+        PH_MARK(c, PH_RESCALE);
         abshlast = absh;
         klast = k;
         hinvGak = h * invGa[k - 1];
         nconhk = 0;
         if (refactor<T>(c, hinvGak, st)) return SONG2_E_SINGULAR;
+        PH_MARK(c, PH_FACT);
         havrate = 0;
       } else
         break;
     }
+    PH_MARK(c, PH_ERR);
     /* accepted step */
     st.n_steps++;
     for (int i = tid; i < n; i += nt) {
@@ -2375,6 +2646,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
       for (int j = k - 1; j >= 0; --j) dif[(size_t)j * n + i] += dif[(size_t)(j + 1) * n + i];
     }
     c.sync();
+    PH_MARK(c, PH_ACCEPT);
     while (jout < nout && tout_at(c, jout) <= tnew) {
       double to = tout_at(c, jout);
       if (to > t || (include_t0 && to == t)) {
@@ -2408,13 +2680,13 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
       for (int q = tid; q < 3; q += nt) {
         double temp, hq = 0.0;
         if (q == 0) {
-          temp = 1.2 * pow(err / rtol, 1.0 / (k + 1));
+          temp = 1.2 * pow_ctl(err / rtol, 1.0 / (k + 1));
           hq = (temp > 0.1) ? absh / temp : 10 * absh;
         } else if (q == 1 && k > 1) {
-          temp = 1.3 * pow(errkm1 * erconst[k - 2] / rtol, 1.0 / k);
+          temp = 1.3 * pow_ctl(errkm1 * erconst[k - 2] / rtol, 1.0 / k);
           hq = (temp > 0.1) ? absh / temp : 10 * absh;
         } else if (q == 2 && k < maxk) {
-          temp = 1.4 * pow(errkp1 * erconst[k] / rtol, 1.0 / (k + 2));
+          temp = 1.4 * pow_ctl(errkp1 * erconst[k] / rtol, 1.0 / (k + 2));
           hq = (temp > 0.1) ? absh / temp : 10 * absh;
         }
         c.sh->ctl[q] = hq;
@@ -2433,6 +2705,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
     t = tnew;
     for (int i = tid; i < n; i += nt) y[i] = ynew[i];
     c.sync();
+    PH_MARK(c, PH_CTRL);
     Jcurrent = 0;
   }
   return SONG2_OK;
@@ -2448,7 +2721,9 @@ template <typename T, class C> __device__ __forceinline__ int solve_triplet(cons
   c.sync();
   if (c.sh->lu_fail) return SONG2_E_CONFIG;
   Tri &t = c.sh->tri;
+  PH_MARK(c, PH_SETUP);
   build_qs_table(c);
+  PH_MARK(c, PH_QTAB);
   int jout = 0;
   for (int iv = 0; iv < t.nint; ++iv) {
     double ta = t.ivb[iv], tb = t.ivb[iv + 1];
@@ -2485,6 +2760,7 @@ template <typename T, class C> __device__ __forceinline__ int solve_triplet(cons
       }
       c.sync();
     }
+    PH_MARK(c, PH_IC);
     int stc = ndf15<T>(c, ta, tb, jout, iv == 0, st);
     if (stc != SONG2_OK) return stc;
   }
@@ -2510,21 +2786,26 @@ template <class C> __device__ void begin_item(const C &c, int item) {
 }
 
 template <typename T, class C> __device__ __forceinline__ void run_item(const C &c, int item) {
+  PH_RESET(c);
   begin_item(c, item);
   song2_triplet_stats st;
   st.status = 0; st.n_steps = 0; st.n_rejected = 0; st.n_rhs = 0; st.n_jac = 0; st.n_lu = 0; st.n_newton_fail = 0;
   st.sources_calls = 0;
+  st.retried = 0;
   int stc = solve_triplet<T>(c, st);
   st.status = stc;
-  if (c.rank == 0) c.p.stats[item] = st;
+  if (c.rank == 0) c.p.stats[c.p.stats_by_ref ? c.p.items[item].ref : item] = st;
+  PH_ITEM_END(c);
   c.sync();
 }
 
 /* CTA or warp per triplet: persistent, one item at a time from the queue.  With
    hierarchy classes (uneven batches, CTA teams only) the item's class spec is
-   copied into shared memory and the team's context is rebuilt for it. */
-template <typename T, int MODE, int CLASSES>
-__global__ void __launch_bounds__(256) evolver_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
+   copied into shared memory and the team's context is rebuilt for it.  MINB is the
+   number of CTAs per SM the register allocation must allow (2 for the launch group
+   of small hierarchy classes, whose shared-memory plans fit two CTAs per SM). */
+template <typename T, int MODE, int CLASSES, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) evolver_kernel(const __grid_constant__ DevSpec s, const __grid_constant__ DevPtrs p) {
   extern __shared__ __align__(16) char smem[];
   __shared__ int s_item[8];
   const int prec = sizeof(T) == sizeof(float) ? SONG2_PREC_MIXED : SONG2_PREC_FP64;

@@ -603,3 +603,73 @@ int song2_tau_grid(int log_sampling, double tau_ini, double tau_end, int tau_siz
   else lin_space(out, tau_ini, tau_end, tau_size);
   return 0;
 }
+
+/* ------------------------------------------------------------ table providers */
+
+int song2_first_order_from_provider(const song2_spec *spec, int fo_l_max, int fo_tau_size, double fo_lntau0,
+                                    double fo_dlntau, song2_fo_provider provider, void *user, int n_provided,
+                                    const int *qs_map, double *fo_out, double *fo_dd_out, song2_tables *tab,
+                                    char *err) {
+  int nq = song2_fo_size(fo_l_max);
+  if (!spec || !provider || !qs_map || !fo_out || !fo_dd_out || !tab || fo_tau_size < 3 || n_provided < 1 ||
+      !(fo_dlntau > 0)) {
+    snprintf(err, SONG2_ERRLEN, "first-order provider: bad arguments");
+    return 1;
+  }
+  for (int q = 0; q < nq; ++q)
+    if (qs_map[q] >= n_provided) {
+      snprintf(err, SONG2_ERRLEN, "first-order provider: quantity %d maps to %d, beyond the %d provided", q,
+               qs_map[q], n_provided);
+      return 1;
+    }
+  double *row = (double *)malloc(sizeof(double) * (size_t)n_provided);
+  if (!row) {
+    snprintf(err, SONG2_ERRLEN, "first-order provider: out of host memory");
+    return 1;
+  }
+  for (int ik = 0; ik < spec->k_size; ++ik) {
+    double *blk = fo_out + (size_t)ik * fo_tau_size * nq;
+    for (int j = 0; j < fo_tau_size; ++j) {
+      double tau = exp(fo_lntau0 + j * fo_dlntau);
+      if (provider(user, ik, spec->k[ik], tau, row)) {
+        snprintf(err, SONG2_ERRLEN, "first-order provider failed at k[%d] = %g, tau = %g", ik, spec->k[ik], tau);
+        free(row);
+        return 1;
+      }
+      for (int q = 0; q < nq; ++q) blk[(size_t)j * nq + q] = qs_map[q] < 0 ? 0.0 : row[qs_map[q]];
+    }
+    song2_spline_uniform(fo_tau_size, nq, fo_dlntau, blk, fo_dd_out + (size_t)ik * fo_tau_size * nq);
+  }
+  free(row);
+  tab->fo_k_size = spec->k_size;
+  tab->fo_tau_size = fo_tau_size;
+  tab->fo_lntau0 = fo_lntau0;
+  tab->fo_dlntau = fo_dlntau;
+  tab->fo_l_max = fo_l_max;
+  tab->fo_size = nq;
+  tab->fo = fo_out;
+  tab->fo_dd = fo_dd_out;
+  return 0;
+}
+
+int song2_background_from_provider(int bg_size, double bg_lntau0, double bg_dlntau, song2_bg_provider provider,
+                                   void *user, double *bg_out, double *bg_dd_out, song2_tables *tab, char *err) {
+  if (!provider || !bg_out || !bg_dd_out || !tab || bg_size < 3 || !(bg_dlntau > 0)) {
+    snprintf(err, SONG2_ERRLEN, "background provider: bad arguments");
+    return 1;
+  }
+  for (int j = 0; j < bg_size; ++j) {
+    double tau = exp(bg_lntau0 + j * bg_dlntau);
+    if (provider(user, tau, bg_out + (size_t)j * SONG2_BG_SIZE)) {
+      snprintf(err, SONG2_ERRLEN, "background provider failed at tau = %g", tau);
+      return 1;
+    }
+  }
+  song2_spline_uniform(bg_size, SONG2_BG_SIZE, bg_dlntau, bg_out, bg_dd_out);
+  tab->bg_size = bg_size;
+  tab->bg_lntau0 = bg_lntau0;
+  tab->bg_dlntau = bg_dlntau;
+  tab->bg = bg_out;
+  tab->bg_dd = bg_dd_out;
+  return 0;
+}

@@ -13,6 +13,8 @@
 #define S2_LMAXP (SONG2_MAX_L + 4)
 #define S2_MAXBLK SONG2_MAX_M
 #define S2_MAXTP 64
+#define S2_MAXCH 3          /* moment chains per m block (I, E/B, N) */
+#define S2_MAXCORE 16       /* largest dense core of an m block */
 
 /* species codes of the state vector and of the quadratic-source vector */
 enum { SP_I = 0, SP_E, SP_B, SP_N, SP_B000, SP_B11, SP_C000, SP_C11, SP_PHI, SP_PHIP, SP_OMEGA, SP_GAMMA, SP_GAMMAP,
@@ -24,6 +26,10 @@ enum { TP_T = 0, TP_E, TP_B, TP_D };
 /* Everything that is constant for a run; passed to the kernel by value. */
 struct DevSpec {
   int l_max_g, l_max_pol, l_max_ur, l_los_t, l_los_p;
+  /* closure coefficients of the hierarchies at their l_max per m
+     (perturbations2.c:7931-7941, 8024-8036, 8120-8130): the l_max - 1 coupling of
+     I and N, of E and B, and the E-B mixing m / l_max_pol */
+  double cl_I[SONG2_MAX_M], cl_N[SONG2_MAX_M], cl_P[SONG2_MAX_M], cmix_P[SONG2_MAX_M];
   int m_size, m[SONG2_MAX_M], compute_m[SONG2_MAX_M], index_m[SONG2_MAX_M];
   int index_m_max[S2_LMAXP];
   int L_big, Lq, mq_max;          /* rotation coefficients for l <= Lq, 0 <= m <= mq_max */
@@ -51,6 +57,7 @@ struct DevSpec {
   int iq_omega_m1_prime, iq_gamma_m2_prime_prime, iq_vv_g, iq_vv_ur, iq_dd_b, iq_vv_b, iq_vv_cdm;
   int iq_vvp_b, iq_vvp_cdm;        /* d/dtau of the velocity products (psi') */
   int n_row_slots, n_qs_slots;     /* species-grouped, warp-padded evaluation orders */
+  int n_qo_slots;                  /* the same for the entries an output time needs */
   short iq_b11[2], iq_c11[2], iq_b000, iq_c000;
   /* state layout (grouped by m blocks) */
   int n;
@@ -72,17 +79,37 @@ struct DevSpec {
   /* launch: lanes per triplet of the team kernel (1..32) */
   int team_lanes;
   /* shared-memory plan */
-  int lu_in_smem;
-  int lu_elems;                    /* sum of blk_size^2 */
-  int lu_stride;                   /* per-team Jacobian/LU scratch (>= lu_elems; the largest class) */
+  int lu_in_smem;                  /* factors of the iteration matrix in shared memory */
+  int lu_elems;                    /* elements of the structured Jacobian (and of its factors) */
+  int lu_stride;                   /* per-team Jacobian/factor scratch (>= lu_elems; the largest class) */
   long qtab_stride;                /* per-team quadratic-source table (doubles) */
-  int lu_off[S2_MAXBLK];
+  /* Structured iteration matrix of every m block.  The block's state splits into a
+     dense core (metric and matter variables and the moments with l <= 2) and up to
+     S2_MAXCH chains of moments with l >= 3 (I; E, or E and B paired when the block
+     has B; N), each coupling only neighbouring l, and coupling to the core only
+     through its first node.  Per block: the core's size, the offset of its state
+     indices in the mx_idx table and of its storage; per chain: the node dimension
+     d (1, or 2 for E/B pairs), the number of nodes, and the same two offsets.  The
+     Jacobian and its factors share one layout (lu_elems elements):
+       chain: per node k, three d x d blocks (J: diagonal, lower, upper coupling;
+              factors: Q_k, Theta_k^-1, P_k), then a d x core block (J: node 0 on
+              the core; factors: R) and a core x d block (J and factors: the core
+              rows on node 0);
+       core:  core x core (J: the core block; factors: the inverse Schur complement). */
+  int core_n[S2_MAXBLK], core_idx[S2_MAXBLK], core_off[S2_MAXBLK];
+  int ch_n[S2_MAXBLK];
+  int ch_d[S2_MAXBLK][S2_MAXCH], ch_len[S2_MAXBLK][S2_MAXCH], ch_idx[S2_MAXBLK][S2_MAXCH], ch_off[S2_MAXBLK][S2_MAXCH];
+  /* the chains of every block listed by node dimension (block << 4 | chain), so
+     that the lanes of a warp sweep chains of one kind along one code path */
+  int n_ch1, n_ch2;
+  short ch1[S2_MAXBLK * S2_MAXCH], ch2[S2_MAXBLK * S2_MAXCH];
 };
 
 /* Per-triplet work item: indices and where its sources go. */
 struct WorkItem {
   int i1, i2, i3, pair;            /* pair = index of (i1,i2) in pair order */
   int cls;                         /* hierarchy class (uneven batches), else 0 */
+  int ref;                         /* index in the reference work order (k1 descending, k2 <= k1, k3) */
 };
 
 /* Tables that depend on the hierarchy layout (one set per class in uneven batches). */
@@ -92,6 +119,11 @@ struct ClassTabs {
   const short *idx_I, *idx_E, *idx_B, *idx_N;        /* [n_lm] -> state index or -1 */
   const short *qs_sp, *qs_l, *qs_m;                  /* [qs2_size] */
   const short *row_slot, *qs_slot;                   /* [n_row_slots], [n_qs_slots]: index or -1 */
+  const short *qo_slot;                              /* [n_qo_slots]: entries read at output times */
+  const short *mx_idx;                               /* [n]: state indices of the cores and chain nodes */
+  const short *mx_pos;                               /* [n]: position of a state index in its block's
+                                                        structure: (chain + 1) << 8 | component << 7 | node,
+                                                        or the core position (chain field 0) */
 };
 
 /* Device pointers of a run. */
@@ -106,17 +138,45 @@ struct DevPtrs {
   const WorkItem *items;
   double *sources;                 /* [tp2][per_type] */
   double *fo_out;                  /* first-order mode: [k][tau][q] */
-  song2_triplet_stats *stats;      /* [n_items] */
-  double *jac;                     /* per-team scratch: sum blk^2 doubles each */
+  song2_triplet_stats *stats;      /* [n_items], or [n_triplets] in reference work order (stats_by_ref) */
+  int stats_by_ref;                /* write a triplet's stats at its WorkItem::ref */
+  double *jac;                     /* per-team structured Jacobian: lu_stride elements of the
+                                      iteration-matrix precision */
   double *qtab;                    /* per-team quadratic-source table: fo_tau_size x 2 x qs2_size doubles */
   const double *spl_c;             /* Thomas recurrence of the natural spline on a uniform grid */
   const double *dt_coup;           /* delta-tilde couplings, see dt_index() */
-  void *lu_global;                 /* per-team LU scratch when not in smem */
-  float *minv_global;              /* mixed form: per-team inverse of the LU blocks when not in smem */
+  void *lu_global;                 /* per-team factor scratch when not in smem */
   double *tslab;                   /* team kernel: per-team vectors, 32/G teams interleaved per warp */
   void *txsol;                     /* team kernel: solve vectors (iteration-matrix precision) */
-  int *tpiv;                       /* team kernel: pivots */
   int *queue;                      /* work-queue counter */
+  unsigned long long *phase;       /* builds with SONG2_PHASE_TIMERS: [S2_NPHASE][2] cycles, count */
+};
+
+/* Phases of the per-phase cycle counters (builds with SONG2_PHASE_TIMERS only):
+   thread 0 of each team attributes the SM clock cycles since its previous mark to
+   the phase that has just ended. */
+enum {
+  PH_SETUP = 0,   /* work item, geometry, start time and approximation intervals */
+  PH_QTAB,        /* per-triplet quadratic-source table and its spline */
+  PH_IC,          /* interval start: initial conditions or TCA remap */
+  PH_START,       /* NDF start: first right-hand side, Jacobian, factorisation */
+  PH_RESCALE,     /* backward differences rescaled for a new step size or order */
+  PH_FACT,        /* iteration matrix formed and factorised (and inverted) */
+  PH_PRED,        /* predictor, error weights and their norm */
+  PH_PREP,        /* background and interpolated quadratic sources at t_new */
+  PH_WS,          /* workspace scalars of the Newton right-hand side */
+  PH_ROWS,        /* rows of the Newton right-hand side */
+  PH_SOLVE,       /* linear solve */
+  PH_NUPD,        /* Newton update, norm and convergence test */
+  PH_JAC,         /* Jacobian refresh after a failed Newton iteration */
+  PH_ERR,         /* local error estimate, rejection and its step-size choice */
+  PH_ACCEPT,      /* backward differences of the accepted step */
+  PH_OUT_RHS,     /* output: state interpolated, derivs at the sampling time */
+  PH_OUT_QS,      /* output: direct quadratic sources and workspace */
+  PH_OUT_STORE,   /* output: source functions written */
+  PH_CTRL,        /* step-size and order selection, state copy */
+  PH_ITEM,        /* whole triplets (count = triplets) */
+  S2_NPHASE = 24
 };
 
 /* Position of the delta-tilde coupling of (field, l, m, l1, m1, l2) in
@@ -130,9 +190,10 @@ inline int dt_table_size(const DevSpec &s) { return 3 * (s.dt_L + 1) * SONG2_MAX
 
 /* host-side launcher implemented in song2_launch.cu.  mode 0: one CTA per
    triplet; 1: one warp per triplet (several per CTA); 2: spec.team_lanes lanes per
-   triplet, arrays in global slabs (tslab, txsol, tpiv, jac, lu_global, qtab);
+   triplet, arrays in global slabs (tslab, txsol, jac, lu_global, qtab);
    3: one CTA per triplet with hierarchy classes (ptrs.class_spec set; the dynamic
-   shared memory starts with song2_class_spec_bytes() for the class spec copy).
+   shared memory starts with song2_class_spec_bytes() for the class spec copy);
+   4: the same with registers for two CTAs per SM.
    Mode 0 with ptrs.class_spec set launches mode 3. */
 int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int mode, int grid, int block,
                          size_t smem, cudaStream_t stream);

@@ -11,6 +11,8 @@ void *song2_kernel_warp_f();
 void *song2_kernel_warp_d();
 void *song2_kernel_class_f();
 void *song2_kernel_class_d();
+void *song2_kernel_class2_f();
+void *song2_kernel_class2_d();
 void *song2_kernel_team_f();
 void *song2_kernel_team_d();
 
@@ -29,13 +31,14 @@ int song2_team_slab_doubles(const DevSpec &spec) { return make_team_plan(spec).t
 
 namespace {
 /* mode 0: CTA per triplet; 1: warp per triplet; 2: lane teams; 3: CTA per triplet
-   with hierarchy classes */
+   with hierarchy classes; 4: the same with registers for two CTAs per SM */
 void *pick_kernel(int precision, int mode) {
   int f = precision == SONG2_PREC_MIXED;
   switch (mode) {
   case 1: return f ? song2_kernel_warp_f() : song2_kernel_warp_d();
   case 2: return f ? song2_kernel_team_f() : song2_kernel_team_d();
   case 3: return f ? song2_kernel_class_f() : song2_kernel_class_d();
+  case 4: return f ? song2_kernel_class2_f() : song2_kernel_class2_d();
   default: return f ? song2_kernel_block_f() : song2_kernel_block_d();
   }
 }
@@ -51,7 +54,7 @@ int song2_max_ctas_per_sm(int precision, int mode, int block, size_t smem) {
 
 int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int mode, int grid, int block,
                          size_t smem, cudaStream_t stream) {
-  if (ptrs.class_spec && mode == 0) mode = 3;
+  if (ptrs.class_spec && mode < 3) mode = 3;
   const void *f = pick_kernel(precision, mode);
   cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   DevSpec sp = spec;

@@ -32,6 +32,36 @@ def gpu_run(lib, prob, precision):
     return src, np.frombuffer(st, dtype=capi.STATS_DTYPE).copy(), ms
 
 
+def nested_slabs(prob):
+    """Host slabs in the reference layout sources[tp][k1][k2<=k1][tau*k3_size+k3]
+    (ppt2->sources) as a double**** for the drop-in entry, and a function that
+    gathers them into a flat buffer."""
+    n = len(prob.k)
+    keep, bufs = [], []
+    tp_level = (C.POINTER(C.POINTER(C.POINTER(C.c_double))) * prob.tp2_size)()
+    for tp in range(prob.tp2_size):
+        k1_level = (C.POINTER(C.POINTER(C.c_double)) * n)()
+        for i1 in range(n):
+            k2_level = (C.POINTER(C.c_double) * (i1 + 1))()
+            for i2 in range(i1 + 1):
+                buf = np.zeros(len(prob.tau) * int(prob.k3_size[i1 * n + i2]))
+                bufs.append((tp, i1, i2, buf))
+                k2_level[i2] = capi.dptr(buf)
+            keep.append(k2_level)
+            k1_level[i1] = k2_level
+        keep.append(k1_level)
+        tp_level[tp] = k1_level
+
+    def gather():
+        flat = np.zeros(prob.tp2_size * prob.per_type)
+        nested = prob.to_nested(flat)
+        for tp, i1, i2, buf in bufs:
+            nested[tp][i1][i2][:] = buf
+        return flat
+    gather.keep = (keep, bufs, tp_level)
+    return C.cast(tp_level, C.c_void_p), gather
+
+
 def floored_errors(test, ref, prob, floor=1e-10):
     """max_tau |S - S_ref| / max_tau |S_ref| per (triplet, source type); the denominator is
     floored at `floor` times the largest source of the triplet, because odd-m sources vanish

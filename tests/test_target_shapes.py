@@ -1,0 +1,134 @@
+"""GPU evolver against the oracle on triplets of the benchmark workloads themselves.
+
+The other parity tests use small hierarchies.  Here the triplets come from the
+uneven batch (50 log k in [1e-5, 0.3]/Mpc, 24 k3 per pair, l_max = min(40, 8 +
+ceil(k tau_rec / 2)), m_max in {0, 2, 4}, T+E+B, 200 source times) and from the
+plain configuration (l_max 12, m in {0, 1, 2}, T+E, 200 source times): for every
+m_max the cheapest triplet of the smallest, a middle and the largest l_max class,
+so that the largest hierarchies (744 equations, five azimuthal blocks) and every
+hierarchy shape are covered.  Both precisions are run through a triplet-list
+context (song2_ctx_create_list) and compared with the oracle at the same rtol
+(bound 10 rtol, as the other parity tests), and an rtol = 1e-5 GPU run is
+compared with the oracle at rtol = 1e-8 (every source within 1e-4 of its maximum
+over time)."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from song_gb300 import capi
+from song_gb300.problem import config_problem
+
+pytestmark = pytest.mark.gpu
+THREADS = os.cpu_count() or 8
+
+
+def class_extremes(p):
+    """Work-order indices: for every m_max, the cheapest triplet (smallest largest
+    wavenumber) of the smallest, a middle and the largest l_max class."""
+    work = p.work_order()
+    n = len(p.k)
+    start, off = {}, 0
+    for i1 in range(n):
+        for i2 in range(i1 + 1):
+            start[(i1, i2)] = off
+            off += int(p.k3_size[i1 * n + i2])
+    cls, kmax = [], []
+    for (i1, i2, i3) in work:
+        cls.append(p.classes[int(p.triplet_class[start[(i1, i2)] + i3])])
+        kmax.append(max(p.k[i1], p.k[i2], p.k3[start[(i1, i2)] + i3]))
+    pick = []
+    for m in sorted({c[1] for c in cls}):
+        ls = sorted({c[0] for c in cls if c[1] == m})
+        for L in (ls[0], ls[len(ls) // 2], ls[-1]):
+            cand = [t for t in range(len(cls)) if cls[t] == (L, m)]
+            pick.append(min(cand, key=lambda t: kmax[t]))
+    return np.array(sorted(set(pick)), dtype=np.int64), cls
+
+
+def gpu_list(lib, p, items, precision, rtol=None):
+    spec = capi.Spec.from_buffer_copy(p.spec)
+    if rtol is not None:
+        spec.rtol = rtol
+    c = C.c_void_p()
+    err = capi.errbuf()
+    arr = np.ascontiguousarray(items, dtype=np.int64)
+    assert lib.song2_ctx_create_list(C.byref(spec), C.byref(p.tables), precision,
+                                     arr.ctypes.data_as(C.POINTER(C.c_int64)), len(arr), C.byref(c), err) == 0, \
+        err.value
+    try:
+        assert lib.song2_ctx_run(c, None, err) == 0, err.value
+        src = np.zeros(p.tp2_size * p.per_type)
+        st = (capi.TripletStats * p.n_triplets)()
+        assert lib.song2_ctx_download(c, capi.dptr(src), st, err) == 0, err.value
+    finally:
+        lib.song2_ctx_destroy(c)
+    return src, np.frombuffer(st, dtype=capi.STATS_DTYPE).copy()
+
+
+def errors_on(p, test, ref, items, floor=1e-10):
+    """max_tau |S - S_ref| / max_tau |S_ref| per (listed triplet, source type), the
+    denominator floored at `floor` times the triplet's largest source (as
+    helpers.floored_errors, restricted to the listed triplets)."""
+    work = p.work_order()
+    a = test.reshape(p.tp2_size, p.per_type)
+    b = ref.reshape(p.tp2_size, p.per_type)
+    out = []
+    for it in items:
+        i1, i2, i3 = work[int(it)]
+        ta, tb = p.triplet_view(a, i1, i2, i3), p.triplet_view(b, i1, i2, i3)
+        den = np.max(np.abs(tb), axis=1)
+        den = np.maximum(den, floor * max(den.max(), 1e-300))
+        out.append(np.max(np.abs(ta - tb), axis=1) / den)
+    return np.array(out)
+
+
+@pytest.fixture(scope="module")
+def uneven(lib):
+    p = config_problem(4)
+    p.first_order_gpu()
+    items, cls = class_extremes(p)
+    return p, items, cls
+
+
+def test_uneven_classes_match_oracle(lib, uneven):
+    p, items, cls = uneven
+    assert {cls[t][1] for t in items} == {0, 2, 4}
+    assert max(cls[t][0] for t in items) == 40
+    ref, st_ref = oracle.evolve(p, nthreads=THREADS, items=items)
+    assert np.all(st_ref["status"][items] == capi.SONG2_OK)
+    for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+        src, st = gpu_list(lib, p, items, precision)
+        assert np.all(st["status"][items] == capi.SONG2_OK)
+        assert np.all(st["sources_calls"][items] == len(p.tau))
+        e = errors_on(p, src, ref, items)
+        assert np.max(e) < 10 * p.spec.rtol, (precision, np.max(e))
+
+
+def test_uneven_classes_against_tight_oracle(lib, uneven):
+    """rtol = 1e-5 on the GPU against the oracle at rtol = 1e-8: every source of
+    every sampled class within 1e-4 of its maximum over time."""
+    p, items, _ = uneven
+    tight, st_t = oracle.evolve(p, nthreads=THREADS, items=items, rtol=1e-8)
+    assert np.all(st_t["status"][items] == capi.SONG2_OK)
+    for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+        src, st = gpu_list(lib, p, items, precision, rtol=1e-5)
+        assert np.all(st["status"][items] == capi.SONG2_OK)
+        e = errors_on(p, src, tight, items)
+        assert np.max(e) < 1e-4, (precision, np.max(e))
+
+
+def test_plain_configuration_matches_oracle(lib):
+    """Triplets of the 4,875-triplet plain configuration (l_max 12, 200 times)."""
+    p = config_problem(2)
+    p.first_order_gpu()
+    order = np.arange(p.n_triplets)
+    items = order[:: max(1, p.n_triplets // 12)][:12]
+    ref, _ = oracle.evolve(p, nthreads=THREADS, items=items)
+    for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+        src, st = gpu_list(lib, p, items, precision)
+        assert np.all(st["status"][items] == capi.SONG2_OK)
+        e = errors_on(p, src, ref, items)
+        assert np.max(e) < 10 * p.spec.rtol, (precision, np.max(e))

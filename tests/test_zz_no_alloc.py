@@ -1,14 +1,15 @@
 """The allocation-free evolver (song2_gpu_evolve_noalloc) against the regular
 C-ABI path.
 
-Some callers cannot allocate device memory: code recorded into a CUDA graph,
-applications whose GPU memory belongs to a fixed pool or another runtime, and
-services that forbid cudaMalloc after start-up.  The allocation-free entry point
-serves them by keeping all its scratch in a fixed array compiled into the
-library; this test checks, through the C ABI, that two calls in a row give the
-same sources as the regular entry point, within the tolerance of the other
-parity tests.  The test allocates the input and output buffers itself, as such
-a caller would have them from its own pool.
+Some callers cannot allocate device memory: applications whose GPU memory
+belongs to a fixed pool or to another runtime, and services that forbid
+cudaMalloc after start-up.  The allocation-free entry point serves them by
+keeping all its scratch in a fixed array compiled into the library; this test
+checks, through the C ABI, that two calls in a row give the same sources as the
+regular entry point, within the tolerance of the other parity tests, and that
+every triplet's stats land in its slot of the reference work order (the same
+step counts as the regular entry's).  The test allocates the input and output
+buffers itself, as such a caller would have them from its own pool.
 """
 import ctypes as C
 
@@ -48,6 +49,8 @@ def test_noalloc_matches_regular_entry_twice(lib, kw):
         assert rc == 0, err.value
         torch.cuda.synchronize()
         got = src.cpu().numpy()
-        status = stats.view(-1, C.sizeof(capi.TripletStats) // 4)[:, 0].cpu().numpy()
-        assert np.all(status == capi.SONG2_OK)
+        st = stats.view(-1, C.sizeof(capi.TripletStats) // 4).cpu().numpy()
+        assert np.all(st[:, 0] == capi.SONG2_OK)
+        # stats in the reference work order: each triplet's step count is the regular run's
+        assert np.array_equal(st[:, 1], st_ref["n_steps"]), call
         assert np.max(floored_errors(got, ref, p)) < 10 * p.spec.rtol, call
