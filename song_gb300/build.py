@@ -23,7 +23,7 @@ CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall"]
 
 C_SOURCES = ["song2_host.c"]
 CU_SOURCES = ["song2_k_block_f.cu", "song2_k_block_d.cu", "song2_k_class_f.cu", "song2_k_class_d.cu",
-              "song2_k_class2_f.cu", "song2_k_class2_d.cu",
+              "song2_k_class2_f.cu", "song2_k_class2_d.cu", "song2_k_block2_f.cu", "song2_k_block2_d.cu",
               "song2_k_warp_f.cu", "song2_k_warp_d.cu", "song2_k_team_f.cu", "song2_k_team_d.cu",
               "song2_launch.cu", "song2_capi.cu"]
 

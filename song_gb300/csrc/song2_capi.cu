@@ -36,6 +36,7 @@ struct song2_ctx {
   float last_ms;
   int last_launches;
   song2_launch launch;
+  int kmode;    /* kernel of single-group runs (song2_launch_evolver's mode) */
   int n_teams;
   /* uneven batches: consecutive item ranges launched one after the other, the
      classes with large shared-memory plans first, so that the small ones run
@@ -489,6 +490,8 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
   s.bg_size = tab->bg_size;
   s.bg_lntau0 = tab->bg_lntau0;
   s.bg_dlntau = tab->bg_dlntau;
+  s.bg_inv_dx = 1.0 / tab->bg_dlntau;
+  s.bg_dx2_6 = tab->bg_dlntau * tab->bg_dlntau / 6.0;
   if (!first_order_mode) {
     s.fo_l_max = tab->fo_l_max;
     s.nfo = song2_fo_size(tab->fo_l_max);
@@ -503,6 +506,8 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
     s.fo_tau_size = tab->fo_tau_size;
     s.fo_lntau0 = tab->fo_lntau0;
     s.fo_dlntau = tab->fo_dlntau;
+    s.fo_inv_dx = 1.0 / tab->fo_dlntau;
+    s.fo_dx2_6 = tab->fo_dlntau * tab->fo_dlntau / 6.0;
     s.fo_k_size = tab->fo_k_size;
   }
   s.fo_E = SONG2_FO_I + (s.fo_l_max + 1);
@@ -630,6 +635,8 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     s.fo_tau_size = fo_tau_size;
     s.fo_lntau0 = fo_lntau0;
     s.fo_dlntau = fo_dlntau;
+    s.fo_inv_dx = 1.0 / fo_dlntau;
+    s.fo_dx2_6 = fo_dlntau * fo_dlntau / 6.0;
     s.fo_k_size = sp->k_size;
     s.fo_E = SONG2_FO_I + (fo_l_max + 1);
     s.fo_N = SONG2_FO_I + 2 * (fo_l_max + 1);
@@ -748,7 +755,15 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
     return 1;
   }
   c->launch = L;
-  int per_sm = song2_max_ctas_per_sm(precision, classes ? 4 : L.warp_team, c->block, c->smem);
+  c->kmode = L.warp_team;
+  if (!classes && L.warp_team == 0) {
+    /* the kernel whose registers allow two CTAs per SM when the shared-memory plan
+       does too (the compiler otherwise spends up to the 255 registers of one) */
+    int p0 = song2_max_ctas_per_sm(precision, 0, c->block, c->smem);
+    int p5 = song2_max_ctas_per_sm(precision, 5, c->block, c->smem);
+    if (p5 > p0) c->kmode = 5;
+  }
+  int per_sm = song2_max_ctas_per_sm(precision, classes ? 4 : c->kmode, c->block, c->smem);
   if (per_sm < 1) {
     snprintf(err, SONG2_ERRLEN, "launch configuration does not fit on an SM");
     return 1;
@@ -1160,7 +1175,7 @@ static int enqueue_part(song2_ctx *c, int part, cudaStream_t st, char *err) {
     int grid = c->groups.empty() ? c->grid : c->groups[g].grid;
     size_t smem = c->groups.empty() ? c->smem : c->groups[g].smem;
     int per_cta = c->groups.empty() ? c->launch.teams_per_cta : 1;
-    int mode = c->groups.empty() ? c->launch.warp_team : c->groups[g].mode;
+    int mode = c->groups.empty() ? c->kmode : c->groups[g].mode;
     grid = std::max(1, std::min(grid, (count + per_cta - 1) / per_cta));
     DevSpec sg = c->spec;
     sg.n_items = count;
@@ -1181,7 +1196,7 @@ static int enqueue_part(song2_ctx *c, int part, cudaStream_t st, char *err) {
 static int enqueue_run(song2_ctx *c, cudaStream_t st, char *err) {
   CK(cudaMemsetAsync(c->d_queue, 0, sizeof(int), st));
   if (c->groups.empty()) {
-    if (song2_launch_evolver(c->spec, c->ptrs, c->precision, c->launch.warp_team, c->grid, c->block, c->smem, st)) {
+    if (song2_launch_evolver(c->spec, c->ptrs, c->precision, c->kmode, c->grid, c->block, c->smem, st)) {
       snprintf(err, SONG2_ERRLEN, "evolver launch failed: %s", cudaGetErrorString(cudaGetLastError()));
       return 1;
     }

@@ -454,15 +454,17 @@ template <class Y, class C> __device__ inline double getc(const C &c, const Y &y
 
 /* ------------------------------------------------------------------ interpolation */
 
-__device__ inline double spl(const double *yv, const double *dd, int n, int ncol, double x0, double dx, int q,
-                             double x) {
-  double u = (x - x0) / dx;
+/* natural cubic spline on a uniform grid, column q at x; inv_dx = 1/dx and
+   dx2_6 = dx^2/6 come precomputed (no FP64 division) */
+__device__ inline double spl(const double *yv, const double *dd, int n, int ncol, double x0, double inv_dx, double dx2_6,
+                             int q, double x) {
+  double u = (x - x0) * inv_dx;
   int i = (int)floor(u);
   i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
   double b = u - i, a = 1.0 - b;
   const double *y0 = yv + (size_t)i * ncol, *d0 = dd + (size_t)i * ncol;
   return a * __ldg(y0 + q) + b * __ldg(y0 + ncol + q) +
-         ((a * a * a - a) * __ldg(d0 + q) + (b * b * b - b) * __ldg(d0 + ncol + q)) * (dx * dx) / 6.0;
+         ((a * a * a - a) * __ldg(d0 + q) + (b * b * b - b) * __ldg(d0 + ncol + q)) * dx2_6;
 }
 
 /* d/dx of the same spline */
@@ -478,7 +480,7 @@ __device__ inline double spl_dx(const double *yv, const double *dd, int n, int n
 }
 
 template <class C> __device__ inline double bg_col(const C &c, int q, double tau) {
-  return spl(c.p.bg, c.p.bg_dd, c.s.bg_size, SONG2_BG_SIZE, c.s.bg_lntau0, c.s.bg_dlntau, q, log(tau));
+  return spl(c.p.bg, c.p.bg_dd, c.s.bg_size, SONG2_BG_SIZE, c.s.bg_lntau0, c.s.bg_inv_dx, c.s.bg_dx2_6, q, log(tau));
 }
 
 /* Field q of BgV from the spline values v[] of the background columns at
@@ -842,7 +844,7 @@ template <class C> __device__ void prepare(const C &c, double tau, int with_sour
   c.sync();
   double x = c.sh->lntau;
   for (int q = tid; q < SONG2_BG_SIZE; q += nt)
-    c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, q, x);
+    c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_inv_dx, s.bg_dx2_6, q, x);
   int use_fo = with_sources && s.has_qs && !s.mode_first_order;
   for (int q = tid; q < 2 * s.nfo; q += nt) {
     int which = q >= s.nfo, qq = which ? q - s.nfo : q;
@@ -850,7 +852,8 @@ template <class C> __device__ void prepare(const C &c, double tau, int with_sour
     if (use_fo) {
       int ik = which ? t.i2 : t.i1;
       size_t stride = (size_t)s.fo_tau_size * s.nfo;
-      v = spl(c.p.fo + stride * ik, c.p.fo_dd + stride * ik, s.fo_tau_size, s.nfo, s.fo_lntau0, s.fo_dlntau, qq, x);
+      v = spl(c.p.fo + stride * ik, c.p.fo_dd + stride * ik, s.fo_tau_size, s.nfo, s.fo_lntau0, s.fo_inv_dx,
+              s.fo_dx2_6, qq, x);
     }
     (which ? c.fo2 : c.fo1)[qq] = v;
   }
@@ -885,16 +888,16 @@ template <class C> __device__ void prepare_table(const C &c, double tau, int ap)
   c.sync();
   double x = c.sh->lntau;
   for (int q = tid; q < SONG2_BG_SIZE; q += nt)
-    c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, q, x);
+    c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_inv_dx, s.bg_dx2_6, q, x);
   int use = s.has_qs && !s.mode_first_order && c.qtab.p != nullptr;
   if (use) {
-    double dx = s.fo_dlntau, u = (x - s.fo_lntau0) / dx;
+    double u = (x - s.fo_lntau0) * s.fo_inv_dx;
     int j0 = c.sh->qt_j0, n = c.sh->qt_n;
     int i = (int)floor(u);
     if (i < j0) i = j0;
     if (i > j0 + n - 2) i = j0 + n - 2;
     double b = u - i, a = 1.0 - b;
-    double ca = (a * a * a - a) * (dx * dx) / 6.0, cb = (b * b * b - b) * (dx * dx) / 6.0;
+    double ca = (a * a * a - a) * s.fo_dx2_6, cb = (b * b * b - b) * s.fo_dx2_6;
     int nq = s.qs2_size;
     auto r0 = c.qtab + (i - j0) * 2 * nq, r1 = r0 + 2 * nq;
     for (int q = tid; q < nq; q += nt) c.qs[q] = a * r0[q] + b * r1[q] + ca * r0[nq + q] + cb * r1[nq + q];
@@ -904,7 +907,8 @@ template <class C> __device__ void prepare_table(const C &c, double tau, int ap)
         int which = q >= s.nfo, qq = which ? q - s.nfo : q;
         int ik = which ? t.i2 : t.i1;
         (which ? c.fo2 : c.fo1)[qq] =
-            spl(c.p.fo + stride * ik, c.p.fo_dd + stride * ik, s.fo_tau_size, s.nfo, s.fo_lntau0, s.fo_dlntau, qq, x);
+            spl(c.p.fo + stride * ik, c.p.fo_dd + stride * ik, s.fo_tau_size, s.nfo, s.fo_lntau0, s.fo_inv_dx,
+              s.fo_dx2_6, qq, x);
       }
     }
   } else {
@@ -935,7 +939,7 @@ template <class C> __device__ void build_qs_table(const C &c) {
   int tid = c.rank, nt = c.size;
   if (!s.has_qs || s.mode_first_order || c.qtab.p == nullptr) return;
   int N = s.fo_tau_size, nq = s.qs2_size;
-  double x0 = s.fo_lntau0, dx = s.fo_dlntau;
+  double x0 = s.fo_lntau0, dx = s.fo_dlntau, six_idx2 = 6.0 * s.fo_inv_dx * s.fo_inv_dx;
   if (tid == 0) {
     int j0 = (int)floor((log(t.tau_ini) - x0) / dx);
     int j1 = (int)ceil((log(t.tau_end) - x0) / dx);
@@ -953,7 +957,7 @@ template <class C> __device__ void build_qs_table(const C &c) {
   for (int j = 0; j < M; ++j) {
     double x = x0 + (j0 + j) * dx;
     for (int q = tid; q < SONG2_BG_SIZE; q += nt)
-      c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_dlntau, q, x);
+      c.bgraw[q] = spl(c.p.bg, c.p.bg_dd, s.bg_size, SONG2_BG_SIZE, s.bg_lntau0, s.bg_inv_dx, s.bg_dx2_6, q, x);
     for (int q = tid; q < 2 * s.nfo; q += nt) {
       int which = q >= s.nfo, qq = which ? q - s.nfo : q;
       (which ? c.fo2 : c.fo1)[qq] = __ldg((which ? v2 : v1) + (size_t)(j0 + j) * s.nfo + qq);
@@ -981,9 +985,9 @@ template <class C> __device__ void build_qs_table(const C &c) {
     for (int j = 1; j < M - 1; ++j) {
       double ym = c.qtab[(j - 1) * 2 * nq + q], y0 = c.qtab[j * 2 * nq + q];
       double yp = c.qtab[(j + 1) * 2 * nq + q];
-      double r = 6.0 * (yp - 2.0 * y0 + ym) / (dx * dx);
-      double bb = 4.0 - __ldg(c.p.spl_c + j - 1);
-      prev = (r - prev) / bb;
+      double r = (yp - 2.0 * y0 + ym) * six_idx2;
+      /* 1 / (4 - spl_c[j-1]) = spl_c[j] */
+      prev = (r - prev) * __ldg(c.p.spl_c + j);
       c.qtab[j * 2 * nq + nq + q] = prev;
     }
     c.qtab[(M - 1) * 2 * nq + nq + q] = 0.0;
@@ -1876,6 +1880,50 @@ template <class C> __device__ double block_max_bits(const C &c, unsigned long lo
   return __longlong_as_double((long long)v);
 }
 
+/* N maxima of non-negative doubles over the team at once, through the same two
+   barriers (the bit-pattern reduction of block_max_bits) */
+template <int N, class C> __device__ void block_max_bits_n(const C &c, unsigned long long (&v)[N], double (&out)[N]) {
+  if constexpr (C::STR) {
+    for (int off = c.size >> 1; off > 0; off >>= 1)
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        unsigned long long o = __shfl_xor_sync(c.tmask, v[q], off);
+        v[q] = o > v[q] ? o : v[q];
+      }
+  } else {
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        unsigned long long o = __shfl_xor_sync(0xffffffffu, v[q], off);
+        v[q] = o > v[q] ? o : v[q];
+      }
+    if (c.size > 32) {
+      static_assert(N * 8 <= 32, "reduction slots");
+      int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      unsigned long long *red = (unsigned long long *)c.sh->red;
+      __syncthreads();
+      if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < N; ++q) red[q * 8 + warp] = v[q];
+      __syncthreads();
+      int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        v[q] = 0;
+        for (int i = 0; i < nw; ++i) {
+          unsigned long long o = red[q * 8 + i];
+          v[q] = o > v[q] ? o : v[q];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    if (v[q] > 0x7ff0000000000000ull) v[q] = 0x7ff0000000000000ull;
+    out[q] = __longlong_as_double((long long)v[q]);
+  }
+}
+
 /* running max of |x| in the bit domain (the sign bit is cleared, NaN stays above inf) */
 __device__ inline void bmax(unsigned long long &acc, double x) {
   unsigned long long b = dbits(x) & 0x7fffffffffffffffull;
@@ -2489,7 +2537,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
       havrate = 0;
     }
     int nofailed = 1;
-    double err = 0, tnew = t;
+    double err = 0, tnew = t, errnrm = 0, ymax = 0;
     for (;;) {
       int gotynew = 0;
       while (!gotynew) {
@@ -2525,15 +2573,24 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
           st.n_rhs++;
           lu_solve<T>(c);
           PH_MARK(c, PH_SOLVE);
-          unsigned long long vn = 0;
+          /* the Newton norm, and with it the norms of the local error estimate and
+             of the new state, should this iteration be the last */
+          unsigned long long vv[3] = {0, 0, 0};
           auto xs = c.template xsol<T>();
           for (int i = tid; i < n; i += nt) {
-            double d = (double)xs[i];
-            bmax(vn, d * invwt[i]);
-            difkp1[i] += d;
-            ynew[i] += d;
+            double d = (double)xs[i], w = invwt[i];
+            double dk = difkp1[i] + d, yn = ynew[i] + d;
+            bmax(vv[0], d * w);
+            bmax(vv[1], dk * w);
+            bmax(vv[2], yn);
+            difkp1[i] = dk;
+            ynew[i] = yn;
           }
-          double newnrm = block_max_bits(c, vn);
+          double nrm[3];
+          block_max_bits_n<3>(c, vv, nrm);
+          double newnrm = nrm[0];
+          errnrm = nrm[1];
+          ymax = nrm[2];
           PH_MARK(c, PH_NUPD);
           if (!(newnrm < INFINITY)) break;
           if (newnrm <= minnrm) { gotynew = 1; break; }
@@ -2582,13 +2639,7 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
           havrate = 0;
         }
       }
-      unsigned long long ve = 0, vfin = 0;
-      for (int i = tid; i < n; i += nt) {
-        bmax(ve, difkp1[i] * invwt[i]);
-        bmax(vfin, ynew[i]);
-      }
-      err = block_max_bits(c, ve) * erconst[k - 1];
-      double ymax = block_max_bits(c, vfin);
+      err = errnrm * erconst[k - 1];
       if (!(ymax < 1e300)) return SONG2_E_NAN;
       if (err > rtol) {
         st.n_rejected++;
@@ -2675,7 +2726,10 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
         if (k > 1) bmax(vk, dif[(size_t)(k - 1) * n + i] * invwt[i]);
         if (k < maxk) bmax(vp, dif[(size_t)(k + 1) * n + i] * invwt[i]);
       }
-      double errkm1 = block_max_bits(c, vk), errkp1 = block_max_bits(c, vp);
+      unsigned long long vkp[2] = {vk, vp};
+      double ekp[2];
+      block_max_bits_n<2>(c, vkp, ekp);
+      double errkm1 = ekp[0], errkp1 = ekp[1];
       /* the three candidate step sizes, side by side */
       for (int q = tid; q < 3; q += nt) {
         double temp, hq = 0.0;
@@ -2703,10 +2757,20 @@ __device__ __forceinline__ int ndf15(const C &c, double t0, double t1, int &jout
       }
     }
     t = tnew;
-    for (int i = tid; i < n; i += nt) y[i] = ynew[i];
+    /* the new state becomes the current one: the two buffers trade places */
+    {
+      auto tmp = y;
+      y = ynew;
+      ynew = tmp;
+    }
     c.sync();
     PH_MARK(c, PH_CTRL);
     Jcurrent = 0;
+  }
+  /* the next interval and the caller find the state in c.y */
+  if (y.p != c.y.p) {
+    for (int i = tid; i < n; i += nt) c.y[i] = y[i];
+    c.sync();
   }
   return SONG2_OK;
 }

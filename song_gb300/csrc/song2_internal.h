@@ -65,9 +65,9 @@ struct DevSpec {
   int idx_phi, idx_phip, idx_omega, idx_gamma, idx_gammap, idx_b000, idx_c000, idx_b11[2], idx_c11[2];
   /* first-order table */
   int fo_l_max, nfo, fo_E, fo_N, fo_CG, fo_tau_size, fo_k_size;
-  double fo_lntau0, fo_dlntau;
+  double fo_lntau0, fo_dlntau, fo_inv_dx, fo_dx2_6;    /* 1/dlntau, dlntau^2/6 (spline evaluation) */
   int bg_size;
-  double bg_lntau0, bg_dlntau;
+  double bg_lntau0, bg_dlntau, bg_inv_dx, bg_dx2_6;
   /* sources */
   int tp2_size;
   int tp_kind[S2_MAXTP], tp_l[S2_MAXTP], tp_m[S2_MAXTP];
@@ -193,7 +193,8 @@ inline int dt_table_size(const DevSpec &s) { return 3 * (s.dt_L + 1) * SONG2_MAX
    triplet, arrays in global slabs (tslab, txsol, jac, lu_global, qtab);
    3: one CTA per triplet with hierarchy classes (ptrs.class_spec set; the dynamic
    shared memory starts with song2_class_spec_bytes() for the class spec copy);
-   4: the same with registers for two CTAs per SM.
+   4: the same with registers for two CTAs per SM; 5: mode 0 with registers for two
+   CTAs per SM.
    Mode 0 with ptrs.class_spec set launches mode 3. */
 int song2_launch_evolver(const DevSpec &spec, const DevPtrs &ptrs, int precision, int mode, int grid, int block,
                          size_t smem, cudaStream_t stream);

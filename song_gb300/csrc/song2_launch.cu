@@ -13,6 +13,8 @@ void *song2_kernel_class_f();
 void *song2_kernel_class_d();
 void *song2_kernel_class2_f();
 void *song2_kernel_class2_d();
+void *song2_kernel_block2_f();
+void *song2_kernel_block2_d();
 void *song2_kernel_team_f();
 void *song2_kernel_team_d();
 
@@ -31,7 +33,8 @@ int song2_team_slab_doubles(const DevSpec &spec) { return make_team_plan(spec).t
 
 namespace {
 /* mode 0: CTA per triplet; 1: warp per triplet; 2: lane teams; 3: CTA per triplet
-   with hierarchy classes; 4: the same with registers for two CTAs per SM */
+   with hierarchy classes; 4: the same with registers for two CTAs per SM; 5: CTA
+   per triplet (one hierarchy) with registers for two CTAs per SM */
 void *pick_kernel(int precision, int mode) {
   int f = precision == SONG2_PREC_MIXED;
   switch (mode) {
@@ -39,6 +42,7 @@ void *pick_kernel(int precision, int mode) {
   case 2: return f ? song2_kernel_team_f() : song2_kernel_team_d();
   case 3: return f ? song2_kernel_class_f() : song2_kernel_class_d();
   case 4: return f ? song2_kernel_class2_f() : song2_kernel_class2_d();
+  case 5: return f ? song2_kernel_block2_f() : song2_kernel_block2_d();
   default: return f ? song2_kernel_block_f() : song2_kernel_block_d();
   }
 }
