@@ -79,6 +79,8 @@ def parse():
                     help="triplets checked against the FP64 oracle at rtol 1e-8 (0: skip)")
     ap.add_argument("--plain-parts", type=int, default=0, help="parts timed in plain FP64 (default: steps/4)")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--autotune-sample", type=int, default=256,
+                    help="triplets the autotuner times its launch candidates on (0: default launch)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--k-size", type=int, default=None, help="override the k grid size (small profiling cases)")
     ap.add_argument("--k3-size", type=int, default=None, help="override the k3 grid size (small profiling cases)")
@@ -339,13 +341,25 @@ def cpu_sample(p, m, threads, offset=0):
 
 # ---------------------------------------------------------------- GPU side
 
-def ctx_create(lib, p, precision):
+def ctx_create(lib, p, precision, launch=None):
     from song_gb300 import capi
     c = C.c_void_p()
     err = capi.errbuf()
-    if lib.song2_ctx_create(C.byref(p.spec), C.byref(p.tables), precision, C.byref(c), err):
+    if lib.song2_ctx_create_ex(C.byref(p.spec), C.byref(p.tables), precision,
+                               C.byref(launch) if launch is not None else None, 0, 1, C.byref(c), err):
         raise RuntimeError(err.value.decode())
     return c
+
+
+def autotune(lib, p, precision, sample):
+    """song2_autotune's pick for this workload (untimed set-up)."""
+    from song_gb300 import capi
+    best = capi.Launch()
+    ms = C.c_double()
+    err = capi.errbuf()
+    if lib.song2_autotune(C.byref(p.spec), C.byref(p.tables), precision, sample, C.byref(best), C.byref(ms), err):
+        raise RuntimeError(err.value.decode())
+    return best, ms.value
 
 
 def run_parts(lib, c, parts, n_parts, torch, flush):
@@ -504,7 +518,13 @@ def main():
         acc = (proc, items, out, time.perf_counter())
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    c = ctx_create(lib, p, capi.SONG2_PREC_MIXED)
+    launch = None
+    if args.autotune_sample > 0:
+        launch, tune_ms = autotune(lib, p, capi.SONG2_PREC_MIXED, args.autotune_sample)
+        config["launch"] = {"warp_team": launch.warp_team, "teams_per_cta": launch.teams_per_cta,
+                            "threads_per_team": launch.threads_per_team, "factors_in_smem": launch.lu_in_smem,
+                            "autotune": f"song2_autotune on {args.autotune_sample} triplets ({tune_ms:.0f} ms)"}
+    c = ctx_create(lib, p, capi.SONG2_PREC_MIXED, launch)
     try:
         run_parts(lib, c, [w % n_parts for w in range(args.warmup)], n_parts, torch, None)
         if world > 1:

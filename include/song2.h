@@ -341,8 +341,10 @@ int song2_ctx_create_ex(const song2_spec *spec, const song2_tables *tab, int pre
                         const song2_launch *launch, int shard, int n_shards, song2_ctx **out, char *err);
 /* The launch configuration a context uses. */
 void song2_ctx_get_launch(song2_ctx *ctx, song2_launch *out, int *grid, int *block, size_t *smem);
-/* Autotuner: times every candidate configuration on a sample of the most
-   expensive triplets (largest max(k1,k2,k3)) and returns the fastest. */
+/* Autotuner: times every candidate launch configuration (CTA teams of 128, 192
+   or 256 threads, warp teams, lane teams; CTA teams only for uneven batches) on
+   `sample` triplets spread over the cost-sorted work list and returns the
+   fastest, with its time on the sample. */
 int song2_autotune(const song2_spec *spec, const song2_tables *tab, int precision, int sample,
                    song2_launch *best, double *best_ms, char *err);
 /* Same, restricted to the given triplets (indices in the reference work order:

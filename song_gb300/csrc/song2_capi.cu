@@ -1121,12 +1121,17 @@ int song2_autotune(const song2_spec *spec, const song2_tables *tab, int precisio
   std::vector<WorkItem> pick;
   size_t stride = std::max<size_t>(1, sorted.size() / (size_t)sample);
   for (size_t i = 0; i < sorted.size() && (int)pick.size() < sample; i += stride) pick.push_back(sorted[i]);
-  const song2_launch cands[] = {
-      {1, 4, 32, 0}, {1, 8, 32, 0}, {0, 1, 128, 0}, {0, 1, 128, 1}, {0, 1, 256, 1}, {0, 1, 256, 0}, {2, 16, 8, 0},
+  /* candidates: CTA teams of 128, 192 or 256 threads with the factors in shared
+     or global memory, warp teams, lane teams; uneven batches (hierarchy classes)
+     run CTA teams only */
+  const song2_launch all[] = {
+      {0, 1, 256, 1}, {0, 1, 192, 1}, {0, 1, 128, 1}, {0, 1, 256, 0}, {1, 4, 32, 0}, {1, 8, 32, 0}, {2, 16, 8, 0},
   };
+  int ncand = spec->n_classes > 0 ? 3 : (int)(sizeof(all) / sizeof(all[0]));
   double bestv = 1e300;
   int found = 0;
-  for (const song2_launch &cand : cands) {
+  for (int ci = 0; ci < ncand; ++ci) {
+    const song2_launch &cand = all[ci];
     song2_ctx *c = new song2_ctx();
     memset((void *)&c->spec, 0, sizeof(c->spec));
     c->launch = cand;

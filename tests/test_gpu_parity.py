@@ -122,6 +122,30 @@ def test_launch_configurations_agree(lib, tiny, launch):
         assert np.array_equal(again, base)
 
 
+def test_autotune_picks_a_layout_that_runs(lib, tiny):
+    """song2_autotune times its candidate launch configurations on a sample of the
+    problem and returns the fastest; a context created with it evolves the triplets
+    as the default does."""
+    p, ref, _ = tiny
+    for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
+        best = capi.Launch()
+        ms = C.c_double()
+        err = capi.errbuf()
+        assert lib.song2_autotune(C.byref(p.spec), C.byref(p.tables), precision, 8, C.byref(best), C.byref(ms),
+                                  err) == 0, err.value
+        assert best.warp_team in (0, 1, 2) and ms.value > 0
+        c = C.c_void_p()
+        assert lib.song2_ctx_create_ex(C.byref(p.spec), C.byref(p.tables), precision, C.byref(best), 0, 1,
+                                       C.byref(c), err) == 0, err.value
+        assert lib.song2_ctx_run(c, None, err) == 0, err.value
+        src = np.zeros_like(ref)
+        st = (capi.TripletStats * p.n_triplets)()
+        lib.song2_ctx_download(c, capi.dptr(src), st, err)
+        lib.song2_ctx_destroy(c)
+        assert np.all(np.frombuffer(st, dtype=capi.STATS_DTYPE)["status"] == capi.SONG2_OK)
+        assert np.max(floored_errors(src, ref, p)) < 10 * p.spec.rtol
+
+
 def test_give_up_path_returns_status(lib, tiny):
     """A triplet that breaches its step limit retires with SONG2_E_MAXSTEPS; the
     kernel neither traps nor hangs."""
