@@ -8,9 +8,12 @@ m_max the cheapest triplet of the smallest, a middle and the largest l_max class
 so that the largest hierarchies (744 equations, five azimuthal blocks) and every
 hierarchy shape are covered.  Both precisions are run through a triplet-list
 context (song2_ctx_create_list) and compared with the oracle at the same rtol
-(bound 10 rtol, as the other parity tests), and an rtol = 1e-5 GPU run is
-compared with the oracle at rtol = 1e-8 (every source within 1e-4 of its maximum
-over time)."""
+(bound 10 rtol, as the other parity tests), and an rtol = 1e-6 GPU run is
+compared with the oracle at rtol = 1e-8: every source within 1e-4 of its maximum
+over time.  (At rtol 1e-5 the E polarisation sources of the most squeezed
+triplets, k2 = 1e-5 /Mpc, still carry up to 5e-4 of global integration error in
+both precisions; rtol 1e-6 is the tolerance at which every sampled source meets
+1e-4.)"""
 import ctypes as C
 import os
 
@@ -108,13 +111,13 @@ def test_uneven_classes_match_oracle(lib, uneven):
 
 
 def test_uneven_classes_against_tight_oracle(lib, uneven):
-    """rtol = 1e-5 on the GPU against the oracle at rtol = 1e-8: every source of
+    """rtol = 1e-6 on the GPU against the oracle at rtol = 1e-8: every source of
     every sampled class within 1e-4 of its maximum over time."""
     p, items, _ = uneven
     tight, st_t = oracle.evolve(p, nthreads=THREADS, items=items, rtol=1e-8)
     assert np.all(st_t["status"][items] == capi.SONG2_OK)
     for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
-        src, st = gpu_list(lib, p, items, precision, rtol=1e-5)
+        src, st = gpu_list(lib, p, items, precision, rtol=1e-6)
         assert np.all(st["status"][items] == capi.SONG2_OK)
         e = errors_on(p, src, tight, items)
         assert np.max(e) < 1e-4, (precision, np.max(e))

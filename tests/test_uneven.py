@@ -101,14 +101,18 @@ def test_gpu_uneven_matches_oracle(lib, uneven, precision):
 @pytest.mark.gpu
 def test_gpu_uneven_launch_groups_match_single_launch(lib, uneven, monkeypatch):
     """Splitting an uneven batch into launch groups by class size (large plans
-    first) computes the same sources as one launch."""
-    from helpers import gpu_run
-    p, _, _ = uneven
+    first) computes the same sources as one launch, within the solver tolerance:
+    the two groups run different instantiations of the kernel (register budgets
+    for one and for two CTAs per SM), compiled separately, whose floating-point
+    contractions may differ in the last bits."""
+    from helpers import floored_errors, gpu_run
+    p, ref, _ = uneven
     one, _, _ = gpu_run(lib, p, 1)
     monkeypatch.setenv("SONG2_CLASS_SPLIT_BYTES", "20000")
     two, st, _ = gpu_run(lib, p, 1)
     assert np.all(st["status"] == 0)
-    assert np.array_equal(one, two)
+    assert np.max(floored_errors(two, one, p)) < 10 * p.spec.rtol
+    assert np.max(floored_errors(two, ref, p)) < 10 * p.spec.rtol
 
 
 @pytest.mark.gpu
