@@ -1439,9 +1439,8 @@ template <typename T, class C, class A> __device__ void newton_rhs(const C &c, i
        x_0 = h_0 - R x_core,   x_k = h_k - P_k x_(k-1).
    Work and storage are O(n) per block (against O(n kl (kl + ku)) for a banded
    LU whose band must span the core), so the factors of every hierarchy class
-   fit in shared memory.  The factorisation stays out of line: inlined into the
-   NDF loop it raises the kernel to 255 registers (one CTA per SM); the solve
-   sweeps are inlined (a call saves and restores the caller's registers). */
+   fit in shared memory.  Each sweep is a linear recurrence, i.e. a composition
+   of affine maps, so a warp evaluates it as a scan (chain_back, chain_fwd). */
 
 template <typename T> __device__ inline T tabs(T x) { return x < T(0) ? -x : x; }
 
@@ -1528,7 +1527,7 @@ template <typename T, int D> __device__ inline bool mx_inv(const T *a, T *r) {
 /* one chain of block b, by one lane: Q_k, Theta_k^-1, P_k from the last node up,
    then R = Theta_0^-1 E and the scaled F.  False on a zero pivot. */
 template <typename T, int D, class C, class VJ, class VF>
-__device__ __noinline__ bool chain_factor(const C &c, int b, int ch, T hg, const VJ &J, const VF &F) {
+__device__ __forceinline__ bool chain_factor(const C &c, int b, int ch, T hg, const VJ &J, const VF &F) {
   const DevSpec &s = c.s;
   constexpr int D2 = D * D;
   int len = s.ch_len[b][ch], cn = s.core_n[b], base = s.ch_off[b][ch];
@@ -1585,7 +1584,7 @@ __device__ __noinline__ bool chain_factor(const C &c, int b, int ch, T hg, const
    complement and its inverse, in place, by Gauss-Jordan elimination with partial
    pivoting (lane j updates columns j, j + W, ...).  False on a zero pivot. */
 template <typename T, class C, class VJ, class VF>
-__device__ __noinline__ bool core_factor(const C &c, int b, T hg, const VJ &J, const VF &F, int lane, int W, unsigned mask) {
+__device__ __forceinline__ bool core_factor(const C &c, int b, T hg, const VJ &J, const VF &F, int lane, int W, unsigned mask) {
   const DevSpec &s = c.s;
   int cn = s.core_n[b], co = s.core_off[b];
   if (cn == 0) return true;
@@ -1679,8 +1678,10 @@ template <class C, class F1, class F2> __device__ void for_chains(const C &c, F1
 
 /* M = I - hinvGak J factorised from the stored Jacobian: every chain on its own
    lane, then the core of every block.  Ends with a barrier; sets sh->lu_fail on a
-   zero pivot. */
-template <typename T, class C> __device__ void form_and_factor(const C &c, double hinvGak) {
+   zero pivot.  One out-of-line call per factorisation: inlined into the NDF loop
+   the chain and core eliminations raise its register spills, and as separate
+   calls each would save and restore the caller's registers. */
+template <typename T, class C> __device__ __noinline__ void form_and_factor(const C &c, double hinvGak) {
   const DevSpec &s = c.s;
   auto J = c.template jacv<T>();
   auto F = c.template lu<T>();
@@ -1695,104 +1696,179 @@ template <typename T, class C> __device__ void form_and_factor(const C &c, doubl
   c.sync();
 }
 
-/* backward sweep of one chain: h_k = Theta_k^-1 g_k into the node entries of x.
-   The next node's right-hand side, state indices and factors are loaded before the
-   current node is stored, so the loop carries only the FMA chain of g. */
+/* An affine map z -> A z + B of d-vectors (d = 1 or 2): the sweeps of a chain are
+   compositions of such maps, evaluated as a scan across the lanes of a group. */
+template <typename T, int D> struct Aff {
+  T A[D * D], B[D];
+};
+template <typename T, int D> __device__ inline Aff<T, D> aff_id() {
+  Aff<T, D> m;
+#pragma unroll
+  for (int e = 0; e < D * D; ++e) m.A[e] = (e % (D + 1) == 0) ? T(1) : T(0);
+#pragma unroll
+  for (int a = 0; a < D; ++a) m.B[a] = T(0);
+  return m;
+}
+/* f o g: z -> fA (gA z + gB) + fB */
+template <typename T, int D> __device__ inline Aff<T, D> aff_after(const Aff<T, D> &f, const Aff<T, D> &g) {
+  Aff<T, D> r;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    T b = f.B[i];
+#pragma unroll
+    for (int k = 0; k < D; ++k) b += f.A[i * D + k] * g.B[k];
+    r.B[i] = b;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T a = T(0);
+#pragma unroll
+      for (int k = 0; k < D; ++k) a += f.A[i * D + k] * g.A[k * D + j];
+      r.A[i * D + j] = a;
+    }
+  }
+  return r;
+}
+template <typename T, int D> __device__ inline Aff<T, D> aff_shfl(const Aff<T, D> &m, int delta, bool down, int W,
+                                                                   unsigned mask) {
+  Aff<T, D> r;
+#pragma unroll
+  for (int e = 0; e < D * D; ++e) r.A[e] = down ? __shfl_down_sync(mask, m.A[e], delta, W) : __shfl_up_sync(mask, m.A[e], delta, W);
+#pragma unroll
+  for (int a = 0; a < D; ++a) r.B[a] = down ? __shfl_down_sync(mask, m.B[a], delta, W) : __shfl_up_sync(mask, m.B[a], delta, W);
+  return r;
+}
+
+/* Backward sweep of one chain by a group of W lanes (W a power of two): g_last =
+   b_last, g_k = b_k - Q_k g_(k+1), and h_k = Theta_k^-1 g_k into the node entries of
+   x.  g_k is the composition f_k o f_(k+1) o ... o f_last of the maps
+   f_k(z) = b_k - Q_k z (Q_last = 0), so each lane composes its own run of
+   P = ceil(len / W) nodes, a suffix scan across the lanes (log2 W shuffle steps)
+   gives every lane the value entering its run, and the lane replays its nodes. */
 template <typename T, int D, class C, class VF, class X>
-__device__ __forceinline__ void chain_back(const C &c, int b, int ch, const VF &F, const X &x) {
+__device__ void chain_back(const C &c, int b, int ch, const VF &F, const X &x, int lane, int W, unsigned mask) {
   const DevSpec &s = c.s;
   constexpr int D2 = D * D;
   int len = s.ch_len[b][ch], base = s.ch_off[b][ch];
   const short *ix = c.mx_s + s.ch_idx[b][ch];
-  T g[D], bn[D], qn[D2], tn[D2];
-  int in[D];
-  int k = len - 1;
+  int P = (len + W - 1) / W, k0 = lane * P, k1 = min(len, k0 + P);
+  Aff<T, D> m = aff_id<T, D>();
+  for (int k = k1 - 1; k >= k0; --k) {
+    Aff<T, D> f;
 #pragma unroll
-  for (int a = 0; a < D; ++a) { in[a] = ix[k * D + a]; bn[a] = x[in[a]]; }
+    for (int e = 0; e < D2; ++e) f.A[e] = -(T)F[base + 3 * D2 * k + e];
 #pragma unroll
-  for (int e = 0; e < D2; ++e) { qn[e] = F[base + 3 * D2 * k + e]; tn[e] = F[base + 3 * D2 * k + D2 + e]; }
-  for (; k >= 0; --k) {
-    T bk[D], q[D2], t[D2];
-    int ik[D];
+    for (int a = 0; a < D; ++a) f.B[a] = x[ix[k * D + a]];
+    m = aff_after(f, m);
+  }
+  for (int off = 1; off < W; off <<= 1) {
+    Aff<T, D> o = aff_shfl(m, off, true, W, mask);
+    if (lane + off < W) m = aff_after(m, o);
+  }
+  T z[D];
 #pragma unroll
-    for (int a = 0; a < D; ++a) { bk[a] = bn[a]; ik[a] = in[a]; }
+  for (int a = 0; a < D; ++a) {
+    z[a] = __shfl_down_sync(mask, m.B[a], 1, W);
+    if (k1 >= len) z[a] = T(0);
+  }
+  for (int k = k1 - 1; k >= k0; --k) {
+    int o = base + 3 * D2 * k;
+    T g[D];
 #pragma unroll
-    for (int e = 0; e < D2; ++e) { q[e] = qn[e]; t[e] = tn[e]; }
-    if (k > 0) {
-      int o = base + 3 * D2 * (k - 1);
+    for (int a = 0; a < D; ++a) {
+      T v = x[ix[k * D + a]];
 #pragma unroll
-      for (int a = 0; a < D; ++a) { in[a] = ix[(k - 1) * D + a]; bn[a] = x[in[a]]; }
-#pragma unroll
-      for (int e = 0; e < D2; ++e) { qn[e] = F[o + e]; tn[e] = F[o + D2 + e]; }
+      for (int r = 0; r < D; ++r) v -= F[o + a * D + r] * z[r];
+      g[a] = v;
     }
-    if (k < len - 1)
-#pragma unroll
-      for (int a = 0; a < D; ++a)
-#pragma unroll
-        for (int r = 0; r < D; ++r) bk[a] -= q[a * D + r] * g[r];
-#pragma unroll
-    for (int a = 0; a < D; ++a) g[a] = bk[a];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       T h = T(0);
 #pragma unroll
-      for (int r = 0; r < D; ++r) h += t[a * D + r] * g[r];
-      x[ik[a]] = h;
+      for (int r = 0; r < D; ++r) h += F[o + D2 + a * D + r] * g[r];
+      x[ix[k * D + a]] = h;
+      z[a] = g[a];
     }
   }
 }
 
-/* forward sweep of one chain: x_0 = h_0 - R x_core, x_k = h_k - P_k x_(k-1), with
-   the next node's h, indices and P loaded ahead */
+/* Forward sweep of one chain by a group of W lanes: x_0 = h_0 - R x_core,
+   x_k = h_k - P_k x_(k-1), a prefix scan of the maps z -> h_k - P_k z (node 0's map
+   is the constant x_0), as in chain_back. */
 template <typename T, int D, class C, class VF, class X>
-__device__ __forceinline__ void chain_fwd(const C &c, int b, int ch, const VF &F, const X &x) {
+__device__ void chain_fwd(const C &c, int b, int ch, const VF &F, const X &x, int lane, int W, unsigned mask) {
   const DevSpec &s = c.s;
   constexpr int D2 = D * D;
   int len = s.ch_len[b][ch], base = s.ch_off[b][ch], cn = s.core_n[b];
   const short *ix = c.mx_s + s.ch_idx[b][ch], *cx = c.mx_s + s.core_idx[b];
   int oe = base + 3 * D2 * len;
-  T prev[D];
+  int P = (len + W - 1) / W, k0 = lane * P, k1 = min(len, k0 + P);
+  T x0[D];
+  if (k0 == 0 && k1 > 0)
 #pragma unroll
-  for (int a = 0; a < D; ++a) {
-    T v = x[ix[a]];
-    for (int j = 0; j < cn; ++j) v -= F[oe + a * cn + j] * (T)x[cx[j]];
-    prev[a] = v;
+    for (int a = 0; a < D; ++a) {
+      T v = x[ix[a]];
+      for (int j = 0; j < cn; ++j) v -= F[oe + a * cn + j] * (T)x[cx[j]];
+      x0[a] = v;
+    }
+  Aff<T, D> m = aff_id<T, D>();
+  for (int k = k0; k < k1; ++k) {
+    Aff<T, D> f;
+    if (k == 0) {
+#pragma unroll
+      for (int e = 0; e < D2; ++e) f.A[e] = T(0);
+#pragma unroll
+      for (int a = 0; a < D; ++a) f.B[a] = x0[a];
+    } else {
+#pragma unroll
+      for (int e = 0; e < D2; ++e) f.A[e] = -(T)F[base + 3 * D2 * k + 2 * D2 + e];
+#pragma unroll
+      for (int a = 0; a < D; ++a) f.B[a] = x[ix[k * D + a]];
+    }
+    m = aff_after(f, m);
   }
+  for (int off = 1; off < W; off <<= 1) {
+    Aff<T, D> o = aff_shfl(m, off, false, W, mask);
+    if (lane >= off) m = aff_after(m, o);
+  }
+  T z[D];
 #pragma unroll
-  for (int a = 0; a < D; ++a) x[ix[a]] = prev[a];
-  if (len < 2) return;
-  T hn[D], pn[D2];
-  int in[D];
-#pragma unroll
-  for (int a = 0; a < D; ++a) { in[a] = ix[D + a]; hn[a] = x[in[a]]; }
-#pragma unroll
-  for (int e = 0; e < D2; ++e) pn[e] = F[base + 3 * D2 + 2 * D2 + e];
-  for (int k = 1; k < len; ++k) {
-    T h[D], pk[D2];
-    int ik[D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) { h[a] = hn[a]; ik[a] = in[a]; }
-#pragma unroll
-    for (int e = 0; e < D2; ++e) pk[e] = pn[e];
-    if (k + 1 < len) {
-      int o = base + 3 * D2 * (k + 1) + 2 * D2;
-#pragma unroll
-      for (int a = 0; a < D; ++a) { in[a] = ix[(k + 1) * D + a]; hn[a] = x[in[a]]; }
-#pragma unroll
-      for (int e = 0; e < D2; ++e) pn[e] = F[o + e];
-    }
+  for (int a = 0; a < D; ++a) z[a] = __shfl_up_sync(mask, m.B[a], 1, W);
+  for (int k = k0; k < k1; ++k) {
     T v[D];
+    if (k == 0) {
 #pragma unroll
-    for (int a = 0; a < D; ++a) {
-      v[a] = h[a];
+      for (int a = 0; a < D; ++a) v[a] = x0[a];
+    } else {
+      int o = base + 3 * D2 * k + 2 * D2;
 #pragma unroll
-      for (int r = 0; r < D; ++r) v[a] -= pk[a * D + r] * prev[r];
+      for (int a = 0; a < D; ++a) {
+        v[a] = x[ix[k * D + a]];
+#pragma unroll
+        for (int r = 0; r < D; ++r) v[a] -= F[o + a * D + r] * z[r];
+      }
     }
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      x[ik[a]] = v[a];
-      prev[a] = v[a];
+      x[ix[k * D + a]] = v[a];
+      z[a] = v[a];
     }
+  }
+}
+
+/* f(b, ch, lane, W, mask) for every chain, each chain by a whole group of lanes:
+   in a CTA team the warps take the chains in turn, otherwise the team takes them
+   one after the other */
+template <class C, class F> __device__ void per_chain_group(const C &c, F f) {
+  const DevSpec &s = c.s;
+  int nc = s.n_ch1 + s.n_ch2;
+  auto pick = [&](int t) { return t < s.n_ch1 ? s.ch1[t] : s.ch2[t - s.n_ch1]; };
+  if constexpr (C::STR) {
+    for (int t = 0; t < nc; ++t) f(pick(t) >> 4, pick(t) & 15, c.rank, c.size, c.tmask);
+  } else if (c.size == 32) {
+    for (int t = 0; t < nc; ++t) f(pick(t) >> 4, pick(t) & 15, c.rank, 32, 0xffffffffu);
+  } else {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int t = warp; t < nc; t += nw) f(pick(t) >> 4, pick(t) & 15, lane, 32, 0xffffffffu);
   }
 }
 
@@ -1832,15 +1908,20 @@ template <typename T, class C> __device__ void core_solve(const C &c, int b, int
    backward sweeps of every chain, the cores, the forward sweeps, separated by
    barriers.  Ends with a barrier. */
 template <typename T, class C> __device__ void lu_solve(const C &c) {
+  const DevSpec &s = c.s;
   auto F = c.template lu<T>();
   auto x = c.template xsol<T>();
-  for_chains(c, [&](int b, int ch) { chain_back<T, 1>(c, b, ch, F, x); },
-             [&](int b, int ch) { chain_back<T, 2>(c, b, ch, F, x); });
+  per_chain_group(c, [&](int b, int ch, int lane, int W, unsigned mask) {
+    if (s.ch_d[b][ch] == 1) chain_back<T, 1>(c, b, ch, F, x, lane, W, mask);
+    else chain_back<T, 2>(c, b, ch, F, x, lane, W, mask);
+  });
   c.sync();
   per_block_group(c, [&](int b, int lane, int W, unsigned mask) { core_solve<T>(c, b, lane, W, mask); });
   c.sync();
-  for_chains(c, [&](int b, int ch) { chain_fwd<T, 1>(c, b, ch, F, x); },
-             [&](int b, int ch) { chain_fwd<T, 2>(c, b, ch, F, x); });
+  per_chain_group(c, [&](int b, int ch, int lane, int W, unsigned mask) {
+    if (s.ch_d[b][ch] == 1) chain_fwd<T, 1>(c, b, ch, F, x, lane, W, mask);
+    else chain_fwd<T, 2>(c, b, ch, F, x, lane, W, mask);
+  });
   c.sync();
 }
 
