@@ -83,6 +83,7 @@ struct HostLayout {
   std::vector<short> eq_sp, eq_l, eq_m, idx_I, idx_E, idx_B, idx_N, qs_sp, qs_l, qs_m, row_slot, qs_slot, qo_slot, mx_idx,
       mx_pos;
   std::vector<double> cmin, cplu, dmin, dplu, dzer;
+  std::vector<GenRow> gen;
 };
 
 /* Build everything that depends only on the spec. */
@@ -426,7 +427,16 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
       used[best]++;
     }
   };
-  slots(H.eq_sp, {s.idx_phip}, H.row_slot);
+  /* the core rows (everything but the hierarchy moments with l >= 3, which run
+     from the GenRow table built below) */
+  {
+    std::vector<short> sp_core(H.eq_sp);
+    for (int i = 0; i < s.n; ++i) {
+      int sp_ = sp_core[i];
+      if ((sp_ == SP_I || sp_ == SP_E || sp_ == SP_B || sp_ == SP_N) && H.eq_l[i] >= 3) sp_core[i] = SP_NONE;
+    }
+    slots(sp_core, {s.idx_phip}, H.row_slot);
+  }
   slots(H.qs_sp, {s.iq_psi, s.iq_phi_prime_prime, s.iq_phi_prime_longitudinal, s.iq_phi_prime_poisson,
                   s.iq_omega_m1_prime, s.iq_gamma_m2_prime_prime, s.iq_vv_g}, H.qs_slot);
   /* the entries the source functions and the workspace read at an output time:
@@ -461,6 +471,57 @@ int build_layout(const song2_spec *sp, const song2_tables *tab, int first_order_
         H.dzer[lm * 3 + m - m1 + 1] = song2_coupling_d_zero(l, m1, m);
       }
     }
+
+  /* the chain rows as table entries (the same couplings and closures as the row
+     function of the evolver) */
+  H.gen.clear();
+  for (int i = 0; i < s.n; ++i) {
+    int sp_ = H.eq_sp[i], l = H.eq_l[i], m = H.eq_m[i];
+    if (!(sp_ == SP_I || sp_ == SP_E || sp_ == SP_B || sp_ == SP_N) || l < 3) continue;
+    GenRow r;
+    memset(&r, 0, sizeof(r));
+    r.i = (short)i;
+    r.j1 = r.j2 = r.j3 = -1;
+    int lm = LM(l, m);
+    auto at = [&](const std::vector<short> &idx, int ll) -> short {
+      if (ll < 0 || ll > s.Lq || m > ll) return -1;
+      return idx[LM(ll, m)];
+    };
+    if (sp_ == SP_I || sp_ == SP_N) {
+      const std::vector<short> &idx = sp_ == SP_I ? H.idx_I : H.idx_N;
+      int lmax = sp_ == SP_I ? s.l_max_g : s.l_max_ur;
+      r.kind = sp_ == SP_I ? 0 : 3;
+      r.q = (short)((sp_ == SP_I ? s.iq_g : s.iq_ur) + lm);
+      r.j1 = at(idx, l - 1);
+      if (l == lmax) {
+        r.c1 = sp_ == SP_I ? s.cl_I[m] : s.cl_N[m];
+        r.cd = l + 1 + m;
+      } else {
+        r.c1 = H.cmin[lm * 3 + 1];
+        r.c2 = -H.cplu[lm * 3 + 1];
+        r.j2 = at(idx, l + 1);
+      }
+    } else {
+      int e = sp_ == SP_E;
+      const std::vector<short> &idx = e ? H.idx_E : H.idx_B;
+      r.kind = e ? 1 : 2;
+      r.q = (short)((e ? s.iq_E : s.iq_B) + lm);
+      r.j1 = l - 1 >= 2 ? at(idx, l - 1) : -1;
+      r.j3 = (m >= 1) ? (e ? H.idx_B[lm] : H.idx_E[lm]) : -1;
+      if (l == s.l_max_pol) {
+        r.c1 = s.cl_P[m];
+        r.c3 = e ? -s.cmix_P[m] : s.cmix_P[m];
+        r.cd = l + 3;
+      } else {
+        r.c1 = H.dmin[lm * 3 + 1];
+        r.c2 = -H.dplu[lm * 3 + 1];
+        r.c3 = e ? -H.dzer[lm * 3 + 1] : H.dzer[lm * 3 + 1];
+        r.j2 = at(idx, l + 1);
+      }
+    }
+    H.gen.push_back(r);
+  }
+  s.n_gen = (int)H.gen.size();
 
   /* source types (perturb2_indices_of_perturbs, perturbations2.c:667-1075) */
   int tp = 0;
@@ -849,6 +910,7 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
   if (upload(c, H.row_slot, &p.tabs.row_slot, st, err) || upload(c, H.qs_slot, &p.tabs.qs_slot, st, err)) return 1;
   if (upload(c, H.mx_idx, &p.tabs.mx_idx, st, err) || upload(c, H.mx_pos, &p.tabs.mx_pos, st, err)) return 1;
   if (upload(c, H.qo_slot, &p.tabs.qo_slot, st, err)) return 1;
+  if (upload(c, H.gen, &p.tabs.gen, st, err)) return 1;
   if (upload(c, gitems, &p.items, st, err)) return 1;
   c->h_items = gitems;
   if (classes) {
@@ -874,7 +936,8 @@ int ctx_setup(song2_ctx *c, const song2_spec *sp, const song2_tables *tab, int p
           upload(c, hc.qs_sp, &t.qs_sp, st, err) || upload(c, hc.qs_l, &t.qs_l, st, err) ||
           upload(c, hc.qs_m, &t.qs_m, st, err) || upload(c, hc.row_slot, &t.row_slot, st, err) ||
           upload(c, hc.qs_slot, &t.qs_slot, st, err) || upload(c, hc.mx_idx, &t.mx_idx, st, err) ||
-          upload(c, hc.mx_pos, &t.mx_pos, st, err) || upload(c, hc.qo_slot, &t.qo_slot, st, err))
+          upload(c, hc.mx_pos, &t.mx_pos, st, err) || upload(c, hc.qo_slot, &t.qo_slot, st, err) ||
+          upload(c, hc.gen, &t.gen, st, err))
         return 1;
       ctabs.push_back(t);
     }
@@ -1560,6 +1623,8 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   size_t o_rsl = take(nrs), o_qsl = take(nqs);
   size_t nmx = sizeof(short) * H.mx_idx.size(), nqo = sizeof(short) * H.qo_slot.size();
   size_t o_mxi = take(nmx), o_mxp = take(nmx), o_qo = take(nqo);
+  size_t ngen = sizeof(GenRow) * H.gen.size();
+  size_t o_gen = take(ngen);
   size_t o_items = take(sizeof(WorkItem) * items.size());
   size_t o_queue = take(sizeof(int));
   std::vector<double> cs(std::max(2, s.fo_tau_size + 1), 0.0);
@@ -1625,6 +1690,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   CK(put(o_qsp, H.qs_sp.data(), nq)); CK(put(o_ql, H.qs_l.data(), nq)); CK(put(o_qm, H.qs_m.data(), nq));
   CK(put(o_rsl, H.row_slot.data(), nrs)); CK(put(o_qsl, H.qs_slot.data(), nqs));
   CK(put(o_mxi, H.mx_idx.data(), nmx)); CK(put(o_mxp, H.mx_pos.data(), nmx)); CK(put(o_qo, H.qo_slot.data(), nqo));
+  CK(put(o_gen, H.gen.data(), ngen));
   CK(put(o_items, items.data(), sizeof(WorkItem) * items.size()));
   CK(put(o_splc, cs.data(), sizeof(double) * cs.size()));
   CK(put(o_dt, dtc.data(), sizeof(double) * dtc.size()));
@@ -1652,6 +1718,7 @@ extern "C" int song2_gpu_evolve_noalloc(const song2_spec *spec, const song2_tabl
   p.tabs.row_slot = (const short *)(base + o_rsl); p.tabs.qs_slot = (const short *)(base + o_qsl);
   p.tabs.mx_idx = (const short *)(base + o_mxi); p.tabs.mx_pos = (const short *)(base + o_mxp);
   p.tabs.qo_slot = (const short *)(base + o_qo);
+  p.tabs.gen = (const GenRow *)(base + o_gen);
   p.items = (const WorkItem *)(base + o_items);
   p.sources = sources_dev;
   p.stats = stats_dev;

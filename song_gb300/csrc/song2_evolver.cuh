@@ -1372,15 +1372,46 @@ __device__ double row(const C &c, int ap, int i, const Y &y, const WS &w, int li
   return w.phi_pp - c.sh->bg.Hc * psi_prime_of(c, ap, y, w, lin, dI20, dN20);
 }
 
-/* dy = f(tau, y): block-wide; prepare(tau) must have run.  Ends with a barrier. */
+/* Row of a hierarchy moment with l >= 3 from its table entry (GenRow): the same
+   free-streaming, Thomson and closure terms as row_h, along one code path for
+   every species, l and m.  Zero where an approximation drops the moment (tight
+   coupling: I and E, B; radiation streaming: all four). */
+template <class Y, class C> __device__ __forceinline__ double gen_row(const C &c, int ap, const GenRow &r, const Y &y) {
+  if (ap == AP_RSA || (ap == AP_TCA && r.kind != 3)) return 0.0;
+  const BgV &bg = c.sh->bg;
+  double yi = y(r.i);
+  double d = c.sh->tri.k * (r.c1 * y(r.j1) + r.c2 * y(r.j2) + r.c3 * y(r.j3) - r.cd * bg.inv_ktau * yi);
+  if (r.kind != 3) d -= bg.kappa_dot * yi;
+  if (c.s.has_qs) d += c.qs[r.q];
+  return d;
+}
+
+/* the table entry of chain row e through the read-only cache */
+template <class C> __device__ inline GenRow load_gen(const C &c, int e) {
+  const GenRow *g = c.ct.gen + e;
+  GenRow r;
+  r.c1 = __ldg(&g->c1); r.c2 = __ldg(&g->c2); r.c3 = __ldg(&g->c3); r.cd = __ldg(&g->cd);
+  r.i = __ldg(&g->i); r.j1 = __ldg(&g->j1); r.j2 = __ldg(&g->j2); r.j3 = __ldg(&g->j3);
+  r.q = __ldg(&g->q); r.kind = __ldg(&g->kind);
+  return r;
+}
+
+/* dy = f(tau, y): block-wide; prepare(tau) must have run.  The core rows (row(),
+   row_slot order) and the chain rows (GenRow table) share one index space over
+   the team's threads.  Ends with a barrier. */
 template <class C, class A, class B> __device__ void rhs(const C &c, int ap, double tau, A y, B dy) {
   const DevSpec &s = c.s;
   auto yv = yvec(y);
   compute_ws_team(c, ap, yv);
   c.sync();
-  for (int e = c.rank; e < s.n_row_slots; e += c.size) {
-    int i = c.row_slot[e];
-    if (i >= 0) dy[i] = row(c, ap, i, yv, c.sh->ws, 0, tau);
+  for (int e = c.rank; e < s.n_row_slots + s.n_gen; e += c.size) {
+    if (e < s.n_row_slots) {
+      int i = c.row_slot[e];
+      if (i >= 0) dy[i] = row(c, ap, i, yv, c.sh->ws, 0, tau);
+    } else {
+      GenRow r = load_gen(c, e - s.n_row_slots);
+      dy[r.i] = gen_row(c, ap, r, yv);
+    }
   }
   c.sync();
 }
@@ -1396,12 +1427,19 @@ template <typename T, class C, class A> __device__ void newton_rhs(const C &c, i
   c.sync();
   PH_MARK(c, PH_WS);
   auto x = c.template xsol<T>();
-  for (int e = c.rank; e < s.n_row_slots; e += c.size) {
-    int i = c.row_slot[e];
-    if (i >= 0) {
-      double fi = row(c, ap, i, yv, c.sh->ws, 0, tau);
-      x[i] = (T)(hinvGak * fi - (c.psiv[i] + c.difkp1[i]));
+  for (int e = c.rank; e < s.n_row_slots + s.n_gen; e += c.size) {
+    int i;
+    double fi;
+    if (e < s.n_row_slots) {
+      i = c.row_slot[e];
+      if (i < 0) continue;
+      fi = row(c, ap, i, yv, c.sh->ws, 0, tau);
+    } else {
+      GenRow r = load_gen(c, e - s.n_row_slots);
+      i = r.i;
+      fi = gen_row(c, ap, r, yv);
     }
+    x[i] = (T)(hinvGak * fi - (c.psiv[i] + c.difkp1[i]));
   }
   c.sync();
   PH_MARK(c, PH_ROWS);

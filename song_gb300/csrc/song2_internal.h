@@ -56,7 +56,9 @@ struct DevSpec {
   int iq_psi, iq_psi_prime, iq_phi_prime_poisson, iq_phi_prime_longitudinal, iq_phi_prime_prime;
   int iq_omega_m1_prime, iq_gamma_m2_prime_prime, iq_vv_g, iq_vv_ur, iq_dd_b, iq_vv_b, iq_vv_cdm;
   int iq_vvp_b, iq_vvp_cdm;        /* d/dtau of the velocity products (psi') */
-  int n_row_slots, n_qs_slots;     /* species-grouped, warp-padded evaluation orders */
+  int n_row_slots, n_qs_slots;     /* species-grouped, warp-padded evaluation orders (rows: the
+                                      core rows; the chain rows come from the GenRow table) */
+  int n_gen;                       /* chain rows (GenRow entries) */
   int n_qo_slots;                  /* the same for the entries an output time needs */
   short iq_b11[2], iq_c11[2], iq_b000, iq_c000;
   /* state layout (grouped by m blocks) */
@@ -105,6 +107,17 @@ struct DevSpec {
   short ch1[S2_MAXBLK * S2_MAXCH], ch2[S2_MAXBLK * S2_MAXCH];
 };
 
+/* A hierarchy moment with l >= 3 (a chain row) as a table entry: its derivative is
+     k (c1 y[j1] + c2 y[j2] + c3 y[j3] - cd y[i] / (k tau)) - kappa' y[i] [I, E, B]
+       + qs[q]
+   (perturbations2.c:7931-7941, 8024-8036, 8120-8130 and the free-streaming rows
+   around them): j1, j2 the same species at l - 1 and l + 1, j3 the E-B partner at
+   the same l (-1: none), cd the closure's 1/(k tau) coefficient at l_max. */
+struct GenRow {
+  double c1, c2, c3, cd;
+  short i, j1, j2, j3, q, kind;    /* kind: 0 I, 1 E, 2 B, 3 N */
+};
+
 /* Per-triplet work item: indices and where its sources go. */
 struct WorkItem {
   int i1, i2, i3, pair;            /* pair = index of (i1,i2) in pair order */
@@ -119,6 +132,7 @@ struct ClassTabs {
   const short *idx_I, *idx_E, *idx_B, *idx_N;        /* [n_lm] -> state index or -1 */
   const short *qs_sp, *qs_l, *qs_m;                  /* [qs2_size] */
   const short *row_slot, *qs_slot;                   /* [n_row_slots], [n_qs_slots]: index or -1 */
+  const GenRow *gen;                                 /* [n_gen]: the chain rows */
   const short *qo_slot;                              /* [n_qo_slots]: entries read at output times */
   const short *mx_idx;                               /* [n]: state indices of the cores and chain nodes */
   const short *mx_pos;                               /* [n]: position of a state index in its block's
