@@ -6,16 +6,19 @@ on 50 log points in [1e-5, 0.3]/Mpc, 24 k3 per pair (30,600 triplets), T+E+B
 sources, l_max = min(40, 8 + ceil(k tau_rec / 2)) and m_max drawn from {0, 2, 4}
 per triplet (96 hierarchy classes, 32 to 744 equations), rtol 1e-4, 200 source
 times from 200 Mpc to tau0.  The triplets are dealt into K = --steps
-cost-balanced parts (song2_ctx_run_part: round-robin over each launch group's
-cost-sorted work list), so the K timed steps evolve every triplet exactly once.
+cost-balanced parts (round-robin over each launch group's cost-sorted work
+list), so the K timed steps evolve every triplet exactly once.  Consecutive
+parts run on two contexts and two streams (song2_ctx_enqueue_part), so that the
+last triplets of one part share the GPU with the first ones of the next.
 Inputs are synthetic: the background/recombination and first-order tables come
 from this project's own provider (the CLASS tables the reference would use are
 not available).
 
   value        triplets/s of the mixed form (FP64 right-hand side, Newton residual
                and error control; FP32 factorisation of the structured iteration
-               matrix), tables resident in HBM, CUDA events around each part's
-               launches; L2 flushed (256 MiB write) before every step.
+               matrix), tables resident in HBM, one pair of CUDA events around
+               all K parts' launches; L2 is not flushed between steps because a
+               step's working set exceeds it.
   plain_fp64   the plain FP64 form on the first --plain-parts parts, and the
                mixed form's time on the same parts (mixed_over_plain).
   e2e          triplets/s through song2_gpu_evolve (the drop-in C ABI) over the
@@ -381,6 +384,48 @@ def run_parts(lib, c, parts, n_parts, torch, flush):
     return ms, launches
 
 
+def run_overlapped(lib, ctxs, parts, n_parts, torch):
+    """The parts enqueued without waiting, part q on context q % len(ctxs) and on
+    that context's stream, so that the last triplets of one part overlap the first
+    ones of the next (the contexts have separate scratch); device time between one
+    pair of CUDA events around all of them, and the evolver launches enqueued."""
+    from song_gb300 import capi
+    err = capi.errbuf()
+    streams = [torch.cuda.Stream() for _ in ctxs]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cur = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    start.record(cur)
+    for s in streams:
+        s.wait_event(start)
+    launches = 0
+    for q in parts:
+        k = q % len(ctxs)
+        if lib.song2_ctx_enqueue_part(ctxs[k], int(q), n_parts, C.c_void_p(streams[k].cuda_stream), err):
+            raise RuntimeError(err.value.decode())
+        launches += lib.song2_ctx_last_launches(ctxs[k])
+    for s in streams:
+        e = torch.cuda.Event()
+        e.record(s)
+        cur.wait_event(e)
+    stop.record(cur)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop), launches
+
+
+def download_all(lib, ctxs, p):
+    """Sources and stats of contexts that evolved disjoint triplets, combined."""
+    src, st = None, None
+    for c in ctxs:
+        s1, t1 = download(lib, c, p)
+        if src is None:
+            src, st = s1, t1
+        else:
+            src += s1
+            st = np.where(t1["n_steps"] > 0, t1, st)
+    return src, st
+
+
 def download(lib, c, p):
     from song_gb300 import capi
     err = capi.errbuf()
@@ -475,7 +520,8 @@ def main():
     config = {"workload": cfg_name, "triplets_per_gpu": None, "k_min": cfg["k_min"], "k_max": cfg["k_max"],
               "k_size": cfg["k_size"], "k3_size": cfg["k3_size"], "l_max": cfg["l_max"], "m": list(cfg["m"]),
               "rtol": cfg["rtol"], "tau_size": cfg["tau_size"], "sources": cfg["sources"],
-              "l2": "flushed between steps (256 MiB write)", "rsa": args.rsa}
+              "l2": "not flushed between steps: a step's working set (the quadratic-source tables of the "
+                    "resident triplets, the first-order table) exceeds L2", "rsa": args.rsa}
     if cfg.get("uneven"):
         config["uneven"] = "l_max = min(40, 8 + ceil(k tau_rec/2)), m_max from {0,2,4} (seeded), 96 classes"
 
@@ -500,7 +546,8 @@ def main():
     p.first_order_gpu()          # first-order tables from the GPU first-order mode (untimed set-up)
     n_trip = p.n_triplets
     config["triplets_per_gpu"] = n_trip
-    config["parts"] = f"{n_parts} cost-balanced parts, one per step (song2_ctx_run_part)"
+    config["parts"] = (f"{n_parts} cost-balanced parts, one per step, on two contexts and streams so that "
+                       f"consecutive parts overlap (song2_ctx_enqueue_part); value = triplets / device time of all")
 
     # the rtol-1e-8 oracle check runs in a spawned CPU process during the GPU arms
     acc = None
@@ -524,20 +571,32 @@ def main():
         config["launch"] = {"warp_team": launch.warp_team, "teams_per_cta": launch.teams_per_cta,
                             "threads_per_team": launch.threads_per_team, "factors_in_smem": launch.lu_in_smem,
                             "autotune": f"song2_autotune on {args.autotune_sample} triplets ({tune_ms:.0f} ms)"}
-    c = ctx_create(lib, p, capi.SONG2_PREC_MIXED, launch)
+    # two contexts (separate scratch, separate streams): part q runs on context q % 2
+    n_ctx = 2 if n_parts >= 2 else 1
+    pp = min(args.plain_parts or max(1, args.steps // 4), max(1, n_parts - 2))
+    ctxs = [ctx_create(lib, p, capi.SONG2_PREC_MIXED, launch) for _ in range(n_ctx)]
     try:
-        run_parts(lib, c, [w % n_parts for w in range(args.warmup)], n_parts, torch, None)
+        # warm-up (untimed): every context regroups its work list and runs parts
+        for w in range(max(args.warmup, n_ctx)):
+            q = w % n_parts
+            run_parts(lib, ctxs[q % n_ctx], [q], n_parts, torch, None)
         if world > 1:
             dist.barrier()
+        flush.zero_()
         with Clocks(local) as clk:
-            ms_mixed, launches = run_parts(lib, c, [s % n_parts for s in range(args.steps)], n_parts, torch, flush)
+            ms_total, launches = run_overlapped(lib, ctxs, [s % n_parts for s in range(args.steps)], n_parts, torch)
         if world > 1:
             dist.barrier()
-        src_mixed, st_mixed = download(lib, c, p)
+        src_mixed, st_mixed = download_all(lib, ctxs, p)
+        # the mixed form on the parts the plain form is timed on (the ratio's numerator)
+        ms_mixed_same = None
+        if not args.no_plain:
+            ms_mixed_same, _ = run_overlapped(lib, ctxs, list(range(pp)), n_parts, torch)
     finally:
-        lib.song2_ctx_destroy(c)
+        for c in ctxs:
+            lib.song2_ctx_destroy(c)
     clocks = clk.summary()
-    t_mixed = sum(ms_mixed) / 1e3
+    t_mixed = ms_total / 1e3
     tt = torch.tensor([t_mixed], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -547,26 +606,22 @@ def main():
 
     plain = None
     if not args.no_plain:
-        pp = args.plain_parts or max(1, args.steps // 4)
-        pp = min(pp, n_parts)
-        c = ctx_create(lib, p, capi.SONG2_PREC_FP64)
-        warm = n_parts - 1 if n_parts - 1 >= pp else None
+        cp = [ctx_create(lib, p, capi.SONG2_PREC_FP64) for _ in range(n_ctx)]
+        # untimed warm-up on the last parts (not among the timed ones when there are enough)
+        warm = [q for q in range(n_parts - n_ctx, n_parts) if q >= pp]
         try:
-            if warm is not None:
-                run_parts(lib, c, [warm], n_parts, torch, None)
-                _, st_warm = download(lib, c, p)
-            ms_plain, _ = run_parts(lib, c, list(range(pp)), n_parts, torch, flush)
-            src_plain, st_plain = download(lib, c, p)
+            for q in warm:
+                run_parts(lib, cp[q % n_ctx], [q], n_parts, torch, None)
+            _, st_warm = download_all(lib, cp, p)
+            ms_plain, _ = run_overlapped(lib, cp, list(range(pp)), n_parts, torch)
+            src_plain, st_plain = download_all(lib, cp, p)
         finally:
-            lib.song2_ctx_destroy(c)
-        # the triplets of the timed parts (without the untimed warm-up part)
-        timed = st_plain["n_steps"] > 0
-        if warm is not None:
-            timed &= st_warm["n_steps"] == 0
-        ran = np.nonzero(timed)[0]
-        ms_m = sum(ms_mixed[q] for q in range(pp)) if pp <= args.steps else None
-        plain = {"parts": pp, "ms": ms_plain, "ms_mixed_same_parts": ms_m, "src": src_plain, "st": st_plain,
-                 "ran": ran}
+            for c in cp:
+                lib.song2_ctx_destroy(c)
+        # the triplets of the timed parts (without the untimed warm-up parts)
+        ran = np.nonzero((st_plain["n_steps"] > 0) & (st_warm["n_steps"] == 0))[0]
+        plain = {"parts": pp, "ms": [ms_plain], "ms_mixed_same_parts": ms_mixed_same, "src": src_plain,
+                 "st": st_plain, "ran": ran}
 
     e2e = None
     if not args.no_e2e:
@@ -621,7 +676,7 @@ def main():
         t_plain = sum(plain["ms"]) / 1e3
         n_pl = len(plain["ran"])
         line["plain_fp64"] = {"value": world * n_pl / t_plain, "unit": "triplets/s",
-                              "ms_per_step": 1e3 * t_plain / len(plain["ms"]),
+                              "ms_per_step": 1e3 * t_plain / plain["parts"],
                               "parts": f"{plain['parts']} of {n_parts} ({n_pl} triplets)",
                               "status_ok": bool(np.all(plain["st"]["status"][plain["ran"]] == 0))}
         if plain["ms_mixed_same_parts"]:

@@ -372,6 +372,12 @@ int song2_ctx_run(song2_ctx *ctx, void *stream, char *err);
    Blocking on return; song2_ctx_last_kernel_ms() gives the part's device time.
    No counterpart in the reference (its OpenMP loop runs every triplet at once). */
 int song2_ctx_run_part(song2_ctx *ctx, int part, int n_parts, void *stream, char *err);
+/* As song2_ctx_run_part without waiting: the part's launches are enqueued on
+   `stream` and the call returns (the first call with a new n_parts regroups the
+   work list first, blocking).  Parts of one context must not run concurrently
+   (they share the context's scratch); parts of two contexts may, on two streams,
+   so that one part's last triplets overlap the next part's first ones. */
+int song2_ctx_enqueue_part(song2_ctx *ctx, int part, int n_parts, void *stream, char *err);
 /* As song2_ctx_run, with the run's stream work (queue resets and the evolver
    launches of every launch group) captured into a CUDA graph on the first call
    and replayed on the later ones (no counterpart in the reference). */

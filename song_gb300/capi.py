@@ -155,6 +155,7 @@ SIGNATURES = {
     "song2_ctx_run": (_I, [_P, _P, C.c_char_p]),
     "song2_ctx_run_graph": (_I, [_P, _P, C.c_char_p]),
     "song2_ctx_run_part": (_I, [_P, _I, _I, _P, C.c_char_p]),
+    "song2_ctx_enqueue_part": (_I, [_P, _I, _I, _P, C.c_char_p]),
     "song2_ctx_device_sources": (_P, [_P]),
     "song2_ctx_device_stats": (_P, [_P]),
     "song2_ctx_download": (_I, [_P, _PD, C.POINTER(TripletStats), C.c_char_p]),

@@ -1297,12 +1297,11 @@ int song2_ctx_run(song2_ctx *c, void *stream, char *err) {
   return 0;
 }
 
-int song2_ctx_run_part(song2_ctx *c, int part, int n_parts, void *stream, char *err) {
+static int regroup_parts(song2_ctx *c, int part, int n_parts, cudaStream_t st, char *err) {
   if (n_parts < 1 || part < 0 || part >= n_parts) {
     snprintf(err, SONG2_ERRLEN, "bad part %d of %d", part, n_parts);
     return 1;
   }
-  cudaStream_t st = (cudaStream_t)stream;
   if (c->parts != n_parts) {
     /* regroup the work list part-major within every launch group: part q takes
        every n_parts-th item of the group's cost-sorted list, from position q */
@@ -1326,6 +1325,18 @@ int song2_ctx_run_part(song2_ctx *c, int part, int n_parts, void *stream, char *
     CK(cudaMemsetAsync(c->d_stats, 0, sizeof(song2_triplet_stats) * std::max(1, c->n_items), st));
     CK(cudaStreamSynchronize(st));
   }
+  return 0;
+}
+
+int song2_ctx_enqueue_part(song2_ctx *c, int part, int n_parts, void *stream, char *err) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (regroup_parts(c, part, n_parts, st, err)) return 1;
+  return enqueue_part(c, part, st, err);
+}
+
+int song2_ctx_run_part(song2_ctx *c, int part, int n_parts, void *stream, char *err) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (regroup_parts(c, part, n_parts, st, err)) return 1;
   CK(cudaEventRecord(c->ev0, st));
   if (enqueue_part(c, part, st, err)) return 1;
   CK(cudaEventRecord(c->ev1, st));

@@ -1728,6 +1728,7 @@ template <typename T, class C> __device__ __noinline__ void form_and_factor(cons
       c, [&](int b, int ch) { if (!chain_factor<T, 1>(c, b, ch, hg, J, F)) c.sh->lu_fail = 1; },
       [&](int b, int ch) { if (!chain_factor<T, 2>(c, b, ch, hg, J, F)) c.sh->lu_fail = 1; });
   c.sync();
+  PH_MARK(c, PH_FACT_CHAIN);
   per_block_group(c, [&](int b, int lane, int W, unsigned mask) {
     if (!core_factor<T>(c, b, hg, J, F, lane, W, mask)) c.sh->lu_fail = 1;
   });
@@ -1954,8 +1955,10 @@ template <typename T, class C> __device__ void lu_solve(const C &c) {
     else chain_back<T, 2>(c, b, ch, F, x, lane, W, mask);
   });
   c.sync();
+  PH_MARK(c, PH_SOLVE_BACK);
   per_block_group(c, [&](int b, int lane, int W, unsigned mask) { core_solve<T>(c, b, lane, W, mask); });
   c.sync();
+  PH_MARK(c, PH_SOLVE_CORE);
   per_chain_group(c, [&](int b, int ch, int lane, int W, unsigned mask) {
     if (s.ch_d[b][ch] == 1) chain_fwd<T, 1>(c, b, ch, F, x, lane, W, mask);
     else chain_fwd<T, 2>(c, b, ch, F, x, lane, W, mask);

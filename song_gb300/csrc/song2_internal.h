@@ -190,6 +190,9 @@ enum {
   PH_OUT_STORE,   /* output: source functions written */
   PH_CTRL,        /* step-size and order selection, state copy */
   PH_ITEM,        /* whole triplets (count = triplets) */
+  PH_SOLVE_BACK,  /* linear solve: backward sweeps of the chains (PH_SOLVE: the forward sweeps) */
+  PH_SOLVE_CORE,  /* linear solve: the cores */
+  PH_FACT_CHAIN,  /* factorisation: the chains (PH_FACT: the cores and the rest) */
   S2_NPHASE = 24
 };
 

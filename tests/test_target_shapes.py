@@ -124,14 +124,22 @@ def test_uneven_classes_against_tight_oracle(lib, uneven):
 
 
 def test_plain_configuration_matches_oracle(lib):
-    """Triplets of the 4,875-triplet plain configuration (l_max 12, 200 times)."""
+    """Triplets of the 4,875-triplet plain configuration (l_max 12, 200 times),
+    from the most squeezed (k1 = 0.1, k2 = 1e-5 /Mpc) to equilateral ones.  The
+    bound is 10 rtol, or three times the oracle's own integration error at this
+    rtol (against the oracle at rtol / 100) where that is larger: the m = 1 E
+    sources of the most squeezed triplet are tiny against the triplet's other
+    sources, the integrator controls them through its absolute error floor only,
+    and the oracle's own rtol-level error on them is 5e-4."""
     p = config_problem(2)
     p.first_order_gpu()
     order = np.arange(p.n_triplets)
     items = order[:: max(1, p.n_triplets // 12)][:12]
     ref, _ = oracle.evolve(p, nthreads=THREADS, items=items)
+    tight, _ = oracle.evolve(p, nthreads=THREADS, items=items, rtol=p.spec.rtol / 100)
+    bound = max(10 * p.spec.rtol, 3 * np.max(errors_on(p, ref, tight, items)))
     for precision in (capi.SONG2_PREC_FP64, capi.SONG2_PREC_MIXED):
         src, st = gpu_list(lib, p, items, precision)
         assert np.all(st["status"][items] == capi.SONG2_OK)
         e = errors_on(p, src, ref, items)
-        assert np.max(e) < 10 * p.spec.rtol, (precision, np.max(e))
+        assert np.max(e) < bound, (precision, np.max(e), bound)
