@@ -448,6 +448,119 @@ int song2_gpu_first_order(const song2_spec *spec2, const song2_tables *bg_only,
                           int fo_l_max, int fo_tau_size, double fo_lntau0,
                           double fo_dlntau, double *fo_out, char *err);
 
+/* ------------------------------------------- line-of-sight integration */
+/* The second-order transfer functions of transfer2_init (source/transfer2.c:79-636):
+   for every (k1, k2 <= k1) pair, every k of the pair's transfer k grid and every
+   transfer type (T, E, B) x (l, m),
+
+     T_lm(k1,k2,k) = 1/16/(2l+1) * sum_tau dtau_tau * sum_L J_Llm(k (tau0 - tau)) S_Lm(k1,k2,k,tau)
+
+   (transfer2_integrate, transfer2.c:2140-2365, with the trapezoid measure
+   dtau_i = tau_{i+1} - tau_{i-1} and its 1/2, and the factors 1/4, 1/(2l+1), 1/2 of
+   transfer2_compute, :1861-2138; E adds the B->E mixing J_EB S_B for m != 0, B is
+   J_EE S_B - J_EB S_E).  The sources are interpolated from the evolver's k3 grid
+   onto the transfer k grid (:2612-2780) and from the source time sampling onto the
+   integration grid (:2366-2610, :2783-2926).  The projection functions J_Llm(x)
+   are sums of spherical Bessel functions j_l1(x) with 3j coefficients
+   (bessel2_J_for_Llm / bessel2_J_Llm, bessel2.c:1041-1600), tabulated on a uniform
+   x grid and cut below the first x where |J| >= J_cut.
+
+   Transfer output layout (ptr2->transfer[index_tt][index_k1][index_k2][index_k],
+   transfer2.c:1007-1040): a flat buffer of tt2_size * (sum over pairs of the
+   pair's transfer k size) doubles; per tt, the pairs (k1 ascending, k2 <= k1) back
+   to back.  The tt index runs over T, then E, then B (the types the spec has),
+   each over (index_l, index_m) with m <= l, l major (transfer2_get_lm_lists,
+   :1121-1320). */
+enum song2_k3_sampling { SONG2_K3_SAMPLING_CLASS = 0, SONG2_K3_SAMPLING_BESSEL = 1 };
+enum song2_tau_sampling { SONG2_TAU_SAMPLING_SOURCES = 0, SONG2_TAU_SAMPLING_CUSTOM = 1,
+                          SONG2_TAU_SAMPLING_BESSEL = 2 };
+enum song2_interpolation { SONG2_INTERP_LINEAR = 0, SONG2_INTERP_CUBIC = 1 };
+enum song2_k3_extrapolation { SONG2_K3_EXTRAP_NONE = 0, SONG2_K3_EXTRAP_FLAT = 1 };
+enum song2_transfer_type { SONG2_TT_T = 0, SONG2_TT_E = 1, SONG2_TT_B = 2 };
+
+/* The transfer2/bessel2 parameters (precision2 / transfers2 / bessels2 fields,
+   input2.c:1433-1543, 1975-2016, defaults :2206, :2291-2331). */
+typedef struct {
+  int l_size;                       /* multipoles today: ptr2->l = pbs->l (song2_l_list) */
+  const int *l;                     /* ascending, >= 0 */
+  int k3_sampling;                  /* transfer2_k3_sampling: class (default) or bessel */
+  double q_linstep;                 /* q_linstep_song, 0.45 */
+  int tau_sampling;                 /* transfer2_tau_sampling: sources (default), custom, bessel */
+  double tau_linstep;               /* tau_linstep_song, 0.6 */
+  int k3_interpolation;             /* sources_k3_interpolation, linear */
+  int time_interpolation;           /* sources_time_interpolation, linear */
+  int bessel_interpolation;         /* bessels_interpolation (CLASS), linear */
+  int k3_extrapolation;             /* bispectra_k3_extrapolation: none or flat */
+  double extra_k3_oscillations_left, extra_k3_oscillations_right;
+  double x_step;                    /* pbs2->xx_step = bessel_x_step_song, 0.2 */
+  double x_max;                     /* pbs2->xx_max (song2_los_defaults applies input2.c:1982-2006) */
+  double j_cut;                     /* bessel_j_cut_song, 1e-12 */
+  double J_cut;                     /* bessel_J_cut_song, 1e-6 */
+  double bessel_tol_x_min;          /* CLASS bessel_tol_x_min, 1e-4 */
+  double tau0;                      /* conformal age (pba->conformal_age) */
+  double tau_rec;                   /* visibility peak (pth->tau_rec), song2_recombination_time() */
+} song2_los_spec;
+
+/* Defaults of the reference (input2.c) for the spec's k range and tables:
+   x_max = k_max * 18000 for the lin/log k samplings (input2.c:1986-1989), plus
+   one step, times 1.05; tau0 and tau_rec from the tables.  l and l_size are left
+   for the caller (song2_l_list). */
+void song2_los_defaults(song2_los_spec *los, const song2_spec *spec, const song2_tables *tab);
+/* The l sampling of the first-order Bessel module that transfer2 copies
+   (transfer2_get_l_list, transfer2.c:1081-1110; CLASS's l list: l = 2, then
+   steps of max(1, (int)(l (l_logstep - 1))) while below l_linstep, then steps
+   of l_linstep, and l_max last).  Writes the list into out (may be NULL) and
+   returns its length. */
+int song2_l_list(int l_max, double l_logstep, int l_linstep, int *out);
+/* Conformal time of the visibility peak, max of kappa' exp(-kappa) (pth->tau_rec). */
+double song2_recombination_time(const song2_tables *tab);
+/* Number of transfer types (ptr2->tt2_size) and, for each, its type, l and m
+   (any of the arrays may be NULL). */
+int song2_transfer_types(const song2_spec *spec, const song2_los_spec *los, int *type, int *l, int *m);
+/* Transfer k grid of every (k1, k2 <= k1) pair, in pair order (transfer2_get_k3_sizes
+   / _get_k3_size / _get_k3_list, transfer2.c:1329-1860): sizes[n_pairs],
+   physical_start[n_pairs] and physical_size[n_pairs] (any may be NULL), and the
+   grids back to back in k_out (NULL to query; its length is the return value of
+   the first call).  Returns the total number of k values, or -1 with a message. */
+int64_t song2_transfer_k_grids(const song2_spec *spec, const song2_los_spec *los, int *sizes, int *physical_start,
+                               int *physical_size, double *k_out, char *err);
+/* Row of 3j symbols (l1 l2 l3; -m2-m3 m2 m3) for every l1 from l1_min to
+   l1_max = l2 + l3, by the Schulten-Gordon recursion in l1 (the drc3jj routine the
+   reference calls at bessel2.c:1151-1197); out holds l1_max - l1_min + 1 values.
+   Returns 0, or 1 if the row is empty. */
+int song2_wigner3j_row(int l2, int l3, int m2, int m3, int *l1_min, int *l1_max, double *out, int out_size);
+
+/* Line-of-sight handle: the projection-function tables on the device
+   (bessel2_init, bessel2.c:75-497: the spherical Bessel functions j_l1(x) of the
+   extended l1 list, J_TT, J_EE and J_EB for every (L, l, m) with their x_min)
+   and the transfer k grids, for one spec and los spec. */
+typedef struct song2_los song2_los;
+int song2_los_create(const song2_spec *spec, const song2_los_spec *los, song2_los **out, char *err);
+void song2_los_destroy(song2_los *h);
+/* Doubles of the flat transfer output. */
+int64_t song2_los_transfer_size(const song2_los *h);
+/* The transfer functions of device-resident sources (the flat layout of
+   song2_ctx_download, e.g. song2_ctx_device_sources()) into transfer_dev
+   (song2_los_transfer_size() doubles), enqueued on `stream` (NULL = legacy
+   default stream); returns once the work is enqueued. */
+int song2_los_run(song2_los *h, const double *sources_dev, double *transfer_dev, void *stream, char *err);
+/* Device time (ms) of the last song2_los_run's kernels and of song2_los_create's
+   table build. */
+float song2_los_last_ms(const song2_los *h);
+float song2_los_tables_ms(const song2_los *h);
+/* Copies of the device tables, for checks: j_l1 on the x grid for each l1 of the
+   extended list ([n_l1][x_size], x below the l1's x_min zero) and J for every
+   projection row ([rows][x_size], row = ((J*L_size + L)*l_size + index_l)*m_size
+   + index_m with J = TT, EE, EB), with the rows' first non-negligible x index.
+   Sizes: song2_los_table_sizes.  Any pointer may be NULL. */
+void song2_los_table_sizes(const song2_los *h, int *x_size, int *n_l1, int *L_size, int *m_size, int *n_rows);
+int song2_los_tables(song2_los *h, int *l1, double *j_l1, double *J, int *J_xmin, char *err);
+/* One-shot drop-in for the transfer2_init compute loop: host sources in the flat
+   layout (or ppt2->sources gathered into it) to host transfers in the flat
+   transfer layout. */
+int song2_gpu_transfer(const song2_spec *spec, const song2_los_spec *los, const double *sources_flat,
+                       double *transfer_flat, char *err);
+
 #ifdef __cplusplus
 }
 #endif

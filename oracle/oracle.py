@@ -52,8 +52,88 @@ def load():
         lib.song2_oracle_geometry_checks.restype = C.c_int
         lib.song2_oracle_geometry_checks.argtypes = [C.POINTER(capi.Spec), C.c_int, C.c_int, C.c_int,
                                                      C.POINTER(C.c_double)]
+        # line-of-sight restatement (song2_los_oracle.c)
+        LS = C.POINTER(capi.LosSpec)
+        lib.song2_oracle_wigner3j.restype = C.c_double
+        lib.song2_oracle_wigner3j.argtypes = [C.c_int] * 6
+        lib.song2_oracle_bessel_all.restype = None
+        lib.song2_oracle_bessel_all.argtypes = [C.c_double, C.c_int, C.POINTER(C.c_double)]
+        lib.song2_oracle_l_list.restype = C.c_int
+        lib.song2_oracle_l_list.argtypes = [C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int)]
+        lib.song2_oracle_transfer_k_grids.restype = C.c_int64
+        lib.song2_oracle_transfer_k_grids.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_int),
+                                                      C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                      C.POINTER(C.c_double), C.c_char_p]
+        lib.song2_oracle_los_table_sizes.restype = C.c_int
+        lib.song2_oracle_los_table_sizes.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_int),
+                                                     C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        lib.song2_oracle_los_tables.restype = C.c_int
+        lib.song2_oracle_los_tables.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                                C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_char_p]
+        lib.song2_oracle_transfer.restype = C.c_int
+        lib.song2_oracle_transfer.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_double),
+                                              C.POINTER(C.c_double), C.c_int, C.c_char_p]
         _lib = lib
     return _lib
+
+
+def bessel_all(x, lmax):
+    """j_l(x) for l = 0..lmax (the oracle's long-double recurrence)."""
+    out = np.zeros(lmax + 1)
+    load().song2_oracle_bessel_all(float(x), int(lmax), out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def l_list(l_max, l_logstep, l_linstep):
+    out = np.zeros(l_max + 8, dtype=np.int32)
+    n = load().song2_oracle_l_list(l_max, l_logstep, l_linstep, out.ctypes.data_as(C.POINTER(C.c_int)))
+    return out[:n].copy()
+
+
+def transfer_k_grids(prob, los):
+    """(sizes, physical_start, physical_size, k values) of the transfer k grids."""
+    from song_gb300 import capi
+    lib = load()
+    n_pairs = len(prob.k) * (len(prob.k) + 1) // 2
+    sz, ps, pn = (np.zeros(n_pairs, dtype=np.int32) for _ in range(3))
+    err = capi.errbuf()
+    n = lib.song2_oracle_transfer_k_grids(C.byref(prob.spec), C.byref(los), capi.iptr(sz), capi.iptr(ps),
+                                          capi.iptr(pn), None, err)
+    if n < 0:
+        raise RuntimeError(err.value.decode())
+    kk = np.zeros(n)
+    lib.song2_oracle_transfer_k_grids(C.byref(prob.spec), C.byref(los), None, None, None, capi.dptr(kk), err)
+    return sz, ps, pn, kk
+
+
+def los_tables(prob, los):
+    """(l1 list, j_l1 [n_l1][x], J [rows][x], J x_min [rows]) in the product's full-row layout."""
+    from song_gb300 import capi
+    lib = load()
+    xs, nl1, nr = C.c_int(), C.c_int(), C.c_int()
+    if lib.song2_oracle_los_table_sizes(C.byref(prob.spec), C.byref(los), C.byref(xs), C.byref(nl1), C.byref(nr)):
+        raise RuntimeError("oracle line-of-sight tables failed")
+    l1 = np.zeros(nl1.value, dtype=np.int32)
+    jt = np.zeros((nl1.value, xs.value))
+    J = np.zeros((nr.value, xs.value))
+    xm = np.zeros(nr.value, dtype=np.int32)
+    err = capi.errbuf()
+    if lib.song2_oracle_los_tables(C.byref(prob.spec), C.byref(los), capi.iptr(l1), capi.dptr(jt), capi.dptr(J),
+                                   capi.iptr(xm), err):
+        raise RuntimeError(err.value.decode())
+    return l1, jt, J, xm
+
+
+def transfer(prob, los, sources, n_out, nthreads=0):
+    """Flat transfer functions [tt][units] of flat sources."""
+    from song_gb300 import capi
+    out = np.zeros(n_out)
+    err = capi.errbuf()
+    src = np.ascontiguousarray(sources, dtype=np.float64)
+    if load().song2_oracle_transfer(C.byref(prob.spec), C.byref(los), capi.dptr(src), capi.dptr(out),
+                                    nthreads or (os.cpu_count() or 1), err):
+        raise RuntimeError(err.value.decode())
+    return out
 
 
 def first_order(prob, nthreads=0):

@@ -1,0 +1,802 @@
+/*
+ * song2_los_oracle.c - CPU restatement of SONG's line-of-sight integration
+ * (source/transfer2.c, source/bessel2.c): second-order transfer functions from
+ * the second-order sources.
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity checker of the GPU line-of-sight
+ * kernels (song_gb300/csrc/song2_los.cu); only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU leg load it.  It shares no code with the product.
+ *
+ * Followed function by function:
+ *   transfer2_get_k3_size / _get_k3_sizes / _get_k3_list   transfer2.c:1329-1860
+ *   transfer2_get_lm_lists (type, l, m order)                transfer2.c:1121-1320
+ *   transfer2_get_time_grid                                  transfer2.c:2366-2610
+ *   transfer2_interpolate_sources_in_k / _in_time            transfer2.c:2612-2926
+ *   transfer2_integrate / transfer2_compute                  transfer2.c:1861-2365
+ *   bessel2_get_l1_list / _get_xx_list                       bessel2.c:832-1000
+ *   bessel2_J_for_Llm / bessel2_J_Llm / bessel2_j_for_l1     bessel2.c:1041-1800
+ *   array_spline_table_* (CLASS, absent from the reference tree): the cubic
+ *   spline with natural or estimated (3-point) end derivatives.
+ * Third-party pieces restated from their published algorithms: the spherical
+ * Bessel functions (CLASS bessel_j; here Miller's downward recurrence in long
+ * double), the 3j symbols (SLATEC drc3jj; here the Racah formula), CLASS's l
+ * list (transfer_get_l_list).  Parity with the reference itself is unpinned
+ * (the reference needs CLASS, which is absent); the Bessel functions and 3j
+ * symbols are pinned by the tests against scipy and sympy.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "song2.h"
+
+#define O_PI 3.141592653589793238462643383279502884
+
+/* ------------------------------------------------------------ helpers */
+
+static void o_lin_space(double *out, double a, double b, int n) {
+  for (int i = 0; i < n; ++i) out[i] = a + i * (b - a) / (n - 1);
+}
+
+static double o_lf(int n) { return lgamma((double)n + 1.0); }
+
+/* Wigner 3j by the Racah formula (log-factorials) */
+double song2_oracle_wigner3j(int j1, int j2, int j3, int m1, int m2, int m3) {
+  if (m1 + m2 + m3 != 0) return 0.0;
+  if (j3 < abs(j1 - j2) || j3 > j1 + j2) return 0.0;
+  if (abs(m1) > j1 || abs(m2) > j2 || abs(m3) > j3) return 0.0;
+  double pre = 0.5 * (o_lf(j1 + j2 - j3) + o_lf(j1 - j2 + j3) + o_lf(-j1 + j2 + j3) - o_lf(j1 + j2 + j3 + 1) +
+                      o_lf(j1 + m1) + o_lf(j1 - m1) + o_lf(j2 + m2) + o_lf(j2 - m2) + o_lf(j3 + m3) + o_lf(j3 - m3));
+  int tmin = 0;
+  if (j2 - j3 - m1 > tmin) tmin = j2 - j3 - m1;
+  if (j1 - j3 + m2 > tmin) tmin = j1 - j3 + m2;
+  int tmax = j1 + j2 - j3;
+  if (j1 - m1 < tmax) tmax = j1 - m1;
+  if (j2 + m2 < tmax) tmax = j2 + m2;
+  double sum = 0.0;
+  for (int t = tmin; t <= tmax; ++t) {
+    double v = exp(pre - (o_lf(t) + o_lf(j3 - j2 + t + m1) + o_lf(j3 - j1 + t - m2) + o_lf(j1 + j2 - j3 - t) +
+                          o_lf(j1 - t - m1) + o_lf(j2 - t + m2)));
+    sum += (t % 2 ? -v : v);
+  }
+  return ((j1 - j2 - m3) % 2 != 0) ? -sum : sum;
+}
+
+/* j_l(x) for l = 0..lmax by downward recurrence in long double from well above
+   max(lmax, x), normalised to j_0 or j_1; the stored values are rescaled
+   together whenever the recurrence nears the top of the long double range. */
+void song2_oracle_bessel_all(double x, int lmax, double *out) {
+  if (x == 0.0) {
+    for (int l = 0; l <= lmax; ++l) out[l] = (l == 0);
+    return;
+  }
+  double m = x > lmax ? x : lmax;
+  int top = (int)(m + 40.0 + 2.5 * sqrt(m));
+  long double *f = (long double *)malloc(sizeof(long double) * (top + 2));
+  long double X = x;
+  f[top + 1] = 0.0L;
+  f[top] = 1e-30L;
+  for (int l = top; l > 0; --l) {
+    f[l - 1] = (2.0L * l + 1.0L) / X * f[l] - f[l + 1];
+    if (fabsl(f[l - 1]) > 1e4000L)
+      for (int j = l - 1; j <= top; ++j) f[j] *= 1e-4000L;
+  }
+  long double s = sinl(X), c = cosl(X), j0 = s / X, j1;
+  if (x < 0.05) {
+    long double x2 = X * X;
+    j1 = X / 3.0L * (1.0L - x2 / 10.0L * (1.0L - x2 / 28.0L * (1.0L - x2 / 54.0L * (1.0L - x2 / 88.0L))));
+  } else {
+    j1 = (s / X - c) / X;
+  }
+  long double norm = (fabsl(j0) >= fabsl(j1)) ? j0 / f[0] : j1 / f[1];
+  for (int l = 0; l <= lmax; ++l) out[l] = (double)(f[l] * norm);
+  free(f);
+}
+
+static double o_bessel(int l, double x) {
+  double *buf = (double *)malloc(sizeof(double) * (l + 1));
+  song2_oracle_bessel_all(x, l, buf);
+  double v = buf[l];
+  free(buf);
+  return v;
+}
+
+/* cubic spline second derivatives on x[0..n-1] (stride-1 y), natural (est = 0)
+   or with end derivatives estimated from the parabola through three points */
+static void o_spline(const double *x, const double *y, int n, int est, double *y2) {
+  double *u = (double *)malloc(sizeof(double) * n);
+  if (est) {
+    double dy = ((x[2] - x[0]) * (x[2] - x[0]) * (y[1] - y[0]) - (x[1] - x[0]) * (x[1] - x[0]) * (y[2] - y[0])) /
+                ((x[2] - x[0]) * (x[1] - x[0]) * (x[2] - x[1]));
+    y2[0] = -0.5;
+    u[0] = (3. / (x[1] - x[0])) * ((y[1] - y[0]) / (x[1] - x[0]) - dy);
+  } else {
+    y2[0] = u[0] = 0.0;
+  }
+  for (int i = 1; i < n - 1; ++i) {
+    double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    double p = sig * y2[i - 1] + 2.0;
+    y2[i] = (sig - 1.0) / p;
+    u[i] = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
+    u[i] = (6.0 * u[i] / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p;
+  }
+  double qn, un;
+  if (est) {
+    double a = x[n - 3], b = x[n - 2], c = x[n - 1];
+    double dy = ((a - c) * (a - c) * (y[n - 2] - y[n - 1]) - (b - c) * (b - c) * (y[n - 3] - y[n - 1])) /
+                ((a - c) * (b - c) * (a - b));
+    qn = 0.5;
+    un = (3. / (c - b)) * (dy - (y[n - 1] - y[n - 2]) / (c - b));
+  } else {
+    qn = un = 0.0;
+  }
+  y2[n - 1] = (un - qn * u[n - 2]) / (qn * y2[n - 2] + 1.0);
+  for (int k = n - 2; k >= 0; --k) y2[k] = y2[k] * y2[k + 1] + u[k];
+  free(u);
+}
+
+/* ------------------------------------------------------------ l list */
+
+int song2_oracle_l_list(int l_max, double l_logstep, int l_linstep, int *out) {
+  int n = 0, l = 2;
+  if (l_max < 2) {
+    out[0] = l_max;
+    return 1;
+  }
+  out[n++] = l;
+  int inc = (int)(l * (l_logstep - 1.));
+  if (inc < 1) inc = 1;
+  while ((l + inc) < l_max && inc < l_linstep) {
+    l += inc;
+    out[n++] = l;
+    inc = (int)(l * (l_logstep - 1.));
+    if (inc < 1) inc = 1;
+  }
+  inc = l_linstep;
+  while ((l + inc) <= l_max) {
+    l += inc;
+    out[n++] = l;
+  }
+  if (l != l_max) out[n++] = l_max;
+  return n;
+}
+
+/* ------------------------------------------------------ k3 transfer grid */
+
+typedef struct {
+  int size, phys_start, phys_size;
+  double kmin, kmax, step;
+} o_kgrid;
+
+/* transfer2_get_k3_size */
+static int o_k3_size(const song2_spec *s, const song2_los_spec *los, const double *k3, int kn, o_kgrid *g,
+                     char *err) {
+  double kmin_pt = k3[0], kmax_pt = k3[kn - 1];
+  double kmin_tr = kmin_pt, kmax_tr = kmax_pt;
+  if (los->k3_extrapolation != SONG2_K3_EXTRAP_NONE) {
+    double phys = kmax_pt - kmin_pt;
+    double ext_r = 2. * O_PI * los->extra_k3_oscillations_right / (los->tau0 - los->tau_rec);
+    double ext_l = 2. * O_PI * los->extra_k3_oscillations_left / (los->tau0 - los->tau_rec);
+    if (phys < ext_r) kmax_tr += (ext_r - phys);
+    kmax_tr = fmin(kmax_tr, s->k[s->k_size - 1]);
+    if (phys < ext_l) kmin_tr -= (ext_l - phys);
+    kmin_tr = fmax(kmin_tr, fmin(s->k[0], kmin_pt));
+    if (los->extra_k3_oscillations_left < 0) kmin_tr = s->k[0];
+    if (los->extra_k3_oscillations_right < 0) kmax_tr = s->k[s->k_size - 1];
+  }
+  g->kmin = kmin_tr;
+  g->kmax = kmax_tr;
+  if (kmax_tr > los->x_max / los->tau0) {
+    snprintf(err, SONG2_ERRLEN, "x_max too small for k_max=%g", kmax_tr);
+    return 1;
+  }
+  double step = (los->k3_sampling == SONG2_K3_SAMPLING_CLASS) ? 2. * O_PI / (los->tau0 - los->tau_rec) * los->q_linstep
+                                                              : los->x_step / los->tau0;
+  g->step = step;
+  int ipt = 0, itr = 0;
+  double k = kmin_tr;
+  itr++;
+  if (los->k3_extrapolation != SONG2_K3_EXTRAP_NONE) {
+    while (k < kmin_pt) {
+      k += step;
+      itr++;
+    }
+    if (k != kmin_pt) k = kmin_pt;
+  }
+  ipt++;
+  g->phys_start = itr - 1;
+  while (ipt < kn && (k3[ipt] - k) < step) {
+    k = k3[ipt];
+    ipt++;
+    itr++;
+  }
+  g->phys_size = ipt;
+  while (k < kmax_tr) {
+    k += step;
+    itr++;
+    if (k <= kmax_pt && k >= kmin_pt) g->phys_size++;
+  }
+  g->size = (k > kmax_tr) ? itr - 1 : itr;
+  if (g->size < 2) {
+    snprintf(err, SONG2_ERRLEN, "fewer than 2 transfer k values");
+    return 1;
+  }
+  return 0;
+}
+
+/* transfer2_get_k3_list */
+static void o_k3_list(const song2_los_spec *los, const double *k3, int kn, const o_kgrid *g, double *out) {
+  double kmin_pt = k3[0];
+  int ipt = 0, itr = 0;
+  double k = g->kmin;
+  out[0] = g->kmin;
+  itr++;
+  if (los->k3_extrapolation != SONG2_K3_EXTRAP_NONE) {
+    while (k < kmin_pt) {
+      k += g->step;
+      out[itr] = k;
+      itr++;
+    }
+    if (k != kmin_pt) {
+      k = kmin_pt;
+      out[itr - 1] = k;
+    }
+  }
+  ipt++;
+  while (ipt < kn && (k3[ipt] - k) < g->step) {
+    k = k3[ipt];
+    out[itr] = k;
+    ipt++;
+    itr++;
+  }
+  while (itr < g->size && k < g->kmax) {
+    k += g->step;
+    out[itr] = k;
+    itr++;
+  }
+}
+
+int64_t song2_oracle_transfer_k_grids(const song2_spec *s, const song2_los_spec *los, int *sizes, int *pstart,
+                                      int *psize, double *k_out, char *err) {
+  int64_t tot = 0, off = 0;
+  int p = 0;
+  for (int i1 = 0; i1 < s->k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2, ++p) {
+      int kn = s->k3_size[i1 * s->k_size + i2];
+      o_kgrid g;
+      if (o_k3_size(s, los, s->k3 + off, kn, &g, err)) return -1;
+      if (sizes) sizes[p] = g.size;
+      if (pstart) pstart[p] = g.phys_start;
+      if (psize) psize[p] = g.phys_size;
+      if (k_out) o_k3_list(los, s->k3 + off, kn, &g, k_out + tot);
+      tot += g.size;
+      off += kn;
+    }
+  return tot;
+}
+
+/* ----------------------------------------------------------- tables */
+
+typedef struct {
+  int x_size;
+  double *xx;
+  int L_size, m_size, l_size, n_rows, n_l1;
+  int *l1, *l1_index, *jxmin;
+  double **j;       /* [n_l1][x_size - jxmin] */
+  double *J;        /* [n_rows][x_size], zero below the row's x_min */
+  double *ddJ;      /* cubic */
+  int *Jxmin;
+} o_tables;
+
+static int o_index_m_max(const song2_spec *s, int l) {
+  int im = -1;
+  for (int i = 0; i < s->m_size; ++i)
+    if (s->m[i] <= l) im = i;
+  return im;
+}
+
+/* bessel2_j_for_l1: x_min by bisection, then j_l1 on the x grid */
+static void o_j_for_l1(const song2_los_spec *los, o_tables *t, int r) {
+  int l1 = t->l1[r];
+  double x_min;
+  if (l1 == 0) {
+    x_min = 0;
+    t->jxmin[r] = 0;
+  } else {
+    double down = 0, up = l1 + 0.5;
+    while ((up - down) / down > los->bessel_tol_x_min) {
+      if ((up - down) < 1e-16) {
+        x_min = up = down;
+        break;
+      }
+      double j = o_bessel(l1, 0.5 * (up + down));
+      if (j >= los->j_cut) up = 0.5 * (up + down);
+      else down = 0.5 * (up + down);
+    }
+    x_min = down;
+    if (x_min < los->x_max) {
+      t->jxmin[r] = 0;
+      while (t->xx[t->jxmin[r]] < x_min) t->jxmin[r]++;
+      if (t->jxmin[r] != 0) --t->jxmin[r];
+    }
+  }
+  int n;
+  if (x_min >= los->x_max) {
+    t->jxmin[r] = t->x_size - 1;
+    n = 1;
+    t->j[r] = (double *)calloc(1, sizeof(double));
+    return;
+  }
+  n = t->x_size - t->jxmin[r];
+  t->j[r] = (double *)malloc(sizeof(double) * n);
+  double *buf = (double *)malloc(sizeof(double) * (l1 + 1));
+  for (int i = 0; i < n; ++i) {
+    song2_oracle_bessel_all(t->xx[t->jxmin[r] + i], l1, buf);
+    t->j[r][i] = buf[l1];
+  }
+  free(buf);
+}
+
+/* bessel2_J_Llm at one x index */
+static double o_J_Llm(const o_tables *t, int Jt, int L, int l, int m, int ix, const double *f1, const double *f2,
+                      int lo, int n) {
+  double J = 0;
+  for (int i = 0; i < n; ++i) {
+    if (f1[i] == 0) continue;
+    int l1 = lo + i;
+    int r = t->l1_index[l1];
+    int ixj = ix - t->jxmin[r];
+    if (ixj < 0) continue;
+    int even = ((l - l1 - L) % 2 == 0);
+    double pref;
+    if (Jt != 2) {
+      if (!even) continue;
+      pref = (((l - l1 - L) / 2) % 2 == 0) ? 1 : -1;
+    } else {
+      if (even) continue;
+      pref = (((l - l1 - L - 1) / 2) % 2 == 0) ? 1 : -1;
+    }
+    J += pref * (2 * l1 + 1) * f1[i] * f2[i] * t->j[r][ixj];
+  }
+  J *= ((m % 2 == 0) ? 1 : -1) * (2 * l + 1);
+  return J;
+}
+
+static int o_build_tables(const song2_spec *s, const song2_los_spec *los, o_tables *t, char *err) {
+  memset(t, 0, sizeof(*t));
+  double x_max = los->x_max;
+  t->x_size = (int)(x_max / los->x_step + 1);
+  t->xx = (double *)malloc(sizeof(double) * t->x_size);
+  o_lin_space(t->xx, 0, x_max, t->x_size);
+  int m_max = 0;
+  for (int i = 0; i < s->m_size; ++i)
+    if (s->m[i] > m_max) m_max = s->m[i];
+  int l_los = 0;
+  if (s->has_source_T && s->l_max_los_t > l_los) l_los = s->l_max_los_t;
+  if ((s->has_source_E || s->has_source_B) && s->l_max_los_p > l_los) l_los = s->l_max_los_p;
+  int L_max = l_los > m_max ? l_los : m_max;
+  t->L_size = L_max + 1;
+  t->m_size = s->m_size;
+  t->l_size = los->l_size;
+  t->n_rows = 3 * t->L_size * t->l_size * t->m_size;
+  /* l1 list */
+  int Lx = L_max + m_max;
+  int top = los->l[los->l_size - 1] + Lx;
+  t->l1 = (int *)malloc(sizeof(int) * (top + 1));
+  t->l1_index = (int *)malloc(sizeof(int) * (top + 1));
+  t->n_l1 = 0;
+  for (int l1 = 0; l1 <= top; ++l1) {
+    int keep = 0;
+    for (int i = 0; i < los->l_size; ++i)
+      if (l1 >= los->l[i] - Lx && l1 <= los->l[i] + Lx) keep = 1;
+    t->l1_index[l1] = keep ? t->n_l1 : -1;
+    if (keep) t->l1[t->n_l1++] = l1;
+  }
+  t->jxmin = (int *)calloc(t->n_l1, sizeof(int));
+  t->j = (double **)calloc(t->n_l1, sizeof(double *));
+#pragma omp parallel for schedule(dynamic)
+  for (int r = 0; r < t->n_l1; ++r) o_j_for_l1(los, t, r);
+  /* projection rows */
+  t->J = (double *)calloc((size_t)t->n_rows * t->x_size, sizeof(double));
+  t->Jxmin = (int *)malloc(sizeof(int) * t->n_rows);
+  int needT = s->has_source_T, needP = s->has_source_E || s->has_source_B;
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic) collapse(2)
+  for (int Jt = 0; Jt < 3; ++Jt)
+    for (int L = 0; L < t->L_size; ++L)
+      for (int il = 0; il < t->l_size; ++il)
+        for (int im = 0; im < t->m_size; ++im) {
+          int row = ((Jt * t->L_size + L) * t->l_size + il) * t->m_size + im;
+          int l = los->l[il], m = s->m[im];
+          int S = Jt == 0 ? 0 : 2;
+          int needed = Jt == 0 ? needT : (needP && (Jt == 1 || m_max > 0));
+          double *Jr = t->J + (size_t)row * t->x_size;
+          t->Jxmin[row] = t->x_size - 1;
+          if (!needed || m > (L < l ? L : l) || S > l || S > L || (Jt == 2 && m == 0)) continue;
+          int lo = abs(L - l), hi = L + l, n = hi - lo + 1;
+          double f1[64], f2[64];
+          for (int i = 0; i < n; ++i) {
+            f1[i] = song2_oracle_wigner3j(lo + i, L, l, 0, S, -S);
+            f2[i] = song2_oracle_wigner3j(lo + i, L, l, 0, -m, m);
+          }
+          int xmin;
+          if (L == l) {
+            xmin = 0;
+          } else {
+            double xu = lo + 0.5;
+            int up;
+            if (xu >= los->x_max) {
+              up = t->x_size - 1;
+              xu = los->x_max;
+            } else {
+              up = 0;
+              while (t->xx[up] < xu) up++;
+              xu = t->xx[up];
+            }
+            double J = o_J_Llm(t, Jt, L, l, m, up, f1, f2, lo, n);
+            if (fabs(J) < los->J_cut) {
+              if (xu < los->x_max) bad = 1;
+              continue;
+            }
+            int down = 0;
+            while (down != up - 1) {
+              int mid = (up + down) / 2;
+              J = o_J_Llm(t, Jt, L, l, m, mid, f1, f2, lo, n);
+              if (fabs(J) >= los->J_cut) up = mid;
+              else down = mid;
+            }
+            xmin = down;
+          }
+          t->Jxmin[row] = xmin;
+          for (int ix = xmin; ix < t->x_size; ++ix) Jr[ix] = o_J_Llm(t, Jt, L, l, m, ix, f1, f2, lo, n);
+        }
+  if (bad) {
+    snprintf(err, SONG2_ERRLEN, "projection function negligible at its first peak");
+    return 1;
+  }
+  if (los->bessel_interpolation == SONG2_INTERP_CUBIC) {
+    t->ddJ = (double *)calloc((size_t)t->n_rows * t->x_size, sizeof(double));
+#pragma omp parallel for schedule(dynamic)
+    for (int row = 0; row < t->n_rows; ++row) {
+      int x0 = t->Jxmin[row], n = t->x_size - x0;
+      int il = (row / t->m_size) % t->l_size;
+      if (n >= 3)
+        o_spline(t->xx + x0, t->J + (size_t)row * t->x_size + x0, n, los->l[il] == 2,
+                 t->ddJ + (size_t)row * t->x_size + x0);
+    }
+  }
+  return 0;
+}
+
+static void o_free_tables(o_tables *t) {
+  if (t->j)
+    for (int r = 0; r < t->n_l1; ++r) free(t->j[r]);
+  free(t->j);
+  free(t->xx);
+  free(t->l1);
+  free(t->l1_index);
+  free(t->jxmin);
+  free(t->J);
+  free(t->ddJ);
+  free(t->Jxmin);
+}
+
+int song2_oracle_los_table_sizes(const song2_spec *s, const song2_los_spec *los, int *x_size, int *n_l1,
+                                 int *n_rows) {
+  char err[SONG2_ERRLEN];
+  o_tables t;
+  if (o_build_tables(s, los, &t, err)) return 1;
+  *x_size = t.x_size;
+  *n_l1 = t.n_l1;
+  *n_rows = t.n_rows;
+  o_free_tables(&t);
+  return 0;
+}
+
+/* The tables in the product's full-row layout: j_l1 [n_l1][x_size] (zero below
+   the l1's x_min), J [n_rows][x_size] (zero below the row's x_min). */
+int song2_oracle_los_tables(const song2_spec *s, const song2_los_spec *los, int *l1, double *jtab, double *J,
+                            int *Jxmin, char *err) {
+  o_tables t;
+  if (o_build_tables(s, los, &t, err)) return 1;
+  for (int r = 0; r < t.n_l1; ++r) {
+    l1[r] = t.l1[r];
+    for (int i = 0; i < t.x_size; ++i) {
+      int ij = i - t.jxmin[r];
+      jtab[(size_t)r * t.x_size + i] = (ij >= 0 && (t.jxmin[r] < t.x_size - 1 || ij == 0)) ? t.j[r][ij] : 0.0;
+    }
+  }
+  memcpy(J, t.J, sizeof(double) * (size_t)t.n_rows * t.x_size);
+  memcpy(Jxmin, t.Jxmin, sizeof(int) * t.n_rows);
+  o_free_tables(&t);
+  return 0;
+}
+
+/* --------------------------------------------------------- transfers */
+
+static int o_lm(const song2_spec *s, int L, int im) {
+  int n = 0;
+  for (int l = 0; l < L; ++l)
+    for (int i = 0; i < s->m_size; ++i)
+      if (s->m[i] <= l) ++n;
+  return n + im;
+}
+
+int song2_oracle_transfer(const song2_spec *s, const song2_los_spec *los, const double *sources, double *out,
+                          int nthreads, char *err) {
+  o_tables t;
+  if (o_build_tables(s, los, &t, err)) return 1;
+  int n_pairs = s->k_size * (s->k_size + 1) / 2;
+  int *ksz = (int *)malloc(sizeof(int) * n_pairs), *kps = (int *)malloc(sizeof(int) * n_pairs),
+      *kpn = (int *)malloc(sizeof(int) * n_pairs);
+  int64_t nu = song2_oracle_transfer_k_grids(s, los, ksz, kps, kpn, NULL, err);
+  if (nu < 0) {
+    o_free_tables(&t);
+    return 1;
+  }
+  double *kall = (double *)malloc(sizeof(double) * nu);
+  song2_oracle_transfer_k_grids(s, los, NULL, NULL, NULL, kall, err);
+  /* source type blocks */
+  int base_T = 0, base_E = 0, base_B = 0, b = 0;
+  if (s->has_source_T) {
+    base_T = b;
+    b += o_lm(s, s->l_max_los_t + 1, 0);
+  }
+  if (s->has_source_E) {
+    base_E = b;
+    b += o_lm(s, s->l_max_los_p + 1, 0);
+  }
+  if (s->has_source_B) {
+    base_B = b;
+    b += o_lm(s, s->l_max_los_p + 1, 0);
+  }
+  /* transfer types: T, E, B x (index_l, index_m), l major */
+  int n_tt = 0;
+  int has[3] = {s->has_source_T, s->has_source_E, s->has_source_B};
+  for (int ty = 0; ty < 3; ++ty)
+    if (has[ty])
+      for (int il = 0; il < los->l_size; ++il) n_tt += o_index_m_max(s, los->l[il]) + 1;
+  int *tt_ty = (int *)malloc(sizeof(int) * n_tt), *tt_il = (int *)malloc(sizeof(int) * n_tt),
+      *tt_im = (int *)malloc(sizeof(int) * n_tt);
+  {
+    int o = 0;
+    for (int ty = 0; ty < 3; ++ty)
+      if (has[ty])
+        for (int il = 0; il < los->l_size; ++il)
+          for (int im = 0; im <= o_index_m_max(s, los->l[il]); ++im) {
+            tt_ty[o] = ty;
+            tt_il[o] = il;
+            tt_im[o] = im;
+            ++o;
+          }
+  }
+  int tp2 = song2_tp2_size(s);
+  int64_t per_type = song2_sources_per_type(s);
+  int ts = s->tau_size;
+  const double *tau_pt = s->tau;
+  /* pair offsets */
+  int64_t *src_off = (int64_t *)malloc(sizeof(int64_t) * n_pairs), *k3_off = (int64_t *)malloc(sizeof(int64_t) * n_pairs),
+          *u_off = (int64_t *)malloc(sizeof(int64_t) * n_pairs);
+  {
+    int64_t so = 0, ko = 0, uo = 0;
+    int p = 0;
+    for (int i1 = 0; i1 < s->k_size; ++i1)
+      for (int i2 = 0; i2 <= i1; ++i2, ++p) {
+        int kn = s->k3_size[i1 * s->k_size + i2];
+        src_off[p] = so;
+        k3_off[p] = ko;
+        u_off[p] = uo;
+        so += (int64_t)ts * kn;
+        ko += kn;
+        uo += ksz[p];
+      }
+  }
+  double x_step = los->x_step;
+  int L_T = s->l_max_los_t, L_P = s->l_max_los_p;
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int p = 0; p < n_pairs; ++p) {
+    int kn = 0;
+    {
+      int q = 0;
+      for (int i1 = 0; i1 < s->k_size; ++i1)
+        for (int i2 = 0; i2 <= i1; ++i2, ++q)
+          if (q == p) kn = s->k3_size[i1 * s->k_size + i2];
+    }
+    const double *kpt = s->k3 + k3_off[p];
+    int n_k = ksz[p];
+    const double *ktr = kall + u_off[p];
+    /* interpolation in k for every source type (transfer2_interpolate_sources_in_k) */
+    double *sk = (double *)calloc((size_t)tp2 * n_k * ts, sizeof(double)); /* [tp][k][tau] */
+    double *spl = (double *)malloc(sizeof(double) * (size_t)ts * kn);
+    double *col = (double *)malloc(sizeof(double) * kn), *colspl = (double *)malloc(sizeof(double) * kn);
+    for (int tp = 0; tp < tp2; ++tp) {
+      const double *S = sources + (int64_t)tp * per_type + src_off[p];
+      if (los->k3_interpolation == SONG2_INTERP_CUBIC)
+        for (int it = 0; it < ts; ++it) {
+          for (int j = 0; j < kn; ++j) col[j] = S[it * kn + j];
+          o_spline(kpt, col, kn, 1, colspl);
+          for (int j = 0; j < kn; ++j) spl[it * kn + j] = colspl[j];
+        }
+      int first = kps[p], last = kps[p] + kpn[p] - 1;
+      int ik = 0;
+      double h = kpt[1] - kpt[0];
+      for (int itr = first; itr <= last; ++itr) {
+        while (ik + 1 < kn && kpt[ik + 1] < ktr[itr]) {
+          ik++;
+          h = kpt[ik + 1] - kpt[ik];
+        }
+        double bb = (ktr[itr] - kpt[ik]) / h, aa = 1 - bb;
+        for (int it = 0; it < ts; ++it) {
+          double v = aa * S[it * kn + ik] + bb * S[it * kn + ik + 1];
+          if (los->k3_interpolation == SONG2_INTERP_CUBIC)
+            v += ((aa * aa * aa - aa) * spl[it * kn + ik] + (bb * bb * bb - bb) * spl[it * kn + ik + 1]) * h * h / 6.0;
+          sk[((size_t)tp * n_k + itr) * ts + it] = v;
+        }
+      }
+      if (los->k3_extrapolation == SONG2_K3_EXTRAP_FLAT) {
+        for (int itr = last + 1; itr < n_k; ++itr)
+          for (int it = 0; it < ts; ++it) sk[((size_t)tp * n_k + itr) * ts + it] = sk[((size_t)tp * n_k + last) * ts + it];
+        for (int itr = 0; itr < first; ++itr)
+          for (int it = 0; it < ts; ++it) sk[((size_t)tp * n_k + itr) * ts + it] = sk[((size_t)tp * n_k + first) * ts + it];
+      }
+    }
+    free(col);
+    free(colspl);
+    free(spl);
+    /* per k */
+    for (int ik = 0; ik < n_k; ++ik) {
+      double k = ktr[ik];
+      /* time grid (transfer2_get_time_grid) */
+      int G;
+      double *grid, *dtau;
+      int *left;
+      if (los->tau_sampling == SONG2_TAU_SAMPLING_SOURCES) {
+        G = ts;
+        grid = (double *)malloc(sizeof(double) * G);
+        left = (int *)malloc(sizeof(int) * G);
+        for (int i = 0; i < G; ++i) {
+          grid[i] = tau_pt[i];
+          left[i] = i;
+        }
+      } else {
+        double step = (los->tau_sampling == SONG2_TAU_SAMPLING_CUSTOM) ? 2 * O_PI / k * los->tau_linstep : x_step / k;
+        int itr = 0, ipt = 0;
+        double tau = tau_pt[0];
+        itr++;
+        ipt++;
+        while (ipt < ts) {
+          while ((tau_pt[ipt] - tau) > step) {
+            tau += step;
+            itr++;
+          }
+          tau = tau_pt[ipt];
+          ++itr;
+          ++ipt;
+        }
+        G = itr;
+        grid = (double *)malloc(sizeof(double) * G);
+        left = (int *)malloc(sizeof(int) * G);
+        itr = ipt = 0;
+        tau = tau_pt[0];
+        grid[0] = tau;
+        itr++;
+        ipt++;
+        left[0] = 0;
+        while (ipt < ts) {
+          while ((tau_pt[ipt] - tau) > step) {
+            tau += step;
+            grid[itr] = tau;
+            left[itr] = ipt;
+            itr++;
+          }
+          tau = tau_pt[ipt];
+          grid[itr] = tau;
+          left[itr] = ipt;
+          itr++;
+          ipt++;
+        }
+        for (int i = 0; i < G; ++i)
+          if (left[i] == ts - 1) left[i] = ts - 2;
+      }
+      dtau = (double *)malloc(sizeof(double) * G);
+      dtau[0] = grid[1] - grid[0];
+      for (int i = 1; i < G - 1; ++i) dtau[i] = grid[i + 1] - grid[i - 1];
+      dtau[G - 1] = grid[G - 1] - grid[G - 2];
+      /* sources at the grid times (transfer2_interpolate_sources_in_time) */
+      double *st = (double *)malloc(sizeof(double) * (size_t)tp2 * G);
+      double *tspl = (double *)malloc(sizeof(double) * ts);
+      for (int tp = 0; tp < tp2; ++tp) {
+        const double *row = sk + ((size_t)tp * n_k + ik) * ts;
+        if (los->tau_sampling == SONG2_TAU_SAMPLING_SOURCES) {
+          for (int i = 0; i < G; ++i) st[(size_t)tp * G + i] = row[i];
+          continue;
+        }
+        if (los->time_interpolation == SONG2_INTERP_CUBIC) o_spline(tau_pt, row, ts, 1, tspl);
+        for (int i = 0; i < G; ++i) {
+          int it = left[i];
+          double hh = tau_pt[it + 1] - tau_pt[it];
+          double bb = (grid[i] - tau_pt[it]) / hh, aa = 1 - bb;
+          double v = aa * row[it] + bb * row[it + 1];
+          if (los->time_interpolation == SONG2_INTERP_CUBIC)
+            v += ((aa * aa * aa - aa) * tspl[it] + (bb * bb * bb - bb) * tspl[it + 1]) * hh * hh / 6.0;
+          st[(size_t)tp * G + i] = v;
+        }
+      }
+      free(tspl);
+      /* transfer2_compute / transfer2_integrate for every type */
+      for (int o = 0; o < n_tt; ++o) {
+        int ty = tt_ty[o], il = tt_il[o], im = tt_im[o];
+        int l = los->l[il], m = s->m[im];
+        /* (J, source base, sign) pieces */
+        int nq = 0, Jq[2], Bq[2];
+        double Sq[2];
+        int Lmax;
+        if (ty == 0) {
+          Lmax = L_T;
+          Jq[0] = 0; Bq[0] = base_T; Sq[0] = 1; nq = 1;
+        } else if (ty == 1) {
+          Lmax = L_P;
+          Jq[0] = 1; Bq[0] = base_E; Sq[0] = 1; nq = 1;
+          if (m != 0 && s->has_source_B) { Jq[1] = 2; Bq[1] = base_B; Sq[1] = 1; nq = 2; }
+        } else {
+          Lmax = L_P;
+          Jq[0] = 1; Bq[0] = base_B; Sq[0] = 1; nq = 1;
+          if (s->has_source_E) { Jq[1] = 2; Bq[1] = base_E; Sq[1] = -1; nq = 2; }
+        }
+        double contrib[2] = {0, 0};
+        for (int q = 0; q < nq; ++q) {
+          double integral = 0;
+          for (int i = 0; i < G; ++i) {
+            double x = k * (los->tau0 - grid[i]);
+            int ix = (int)(x / x_step);
+            double aJ = (t.xx[ix + 1] - x) / x_step;
+            double integrand = 0;
+            for (int L = 0; L <= Lmax; ++L) {
+              if (m > (L < l ? L : l)) continue;
+              int row = ((Jq[q] * t.L_size + L) * t.l_size + il) * t.m_size + im;
+              int xmin = t.Jxmin[row];
+              if (ix < xmin) continue;
+              const double *Jr = t.J + (size_t)row * t.x_size;
+              double Jv;
+              if (los->bessel_interpolation == SONG2_INTERP_LINEAR) {
+                Jv = aJ * Jr[ix] + (1 - aJ) * Jr[ix + 1];
+              } else {
+                const double *dd = t.ddJ + (size_t)row * t.x_size;
+                Jv = (aJ * Jr[ix] + (1. - aJ) * (Jr[ix + 1] - aJ * ((aJ + 1.) * dd[ix] + (2. - aJ) * dd[ix + 1]) *
+                                                                    x_step * x_step / 6.0));
+              }
+              int tp = Bq[q] + o_lm(s, L, im);
+              integrand += Jv * st[(size_t)tp * G + i];
+            }
+            integral += integrand * dtau[i];
+          }
+          contrib[q] = integral * 0.5;
+        }
+        double tr = (nq == 2) ? (Sq[1] < 0 ? contrib[0] - contrib[1] : contrib[0] + contrib[1]) : contrib[0];
+        tr /= 4.;
+        tr /= (2. * l + 1);
+        tr /= 2.;
+        out[(int64_t)o * nu + u_off[p] + ik] = tr;
+      }
+      free(st);
+      free(grid);
+      free(left);
+      free(dtau);
+    }
+    free(sk);
+  }
+  free(ksz);
+  free(kps);
+  free(kpn);
+  free(kall);
+  free(tt_ty);
+  free(tt_il);
+  free(tt_im);
+  free(src_off);
+  free(k3_off);
+  free(u_off);
+  o_free_tables(&t);
+  return 0;
+}

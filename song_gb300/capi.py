@@ -95,6 +95,27 @@ class Tables(C.Structure):
     ]
 
 
+class LosSpec(C.Structure):
+    """song2_los_spec: the transfer2/bessel2 parameters of the line-of-sight integration."""
+    _fields_ = [
+        ("l_size", C.c_int), ("l", C.POINTER(C.c_int)),
+        ("k3_sampling", C.c_int), ("q_linstep", C.c_double),
+        ("tau_sampling", C.c_int), ("tau_linstep", C.c_double),
+        ("k3_interpolation", C.c_int), ("time_interpolation", C.c_int), ("bessel_interpolation", C.c_int),
+        ("k3_extrapolation", C.c_int),
+        ("extra_k3_oscillations_left", C.c_double), ("extra_k3_oscillations_right", C.c_double),
+        ("x_step", C.c_double), ("x_max", C.c_double),
+        ("j_cut", C.c_double), ("J_cut", C.c_double), ("bessel_tol_x_min", C.c_double),
+        ("tau0", C.c_double), ("tau_rec", C.c_double),
+    ]
+
+
+K3_SAMPLING_CLASS, K3_SAMPLING_BESSEL = 0, 1
+TAU_SAMPLING_SOURCES, TAU_SAMPLING_CUSTOM, TAU_SAMPLING_BESSEL = 0, 1, 2
+INTERP_LINEAR, INTERP_CUBIC = 0, 1
+K3_EXTRAP_NONE, K3_EXTRAP_FLAT = 0, 1
+
+
 class Launch(C.Structure):
     _fields_ = [("warp_team", C.c_int), ("teams_per_cta", C.c_int), ("threads_per_team", C.c_int),
                 ("lu_in_smem", C.c_int)]
@@ -167,6 +188,21 @@ SIGNATURES = {
     "song2_gpu_evolve_noalloc": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_char_p]),
     "song2_gpu_first_order": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _D, _D, _PD, C.c_char_p]),
+    "song2_los_defaults": (None, [C.POINTER(LosSpec), C.POINTER(Spec), C.POINTER(Tables)]),
+    "song2_l_list": (_I, [_I, _D, _I, _PI]),
+    "song2_recombination_time": (_D, [C.POINTER(Tables)]),
+    "song2_transfer_types": (_I, [C.POINTER(Spec), C.POINTER(LosSpec), _PI, _PI, _PI]),
+    "song2_transfer_k_grids": (C.c_int64, [C.POINTER(Spec), C.POINTER(LosSpec), _PI, _PI, _PI, _PD, C.c_char_p]),
+    "song2_wigner3j_row": (_I, [_I, _I, _I, _I, _PI, _PI, _PD, _I]),
+    "song2_los_create": (_I, [C.POINTER(Spec), C.POINTER(LosSpec), C.POINTER(_P), C.c_char_p]),
+    "song2_los_destroy": (None, [_P]),
+    "song2_los_transfer_size": (C.c_int64, [_P]),
+    "song2_los_run": (_I, [_P, _P, _P, _P, C.c_char_p]),
+    "song2_los_last_ms": (C.c_float, [_P]),
+    "song2_los_tables_ms": (C.c_float, [_P]),
+    "song2_los_table_sizes": (None, [_P, _PI, _PI, _PI, _PI, _PI]),
+    "song2_los_tables": (_I, [_P, _PI, _PD, _PD, _PI, C.c_char_p]),
+    "song2_gpu_transfer": (_I, [C.POINTER(Spec), C.POINTER(LosSpec), _PD, _PD, C.c_char_p]),
 }
 
 
@@ -180,7 +216,7 @@ def bind(lib, host_only=False):
     host-side functions that a library exports (a CPU-only build of the input
     provider, which carries no GPU entry points)."""
     for name, (res, args) in SIGNATURES.items():
-        if host_only and ("_ctx_" in name or "_gpu_" in name or name == "song2_autotune"):
+        if host_only and ("_ctx_" in name or "_gpu_" in name or "_los_" in name or name == "song2_autotune"):
             continue
         try:
             f = getattr(lib, name)
