@@ -8,8 +8,8 @@ per triplet (96 hierarchy classes, 32 to 744 equations), rtol 1e-4, 200 source
 times from 200 Mpc to tau0.  The triplets are dealt into K = --steps
 cost-balanced parts (round-robin over each launch group's cost-sorted work
 list), so the K timed steps evolve every triplet exactly once.  Consecutive
-parts run on two contexts and two streams (song2_ctx_enqueue_part), so that the
-last triplets of one part share the GPU with the first ones of the next.
+parts run on --contexts contexts and streams (song2_ctx_enqueue_part), so that
+the last triplets of one part share the GPU with the next parts.
 Inputs are synthetic: the background/recombination and first-order tables come
 from this project's own provider (the CLASS tables the reference would use are
 not available).
@@ -26,6 +26,12 @@ not available).
                slabs filled inside the timed region.
   cpu_baseline the CPU restatement (oracle/) on this machine's host cores, on a
                bounded cost-stratified sample of the same triplets.
+  contract     the mixed form at rtol 1e-6, where every sampled source meets
+               the 1e-4 bound: throughput on the first --contract-parts parts
+               and the error on the accuracy sample.
+  transfer2    the line-of-sight integral (transfer2) of this run's sources on
+               the device: transfer functions/s, the projection-table build, the
+               CPU restatement on the heaviest pairs as baseline and parity check.
   err_vs_fp64_oracle
                per (source type, triplet) max_tau |S - S_ref| / max_tau |S_ref| of
                the GPU sources against the oracle at rtol 1e-8, on triplets spread
@@ -58,6 +64,13 @@ sys.path.insert(0, ROOT)
 METRIC = "2nd-order k-triplets/s at rtol 1e-4: mixed+batched vs plain FP64 GPU; err vs FP64"
 WORKLOAD = 4
 ERR_BOUND = 1e-4
+# the rtol at which every sampled config-4 source meets ERR_BOUND against the
+# rtol-1e-8 oracle (the global error of an rtol-1e-4 integration, GPU or CPU,
+# is about 1.7e-3 on the squeezed triplets)
+CONTRACT_RTOL = 1e-6
+# line-of-sight leg: the l sampling of the reference's precision presets
+# (pre/*lmax2000.pre: l_max_scalars 2000, l_logstep 1.25, l_linstep 36)
+LOS_L = (2000, 1.25, 36)
 # FP64 work of the mixed-form evolver per NDF step and FP64 warp instructions per
 # NDF step (ncu counters of this kernel on the reduced config-4 case, see
 # profiles/), and the FP64 issue rate of a GB300 SM (one FP64 warp instruction per
@@ -85,6 +98,13 @@ def parse():
     ap.add_argument("--autotune-sample", type=int, default=256,
                     help="triplets the autotuner times its launch candidates on (0: default launch)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--contexts", type=int, default=4, help="contexts (and streams) the parts alternate over")
+    ap.add_argument("--contract-parts", type=int, default=2,
+                    help="parts timed at the contract rtol (0: skip the contract leg)")
+    ap.add_argument("--no-los", action="store_true", help="skip the line-of-sight (transfer2) leg")
+    ap.add_argument("--los-reps", type=int, default=3)
+    ap.add_argument("--los-cpu-share", type=float, default=0.05,
+                    help="share of the transfer k units the CPU baseline of the line of sight runs")
     ap.add_argument("--k-size", type=int, default=None, help="override the k grid size (small profiling cases)")
     ap.add_argument("--k3-size", type=int, default=None, help="override the k3 grid size (small profiling cases)")
     ap.add_argument("--rsa", type=int, default=0, choices=[0, 1, 2],
@@ -413,6 +433,126 @@ def run_overlapped(lib, ctxs, parts, n_parts, torch):
     return start.elapsed_time(stop), launches
 
 
+class _RtolView:
+    """The problem with another ODE rtol (a spec copy sharing the grids and tables)."""
+
+    def __init__(self, p, rtol):
+        from song_gb300 import capi
+        self.spec = capi.Spec.from_buffer_copy(p.spec)
+        self.spec.rtol = rtol
+        self.tables = p.tables
+
+
+def contract_leg(lib, p, launch, parts, n_parts, n_ctx, items, torch):
+    """The mixed form at CONTRACT_RTOL: device time of the given parts (overlapped
+    like the headline run) and the sources of the accuracy sample."""
+    from song_gb300 import capi
+    v = _RtolView(p, CONTRACT_RTOL)
+    ctxs = [ctx_create(lib, v, capi.SONG2_PREC_MIXED, launch) for _ in range(n_ctx)]
+    try:
+        for q in range(n_ctx):  # regroup (untimed)
+            run_parts(lib, ctxs[q], [parts[q % len(parts)]], n_parts, torch, None)
+        ms, _ = run_overlapped(lib, ctxs, parts, n_parts, torch)
+        _, st = download_all(lib, ctxs, p)
+    finally:
+        for c in ctxs:
+            lib.song2_ctx_destroy(c)
+    ran = int(np.count_nonzero(st["n_steps"]))
+    src_acc = None
+    if items is not None and len(items):
+        c = C.c_void_p()
+        err = capi.errbuf()
+        it = np.ascontiguousarray(items, dtype=np.int64)
+        if lib.song2_ctx_create_list(C.byref(v.spec), C.byref(v.tables), capi.SONG2_PREC_MIXED,
+                                     it.ctypes.data_as(C.POINTER(C.c_int64)), len(it), C.byref(c), err):
+            raise RuntimeError(err.value.decode())
+        try:
+            if lib.song2_ctx_run(c, None, err):
+                raise RuntimeError(err.value.decode())
+            src_acc, _ = download(lib, c, p)
+        finally:
+            lib.song2_ctx_destroy(c)
+    return {"ms": ms, "triplets": ran, "status_ok": bool(np.all(st["status"] == 0)), "src": src_acc}
+
+
+def los_leg(lib, p, src_host, torch, reps, cpu_share):
+    """transfer2 on the device: projection tables built once, then the line-of-sight
+    integral of the config's sources (already in HBM) timed over `reps` runs; the CPU
+    restatement on a contiguous run of the heaviest pairs as the baseline, and the
+    GPU transfers of those pairs checked against it."""
+    from song_gb300 import capi
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    los = capi.LosSpec()
+    lib.song2_los_defaults(C.byref(los), C.byref(p.spec), C.byref(p.tables))
+    n_l = lib.song2_l_list(*LOS_L, None)
+    ls = np.zeros(n_l, dtype=np.int32)
+    lib.song2_l_list(*LOS_L, capi.iptr(ls))
+    los.l_size = n_l
+    los.l = capi.iptr(ls)
+    err = capi.errbuf()
+    n_pairs = len(p.k) * (len(p.k) + 1) // 2
+    ksz = np.zeros(n_pairs, dtype=np.int32)
+    n_units = lib.song2_transfer_k_grids(C.byref(p.spec), C.byref(los), capi.iptr(ksz), None, None, None, err)
+    n_tt = lib.song2_transfer_types(C.byref(p.spec), C.byref(los), None, None, None)
+    h = C.c_void_p()
+    t0 = time.perf_counter()
+    if lib.song2_los_create(C.byref(p.spec), C.byref(los), C.byref(h), err):
+        raise RuntimeError(err.value.decode())
+    create_s = time.perf_counter() - t0
+    try:
+        xs, nl1, nr = C.c_int(), C.c_int(), C.c_int()
+        lib.song2_los_table_sizes(h, C.byref(xs), C.byref(nl1), None, None, C.byref(nr))
+        n_out = lib.song2_los_transfer_size(h)
+        d_src = torch.from_numpy(src_host).cuda()
+        d_out = torch.zeros(n_out, dtype=torch.float64, device="cuda")
+        ms = []
+        for r in range(reps + 1):
+            if lib.song2_los_run(h, C.c_void_p(d_src.data_ptr()), C.c_void_p(d_out.data_ptr()), None, err):
+                raise RuntimeError(err.value.decode())
+            if r:
+                ms.append(lib.song2_los_last_ms(h))
+        tables_ms = lib.song2_los_tables_ms(h)
+        out = d_out.cpu().numpy()
+    finally:
+        lib.song2_los_destroy(h)
+        d_src = d_out = None
+    t_run = sum(ms) / len(ms) / 1e3
+    # CPU restatement on the heaviest pairs (the last ones), about cpu_share of the units
+    cum = np.cumsum(ksz[::-1])
+    n_last = int(np.searchsorted(cum, cpu_share * n_units)) + 1
+    lo = n_pairs - n_last
+    units_cpu = int(ksz[lo:].sum())
+    t0 = time.perf_counter()
+    ref = oracle.transfer(p, los, src_host, n_out, nthreads=os.cpu_count(), pairs=(lo, n_pairs))
+    cpu_s = time.perf_counter() - t0
+    u0 = int(ksz[:lo].sum())
+    g = out.reshape(n_tt, n_units)[:, u0:]
+    r_ = ref.reshape(n_tt, n_units)[:, u0:]
+    scale = np.max(np.abs(r_), axis=1)
+    ok = scale > 0
+    rel = float(np.max(np.max(np.abs(g - r_), axis=1)[ok] / scale[ok])) if ok.any() else 0.0
+    zero_bad = float(np.max(np.abs(g[~ok]))) if (~ok).any() else 0.0
+    return {
+        "metric": "second-order transfer functions T_lm(k1,k2,k) per second (transfer2 line of sight)",
+        "value": n_out / t_run, "unit": "transfers/s", "ms_per_run": 1e3 * t_run, "runs": reps,
+        "units_per_s": n_units / t_run,
+        "workload": {"sources": "this run's mixed-form sources of every triplet (already in HBM)",
+                     "pairs": n_pairs, "k_units": int(n_units), "transfer_types": int(n_tt),
+                     "l_list": f"l_max {LOS_L[0]}, l_logstep {LOS_L[1]}, l_linstep {LOS_L[2]} ({n_l} l)",
+                     "x_grid": f"{xs.value} nodes of 0.2 to x_max {los.x_max:.0f}",
+                     "projection_rows": int(nr.value), "bessel_l1": int(nl1.value),
+                     "sampling": "k3 class (q_linstep 0.45), tau = source sampling, linear interpolation "
+                                 "(transfer2 defaults)"},
+        "tables_ms": float(tables_ms), "create_s": create_s,
+        "cpu_baseline": {"value": n_tt * units_cpu / (cpu_s), "unit": "transfers/s", "cores": os.cpu_count(),
+                         "kind": "port", "sample": f"the {n_last} pairs of largest k1 ({units_cpu} of {n_units} "
+                                                   f"k units; {cpu_s:.1f} s including the tables)"},
+        "max_rel_err_vs_cpu": rel, "zero_rows_nonzero": zero_bad, "tolerance": 1e-9,
+        "within_tolerance": bool(rel <= 1e-9 and zero_bad == 0.0),
+    }
+
+
 def download_all(lib, ctxs, p):
     """Sources and stats of contexts that evolved disjoint triplets, combined."""
     src, st = None, None
@@ -546,8 +686,9 @@ def main():
     p.first_order_gpu()          # first-order tables from the GPU first-order mode (untimed set-up)
     n_trip = p.n_triplets
     config["triplets_per_gpu"] = n_trip
-    config["parts"] = (f"{n_parts} cost-balanced parts, one per step, on two contexts and streams so that "
-                       f"consecutive parts overlap (song2_ctx_enqueue_part); value = triplets / device time of all")
+    config["parts"] = (f"{n_parts} cost-balanced parts, one per step, on {max(1, min(args.contexts, n_parts))} "
+                       f"contexts and streams so that consecutive parts overlap (song2_ctx_enqueue_part); "
+                       f"value = triplets / device time of all")
 
     # the rtol-1e-8 oracle check runs in a spawned CPU process during the GPU arms
     acc = None
@@ -571,8 +712,8 @@ def main():
         config["launch"] = {"warp_team": launch.warp_team, "teams_per_cta": launch.teams_per_cta,
                             "threads_per_team": launch.threads_per_team, "factors_in_smem": launch.lu_in_smem,
                             "autotune": f"song2_autotune on {args.autotune_sample} triplets ({tune_ms:.0f} ms)"}
-    # two contexts (separate scratch, separate streams): part q runs on context q % 2
-    n_ctx = 2 if n_parts >= 2 else 1
+    # several contexts (separate scratch, separate streams): part q runs on context q % n_ctx
+    n_ctx = max(1, min(args.contexts, n_parts))
     pp = min(args.plain_parts or max(1, args.steps // 4), max(1, n_parts - 2))
     ctxs = [ctx_create(lib, p, capi.SONG2_PREC_MIXED, launch) for _ in range(n_ctx)]
     try:
@@ -623,6 +764,13 @@ def main():
         plain = {"parts": pp, "ms": [ms_plain], "ms_mixed_same_parts": ms_mixed_same, "src": src_plain,
                  "st": st_plain, "ran": ran}
 
+    contract = None
+    if args.contract_parts > 0:
+        cp_parts = list(range(min(args.contract_parts, n_parts)))
+        contract = contract_leg(lib, p, launch, cp_parts, n_parts, min(n_ctx, len(cp_parts)) or 1,
+                                acc[1] if acc is not None else None, torch)
+        contract["parts"] = f"{len(cp_parts)} of {n_parts}"
+
     e2e = None
     if not args.no_e2e:
         te, h2d, d2h = run_e2e(lib, p, capi.SONG2_PREC_MIXED)
@@ -633,6 +781,13 @@ def main():
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "note": "whole workload through song2_gpu_evolve (one call: set-up, upload, evolve, download, "
                        "scatter into the nested host slabs)"}
+
+    los_line = None
+    if rank == 0 and world == 1 and not args.no_los:
+        try:
+            los_line = los_leg(lib, p, src_mixed, torch, args.los_reps, args.los_cpu_share)
+        except Exception as ex:  # noqa: BLE001
+            los_line = {"error": str(ex)[:300]}
 
     if rank != 0:
         if world > 1:
@@ -669,6 +824,7 @@ def main():
             "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "roofline_fp64": roofline_fp64,
             "e2e": e2e,
             "status_ok": bool(np.all(st_mixed["status"] == 0)),
+            "triplets_ok": bool(np.all(st_mixed["status"] == 0)),
             "counters": {"ndf_steps": steps_tot, "rhs": int(st_mixed["n_rhs"].sum()),
                          "jacobians": int(st_mixed["n_jac"].sum()), "factorisations": int(st_mixed["n_lu"].sum()),
                          "rejected": int(st_mixed["n_rejected"].sum())}}
@@ -684,6 +840,14 @@ def main():
         if n_pl:
             e, _ = source_error(p, src_mixed, plain["src"], plain["ran"], floor=1e-10)
             line["mixed_vs_plain_max_rel"] = e
+    if contract is not None:
+        line["contract"] = {"rtol": CONTRACT_RTOL, "value": world * contract["triplets"] / (contract["ms"] / 1e3),
+                            "unit": "triplets/s", "parts": contract["parts"], "triplets": contract["triplets"],
+                            "ms": contract["ms"], "status_ok": contract["status_ok"], "bound": ERR_BOUND,
+                            "note": "the mixed form at the rtol where every sampled source meets the bound "
+                                    "(same launch and overlap as the headline run)"}
+    if los_line is not None:
+        line["transfer2"] = los_line
     if rank == 0 and world == 1:
         # the CPU leg: the oracle timed on a bounded sample (after the accuracy worker)
         if acc is not None:
@@ -713,6 +877,11 @@ def main():
                            "class, then triplets spread over the cost-sorted order without its top tenth")
                 if not line["err_vs_fp64_oracle"]["within_bound"]:
                     line["status_ok"] = False
+                if contract is not None and contract["src"] is not None:
+                    e, w = source_error(p, contract["src"], ref, items)
+                    line["contract"]["err_vs_fp64_oracle"] = e
+                    line["contract"]["worst"] = {"source": list(tp[w[0]]), "triplet": list(work[w[1]])}
+                    line["contract"]["within_bound"] = bool(e <= ERR_BOUND)
             except (OSError, KeyError, ValueError) as ex:
                 line["err_vs_fp64_oracle"] = {"error": str(ex)[:200]}
         try:

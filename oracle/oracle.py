@@ -70,6 +70,9 @@ def load():
         lib.song2_oracle_los_tables.restype = C.c_int
         lib.song2_oracle_los_tables.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                                 C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_char_p]
+        lib.song2_oracle_transfer_pairs.restype = C.c_int
+        lib.song2_oracle_transfer_pairs.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_double),
+                                                    C.POINTER(C.c_double), C.c_int, C.c_int, C.c_int, C.c_char_p]
         lib.song2_oracle_transfer.restype = C.c_int
         lib.song2_oracle_transfer.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_double),
                                               C.POINTER(C.c_double), C.c_int, C.c_char_p]
@@ -124,14 +127,16 @@ def los_tables(prob, los):
     return l1, jt, J, xm
 
 
-def transfer(prob, los, sources, n_out, nthreads=0):
-    """Flat transfer functions [tt][units] of flat sources."""
+def transfer(prob, los, sources, n_out, nthreads=0, pairs=None):
+    """Flat transfer functions [tt][units] of flat sources (of the pairs
+    pairs = (lo, hi) only, the rest left zero, when given)."""
     from song_gb300 import capi
     out = np.zeros(n_out)
     err = capi.errbuf()
     src = np.ascontiguousarray(sources, dtype=np.float64)
-    if load().song2_oracle_transfer(C.byref(prob.spec), C.byref(los), capi.dptr(src), capi.dptr(out),
-                                    nthreads or (os.cpu_count() or 1), err):
+    lo, hi = pairs if pairs is not None else (0, 1 << 30)
+    if load().song2_oracle_transfer_pairs(C.byref(prob.spec), C.byref(los), capi.dptr(src), capi.dptr(out), lo, hi,
+                                          nthreads or (os.cpu_count() or 1), err):
         raise RuntimeError(err.value.decode())
     return out
 

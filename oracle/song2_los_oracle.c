@@ -283,7 +283,7 @@ typedef struct {
   int x_size;
   double *xx;
   int L_size, m_size, l_size, n_rows, n_l1;
-  int *l1, *l1_index, *jxmin;
+  int *l1, *l1_index, *jxmin, *jneg;
   double **j;       /* [n_l1][x_size - jxmin] */
   double *J;        /* [n_rows][x_size], zero below the row's x_min */
   double *ddJ;      /* cubic */
@@ -297,7 +297,9 @@ static int o_index_m_max(const song2_spec *s, int l) {
   return im;
 }
 
-/* bessel2_j_for_l1: x_min by bisection, then j_l1 on the x grid */
+/* bessel2_j_for_l1: x_min by bisection and the storage of j_l1 from there on
+   (the values themselves are filled x by x, one recurrence per x, in
+   o_fill_j) */
 static void o_j_for_l1(const song2_los_spec *los, o_tables *t, int r) {
   int l1 = t->l1[r];
   double x_min;
@@ -327,16 +329,31 @@ static void o_j_for_l1(const song2_los_spec *los, o_tables *t, int r) {
     t->jxmin[r] = t->x_size - 1;
     n = 1;
     t->j[r] = (double *)calloc(1, sizeof(double));
+    t->jneg[r] = 1;
     return;
   }
   n = t->x_size - t->jxmin[r];
   t->j[r] = (double *)malloc(sizeof(double) * n);
-  double *buf = (double *)malloc(sizeof(double) * (l1 + 1));
-  for (int i = 0; i < n; ++i) {
-    song2_oracle_bessel_all(t->xx[t->jxmin[r] + i], l1, buf);
-    t->j[r][i] = buf[l1];
+}
+
+static void o_fill_j(const song2_los_spec *los, o_tables *t) {
+  int lmax = t->l1[t->n_l1 - 1];
+#pragma omp parallel
+  {
+    double *buf = (double *)malloc(sizeof(double) * (lmax + 1));
+#pragma omp for schedule(dynamic, 16)
+    for (int i = 0; i < t->x_size; ++i) {
+      song2_oracle_bessel_all(t->xx[i], lmax, buf);
+      for (int r = 0; r < t->n_l1; ++r) {
+        int ij = i - t->jxmin[r];
+        if (ij < 0) continue;
+        if (t->jneg[r]) continue;  /* negligible everywhere: the single stored value stays zero */
+        t->j[r][ij] = buf[t->l1[r]];
+      }
+    }
+    free(buf);
   }
-  free(buf);
+  (void)los;
 }
 
 /* bessel2_J_Llm at one x index */
@@ -395,9 +412,11 @@ static int o_build_tables(const song2_spec *s, const song2_los_spec *los, o_tabl
     if (keep) t->l1[t->n_l1++] = l1;
   }
   t->jxmin = (int *)calloc(t->n_l1, sizeof(int));
+  t->jneg = (int *)calloc(t->n_l1, sizeof(int));
   t->j = (double **)calloc(t->n_l1, sizeof(double *));
 #pragma omp parallel for schedule(dynamic)
   for (int r = 0; r < t->n_l1; ++r) o_j_for_l1(los, t, r);
+  o_fill_j(los, t);
   /* projection rows */
   t->J = (double *)calloc((size_t)t->n_rows * t->x_size, sizeof(double));
   t->Jxmin = (int *)malloc(sizeof(int) * t->n_rows);
@@ -478,6 +497,7 @@ static void o_free_tables(o_tables *t) {
   free(t->l1);
   free(t->l1_index);
   free(t->jxmin);
+  free(t->jneg);
   free(t->J);
   free(t->ddJ);
   free(t->Jxmin);
@@ -524,8 +544,11 @@ static int o_lm(const song2_spec *s, int L, int im) {
   return n + im;
 }
 
-int song2_oracle_transfer(const song2_spec *s, const song2_los_spec *los, const double *sources, double *out,
-                          int nthreads, char *err) {
+/* Transfers of the pairs pair_lo <= p < pair_hi (pair order: k1 ascending,
+   k2 <= k1); the other pairs' entries of out are left untouched.  The tables
+   are built first (their time is not separable from the call). */
+int song2_oracle_transfer_pairs(const song2_spec *s, const song2_los_spec *los, const double *sources, double *out,
+                                int pair_lo, int pair_hi, int nthreads, char *err) {
   o_tables t;
   if (o_build_tables(s, los, &t, err)) return 1;
   int n_pairs = s->k_size * (s->k_size + 1) / 2;
@@ -596,7 +619,7 @@ int song2_oracle_transfer(const song2_spec *s, const song2_los_spec *los, const 
   double x_step = los->x_step;
   int L_T = s->l_max_los_t, L_P = s->l_max_los_p;
 #pragma omp parallel for schedule(dynamic) num_threads(nthreads > 0 ? nthreads : 1)
-  for (int p = 0; p < n_pairs; ++p) {
+  for (int p = pair_lo; p < (pair_hi < n_pairs ? pair_hi : n_pairs); ++p) {
     int kn = 0;
     {
       int q = 0;
@@ -799,4 +822,9 @@ int song2_oracle_transfer(const song2_spec *s, const song2_los_spec *los, const 
   free(u_off);
   o_free_tables(&t);
   return 0;
+}
+
+int song2_oracle_transfer(const song2_spec *s, const song2_los_spec *los, const double *sources, double *out,
+                          int nthreads, char *err) {
+  return song2_oracle_transfer_pairs(s, los, sources, out, 0, 1 << 30, nthreads, err);
 }

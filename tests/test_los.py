@@ -10,9 +10,11 @@ transfer functions against the oracle on seeded synthetic sources, for every
 sampling and interpolation option of the reference, and on sources from the
 evolver through the device pointer of a context.
 
-Tolerances: tables 1e-12 of the row's largest value (the two sides use
-different Bessel and 3j algorithms); transfers 1e-9 of the largest |T| of the
-transfer type over all k (different summation order of the same FP64 terms).
+Tolerances: j_l1 1e-12 of the row's largest value (the two sides use
+different Bessel recurrences); J_Llm 1e-10 of the row's largest value (the
+oracle's Racah 3j symbols from log-factorials carry about 1e-12 relative error
+at l ~ 300); transfers 1e-9 of the largest |T| of the transfer type over all k
+(different summation order of the same FP64 terms).
 """
 import ctypes as C
 
@@ -244,7 +246,7 @@ def test_device_tables_match_oracle(lib, lmax, kmax):
         a, b = J[r, xm[r]:], rJ[r, xm[r]:]
         s = np.max(np.abs(b))
         if s > 0:
-            assert np.max(np.abs(a - b)) <= 1e-12 * s, r
+            assert np.max(np.abs(a - b)) <= 1e-10 * s, r
 
 
 LOS_CASES = [
