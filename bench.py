@@ -68,6 +68,7 @@ ERR_BOUND = 1e-4
 # rtol-1e-8 oracle (the global error of an rtol-1e-4 integration, GPU or CPU,
 # is about 1.7e-3 on the squeezed triplets)
 CONTRACT_RTOL = 1e-6
+CONTRACT_PARTS = 20
 # line-of-sight leg: the l sampling of the reference's precision presets
 # (pre/*lmax2000.pre: l_max_scalars 2000, l_logstep 1.25, l_linstep 36)
 LOS_L = (2000, 1.25, 36)
@@ -100,7 +101,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--contexts", type=int, default=4, help="contexts (and streams) the parts alternate over")
     ap.add_argument("--contract-parts", type=int, default=2,
-                    help="parts timed at the contract rtol (0: skip the contract leg)")
+                    help="parts (of 20) timed at the contract rtol (0: skip the contract leg)")
     ap.add_argument("--no-los", action="store_true", help="skip the line-of-sight (transfer2) leg")
     ap.add_argument("--los-reps", type=int, default=3)
     ap.add_argument("--los-cpu-share", type=float, default=0.05,
@@ -766,10 +767,11 @@ def main():
 
     contract = None
     if args.contract_parts > 0:
-        cp_parts = list(range(min(args.contract_parts, n_parts)))
-        contract = contract_leg(lib, p, launch, cp_parts, n_parts, min(n_ctx, len(cp_parts)) or 1,
+        # its own partition into CONTRACT_PARTS parts, whatever --steps is
+        cp_parts = list(range(min(args.contract_parts, CONTRACT_PARTS)))
+        contract = contract_leg(lib, p, launch, cp_parts, CONTRACT_PARTS, len(cp_parts),
                                 acc[1] if acc is not None else None, torch)
-        contract["parts"] = f"{len(cp_parts)} of {n_parts}"
+        contract["parts"] = f"{len(cp_parts)} of {CONTRACT_PARTS}"
 
     e2e = None
     if not args.no_e2e:

@@ -333,6 +333,7 @@ __device__ int block_exclusive_scan(int v, int *sh_warp, int &excl) {
 
 struct GridPtrs {
   double *tau, *dtau, *aJ, *a, *b, *h;
+  double *wa, *wb;  // aJ dtau and (1 - aJ) dtau: the point's weights of J[ix] and J[ix+1]
   int *ix, *left;
 };
 
@@ -344,14 +345,17 @@ __device__ __forceinline__ GridPtrs grid_ptrs(double *base, int cap) {
   g.a = base + 3 * cap;
   g.b = base + 4 * cap;
   g.h = base + 5 * cap;
-  g.ix = reinterpret_cast<int *>(base + 6 * cap);
+  g.wa = base + 6 * cap;
+  g.wb = base + 7 * cap;
+  g.ix = reinterpret_cast<int *>(base + 8 * cap);
   g.left = g.ix + cap;
   return g;
 }
 
-__device__ __forceinline__ int grid_doubles(int cap) { return 7 * cap; }
+constexpr int GRID_DOUBLES_PER_POINT = 9;
+__host__ __device__ __forceinline__ int grid_doubles(int cap) { return GRID_DOUBLES_PER_POINT * cap; }
 
-__global__ void __launch_bounds__(LOS_THREADS) los_kernel(LosDev d, const double *__restrict__ S,
+__global__ void __launch_bounds__(LOS_THREADS, 3) los_kernel(LosDev d, const double *__restrict__ S,
                                                           double *__restrict__ T) {
   extern __shared__ double sm[];
   __shared__ long long s_unit;
@@ -456,7 +460,10 @@ __global__ void __launch_bounds__(LOS_THREADS) los_kernel(LosDev d, const double
       int ix = (int)(x / d.x_step);
       ix = max(0, min(ix, d.x_size - 2));  // in range by the host's check of k tau0 against x_max
       g.ix[i] = ix;
-      g.aJ[i] = (s2los_x_of(ix + 1, d.x_size, d.x_max) - x) / d.x_step;
+      const double aJ = (s2los_x_of(ix + 1, d.x_size, d.x_max) - x) / d.x_step;
+      g.aJ[i] = aJ;
+      g.wa[i] = aJ * dt;
+      g.wb[i] = (1 - aJ) * dt;
       if (d.tau_sampling != SONG2_TAU_SAMPLING_SOURCES) {
         int l = g.left[i];
         double h = d.tau[l + 1] - d.tau[l];
@@ -481,22 +488,21 @@ __global__ void __launch_bounds__(LOS_THREADS) los_kernel(LosDev d, const double
       const Term *tm = d.terms + (size_t)o * MAXTERM;
       const int nt = d.tt_nterm[o];
       double dir = 0.0, mix = 0.0;
+      // Per grid point the interpolated J of every term is aJ J[ix] + (1 - aJ) J[ix+1]
+      // (plus the spline terms in dd[ix], dd[ix+1] for cubic interpolation): the
+      // weights belong to the point, so each term adds J[ix] S and J[ix+1] S (and
+      // dd[ix] S, dd[ix+1] S) to running sums and the weights are applied once.
+      const double q6 = d.x_step * d.x_step / 6.0;
+      const bool has_mix = tm[nt > 0 ? nt - 1 : 0].mix && nt > 0;
+      double dir0 = 0.0, dir1 = 0.0, mix0 = 0.0, mix1 = 0.0;
       for (int i = lane; i < G; i += 32) {
         const int ix = g.ix[i];
-        const double aJ = g.aJ[i];
-        double sd = 0.0, sm_ = 0.0;
+        double d0 = 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0;  // direct terms
+        double m0 = 0.0, m1 = 0.0, m2 = 0.0, m3 = 0.0;  // mixing terms
         for (int c = 0; c < nt; ++c) {
           const Term t = tm[c];
           if (ix < t.xmin) continue;
           const double *Jr = d.J + (size_t)t.row * d.x_size + ix;
-          double Jv;
-          if (!d.bessel_cubic) {
-            Jv = aJ * __ldg(Jr) + (1 - aJ) * __ldg(Jr + 1);
-          } else {
-            const double *dd = d.ddJ + (size_t)t.row * d.x_size + ix;
-            Jv = (aJ * __ldg(Jr) + (1. - aJ) * (__ldg(Jr + 1) - aJ * ((aJ + 1.) * __ldg(dd) + (2. - aJ) * __ldg(dd + 1)) *
-                                                                   d.x_step * d.x_step / 6.0));
-          }
           const double *Sr = Srow + (size_t)t.tp * ts;
           double Sv;
           if (d.tau_sampling == SONG2_TAU_SAMPLING_SOURCES) {
@@ -511,12 +517,45 @@ __global__ void __launch_bounds__(LOS_THREADS) los_kernel(LosDev d, const double
               Sv += ((a * a * a - a) * Sd[l] + (b * b * b - b) * Sd[l + 1]) * h * h / 6.0;
             }
           }
-          if (t.mix) sm_ += Jv * Sv;
-          else sd += Jv * Sv;
+          const double J0 = __ldg(Jr), J1 = __ldg(Jr + 1);
+          double D0 = 0.0, D1 = 0.0;
+          if (d.bessel_cubic) {
+            const double *dd = d.ddJ + (size_t)t.row * d.x_size + ix;
+            D0 = __ldg(dd);
+            D1 = __ldg(dd + 1);
+          }
+          if (!t.mix) {
+            d0 = fma(J0, Sv, d0);
+            d1 = fma(J1, Sv, d1);
+            if (d.bessel_cubic) {
+              d2 = fma(D0, Sv, d2);
+              d3 = fma(D1, Sv, d3);
+            }
+          } else {
+            m0 = fma(J0, Sv, m0);
+            m1 = fma(J1, Sv, m1);
+            if (d.bessel_cubic) {
+              m2 = fma(D0, Sv, m2);
+              m3 = fma(D1, Sv, m3);
+            }
+          }
         }
-        dir += sd * g.dtau[i];
-        mix += sm_ * g.dtau[i];
+        const double wa = g.wa[i], wb = g.wb[i];
+        dir0 = fma(d0, wa, dir0);
+        dir1 = fma(d1, wb, dir1);
+        if (has_mix) {
+          mix0 = fma(m0, wa, mix0);
+          mix1 = fma(m1, wb, mix1);
+        }
+        if (d.bessel_cubic) {
+          const double aJ = g.aJ[i], bJ = 1 - aJ, dt = g.dtau[i];
+          const double c2 = -bJ * aJ * (aJ + 1.) * q6 * dt, c3 = -bJ * aJ * (2. - aJ) * q6 * dt;
+          dir = fma(c2, d2, fma(c3, d3, dir));
+          mix = fma(c2, m2, fma(c3, m3, mix));
+        }
       }
+      dir += dir0 + dir1;
+      mix += mix0 + mix1;
       dir = warp_sum(dir);
       mix = warp_sum(mix);
       if (lane == 0) {
@@ -991,7 +1030,7 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
   }
   size_t s_src = sizeof(double) * ((size_t)h->n_rows_src * s.tau_size * (d.time_cubic ? 2 : 1) +
                                     (d.time_cubic ? (size_t)LOS_WARPS * s.tau_size : 0));
-  size_t s_grid = sizeof(double) * (size_t)7 * cap;
+  size_t s_grid = sizeof(double) * (size_t)grid_doubles(cap);
   d.grid_in_smem = (cap <= GRID_SMEM_MAX) && (s_src + s_grid + 1024 <= smem_optin);
   h->smem = s_src + (d.grid_in_smem ? s_grid : 0);
   if (h->smem + 1024 > smem_optin) {
@@ -1007,7 +1046,7 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
   }
   h->grid = (int)std::min<long long>((long long)per_sm * n_sm, std::max<long long>(1, h->n_units));
   if (!d.grid_in_smem) {
-    if (dev_alloc(h, sizeof(double) * (size_t)7 * cap * h->grid, &tmp, err)) return fail();
+    if (dev_alloc(h, sizeof(double) * (size_t)grid_doubles(cap) * h->grid, &tmp, err)) return fail();
     d.grid_scratch = (double *)tmp;
   }
   if (d.k3_cubic) {
