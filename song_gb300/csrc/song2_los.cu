@@ -87,6 +87,8 @@ struct LosDev {
   const int *tt_l;
   const double *tt_msign;     // sign of the mixing contribution (-1 for E->B)
   const int *tt_nterm;
+  const int *tt_ndir;         // direct terms (they come first)
+  const int *tt_xmin;         // smallest x_min of the type's terms
   const Term *terms;          // [n_tt][MAXTERM]
   // sampling options
   int tau_sampling, time_cubic, k3_cubic, bessel_cubic;
@@ -333,7 +335,6 @@ __device__ int block_exclusive_scan(int v, int *sh_warp, int &excl) {
 
 struct GridPtrs {
   double *tau, *dtau, *aJ, *a, *b, *h;
-  double *wa, *wb;  // aJ dtau and (1 - aJ) dtau: the point's weights of J[ix] and J[ix+1]
   int *ix, *left;
 };
 
@@ -345,16 +346,18 @@ __device__ __forceinline__ GridPtrs grid_ptrs(double *base, int cap) {
   g.a = base + 3 * cap;
   g.b = base + 4 * cap;
   g.h = base + 5 * cap;
-  g.wa = base + 6 * cap;
-  g.wb = base + 7 * cap;
-  g.ix = reinterpret_cast<int *>(base + 8 * cap);
+  g.ix = reinterpret_cast<int *>(base + 6 * cap);
   g.left = g.ix + cap;
   return g;
 }
 
-constexpr int GRID_DOUBLES_PER_POINT = 9;
+constexpr int GRID_DOUBLES_PER_POINT = 7;
 __host__ __device__ __forceinline__ int grid_doubles(int cap) { return GRID_DOUBLES_PER_POINT * cap; }
 
+// INTERP_T: the integration grid is not the source sampling (time interpolation);
+// CUBIC_J: cubic interpolation of the projection functions.  Both are template
+// parameters so that the inner loop carries no runtime branch on them.
+template <bool INTERP_T, bool CUBIC_J>
 __global__ void __launch_bounds__(LOS_THREADS, 3) los_kernel(LosDev d, const double *__restrict__ S,
                                                           double *__restrict__ T) {
   extern __shared__ double sm[];
@@ -460,10 +463,7 @@ __global__ void __launch_bounds__(LOS_THREADS, 3) los_kernel(LosDev d, const dou
       int ix = (int)(x / d.x_step);
       ix = max(0, min(ix, d.x_size - 2));  // in range by the host's check of k tau0 against x_max
       g.ix[i] = ix;
-      const double aJ = (s2los_x_of(ix + 1, d.x_size, d.x_max) - x) / d.x_step;
-      g.aJ[i] = aJ;
-      g.wa[i] = aJ * dt;
-      g.wb[i] = (1 - aJ) * dt;
+      g.aJ[i] = (s2los_x_of(ix + 1, d.x_size, d.x_max) - x) / d.x_step;
       if (d.tau_sampling != SONG2_TAU_SAMPLING_SOURCES) {
         int l = g.left[i];
         double h = d.tau[l + 1] - d.tau[l];
@@ -483,79 +483,71 @@ __global__ void __launch_bounds__(LOS_THREADS, 3) los_kernel(LosDev d, const dou
       __syncthreads();
     }
 
-    // 3. the integrals, one warp per transfer type
+    // 3. the integrals, one warp per transfer type, its lanes over the grid
+    // points.  x = k (tau0 - tau) falls along the grid, so the points where any
+    // term of the type can be non-negligible (ix >= the smallest x_min of its
+    // terms) are a prefix of the grid, found by bisection; the rest add nothing.
     for (int o = warp; o < d.n_tt; o += LOS_WARPS) {
       const Term *tm = d.terms + (size_t)o * MAXTERM;
-      const int nt = d.tt_nterm[o];
+      const int nt = d.tt_nterm[o], nd = d.tt_ndir[o];
+      const int xlo = d.tt_xmin[o];
+      int P = 0;
+      if (nt > 0 && g.ix[0] >= xlo) {
+        int lo = 0, hi = G;  // g.ix[lo] >= xlo, and g.ix[hi] < xlo (hi == G: none)
+        while (hi - lo > 1) {
+          int mid = (lo + hi) >> 1;
+          if (g.ix[mid] >= xlo) lo = mid;
+          else hi = mid;
+        }
+        P = hi;
+      }
       double dir = 0.0, mix = 0.0;
-      // Per grid point the interpolated J of every term is aJ J[ix] + (1 - aJ) J[ix+1]
-      // (plus the spline terms in dd[ix], dd[ix+1] for cubic interpolation): the
-      // weights belong to the point, so each term adds J[ix] S and J[ix+1] S (and
-      // dd[ix] S, dd[ix+1] S) to running sums and the weights are applied once.
-      const double q6 = d.x_step * d.x_step / 6.0;
-      const bool has_mix = tm[nt > 0 ? nt - 1 : 0].mix && nt > 0;
-      double dir0 = 0.0, dir1 = 0.0, mix0 = 0.0, mix1 = 0.0;
-      for (int i = lane; i < G; i += 32) {
+      for (int i = lane; i < P; i += 32) {
         const int ix = g.ix[i];
-        double d0 = 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0;  // direct terms
-        double m0 = 0.0, m1 = 0.0, m2 = 0.0, m3 = 0.0;  // mixing terms
-        for (int c = 0; c < nt; ++c) {
-          const Term t = tm[c];
-          if (ix < t.xmin) continue;
+        const double aJ = g.aJ[i], bJ = 1 - aJ;
+        int l = 0;
+        double ta = 0.0, tb = 0.0, th = 0.0;
+        if constexpr (INTERP_T) {
+          l = g.left[i];
+          ta = g.a[i];
+          tb = g.b[i];
+          th = g.h[i];
+        }
+        auto term = [&](const Term &t) -> double {
           const double *Jr = d.J + (size_t)t.row * d.x_size + ix;
+          double Jv;
+          if constexpr (!CUBIC_J) {
+            Jv = aJ * __ldg(Jr) + bJ * __ldg(Jr + 1);
+          } else {
+            const double *dd = d.ddJ + (size_t)t.row * d.x_size + ix;
+            Jv = (aJ * __ldg(Jr) + bJ * (__ldg(Jr + 1) - aJ * ((aJ + 1.) * __ldg(dd) + (2. - aJ) * __ldg(dd + 1)) *
+                                                            d.x_step * d.x_step / 6.0));
+          }
           const double *Sr = Srow + (size_t)t.tp * ts;
           double Sv;
-          if (d.tau_sampling == SONG2_TAU_SAMPLING_SOURCES) {
+          if constexpr (!INTERP_T) {
             Sv = Sr[i];
           } else {
-            int l = g.left[i];
-            double a = g.a[i], b = g.b[i];
-            Sv = a * Sr[l] + b * Sr[l + 1];
+            Sv = ta * Sr[l] + tb * Sr[l + 1];
             if (tcub) {
               const double *Sd = Sdd + (size_t)t.tp * ts;
-              double h = g.h[i];
-              Sv += ((a * a * a - a) * Sd[l] + (b * b * b - b) * Sd[l + 1]) * h * h / 6.0;
+              Sv += ((ta * ta * ta - ta) * Sd[l] + (tb * tb * tb - tb) * Sd[l + 1]) * th * th / 6.0;
             }
           }
-          const double J0 = __ldg(Jr), J1 = __ldg(Jr + 1);
-          double D0 = 0.0, D1 = 0.0;
-          if (d.bessel_cubic) {
-            const double *dd = d.ddJ + (size_t)t.row * d.x_size + ix;
-            D0 = __ldg(dd);
-            D1 = __ldg(dd + 1);
-          }
-          if (!t.mix) {
-            d0 = fma(J0, Sv, d0);
-            d1 = fma(J1, Sv, d1);
-            if (d.bessel_cubic) {
-              d2 = fma(D0, Sv, d2);
-              d3 = fma(D1, Sv, d3);
-            }
-          } else {
-            m0 = fma(J0, Sv, m0);
-            m1 = fma(J1, Sv, m1);
-            if (d.bessel_cubic) {
-              m2 = fma(D0, Sv, m2);
-              m3 = fma(D1, Sv, m3);
-            }
-          }
+          return Jv * Sv;
+        };
+        double sd = 0.0, sx = 0.0;
+        for (int c = 0; c < nd; ++c) {
+          const Term t = tm[c];
+          if (ix >= t.xmin) sd += term(t);
         }
-        const double wa = g.wa[i], wb = g.wb[i];
-        dir0 = fma(d0, wa, dir0);
-        dir1 = fma(d1, wb, dir1);
-        if (has_mix) {
-          mix0 = fma(m0, wa, mix0);
-          mix1 = fma(m1, wb, mix1);
+        for (int c = nd; c < nt; ++c) {
+          const Term t = tm[c];
+          if (ix >= t.xmin) sx += term(t);
         }
-        if (d.bessel_cubic) {
-          const double aJ = g.aJ[i], bJ = 1 - aJ, dt = g.dtau[i];
-          const double c2 = -bJ * aJ * (aJ + 1.) * q6 * dt, c3 = -bJ * aJ * (2. - aJ) * q6 * dt;
-          dir = fma(c2, d2, fma(c3, d3, dir));
-          mix = fma(c2, m2, fma(c3, m3, mix));
-        }
+        dir += sd * g.dtau[i];
+        mix += sx * g.dtau[i];
       }
-      dir += dir0 + dir1;
-      mix += mix0 + mix1;
       dir = warp_sum(dir);
       mix = warp_sum(mix);
       if (lane == 0) {
@@ -570,6 +562,13 @@ __global__ void __launch_bounds__(LOS_THREADS, 3) los_kernel(LosDev d, const dou
     }
     __syncthreads();
   }
+}
+
+typedef void (*LosKernel)(LosDev, const double *, double *);
+
+LosKernel los_kernel_for(bool interp_t, bool cubic_j) {
+  if (interp_t) return cubic_j ? los_kernel<true, true> : los_kernel<true, false>;
+  return cubic_j ? los_kernel<false, true> : los_kernel<false, false>;
 }
 
 }  // namespace
@@ -593,7 +592,7 @@ struct song2_los {
   int grid = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   float last_ms = 0.f, tables_ms = 0.f;
-  int sources_cubic_ready = 0;
+  LosKernel kernel = nullptr;
 };
 
 template <class T>
@@ -791,6 +790,7 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
   h->n_tt = song2_transfer_types(&h->spec, &h->los, nullptr, nullptr, nullptr);
   std::vector<int> tt_type(h->n_tt), tt_l(h->n_tt), tt_m(h->n_tt), tt_nterm(h->n_tt, 0);
   std::vector<double> tt_msign(h->n_tt, 1.0);
+  std::vector<int> tt_ndir(h->n_tt, 0);
   song2_transfer_types(&h->spec, &h->los, tt_type.data(), tt_l.data(), tt_m.data());
   std::vector<Term> terms((size_t)h->n_tt * MAXTERM);
   for (int o = 0; o < h->n_tt; ++o) {
@@ -828,6 +828,7 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
         t.xmin = 0;  // filled from the device x_min table below
         t.mix = Mx[q];
         if (Mx[q]) tt_msign[o] = Sg[q];
+        else tt_ndir[o]++;
       }
     tt_nterm[o] = n;
   }
@@ -932,11 +933,24 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
   // x_min of each term
   std::vector<int> Jxmin(h->n_rows);
   CKL(cudaMemcpy(Jxmin.data(), h->d_Jxmin, sizeof(int) * h->n_rows, cudaMemcpyDeviceToHost));
-  for (int o = 0; o < h->n_tt; ++o)
+  // drop the terms whose projection row is negligible at every x (x index
+  // x_size - 1 is never reached), keeping the direct terms first, and record
+  // each type's smallest x_min
+  std::vector<int> tt_xmin(h->n_tt, h->x_size);
+  for (int o = 0; o < h->n_tt; ++o) {
+    Term *to = terms.data() + (size_t)o * MAXTERM;
+    int n = 0, nd = 0;
     for (int c = 0; c < tt_nterm[o]; ++c) {
-      Term &t = terms[(size_t)o * MAXTERM + c];
+      Term t = to[c];
       t.xmin = Jxmin[t.row];
+      if (t.xmin >= h->x_size - 1) continue;
+      if (!t.mix) ++nd;
+      to[n++] = t;
+      tt_xmin[o] = std::min(tt_xmin[o], t.xmin);
     }
+    tt_nterm[o] = n;
+    tt_ndir[o] = nd;
+  }
 
   // ---- every x = k (tau0 - tau) inside the projection tables
   {
@@ -982,6 +996,7 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
   const double *p_tau, *p_k3, *p_unit_k, *p_unit_b;
   const int *p_k3off, *p_k3n, *p_unit_pair, *p_unit_left, *p_src_tp, *p_tt_l, *p_tt_nterm;
   const double *p_tt_msign;
+  const int *p_tt_ndir, *p_tt_xmin;
   const long long *p_src_off;
   const Term *p_terms;
   if (dev_upload(h, h->tau, &p_tau, err) || dev_upload(h, h->k3, &p_k3, err) || dev_upload(h, k3off, &p_k3off, err) ||
@@ -990,7 +1005,8 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
       dev_upload(h, unit_pair, &p_unit_pair, err) || dev_upload(h, unit_left, &p_unit_left, err) ||
       dev_upload(h, src_tp, &p_src_tp, err) || dev_upload(h, tt_l, &p_tt_l, err) ||
       dev_upload(h, tt_nterm, &p_tt_nterm, err) || dev_upload(h, terms, &p_terms, err) ||
-      dev_upload(h, tt_msign, &p_tt_msign, err))
+      dev_upload(h, tt_msign, &p_tt_msign, err) || dev_upload(h, tt_ndir, &p_tt_ndir, err) ||
+      dev_upload(h, tt_xmin, &p_tt_xmin, err))
     return fail();
   d.tau = p_tau;
   d.k3 = p_k3;
@@ -1008,6 +1024,8 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
   d.n_tt = h->n_tt;
   d.tt_l = p_tt_l;
   d.tt_msign = p_tt_msign;
+  d.tt_ndir = p_tt_ndir;
+  d.tt_xmin = p_tt_xmin;
   d.tt_nterm = p_tt_nterm;
   d.terms = p_terms;
   d.tau_sampling = h->los.tau_sampling;
@@ -1037,9 +1055,10 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
     snprintf(err, SONG2_ERRLEN, "source rows of one k (%zu bytes) exceed shared memory", s_src);
     return fail();
   }
-  CKL(cudaFuncSetAttribute(los_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
+  h->kernel = los_kernel_for(d.tau_sampling != SONG2_TAU_SAMPLING_SOURCES, d.bessel_cubic);
+  CKL(cudaFuncSetAttribute(h->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
   int per_sm = 0;
-  CKL(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, los_kernel, LOS_THREADS, h->smem));
+  CKL(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->kernel, LOS_THREADS, h->smem));
   if (per_sm < 1) {
     snprintf(err, SONG2_ERRLEN, "line-of-sight kernel does not fit on an SM");
     return fail();
@@ -1084,7 +1103,7 @@ extern "C" int song2_los_run(song2_los *h, const double *sources_dev, double *tr
                                                                  h->dev.k3_n, h->dev.src_off, h->per_type,
                                                                  sources_dev, h->d_ddk, h->d_status);
   }
-  los_kernel<<<h->grid, LOS_THREADS, h->smem, st>>>(h->dev, sources_dev, transfer_dev);
+  h->kernel<<<h->grid, LOS_THREADS, h->smem, st>>>(h->dev, sources_dev, transfer_dev);
   CKL(cudaGetLastError());
   CKL(cudaEventRecord(h->e1, st));
   CKL(cudaEventSynchronize(h->e1));
