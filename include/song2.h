@@ -501,6 +501,40 @@ typedef struct {
   double tau_rec;                   /* visibility peak (pth->tau_rec), song2_recombination_time() */
 } song2_los_spec;
 
+/* ------------------------------------------------ parameter files */
+/* The reference's ini/pre files (input2.c) read for the keys of the hot path. */
+enum song2_sampling { SONG2_SAMPLING_LIN = 0, SONG2_SAMPLING_LOG = 1, SONG2_SAMPLING_SMART = 2,
+                      SONG2_SAMPLING_SYM = 3, SONG2_SAMPLING_THETA12 = 4 };
+/* Grid settings of a parameter file (defaults of input2.c:2071-2075, 2316-2325). */
+typedef struct {
+  int k_sampling;            /* sources2_k_sampling (default smart) */
+  double k_min, k_max;       /* k_min_custom_song, k_max_custom_song (lin/log) */
+  int k_size;                /* k_size_custom_song */
+  int k3_sampling;           /* sources2_k3_sampling (default smart) */
+  int k3_size;               /* k3_size (lin/log) */
+  int custom_tau;            /* custom_time_sampling_song_sources */
+  int tau_sampling;          /* custom_tau_mode_song_sources: SONG2_SAMPLING_LIN / _LOG */
+  double tau_ini, tau_end;   /* custom_tau_ini/end_song_sources (tau_end 0: today) */
+  int tau_size;              /* custom_tau_size_song_sources */
+  int l_max_scalars;         /* CLASS l sampling: l_max_scalars, l_logstep, l_linstep */
+  double l_logstep;
+  int l_linstep;
+} song2_params;
+void song2_params_defaults(song2_params *grids);
+/* Reads an ini and a pre file (either may be NULL; a name may appear once in
+   the two) into spec (starting from song2_spec_defaults with the reference's
+   default radiation-streaming approximation, rsa2_MD), the grid settings and,
+   when los is not NULL, the line-of-sight settings (its l list, tau0 and
+   tau_rec are kept).  Names and their obsolete aliases, the yes/no rules and
+   the output string follow input2.c:137-2016 and perturb2_indices_of_perturbs
+   (perturbations2.c:843-945).  Settings the evolver does not implement
+   (imperfect fluids, perturbed recombination, other phi equations) are errors.
+   The smart, sym and theta_12 samplings are reported in grids; building their
+   grids is the caller's (the drop-in takes ppt2->k and ppt2->k3 as they are).
+   Not reentrant. */
+int song2_read_params(const char *ini_path, const char *pre_path, song2_spec *spec, song2_params *grids,
+                      song2_los_spec *los, char *err);
+
 /* Defaults of the reference (input2.c) for the spec's k range and tables:
    x_max = k_max * 18000 for the lin/log k samplings (input2.c:1986-1989), plus
    one step, times 1.05; tau0 and tau_rec from the tables.  l and l_size are left

@@ -116,6 +116,17 @@ INTERP_LINEAR, INTERP_CUBIC = 0, 1
 K3_EXTRAP_NONE, K3_EXTRAP_FLAT = 0, 1
 
 
+class Params(C.Structure):
+    """song2_params: the grid settings of a parameter file."""
+    _fields_ = [("k_sampling", C.c_int), ("k_min", C.c_double), ("k_max", C.c_double), ("k_size", C.c_int),
+                ("k3_sampling", C.c_int), ("k3_size", C.c_int), ("custom_tau", C.c_int), ("tau_sampling", C.c_int),
+                ("tau_ini", C.c_double), ("tau_end", C.c_double), ("tau_size", C.c_int),
+                ("l_max_scalars", C.c_int), ("l_logstep", C.c_double), ("l_linstep", C.c_int)]
+
+
+SAMPLING_LIN, SAMPLING_LOG, SAMPLING_SMART, SAMPLING_SYM, SAMPLING_THETA12 = 0, 1, 2, 3, 4
+
+
 class Launch(C.Structure):
     _fields_ = [("warp_team", C.c_int), ("teams_per_cta", C.c_int), ("threads_per_team", C.c_int),
                 ("lu_in_smem", C.c_int)]
@@ -189,6 +200,9 @@ SIGNATURES = {
                                       C.c_char_p]),
     "song2_gpu_first_order": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _D, _D, _PD, C.c_char_p]),
     "song2_los_defaults": (None, [C.POINTER(LosSpec), C.POINTER(Spec), C.POINTER(Tables)]),
+    "song2_params_defaults": (None, [C.POINTER(Params)]),
+    "song2_read_params": (_I, [C.c_char_p, C.c_char_p, C.POINTER(Spec), C.POINTER(Params), C.POINTER(LosSpec),
+                               C.c_char_p]),
     "song2_l_list": (_I, [_I, _D, _I, _PI]),
     "song2_recombination_time": (_D, [C.POINTER(Tables)]),
     "song2_transfer_types": (_I, [C.POINTER(Spec), C.POINTER(LosSpec), _PI, _PI, _PI]),

@@ -1,0 +1,421 @@
+/* song2_params.c - reader of the reference's ini/pre parameter files for the
+ * keys of the hot path: the problem (song2_spec), its grids and the
+ * line-of-sight settings (input2.c:137-2016 parses them into ppt2/ppr2/ptr2/pbs2).
+ *
+ * File format (CLASS's parser): one `name = value` per line, '#' starts a
+ * comment, blank lines and lines without '=' are ignored, names and values are
+ * trimmed; the ini and pre files form one list and a name may appear only once.
+ */
+#include <ctype.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "song2.h"
+
+#define P_MAXN 512
+#define P_KEY 128
+#define P_VAL 512
+
+typedef struct {
+  int n;
+  char key[P_MAXN][P_KEY];
+  char val[P_MAXN][P_VAL];
+  char src[P_MAXN][16];
+} plist;
+
+static char *trim(char *s) {
+  while (*s && isspace((unsigned char)*s)) ++s;
+  char *e = s + strlen(s);
+  while (e > s && isspace((unsigned char)e[-1])) *--e = 0;
+  return s;
+}
+
+static int read_file(const char *path, const char *tag, plist *pl, char *err) {
+  if (!path) return 0;
+  FILE *f = fopen(path, "r");
+  if (!f) {
+    snprintf(err, SONG2_ERRLEN, "cannot open %.900s", path);
+    return 1;
+  }
+  char line[2048];
+  int ln = 0;
+  while (fgets(line, sizeof line, f)) {
+    ++ln;
+    char *h = strchr(line, '#');
+    if (h) *h = 0;
+    char *eq = strchr(line, '=');
+    if (!eq) continue;
+    *eq = 0;
+    char *k = trim(line), *v = trim(eq + 1);
+    if (!*k) continue;
+    for (int i = 0; i < pl->n; ++i)
+      if (!strcmp(pl->key[i], k)) {
+        snprintf(err, SONG2_ERRLEN, "multiple entries of '%.100s' (%s and %s:%d)", k, pl->src[i], tag, ln);
+        fclose(f);
+        return 1;
+      }
+    if (pl->n >= P_MAXN || strlen(k) >= P_KEY || strlen(v) >= P_VAL) {
+      snprintf(err, SONG2_ERRLEN, "parameter list too long at %s:%d", tag, ln);
+      fclose(f);
+      return 1;
+    }
+    strcpy(pl->key[pl->n], k);
+    strcpy(pl->val[pl->n], v);
+    snprintf(pl->src[pl->n], sizeof pl->src[0], "%s:%d", tag, ln);
+    pl->n++;
+  }
+  fclose(f);
+  return 0;
+}
+
+static const char *get(const plist *pl, const char *k) {
+  for (int i = 0; i < pl->n; ++i)
+    if (!strcmp(pl->key[i], k)) return pl->val[i];
+  return NULL;
+}
+
+/* the newer name wins over its obsolete alias (input2.c reads the alias first) */
+static const char *get2(const plist *pl, const char *old_name, const char *new_name) {
+  const char *v = get(pl, new_name);
+  return v ? v : get(pl, old_name);
+}
+
+static int yes(const char *v) { return v && (strchr(v, 'y') || strchr(v, 'Y')); }
+
+static int num(const char *v, const char *k, double *out, char *err) {
+  char *end;
+  double d = strtod(v, &end);
+  if (end == v || *trim(end)) {
+    snprintf(err, SONG2_ERRLEN, "'%s = %.200s' is not a number", k, v);
+    return 1;
+  }
+  *out = d;
+  return 0;
+}
+
+#define RD_D(name, dst)                                  \
+  do {                                                   \
+    const char *v_ = get(pl, name);                      \
+    if (v_ && num(v_, name, &(dst), err)) return 1;      \
+  } while (0)
+#define RD_D2(old, name, dst)                            \
+  do {                                                   \
+    const char *v_ = get2(pl, old, name);                \
+    if (v_ && num(v_, name, &(dst), err)) return 1;      \
+  } while (0)
+#define RD_I2(old, name, dst)                            \
+  do {                                                   \
+    const char *v_ = get2(pl, old, name);                \
+    double d_;                                           \
+    if (v_) {                                            \
+      if (num(v_, name, &d_, err)) return 1;             \
+      (dst) = (int)d_;                                   \
+    }                                                    \
+  } while (0)
+
+void song2_params_defaults(song2_params *g) {
+  memset(g, 0, sizeof(*g));
+  /* input2.c:2071-2075, 2316-2325: smart samplings, custom grids as below */
+  g->k_sampling = SONG2_SAMPLING_SMART;
+  g->k_min = 1e-4;
+  g->k_max = 0.1;
+  g->k_size = 10;
+  g->k3_sampling = SONG2_SAMPLING_SMART;
+  g->k3_size = 100;
+  g->custom_tau = 0;
+  g->tau_sampling = SONG2_SAMPLING_LIN;
+  g->tau_ini = 1;
+  g->tau_end = 0;
+  g->tau_size = 2000;
+  /* CLASS's l sampling of the Bessel module */
+  g->l_max_scalars = 2500;
+  g->l_logstep = 1.12;
+  g->l_linstep = 40;
+}
+
+static int sampling(const char *v, const char *k, int *out, char *err) {
+  if (!strcmp(v, "lin") || !strcmp(v, "linear")) *out = SONG2_SAMPLING_LIN;
+  else if (!strcmp(v, "log") || !strcmp(v, "logarithmic")) *out = SONG2_SAMPLING_LOG;
+  else if (!strcmp(v, "smart") || !strcmp(v, "class")) *out = SONG2_SAMPLING_SMART;
+  else if (!strcmp(v, "sym") || !strcmp(v, "symmetric")) *out = SONG2_SAMPLING_SYM;
+  else if (!strcmp(v, "theta_12")) *out = SONG2_SAMPLING_THETA12;
+  else {
+    snprintf(err, SONG2_ERRLEN, "%s = %.200s is not a sampling the reference knows", k, v);
+    return 1;
+  }
+  return 0;
+}
+
+int song2_read_params(const char *ini_path, const char *pre_path, song2_spec *s, song2_params *g,
+                      song2_los_spec *los, char *err) {
+  static plist list;  /* large; the reader is not reentrant */
+  plist *pl = &list;
+  pl->n = 0;
+  if (read_file(ini_path, "ini", pl, err) || read_file(pre_path, "pre", pl, err)) return 1;
+  song2_spec_defaults(s);
+  s->radiation_streaming_approximation = SONG2_RSA_MD; /* the reference's default (input2.c:2139) */
+  song2_params_defaults(g);
+
+  /* output: which line-of-sight sources (input2.c:209-277, perturbations2.c:843-945) */
+  int has_t = 0, has_e = 0, has_b = 0, has_cdm = 0, stop_p2 = 0, stop_t2 = 0;
+  const char *v = get(pl, "output");
+  if (v) {
+    if (strstr(v, "tBisp") || strstr(v, "TBISP") || strstr(v, "tCl2") || strstr(v, "TCL2")) has_t = 1;
+    if (strstr(v, "pBisp") || strstr(v, "PBISP") || strstr(v, "eBisp") || strstr(v, "EBISP") || strstr(v, "pCl2") ||
+        strstr(v, "PCL2") || strstr(v, "eCl2") || strstr(v, "ECL2"))
+      has_e = 1;
+    if (strstr(v, "bBisp") || strstr(v, "BBISP") || strstr(v, "bCl2") || strstr(v, "BCL2")) has_b = 1;
+    if (strstr(v, "delta_cdm_pk") || strstr(v, "pk_delta_cdm") || strstr(v, "mPk") || strstr(v, "delta_cdm_bk") ||
+        strstr(v, "bk_delta_cdm") || strstr(v, "mBisp"))
+      has_cdm = 1;
+    if (strstr(v, "stop_at_perturbations2") || strstr(v, "P2")) stop_p2 = 1;
+    if (strstr(v, "stop_at_transfers2") || strstr(v, "T2")) stop_t2 = 1;
+  }
+
+  /* physics switches (input2.c:534-760) */
+  if ((v = get(pl, "quadratic_sources")) && !yes(v)) s->has_quadratic_sources = 0;
+  if ((v = get(pl, "quadratic_liouville")) && !yes(v)) s->has_quadratic_liouville = 0;
+  if ((v = get(pl, "quadratic_collision")) && !yes(v)) s->has_quadratic_collision = 0;
+  if (!s->has_quadratic_sources) s->has_quadratic_liouville = s->has_quadratic_collision = 0;
+  if ((v = get(pl, "polarization_second_order")) && !yes(v)) s->has_polarization2 = 0;
+  if ((v = get(pl, "perfect_baryons")) && !yes(v)) {
+    snprintf(err, SONG2_ERRLEN, "perfect_baryons = no (imperfect baryons) is not supported");
+    return 1;
+  }
+  if ((v = get(pl, "perfect_cdm")) && !yes(v)) {
+    snprintf(err, SONG2_ERRLEN, "perfect_cdm = no (imperfect CDM) is not supported");
+    return 1;
+  }
+  RD_D2("tol_perturb_integration_2nd_order", "tol_perturb_integration_song", s->rtol);
+  if ((v = get(pl, "perturbed_recombination_song")) && yes(v)) {
+    snprintf(err, SONG2_ERRLEN, "perturbed_recombination_song = yes is not supported");
+    return 1;
+  }
+  s->has_pure_scattering_in_los = yes(get2(pl, "include_pure_scattering_in_los_2nd_order", "include_pure_scattering_song"));
+  s->has_quad_scattering_in_los = yes(get2(pl, "include_quad_scattering_in_los_2nd_order", "include_quad_scattering_song"));
+  {
+    const char *m1 = get(pl, "include_metric_in_los_2nd_order"), *m2 = get(pl, "include_metric_song"),
+               *m3 = get(pl, "include_pure_metric_song");
+    s->has_pure_metric_in_los = yes(m3 ? m3 : (m2 ? m2 : m1));
+  }
+  s->has_quad_metric_in_los = yes(get2(pl, "include_quad_metric_in_los_2nd_order", "include_quad_metric_song"));
+  s->has_time_delay_in_los = yes(get2(pl, "include_time_delay_in_los_2nd_order", "include_time_delay_song"));
+  s->has_redshift_in_los = yes(get2(pl, "include_redshift_in_los_2nd_order", "include_redshift_song"));
+  s->has_lensing_in_los = yes(get2(pl, "include_lensing_in_los_2nd_order", "include_lensing_song"));
+  s->has_sw = yes(get2(pl, "include_sachs_wolfe_in_los_2nd_order", "include_sachs_wolfe_song"));
+  s->has_isw = yes(get2(pl, "include_integrated_sachs_wolfe_in_los_2nd_order", "include_integrated_sachs_wolfe_song"));
+  if (s->has_sw || s->has_isw) s->has_pure_metric_in_los = 0;
+  s->use_delta_tilde_in_los = yes(get(pl, "use_delta_tilde_in_los"));
+  s->use_exponential_potentials = yes(get(pl, "use_exponential_potentials"));
+  if (s->has_isw && yes(get(pl, "only_early_isw"))) {
+    snprintf(err, SONG2_ERRLEN, "only_early_isw = yes is not supported");
+    return 1;
+  }
+  if (s->use_delta_tilde_in_los && s->has_redshift_in_los) {
+    snprintf(err, SONG2_ERRLEN, "the delta_tilde options are not compatible with the redshift term");
+    return 1;
+  }
+  if ((v = get2(pl, "phi_prime_equation", "phi_equation_song")) && !strstr(v, "huang")) {
+    snprintf(err, SONG2_ERRLEN, "phi_equation_song = %.200s: only the Huang equation is supported", v);
+    return 1;
+  }
+  if ((v = get2(pl, "ic_2nd_order", "ic_song"))) {
+    if (!strcmp(v, "ad") || !strcmp(v, "AD")) s->ic = SONG2_IC_AD;
+    else if (strstr(v, "ad_first_order") || strstr(v, "AD_1ST") || strstr(v, "ad1")) s->ic = SONG2_IC_AD_FIRST_ORDER;
+    else if (strstr(v, "zero") || strstr(v, "ZERO")) s->ic = SONG2_IC_ZERO;
+    else {
+      snprintf(err, SONG2_ERRLEN, "ic_song = %.200s not supported (ad, ad_first_order, zero)", v);
+      return 1;
+    }
+  }
+  RD_D("primordial_local_fnl_phi", s->primordial_local_fnl_phi);
+  RD_I2("tight_coupling_approximation_2nd_order", "tight_coupling_approximation_song", s->tight_coupling);
+  RD_D2("tight_coupling_trigger_tau_c_over_tau_h_2nd_order", "tight_coupling_trigger_tau_c_over_tau_h_song",
+        s->tca_trigger_tau_c_over_tau_h);
+  RD_D2("tight_coupling_trigger_tau_c_over_tau_k_2nd_order", "tight_coupling_trigger_tau_c_over_tau_k_song",
+        s->tca_trigger_tau_c_over_tau_k);
+  RD_I2("radiation_streaming_approximation_2nd_order", "radiation_streaming_approximation_song",
+        s->radiation_streaming_approximation);
+  RD_D2("radiation_streaming_trigger_tau_over_tau_k_2nd_order", "radiation_streaming_trigger_tau_over_tau_k_song",
+        s->radiation_streaming_trigger_tau_over_tau_k);
+  if (s->tight_coupling < 0 || s->tight_coupling > 1 || s->radiation_streaming_approximation < 0 ||
+      s->radiation_streaming_approximation > 2) {
+    snprintf(err, SONG2_ERRLEN, "unknown tight-coupling (%d) or radiation-streaming (%d) method", s->tight_coupling,
+             s->radiation_streaming_approximation);
+    return 1;
+  }
+  RD_D2("start_small_k_at_tau_c_over_tau_h_2nd_order", "start_small_k_at_tau_c_over_tau_h_song",
+        s->start_small_k_at_tau_c_over_tau_h);
+  RD_D2("start_large_k_at_tau_h_over_tau_k_2nd_order", "start_large_k_at_tau_h_over_tau_k_song",
+        s->start_large_k_at_tau_h_over_tau_k);
+
+  /* hierarchies and line of sight (input2.c:1748-1880) */
+  RD_I2("l_max_g_2nd_order", "l_max_g_song", s->l_max_g);
+  RD_I2("l_max_pol_g_2nd_order", "l_max_pol_g_song", s->l_max_pol_g);
+  RD_I2("l_max_ur_2nd_order", "l_max_ur_song", s->l_max_ur);
+  {
+    const char *vt = get2(pl, "l_max_T_los", "l_max_los_t");
+    const char *vp = get(pl, "l_max_los_p");
+    if (!vp) vp = get(pl, "l_max_B_los");
+    if (!vp) vp = get(pl, "l_max_E_los");
+    double d;
+    if (vt) {
+      if (num(vt, "l_max_los_t", &d, err)) return 1;
+      s->l_max_los_t = (int)d;
+    }
+    if (vp) {
+      if (num(vp, "l_max_los_p", &d, err)) return 1;
+      s->l_max_los_p = (int)d;
+    }
+    vt = get2(pl, "l_max_T_quadratic_los", "l_max_los_quadratic_t");
+    vp = get(pl, "l_max_los_quadratic_p");
+    if (!vp) vp = get(pl, "l_max_B_quadratic_los");
+    if (!vp) vp = get(pl, "l_max_E_quadratic_los");
+    if (vt) {
+      if (num(vt, "l_max_los_quadratic_t", &d, err)) return 1;
+      s->l_max_los_quadratic_t = (int)d;
+    }
+    if (vp) {
+      if (num(vp, "l_max_los_quadratic_p", &d, err)) return 1;
+      s->l_max_los_quadratic_p = (int)d;
+    }
+  }
+  if ((v = get2(pl, "modes_2nd_order", "modes_song"))) {
+    char buf[P_VAL];
+    strcpy(buf, v);
+    int n = 0;
+    for (char *tok = strtok(buf, ","); tok; tok = strtok(NULL, ",")) {
+      double d;
+      if (num(trim(tok), "modes_song", &d, err)) return 1;
+      if (n >= SONG2_MAX_M) {
+        snprintf(err, SONG2_ERRLEN, "modes_song holds more than %d values", SONG2_MAX_M);
+        return 1;
+      }
+      s->m[n++] = (int)d;
+    }
+    s->m_size = n;
+    for (int i = 0; i + 1 < n; ++i)
+      if (s->m[i] >= s->m[i + 1]) {
+        snprintf(err, SONG2_ERRLEN, "the m-list provided in modes_song is not strictly ascending");
+        return 1;
+      }
+    if (n < 1 || s->m[0] < 0 || s->m[n - 1] >= SONG2_MAX_M) {
+      snprintf(err, SONG2_ERRLEN, "modes_song must hold values in 0..%d", SONG2_MAX_M - 1);
+      return 1;
+    }
+  }
+  int m_max = s->m[s->m_size - 1];
+  s->has_source_T = has_t;
+  s->has_source_E = has_e || has_b;
+  s->has_source_B = (has_e || has_b) && m_max != 0;
+  s->has_source_delta_cdm = has_cdm;
+  if (!s->has_polarization2 && (has_e || has_b)) {
+    snprintf(err, SONG2_ERRLEN, "polarization_second_order must be yes for E or B outputs");
+    return 1;
+  }
+  /* rescaling of the CMB sources (input2.c:1955-1971) */
+  s->rescale_cmb_sources = !(stop_p2 || stop_t2) && m_max != 0;
+
+  /* grids (input2.c:320-530) */
+  if ((v = get(pl, "sources2_k_sampling")) && sampling(v, "sources2_k_sampling", &g->k_sampling, err)) return 1;
+  RD_D2("k_min_scalars", "k_min_custom_song", g->k_min);
+  RD_D2("k_max_scalars", "k_max_custom_song", g->k_max);
+  RD_I2("k_size_scalars", "k_size_custom_song", g->k_size);
+  if ((v = get(pl, "sources2_k3_sampling")) && sampling(v, "sources2_k3_sampling", &g->k3_sampling, err)) return 1;
+  {
+    double d;
+    if ((v = get(pl, "k3_size"))) {
+      if (num(v, "k3_size", &d, err)) return 1;
+      g->k3_size = (int)d;
+    }
+  }
+  v = get2(pl, "custom_time_sampling_for_2nd_order_sources", "custom_time_sampling_song_sources");
+  g->custom_tau = yes(v);
+  RD_D2("custom_tau_ini_2nd_order_sources", "custom_tau_ini_song_sources", g->tau_ini);
+  RD_D2("custom_tau_end_2nd_order_sources", "custom_tau_end_song_sources", g->tau_end);
+  RD_I2("custom_tau_size_2nd_order_sources", "custom_tau_size_song_sources", g->tau_size);
+  if ((v = get2(pl, "custom_tau_mode_2nd_order_sources", "custom_tau_mode_song_sources"))) {
+    if (strstr(v, "lin") || strstr(v, "LIN")) g->tau_sampling = SONG2_SAMPLING_LIN;
+    else if (strstr(v, "log") || strstr(v, "LOG")) g->tau_sampling = SONG2_SAMPLING_LOG;
+    else {
+      snprintf(err, SONG2_ERRLEN, "custom_tau_mode_song_sources = %.200s (lin or log)", v);
+      return 1;
+    }
+  }
+  if (g->custom_tau && g->tau_ini <= 0) {
+    snprintf(err, SONG2_ERRLEN, "please choose 'tau_ini' greater than zero");
+    return 1;
+  }
+  /* CLASS's l sampling keys */
+  {
+    double d;
+    if ((v = get(pl, "l_max_scalars"))) {
+      if (num(v, "l_max_scalars", &d, err)) return 1;
+      g->l_max_scalars = (int)d;
+    }
+    RD_D("l_logstep", g->l_logstep);
+    if ((v = get(pl, "l_linstep"))) {
+      if (num(v, "l_linstep", &d, err)) return 1;
+      g->l_linstep = (int)d;
+    }
+  }
+
+  /* line of sight (input2.c:1433-1543, 1699-1740) */
+  if (los) {
+    song2_los_spec keep = *los;
+    song2_los_defaults(los, NULL, NULL);
+    los->l_size = keep.l_size;
+    los->l = keep.l;
+    los->tau0 = keep.tau0;
+    los->tau_rec = keep.tau_rec;
+    if ((v = get2(pl, "transfer2_k_sampling", "transfer2_k3_sampling"))) {
+      if (strstr(v, "bessel")) los->k3_sampling = SONG2_K3_SAMPLING_BESSEL;
+      else if (strstr(v, "class") || strstr(v, "smart")) los->k3_sampling = SONG2_K3_SAMPLING_CLASS;
+      else {
+        snprintf(err, SONG2_ERRLEN, "transfer2_k3_sampling = %.200s (bessel, smart or class)", v);
+        return 1;
+      }
+    }
+    RD_D2("k_step_trans_scalars_2nd_order", "q_linstep_song", los->q_linstep);
+    if (get(pl, "k_step_trans_scalars_2nd_order") && !get(pl, "q_linstep_song")) los->q_linstep *= 95; /* :1489-1503 */
+    if ((v = get(pl, "transfer2_tau_sampling"))) {
+      if (strstr(v, "sources") || strstr(v, "source")) los->tau_sampling = SONG2_TAU_SAMPLING_SOURCES;
+      else if (strstr(v, "custom") || strstr(v, "smart")) los->tau_sampling = SONG2_TAU_SAMPLING_CUSTOM;
+      else if (strstr(v, "bessel")) los->tau_sampling = SONG2_TAU_SAMPLING_BESSEL;
+      else {
+        snprintf(err, SONG2_ERRLEN, "transfer2_tau_sampling = %.200s (sources, custom or bessel)", v);
+        return 1;
+      }
+    }
+    {
+      const char *a = get(pl, "tau_step_trans_2nd_order"), *b = get(pl, "tau_step_trans_song"),
+                 *c = get(pl, "tau_linstep_song");
+      double d;
+      if (c) {
+        if (num(c, "tau_linstep_song", &d, err)) return 1;
+        los->tau_linstep = d;
+      } else if (b || a) {
+        if (num(b ? b : a, "tau_step_trans_song", &d, err)) return 1;
+        los->tau_linstep = d / (2 * 3.141592653589793);
+      }
+      if (los->tau_linstep < 0) los->tau_linstep = 1e300; /* no points added (:1542-1543) */
+    }
+    if ((v = get(pl, "sources_time_interpolation")))
+      los->time_interpolation = (strstr(v, "cubic") || strstr(v, "spline")) ? SONG2_INTERP_CUBIC : SONG2_INTERP_LINEAR;
+    if ((v = get(pl, "sources_k3_interpolation")))
+      los->k3_interpolation = (strstr(v, "cubic") || strstr(v, "spline")) ? SONG2_INTERP_CUBIC : SONG2_INTERP_LINEAR;
+    if ((v = get(pl, "bessels_interpolation")))
+      los->bessel_interpolation = strstr(v, "cubic") ? SONG2_INTERP_CUBIC : SONG2_INTERP_LINEAR;
+    if ((v = get(pl, "bispectra_k3_extrapolation")))
+      los->k3_extrapolation = strstr(v, "flat") ? SONG2_K3_EXTRAP_FLAT : SONG2_K3_EXTRAP_NONE;
+    RD_D("extra_k3_oscillations_left", los->extra_k3_oscillations_left);
+    RD_D("extra_k3_oscillations_right", los->extra_k3_oscillations_right);
+    RD_D2("bessel_x_step_2nd_order", "bessel_x_step_song", los->x_step);
+    RD_D2("bessel_j_cut_2nd_order", "bessel_j_cut_song", los->j_cut);
+    RD_D2("bessel_J_cut_2nd_order", "bessel_J_cut_song", los->J_cut);
+    /* pbs2->xx_max for the lin/log k samplings (input2.c:1982-2006) */
+    los->x_max = (g->k_max * 18000.0 + los->x_step) * 1.05;
+  }
+  return 0;
+}

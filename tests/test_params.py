@@ -1,0 +1,144 @@
+"""The reader of the reference's ini/pre parameter files (input2.c) for the keys
+of the hot path.  The files are written by the tests; names, aliases, yes/no
+rules and defaults follow input2.c:137-2016 and perturbations2.c:843-945.  CPU only."""
+import ctypes as C
+
+import pytest
+
+from song_gb300 import capi
+
+INI = """
+# second-order run: temperature and E-mode bispectra
+output = tBisp, eBisp
+modes_song = 0, 1, 2
+l_max_g_song = 10
+l_max_pol_g_song = 9
+l_max_ur_song = 8
+tol_perturb_integration_song = 1e-5
+ic_song = ad
+include_pure_scattering_song = yes
+include_quad_scattering_song = yes
+include_sachs_wolfe_song = yes
+include_integrated_sachs_wolfe_song = yes
+include_pure_metric_song = yes          # dropped because SW and ISW are on
+use_exponential_potentials = yes
+sources2_k_sampling = log
+k_min_custom_song = 1e-4
+k_max_custom_song = 0.05
+k_size_custom_song = 8
+sources2_k3_sampling = lin
+k3_size = 6
+custom_time_sampling_song_sources = yes
+custom_tau_ini_song_sources = 200
+custom_tau_end_song_sources = 0
+custom_tau_size_song_sources = 100
+custom_tau_mode_song_sources = log
+"""
+
+PRE = """
+radiation_streaming_approximation_song = 0
+tight_coupling_trigger_tau_c_over_tau_h_song = 0.015
+tight_coupling_trigger_tau_c_over_tau_k_2nd_order = 0.005
+l_max_scalars = 2000
+l_logstep = 1.25
+l_linstep = 36
+transfer2_k3_sampling = smart
+q_linstep_song = 0.3
+transfer2_tau_sampling = custom
+tau_linstep_song = 0.5
+bessels_interpolation = linear
+sources_time_interpolation = cubic
+bispectra_k3_extrapolation = flat_extrapolation
+extra_k3_oscillations_right = 20
+extra_k3_oscillations_left = 10
+"""
+
+
+def read(lib, tmp_path, ini, pre, los=True):
+    pi, pp = tmp_path / "run.ini", tmp_path / "run.pre"
+    pi.write_text(ini)
+    pp.write_text(pre)
+    s, g = capi.Spec(), capi.Params()
+    ls = capi.LosSpec() if los else None
+    err = capi.errbuf()
+    rc = lib.song2_read_params(str(pi).encode(), str(pp).encode(), C.byref(s), C.byref(g),
+                               C.byref(ls) if ls is not None else None, err)
+    return rc, s, g, ls, err.value.decode()
+
+
+def test_reads_the_hot_path_keys(lib, tmp_path):
+    rc, s, g, ls, err = read(lib, tmp_path, INI, PRE)
+    assert rc == 0, err
+    assert (s.has_source_T, s.has_source_E, s.has_source_B, s.has_source_delta_cdm) == (1, 1, 1, 0)
+    assert [s.m[i] for i in range(s.m_size)] == [0, 1, 2]
+    assert (s.l_max_g, s.l_max_pol_g, s.l_max_ur) == (10, 9, 8)
+    assert s.rtol == 1e-5 and s.ic == 0
+    assert s.has_pure_scattering_in_los and s.has_quad_scattering_in_los and s.has_sw and s.has_isw
+    assert s.has_pure_metric_in_los == 0 and s.use_exponential_potentials == 1
+    assert s.rescale_cmb_sources == 1          # m_max > 0 and no stop_at_* output
+    assert s.radiation_streaming_approximation == 0
+    assert s.tca_trigger_tau_c_over_tau_h == 0.015 and s.tca_trigger_tau_c_over_tau_k == 0.005
+    assert (g.k_sampling, g.k_min, g.k_max, g.k_size) == (capi.SAMPLING_LOG, 1e-4, 0.05, 8)
+    assert (g.k3_sampling, g.k3_size) == (capi.SAMPLING_LIN, 6)
+    assert (g.custom_tau, g.tau_sampling, g.tau_ini, g.tau_end, g.tau_size) == (1, capi.SAMPLING_LOG, 200, 0, 100)
+    assert (g.l_max_scalars, g.l_logstep, g.l_linstep) == (2000, 1.25, 36)
+    assert ls.k3_sampling == capi.K3_SAMPLING_CLASS and ls.q_linstep == 0.3
+    assert ls.tau_sampling == capi.TAU_SAMPLING_CUSTOM and ls.tau_linstep == 0.5
+    assert ls.time_interpolation == capi.INTERP_CUBIC and ls.bessel_interpolation == capi.INTERP_LINEAR
+    assert ls.k3_extrapolation == capi.K3_EXTRAP_FLAT
+    assert (ls.extra_k3_oscillations_left, ls.extra_k3_oscillations_right) == (10, 20)
+    assert abs(ls.x_max - (0.05 * 18000 + 0.2) * 1.05) < 1e-9
+
+
+def test_defaults_are_the_reference_defaults(lib, tmp_path):
+    rc, s, g, ls, err = read(lib, tmp_path, "output = tBisp\n", "")
+    assert rc == 0, err
+    ref = capi.Spec()
+    lib.song2_spec_defaults(C.byref(ref))
+    for f in ("l_max_g", "l_max_pol_g", "l_max_ur", "rtol", "tight_coupling", "has_quadratic_sources",
+              "has_polarization2", "start_small_k_at_tau_c_over_tau_h"):
+        assert getattr(s, f) == getattr(ref, f), f
+    assert s.radiation_streaming_approximation == capi.SONG2_RSA_MD     # rsa2_MD, input2.c:2139
+    assert (s.has_source_T, s.has_source_E, s.has_source_B) == (1, 0, 0)
+    assert g.k_sampling == capi.SAMPLING_SMART and g.k3_sampling == capi.SAMPLING_SMART
+    assert g.custom_tau == 0 and g.tau_size == 2000
+
+
+def test_switches_and_outputs(lib, tmp_path):
+    rc, s, *_ , err = read(lib, tmp_path, "output = bBisp, mBisp\nmodes_song = 0\nquadratic_sources = no\n", "")
+    assert rc == 0, err
+    # B output needs E sources; B sources vanish for m = 0 only runs
+    assert (s.has_source_T, s.has_source_E, s.has_source_B, s.has_source_delta_cdm) == (0, 1, 0, 1)
+    assert s.has_quadratic_sources == 0 and s.has_quadratic_liouville == 0 and s.has_quadratic_collision == 0
+    assert s.rescale_cmb_sources == 0
+    rc, s, *_ , err = read(lib, tmp_path, "output = tCl2, T2\nmodes_song = 0,2\n", "")
+    assert rc == 0 and s.rescale_cmb_sources == 0          # stop_at_transfers2
+    rc, s, *_ , err = read(lib, tmp_path, "ic_song = ad_first_order\n", "")
+    assert rc == 0 and s.ic == capi.SONG2_IC_AD_FIRST_ORDER
+
+
+def test_obsolete_alias_loses_to_the_new_name(lib, tmp_path):
+    rc, s, *_ , err = read(lib, tmp_path, "l_max_g_2nd_order = 5\nl_max_g_song = 7\nl_max_ur_2nd_order = 6\n", "")
+    assert rc == 0, err
+    assert s.l_max_g == 7 and s.l_max_ur == 6
+
+
+@pytest.mark.parametrize("ini,pre,msg", [
+    ("l_max_g_song = 8\n", "l_max_g_song = 9\n", "multiple entries"),
+    ("modes_song = 2, 1\n", "", "strictly ascending"),
+    ("output = eBisp\npolarization_second_order = no\n", "", "polarization_second_order"),
+    ("sources2_k_sampling = spiral\n", "", "sampling"),
+    ("perfect_baryons = no\n", "", "perfect_baryons"),
+    ("tol_perturb_integration_song = small\n", "", "not a number"),
+    ("custom_time_sampling_song_sources = yes\ncustom_tau_ini_song_sources = 0\n", "", "tau_ini"),
+])
+def test_bad_files_are_errors(lib, tmp_path, ini, pre, msg):
+    rc, *_ , err = read(lib, tmp_path, ini, pre)
+    assert rc == 1 and msg in err, err
+
+
+def test_missing_file_is_an_error(lib, tmp_path):
+    s, g = capi.Spec(), capi.Params()
+    err = capi.errbuf()
+    assert lib.song2_read_params(str(tmp_path / "none.ini").encode(), None, C.byref(s), C.byref(g), None, err) == 1
+    assert b"cannot open" in err.value
