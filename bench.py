@@ -72,13 +72,17 @@ CONTRACT_PARTS = 20
 # line-of-sight leg: the l sampling of the reference's precision presets
 # (pre/*lmax2000.pre: l_max_scalars 2000, l_logstep 1.25, l_linstep 36)
 LOS_L = (2000, 1.25, 36)
-# FP64 work of the mixed-form evolver per NDF step and FP64 warp instructions per
-# NDF step (ncu counters of this kernel on the reduced config-4 case, see
-# profiles/), and the FP64 issue rate of a GB300 SM (one FP64 warp instruction per
-# ~19 SM cycles whatever the number of active lanes; DFMA probe, see profiles/)
-FP64_FLOPS_PER_STEP = 47.0e3
-FP64_WARP_INSTR_PER_STEP = 2.74e3
+# Work of the mixed-form evolver per NDF step and DRAM traffic per triplet, from
+# the ncu counters of both launch groups of the reduced config-4 case
+# (python -m song_gb300.cases evolver --k-size 6: 504 triplets, 3.95 M NDF steps;
+# FP64 flops = 2 DFMA + DMUL + DADD thread instructions, FP32 likewise), and the
+# FP64 issue rate of a GB300 SM (one FP64 warp instruction per ~19 SM cycles
+# whatever the number of active lanes; DFMA probe)
+FP64_FLOPS_PER_STEP = 46.3e3
+FP32_FLOPS_PER_STEP = 45.3e3
+FP64_WARP_INSTR_PER_STEP = 1.73e3
 FP64_WARP_INSTR_PER_SM_CYCLE = 0.0526
+DRAM_BYTES_PER_TRIPLET = 10.8e6
 
 
 def parse():
@@ -802,8 +806,17 @@ def main():
     alg = algorithmic_bytes(p) * (trip_timed / n_trip) / args.steps
     hbm_peak = peaks.get("hbm_gbs")
     achieved = alg / (ms_step / 1e3) / 1e9
+    # DRAM traffic of one step: the measured bytes per triplet of the reduced case, times
+    # the triplets of a step (the traffic grows with the triplets: each writes and
+    # re-reads its own quadratic-source table, which the resident CTAs' tables spill
+    # from L2)
+    traffic = DRAM_BYTES_PER_TRIPLET * trip_timed / args.steps
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak or 6800.0, "unit": "GB/s",
-                "frac": achieved / (hbm_peak or 6800.0), "traffic": None,
+                "frac": achieved / (hbm_peak or 6800.0), "traffic": traffic,
+                "traffic_note": "bytes per step: ncu dram__bytes_read+write per triplet of the reduced config-4 "
+                                "case (10.8 MB) times the triplets of a step; the excess over the algorithmic "
+                                "bytes is the per-triplet quadratic-source tables, written and re-read by their "
+                                "CTA, spilling from L2; DRAM runs at 0.03 % of peak",
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else "fallback 6800",
                 "note": "the evolver is bound by the latency of its FP64 chains and the FP64 pipe, not by HBM; "
                         "bytes = first-order rows of every (k1,k2) pair + background + source writes"}
@@ -814,8 +827,10 @@ def main():
     fp64_peak = FP64_WARP_INSTR_PER_SM_CYCLE * 32 * 2 * sm_mhz * 1e6 * nsm
     fp64_slots = steps_tot * FP64_WARP_INSTR_PER_STEP / t_mixed * (args.steps / n_parts)
     slot_peak = FP64_WARP_INSTR_PER_SM_CYCLE * sm_mhz * 1e6 * nsm
+    fp32_flops = steps_tot * FP32_FLOPS_PER_STEP / t_mixed * (args.steps / n_parts)
     roofline_fp64 = {"bound": "fp64", "achieved": fp64_flops / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
                      "frac": fp64_flops / fp64_peak, "issue_slots_frac": fp64_slots / slot_peak,
+                     "fp32_tflops": fp32_flops / 1e12,
                      "note": "FP64 flops (FMA = 2) per NDF step from the ncu counters of this kernel; peak from "
                              "the DFMA probe (one FP64 warp instruction per ~19 SM cycles, any lane count); "
                              "issue_slots_frac counts FP64 warp instructions against that rate"}
