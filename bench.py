@@ -95,7 +95,7 @@ def parse():
     ap.add_argument("--parts", type=int, default=0, help="parts of the workload (default: --steps)")
     ap.add_argument("--cpu-sample", type=int, default=256,
                     help="triplets of the CPU-baseline sample (every n/N-th of the cost-sorted workload)")
-    ap.add_argument("--ref-step-items", type=int, default=192, help="triplets per reference-arm step")
+    ap.add_argument("--ref-step-items", type=int, default=64, help="triplets per reference-arm step")
     ap.add_argument("--accuracy-sample", type=int, default=16,
                     help="triplets checked against the FP64 oracle at rtol 1e-8 (0: skip)")
     ap.add_argument("--plain-parts", type=int, default=0, help="parts timed in plain FP64 (default: steps/4)")
