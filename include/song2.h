@@ -519,8 +519,33 @@ typedef struct {
   int l_max_scalars;         /* CLASS l sampling: l_max_scalars, l_logstep, l_linstep */
   double l_logstep;
   int l_linstep;
+  /* smart k1/k2 sampling (input2.c:386-470, defaults :2290-2299) */
+  double k_min_tau0, k_max_tau0_over_l_max, k_step_sub, k_step_super, k_logstep_super, k_step_transition;
+  double k_per_decade_for_pk, k_per_decade_for_bao, k_bao_center, k_bao_width;
+  double k_max_for_pk;       /* 1/Mpc (P_k_max_1/Mpc_song, or P_k_max_h/Mpc_song times h) */
+  double h;                  /* the cosmology's h (CLASS key h), for P_k_max_h/Mpc_song */
+  int k3_size_min;           /* smart k3 sampling: at least this many k3 per pair */
+  int has_cmb, has_lss;      /* from the output string (perturbations2.c:836-950) */
 } song2_params;
 void song2_params_defaults(song2_params *grids);
+/* Comoving sound horizon int_0^tau c_s dtau', c_s^2 = 1/(3 (1 + 3 rho_b / 4 rho_g)),
+   on the background table (CLASS's pth->rs_rec at tau = song2_recombination_time). */
+double song2_sound_horizon(const song2_tables *tab, double tau);
+/* The smart k1/k2 sampling of perturb2_get_k_lists (perturbations2.c:1610-1766):
+   from k_min_tau0/tau0 by the smaller of a logarithmic and a tanh-blended linear
+   step in units of k_rec = 2 pi / rs_rec up to k_max_tau0_over_l_max l_scalar_max /
+   tau0 (CMB outputs), then logarithmically with the BAO-weighted density up to
+   k_max_for_pk (LSS outputs); the last value is exactly the larger k_max.  Writes
+   k_out when not NULL and returns the size, or -1 with a message. */
+int song2_k_grid_smart(const song2_params *grids, double tau0, double rs_rec, int l_scalar_max, double *k_out,
+                       char *err);
+/* The smart k3 sampling (perturbations2.c:2086-2178): for every pair the points of
+   the k grid within [k3_min, k3_max] (the same limits as song2_k3_grids), merged
+   with the two limits, and with k3_size_min - n + 2 evenly spaced points between
+   them merged in when the pair has n < k3_size_min points; sorted, duplicates
+   removed (CLASS's merge_arrays_double).  Same outputs as song2_k3_grids. */
+int song2_k3_grids_smart(const double *k, int k_size, int k3_size_min, int *k3_size_out, double *k3_out,
+                         char *err);
 /* Reads an ini and a pre file (either may be NULL; a name may appear once in
    the two) into spec (starting from song2_spec_defaults with the reference's
    default radiation-streaming approximation, rsa2_MD), the grid settings and,

@@ -121,7 +121,12 @@ class Params(C.Structure):
     _fields_ = [("k_sampling", C.c_int), ("k_min", C.c_double), ("k_max", C.c_double), ("k_size", C.c_int),
                 ("k3_sampling", C.c_int), ("k3_size", C.c_int), ("custom_tau", C.c_int), ("tau_sampling", C.c_int),
                 ("tau_ini", C.c_double), ("tau_end", C.c_double), ("tau_size", C.c_int),
-                ("l_max_scalars", C.c_int), ("l_logstep", C.c_double), ("l_linstep", C.c_int)]
+                ("l_max_scalars", C.c_int), ("l_logstep", C.c_double), ("l_linstep", C.c_int),
+                ("k_min_tau0", C.c_double), ("k_max_tau0_over_l_max", C.c_double), ("k_step_sub", C.c_double),
+                ("k_step_super", C.c_double), ("k_logstep_super", C.c_double), ("k_step_transition", C.c_double),
+                ("k_per_decade_for_pk", C.c_double), ("k_per_decade_for_bao", C.c_double),
+                ("k_bao_center", C.c_double), ("k_bao_width", C.c_double), ("k_max_for_pk", C.c_double),
+                ("h", C.c_double), ("k3_size_min", C.c_int), ("has_cmb", C.c_int), ("has_lss", C.c_int)]
 
 
 SAMPLING_LIN, SAMPLING_LOG, SAMPLING_SMART, SAMPLING_SYM, SAMPLING_THETA12 = 0, 1, 2, 3, 4
@@ -201,6 +206,9 @@ SIGNATURES = {
     "song2_gpu_first_order": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _D, _D, _PD, C.c_char_p]),
     "song2_los_defaults": (None, [C.POINTER(LosSpec), C.POINTER(Spec), C.POINTER(Tables)]),
     "song2_params_defaults": (None, [C.POINTER(Params)]),
+    "song2_sound_horizon": (_D, [C.POINTER(Tables), _D]),
+    "song2_k_grid_smart": (_I, [C.POINTER(Params), _D, _D, _I, _PD, C.c_char_p]),
+    "song2_k3_grids_smart": (_I, [_PD, _I, _I, _PI, _PD, C.c_char_p]),
     "song2_read_params": (_I, [C.c_char_p, C.c_char_p, C.POINTER(Spec), C.POINTER(Params), C.POINTER(LosSpec),
                                C.c_char_p]),
     "song2_l_list": (_I, [_I, _D, _I, _PI]),

@@ -7,6 +7,8 @@
  * trimmed; the ini and pre files form one list and a name may appear only once.
  */
 #include <ctype.h>
+#include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -132,6 +134,22 @@ void song2_params_defaults(song2_params *g) {
   g->l_max_scalars = 2500;
   g->l_logstep = 1.12;
   g->l_linstep = 40;
+  /* smart sampling (input2.c:2290-2299, 2175, 2316) */
+  g->k_min_tau0 = 0.1;
+  g->k_max_tau0_over_l_max = 2;
+  g->k_step_sub = 0.1;
+  g->k_step_super = 0.025;
+  g->k_logstep_super = 1.8;
+  g->k_step_transition = 0.2;
+  g->k_per_decade_for_pk = 10;
+  g->k_per_decade_for_bao = 70;
+  g->k_bao_center = 3;
+  g->k_bao_width = 4;
+  g->k_max_for_pk = 0.1;
+  g->h = 0.67556;
+  g->k3_size_min = 5;
+  g->has_cmb = 0;
+  g->has_lss = 0;
 }
 
 static int sampling(const char *v, const char *k, int *out, char *err) {
@@ -316,6 +334,8 @@ int song2_read_params(const char *ini_path, const char *pre_path, song2_spec *s,
   }
   /* rescaling of the CMB sources (input2.c:1955-1971) */
   s->rescale_cmb_sources = !(stop_p2 || stop_t2) && m_max != 0;
+  g->has_cmb = has_t || has_e || has_b;
+  g->has_lss = has_cdm;
 
   /* grids (input2.c:320-530) */
   if ((v = get(pl, "sources2_k_sampling")) && sampling(v, "sources2_k_sampling", &g->k_sampling, err)) return 1;
@@ -346,6 +366,51 @@ int song2_read_params(const char *ini_path, const char *pre_path, song2_spec *s,
   if (g->custom_tau && g->tau_ini <= 0) {
     snprintf(err, SONG2_ERRLEN, "please choose 'tau_ini' greater than zero");
     return 1;
+  }
+  /* smart k sampling (input2.c:405-470) */
+  RD_D2("k_scalar_min_tau0_2nd_order", "k_min_tau0_song", g->k_min_tau0);
+  RD_D2("k_scalar_max_tau0_over_l_max_2nd_order", "k_max_tau0_over_l_max_song", g->k_max_tau0_over_l_max);
+  RD_D2("k_scalar_step_sub_2nd_order", "k_step_sub_song", g->k_step_sub);
+  {
+    const char *a = get(pl, "k_scalar_linstep_super_2nd_order"), *b = get(pl, "k_linstep_super_2nd_order"),
+               *c = get(pl, "k_step_super_song");
+    const char *w = c ? c : (b ? b : a);
+    if (w && num(w, "k_step_super_song", &g->k_step_super, err)) return 1;
+  }
+  RD_D2("k_scalar_logstep_super_2nd_order", "k_logstep_super_song", g->k_logstep_super);
+  RD_D2("k_scalar_step_transition_2nd_order", "k_step_transition_song", g->k_step_transition);
+  RD_D("k_per_decade_for_pk_song", g->k_per_decade_for_pk);
+  RD_D("k_per_decade_for_bao_song", g->k_per_decade_for_bao);
+  RD_D("k_bao_center", g->k_bao_center);
+  RD_D("k_bao_width", g->k_bao_width);
+  RD_D("h", g->h);
+  if (g->k_logstep_super <= 1) {
+    snprintf(err, SONG2_ERRLEN, "logarithmic step must be larger than 1");
+    return 1;
+  }
+  if (g->has_lss) {
+    const char *ph = get(pl, "P_k_max_h/Mpc_song"), *p1 = get(pl, "P_k_max_1/Mpc_song");
+    if (ph && p1) {
+      snprintf(err, SONG2_ERRLEN, "you cannot enter both P_k_max_h/Mpc and P_k_max_1/Mpc, choose one");
+      return 1;
+    }
+    double d;
+    if (ph) {
+      if (num(ph, "P_k_max_h/Mpc_song", &d, err)) return 1;
+      g->k_max_for_pk = d * g->h;
+    }
+    if (p1) {
+      if (num(p1, "P_k_max_1/Mpc_song", &d, err)) return 1;
+      g->k_max_for_pk = d;
+    }
+    RD_D("k_max_for_pk", g->k_max_for_pk);
+  }
+  {
+    double d;
+    if ((v = get(pl, "k3_size_min"))) {
+      if (num(v, "k3_size_min", &d, err)) return 1;
+      g->k3_size_min = (int)d;
+    }
   }
   /* CLASS's l sampling keys */
   {
@@ -417,5 +482,157 @@ int song2_read_params(const char *ini_path, const char *pre_path, song2_spec *s,
     /* pbs2->xx_max for the lin/log k samplings (input2.c:1982-2006) */
     los->x_max = (g->k_max * 18000.0 + los->x_step) * 1.05;
   }
+  return 0;
+}
+
+/* ----------------------------------------------------------- smart grids */
+
+static double bgc(const song2_tables *t, int col, double x) {
+  double u = (x - t->bg_lntau0) / t->bg_dlntau;
+  int i = (int)floor(u);
+  if (i < 0) i = 0;
+  if (i > t->bg_size - 2) i = t->bg_size - 2;
+  double b = u - i, a = 1.0 - b, h = t->bg_dlntau;
+  const double *y0 = t->bg + (size_t)i * SONG2_BG_SIZE, *y1 = y0 + SONG2_BG_SIZE;
+  const double *d0 = t->bg_dd + (size_t)i * SONG2_BG_SIZE, *d1 = d0 + SONG2_BG_SIZE;
+  return a * y0[col] + b * y1[col] + ((a * a * a - a) * d0[col] + (b * b * b - b) * d1[col]) * h * h / 6.0;
+}
+
+static double sound_speed(const song2_tables *t, double x) {
+  double R = 0.75 * exp(bgc(t, SONG2_BG_LN_RHO_B, x) - bgc(t, SONG2_BG_LN_RHO_G, x));
+  return 1.0 / sqrt(3.0 * (1.0 + R));
+}
+
+double song2_sound_horizon(const song2_tables *t, double tau) {
+  /* before the table: radiation domination with R -> 0, c_s -> 1/sqrt(3) */
+  double x0 = t->bg_lntau0, x1 = log(tau);
+  double rs = exp(x0) * sound_speed(t, x0);
+  if (x1 <= x0) return tau * sound_speed(t, x0);
+  /* Simpson's rule in ln tau (dtau = tau dln tau) on the table's spacing, halved */
+  int n = 2 * (int)ceil((x1 - x0) / t->bg_dlntau);
+  if (n < 2) n = 2;
+  double h = (x1 - x0) / n, sum = 0.0;
+  for (int i = 0; i <= n; ++i) {
+    double x = x0 + i * h;
+    double f = exp(x) * sound_speed(t, x);
+    sum += f * ((i == 0 || i == n) ? 1.0 : (i % 2 ? 4.0 : 2.0));
+  }
+  return rs + sum * h / 3.0;
+}
+
+#define S2_PI 3.141592653589793238462643383279502884
+#define S2_K_SIZE_CAP 1000000
+
+int song2_k_grid_smart(const song2_params *g, double tau0, double rs_rec, int l_scalar_max, double *k_out,
+                       char *err) {
+  if (g->k_step_transition == 0 || rs_rec == 0 || tau0 <= 0) {
+    snprintf(err, SONG2_ERRLEN, "smart k sampling: k_step_transition, rs_rec and tau0 must be non-zero");
+    return -1;
+  }
+  double k_min = g->k_min_tau0 / tau0;
+  int n = 0;
+  double prev = k_min, k = k_min;
+  if (k_out) k_out[n] = k_min;
+  ++n;
+  double k_rec = 2 * S2_PI / rs_rec;
+  double k_max_cmb = 0, k_max_lss = 0;
+  if (g->has_cmb) {
+    k_max_cmb = g->k_max_tau0_over_l_max * l_scalar_max / tau0;
+    while (k < k_max_cmb) {
+      double lin_step = g->k_step_super +
+                        0.5 * (tanh((prev - k_rec) / k_rec / g->k_step_transition) + 1) * (g->k_step_sub - g->k_step_super);
+      double log_step = prev * (g->k_logstep_super - 1.);
+      double st = lin_step * k_rec < log_step ? lin_step * k_rec : log_step;
+      if (st / k < 1e-16) {
+        snprintf(err, SONG2_ERRLEN, "k step = %e < machine precision", st);
+        return -1;
+      }
+      if ((log_step > (lin_step * k_rec)) || (prev > k_rec)) k = prev + lin_step * k_rec;
+      else k = prev * g->k_logstep_super;
+      if (k_out) k_out[n] = k;
+      ++n;
+      prev = k;
+      if (n + 1 > S2_K_SIZE_CAP) {
+        snprintf(err, SONG2_ERRLEN, "k size for CMB is too large; check k_step_sub, k_step_super and k_logstep_super");
+        return -1;
+      }
+    }
+  }
+  if (g->has_lss) {
+    k_max_lss = g->k_max_for_pk;
+    while (k < k_max_lss) {
+      k *= pow(10, 1 / (g->k_per_decade_for_pk +
+                        (g->k_per_decade_for_bao - g->k_per_decade_for_pk) *
+                            (1 - tanh(pow((log(k) - log(g->k_bao_center * k_rec)) / log(g->k_bao_width), 4)))));
+      if (k_out) k_out[n] = k;
+      ++n;
+      if (n + 1 > S2_K_SIZE_CAP) {
+        snprintf(err, SONG2_ERRLEN, "k size for LSS is too large; check k_per_decade_for_pk and k_per_decade_for_bao");
+        return -1;
+      }
+    }
+  }
+  if (k_out) k_out[n - 1] = k_max_cmb > k_max_lss ? k_max_cmb : k_max_lss;
+  return n;
+}
+
+static int cmp_d(const void *a, const void *b) {
+  double x = *(const double *)a, y = *(const double *)b;
+  return (x > y) - (x < y);
+}
+
+/* merge_arrays_double: the union of two arrays, sorted, exact duplicates removed */
+static int merge_sorted(double *buf, int n) {
+  qsort(buf, n, sizeof(double), cmp_d);
+  int m = 0;
+  for (int i = 0; i < n; ++i)
+    if (m == 0 || buf[i] != buf[m - 1]) buf[m++] = buf[i];
+  return m;
+}
+
+int song2_k3_grids_smart(const double *k, int k_size, int k3_size_min, int *k3_size_out, double *k3_out,
+                         char *err) {
+  int64_t off = 0;
+  for (int i1 = 0; i1 < k_size; ++i1)
+    for (int i2 = 0; i2 < k_size; ++i2) k3_size_out[i1 * k_size + i2] = 0;
+  int cap = k_size + 2 + (k3_size_min > 0 ? k3_size_min + 2 : 0);
+  double *buf = (double *)malloc(sizeof(double) * cap);
+  if (!buf) {
+    snprintf(err, SONG2_ERRLEN, "out of memory");
+    return 1;
+  }
+  for (int i1 = 0; i1 < k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2) {
+      double k1 = k[i1], k2 = k[i2];
+      double k3_min = fabs(k1 - k2) + 1e-10, k3_max = k1 + k2 - 1e-10;
+      if ((k1 + k2) / 100 > k3_min) k3_min = (k1 + k2) / 100;
+      if (k[0] > k3_min) k3_min = k[0];
+      if (k[k_size - 1] < k3_max) k3_max = k[k_size - 1];
+      if (k3_min >= k3_max || k3_min < k[0] || k3_min > k[k_size - 1] || k3_max < k[0] || k3_max > k[k_size - 1]) {
+        snprintf(err, SONG2_ERRLEN, "found k3_min=%g, k3_max=%g for k1(%d)=%g and k2(%d)=%g", k3_min, k3_max, i1, k1,
+                 i2, k2);
+        free(buf);
+        return 1;
+      }
+      int lo = 0;
+      while (k[lo] < k3_min) ++lo;
+      int hi = k_size - 1;
+      while (k[hi] > k3_max) --hi;
+      int n = hi - lo + 1;
+      if (n < 0) n = 0;
+      for (int j = 0; j < n; ++j) buf[j] = k[lo + j];
+      buf[n] = k3_min;
+      buf[n + 1] = k3_max;
+      n = merge_sorted(buf, n + 2);
+      if (n < k3_size_min) {
+        int extra = k3_size_min - n + 2;
+        for (int j = 0; j < extra; ++j) buf[n + j] = k3_min + j * (k3_max - k3_min) / (extra - 1);
+        n = merge_sorted(buf, n + extra);
+      }
+      k3_size_out[i1 * k_size + i2] = n;
+      if (k3_out) memcpy(k3_out + off, buf, sizeof(double) * n);
+      off += n;
+    }
+  free(buf);
   return 0;
 }

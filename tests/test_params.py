@@ -142,3 +142,104 @@ def test_missing_file_is_an_error(lib, tmp_path):
     err = capi.errbuf()
     assert lib.song2_read_params(str(tmp_path / "none.ini").encode(), None, C.byref(s), C.byref(g), None, err) == 1
     assert b"cannot open" in err.value
+
+
+# ------------------------------------------------------------ smart samplings
+
+def oracle_lib():
+    import numpy as np  # noqa: F401
+    import oracle
+    lib = oracle.load()
+    f = lib.song2_oracle_k_grid_smart
+    f.restype = C.c_int
+    f.argtypes = [C.c_double] * 11 + [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double),
+                                      C.c_int]
+    g = lib.song2_oracle_k3_grids_smart
+    g.restype = C.c_int
+    g.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    h = lib.song2_oracle_sound_horizon
+    h.restype = C.c_double
+    h.argtypes = [C.POINTER(capi.Tables), C.c_double]
+    return lib
+
+
+def smart_k(lib, g, tau0, rs_rec, l_max):
+    import numpy as np
+    err = capi.errbuf()
+    n = lib.song2_k_grid_smart(C.byref(g), tau0, rs_rec, l_max, None, err)
+    assert n > 0, err.value
+    k = np.zeros(n)
+    assert lib.song2_k_grid_smart(C.byref(g), tau0, rs_rec, l_max, capi.dptr(k), err) == n
+    return k
+
+
+@pytest.mark.parametrize("cmb,lss,l_max", [(1, 0, 2000), (1, 1, 400), (0, 1, 2000)])
+def test_smart_k_grid_matches_oracle(lib, cmb, lss, l_max):
+    import numpy as np
+    g = capi.Params()
+    lib.song2_params_defaults(C.byref(g))
+    g.has_cmb, g.has_lss, g.k_max_for_pk = cmb, lss, 1.0
+    tau0, rs_rec = 14162.7, 145.3
+    k = smart_k(lib, g, tau0, rs_rec, l_max)
+    ol = oracle_lib()
+    out = np.zeros(100000)
+    n = ol.song2_oracle_k_grid_smart(g.k_min_tau0, g.k_max_tau0_over_l_max, g.k_step_sub, g.k_step_super,
+                                     g.k_logstep_super, g.k_step_transition, g.k_per_decade_for_pk,
+                                     g.k_per_decade_for_bao, g.k_bao_center, g.k_bao_width, g.k_max_for_pk,
+                                     cmb, lss, tau0, rs_rec, l_max, capi.dptr(out), out.size)
+    assert np.array_equal(k, out[:n])
+    assert k[0] == g.k_min_tau0 / tau0 and np.all(np.diff(k) > 0)
+    assert k[-1] == max(cmb * g.k_max_tau0_over_l_max * l_max / tau0, lss * 1.0)
+
+
+def test_smart_k3_grids_match_oracle(lib):
+    import numpy as np
+    g = capi.Params()
+    lib.song2_params_defaults(C.byref(g))
+    g.has_cmb = 1
+    k = smart_k(lib, g, 14162.7, 145.3, 600)
+    n = len(k)
+    sz = np.zeros(n * n, dtype=np.int32)
+    err = capi.errbuf()
+    assert lib.song2_k3_grids_smart(capi.dptr(k), n, g.k3_size_min, capi.iptr(sz), None, err) == 0, err.value
+    k3 = np.zeros(int(sz.sum()))
+    assert lib.song2_k3_grids_smart(capi.dptr(k), n, g.k3_size_min, capi.iptr(sz), capi.dptr(k3), err) == 0
+    ol = oracle_lib()
+    osz = np.zeros(n * (n + 1) // 2, dtype=np.int32)
+    ok3 = np.zeros(k3.size)
+    assert ol.song2_oracle_k3_grids_smart(capi.dptr(k), n, g.k3_size_min, capi.iptr(osz), capi.dptr(ok3)) == 0
+    pair_sizes = [int(sz[i1 * n + i2]) for i1 in range(n) for i2 in range(i1 + 1)]
+    assert pair_sizes == list(osz) and np.array_equal(k3, ok3)
+    off = 0
+    for i1 in range(n):
+        for i2 in range(i1 + 1):
+            grid = k3[off: off + sz[i1 * n + i2]]
+            off += sz[i1 * n + i2]
+            assert np.all(np.diff(grid) > 0)
+            assert grid[0] >= abs(k[i1] - k[i2]) and grid[-1] <= k[i1] + k[i2] and grid[-1] <= k[-1]
+
+
+def test_sound_horizon_matches_oracle(lib):
+    from helpers import problem
+    p = problem()
+    tr = lib.song2_recombination_time(C.byref(p.tables))
+    rs = lib.song2_sound_horizon(C.byref(p.tables), tr)
+    ref = oracle_lib().song2_oracle_sound_horizon(C.byref(p.tables), tr)
+    assert abs(rs - ref) <= 1e-6 * ref
+    assert 130.0 < rs < 160.0      # the comoving sound horizon of this flat LCDM at the visibility peak
+
+
+def test_reader_grids_of_a_smart_preset(lib, tmp_path):
+    import numpy as np
+    rc, s, g, ls, err = read(lib, tmp_path, "output = tBisp, eBisp\nmodes_song = 0,1,2\n",
+                             "sources2_k_sampling = smart\nsources2_k3_sampling = smart\nk3_size_min = 7\n"
+                             "l_max_scalars = 500\nk_min_tau0_song = 0.05\n")
+    assert rc == 0, err
+    assert g.k_sampling == capi.SAMPLING_SMART and g.k3_sampling == capi.SAMPLING_SMART and g.has_cmb == 1
+    assert g.k3_size_min == 7 and g.k_min_tau0 == 0.05 and g.l_max_scalars == 500
+    k = smart_k(lib, g, 14162.7, 145.3, g.l_max_scalars)
+    n = len(k)
+    sz = np.zeros(n * n, dtype=np.int32)
+    errb = capi.errbuf()
+    assert lib.song2_k3_grids_smart(capi.dptr(k), n, g.k3_size_min, capi.iptr(sz), None, errb) == 0
+    assert min(int(sz[i1 * n + i2]) for i1 in range(n) for i2 in range(i1 + 1)) >= 2
