@@ -233,6 +233,21 @@ int64_t song2_sources_per_type(const song2_spec *spec);
    perturb2_load_sources_k3_tau :575-602), so transfer2 reads the files unchanged. */
 int song2_store_sources(const song2_spec *spec, const double *flat, const char *dir, int index_k1, char *err);
 int song2_load_sources(const song2_spec *spec, double *flat, const char *dir, int index_k1, char *err);
+/* Self-describing source files in the layout of perturb2_output
+   (perturbations2.c:14688-15340) that the reference's python/songy.py reads:
+   song2_write_sources_k writes the sources of one (k1, k2 <= k1) pair as a
+   function of (k3, tau) with the pair's grids, the scale factor and Hubble rate
+   at every source time and the first-order quantities of k1 and k2 (songy
+   Fixedk1k2File, the reference's sources_song_k%03d.dat); song2_write_sources_tau
+   writes every triplet's sources at source time index_tau with the k and k3
+   grids and the first-order quantities of every k (songy FixedTauFile, the
+   reference's sources_song_tau%03d.dat).  An ASCII header (file type on the
+   first line, then a block map) precedes the binary blocks.  The tables must
+   hold the first-order quantities. */
+int song2_write_sources_k(const song2_spec *spec, const song2_tables *tab, const double *flat, int index_k1,
+                          int index_k2, const char *path, char *err);
+int song2_write_sources_tau(const song2_spec *spec, const song2_tables *tab, const double *flat, int index_tau,
+                            const char *path, char *err);
 /* Default spec values from source/input2.c:2027-2371 (pointers left NULL). */
 void song2_spec_defaults(song2_spec *spec);
 

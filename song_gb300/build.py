@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall"]
 
-C_SOURCES = ["song2_host.c", "song2_transfer_host.c", "song2_params.c"]
+C_SOURCES = ["song2_host.c", "song2_transfer_host.c", "song2_params.c", "song2_output.c"]
 CU_SOURCES = ["song2_k_block_f.cu", "song2_k_block_d.cu", "song2_k_class_f.cu", "song2_k_class_d.cu",
               "song2_k_class2_f.cu", "song2_k_class2_d.cu", "song2_k_block2_f.cu", "song2_k_block2_d.cu",
               "song2_k_warp_f.cu", "song2_k_warp_d.cu", "song2_k_team_f.cu", "song2_k_team_d.cu",

@@ -206,6 +206,8 @@ SIGNATURES = {
     "song2_gpu_first_order": (_I, [C.POINTER(Spec), C.POINTER(Tables), _I, _I, _D, _D, _PD, C.c_char_p]),
     "song2_los_defaults": (None, [C.POINTER(LosSpec), C.POINTER(Spec), C.POINTER(Tables)]),
     "song2_params_defaults": (None, [C.POINTER(Params)]),
+    "song2_write_sources_k": (_I, [C.POINTER(Spec), C.POINTER(Tables), _PD, _I, _I, C.c_char_p, C.c_char_p]),
+    "song2_write_sources_tau": (_I, [C.POINTER(Spec), C.POINTER(Tables), _PD, _I, C.c_char_p, C.c_char_p]),
     "song2_sound_horizon": (_D, [C.POINTER(Tables), _D]),
     "song2_k_grid_smart": (_I, [C.POINTER(Params), _D, _D, _I, _PD, C.c_char_p]),
     "song2_k3_grids_smart": (_I, [_PD, _I, _I, _PI, _PD, C.c_char_p]),
