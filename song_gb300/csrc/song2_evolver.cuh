@@ -1408,6 +1408,9 @@ template <class C, class A, class B> __device__ void rhs(const C &c, int ap, dou
     if (e < s.n_row_slots) {
       int i = c.row_slot[e];
       if (i >= 0) dy[i] = row(c, ap, i, yv, c.sh->ws, 0, tau);
+    } else if (ap == AP_RSA) {
+      /* radiation streaming: the moments with l >= 3 are frozen, their rows zero */
+      dy[__ldg(&c.ct.gen[e - s.n_row_slots].i)] = 0.0;
     } else {
       GenRow r = load_gen(c, e - s.n_row_slots);
       dy[r.i] = gen_row(c, ap, r, yv);
@@ -1434,6 +1437,9 @@ template <typename T, class C, class A> __device__ void newton_rhs(const C &c, i
       i = c.row_slot[e];
       if (i < 0) continue;
       fi = row(c, ap, i, yv, c.sh->ws, 0, tau);
+    } else if (ap == AP_RSA) {
+      i = __ldg(&c.ct.gen[e - s.n_row_slots].i);
+      fi = 0.0;
     } else {
       GenRow r = load_gen(c, e - s.n_row_slots);
       i = r.i;
@@ -1622,14 +1628,15 @@ __device__ __forceinline__ bool chain_factor(const C &c, int b, int ch, T hg, co
    complement and its inverse, in place, by Gauss-Jordan elimination with partial
    pivoting (lane j updates columns j, j + W, ...).  False on a zero pivot. */
 template <typename T, class C, class VJ, class VF>
-__device__ __forceinline__ bool core_factor(const C &c, int b, T hg, const VJ &J, const VF &F, int lane, int W, unsigned mask) {
+__device__ __forceinline__ bool core_factor(const C &c, int b, T hg, const VJ &J, const VF &F, int lane, int W, unsigned mask,
+                                            int nch) {
   const DevSpec &s = c.s;
   int cn = s.core_n[b], co = s.core_off[b];
   if (cn == 0) return true;
   for (int e = lane; e < cn * cn; e += W) {
     int i = e / cn, j = e % cn;
     T v = (i == j ? T(1) : T(0)) - hg * J[co + e];
-    for (int ch = 0; ch < s.ch_n[b]; ++ch) {
+    for (int ch = 0; ch < nch; ++ch) {
       int d = s.ch_d[b][ch], oe = s.ch_off[b][ch] + 3 * d * d * s.ch_len[b][ch];
       for (int a = 0; a < d; ++a) v -= F[oe + d * cn + i * d + a] * F[oe + a * cn + j];
     }
@@ -1724,13 +1731,17 @@ template <typename T, class C> __device__ __noinline__ void form_and_factor(cons
   auto J = c.template jacv<T>();
   auto F = c.template lu<T>();
   T hg = (T)hinvGak;
-  for_chains(
-      c, [&](int b, int ch) { if (!chain_factor<T, 1>(c, b, ch, hg, J, F)) c.sh->lu_fail = 1; },
-      [&](int b, int ch) { if (!chain_factor<T, 2>(c, b, ch, hg, J, F)) c.sh->lu_fail = 1; });
+  /* radiation streaming: the chains' rows are zero, so their blocks of M are the
+     identity and their coupling to the cores vanishes; only the cores are factorised */
+  const bool chains = c.sh->ap != AP_RSA;
+  if (chains)
+    for_chains(
+        c, [&](int b, int ch) { if (!chain_factor<T, 1>(c, b, ch, hg, J, F)) c.sh->lu_fail = 1; },
+        [&](int b, int ch) { if (!chain_factor<T, 2>(c, b, ch, hg, J, F)) c.sh->lu_fail = 1; });
   c.sync();
   PH_MARK(c, PH_FACT_CHAIN);
   per_block_group(c, [&](int b, int lane, int W, unsigned mask) {
-    if (!core_factor<T>(c, b, hg, J, F, lane, W, mask)) c.sh->lu_fail = 1;
+    if (!core_factor<T>(c, b, hg, J, F, lane, W, mask, chains ? s.ch_n[b] : 0)) c.sh->lu_fail = 1;
   });
   c.sync();
 }
@@ -1913,11 +1924,11 @@ template <class C, class F> __device__ void per_chain_group(const C &c, F f) {
 
 /* the core of block b in M x = xsol: x_core = S^-1 (b_core - sum F h_0), by a group
    of W lanes, after the chains' backward sweeps */
-template <typename T, class C> __device__ void core_solve(const C &c, int b, int lane, int W, unsigned mask) {
+template <typename T, class C> __device__ void core_solve(const C &c, int b, int lane, int W, unsigned mask, bool chains) {
   const DevSpec &s = c.s;
   auto F = c.template lu<T>();
   auto x = c.template xsol<T>();
-  int nch = s.ch_n[b], cn = s.core_n[b];
+  int nch = chains ? s.ch_n[b] : 0, cn = s.core_n[b];
   if (cn == 0) return;
   const short *cx = c.mx_s + s.core_idx[b];
   for (int i = lane; i < cn; i += W) {
@@ -1950,20 +1961,27 @@ template <typename T, class C> __device__ void lu_solve(const C &c) {
   const DevSpec &s = c.s;
   auto F = c.template lu<T>();
   auto x = c.template xsol<T>();
-  per_chain_group(c, [&](int b, int ch, int lane, int W, unsigned mask) {
-    if (s.ch_d[b][ch] == 1) chain_back<T, 1>(c, b, ch, F, x, lane, W, mask);
-    else chain_back<T, 2>(c, b, ch, F, x, lane, W, mask);
-  });
-  c.sync();
+  /* radiation streaming: the chains' right-hand sides are zero and their blocks
+     the identity, so their solution is zero and only the cores are solved */
+  const bool chains = c.sh->ap != AP_RSA;
+  if (chains) {
+    per_chain_group(c, [&](int b, int ch, int lane, int W, unsigned mask) {
+      if (s.ch_d[b][ch] == 1) chain_back<T, 1>(c, b, ch, F, x, lane, W, mask);
+      else chain_back<T, 2>(c, b, ch, F, x, lane, W, mask);
+    });
+    c.sync();
+  }
   PH_MARK(c, PH_SOLVE_BACK);
-  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { core_solve<T>(c, b, lane, W, mask); });
+  per_block_group(c, [&](int b, int lane, int W, unsigned mask) { core_solve<T>(c, b, lane, W, mask, chains); });
   c.sync();
   PH_MARK(c, PH_SOLVE_CORE);
-  per_chain_group(c, [&](int b, int ch, int lane, int W, unsigned mask) {
-    if (s.ch_d[b][ch] == 1) chain_fwd<T, 1>(c, b, ch, F, x, lane, W, mask);
-    else chain_fwd<T, 2>(c, b, ch, F, x, lane, W, mask);
-  });
-  c.sync();
+  if (chains) {
+    per_chain_group(c, [&](int b, int ch, int lane, int W, unsigned mask) {
+      if (s.ch_d[b][ch] == 1) chain_fwd<T, 1>(c, b, ch, F, x, lane, W, mask);
+      else chain_fwd<T, 2>(c, b, ch, F, x, lane, W, mask);
+    });
+    c.sync();
+  }
 }
 
 /* ------------------------------------------------------------------ reductions */
