@@ -900,7 +900,13 @@ template <class C> __device__ void prepare_table(const C &c, double tau, int ap)
     double ca = (a * a * a - a) * s.fo_dx2_6, cb = (b * b * b - b) * s.fo_dx2_6;
     int nq = s.qs2_size;
     auto r0 = c.qtab + (i - j0) * 2 * nq, r1 = r0 + 2 * nq;
-    for (int q = tid; q < nq; q += nt) c.qs[q] = a * r0[q] + b * r1[q] + ca * r0[nq + q] + cb * r1[nq + q];
+    /* radiation streaming: the rows of the moments with l >= 3 are not evaluated,
+       so neither are their quadratic sources */
+    const bool rsa = ap == AP_RSA;
+    for (int q = tid; q < nq; q += nt) {
+      if (rsa && c.qs_sp[q] <= SP_N && c.qs_l[q] >= 3) continue;
+      c.qs[q] = a * r0[q] + b * r1[q] + ca * r0[nq + q] + cb * r1[nq + q];
+    }
     if (ap) {
       size_t stride = (size_t)s.fo_tau_size * s.nfo;
       for (int q = tid; q < 2 * s.nfo; q += nt) {
@@ -923,7 +929,7 @@ template <class C> __device__ void prepare_table(const C &c, double tau, int ap)
     const BgV &bg = c.sh->bg;
     for (int e = tid; e < s.n_qs_slots; e += nt) {
       int q = c.qs_slot[e];
-      if (q >= 0) qc_entry(c, bg, q);
+      if (q >= 0 && !(ap == AP_RSA && c.qs_sp[q] <= SP_N && c.qs_l[q] >= 3)) qc_entry(c, bg, q);
     }
     c.sync();
   }
