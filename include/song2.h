@@ -541,8 +541,25 @@ typedef struct {
   double h;                  /* the cosmology's h (CLASS key h), for P_k_max_h/Mpc_song */
   int k3_size_min;           /* smart k3 sampling: at least this many k3 per pair */
   int has_cmb, has_lss;      /* from the output string (perturbations2.c:836-950) */
+  /* source time sampling without a custom grid (song2_tau_grid_class) */
+  double tau_stepsize;       /* perturb_sampling_stepsize_song (default 0.4) */
+  double tau_late_boost;     /* perturb_sampling_late_time_boost (default 1) */
+  double tau_start_c_over_h; /* start_sources_at_tau_c_over_tau_h (CLASS default 0.008) */
 } song2_params;
 void song2_params_defaults(song2_params *grids);
+/* The source time sampling of perturb2_timesampling_for_sources when no custom
+   sampling is asked for (perturbations2.c:2604-2869): the first time by bisection
+   for (aH)/kappa' = start_tau_c_over_tau_h between z = 1e4 and the visibility peak
+   (only with CMB outputs; else the peak itself), then steps of
+   stepsize / sqrt(rate^2 + late_boost^2 |2 a''/a - (aH)^2|) with CLASS's
+   variation rate of the thermodynamics, rate = sqrt(kappa1^2 + (kappa2/kappa1)^2 +
+   |kappa3/kappa1|) for the first three conformal-time derivatives of the optical
+   depth (CMB outputs; else stepsize / (aH)), until tau0, the last time exactly
+   tau0.  The bisection stops at tau_upper - tau_lower <= tol_tau (CLASS's
+   tol_tau_approx, 1e-10).  Writes out (NULL to query) and returns the size, at
+   most 1e6, or -1 with a message. */
+int song2_tau_grid_class(const song2_tables *tab, double stepsize, double late_boost, double start_tau_c_over_tau_h,
+                         double tol_tau, int has_cmb, double *out, char *err);
 /* Comoving sound horizon int_0^tau c_s dtau', c_s^2 = 1/(3 (1 + 3 rho_b / 4 rho_g)),
    on the background table (CLASS's pth->rs_rec at tau = song2_recombination_time). */
 double song2_sound_horizon(const song2_tables *tab, double tau);

@@ -140,3 +140,109 @@ double song2_oracle_sound_horizon(const song2_tables *t, double tau) {
   }
   return u0 + s * h;
 }
+
+/* ------------------------------------------- source time sampling
+   perturb2_timesampling_for_sources without a custom grid
+   (source/perturbations2.c:2620-2869).  The splines of the background table are
+   evaluated here in polynomial form on each interval,
+   s(x) = y0 + c1 t + M0 t^2 / 2 + (M1 - M0) t^3 / (6 h), t = x - x_i, so that the
+   derivatives come from the coefficients rather than the product's a/b basis. */
+static void o_poly(const song2_tables *t, int col, double x, double *s, double *s1, double *s2) {
+  double h = t->bg_dlntau;
+  int i = (int)floor((x - t->bg_lntau0) / h);
+  if (i < 0) i = 0;
+  if (i > t->bg_size - 2) i = t->bg_size - 2;
+  double u = x - (t->bg_lntau0 + i * h);
+  double y0 = t->bg[(size_t)i * SONG2_BG_SIZE + col], y1 = t->bg[(size_t)(i + 1) * SONG2_BG_SIZE + col];
+  double m0 = t->bg_dd[(size_t)i * SONG2_BG_SIZE + col], m1 = t->bg_dd[(size_t)(i + 1) * SONG2_BG_SIZE + col];
+  double c1 = (y1 - y0) / h - h * (2 * m0 + m1) / 6, c2 = m0 / 2, c3 = (m1 - m0) / (6 * h);
+  *s = y0 + u * (c1 + u * (c2 + u * c3));
+  *s1 = c1 + u * (2 * c2 + 3 * c3 * u);
+  *s2 = 2 * c2 + 6 * c3 * u;
+}
+
+/* kappa' = dkappa/dtau, CLASS's thermodynamics variation rate
+   sqrt(kappa'^2 + (kappa''/kappa')^2 + |kappa'''/kappa'|), aH and a''/a at tau */
+void song2_oracle_thermo_rates(const song2_tables *t, double tau, double *out4) {
+  double x = log(tau), l, lx, lxx, h, hx, hxx;
+  o_poly(t, SONG2_BG_LN_KAPPA_DOT, x, &l, &lx, &lxx);
+  o_poly(t, SONG2_BG_LN_HC, x, &h, &hx, &hxx);
+  /* f(tau) = e^{l(ln tau)}: f'/f = lx/tau, f''/f = (lx^2 - lx + lxx)/tau^2 */
+  double kd = exp(l);
+  double r1 = lx / tau;                                   /* kappa''/kappa' */
+  double r2 = (lxx - lx + lx * lx) / (tau * tau);         /* kappa'''/kappa' */
+  double aH = exp(h);
+  out4[0] = kd;
+  out4[1] = sqrt(kd * kd + r1 * r1 + fabs(r2));
+  out4[2] = aH;
+  out4[3] = aH * hx / tau + aH * aH; /* a''/a = (aH)' + (aH)^2 */
+}
+
+/* visibility peak: the maximum of g = kappa' e^{-kappa} on a fine ln tau scan,
+   refined by parabolic steps (independent of the product's golden section) */
+static double o_tau_rec(const song2_tables *t) {
+  int n = 20000, best = 0;
+  double x0 = t->bg_lntau0, x1 = t->bg_lntau0 + (t->bg_size - 1) * t->bg_dlntau, bestv = -1e300;
+  double dx = (x1 - x0) / n;
+  for (int i = 0; i <= n; ++i) {
+    double x = x0 + i * dx, a, b, c, d, e, f;
+    o_poly(t, SONG2_BG_LN_KAPPA_DOT, x, &a, &b, &c);
+    o_poly(t, SONG2_BG_KAPPA, x, &d, &e, &f);
+    double v = a - d;
+    if (v > bestv) bestv = v, best = i;
+  }
+  double lo = x0 + (best - 1) * dx, hi = x0 + (best + 1) * dx;
+  for (int it = 0; it < 200; ++it) { /* ternary search on a unimodal bracket */
+    double m1 = lo + (hi - lo) / 3, m2 = hi - (hi - lo) / 3, a, b, c, d, e, f;
+    o_poly(t, SONG2_BG_LN_KAPPA_DOT, m1, &a, &b, &c);
+    o_poly(t, SONG2_BG_KAPPA, m1, &d, &e, &f);
+    double v1 = a - d;
+    o_poly(t, SONG2_BG_LN_KAPPA_DOT, m2, &a, &b, &c);
+    o_poly(t, SONG2_BG_KAPPA, m2, &d, &e, &f);
+    if (v1 < a - d) lo = m1;
+    else hi = m2;
+  }
+  return exp(0.5 * (lo + hi));
+}
+
+int song2_oracle_tau_grid_class(const song2_tables *t, double stepsize, double boost, double start, double tol,
+                                int has_cmb, int cap, double *out) {
+  double tau;
+  if (has_cmb) {
+    /* the thermodynamics table starts at z = 1e4: a = 1 / (1 + 1e4) */
+    double lo = t->bg_lntau0, hi = log(o_tau_rec(t));
+    for (int it = 0; it < 300; ++it) {
+      double mid = 0.5 * (lo + hi), a, b, c;
+      o_poly(t, SONG2_BG_LN_A, mid, &a, &b, &c);
+      if (a < -log(1.0 + 1e4)) lo = mid;
+      else hi = mid;
+    }
+    double tl = exp(0.5 * (lo + hi)), tu = o_tau_rec(t), r[4];
+    song2_oracle_thermo_rates(t, tl, r);
+    if (r[2] / r[0] > start) return -1;
+    song2_oracle_thermo_rates(t, tu, r);
+    if (r[2] / r[0] < start) return -1;
+    while (tu - tl > tol) {
+      double tm = 0.5 * (tl + tu);
+      song2_oracle_thermo_rates(t, tm, r);
+      if (r[2] / r[0] > start) tu = tm;
+      else tl = tm;
+    }
+    tau = 0.5 * (tl + tu);
+  } else {
+    tau = o_tau_rec(t);
+  }
+  int n = 0;
+  out[n++] = tau;
+  while (tau < t->tau0 && n < cap) {
+    double r[4];
+    song2_oracle_thermo_rates(t, tau, r);
+    double dt = has_cmb ? stepsize / sqrt(r[1] * r[1] + boost * boost * fabs(2 * r[3] - r[2] * r[2]))
+                        : stepsize / r[2];
+    tau += dt;
+    out[n++] = tau;
+  }
+  if (tau < t->tau0) return -1;
+  out[n - 1] = t->tau0;
+  return n;
+}

@@ -126,7 +126,8 @@ class Params(C.Structure):
                 ("k_step_super", C.c_double), ("k_logstep_super", C.c_double), ("k_step_transition", C.c_double),
                 ("k_per_decade_for_pk", C.c_double), ("k_per_decade_for_bao", C.c_double),
                 ("k_bao_center", C.c_double), ("k_bao_width", C.c_double), ("k_max_for_pk", C.c_double),
-                ("h", C.c_double), ("k3_size_min", C.c_int), ("has_cmb", C.c_int), ("has_lss", C.c_int)]
+                ("h", C.c_double), ("k3_size_min", C.c_int), ("has_cmb", C.c_int), ("has_lss", C.c_int),
+                ("tau_stepsize", C.c_double), ("tau_late_boost", C.c_double), ("tau_start_c_over_h", C.c_double)]
 
 
 SAMPLING_LIN, SAMPLING_LOG, SAMPLING_SMART, SAMPLING_SYM, SAMPLING_THETA12 = 0, 1, 2, 3, 4
@@ -209,6 +210,7 @@ SIGNATURES = {
     "song2_write_sources_k": (_I, [C.POINTER(Spec), C.POINTER(Tables), _PD, _I, _I, C.c_char_p, C.c_char_p]),
     "song2_write_sources_tau": (_I, [C.POINTER(Spec), C.POINTER(Tables), _PD, _I, C.c_char_p, C.c_char_p]),
     "song2_sound_horizon": (_D, [C.POINTER(Tables), _D]),
+    "song2_tau_grid_class": (_I, [C.POINTER(Tables), _D, _D, _D, _D, _I, _PD, C.c_char_p]),
     "song2_k_grid_smart": (_I, [C.POINTER(Params), _D, _D, _I, _PD, C.c_char_p]),
     "song2_k3_grids_smart": (_I, [_PD, _I, _I, _PI, _PD, C.c_char_p]),
     "song2_read_params": (_I, [C.c_char_p, C.c_char_p, C.POINTER(Spec), C.POINTER(Params), C.POINTER(LosSpec),

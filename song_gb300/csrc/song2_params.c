@@ -7,6 +7,7 @@
  * trimmed; the ini and pre files form one list and a name may appear only once.
  */
 #include <ctype.h>
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -150,6 +151,10 @@ void song2_params_defaults(song2_params *g) {
   g->k3_size_min = 5;
   g->has_cmb = 0;
   g->has_lss = 0;
+  /* input2.c:2278-2279; CLASS's precision default for the start */
+  g->tau_stepsize = 0.4;
+  g->tau_late_boost = 1;
+  g->tau_start_c_over_h = 0.008;
 }
 
 static int sampling(const char *v, const char *k, int *out, char *err) {
@@ -362,6 +367,14 @@ int song2_read_params(const char *ini_path, const char *pre_path, song2_spec *s,
       snprintf(err, SONG2_ERRLEN, "custom_tau_mode_song_sources = %.200s (lin or log)", v);
       return 1;
     }
+  }
+  /* input2.c:362-377 (the first key is the obsolete spelling) */
+  RD_D2("perturb_sampling_stepsize_for_2nd_order", "perturb_sampling_stepsize_song", g->tau_stepsize);
+  RD_D("perturb_sampling_late_time_boost", g->tau_late_boost);
+  RD_D("start_sources_at_tau_c_over_tau_h", g->tau_start_c_over_h);
+  if (g->tau_stepsize <= 0) {
+    snprintf(err, SONG2_ERRLEN, "perturb_sampling_stepsize_song = %g must be positive", g->tau_stepsize);
+    return 1;
   }
   if (g->custom_tau && g->tau_ini <= 0) {
     snprintf(err, SONG2_ERRLEN, "please choose 'tau_ini' greater than zero");
@@ -635,4 +648,108 @@ int song2_k3_grids_smart(const double *k, int k_size, int k3_size_min, int *k3_s
     }
   free(buf);
   return 0;
+}
+
+/* ---------------------------------------------------- source time grid */
+
+/* value and first two x-derivatives of a column's spline at x = ln tau */
+static void bg_d2(const song2_tables *t, int col, double x, double *v, double *d1, double *d2) {
+  double u = (x - t->bg_lntau0) / t->bg_dlntau;
+  int i = (int)floor(u);
+  if (i < 0) i = 0;
+  if (i > t->bg_size - 2) i = t->bg_size - 2;
+  double h = t->bg_dlntau, b = u - i, a = 1.0 - b;
+  const double *y0 = t->bg + (size_t)i * SONG2_BG_SIZE, *y1 = y0 + SONG2_BG_SIZE;
+  const double *q0 = t->bg_dd + (size_t)i * SONG2_BG_SIZE, *q1 = q0 + SONG2_BG_SIZE;
+  *v = a * y0[col] + b * y1[col] + ((a * a * a - a) * q0[col] + (b * b * b - b) * q1[col]) * h * h / 6.0;
+  *d1 = (y1[col] - y0[col]) / h - (3 * a * a - 1) / 6.0 * h * q0[col] + (3 * b * b - 1) / 6.0 * h * q1[col];
+  *d2 = a * q0[col] + b * q1[col];
+}
+
+/* kappa', CLASS's variation rate of the thermodynamics
+   sqrt(kappa1^2 + (kappa2 / kappa1)^2 + |kappa3 / kappa1|) with kappa1..3 the first
+   three conformal-time derivatives of the optical depth, from the spline of
+   s = ln kappa1 in x = ln tau; the conformal Hubble rate aH and a''/a */
+static void thermo_rates(const song2_tables *t, double tau, double *kd, double *rate, double *hc, double *app_a) {
+  double x = log(tau), s, sx, sxx;
+  bg_d2(t, SONG2_BG_LN_KAPPA_DOT, x, &s, &sx, &sxx);
+  /* d/dtau = (1/tau) d/dx: ds/dtau = sx / tau, d2s/dtau2 = (sxx - sx) / tau^2 */
+  double s1 = sx / tau, s2 = (sxx - sx) / (tau * tau);
+  double k1 = exp(s);
+  double k2 = k1 * s1;
+  double k3 = k1 * (s2 + s1 * s1);
+  *kd = k1;
+  *rate = sqrt(k1 * k1 + (k2 / k1) * (k2 / k1) + fabs(k3 / k1));
+  double lh, lhx, lhxx;
+  bg_d2(t, SONG2_BG_LN_HC, x, &lh, &lhx, &lhxx);
+  double H = exp(lh);        /* aH */
+  double Hp = H * lhx / tau; /* (aH)' */
+  *hc = H;
+  *app_a = Hp + H * H;       /* a''/a = (aH)' + (aH)^2 */
+}
+
+int song2_tau_grid_class(const song2_tables *t, double stepsize, double late_boost, double start_tau_c_over_tau_h,
+                         double tol_tau, int has_cmb, double *out, char *err) {
+  double tau_rec = song2_recombination_time(t);
+  double tau_ini;
+  if (has_cmb) {
+    /* the thermodynamics table's start: z = 1e4 (CLASS recfast_z_initial) */
+    double lo = t->bg_lntau0, hi = log(tau_rec), target = -log(1e4 + 1.0);
+    for (int it = 0; it < 200 && hi - lo > 1e-14; ++it) {
+      double mid = 0.5 * (lo + hi), v, d1, d2;
+      bg_d2(t, SONG2_BG_LN_A, mid, &v, &d1, &d2);
+      if (v < target) lo = mid;
+      else hi = mid;
+    }
+    double tau_lower = exp(0.5 * (lo + hi)), tau_upper = tau_rec, kd, rate, hc, app;
+    thermo_rates(t, tau_lower, &kd, &rate, &hc, &app);
+    if (hc / kd > start_tau_c_over_tau_h) {
+      snprintf(err, SONG2_ERRLEN, "start of the source sampling before the thermodynamics table (tau=%g)", tau_lower);
+      return -1;
+    }
+    thermo_rates(t, tau_upper, &kd, &rate, &hc, &app);
+    if (hc / kd < start_tau_c_over_tau_h) {
+      snprintf(err, SONG2_ERRLEN,
+               "start of the source sampling after recombination; decrease start_sources_at_tau_c_over_tau_h");
+      return -1;
+    }
+    double tau_mid = 0.5 * (tau_lower + tau_upper);
+    for (int it = 0; it < 400 && tau_upper - tau_lower > tol_tau; ++it) {
+      thermo_rates(t, tau_mid, &kd, &rate, &hc, &app);
+      if (hc / kd > start_tau_c_over_tau_h) tau_upper = tau_mid;
+      else tau_lower = tau_mid;
+      tau_mid = 0.5 * (tau_lower + tau_upper);
+    }
+    tau_ini = tau_mid;
+  } else {
+    tau_ini = tau_rec;
+  }
+  int n = 0;
+  double tau = tau_ini;
+  if (out) out[n] = tau;
+  ++n;
+  while (tau < t->tau0) {
+    double kd, rate, hc, app, timescale;
+    thermo_rates(t, tau, &kd, &rate, &hc, &app);
+    if (has_cmb) {
+      double isw2 = fabs(2 * app - hc * hc) * late_boost * late_boost;
+      timescale = 1 / sqrt(rate * rate + isw2);
+    } else {
+      timescale = 1 / hc;
+    }
+    double step = stepsize * timescale;
+    if (fabs(step / tau) < 10 * DBL_EPSILON) { /* CLASS's smallest_allowed_variation */
+      snprintf(err, SONG2_ERRLEN, "integration step = %e < machine precision", step);
+      return -1;
+    }
+    tau += step;
+    if (out) out[n] = tau;
+    ++n;
+    if (n + 1 > 1000000) {
+      snprintf(err, SONG2_ERRLEN, "source time sampling too large; check perturb_sampling_stepsize_song");
+      return -1;
+    }
+  }
+  if (out) out[n - 1] = t->tau0;
+  return n;
 }

@@ -243,3 +243,97 @@ def test_reader_grids_of_a_smart_preset(lib, tmp_path):
     errb = capi.errbuf()
     assert lib.song2_k3_grids_smart(capi.dptr(k), n, g.k3_size_min, capi.iptr(sz), None, errb) == 0
     assert min(int(sz[i1 * n + i2]) for i1 in range(n) for i2 in range(i1 + 1)) >= 2
+
+
+# ------------------------------------------------------- source time sampling
+
+def tau_grid(lib, p, step, boost, start, cmb):
+    import numpy as np
+    err = capi.errbuf()
+    n = lib.song2_tau_grid_class(C.byref(p.tables), step, boost, start, 1e-10, cmb, None, err)
+    assert n > 0, err.value
+    out = np.zeros(n)
+    assert lib.song2_tau_grid_class(C.byref(p.tables), step, boost, start, 1e-10, cmb, capi.dptr(out), err) == n
+    return out
+
+
+def oracle_tau(p, step, boost, start, cmb):
+    import numpy as np
+    ol = oracle_lib()
+    f = ol.song2_oracle_tau_grid_class
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(capi.Tables), C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                  C.POINTER(C.c_double)]
+    r = ol.song2_oracle_thermo_rates
+    r.restype = None
+    r.argtypes = [C.POINTER(capi.Tables), C.c_double, C.POINTER(C.c_double)]
+    out = np.zeros(1000000)
+    n = f(C.byref(p.tables), step, boost, start, 1e-10, cmb, out.size, capi.dptr(out))
+    assert n > 0
+
+    def rates(tau):
+        v = np.zeros(4)
+        r(C.byref(p.tables), tau, capi.dptr(v))
+        return v
+    return out[:n], rates
+
+
+@pytest.mark.parametrize("step,boost,start", [(0.4, 1.0, 0.008), (0.4, 16.0, 0.01), (1.5, 4.0, 0.02)])
+def test_source_time_grid_matches_oracle(lib, step, boost, start):
+    import numpy as np
+    from helpers import problem
+    p = problem()
+    tau = tau_grid(lib, p, step, boost, start, 1)
+    ref, rates = oracle_tau(p, step, boost, start, 1)
+    assert tau.size == ref.size
+    assert np.allclose(tau, ref, rtol=1e-10, atol=0)
+    assert np.all(np.diff(tau) > 0) and tau[-1] == p.tables.tau0
+    kd, _, aH, _ = rates(tau[0])
+    assert abs(aH / kd - start) < 1e-6 * start              # the bisection's root
+    # each step is stepsize / sqrt(rate^2 + boost^2 |2 a''/a - (aH)^2|) at the point before it
+    for i in range(0, tau.size - 2, max(1, tau.size // 50)):
+        _, rate, aH, app = rates(tau[i])
+        want = step / np.sqrt(rate ** 2 + boost ** 2 * abs(2 * app - aH ** 2))
+        assert abs((tau[i + 1] - tau[i]) - want) <= 1e-9 * want
+    # a later start and a larger boost give more points
+    assert tau.size > 20
+
+
+def test_source_time_grid_without_cmb(lib):
+    import numpy as np
+    from helpers import problem
+    p = problem()
+    tau = tau_grid(lib, p, 0.4, 1.0, 0.008, 0)
+    ref, rates = oracle_tau(p, 0.4, 1.0, 0.008, 0)
+    # the grid starts at the visibility peak, whose location a maximum search
+    # fixes only to about sqrt(machine epsilon)
+    assert tau.size == ref.size and np.allclose(tau, ref, rtol=1e-7, atol=0)
+    tr = lib.song2_recombination_time(C.byref(p.tables))
+    assert tau[0] == tr
+    # steps of stepsize / (aH): roughly logarithmic in tau
+    _, _, aH, _ = rates(tau[3])
+    assert abs((tau[4] - tau[3]) - 0.4 / aH) <= 1e-12 * tau[4]
+
+
+def test_source_time_grid_errors(lib):
+    from helpers import problem
+    p = problem()
+    err = capi.errbuf()
+    # a start after recombination: tau_c / tau_h at the visibility peak is far below 10
+    assert lib.song2_tau_grid_class(C.byref(p.tables), 0.4, 1.0, 10.0, 1e-10, 1, None, err) == -1
+    assert b"after recombination" in err.value
+    assert lib.song2_tau_grid_class(C.byref(p.tables), 0.4, 1.0, 1e-9, 1e-10, 1, None, err) == -1
+    assert b"thermodynamics table" in err.value
+
+
+def test_reader_source_time_sampling_keys(lib, tmp_path):
+    rc, s, g, ls, err = read(lib, tmp_path, "output = tBisp\n",
+                             "start_sources_at_tau_c_over_tau_h = 0.01\nperturb_sampling_stepsize_song = 0.3\n"
+                             "perturb_sampling_late_time_boost = 16\n")
+    assert rc == 0, err
+    assert (g.tau_start_c_over_h, g.tau_stepsize, g.tau_late_boost) == (0.01, 0.3, 16.0)
+    rc, s, g, ls, err = read(lib, tmp_path, "output = tBisp\n", "perturb_sampling_stepsize_for_2nd_order = 0.2\n")
+    assert rc == 0, err
+    assert (g.tau_start_c_over_h, g.tau_stepsize, g.tau_late_boost) == (0.008, 0.2, 1.0)
+    rc, *_, err = read(lib, tmp_path, "output = tBisp\n", "perturb_sampling_stepsize_song = 0\n")
+    assert rc == 1 and "positive" in err
