@@ -652,6 +652,69 @@ int song2_los_tables(song2_los *h, int *l1, double *j_l1, double *J, int *J_xmin
 int song2_gpu_transfer(const song2_spec *spec, const song2_los_spec *los, const double *sources_flat,
                        double *transfer_flat, char *err);
 
+/* ------------------------------------------------ intrinsic bispectrum
+   bispectra2_intrinsic_init and its integrals (bispectra2.c:300-3030): for every
+   second-order field X, azimuthal number M3 of the spec's m list and offset L3 =
+   |l3 - M3| + offset_L3 allowed by the parity, the k3 integral
+   I_l3(r,k1,k2) = 2 c_M3 int dk3 k3^2 j_L3(r k3) T^(2)_l3M3(k1,k2,k3), then for
+   every first-order field Y the k2 integral of I_l3, interpolated in k2 onto the
+   first-order grid q with the window 1/k^2, times P(q) T^(1)_l2(q) j_l2(r q);
+   for every even offset L1 = |l1 - M3| + offset_L1 and field Z the k1 integral
+   with j_L1(r q) T^(1)_l1(q) P(q), the r integral int dr r^2, and the
+   geometrical factors (four 3j symbols and a 6j symbol); the result is
+   symmetrised over the position of the second-order field
+   (bispectra2.c:760-790).  All integrals are trapezoidal on the grids given,
+   j_l from the line-of-sight handle's Bessel table (bessel2_convolution,
+   bessel2.c:499-600).
+
+   Fields are the transfer types SONG2_TT_T, _E, _B; the field parity (0 for T
+   and E, 1 for B) of the last field combination governs every combination, as
+   the reference sets it once (bispectra2.c:967).  With an m list of {0} only,
+   the reduced bispectrum is 8/pi^3 times the integral for every (l1, l2, l3)
+   (bispectra2.c:2824-2832).
+
+   Output layout: [X][Y][Z][conf] doubles (bf_size^3 * n_conf), conf running
+   over index_l1 ascending, index_l2 <= index_l1 and index_l3 from the first l
+   >= |l1 - l2| to min(index_l2, the last l <= l1 + l2), as song2_bispectra_configs
+   lists them (the reference's loop order at bispectra2.c:760-764). */
+typedef struct {
+  int bf_size;                /* fields (pbi->bf_size) */
+  const int *bf;              /* SONG2_TT_T / _E / _B each, distinct */
+  int r_size;                 /* integration grid in r (pwb->r), ascending, positive */
+  const double *r;
+  int q_size;                 /* first-order transfer grid (ptr->q), ascending, within the spec's k range */
+  const double *q;
+  const double *pk;           /* primordial spectrum on q (pbi->pk) */
+  const double *transfer1;    /* first-order transfers [bf][index_l][q] on the line-of-sight l list
+                                 (ptr->transfer, scalar adiabatic) */
+  int k1_interpolation;       /* transfers_k1_interpolation: SONG2_INTERP_LINEAR / _CUBIC */
+  int k2_interpolation;       /* transfers_k2_interpolation */
+} song2_bispectra_spec;
+/* The (index_l1, index_l2, index_l3) configurations of the output, in order
+   (any array may be NULL); returns their number. */
+int64_t song2_bispectra_configs(int l_size, const int *l, int *i1, int *i2, int *i3);
+typedef struct song2_bispectra song2_bispectra;
+/* Binds a bispectrum run to a line-of-sight handle (its l list, transfer k grids,
+   transfer types and Bessel table) and uploads the first-order inputs. */
+int song2_bispectra_create(song2_los *los, const song2_bispectra_spec *bs, song2_bispectra **out, char *err);
+void song2_bispectra_destroy(song2_bispectra *h);
+/* Doubles of the output (bf_size^3 * n_conf). */
+int64_t song2_bispectra_size(const song2_bispectra *h);
+/* The bispectra of device-resident second-order transfers (the flat layout of
+   song2_los_run) into out_dev (song2_bispectra_size() doubles), on `stream`
+   (NULL = legacy default stream); returns when the result is complete. */
+int song2_bispectra_run(song2_bispectra *h, const double *transfer2_dev, double *out_dev, void *stream, char *err);
+/* Device time (ms) of the last song2_bispectra_run. */
+float song2_bispectra_last_ms(const song2_bispectra *h);
+/* One shot: host second-order transfers in the flat layout to host bispectra. */
+int song2_gpu_bispectra(const song2_spec *spec, const song2_los_spec *los, const song2_bispectra_spec *bs,
+                        const double *transfer2_flat, double *out, char *err);
+/* bispectra2_add_quadratic_corrections (bispectra2.c:3031-3106): adds to the
+   intrinsic bispectrum -3/8 of the quadratic bispectrum (bolometric temperature)
+   and, with use_delta_tilde, +4/8 of it (the redshift term the delta-tilde
+   sources absorb); b and b_quadratic share the output layout. */
+void song2_bispectra_add_quadratic(double *b, const double *b_quadratic, int64_t n, int use_delta_tilde);
+
 #ifdef __cplusplus
 }
 #endif

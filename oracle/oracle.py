@@ -73,6 +73,11 @@ def load():
         lib.song2_oracle_transfer_pairs.restype = C.c_int
         lib.song2_oracle_transfer_pairs.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_double),
                                                     C.POINTER(C.c_double), C.c_int, C.c_int, C.c_int, C.c_char_p]
+        lib.song2_oracle_wigner6j.restype = C.c_double
+        lib.song2_oracle_wigner6j.argtypes = [C.c_int] * 6
+        lib.song2_oracle_bispectra.restype = C.c_int
+        lib.song2_oracle_bispectra.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(capi.BispectraSpec),
+                                               C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_char_p]
         lib.song2_oracle_transfer.restype = C.c_int
         lib.song2_oracle_transfer.argtypes = [C.POINTER(capi.Spec), LS, C.POINTER(C.c_double),
                                               C.POINTER(C.c_double), C.c_int, C.c_char_p]
@@ -137,6 +142,18 @@ def transfer(prob, los, sources, n_out, nthreads=0, pairs=None):
     lo, hi = pairs if pairs is not None else (0, 1 << 30)
     if load().song2_oracle_transfer_pairs(C.byref(prob.spec), C.byref(los), capi.dptr(src), capi.dptr(out), lo, hi,
                                           nthreads or (os.cpu_count() or 1), err):
+        raise RuntimeError(err.value.decode())
+    return out
+
+
+def bispectra(prob, los, bs, transfer2, n_out):
+    """Symmetrised intrinsic bispectra [X][Y][Z][conf] of flat second-order transfers."""
+    from song_gb300 import capi
+    out = np.zeros(n_out)
+    err = capi.errbuf()
+    t2 = np.ascontiguousarray(transfer2, dtype=np.float64)
+    if load().song2_oracle_bispectra(C.byref(prob.spec), C.byref(los), C.byref(bs), capi.dptr(t2), capi.dptr(out),
+                                     err):
         raise RuntimeError(err.value.decode())
     return out
 

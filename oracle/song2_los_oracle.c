@@ -828,3 +828,420 @@ int song2_oracle_transfer(const song2_spec *s, const song2_los_spec *los, const 
                           int nthreads, char *err) {
   return song2_oracle_transfer_pairs(s, los, sources, out, 0, 1 << 30, nthreads, err);
 }
+
+/* ================================================== intrinsic bispectrum
+   bispectra2_intrinsic_init and its integrals, in the reference's order
+   (bispectra2.c:300-3030): for each second-order field X, M3 of the m list
+   and parity-allowed offset_L3, the k3 integral on every (l3, r, k1, k2 <= k1)
+   (bispectra2_intrinsic_integrate_over_k3, :1107-1447); for each field Y the
+   interpolation of I_l3 in k2 onto q (bispectra2_interpolate_over_k2,
+   :1448-1612) and its Bessel convolution with T1_l2 (:1613-1849); for each
+   even offset_L1 and field Z the interpolation in k1 (:1850-1994), the
+   convolution with T1_l1 (:1995-2292), the r integral (:2293-2455) and the
+   geometrical factors (:2456-2880); then the symmetrisation (:760-790).
+   The first-order convolution uses the same Bessel table (CLASS's bessel
+   module is absent from the reference tree).  3j and 6j symbols by Racah's
+   formulas in long double (the reference calls SLATEC's drc3jj/drc6j). */
+
+static long double o_lfl(int n) { return lgammal((long double)n + 1.0L); }
+
+static int o_tri(int a, int b, int c) { return c >= abs(a - b) && c <= a + b; }
+
+static long double o_w3j000(int a, int b, int c) {
+  if (!o_tri(a, b, c)) return 0;
+  int J = a + b + c;
+  if (J % 2) return 0;
+  int g = J / 2;
+  long double v = expl(0.5L * (o_lfl(J - 2 * a) + o_lfl(J - 2 * b) + o_lfl(J - 2 * c) - o_lfl(J + 1)) + o_lfl(g) -
+                       o_lfl(g - a) - o_lfl(g - b) - o_lfl(g - c));
+  return (g % 2) ? -v : v;
+}
+
+static long double o_w3j(int j1, int j2, int j3, int m1, int m2, int m3) {
+  if (m1 + m2 + m3 != 0 || !o_tri(j1, j2, j3) || abs(m1) > j1 || abs(m2) > j2 || abs(m3) > j3) return 0;
+  if (m1 == 0 && m2 == 0) return o_w3j000(j1, j2, j3);
+  long double pre = 0.5L * (o_lfl(j1 + j2 - j3) + o_lfl(j1 - j2 + j3) + o_lfl(-j1 + j2 + j3) -
+                            o_lfl(j1 + j2 + j3 + 1) + o_lfl(j1 + m1) + o_lfl(j1 - m1) + o_lfl(j2 + m2) +
+                            o_lfl(j2 - m2) + o_lfl(j3 + m3) + o_lfl(j3 - m3));
+  int lo = 0, hi = j1 + j2 - j3;
+  if (j2 - j3 - m1 > lo) lo = j2 - j3 - m1;
+  if (j1 - j3 + m2 > lo) lo = j1 - j3 + m2;
+  if (j1 - m1 < hi) hi = j1 - m1;
+  if (j2 + m2 < hi) hi = j2 + m2;
+  long double s = 0;
+  for (int k = lo; k <= hi; ++k) {
+    long double v = expl(pre - (o_lfl(k) + o_lfl(j3 - j2 + k + m1) + o_lfl(j3 - j1 + k - m2) +
+                                o_lfl(j1 + j2 - j3 - k) + o_lfl(j1 - k - m1) + o_lfl(j2 - k + m2)));
+    s += (k % 2) ? -v : v;
+  }
+  return ((j1 - j2 - m3) % 2) ? -s : s;
+}
+
+static long double o_ldelta(int a, int b, int c) {
+  return o_lfl(a + b - c) + o_lfl(a - b + c) + o_lfl(-a + b + c) - o_lfl(a + b + c + 1);
+}
+
+/* {a b c; d e f} */
+long double song2_oracle_wigner6j_l(int a, int b, int c, int d, int e, int f) {
+  if (!o_tri(a, b, c) || !o_tri(a, e, f) || !o_tri(d, b, f) || !o_tri(d, e, c)) return 0;
+  long double ld = 0.5L * (o_ldelta(a, b, c) + o_ldelta(a, e, f) + o_ldelta(d, b, f) + o_ldelta(d, e, c));
+  int lo = a + b + c;
+  if (a + e + f > lo) lo = a + e + f;
+  if (d + b + f > lo) lo = d + b + f;
+  if (d + e + c > lo) lo = d + e + c;
+  int hi = a + b + d + e;
+  if (b + c + e + f < hi) hi = b + c + e + f;
+  if (c + a + f + d < hi) hi = c + a + f + d;
+  long double s = 0;
+  for (int t = lo; t <= hi; ++t) {
+    long double v = expl(ld + o_lfl(t + 1) -
+                         (o_lfl(t - a - b - c) + o_lfl(t - a - e - f) + o_lfl(t - d - b - f) + o_lfl(t - d - e - c) +
+                          o_lfl(a + b + d + e - t) + o_lfl(b + c + e + f - t) + o_lfl(c + a + f + d - t)));
+    s += (t % 2) ? -v : v;
+  }
+  return s;
+}
+
+double song2_oracle_wigner6j(int a, int b, int c, int d, int e, int f) {
+  return (double)song2_oracle_wigner6j_l(a, b, c, d, e, f);
+}
+
+typedef struct {
+  const o_tables *t;
+  double x_step;
+  double **ddj;  /* cubic */
+  int cubic;
+  int bad;
+} o_bes;
+
+/* bessel2_convolution (bessel2.c:499-600) */
+static double o_convolve(o_bes *B, const double *kk, const double *dk, int n, const double *f, const double *g, int L,
+                         double r) {
+  const o_tables *t = B->t;
+  int row = t->l1_index[L];
+  double xmin = t->jneg[row] ? t->xx[t->x_size - 1] : t->xx[t->jxmin[row]];
+  int nx = t->jneg[row] ? 1 : t->x_size - t->jxmin[row];
+  double s = 0;
+  for (int i = 0; i < n; ++i) {
+    double fv = f[i];
+    if (fv == 0.) continue;
+    double gv = 1.;
+    if (g) {
+      gv = g[i];
+      if (gv == 0.) continue;
+    }
+    double k = kk[i], x = k * r;
+    if (x < xmin) continue;
+    int ix = (int)((x - xmin) / B->x_step);
+    if (ix + 1 >= nx) {
+      B->bad = 1;
+      continue;
+    }
+    double a = (xmin + B->x_step * (ix + 1) - x) / B->x_step;
+    const double *jr = t->j[row];
+    double j;
+    if (!B->cubic) {
+      j = a * jr[ix] + (1. - a) * jr[ix + 1];
+    } else {
+      const double *dd = B->ddj[row];
+      j = a * jr[ix] + (1. - a) * (jr[ix + 1] - a * ((a + 1.) * dd[ix] + (2. - a) * dd[ix + 1]) * B->x_step *
+                                                    B->x_step / 6.0);
+    }
+    s += k * k * j * fv * gv * dk[i];
+  }
+  return 0.5 * s;
+}
+
+static void o_trap(const double *x, int n, double *d) {
+  d[0] = x[1] - x[0];
+  for (int i = 1; i < n - 1; ++i) d[i] = x[i + 1] - x[i - 1];
+  d[n - 1] = x[n - 1] - x[n - 2];
+}
+
+/* interpolation of f (times the window 1/k^2) from the k grid onto q, times q^2
+   and P(q) (bispectra2_interpolate_over_k2/k1) */
+static int o_interp_k(const double *k, int K, double *f, int cubic, const double *q, int Q, const double *pk,
+                      double *out) {
+  double *spl = NULL;
+  if (cubic) {
+    spl = (double *)malloc(sizeof(double) * K);
+    o_spline(k, f, K, 1, spl);
+  }
+  int ik = 0;
+  double h = k[1] - k[0];
+  for (int iq = 0; iq < Q; ++iq) {
+    while (ik + 1 < K && k[ik + 1] < q[iq]) {
+      ik++;
+      h = k[ik + 1] - k[ik];
+    }
+    if (ik + 1 >= K) {
+      free(spl);
+      return 1;
+    }
+    double b = (q[iq] - k[ik]) / h, a = 1. - b;
+    double v = a * f[ik] + b * f[ik + 1];
+    if (cubic) v += ((a * a * a - a) * spl[ik] + (b * b * b - b) * spl[ik + 1]) * h * h / 6.0;
+    v *= q[iq] * q[iq];
+    v *= pk[iq];
+    out[iq] = v;
+  }
+  free(spl);
+  return 0;
+}
+
+int song2_oracle_bispectra(const song2_spec *s, const song2_los_spec *los, const song2_bispectra_spec *bs,
+                           const double *T2, double *out, char *err) {
+  o_tables t;
+  if (o_build_tables(s, los, &t, err)) return 1;
+  o_bes B = {&t, los->x_step, NULL, los->bessel_interpolation == SONG2_INTERP_CUBIC, 0};
+  if (B.cubic) {
+    B.ddj = (double **)calloc(t.n_l1, sizeof(double *));
+    for (int r = 0; r < t.n_l1; ++r) {
+      int n = t.jneg[r] ? 1 : t.x_size - t.jxmin[r];
+      B.ddj[r] = (double *)calloc(n, sizeof(double));
+      if (n >= 3) o_spline(t.xx + t.jxmin[r], t.j[r], n, 0, B.ddj[r]);
+    }
+  }
+  const int L = los->l_size, R = bs->r_size, Q = bs->q_size, K = s->k_size, bf = bs->bf_size;
+  const int *l = los->l;
+  int n_pairs = K * (K + 1) / 2;
+  int *ksz = (int *)malloc(sizeof(int) * n_pairs);
+  int64_t nu = song2_oracle_transfer_k_grids(s, los, ksz, NULL, NULL, NULL, err);
+  double *kall = (double *)malloc(sizeof(double) * nu), *dkall = (double *)malloc(sizeof(double) * nu);
+  song2_oracle_transfer_k_grids(s, los, NULL, NULL, NULL, kall, err);
+  int64_t *uoff = (int64_t *)malloc(sizeof(int64_t) * n_pairs);
+  {
+    int64_t o = 0;
+    for (int p = 0; p < n_pairs; ++p) {
+      uoff[p] = o;
+      o_trap(kall + o, ksz[p], dkall + o);
+      o += ksz[p];
+    }
+  }
+  /* transfer types: T, E, B blocks; (l, m <= l) inside (transfer2_get_lm_lists) */
+  int has[3] = {s->has_source_T, s->has_source_E, s->has_source_B};
+  int tt_base[3] = {0, 0, 0}, per_type = 0;
+  for (int il = 0; il < L; ++il) per_type += o_index_m_max(s, l[il]) + 1;
+  {
+    int b = 0;
+    for (int f = 0; f < 3; ++f)
+      if (has[f]) {
+        tt_base[f] = b;
+        b += per_type;
+      }
+  }
+  int *lm_off = (int *)malloc(sizeof(int) * L);
+  {
+    int o = 0;
+    for (int il = 0; il < L; ++il) {
+      lm_off[il] = o;
+      o += o_index_m_max(s, l[il]) + 1;
+    }
+  }
+  /* triangles */
+  int *tmin = (int *)malloc(sizeof(int) * L * L), *tmax = (int *)malloc(sizeof(int) * L * L);
+  for (int a = 0; a < L; ++a)
+    for (int b = 0; b < L; ++b) {
+      int lo = 0, hi = L - 1;
+      while (lo < L && l[lo] < abs(l[a] - l[b])) lo++;
+      while (hi >= 0 && l[hi] > l[a] + l[b]) hi--;
+      tmin[a * L + b] = lo;
+      tmax[a * L + b] = hi;
+    }
+  /* grids */
+  const double *kp = s->k, *q = bs->q, *r = bs->r;
+  double *dq = (double *)malloc(sizeof(double) * Q), *dr = (double *)malloc(sizeof(double) * R);
+  o_trap(q, Q, dq);
+  o_trap(r, R, dr);
+  int m_max = 0;
+  for (int i = 0; i < s->m_size; ++i)
+    if (s->m[i] > m_max) m_max = s->m[i];
+  int fpar[3] = {0, 0, 1};
+  int parity = (3 * fpar[bs->bf[bf - 1]]) % 2;  /* set once, from the last combination (bispectra2.c:967) */
+  /* unsymmetrised bispectrum U[X][Y][Z][a][b][c - tmin(a, b)], c up to L */
+  size_t ucount = (size_t)bf * bf * bf * L * L * L;
+  double *U = (double *)calloc(ucount, sizeof(double));
+#define UIDX(X, Y, Z, a, b, c) (((((size_t)((X) * bf + (Y)) * bf + (Z)) * L + (a)) * L + (b)) * L + (c))
+  double *I3 = (double *)malloc(sizeof(double) * (size_t)L * R * K * K);
+  double *I2 = (double *)malloc(sizeof(double) * (size_t)L * L * R * K);
+  double *I1 = (double *)malloc(sizeof(double) * (size_t)L * L * L * R);
+  double *Ir = (double *)malloc(sizeof(double) * (size_t)L * L * L);
+  double *f = (double *)malloc(sizeof(double) * K), *ip = (double *)malloc(sizeof(double) * Q);
+  int rc = 0;
+  for (int X = 0; X < bf && !rc; ++X)
+    for (int im = 0; im < s->m_size && !rc; ++im) {
+      int M3 = s->m[im];
+      double fa = 1, f2a = 1;
+      for (int c = M3; c > 0; --c) fa *= c;
+      for (int c = 2 * M3; c > 0; --c) f2a *= c;
+      double coef = pow(2., M3) * fa / sqrt(f2a);
+      for (int oL3 = 0; oL3 < 2 * M3 + 1 && !rc; ++oL3) {
+        if (parity == 0 ? (oL3 % 2 != 0) : (oL3 % 2 == 0)) continue;
+        /* k3 */
+        memset(I3, 0, sizeof(double) * (size_t)L * R * K * K);
+        for (int il3 = 0; il3 < L; ++il3) {
+          int l3 = l[il3], L3 = abs(l3 - M3) + oL3;
+          if (M3 > l3 || L3 > l3 + M3) continue;
+          int tt = tt_base[bs->bf[X]] + lm_off[il3] + im;
+          int p = 0;
+          for (int k1 = 0; k1 < K; ++k1)
+            for (int k2 = 0; k2 <= k1; ++k2, ++p) {
+              const double *T = T2 + (size_t)tt * nu + uoff[p];
+              for (int ir = 0; ir < R; ++ir) {
+                double v = o_convolve(&B, kall + uoff[p], dkall + uoff[p], ksz[p], T, NULL, L3, r[ir]);
+                if (M3 != 0) v *= coef;
+                v *= 2;
+                I3[(((size_t)il3 * R + ir) * K + k1) * K + k2] = v;
+              }
+            }
+        }
+        for (int Y = 0; Y < bf && !rc; ++Y) {
+          /* k2 */
+          memset(I2, 0, sizeof(double) * (size_t)L * L * R * K);
+          for (int ir = 0; ir < R && !rc; ++ir)
+            for (int il3 = 0; il3 < L && !rc; ++il3) {
+              if (M3 > l[il3]) continue;
+              for (int k1 = 0; k1 < K && !rc; ++k1) {
+                for (int k2 = 0; k2 < K; ++k2) {
+                  if (k1 > k2) f[k2] = I3[(((size_t)il3 * R + ir) * K + k1) * K + k2];
+                  else f[k2] = I3[(((size_t)il3 * R + ir) * K + k2) * K + k1] * pow(-kp[k1] / kp[k2], M3);
+                  f[k2] *= 1 / pow(kp[k2], 2);
+                }
+                if (o_interp_k(kp, K, f, bs->k2_interpolation == SONG2_INTERP_CUBIC, q, Q, bs->pk, ip)) {
+                  snprintf(err, SONG2_ERRLEN, "q beyond the largest k");
+                  rc = 1;
+                  break;
+                }
+                for (int il2 = 0; il2 < L; ++il2) {
+                  const double *T1 = bs->transfer1 + ((size_t)Y * L + il2) * Q;
+                  I2[(((size_t)il3 * L + il2) * R + ir) * K + k1] = o_convolve(&B, q, dq, Q, ip, T1, l[il2], r[ir]);
+                }
+              }
+            }
+          for (int oL1 = 0; oL1 < 2 * M3 + 1 && !rc; ++oL1) {
+            if (oL1 % 2 != 0) continue;
+            for (int Z = 0; Z < bf && !rc; ++Z) {
+              /* k1 */
+              for (int ir = 0; ir < R && !rc; ++ir)
+                for (int il3 = 0; il3 < L && !rc; ++il3) {
+                  if (M3 > l[il3]) continue;
+                  for (int il2 = 0; il2 < L && !rc; ++il2) {
+                    int a = tmin[il3 * L + il2], b = tmax[il3 * L + il2];
+                    if (b < a) continue;
+                    for (int k1 = 0; k1 < K; ++k1)
+                      f[k1] = I2[(((size_t)il3 * L + il2) * R + ir) * K + k1] * (1 / pow(kp[k1], 2));
+                    if (o_interp_k(kp, K, f, bs->k1_interpolation == SONG2_INTERP_CUBIC, q, Q, bs->pk, ip)) {
+                      snprintf(err, SONG2_ERRLEN, "q beyond the largest k");
+                      rc = 1;
+                      break;
+                    }
+                    for (int il1 = a; il1 <= b; ++il1) {
+                      int l1 = l[il1], L1 = abs(l1 - M3) + oL1;
+                      double v = 0;
+                      if (L1 <= l1 + M3) {
+                        const double *T1 = bs->transfer1 + ((size_t)Z * L + il1) * Q;
+                        v = o_convolve(&B, q, dq, Q, ip, T1, L1, r[ir]);
+                      }
+                      I1[(((size_t)il3 * L + il2) * L + il1) * R + ir] = v;
+                    }
+                  }
+                }
+              /* r */
+              for (int il3 = 0; il3 < L; ++il3)
+                for (int il2 = 0; il2 < L; ++il2)
+                  for (int il1 = tmin[il3 * L + il2]; il1 <= tmax[il3 * L + il2]; ++il1) {
+                    const double *I = I1 + (((size_t)il3 * L + il2) * L + il1) * R;
+                    double sum = 0;
+                    for (int ir = 0; ir < R; ++ir) {
+                      double v = r[ir] * r[ir] * I[ir];
+                      if (v == 0.) continue;
+                      sum += v * dr[ir];
+                    }
+                    Ir[((size_t)il3 * L + il2) * L + il1] = 0.5 * sum;
+                  }
+              /* geometry */
+              for (int il3 = 0; il3 < L; ++il3) {
+                int l3 = l[il3], L3 = abs(l3 - M3) + oL3;
+                if (L3 > l3 + M3 || M3 > l3) continue;
+                long double F3 = o_w3j(L3, M3, l3, 0, -M3, M3), S3 = F3;
+                if (M3 != 0) {
+                  long double sg = (oL3 % 2) ? -1 : 1;
+                  S3 = parity == 0 ? F3 + sg * F3 : F3 - sg * F3;
+                }
+                for (int il2 = 0; il2 < L; ++il2) {
+                  int l2 = l[il2];
+                  for (int il1 = tmin[il3 * L + il2]; il1 <= tmax[il3 * L + il2]; ++il1) {
+                    int l1 = l[il1], L1 = abs(l1 - M3) + oL1;
+                    if (L1 > l1 + M3) continue;
+                    if (!o_tri(L1, l2, L3)) continue;
+                    int even_conf = ((l1 + l2 + l3) % 2 == 0);
+                    long double F123 = o_w3j000(l1, l2, l3), FL1 = o_w3j000(L1, l2, L3),
+                                F1 = o_w3j000(L1, l1, M3), F6 = song2_oracle_wigner6j_l(L1, L3, l2, l3, l1, M3);
+                    double integral = Ir[((size_t)il3 * L + il2) * L + il1];
+                    long double pref = parity == 0
+                                           ? 8 / (O_PI * O_PI * O_PI) * (2 * L1 + 1.) * (2 * L3 + 1.)
+                                           : -0.5 / (4 * O_PI * O_PI * O_PI * O_PI) * (2 * L1 + 1.) * (2 * L3 + 1.) *
+                                                 (2 * l1 + 1) * (2 * l2 + 1);
+                    long double geo = S3 * F1 * FL1 * F6;
+                    if (parity == 0 && even_conf) geo /= F123;
+                    int ex = parity == 0 ? l3 + L3 - l1 - L1 : l3 + L3 - l1 - L1 - 1;
+                    double sg = ((ex / 2) % 2 == 0) ? 1 : -1;
+                    double *dst = U + UIDX(X, Y, Z, il3, il2, il1);
+                    if (parity == 0 && m_max == 0) *dst = 8 / (O_PI * O_PI * O_PI) * integral;
+                    else *dst += (double)(sg * pref * geo * integral);
+                  }
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  if (!rc && B.bad) {
+    snprintf(err, SONG2_ERRLEN, "a Bessel argument fell outside the table");
+    rc = 1;
+  }
+  if (!rc) {
+    /* symmetrisation over the position of the second-order field */
+    int64_t n = 0;
+    for (int a = 0; a < L; ++a)
+      for (int b = 0; b <= a; ++b) {
+        int lo = tmin[a * L + b], hi = tmax[a * L + b] < b ? tmax[a * L + b] : b;
+        for (int c = lo; c <= hi; ++c) ++n;
+      }
+    int64_t ci = 0;
+    for (int a = 0; a < L; ++a)
+      for (int b = 0; b <= a; ++b) {
+        int lo = tmin[a * L + b], hi = tmax[a * L + b] < b ? tmax[a * L + b] : b;
+        for (int c = lo; c <= hi; ++c, ++ci)
+          for (int X = 0; X < bf; ++X)
+            for (int Y = 0; Y < bf; ++Y)
+              for (int Z = 0; Z < bf; ++Z)
+                out[((size_t)(X * bf + Y) * bf + Z) * n + ci] =
+                    U[UIDX(X, Y, Z, a, b, c)] + U[UIDX(Y, X, Z, b, a, c)] + U[UIDX(Z, Y, X, c, b, a)];
+      }
+  }
+#undef UIDX
+  free(U);
+  free(I3);
+  free(I2);
+  free(I1);
+  free(Ir);
+  free(f);
+  free(ip);
+  free(dq);
+  free(dr);
+  free(tmin);
+  free(tmax);
+  free(lm_off);
+  free(ksz);
+  free(kall);
+  free(dkall);
+  free(uoff);
+  if (B.ddj) {
+    for (int rr = 0; rr < t.n_l1; ++rr) free(B.ddj[rr]);
+    free(B.ddj);
+  }
+  o_free_tables(&t);
+  return rc;
+}

@@ -25,7 +25,7 @@ C_SOURCES = ["song2_host.c", "song2_transfer_host.c", "song2_params.c", "song2_o
 CU_SOURCES = ["song2_k_block_f.cu", "song2_k_block_d.cu", "song2_k_class_f.cu", "song2_k_class_d.cu",
               "song2_k_class2_f.cu", "song2_k_class2_d.cu", "song2_k_block2_f.cu", "song2_k_block2_d.cu",
               "song2_k_warp_f.cu", "song2_k_warp_d.cu", "song2_k_team_f.cu", "song2_k_team_d.cu",
-              "song2_launch.cu", "song2_capi.cu", "song2_los.cu"]
+              "song2_launch.cu", "song2_capi.cu", "song2_los.cu", "song2_bispectra.cu"]
 
 
 def _nvcc():

@@ -110,6 +110,17 @@ class LosSpec(C.Structure):
     ]
 
 
+class BispectraSpec(C.Structure):
+    """song2_bispectra_spec: fields, r and q grids, P(q) and the first-order transfers."""
+    _fields_ = [
+        ("bf_size", C.c_int), ("bf", C.POINTER(C.c_int)),
+        ("r_size", C.c_int), ("r", C.POINTER(C.c_double)),
+        ("q_size", C.c_int), ("q", C.POINTER(C.c_double)),
+        ("pk", C.POINTER(C.c_double)), ("transfer1", C.POINTER(C.c_double)),
+        ("k1_interpolation", C.c_int), ("k2_interpolation", C.c_int),
+    ]
+
+
 K3_SAMPLING_CLASS, K3_SAMPLING_BESSEL = 0, 1
 TAU_SAMPLING_SOURCES, TAU_SAMPLING_CUSTOM, TAU_SAMPLING_BESSEL = 0, 1, 2
 INTERP_LINEAR, INTERP_CUBIC = 0, 1
@@ -229,6 +240,15 @@ SIGNATURES = {
     "song2_los_table_sizes": (None, [_P, _PI, _PI, _PI, _PI, _PI]),
     "song2_los_tables": (_I, [_P, _PI, _PD, _PD, _PI, C.c_char_p]),
     "song2_gpu_transfer": (_I, [C.POINTER(Spec), C.POINTER(LosSpec), _PD, _PD, C.c_char_p]),
+    "song2_bispectra_configs": (C.c_int64, [_I, _PI, _PI, _PI, _PI]),
+    "song2_bispectra_create": (_I, [_P, C.POINTER(BispectraSpec), C.POINTER(_P), C.c_char_p]),
+    "song2_bispectra_destroy": (None, [_P]),
+    "song2_bispectra_size": (C.c_int64, [_P]),
+    "song2_bispectra_run": (_I, [_P, _P, _P, _P, C.c_char_p]),
+    "song2_bispectra_last_ms": (C.c_float, [_P]),
+    "song2_gpu_bispectra": (_I, [C.POINTER(Spec), C.POINTER(LosSpec), C.POINTER(BispectraSpec), _PD, _PD,
+                                 C.c_char_p]),
+    "song2_bispectra_add_quadratic": (None, [_PD, _PD, C.c_int64, _I]),
 }
 
 

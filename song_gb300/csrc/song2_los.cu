@@ -30,6 +30,7 @@
 
 #include "song2.h"
 #include "song2_los.h"
+#include "song2_los_view.h"
 
 #define CKL(x)                                                                                     \
   do {                                                                                             \
@@ -584,6 +585,10 @@ struct song2_los {
   int x_size = 0, L_size = 0, m_size = 0, n_rows = 0, n_l1 = 0, n_tt = 0, n_pairs = 0, n_rows_src = 0;
   long long n_units = 0, per_type = 0;
   std::vector<int> l1;
+  std::vector<int> jxmin, unit_size;  // host copies for the bispectrum integrals
+  std::vector<double> unit_k;
+  const double *d_unit_k = nullptr;
+  double *d_ddj = nullptr;            // j_l1 spline table (cubic Bessel interpolation in the bispectrum)
   std::vector<void *> allocs;
   double *d_jtab = nullptr, *d_J = nullptr, *d_ddJ = nullptr, *d_ddk = nullptr, *d_grid = nullptr;
   int *d_Jxmin = nullptr, *d_status = nullptr, *d_queue = nullptr;
@@ -702,6 +707,7 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
   for (int r = 0; r < h->n_l1; ++r) l1_index[h->l1[r]] = r;
   std::vector<int> jxmin(h->n_l1);
   for (int r = 0; r < h->n_l1; ++r) jxmin[r] = s2los_bessel_xmin(h->l1[r], &h->los, h->x_size, x_max);
+  h->jxmin = jxmin;
 
   // ---- projection rows (bessel2_J_for_Llm)
   const bool needT = s.has_source_T, needP = s.has_source_E || s.has_source_B;
@@ -1008,6 +1014,9 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
       dev_upload(h, tt_msign, &p_tt_msign, err) || dev_upload(h, tt_ndir, &p_tt_ndir, err) ||
       dev_upload(h, tt_xmin, &p_tt_xmin, err))
     return fail();
+  h->unit_k = unit_k;
+  h->unit_size = ksz;
+  h->d_unit_k = p_unit_k;
   d.tau = p_tau;
   d.k3 = p_k3;
   d.k3_off = p_k3off;
@@ -1075,6 +1084,45 @@ extern "C" int song2_los_create(const song2_spec *spec, const song2_los_spec *lo
     d.ddk = h->d_ddk;
   }
   *out = h;
+  return 0;
+}
+
+int s2los_view(song2_los *h, S2LosView *v, char *err) {
+  if (h->los.bessel_interpolation == SONG2_INTERP_CUBIC && !h->d_ddj) {
+    // natural spline of each j_l1 row from its x_min on (bessel2.c:437-456)
+    void *tmp;
+    if (dev_alloc(h, sizeof(double) * (size_t)h->n_l1 * h->x_size, &tmp, err)) return 1;
+    h->d_ddj = (double *)tmp;
+    CKL(cudaMemset(h->d_ddj, 0, sizeof(double) * (size_t)h->n_l1 * h->x_size));
+    const int *d_xmin, *d_est;
+    std::vector<int> zeros(h->n_l1, 0);
+    if (dev_upload(h, h->jxmin, &d_xmin, err) || dev_upload(h, zeros, &d_est, err)) return 1;
+    double *scratch;
+    CKL(cudaMalloc((void **)&scratch, sizeof(double) * (size_t)h->n_l1 * h->x_size));
+    ddJ_kernel<<<(h->n_l1 + 63) / 64, 64>>>(h->x_size, h->los.x_max, h->n_l1, d_xmin, d_est, h->d_jtab, h->d_ddj,
+                                            scratch);
+    cudaError_t e = cudaDeviceSynchronize();
+    cudaFree(scratch);
+    CKL(e);
+  }
+  v->spec = &h->spec;
+  v->los = &h->los;
+  v->l_size = h->los.l_size;
+  v->l = h->l.data();
+  v->x_size = h->x_size;
+  v->x_max = h->los.x_max;
+  v->x_step = h->los.x_step;
+  v->n_l1 = h->n_l1;
+  v->l1 = h->l1.data();
+  v->jxmin = h->jxmin.data();
+  v->jtab_dev = h->d_jtab;
+  v->ddj_dev = h->d_ddj;
+  v->n_pairs = h->n_pairs;
+  v->n_units = h->n_units;
+  v->unit_size = h->unit_size.data();
+  v->unit_k = h->unit_k.data();
+  v->unit_k_dev = h->d_unit_k;
+  v->n_tt = h->n_tt;
   return 0;
 }
 
