@@ -110,6 +110,9 @@ def parse():
     ap.add_argument("--los-reps", type=int, default=3)
     ap.add_argument("--los-cpu-share", type=float, default=0.05,
                     help="share of the transfer k units the CPU baseline of the line of sight runs")
+    ap.add_argument("--no-bispectra", action="store_true", help="skip the intrinsic bispectrum leg")
+    ap.add_argument("--bi-cpu-l", type=int, default=3,
+                    help="multipoles (a prefix of the l list) of the bispectrum's CPU sample")
     ap.add_argument("--k-size", type=int, default=None, help="override the k grid size (small profiling cases)")
     ap.add_argument("--k3-size", type=int, default=None, help="override the k3 grid size (small profiling cases)")
     ap.add_argument("--rsa", type=int, default=0, choices=[0, 1, 2],
@@ -480,7 +483,123 @@ def contract_leg(lib, p, launch, parts, n_parts, n_ctx, items, torch):
     return {"ms": ms, "triplets": ran, "status_ok": bool(np.all(st["status"] == 0)), "src": src_acc}
 
 
-def los_leg(lib, p, src_host, torch, reps, cpu_share):
+BI_R_SIZE = 75          # r samples of the bispectrum integral (r_size of the shipped precision files)
+BI_Q_LINSTEP = 0.4      # q step of the first-order transfers in units of 2 pi / (tau0 - tau_rec)
+
+
+def bispectra_inputs(p, los, ls, fields):
+    """Synthetic first-order inputs of the bispectrum: an r grid of BI_R_SIZE points
+    around the last-scattering distance, a q grid with the step of CLASS's transfer
+    sampling (q_linstep 0.4) inside the sources' k range, the primordial spectrum
+    2 pi^2 A_s (q/0.05)^(n_s-1) / q^3 of the benchmark cosmology, and Sachs-Wolfe-like
+    first-order transfers T_l(q) = j_l(q (tau0 - tau_rec)) / 3 (E: a tenth of it)."""
+    from scipy.special import spherical_jn
+    tau0, trec = los.tau0, los.tau_rec
+    r = np.linspace(tau0 - 2.5 * trec, tau0 + 0.5 * trec, BI_R_SIZE)
+    step = BI_Q_LINSTEP * 2 * np.pi / (tau0 - trec)
+    q = np.arange(p.k[0] * 1.0001, p.k[-1], step)
+    pk = 2 * np.pi ** 2 * 2.1e-9 * (q / 0.05) ** (0.966 - 1) / q ** 3
+    T1 = np.zeros((len(fields), len(ls), len(q)))
+    for f, fld in enumerate(fields):
+        for i, l in enumerate(ls):
+            T1[f, i] = spherical_jn(int(l), q * (tau0 - trec)) / 3.0 * (1.0 if fld == 0 else 0.1)
+    return r, q, pk, T1
+
+
+def bispectra_spec(fields, r, q, pk, T1):
+    from song_gb300 import capi
+    bs = capi.BispectraSpec()
+    bf = np.array(fields, dtype=np.int32)
+    T1 = np.ascontiguousarray(T1)
+    bs.bf_size, bs.bf = len(fields), capi.iptr(bf)
+    bs.r_size, bs.r = len(r), capi.dptr(r)
+    bs.q_size, bs.q = len(q), capi.dptr(q)
+    bs.pk, bs.transfer1 = capi.dptr(pk), capi.dptr(T1)
+    bs.k1_interpolation = bs.k2_interpolation = capi.INTERP_LINEAR
+    bs._keep = (bf, r, q, pk, T1)
+    return bs
+
+
+def bispectra_leg(lib, p, los, ls, h_los, d_t2, t2_host, torch, reps, cpu_l):
+    """The intrinsic bispectrum (T, E) of this run's second-order transfers, still in
+    HBM after the line of sight: first-order tables once per handle, then the k3, k2,
+    k1, r integrals and the geometry timed over `reps` runs.  The CPU restatement on
+    the same inputs with the l list cut to its first cpu_l multipoles, and the GPU on
+    that same cut, compared."""
+    from song_gb300 import capi
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    fields = [0, 1]
+    r, q, pk, T1 = bispectra_inputs(p, los, ls, fields)
+    bs = bispectra_spec(fields, r, q, pk, T1)
+    err = capi.errbuf()
+    bh = C.c_void_p()
+    t0 = time.perf_counter()
+    if lib.song2_bispectra_create(h_los, C.byref(bs), C.byref(bh), err):
+        raise RuntimeError(err.value.decode())
+    torch.cuda.synchronize()
+    create_s = time.perf_counter() - t0
+    try:
+        n_out = lib.song2_bispectra_size(bh)
+        d_b = torch.zeros(n_out, dtype=torch.float64, device="cuda")
+        ms = []
+        for i in range(reps + 1):
+            if lib.song2_bispectra_run(bh, C.c_void_p(d_t2.data_ptr()), C.c_void_p(d_b.data_ptr()), None, err):
+                raise RuntimeError(err.value.decode())
+            if i:
+                ms.append(lib.song2_bispectra_last_ms(bh))
+        b_full = d_b.cpu().numpy()
+    finally:
+        lib.song2_bispectra_destroy(bh)
+    n_conf = n_out // 8
+    # the cut: the first cpu_l multipoles, their transfer types, the same k units
+    n_types = lib.song2_transfer_types(C.byref(p.spec), C.byref(los), None, None, None)
+    ty = np.zeros(n_types, dtype=np.int32)
+    tl = np.zeros(n_types, dtype=np.int32)
+    lib.song2_transfer_types(C.byref(p.spec), C.byref(los), capi.iptr(ty), None, None)
+    lib.song2_transfer_types(C.byref(p.spec), C.byref(los), None, capi.iptr(tl), None)
+    keep = tl <= ls[cpu_l - 1]
+    t2 = t2_host.reshape(n_types, -1)[keep].ravel()
+    ls_cut = np.ascontiguousarray(ls[:cpu_l])
+    los_cut = capi.LosSpec()
+    C.memmove(C.byref(los_cut), C.byref(los), C.sizeof(capi.LosSpec))
+    los_cut.l_size, los_cut.l = cpu_l, capi.iptr(ls_cut)
+    bs_cut = bispectra_spec(fields, r, q, pk, T1[:, :cpu_l])
+    n_cut = lib.song2_bispectra_configs(cpu_l, capi.iptr(ls_cut), None, None, None) * 8
+    g_cut = np.zeros(n_cut)
+    t0 = time.perf_counter()
+    if lib.song2_gpu_bispectra(C.byref(p.spec), C.byref(los_cut), C.byref(bs_cut), capi.dptr(t2),
+                               capi.dptr(g_cut), err):
+        raise RuntimeError(err.value.decode())
+    gpu_cut_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ref = oracle.bispectra(p, los_cut, bs_cut, t2, n_cut)
+    cpu_s = time.perf_counter() - t0
+    g, w = g_cut.reshape(8, -1), ref.reshape(8, -1)
+    scale = np.max(np.abs(w), axis=1)
+    rel = float(np.max(np.max(np.abs(g - w), axis=1) / np.where(scale > 0, scale, 1.0)))
+    t_run = sum(ms) / len(ms) / 1e3
+    return {
+        "metric": "intrinsic bispectrum b_l1l2l3 of every (l1 >= l2 >= l3) configuration and field combination "
+                  "per second (bispectra2)",
+        "value": n_out / t_run, "unit": "bispectrum values/s", "ms_per_run": 1e3 * t_run, "runs": reps,
+        "workload": {"second_order": "this run's transfer functions (line of sight above), T and E, in HBM",
+                     "configurations": int(n_conf), "fields": "TT, TE, ... (2^3 combinations)",
+                     "m_list": [int(x) for x in p.spec.m[:p.spec.m_size]],
+                     "r_size": BI_R_SIZE, "q_size": int(len(q)),
+                     "first_order": "synthetic Sachs-Wolfe-like T_l(q) = j_l(q (tau0 - tau_rec))/3, E a tenth",
+                     "interpolation": "linear in k1, k2 and the Bessel functions (the shipped precision files)"},
+        "create_s": create_s,
+        "cpu_baseline": {"value": n_cut / cpu_s, "unit": "bispectrum values/s", "cores": os.cpu_count(),
+                         "kind": "port",
+                         "sample": f"the same inputs with the l list cut to its first {cpu_l} multipoles "
+                                   f"({n_cut // 8} configurations): CPU {cpu_s:.2f} s, GPU one-shot "
+                                   f"{gpu_cut_s:.2f} s including its Bessel tables"},
+        "max_rel_err_vs_cpu": rel, "tolerance": 1e-8, "within_tolerance": bool(rel <= 1e-8),
+    }
+
+
+def los_leg(lib, p, src_host, torch, reps, cpu_share, bispectra=True, bi_cpu_l=3):
     """transfer2 on the device: projection tables built once, then the line-of-sight
     integral of the config's sources (already in HBM) timed over `reps` runs; the CPU
     restatement on a contiguous run of the heaviest pairs as the baseline, and the
@@ -519,6 +638,12 @@ def los_leg(lib, p, src_host, torch, reps, cpu_share):
                 ms.append(lib.song2_los_last_ms(h))
         tables_ms = lib.song2_los_tables_ms(h)
         out = d_out.cpu().numpy()
+        bi_line = None
+        if bispectra:
+            try:
+                bi_line = bispectra_leg(lib, p, los, ls, h, d_out, out, torch, reps, bi_cpu_l)
+            except Exception as ex:  # noqa: BLE001
+                bi_line = {"error": str(ex)[:300]}
     finally:
         lib.song2_los_destroy(h)
         d_src = d_out = None
@@ -555,6 +680,7 @@ def los_leg(lib, p, src_host, torch, reps, cpu_share):
                                                    f"k units; {cpu_s:.1f} s including the tables)"},
         "max_rel_err_vs_cpu": rel, "zero_rows_nonzero": zero_bad, "tolerance": 1e-9,
         "within_tolerance": bool(rel <= 1e-9 and zero_bad == 0.0),
+        "bispectra": bi_line,
     }
 
 
@@ -791,7 +917,8 @@ def main():
     los_line = None
     if rank == 0 and world == 1 and not args.no_los:
         try:
-            los_line = los_leg(lib, p, src_mixed, torch, args.los_reps, args.los_cpu_share)
+            los_line = los_leg(lib, p, src_mixed, torch, args.los_reps, args.los_cpu_share,
+                               bispectra=not args.no_bispectra, bi_cpu_l=args.bi_cpu_l)
         except Exception as ex:  # noqa: BLE001
             los_line = {"error": str(ex)[:300]}
 

@@ -1066,7 +1066,6 @@ int song2_oracle_bispectra(const song2_spec *s, const song2_los_spec *los, const
   double *I2 = (double *)malloc(sizeof(double) * (size_t)L * L * R * K);
   double *I1 = (double *)malloc(sizeof(double) * (size_t)L * L * L * R);
   double *Ir = (double *)malloc(sizeof(double) * (size_t)L * L * L);
-  double *f = (double *)malloc(sizeof(double) * K), *ip = (double *)malloc(sizeof(double) * Q);
   int rc = 0;
   for (int X = 0; X < bf && !rc; ++X)
     for (int im = 0; im < s->m_size && !rc; ++im) {
@@ -1079,6 +1078,7 @@ int song2_oracle_bispectra(const song2_spec *s, const song2_los_spec *los, const
         if (parity == 0 ? (oL3 % 2 != 0) : (oL3 % 2 == 0)) continue;
         /* k3 */
         memset(I3, 0, sizeof(double) * (size_t)L * R * K * K);
+#pragma omp parallel for schedule(dynamic)
         for (int il3 = 0; il3 < L; ++il3) {
           int l3 = l[il3], L3 = abs(l3 - M3) + oL3;
           if (M3 > l3 || L3 > l3 + M3) continue;
@@ -1098,18 +1098,20 @@ int song2_oracle_bispectra(const song2_spec *s, const song2_los_spec *los, const
         for (int Y = 0; Y < bf && !rc; ++Y) {
           /* k2 */
           memset(I2, 0, sizeof(double) * (size_t)L * L * R * K);
-          for (int ir = 0; ir < R && !rc; ++ir)
-            for (int il3 = 0; il3 < L && !rc; ++il3) {
+          int bad2 = 0;
+#pragma omp parallel for schedule(dynamic) reduction(| : bad2)
+          for (int ir = 0; ir < R; ++ir) {
+            double *f = (double *)malloc(sizeof(double) * K), *ip = (double *)malloc(sizeof(double) * Q);
+            for (int il3 = 0; il3 < L && !bad2; ++il3) {
               if (M3 > l[il3]) continue;
-              for (int k1 = 0; k1 < K && !rc; ++k1) {
+              for (int k1 = 0; k1 < K && !bad2; ++k1) {
                 for (int k2 = 0; k2 < K; ++k2) {
                   if (k1 > k2) f[k2] = I3[(((size_t)il3 * R + ir) * K + k1) * K + k2];
                   else f[k2] = I3[(((size_t)il3 * R + ir) * K + k2) * K + k1] * pow(-kp[k1] / kp[k2], M3);
                   f[k2] *= 1 / pow(kp[k2], 2);
                 }
                 if (o_interp_k(kp, K, f, bs->k2_interpolation == SONG2_INTERP_CUBIC, q, Q, bs->pk, ip)) {
-                  snprintf(err, SONG2_ERRLEN, "q beyond the largest k");
-                  rc = 1;
+                  bad2 = 1;
                   break;
                 }
                 for (int il2 = 0; il2 < L; ++il2) {
@@ -1118,21 +1120,30 @@ int song2_oracle_bispectra(const song2_spec *s, const song2_los_spec *los, const
                 }
               }
             }
+            free(f);
+            free(ip);
+          }
+          if (bad2) {
+            snprintf(err, SONG2_ERRLEN, "q beyond the largest k");
+            rc = 1;
+          }
           for (int oL1 = 0; oL1 < 2 * M3 + 1 && !rc; ++oL1) {
             if (oL1 % 2 != 0) continue;
             for (int Z = 0; Z < bf && !rc; ++Z) {
               /* k1 */
-              for (int ir = 0; ir < R && !rc; ++ir)
-                for (int il3 = 0; il3 < L && !rc; ++il3) {
+              int bad1 = 0;
+#pragma omp parallel for schedule(dynamic) reduction(| : bad1)
+              for (int ir = 0; ir < R; ++ir) {
+                double *f = (double *)malloc(sizeof(double) * K), *ip = (double *)malloc(sizeof(double) * Q);
+                for (int il3 = 0; il3 < L && !bad1; ++il3) {
                   if (M3 > l[il3]) continue;
-                  for (int il2 = 0; il2 < L && !rc; ++il2) {
+                  for (int il2 = 0; il2 < L && !bad1; ++il2) {
                     int a = tmin[il3 * L + il2], b = tmax[il3 * L + il2];
                     if (b < a) continue;
                     for (int k1 = 0; k1 < K; ++k1)
                       f[k1] = I2[(((size_t)il3 * L + il2) * R + ir) * K + k1] * (1 / pow(kp[k1], 2));
                     if (o_interp_k(kp, K, f, bs->k1_interpolation == SONG2_INTERP_CUBIC, q, Q, bs->pk, ip)) {
-                      snprintf(err, SONG2_ERRLEN, "q beyond the largest k");
-                      rc = 1;
+                      bad1 = 1;
                       break;
                     }
                     for (int il1 = a; il1 <= b; ++il1) {
@@ -1146,6 +1157,14 @@ int song2_oracle_bispectra(const song2_spec *s, const song2_los_spec *los, const
                     }
                   }
                 }
+                free(f);
+                free(ip);
+              }
+              if (bad1) {
+                snprintf(err, SONG2_ERRLEN, "q beyond the largest k");
+                rc = 1;
+                continue;
+              }
               /* r */
               for (int il3 = 0; il3 < L; ++il3)
                 for (int il2 = 0; il2 < L; ++il2)
@@ -1227,8 +1246,6 @@ int song2_oracle_bispectra(const song2_spec *s, const song2_los_spec *los, const
   free(I2);
   free(I1);
   free(Ir);
-  free(f);
-  free(ip);
   free(dq);
   free(dr);
   free(tmin);
