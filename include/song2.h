@@ -576,6 +576,12 @@ int song2_k_grid_smart(const song2_params *grids, double tau0, double rs_rec, in
    with the two limits, and with k3_size_min - n + 2 evenly spaced points between
    them merged in when the pair has n < k3_size_min points; sorted, duplicates
    removed (CLASS's merge_arrays_double).  Same outputs as song2_k3_grids. */
+/* The theta_12 k3 sampling of perturb2_get_k_lists (perturbations2.c:2029-2060):
+   for every pair, k3_size values linear in the angle between k1 and k2 over the
+   limits of the lin/log samplings, k3 = sqrt(k1^2 + k2^2 + 2 cos(theta) k1 k2);
+   for k1 = k2 the first angle moves a fifth of a step inwards.  Same outputs as
+   song2_k3_grids. */
+int song2_k3_grids_theta12(const double *k, int k_size, int k3_size, int *k3_size_out, double *k3_out, char *err);
 int song2_k3_grids_smart(const double *k, int k_size, int k3_size_min, int *k3_size_out, double *k3_out,
                          char *err);
 /* Reads an ini and a pre file (either may be NULL; a name may appear once in

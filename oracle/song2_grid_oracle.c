@@ -246,3 +246,29 @@ int song2_oracle_tau_grid_class(const song2_tables *t, double stepsize, double b
   out[n - 1] = t->tau0;
   return n;
 }
+
+/* theta_12 k3 sampling (perturbations2.c:2029-2060): angles linear between
+   the angles of the clipped limits, written with the law of cosines */
+int song2_oracle_k3_grids_theta12(const double *k, int nk, int n3, int *sizes, double *out) {
+  int off = 0, p = 0;
+  for (int i1 = 0; i1 < nk; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2, ++p) {
+      double a = k[i1], b = k[i2];
+      double lo = fabs(a - b) + 1e-10, hi = a + b - 1e-10;
+      if ((a + b) / 100 > lo) lo = (a + b) / 100;
+      if (k[0] > lo) lo = k[0];
+      if (k[nk - 1] < hi) hi = k[nk - 1];
+      if (!(lo < hi)) return 1;
+      double t0 = acos((lo * lo - a * a - b * b) / (2 * a * b));
+      double t1 = acos((hi * hi - a * a - b * b) / (2 * a * b));
+      double dt = (t1 - t0) / (n3 - 1);
+      if (i1 == i2) {
+        t0 = t0 + dt / 5;
+        dt = (t1 - t0) / (n3 - 1);
+      }
+      sizes[p] = n3;
+      for (int j = 0; j < n3; ++j) out[off + j] = sqrt(a * a + b * b + 2 * cos(t0 + j * dt) * a * b);
+      off += n3;
+    }
+  return 0;
+}

@@ -753,3 +753,49 @@ int song2_tau_grid_class(const song2_tables *t, double stepsize, double late_boo
   if (out) out[n - 1] = t->tau0;
   return n;
 }
+
+/* ------------------------------------------------- theta_12 k3 sampling */
+
+int song2_k3_grids_theta12(const double *k, int k_size, int k3_size, int *k3_size_out, double *k3_out, char *err) {
+  if (k3_size < 2) {
+    snprintf(err, SONG2_ERRLEN, "theta_12 sampling needs k3_size >= 2, got %d", k3_size);
+    return 1;
+  }
+  int64_t off = 0;
+  for (int i = 0; i < k_size * k_size; ++i) k3_size_out[i] = 0;
+  for (int i1 = 0; i1 < k_size; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2) {
+      double k1 = k[i1], k2 = k[i2];
+      /* the limits of the lin/log samplings (perturbations2.c:1973-1984) */
+      double k3_min = fabs(k1 - k2) + 1e-10, k3_max = k1 + k2 - 1e-10;
+      if ((k1 + k2) / 100 > k3_min) k3_min = (k1 + k2) / 100;
+      if (k[0] > k3_min) k3_min = k[0];
+      if (k[k_size - 1] < k3_max) k3_max = k[k_size - 1];
+      if (k3_min >= k3_max) {
+        snprintf(err, SONG2_ERRLEN, "found k3_min=%g>k3_max=%g for k1(%d)=%g and k2(%d)=%g", k3_min, k3_max, i1, k1,
+                 i2, k2);
+        return 1;
+      }
+      double cmin = (k3_min * k3_min - k1 * k1 - k2 * k2) / (2 * k1 * k2);
+      double cmax = (k3_max * k3_max - k1 * k1 - k2 * k2) / (2 * k1 * k2);
+      if (fabs(cmin) > 1 || fabs(cmax) > 1) {
+        snprintf(err, SONG2_ERRLEN, "cos(theta_12) out of [-1, 1] for k1(%d)=%g and k2(%d)=%g", i1, k1, i2, k2);
+        return 1;
+      }
+      /* linear in the angle between k1 and k2 (perturbations2.c:2029-2060) */
+      double th_min = acos(cmin), th_max = acos(cmax);
+      double step = (th_max - th_min) / (k3_size - 1);
+      if (i1 == i2) {
+        th_min += step / 5;
+        step = (th_max - th_min) / (k3_size - 1);
+      }
+      k3_size_out[i1 * k_size + i2] = k3_size;
+      if (k3_out)
+        for (int i3 = 0; i3 < k3_size; ++i3) {
+          double c = cos(th_min + i3 * step);
+          k3_out[off + i3] = sqrt(k1 * k1 + k2 * k2 + 2 * c * k1 * k2);
+        }
+      off += k3_size;
+    }
+  return 0;
+}

@@ -337,3 +337,41 @@ def test_reader_source_time_sampling_keys(lib, tmp_path):
     assert (g.tau_start_c_over_h, g.tau_stepsize, g.tau_late_boost) == (0.008, 0.2, 1.0)
     rc, *_, err = read(lib, tmp_path, "output = tBisp\n", "perturb_sampling_stepsize_song = 0\n")
     assert rc == 1 and "positive" in err
+
+
+def test_theta12_k3_grids_match_oracle(lib):
+    import numpy as np
+    k = np.geomspace(1e-4, 0.2, 12)
+    n = len(k)
+    sz = np.zeros(n * n, dtype=np.int32)
+    err = capi.errbuf()
+    assert lib.song2_k3_grids_theta12(capi.dptr(k), n, 9, capi.iptr(sz), None, err) == 0, err.value
+    k3 = np.zeros(int(sz.sum()))
+    assert lib.song2_k3_grids_theta12(capi.dptr(k), n, 9, capi.iptr(sz), capi.dptr(k3), err) == 0
+    ol = oracle_lib()
+    f = ol.song2_oracle_k3_grids_theta12
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    osz = np.zeros(n * (n + 1) // 2, dtype=np.int32)
+    ok3 = np.zeros(k3.size)
+    assert f(capi.dptr(k), n, 9, capi.iptr(osz), capi.dptr(ok3)) == 0
+    assert np.allclose(k3, ok3, rtol=1e-14, atol=0)
+    off = 0
+    for i1 in range(n):
+        for i2 in range(i1 + 1):
+            g = k3[off: off + 9]
+            off += 9
+            assert np.all(np.diff(g) > 0)
+            lo = max(abs(k[i1] - k[i2]) + 1e-10, (k[i1] + k[i2]) / 100, k[0])
+            hi = min(k[i1] + k[i2] - 1e-10, k[-1])
+            # the angles are linear: the first and last k3 are the clipped limits
+            # (the first moved inwards by a fifth of a step when k1 = k2)
+            assert abs(g[-1] - hi) <= 1e-12 * hi
+            if i1 != i2:
+                assert abs(g[0] - lo) <= 1e-9 * lo
+            else:
+                assert g[0] > lo
+            cos_t = (g ** 2 - k[i1] ** 2 - k[i2] ** 2) / (2 * k[i1] * k[i2])
+            th = np.arccos(np.clip(cos_t, -1, 1))
+            assert np.allclose(np.diff(th), np.diff(th)[0], rtol=1e-6, atol=1e-12)
+    assert lib.song2_k3_grids_theta12(capi.dptr(k), n, 1, capi.iptr(sz), None, err) == 1
