@@ -6,6 +6,10 @@
     python -m song_gb300.cases los [--k-size 16] [--runs 3]
         the line-of-sight integral (transfer2) of config-4 geometry on a reduced k
         grid with seeded sources: projection tables once, then whole runs.
+    python -m song_gb300.cases bispectra [--k-size 50] [--l-max 2000] [--runs 2]
+        the intrinsic bispectrum (T, E; m <= 4) of seeded second-order transfers
+        on config-4 geometry: line-of-sight tables and first-order tables once,
+        then whole runs of the k3, k2, k1/r integrals and the symmetrisation.
     python -m song_gb300.cases phases [--config 4] [--parts 20]
         the per-phase clock64 cycle table of the evolver (a separate build with
         the phase timers compiled in), over one part of the workload.
@@ -81,6 +85,51 @@ def los(args):
         lib.song2_los_destroy(h)
 
 
+def bispectra(args):
+    import torch
+    from song_gb300 import capi
+    from song_gb300.problem import config_problem
+    from scipy.special import spherical_jn
+    lib = capi.load()
+    p = config_problem(4, k_size=args.k_size)
+    los = capi.LosSpec()
+    lib.song2_los_defaults(C.byref(los), C.byref(p.spec), C.byref(p.tables))
+    n = lib.song2_l_list(args.l_max, 1.25, 36, None)
+    ls = np.zeros(n, dtype=np.int32)
+    lib.song2_l_list(args.l_max, 1.25, 36, capi.iptr(ls))
+    los.l_size = n
+    los.l = capi.iptr(ls)
+    err = capi.errbuf()
+    h = C.c_void_p()
+    if lib.song2_los_create(C.byref(p.spec), C.byref(los), C.byref(h), err):
+        raise RuntimeError(err.value.decode())
+    b = C.c_void_p()
+    try:
+        tau0, trec = los.tau0, los.tau_rec
+        r = np.linspace(tau0 - 2.5 * trec, tau0 + 0.5 * trec, 75)
+        q = np.arange(p.k[0] * 1.0001, p.k[-1], 0.4 * 2 * np.pi / (tau0 - trec))
+        pk = 2 * np.pi ** 2 * 2.1e-9 * (q / 0.05) ** (0.966 - 1) / q ** 3
+        T1 = np.stack([np.stack([spherical_jn(int(l), q * (tau0 - trec)) / 3.0 * s_ for l in ls])
+                       for s_ in (1.0, 0.1)])
+        bf = np.array([0, 1], dtype=np.int32)
+        bs = capi.BispectraSpec(2, capi.iptr(bf), len(r), capi.dptr(r), len(q), capi.dptr(q), capi.dptr(pk),
+                                capi.dptr(np.ascontiguousarray(T1)), capi.INTERP_LINEAR, capi.INTERP_LINEAR)
+        if lib.song2_bispectra_create(h, C.byref(bs), C.byref(b), err):
+            raise RuntimeError(err.value.decode())
+        rng = np.random.default_rng(3)
+        t2 = torch.from_numpy(rng.normal(size=lib.song2_los_transfer_size(h))).cuda()
+        out = torch.zeros(lib.song2_bispectra_size(b), dtype=torch.float64, device="cuda")
+        for i in range(args.runs):
+            if lib.song2_bispectra_run(b, C.c_void_p(t2.data_ptr()), C.c_void_p(out.data_ptr()), None, err):
+                raise RuntimeError(err.value.decode())
+            print(f"run {i}: {lib.song2_bispectra_last_ms(b):.1f} ms", flush=True)
+        print(f"l {n}, r {len(r)}, q {len(q)}, k {len(p.k)}, bispectrum values {out.numel()}")
+    finally:
+        if b:
+            lib.song2_bispectra_destroy(b)
+        lib.song2_los_destroy(h)
+
+
 def phases(args):
     from song_gb300 import build
     here = os.path.dirname(os.path.abspath(__file__))
@@ -125,7 +174,8 @@ def phases(args):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("case", choices=["evolver", "los", "phases"])
+    ap.add_argument("case", choices=["evolver", "los", "bispectra", "phases"])
+    ap.add_argument("--l-max", type=int, default=2000)
     ap.add_argument("--k-size", type=int, default=None)
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--runs", type=int, default=None)
@@ -140,6 +190,10 @@ def main(argv=None):
         args.k_size = args.k_size or 16
         args.runs = args.runs or 3
         los(args)
+    elif args.case == "bispectra":
+        args.k_size = args.k_size or 50
+        args.runs = args.runs or 2
+        bispectra(args)
     else:
         phases(args)
     return 0

@@ -116,7 +116,7 @@ struct JTab {
   const double *tab, *dd;
   const int *xmin;  // per row
   int x_size;
-  double x_max, x_step;
+  double x_max, x_step, inv_step;
   int cubic;
   int *status;
 };
@@ -125,14 +125,20 @@ __device__ __forceinline__ double jl_at(const JTab &t, int row, double x) {
   int x0 = __ldg(&t.xmin[row]);
   double xm = s2los_x_of(x0, t.x_size, t.x_max);
   if (x < xm) return 0.0;
-  int ix = (int)((x - xm) / t.x_step);
+  // index and weight of bessel2_convolution, (xm + x_step (ix + 1) - x) / x_step,
+  // written as ix + 1 - u with u = (x - xm) / x_step
+  const double u = (x - xm) * t.inv_step;
+  int ix = (int)u;
   if (x0 + ix + 1 >= t.x_size) {  // outside the table: record and drop the term
     atomicOr(t.status, 1);
     return 0.0;
   }
-  double a = (xm + t.x_step * (ix + 1) - x) / t.x_step;
+  double a = (double)(ix + 1) - u;
   const double *r = t.tab + (size_t)row * t.x_size + x0 + ix;
-  if (!t.cubic) return a * __ldg(r) + (1. - a) * __ldg(r + 1);
+  if (!t.cubic) {
+    const double j1 = __ldg(r + 1);
+    return fma(a, __ldg(r) - j1, j1);
+  }
   const double *q = t.dd + (size_t)row * t.x_size + x0 + ix;
   return a * __ldg(r) +
          (1. - a) * (__ldg(r + 1) - a * ((a + 1.) * __ldg(q) + (2. - a) * __ldg(q + 1)) * t.x_step * t.x_step / 6.0);
@@ -155,14 +161,15 @@ struct CoefArgs {
   const double *window;  // [k_size] 1/k^2
   const double *r;
   const double *rfac;    // [r_size]
-  double *out;           // [r][l][k]
+  int l_major;           // 0: out[r][l][k] (C), 1: out[l][r][k] (D)
+  double *out;
 };
 
 __global__ void __launch_bounds__(128) coef_kernel(CoefArgs a) {
   extern __shared__ double sh[];
   double *A = sh, *B = sh + a.k_size, *SA = sh + 2 * a.k_size, *SB = sh + 3 * a.k_size;
   const int il = blockIdx.x / a.r_size, ir = blockIdx.x % a.r_size;
-  double *out = a.out + ((size_t)ir * a.l_size + il) * a.k_size;
+  double *out = a.out + (a.l_major ? ((size_t)il * a.r_size + ir) : ((size_t)ir * a.l_size + il)) * a.k_size;
   const int row = a.row_of_l[il];
   if (row < 0) {
     for (int k = threadIdx.x; k < a.k_size; k += blockDim.x) out[k] = 0.0;
@@ -212,7 +219,7 @@ struct K3Args {
   const int *tt;              // transfer type of (X, l3, M3) at tt[il3 * tt_stride], -1 if none
   int tt_stride;
   const double *r;
-  const double *unit_k, *unit_dk;
+  const double *unit_k, *unit_w;  // k and k^2 dk of every transfer k unit
   const long long *unit_off;  // [n_pairs]
   const int *unit_n;
   const double *T2;
@@ -236,16 +243,15 @@ __global__ void __launch_bounds__(BI_THREADS) k3_kernel(K3Args a) {
   const long long u0 = a.unit_off[p];
   const int n = a.unit_n[p];
   const double *T = a.T2 + (size_t)tt * a.n_units + u0;
-  const double *kk = a.unit_k + u0, *dk = a.unit_dk + u0;
+  const double *kk = a.unit_k + u0, *w = a.unit_w + u0;
   for (int ir = lane; ir < a.r_size; ir += 32) {
     const double r = a.r[ir];
     double s = 0.0;
     for (int i = 0; i < n; ++i) {
       double f = __ldg(&T[i]);
       if (f == 0.0) continue;
-      double k = __ldg(&kk[i]);
-      double j = jl_at(a.jt, row, k * r);
-      s += k * k * j * f * __ldg(&dk[i]);
+      double j = jl_at(a.jt, row, __ldg(&kk[i]) * r);
+      s = fma(__ldg(&w[i]) * f, j, s);
     }
     double v = 0.5 * s;
     if (a.M3 != 0) v *= a.coef;
@@ -301,36 +307,34 @@ __global__ void __launch_bounds__(BI_THREADS) k2_kernel(K2Args a) {
 }
 
 // ------------------------------------------------------------ k1 and r integrals, geometry
+// One block per (l3, l2) for one (X, M3, offset_L3, Y): the k2 integrals of the
+// pair over (r, k) staged in shared memory once, then, warp by warp, every
+// (offset_L1, l1) of the triangle with both D tables of its Z fields.
+constexpr int BI_MAX_Z = 3;
 struct K1Args {
-  int l_size, r_size, k_size, M3, offset_L3, offset_L1, parity, m_max;
+  int l_size, r_size, k_size, M3, offset_L3, parity, m_max, bf;
   const int *l;
   const int *tri_min, *tri_max;  // [l_size][l_size] index range of the third multipole
   const long long *tri_off;      // [l_size][l_size] offset in the packed triangle arrays
   const double *I2;              // [l3][l2][r][k]
-  const double *D;               // [r][l1][k]
+  const double *D[BI_MAX_Z];     // per Z: offset_L1 slabs [o][l1][r][k], o = offset_L1 / 2
   const double *lf;              // ln n!
-  double *U;                     // unsymmetrised bispectrum of (X, Y, Z), packed
+  double *U[BI_MAX_Z];           // per Z: unsymmetrised bispectrum of (X, Y, Z), packed
 };
 
-// bispectra2_intrinsic_geometrical_factors (bispectra2.c:2456-2880) for one
-// (l3, l2, l1) and (M3, L3, L1), added to (or, with an m list of {0} and even
-// parity, written into) the unsymmetrised bispectrum
-__device__ void accumulate(const K1Args &a, int il3, int il2, int il1, int t0, int L3, int L1, double integral) {
-  const int l3 = a.l[il3], l2 = a.l[il2], l1 = a.l[il1], M3 = a.M3;
-  const bool even = a.parity == 0;
-  double *dst = a.U + a.tri_off[il3 * a.l_size + il2] + (il1 - t0);
-  if (even && a.m_max == 0) {
-    *dst = 8.0 / (BI_PI * BI_PI * BI_PI) * integral;
-    return;
-  }
-  double f_l3L3 = w3j(L3, M3, l3, 0, -M3, M3, a.lf);
+// bispectra2_intrinsic_geometrical_factors (bispectra2.c:2456-2880): the
+// factor of one (l3, l2, l1) and (M3, L3, L1); it does not depend on Z
+__device__ __noinline__ double geometry_factor(int M3, int offset_L3, int parity, const double *__restrict__ lf,
+                                               int l3, int l2, int l1, int L3, int L1) {
+  const bool even = parity == 0;
+  double f_l3L3 = w3j(L3, M3, l3, 0, -M3, M3, lf);
   double summed = f_l3L3;
-  if (M3 != 0) summed = even ? f_l3L3 + ((a.offset_L3 & 1) ? -f_l3L3 : f_l3L3)
-                              : f_l3L3 - ((a.offset_L3 & 1) ? -f_l3L3 : f_l3L3);
-  double f_l1l2l3 = w3j000(l1, l2, l3, a.lf);
-  double f_L1l2L3 = w3j000(L1, l2, L3, a.lf);
-  double f_l1L1M3 = w3j000(L1, l1, M3, a.lf);
-  double f_6j = w6j(L1, L3, l2, l3, l1, M3, a.lf);
+  if (M3 != 0) summed = even ? f_l3L3 + ((offset_L3 & 1) ? -f_l3L3 : f_l3L3)
+                              : f_l3L3 - ((offset_L3 & 1) ? -f_l3L3 : f_l3L3);
+  double f_l1l2l3 = w3j000(l1, l2, l3, lf);
+  double f_L1l2L3 = w3j000(L1, l2, L3, lf);
+  double f_l1L1M3 = w3j000(L1, l1, M3, lf);
+  double f_6j = w6j(L1, L3, l2, l3, l1, M3, lf);
   bool even_conf = ((l1 + l2 + l3) % 2 == 0);
   double prefactor = even ? 8.0 / (BI_PI * BI_PI * BI_PI) * (2 * L1 + 1.) * (2 * L3 + 1.)
                           : -0.5 / (4 * BI_PI * BI_PI * BI_PI * BI_PI) * (2 * L1 + 1.) * (2 * L3 + 1.) *
@@ -339,10 +343,11 @@ __device__ void accumulate(const K1Args &a, int il3, int il2, int il1, int t0, i
   if (even && even_conf) geometry /= f_l1l2l3;
   int exponent = even ? l3 + L3 - l1 - L1 : l3 + L3 - l1 - L1 - 1;
   double sign = ((exponent / 2) % 2 == 0) ? 1.0 : -1.0;
-  *dst += sign * prefactor * geometry * integral;
+  return sign * prefactor * geometry;
 }
 
 __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
+  extern __shared__ double G[];  // [r][k]
   const int il3 = blockIdx.x / a.l_size, il2 = blockIdx.x % a.l_size;
   const int l3 = a.l[il3], l2 = a.l[il2], M3 = a.M3;
   if (M3 > l3) return;
@@ -350,21 +355,43 @@ __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
   if (L3 > l3 + M3) return;
   const int t0 = a.tri_min[il3 * a.l_size + il2], t1 = a.tri_max[il3 * a.l_size + il2];
   if (t1 < t0) return;
+  const int RK = a.r_size * a.k_size;
+  const double *g = a.I2 + ((size_t)il3 * a.l_size + il2) * RK;
+  for (int i = threadIdx.x; i < RK; i += blockDim.x) G[i] = g[i];
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int K = a.k_size, RK = a.r_size * K;
-  const double *G = a.I2 + ((size_t)il3 * a.l_size + il2) * RK;
-  for (int il1 = t0 + warp; il1 <= t1; il1 += BI_WARPS) {
+  const int n_tri = t1 - t0 + 1, n_off = M3 + 1;  // even offsets 0, 2, ..., 2 M3
+  const size_t slab = (size_t)a.l_size * RK;
+  const long long base = a.tri_off[il3 * a.l_size + il2];
+  for (int item = warp; item < n_off * n_tri; item += BI_WARPS) {
+    const int o = item / n_tri, il1 = t0 + item % n_tri;
     const int l1 = a.l[il1];
-    const int L1 = abs(l1 - M3) + a.offset_L1;
+    const int L1 = abs(l1 - M3) + 2 * o;
     if (L1 > l1 + M3) continue;
     if (!triangle(L1, l2, L3)) continue;
-    double s = 0.0;
+    double s[BI_MAX_Z];
+    const size_t off = o * slab + (size_t)il1 * RK;
+#pragma unroll
+    for (int z = 0; z < BI_MAX_Z; ++z) s[z] = 0.0;
     for (int i = lane; i < RK; i += 32) {
-      int ir = i / K, k = i % K;
-      s += a.D[((size_t)ir * a.l_size + il1) * K + k] * G[i];
+      const double gi = G[i];
+#pragma unroll
+      for (int z = 0; z < BI_MAX_Z; ++z)
+        if (z < a.bf) s[z] = fma(__ldg(&a.D[z][off + i]), gi, s[z]);
     }
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) accumulate(a, il3, il2, il1, t0, L3, L1, s);
+#pragma unroll
+    for (int z = 0; z < BI_MAX_Z; ++z)
+#pragma unroll
+      for (int w = 16; w; w >>= 1) s[z] += __shfl_xor_sync(0xffffffffu, s[z], w);
+    if (lane != 0) continue;
+    const bool m0 = a.parity == 0 && a.m_max == 0;
+    const double f = m0 ? 8.0 / (BI_PI * BI_PI * BI_PI) : geometry_factor(M3, a.offset_L3, a.parity, a.lf, l3, l2, l1, L3, L1);
+#pragma unroll
+    for (int z = 0; z < BI_MAX_Z; ++z)
+      if (z < a.bf) {
+        double *dst = a.U[z] + base + (il1 - t0);
+        *dst = m0 ? f * s[z] : *dst + f * s[z];
+      }
   }
 }
 
@@ -481,7 +508,7 @@ struct song2_bispectra {
   const int *d_l = nullptr, *d_row_of_L = nullptr, *d_tri_min = nullptr, *d_tri_max = nullptr;
   const int *d_unit_n = nullptr, *d_c1 = nullptr, *d_c2 = nullptr, *d_c3 = nullptr, *d_tt = nullptr;
   const long long *d_tri_off = nullptr, *d_unit_off = nullptr;
-  const double *d_r = nullptr, *d_k = nullptr, *d_unit_dk = nullptr, *d_lf = nullptr;
+  const double *d_r = nullptr, *d_k = nullptr, *d_unit_w = nullptr, *d_lf = nullptr;
   double *d_C = nullptr;  // [bf][r][l][k]
   double *d_D = nullptr;  // [bf][(im, offset_L1/2)][r][l][k]
   std::vector<long long> d_slot;  // D slot of (im, offset_L1) pairs: index im * (m_max + 1) + offset_L1 / 2
@@ -688,6 +715,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
         return fail();
       }
       trapezoid(v.unit_k + o, un[p], udk.data() + o);
+      for (int i = 0; i < un[p]; ++i) udk[o + i] *= v.unit_k[o + i] * v.unit_k[o + i];  // k^2 dk
       o += un[p];
     }
   }
@@ -700,7 +728,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   std::vector<int> jx(v.jxmin, v.jxmin + v.n_l1);
   if (bup(h, lv, &h->d_l, err) || bup(h, row_of, &h->d_row_of_L, err) || bup(h, h->tri_min, &h->d_tri_min, err) ||
       bup(h, h->tri_max, &h->d_tri_max, err) || bup(h, h->tri_off, &h->d_tri_off, err) ||
-      bup(h, un, &h->d_unit_n, err) || bup(h, uoff, &h->d_unit_off, err) || bup(h, udk, &h->d_unit_dk, err) ||
+      bup(h, un, &h->d_unit_n, err) || bup(h, uoff, &h->d_unit_off, err) || bup(h, udk, &h->d_unit_w, err) ||
       bup(h, c1, &h->d_c1, err) || bup(h, c2, &h->d_c2, err) || bup(h, c3, &h->d_c3, err) ||
       bup(h, h->tt, &h->d_tt, err) || bup(h, r, &h->d_r, err) || bup(h, h->k, &h->d_k, err) ||
       bup(h, lf, &h->d_lf, err) || bup(h, q, &d_q, err) || bup(h, qw, &d_qw, err) || bup(h, qa, &d_qa, err) ||
@@ -718,6 +746,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   h->jt.x_size = v.x_size;
   h->jt.x_max = v.x_max;
   h->jt.x_step = v.x_step;
+  h->jt.inv_step = 1.0 / v.x_step;
   h->jt.cubic = v.los->bessel_interpolation == SONG2_INTERP_CUBIC;
   h->jt.status = h->d_status;
   // coefficient tables
@@ -771,6 +800,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
         ca.row_of_l = d_rows;
         ca.cubic = k1c;
         ca.rfac = d_rfac;
+        ca.l_major = 1;
         ca.out = h->d_D + ((size_t)b * h->n_dslots + h->d_slot[(size_t)im * (h->m_max + 1) + o / 2]) * slab;
         coef_kernel<<<L * R, 128, csm>>>(ca);
         CKB(cudaGetLastError());
@@ -794,6 +824,17 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   h->d_U = (double *)tmp;
   CKB(cudaFuncSetAttribute(k2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(sizeof(double) * BI_MAX_K * BI_MAX_K)));
+  {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    size_t need = sizeof(double) * (size_t)R * K;
+    if (need > (size_t)optin) {
+      snprintf(err, SONG2_ERRLEN, "r_size * k_size = %d * %d too large for the k1 integral's shared memory", R, K);
+      return fail();
+    }
+    CKB(cudaFuncSetAttribute(k1r_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+  }
   cudaEventCreate(&h->e0);
   cudaEventCreate(&h->e1);
   *out = h;
@@ -839,7 +880,7 @@ extern "C" int song2_bispectra_run(song2_bispectra *h, const double *transfer2_d
         ka.tt_stride = h->m_size;
         ka.r = h->d_r;
         ka.unit_k = v.unit_k_dev;
-        ka.unit_dk = h->d_unit_dk;
+        ka.unit_w = h->d_unit_w;
         ka.unit_off = h->d_unit_off;
         ka.unit_n = h->d_unit_n;
         ka.T2 = transfer2_dev;
@@ -862,28 +903,27 @@ extern "C" int song2_bispectra_run(song2_bispectra *h, const double *transfer2_d
           k2.I2 = h->d_I2;
           k2_kernel<<<L * R, BI_THREADS, sizeof(double) * K * K, st>>>(k2);
           CKB(cudaGetLastError());
-          for (int oL1 = 0; oL1 < 2 * M3 + 1; oL1 += 2)
-            for (int Z = 0; Z < bf; ++Z) {
-              K1Args k1{};
-              k1.l_size = L;
-              k1.r_size = R;
-              k1.k_size = K;
-              k1.M3 = M3;
-              k1.offset_L3 = oL3;
-              k1.offset_L1 = oL1;
-              k1.parity = h->parity;
-              k1.m_max = h->m_max;
-              k1.l = h->d_l;
-              k1.tri_min = h->d_tri_min;
-              k1.tri_max = h->d_tri_max;
-              k1.tri_off = h->d_tri_off;
-              k1.I2 = h->d_I2;
-              k1.D = h->d_D + ((size_t)Z * h->n_dslots + h->d_slot[(size_t)im * (h->m_max + 1) + oL1 / 2]) * slab;
-              k1.lf = h->d_lf;
-              k1.U = h->d_U + ((size_t)(X * bf + Y) * bf + Z) * h->n_tri;
-              k1r_kernel<<<L * L, BI_THREADS, 0, st>>>(k1);
-              CKB(cudaGetLastError());
-            }
+          K1Args k1{};
+          k1.l_size = L;
+          k1.r_size = R;
+          k1.k_size = K;
+          k1.M3 = M3;
+          k1.offset_L3 = oL3;
+          k1.parity = h->parity;
+          k1.m_max = h->m_max;
+          k1.bf = bf;
+          k1.l = h->d_l;
+          k1.tri_min = h->d_tri_min;
+          k1.tri_max = h->d_tri_max;
+          k1.tri_off = h->d_tri_off;
+          k1.I2 = h->d_I2;
+          for (int Z = 0; Z < bf; ++Z) {
+            k1.D[Z] = h->d_D + ((size_t)Z * h->n_dslots + h->d_slot[(size_t)im * (h->m_max + 1)]) * slab;
+            k1.U[Z] = h->d_U + ((size_t)(X * bf + Y) * bf + Z) * h->n_tri;
+          }
+          k1.lf = h->d_lf;
+          k1r_kernel<<<L * L, BI_THREADS, sizeof(double) * R * K, st>>>(k1);
+          CKB(cudaGetLastError());
         }
       }
     }
