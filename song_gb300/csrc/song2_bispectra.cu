@@ -360,38 +360,49 @@ __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
   for (int i = threadIdx.x; i < RK; i += blockDim.x) G[i] = g[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_tri = t1 - t0 + 1, n_off = M3 + 1;  // even offsets 0, 2, ..., 2 M3
+  const int n_off = M3 + 1;  // even offsets 0, 2, ..., 2 M3
   const size_t slab = (size_t)a.l_size * RK;
   const long long base = a.tri_off[il3 * a.l_size + il2];
-  for (int item = warp; item < n_off * n_tri; item += BI_WARPS) {
-    const int o = item / n_tri, il1 = t0 + item % n_tri;
+  // one warp per l1: its offsets of L1 in turn, so that each output has one writer
+  for (int il1 = t0 + warp; il1 <= t1; il1 += BI_WARPS) {
     const int l1 = a.l[il1];
-    const int L1 = abs(l1 - M3) + 2 * o;
-    if (L1 > l1 + M3) continue;
-    if (!triangle(L1, l2, L3)) continue;
-    double s[BI_MAX_Z];
-    const size_t off = o * slab + (size_t)il1 * RK;
+    double acc[BI_MAX_Z];
 #pragma unroll
-    for (int z = 0; z < BI_MAX_Z; ++z) s[z] = 0.0;
-    for (int i = lane; i < RK; i += 32) {
-      const double gi = G[i];
+    for (int z = 0; z < BI_MAX_Z; ++z) acc[z] = 0.0;
+    const bool m0 = a.parity == 0 && a.m_max == 0;
+    for (int o = 0; o < n_off; ++o) {
+      const int L1 = abs(l1 - M3) + 2 * o;
+      if (L1 > l1 + M3) continue;
+      if (!triangle(L1, l2, L3)) continue;
+      double s[BI_MAX_Z];
+      const size_t off = o * slab + (size_t)il1 * RK;
+#pragma unroll
+      for (int z = 0; z < BI_MAX_Z; ++z) s[z] = 0.0;
+      for (int i = lane; i < RK; i += 32) {
+        const double gi = G[i];
+#pragma unroll
+        for (int z = 0; z < BI_MAX_Z; ++z)
+          if (z < a.bf) s[z] = fma(__ldg(&a.D[z][off + i]), gi, s[z]);
+      }
 #pragma unroll
       for (int z = 0; z < BI_MAX_Z; ++z)
-        if (z < a.bf) s[z] = fma(__ldg(&a.D[z][off + i]), gi, s[z]);
-    }
 #pragma unroll
-    for (int z = 0; z < BI_MAX_Z; ++z)
+        for (int w = 16; w; w >>= 1) s[z] += __shfl_xor_sync(0xffffffffu, s[z], w);
+      if (lane == 0) {
+        const double f = m0 ? 8.0 / (BI_PI * BI_PI * BI_PI)
+                            : geometry_factor(M3, a.offset_L3, a.parity, a.lf, l3, l2, l1, L3, L1);
 #pragma unroll
-      for (int w = 16; w; w >>= 1) s[z] += __shfl_xor_sync(0xffffffffu, s[z], w);
-    if (lane != 0) continue;
-    const bool m0 = a.parity == 0 && a.m_max == 0;
-    const double f = m0 ? 8.0 / (BI_PI * BI_PI * BI_PI) : geometry_factor(M3, a.offset_L3, a.parity, a.lf, l3, l2, l1, L3, L1);
-#pragma unroll
-    for (int z = 0; z < BI_MAX_Z; ++z)
-      if (z < a.bf) {
-        double *dst = a.U[z] + base + (il1 - t0);
-        *dst = m0 ? f * s[z] : *dst + f * s[z];
+        for (int z = 0; z < BI_MAX_Z; ++z) acc[z] += f * s[z];
       }
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int z = 0; z < BI_MAX_Z; ++z)
+        if (z < a.bf) {
+          double *dst = a.U[z] + base + (il1 - t0);
+          *dst = m0 ? acc[z] : *dst + acc[z];
+        }
+    }
   }
 }
 
