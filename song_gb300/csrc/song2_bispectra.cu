@@ -796,6 +796,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
     ca.T1 = d_T1 + (size_t)b * L * Q;
     ca.cubic = k2c;
     ca.rfac = d_ones;
+    ca.l_major = 0;
     ca.out = h->d_C + (size_t)b * slab;
     coef_kernel<<<L * R, 128, csm>>>(ca);
     CKB(cudaGetLastError());
