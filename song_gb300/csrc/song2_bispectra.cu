@@ -114,7 +114,8 @@ __device__ double w6j(int a, int b, int c, int d, int e, int f, const double *__
 // starts at its x_min node, steps of x_step from there.
 struct JTab {
   const double *tab, *dd;
-  const int *xmin;  // per row
+  const int *xmin;     // per row: first stored x index
+  const double *xmin_x;  // per row: its x (the lin_space node)
   int x_size;
   double x_max, x_step, inv_step;
   int cubic;
@@ -122,9 +123,9 @@ struct JTab {
 };
 
 __device__ __forceinline__ double jl_at(const JTab &t, int row, double x) {
-  int x0 = __ldg(&t.xmin[row]);
-  double xm = s2los_x_of(x0, t.x_size, t.x_max);
+  const double xm = __ldg(&t.xmin_x[row]);
   if (x < xm) return 0.0;
+  const int x0 = __ldg(&t.xmin[row]);
   // index and weight of bessel2_convolution, (xm + x_step (ix + 1) - x) / x_step,
   // written as ix + 1 - u with u = (x - xm) / x_step
   const double u = (x - xm) * t.inv_step;
@@ -228,35 +229,36 @@ struct K3Args {
 };
 
 __global__ void __launch_bounds__(BI_THREADS) k3_kernel(K3Args a) {
-  const int warp = blockIdx.x * BI_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (warp >= a.l_size * a.n_pairs) return;
-  const int il3 = warp / a.n_pairs, p = warp % a.n_pairs;
+  // one thread per (l3, pair, r), r fastest
+  const unsigned t = blockIdx.x * BI_THREADS + threadIdx.x;
+  if (t >= (unsigned)(a.l_size * a.n_pairs * a.r_size)) return;
+  const int ir = (int)(t % (unsigned)a.r_size);
+  const unsigned w = t / (unsigned)a.r_size;
+  const int il3 = (int)(w / (unsigned)a.n_pairs), p = (int)(w % (unsigned)a.n_pairs);
   const int l3 = a.l[il3];
   const int L3 = abs(l3 - a.M3) + a.offset_L3;
-  double *out = a.I3 + (size_t)il3 * a.r_size * a.n_pairs + p;
+  double *out = a.I3 + ((size_t)il3 * a.r_size + ir) * a.n_pairs + p;
   const int tt = a.tt[il3 * a.tt_stride];
   if (a.M3 > l3 || L3 > l3 + a.M3 || tt < 0) {
-    for (int ir = lane; ir < a.r_size; ir += 32) out[(size_t)ir * a.n_pairs] = 0.0;
+    *out = 0.0;
     return;
   }
   const int row = a.row_of_L[L3];
   const long long u0 = a.unit_off[p];
   const int n = a.unit_n[p];
   const double *T = a.T2 + (size_t)tt * a.n_units + u0;
-  const double *kk = a.unit_k + u0, *w = a.unit_w + u0;
-  for (int ir = lane; ir < a.r_size; ir += 32) {
-    const double r = a.r[ir];
-    double s = 0.0;
-    for (int i = 0; i < n; ++i) {
-      double f = __ldg(&T[i]);
-      if (f == 0.0) continue;
-      double j = jl_at(a.jt, row, __ldg(&kk[i]) * r);
-      s = fma(__ldg(&w[i]) * f, j, s);
-    }
-    double v = 0.5 * s;
-    if (a.M3 != 0) v *= a.coef;
-    out[(size_t)ir * a.n_pairs] = v * 2.0;
+  const double *kk = a.unit_k + u0, *wk = a.unit_w + u0;
+  const double r = a.r[ir];
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double f = __ldg(&T[i]);
+    if (f == 0.0) continue;
+    double j = jl_at(a.jt, row, __ldg(&kk[i]) * r);
+    s = fma(__ldg(&wk[i]) * f, j, s);
   }
+  double v = 0.5 * s;
+  if (a.M3 != 0) v *= a.coef;
+  *out = v * 2.0;
 }
 
 // ------------------------------------------------------------ k2 integral
@@ -313,6 +315,7 @@ __global__ void __launch_bounds__(BI_THREADS) k2_kernel(K2Args a) {
 constexpr int BI_MAX_Z = 3;
 struct K1Args {
   int l_size, r_size, k_size, M3, offset_L3, parity, m_max, bf;
+  int g2;                        // l2 values per block
   const int *l;
   const int *tri_min, *tri_max;  // [l_size][l_size] index range of the third multipole
   const long long *tri_off;      // [l_size][l_size] offset in the packed triangle arrays
@@ -346,61 +349,111 @@ __device__ __noinline__ double geometry_factor(int M3, int offset_L3, int parity
   return sign * prefactor * geometry;
 }
 
+constexpr int BI_MAX_G2 = 2;  // l2 values per block sharing the D loads
+
 __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
-  extern __shared__ double G[];  // [r][k]
-  const int il3 = blockIdx.x / a.l_size, il2 = blockIdx.x % a.l_size;
-  const int l3 = a.l[il3], l2 = a.l[il2], M3 = a.M3;
+  extern __shared__ double G[];  // [g][r][k]
+  const int n_grp = (a.l_size + a.g2 - 1) / a.g2;
+  const int il3 = blockIdx.x / n_grp, il2_0 = (blockIdx.x % n_grp) * a.g2;
+  const int l3 = a.l[il3], M3 = a.M3;
   if (M3 > l3) return;
   const int L3 = abs(l3 - M3) + a.offset_L3;
   if (L3 > l3 + M3) return;
-  const int t0 = a.tri_min[il3 * a.l_size + il2], t1 = a.tri_max[il3 * a.l_size + il2];
-  if (t1 < t0) return;
+  const int ng = min(a.g2, a.l_size - il2_0);
   const int RK = a.r_size * a.k_size;
-  const double *g = a.I2 + ((size_t)il3 * a.l_size + il2) * RK;
-  for (int i = threadIdx.x; i < RK; i += blockDim.x) G[i] = g[i];
+  int t0[BI_MAX_G2], t1[BI_MAX_G2], l2v[BI_MAX_G2], lo = a.l_size, hi = -1;
+#pragma unroll
+  for (int g = 0; g < BI_MAX_G2; ++g) {
+    t0[g] = 0;
+    t1[g] = -1;
+    l2v[g] = 0;
+    if (g < ng) {
+      t0[g] = a.tri_min[il3 * a.l_size + il2_0 + g];
+      t1[g] = a.tri_max[il3 * a.l_size + il2_0 + g];
+      l2v[g] = a.l[il2_0 + g];
+      if (t1[g] >= t0[g]) {
+        lo = min(lo, t0[g]);
+        hi = max(hi, t1[g]);
+      }
+    }
+  }
+  if (hi < lo) return;
+  for (int g = 0; g < ng; ++g) {
+    const double *src = a.I2 + ((size_t)il3 * a.l_size + il2_0 + g) * RK;
+    for (int i = threadIdx.x; i < RK; i += blockDim.x) G[g * RK + i] = src[i];
+  }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_off = M3 + 1;  // even offsets 0, 2, ..., 2 M3
   const size_t slab = (size_t)a.l_size * RK;
-  const long long base = a.tri_off[il3 * a.l_size + il2];
+  const bool m0 = a.parity == 0 && a.m_max == 0;
   // one warp per l1: its offsets of L1 in turn, so that each output has one writer
-  for (int il1 = t0 + warp; il1 <= t1; il1 += BI_WARPS) {
+  for (int il1 = lo + warp; il1 <= hi; il1 += BI_WARPS) {
     const int l1 = a.l[il1];
-    double acc[BI_MAX_Z];
+    double acc[BI_MAX_Z][BI_MAX_G2];
 #pragma unroll
-    for (int z = 0; z < BI_MAX_Z; ++z) acc[z] = 0.0;
-    const bool m0 = a.parity == 0 && a.m_max == 0;
+    for (int z = 0; z < BI_MAX_Z; ++z)
+#pragma unroll
+      for (int g = 0; g < BI_MAX_G2; ++g) acc[z][g] = 0.0;
     for (int o = 0; o < n_off; ++o) {
       const int L1 = abs(l1 - M3) + 2 * o;
       if (L1 > l1 + M3) continue;
-      if (!triangle(L1, l2, L3)) continue;
-      double s[BI_MAX_Z];
+      bool on[BI_MAX_G2];
+      bool any = false;
+#pragma unroll
+      for (int g = 0; g < BI_MAX_G2; ++g) {
+        on[g] = g < ng && il1 >= t0[g] && il1 <= t1[g] && triangle(L1, l2v[g], L3);
+        any = any || on[g];
+      }
+      if (!any) continue;
+      double s[BI_MAX_Z][BI_MAX_G2];
+#pragma unroll
+      for (int z = 0; z < BI_MAX_Z; ++z)
+#pragma unroll
+        for (int g = 0; g < BI_MAX_G2; ++g) s[z][g] = 0.0;
       const size_t off = o * slab + (size_t)il1 * RK;
-#pragma unroll
-      for (int z = 0; z < BI_MAX_Z; ++z) s[z] = 0.0;
+#pragma unroll 2
       for (int i = lane; i < RK; i += 32) {
-        const double gi = G[i];
+        double d[BI_MAX_Z];
 #pragma unroll
-        for (int z = 0; z < BI_MAX_Z; ++z)
-          if (z < a.bf) s[z] = fma(__ldg(&a.D[z][off + i]), gi, s[z]);
+        for (int z = 0; z < BI_MAX_Z; ++z) d[z] = (z < a.bf) ? __ldg(&a.D[z][off + i]) : 0.0;
+#pragma unroll
+        for (int g = 0; g < BI_MAX_G2; ++g)
+          if (on[g]) {
+            const double gi = G[g * RK + i];
+#pragma unroll
+            for (int z = 0; z < BI_MAX_Z; ++z)
+              if (z < a.bf) s[z][g] = fma(d[z], gi, s[z][g]);
+          }
       }
 #pragma unroll
       for (int z = 0; z < BI_MAX_Z; ++z)
 #pragma unroll
-        for (int w = 16; w; w >>= 1) s[z] += __shfl_xor_sync(0xffffffffu, s[z], w);
-      if (lane == 0) {
-        const double f = m0 ? 8.0 / (BI_PI * BI_PI * BI_PI)
-                            : geometry_factor(M3, a.offset_L3, a.parity, a.lf, l3, l2, l1, L3, L1);
+        for (int g = 0; g < BI_MAX_G2; ++g)
 #pragma unroll
-        for (int z = 0; z < BI_MAX_Z; ++z) acc[z] += f * s[z];
+          for (int w = 16; w; w >>= 1) s[z][g] += __shfl_xor_sync(0xffffffffu, s[z][g], w);
+      if (lane == 0) {
+#pragma unroll
+        for (int g = 0; g < BI_MAX_G2; ++g)
+          if (on[g]) {
+            const double f = m0 ? 8.0 / (BI_PI * BI_PI * BI_PI)
+                                : geometry_factor(M3, a.offset_L3, a.parity, a.lf, l3, l2v[g], l1, L3, L1);
+#pragma unroll
+            for (int z = 0; z < BI_MAX_Z; ++z) acc[z][g] += f * s[z][g];
+          }
       }
     }
     if (lane == 0) {
 #pragma unroll
-      for (int z = 0; z < BI_MAX_Z; ++z)
-        if (z < a.bf) {
-          double *dst = a.U[z] + base + (il1 - t0);
-          *dst = m0 ? acc[z] : *dst + acc[z];
+      for (int g = 0; g < BI_MAX_G2; ++g)
+        if (g < ng && il1 >= t0[g] && il1 <= t1[g]) {
+          const long long base = a.tri_off[il3 * a.l_size + il2_0 + g] + (il1 - t0[g]);
+#pragma unroll
+          for (int z = 0; z < BI_MAX_Z; ++z)
+            if (z < a.bf) {
+              double *dst = a.U[z] + base;
+              *dst = m0 ? acc[z][g] : *dst + acc[z][g];
+            }
         }
     }
   }
@@ -505,7 +558,7 @@ static void trapezoid(const double *x, int n, double *d) {
 struct song2_bispectra {
   song2_los *los = nullptr;
   S2LosView v{};
-  int bf = 0, bfs[3] = {0, 0, 0}, parity = 0, m_max = 0, m_size = 0;
+  int bf = 0, bfs[3] = {0, 0, 0}, parity = 0, m_max = 0, m_size = 0, g2 = 1;
   std::vector<int> m;
   int l_size = 0, r_size = 0, k_size = 0, q_size = 0;
   long long n_tri = 0, n_conf = 0;
@@ -628,6 +681,10 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
       return fail();
     }
   }
+  if ((double)h->l_size * v.n_pairs * R >= 2147483647.0) {
+    snprintf(err, SONG2_ERRLEN, "l_size * pairs * r_size too large for one k3 launch");
+    return fail();
+  }
   // Bessel rows of every order needed: l (first-order convolution) and
   // |l - M3| .. l + M3 (the extended list holds them)
   std::vector<int> row_of(v.l1[v.n_l1 - 1] + 1, -1);
@@ -736,7 +793,10 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   std::vector<double> ones(R, 0.5);  // the k2 trapezoid's 1/2
   std::vector<double> T1(bs->transfer1, bs->transfer1 + (size_t)h->bf * L * Q);
   const int *d_jxmin;
+  const double *d_jxmin_x;
   std::vector<int> jx(v.jxmin, v.jxmin + v.n_l1);
+  std::vector<double> jxx(v.n_l1);
+  for (int i = 0; i < v.n_l1; ++i) jxx[i] = s2los_x_of(jx[i], v.x_size, v.x_max);
   if (bup(h, lv, &h->d_l, err) || bup(h, row_of, &h->d_row_of_L, err) || bup(h, h->tri_min, &h->d_tri_min, err) ||
       bup(h, h->tri_max, &h->d_tri_max, err) || bup(h, h->tri_off, &h->d_tri_off, err) ||
       bup(h, un, &h->d_unit_n, err) || bup(h, uoff, &h->d_unit_off, err) || bup(h, udk, &h->d_unit_w, err) ||
@@ -745,7 +805,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
       bup(h, lf, &h->d_lf, err) || bup(h, q, &d_q, err) || bup(h, qw, &d_qw, err) || bup(h, qa, &d_qa, err) ||
       bup(h, qb, &d_qb, err) || bup(h, hk, &d_hk, err) || bup(h, S, &d_S, err) || bup(h, window, &d_win, err) ||
       bup(h, rfac, &d_rfac, err) || bup(h, ones, &d_ones, err) || bup(h, T1, &d_T1, err) ||
-      bup(h, qbeg, &d_qbeg, err) || bup(h, jx, &d_jxmin, err))
+      bup(h, qbeg, &d_qbeg, err) || bup(h, jx, &d_jxmin, err) || bup(h, jxx, &d_jxmin_x, err))
     return fail();
   void *tmp;
   if (balloc(h, sizeof(int) * 4, &tmp, err)) return fail();
@@ -754,6 +814,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   h->jt.tab = v.jtab_dev;
   h->jt.dd = v.ddj_dev;
   h->jt.xmin = d_jxmin;
+  h->jt.xmin_x = d_jxmin_x;
   h->jt.x_size = v.x_size;
   h->jt.x_max = v.x_max;
   h->jt.x_step = v.x_step;
@@ -845,7 +906,8 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
       snprintf(err, SONG2_ERRLEN, "r_size * k_size = %d * %d too large for the k1 integral's shared memory", R, K);
       return fail();
     }
-    CKB(cudaFuncSetAttribute(k1r_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    h->g2 = (BI_MAX_G2 * need <= (size_t)optin) ? BI_MAX_G2 : 1;
+    CKB(cudaFuncSetAttribute(k1r_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(need * h->g2)));
   }
   cudaEventCreate(&h->e0);
   cudaEventCreate(&h->e1);
@@ -898,8 +960,8 @@ extern "C" int song2_bispectra_run(song2_bispectra *h, const double *transfer2_d
         ka.T2 = transfer2_dev;
         ka.n_units = v.n_units;
         ka.I3 = h->d_I3;
-        long long warps = (long long)L * v.n_pairs;
-        k3_kernel<<<(unsigned)((warps + BI_WARPS - 1) / BI_WARPS), BI_THREADS, 0, st>>>(ka);
+        long long threads = (long long)L * v.n_pairs * R;
+        k3_kernel<<<(unsigned)((threads + BI_THREADS - 1) / BI_THREADS), BI_THREADS, 0, st>>>(ka);
         CKB(cudaGetLastError());
         for (int Y = 0; Y < bf; ++Y) {
           K2Args k2{};
@@ -934,7 +996,8 @@ extern "C" int song2_bispectra_run(song2_bispectra *h, const double *transfer2_d
             k1.U[Z] = h->d_U + ((size_t)(X * bf + Y) * bf + Z) * h->n_tri;
           }
           k1.lf = h->d_lf;
-          k1r_kernel<<<L * L, BI_THREADS, sizeof(double) * R * K, st>>>(k1);
+          k1.g2 = h->g2;
+          k1r_kernel<<<L * ((L + h->g2 - 1) / h->g2), BI_THREADS, sizeof(double) * R * K * h->g2, st>>>(k1);
           CKB(cudaGetLastError());
         }
       }
