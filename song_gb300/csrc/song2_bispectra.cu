@@ -316,6 +316,8 @@ constexpr int BI_MAX_Z = 3;
 struct K1Args {
   int l_size, r_size, k_size, M3, offset_L3, parity, m_max, bf;
   int g2;                        // l2 values per block
+  const double *geo;             // [o][packed triangle entry]: geometrical factor of (M3, L3, L1 offset 2o)
+  long long n_tri;
   const int *l;
   const int *tri_min, *tri_max;  // [l_size][l_size] index range of the third multipole
   const long long *tri_off;      // [l_size][l_size] offset in the packed triangle arrays
@@ -347,6 +349,31 @@ __device__ __noinline__ double geometry_factor(int M3, int offset_L3, int parity
   int exponent = even ? l3 + L3 - l1 - L1 : l3 + L3 - l1 - L1 - 1;
   double sign = ((exponent / 2) % 2 == 0) ? 1.0 : -1.0;
   return sign * prefactor * geometry;
+}
+
+// The geometrical factor of every packed (l3, l2, l1) triangle entry and even
+// offset of L1, for one (M3, offset_L3): one thread per value.
+struct GeoArgs {
+  int l_size, M3, offset_L3, parity, m_max, n_off;
+  long long n_tri;
+  const int *l;
+  const int *ta, *tb, *tc;  // [n_tri] index of l3, l2, l1 of each entry
+  const double *lf;
+  double *geo;              // [n_off][n_tri]
+};
+
+__global__ void geo_kernel(GeoArgs a) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.n_tri * a.n_off) return;
+  const int o = (int)(t / a.n_tri);
+  const long long e = t % a.n_tri;
+  const int l3 = a.l[a.ta[e]], l2 = a.l[a.tb[e]], l1 = a.l[a.tc[e]], M3 = a.M3;
+  const int L3 = abs(l3 - M3) + a.offset_L3, L1 = abs(l1 - M3) + 2 * o;
+  double v = 0.0;
+  if (M3 <= l3 && L3 <= l3 + M3 && L1 <= l1 + M3 && triangle(L1, l2, L3))
+    v = (a.parity == 0 && a.m_max == 0) ? 8.0 / (BI_PI * BI_PI * BI_PI)
+                                        : geometry_factor(M3, a.offset_L3, a.parity, a.lf, l3, l2, l1, L3, L1);
+  a.geo[t] = v;
 }
 
 constexpr int BI_MAX_G2 = 2;  // l2 values per block sharing the D loads
@@ -436,8 +463,8 @@ __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
 #pragma unroll
         for (int g = 0; g < BI_MAX_G2; ++g)
           if (on[g]) {
-            const double f = m0 ? 8.0 / (BI_PI * BI_PI * BI_PI)
-                                : geometry_factor(M3, a.offset_L3, a.parity, a.lf, l3, l2v[g], l1, L3, L1);
+            const double f =
+                a.geo[o * a.n_tri + a.tri_off[il3 * a.l_size + il2_0 + g] + (il1 - t0[g])];
 #pragma unroll
             for (int z = 0; z < BI_MAX_Z; ++z) acc[z][g] += f * s[z][g];
           }
@@ -571,6 +598,8 @@ struct song2_bispectra {
   JTab jt{};
   const int *d_l = nullptr, *d_row_of_L = nullptr, *d_tri_min = nullptr, *d_tri_max = nullptr;
   const int *d_unit_n = nullptr, *d_c1 = nullptr, *d_c2 = nullptr, *d_c3 = nullptr, *d_tt = nullptr;
+  const int *d_ta = nullptr, *d_tb = nullptr, *d_tc = nullptr;
+  double *d_geo = nullptr;  // [offset_L1 / 2][packed triangle entry]
   const long long *d_tri_off = nullptr, *d_unit_off = nullptr;
   const double *d_r = nullptr, *d_k = nullptr, *d_unit_w = nullptr, *d_lf = nullptr;
   double *d_C = nullptr;  // [bf][r][l][k]
@@ -723,6 +752,17 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
       h->tri_off[t] = h->n_tri;
       h->n_tri += std::max(0, h->tri_max[t] - h->tri_min[t] + 1);
     }
+  std::vector<int> ta(h->n_tri), tb(h->n_tri), tc(h->n_tri);
+  for (int a = 0; a < L; ++a)
+    for (int b = 0; b < L; ++b) {
+      int t = a * L + b;
+      for (int c = h->tri_min[t]; c <= h->tri_max[t]; ++c) {
+        long long e = h->tri_off[t] + (c - h->tri_min[t]);
+        ta[e] = a;
+        tb[e] = b;
+        tc[e] = c;
+      }
+    }
   h->n_conf = song2_bispectra_configs(L, v.l, nullptr, nullptr, nullptr);
   std::vector<int> c1(h->n_conf), c2(h->n_conf), c3(h->n_conf);
   song2_bispectra_configs(L, v.l, c1.data(), c2.data(), c3.data());
@@ -805,7 +845,8 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
       bup(h, lf, &h->d_lf, err) || bup(h, q, &d_q, err) || bup(h, qw, &d_qw, err) || bup(h, qa, &d_qa, err) ||
       bup(h, qb, &d_qb, err) || bup(h, hk, &d_hk, err) || bup(h, S, &d_S, err) || bup(h, window, &d_win, err) ||
       bup(h, rfac, &d_rfac, err) || bup(h, ones, &d_ones, err) || bup(h, T1, &d_T1, err) ||
-      bup(h, qbeg, &d_qbeg, err) || bup(h, jx, &d_jxmin, err) || bup(h, jxx, &d_jxmin_x, err))
+      bup(h, qbeg, &d_qbeg, err) || bup(h, jx, &d_jxmin, err) || bup(h, jxx, &d_jxmin_x, err) ||
+      bup(h, ta, &h->d_ta, err) || bup(h, tb, &h->d_tb, err) || bup(h, tc, &h->d_tc, err))
     return fail();
   void *tmp;
   if (balloc(h, sizeof(int) * 4, &tmp, err)) return fail();
@@ -895,6 +936,9 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   if (balloc(h, sizeof(double) * (size_t)h->bf * h->bf * h->bf * std::max<long long>(1, h->n_tri), &tmp, err))
     return fail();
   h->d_U = (double *)tmp;
+  if (balloc(h, sizeof(double) * (size_t)(h->m_max + 1) * std::max<long long>(1, h->n_tri), &tmp, err))
+    return fail();
+  h->d_geo = (double *)tmp;
   CKB(cudaFuncSetAttribute(k2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(sizeof(double) * BI_MAX_K * BI_MAX_K)));
   {
@@ -960,6 +1004,25 @@ extern "C" int song2_bispectra_run(song2_bispectra *h, const double *transfer2_d
         ka.T2 = transfer2_dev;
         ka.n_units = v.n_units;
         ka.I3 = h->d_I3;
+        GeoArgs ga{};
+        ga.l_size = L;
+        ga.M3 = M3;
+        ga.offset_L3 = oL3;
+        ga.parity = h->parity;
+        ga.m_max = h->m_max;
+        ga.n_off = M3 + 1;
+        ga.n_tri = h->n_tri;
+        ga.l = h->d_l;
+        ga.ta = h->d_ta;
+        ga.tb = h->d_tb;
+        ga.tc = h->d_tc;
+        ga.lf = h->d_lf;
+        ga.geo = h->d_geo;
+        if (h->n_tri > 0) {
+          long long ng = h->n_tri * (M3 + 1);
+          geo_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(ga);
+          CKB(cudaGetLastError());
+        }
         long long threads = (long long)L * v.n_pairs * R;
         k3_kernel<<<(unsigned)((threads + BI_THREADS - 1) / BI_THREADS), BI_THREADS, 0, st>>>(ka);
         CKB(cudaGetLastError());
@@ -997,6 +1060,8 @@ extern "C" int song2_bispectra_run(song2_bispectra *h, const double *transfer2_d
           }
           k1.lf = h->d_lf;
           k1.g2 = h->g2;
+          k1.geo = h->d_geo;
+          k1.n_tri = h->n_tri;
           k1r_kernel<<<L * ((L + h->g2 - 1) / h->g2), BI_THREADS, sizeof(double) * R * K * h->g2, st>>>(k1);
           CKB(cudaGetLastError());
         }
