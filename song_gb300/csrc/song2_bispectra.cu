@@ -322,7 +322,8 @@ struct K1Args {
   const int *tri_min, *tri_max;  // [l_size][l_size] index range of the third multipole
   const long long *tri_off;      // [l_size][l_size] offset in the packed triangle arrays
   const double *I2;              // [l3][l2][r][k]
-  const double *D[BI_MAX_Z];     // per Z: offset_L1 slabs [o][l1][r][k], o = offset_L1 / 2
+  const float2 *D[BI_MAX_Z];     // per Z: offset_L1 slabs [o][l1][r][k] as double-float (hi, lo), o = offset_L1 / 2
+  const int *De[BI_MAX_Z];       // per Z: [o][l1] power-of-two exponent of each scaled row
   const double *lf;              // ln n!
   double *U[BI_MAX_Z];           // per Z: unsymmetrised bispectrum of (X, Y, Z), packed
 };
@@ -378,8 +379,30 @@ __global__ void geo_kernel(GeoArgs a) {
 
 constexpr int BI_MAX_G2 = 2;  // l2 values per block sharing the D loads
 
-__global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
-  extern __shared__ double G[];  // [g][r][k]
+// Double-float arithmetic on the FP32 pipe (GB300's FP64 pipe is 64 times
+// narrower): a value is hi + lo with |lo| <= ulp(hi)/2; the product of two is
+// formed without error in its leading part (fmaf) and added to the running sum
+// by Knuth's two-sum, so a dot product keeps about 46 bits.
+__device__ __forceinline__ float2 df_split(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+
+__device__ __forceinline__ void df_fma(float2 d, float2 g, float &hi, float &lo) {
+  const float p = d.x * g.x;
+  float e = fmaf(d.x, g.x, -p);
+  e = fmaf(d.x, g.y, e);
+  e = fmaf(d.y, g.x, e);
+  const float s = hi + p;
+  const float v = s - hi;
+  lo += ((hi - (s - v)) + (p - v)) + e;
+  hi = s;
+}
+
+__global__ void __launch_bounds__(BI_THREADS, 2) k1r_kernel(K1Args a) {
+  extern __shared__ float2 G2[];  // [g][r][k], each (l3, l2) row scaled by 2^-e
+  __shared__ double red[BI_WARPS];
+  __shared__ int ge[BI_MAX_G2];
   const int n_grp = (a.l_size + a.g2 - 1) / a.g2;
   const int il3 = blockIdx.x / n_grp, il2_0 = (blockIdx.x % n_grp) * a.g2;
   const int l3 = a.l[il3], M3 = a.M3;
@@ -405,12 +428,27 @@ __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
     }
   }
   if (hi < lo) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // stage the k2 integrals, each row scaled to a largest magnitude in [0.5, 1)
   for (int g = 0; g < ng; ++g) {
     const double *src = a.I2 + ((size_t)il3 * a.l_size + il2_0 + g) * RK;
-    for (int i = threadIdx.x; i < RK; i += blockDim.x) G[g * RK + i] = src[i];
+    double m = 0.0;
+    for (int i = threadIdx.x; i < RK; i += blockDim.x) m = fmax(m, fabs(src[i]));
+    for (int w = 16; w; w >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, w));
+    if (lane == 0) red[warp] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double mm = 0.0;
+      for (int w = 0; w < BI_WARPS; ++w) mm = fmax(mm, red[w]);
+      int e = 0;
+      if (mm > 0.0) frexp(mm, &e);
+      ge[g] = e;
+    }
+    __syncthreads();
+    const int e = ge[g];
+    for (int i = threadIdx.x; i < RK; i += blockDim.x) G2[g * RK + i] = df_split(ldexp(src[i], -e));
+    __syncthreads();
   }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_off = M3 + 1;  // even offsets 0, 2, ..., 2 M3
   const size_t slab = (size_t)a.l_size * RK;
   const bool m0 = a.parity == 0 && a.m_max == 0;
@@ -433,32 +471,36 @@ __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
         any = any || on[g];
       }
       if (!any) continue;
+      float sh[BI_MAX_Z][BI_MAX_G2], sl[BI_MAX_Z][BI_MAX_G2];
+#pragma unroll
+      for (int z = 0; z < BI_MAX_Z; ++z)
+#pragma unroll
+        for (int g = 0; g < BI_MAX_G2; ++g) sh[z][g] = sl[z][g] = 0.0f;
+      const size_t off = o * slab + (size_t)il1 * RK;
+#pragma unroll 2
+      for (int i = lane; i < RK; i += 32) {
+        float2 d[BI_MAX_Z];
+#pragma unroll
+        for (int z = 0; z < BI_MAX_Z; ++z) d[z] = (z < a.bf) ? __ldg(&a.D[z][off + i]) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int g = 0; g < BI_MAX_G2; ++g)
+          if (on[g]) {
+            const float2 gi = G2[g * RK + i];
+#pragma unroll
+            for (int z = 0; z < BI_MAX_Z; ++z)
+              if (z < a.bf) df_fma(d[z], gi, sh[z][g], sl[z][g]);
+          }
+      }
       double s[BI_MAX_Z][BI_MAX_G2];
 #pragma unroll
       for (int z = 0; z < BI_MAX_Z; ++z)
 #pragma unroll
-        for (int g = 0; g < BI_MAX_G2; ++g) s[z][g] = 0.0;
-      const size_t off = o * slab + (size_t)il1 * RK;
-#pragma unroll 2
-      for (int i = lane; i < RK; i += 32) {
-        double d[BI_MAX_Z];
+        for (int g = 0; g < BI_MAX_G2; ++g) {
+          double v = (double)sh[z][g] + (double)sl[z][g];
 #pragma unroll
-        for (int z = 0; z < BI_MAX_Z; ++z) d[z] = (z < a.bf) ? __ldg(&a.D[z][off + i]) : 0.0;
-#pragma unroll
-        for (int g = 0; g < BI_MAX_G2; ++g)
-          if (on[g]) {
-            const double gi = G[g * RK + i];
-#pragma unroll
-            for (int z = 0; z < BI_MAX_Z; ++z)
-              if (z < a.bf) s[z][g] = fma(d[z], gi, s[z][g]);
-          }
-      }
-#pragma unroll
-      for (int z = 0; z < BI_MAX_Z; ++z)
-#pragma unroll
-        for (int g = 0; g < BI_MAX_G2; ++g)
-#pragma unroll
-          for (int w = 16; w; w >>= 1) s[z][g] += __shfl_xor_sync(0xffffffffu, s[z][g], w);
+          for (int w = 16; w; w >>= 1) v += __shfl_xor_sync(0xffffffffu, v, w);
+          s[z][g] = v;
+        }
       if (lane == 0) {
 #pragma unroll
         for (int g = 0; g < BI_MAX_G2; ++g)
@@ -466,7 +508,8 @@ __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
             const double f =
                 a.geo[o * a.n_tri + a.tri_off[il3 * a.l_size + il2_0 + g] + (il1 - t0[g])];
 #pragma unroll
-            for (int z = 0; z < BI_MAX_Z; ++z) acc[z][g] += f * s[z][g];
+            for (int z = 0; z < BI_MAX_Z; ++z)
+              if (z < a.bf) acc[z][g] += f * ldexp(s[z][g], a.De[z][o * a.l_size + il1] + ge[g]);
           }
       }
     }
@@ -484,6 +527,33 @@ __global__ void __launch_bounds__(BI_THREADS) k1r_kernel(K1Args a) {
         }
     }
   }
+}
+
+// D rows (l1 of one (Z, offset) slab) scaled to a largest magnitude in
+// [0.5, 1) and split into double-float; one block per row.
+__global__ void split_rows_kernel(const double *__restrict__ D, int rows, int RK, float2 *__restrict__ D2,
+                                  int *__restrict__ De) {
+  __shared__ double red[BI_WARPS];
+  __shared__ int e_s;
+  const int row = blockIdx.x;
+  if (row >= rows) return;
+  const double *src = D + (size_t)row * RK;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < RK; i += blockDim.x) m = fmax(m, fabs(src[i]));
+  for (int w = 16; w; w >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, w));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmax(mm, red[w]);
+    int e = 0;
+    if (mm > 0.0) frexp(mm, &e);
+    e_s = e;
+    De[row] = e;
+  }
+  __syncthreads();
+  const int e = e_s;
+  for (int i = threadIdx.x; i < RK; i += blockDim.x) D2[(size_t)row * RK + i] = df_split(ldexp(src[i], -e));
 }
 
 // ------------------------------------------------------------ symmetrisation
@@ -603,7 +673,9 @@ struct song2_bispectra {
   const long long *d_tri_off = nullptr, *d_unit_off = nullptr;
   const double *d_r = nullptr, *d_k = nullptr, *d_unit_w = nullptr, *d_lf = nullptr;
   double *d_C = nullptr;  // [bf][r][l][k]
-  double *d_D = nullptr;  // [bf][(im, offset_L1/2)][r][l][k]
+  double *d_D = nullptr;  // [bf][(im, offset_L1/2)][l][r][k]
+  float2 *d_D2 = nullptr; // the same, scaled per row, as double-float
+  int *d_De = nullptr;    // [bf][(im, offset_L1/2)][l]: the rows' exponents
   std::vector<long long> d_slot;  // D slot of (im, offset_L1) pairs: index im * (m_max + 1) + offset_L1 / 2
   long long n_dslots = 0;
   double *d_I3 = nullptr, *d_I2 = nullptr, *d_U = nullptr;
@@ -921,6 +993,15 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
       }
     }
   }
+  {
+    const int rows = h->bf * (int)h->n_dslots * L;
+    if (balloc(h, sizeof(float2) * (size_t)rows * R * K, &tmp, err)) return fail();
+    h->d_D2 = (float2 *)tmp;
+    if (balloc(h, sizeof(int) * (size_t)rows, &tmp, err)) return fail();
+    h->d_De = (int *)tmp;
+    split_rows_kernel<<<rows, 256>>>(h->d_D, rows, R * K, h->d_D2, h->d_De);
+    CKB(cudaGetLastError());
+  }
   CKB(cudaDeviceSynchronize());
   int st[4];
   CKB(cudaMemcpy(st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost));
@@ -945,7 +1026,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    size_t need = sizeof(double) * (size_t)R * K;
+    size_t need = sizeof(float2) * (size_t)R * K;
     if (need > (size_t)optin) {
       snprintf(err, SONG2_ERRLEN, "r_size * k_size = %d * %d too large for the k1 integral's shared memory", R, K);
       return fail();
@@ -1055,14 +1136,16 @@ extern "C" int song2_bispectra_run(song2_bispectra *h, const double *transfer2_d
           k1.tri_off = h->d_tri_off;
           k1.I2 = h->d_I2;
           for (int Z = 0; Z < bf; ++Z) {
-            k1.D[Z] = h->d_D + ((size_t)Z * h->n_dslots + h->d_slot[(size_t)im * (h->m_max + 1)]) * slab;
+            const size_t sl0 = (size_t)Z * h->n_dslots + h->d_slot[(size_t)im * (h->m_max + 1)];
+            k1.D[Z] = h->d_D2 + sl0 * slab;
+            k1.De[Z] = h->d_De + sl0 * L;
             k1.U[Z] = h->d_U + ((size_t)(X * bf + Y) * bf + Z) * h->n_tri;
           }
           k1.lf = h->d_lf;
           k1.g2 = h->g2;
           k1.geo = h->d_geo;
           k1.n_tri = h->n_tri;
-          k1r_kernel<<<L * ((L + h->g2 - 1) / h->g2), BI_THREADS, sizeof(double) * R * K * h->g2, st>>>(k1);
+          k1r_kernel<<<L * ((L + h->g2 - 1) / h->g2), BI_THREADS, sizeof(float2) * R * K * h->g2, st>>>(k1);
           CKB(cudaGetLastError());
         }
       }
