@@ -262,17 +262,39 @@ __global__ void __launch_bounds__(BI_THREADS) k3_kernel(K3Args a) {
 }
 
 // ------------------------------------------------------------ k2 integral
+// Double-float arithmetic on the FP32 pipe (GB300's FP64 pipe is 64 times
+// narrower): a value is hi + lo with |lo| <= ulp(hi)/2; the product of two is
+// formed without error in its leading part (fmaf) and added to the running sum
+// by Knuth's two-sum, so a dot product keeps about 46 bits.
+__device__ __forceinline__ float2 df_split(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+
+__device__ __forceinline__ void df_fma(float2 d, float2 g, float &hi, float &lo) {
+  const float p = d.x * g.x;
+  float e = fmaf(d.x, g.x, -p);
+  e = fmaf(d.x, g.y, e);
+  e = fmaf(d.y, g.x, e);
+  const float s = hi + p;
+  const float v = s - hi;
+  lo += ((hi - (s - v)) + (p - v)) + e;
+  hi = s;
+}
+
 struct K2Args {
   int l_size, r_size, k_size, n_pairs, M3;
   const int *l;
   const double *k;
   const double *I3;  // [l3][r][pair]
-  const double *C;   // [r][l2][k]
+  const float2 *C;   // [r][l2][k] as double-float, each (r, l2) row scaled by 2^-Ce
+  const int *Ce;     // [r][l2]
   double *I2;        // [l3][l2][r][k1]
 };
 
 __global__ void __launch_bounds__(BI_THREADS) k2_kernel(K2Args a) {
-  extern __shared__ double F[];  // [k1][k]
+  extern __shared__ double F[];  // [k1][k] doubles, then the same as double-float
+  __shared__ int fe[BI_MAX_K];
   const int il3 = blockIdx.x / a.r_size, ir = blockIdx.x % a.r_size;
   const int K = a.k_size;
   if (a.M3 > a.l[il3]) {
@@ -282,6 +304,7 @@ __global__ void __launch_bounds__(BI_THREADS) k2_kernel(K2Args a) {
     }
     return;
   }
+  float2 *F2 = (float2 *)(F + K * K);
   const double *I = a.I3 + ((size_t)il3 * a.r_size + ir) * a.n_pairs;
   for (int i = threadIdx.x; i < K * K; i += blockDim.x) {
     int k1 = i / K, k2 = i % K;
@@ -298,13 +321,27 @@ __global__ void __launch_bounds__(BI_THREADS) k2_kernel(K2Args a) {
     F[i] = v;
   }
   __syncthreads();
+  // each k1 row scaled to a largest magnitude in [0.5, 1), split into double-float
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int k1 = warp; k1 < K; k1 += BI_WARPS) {
+    double m = 0.0;
+    for (int j = lane; j < K; j += 32) m = fmax(m, fabs(F[k1 * K + j]));
+    for (int w = 16; w; w >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, w));
+    int e = 0;
+    if (m > 0.0) frexp(m, &e);
+    if (lane == 0) fe[k1] = e;
+    for (int j = lane; j < K; j += 32) F2[k1 * K + j] = df_split(ldexp(F[k1 * K + j], -e));
+  }
+  __syncthreads();
   for (int i = threadIdx.x; i < a.l_size * K; i += blockDim.x) {
     int il2 = i / K, k1 = i % K;
-    const double *c = a.C + ((size_t)ir * a.l_size + il2) * K;
-    const double *f = F + k1 * K;
-    double s = 0.0;
-    for (int j = 0; j < K; ++j) s += c[j] * f[j];
-    a.I2[(((size_t)il3 * a.l_size + il2) * a.r_size + ir) * K + k1] = s;
+    const size_t row = (size_t)ir * a.l_size + il2;
+    const float2 *c = a.C + row * K;
+    const float2 *f = F2 + k1 * K;
+    float hi = 0.f, lo = 0.f;
+    for (int j = 0; j < K; ++j) df_fma(__ldg(&c[j]), f[j], hi, lo);
+    a.I2[(((size_t)il3 * a.l_size + il2) * a.r_size + ir) * K + k1] =
+        ldexp((double)hi + (double)lo, __ldg(&a.Ce[row]) + fe[k1]);
   }
 }
 
@@ -378,26 +415,6 @@ __global__ void geo_kernel(GeoArgs a) {
 }
 
 constexpr int BI_MAX_G2 = 2;  // l2 values per block sharing the D loads
-
-// Double-float arithmetic on the FP32 pipe (GB300's FP64 pipe is 64 times
-// narrower): a value is hi + lo with |lo| <= ulp(hi)/2; the product of two is
-// formed without error in its leading part (fmaf) and added to the running sum
-// by Knuth's two-sum, so a dot product keeps about 46 bits.
-__device__ __forceinline__ float2 df_split(double x) {
-  const float h = __double2float_rn(x);
-  return make_float2(h, __double2float_rn(x - (double)h));
-}
-
-__device__ __forceinline__ void df_fma(float2 d, float2 g, float &hi, float &lo) {
-  const float p = d.x * g.x;
-  float e = fmaf(d.x, g.x, -p);
-  e = fmaf(d.x, g.y, e);
-  e = fmaf(d.y, g.x, e);
-  const float s = hi + p;
-  const float v = s - hi;
-  lo += ((hi - (s - v)) + (p - v)) + e;
-  hi = s;
-}
 
 __global__ void __launch_bounds__(BI_THREADS, 2) k1r_kernel(K1Args a) {
   extern __shared__ float2 G2[];  // [g][r][k], each (l3, l2) row scaled by 2^-e
@@ -675,6 +692,8 @@ struct song2_bispectra {
   double *d_C = nullptr;  // [bf][r][l][k]
   double *d_D = nullptr;  // [bf][(im, offset_L1/2)][l][r][k]
   float2 *d_D2 = nullptr; // the same, scaled per row, as double-float
+  float2 *d_C2 = nullptr; // C scaled per (Y, r, l2) row, as double-float
+  int *d_Ce = nullptr;
   int *d_De = nullptr;    // [bf][(im, offset_L1/2)][l]: the rows' exponents
   std::vector<long long> d_slot;  // D slot of (im, offset_L1) pairs: index im * (m_max + 1) + offset_L1 / 2
   long long n_dslots = 0;
@@ -1001,6 +1020,13 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
     h->d_De = (int *)tmp;
     split_rows_kernel<<<rows, 256>>>(h->d_D, rows, R * K, h->d_D2, h->d_De);
     CKB(cudaGetLastError());
+    const int crows = h->bf * R * L;
+    if (balloc(h, sizeof(float2) * (size_t)crows * K, &tmp, err)) return fail();
+    h->d_C2 = (float2 *)tmp;
+    if (balloc(h, sizeof(int) * (size_t)crows, &tmp, err)) return fail();
+    h->d_Ce = (int *)tmp;
+    split_rows_kernel<<<crows, 64>>>(h->d_C, crows, K, h->d_C2, h->d_Ce);
+    CKB(cudaGetLastError());
   }
   CKB(cudaDeviceSynchronize());
   int st[4];
@@ -1020,12 +1046,16 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   if (balloc(h, sizeof(double) * (size_t)(h->m_max + 1) * std::max<long long>(1, h->n_tri), &tmp, err))
     return fail();
   h->d_geo = (double *)tmp;
-  CKB(cudaFuncSetAttribute(k2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(sizeof(double) * BI_MAX_K * BI_MAX_K)));
   {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t need2 = (sizeof(double) + sizeof(float2)) * (size_t)K * K;
+    if (need2 > (size_t)optin) {
+      snprintf(err, SONG2_ERRLEN, "k_size = %d too large for the k2 integral's shared memory", K);
+      return fail();
+    }
+    CKB(cudaFuncSetAttribute(k2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need2));
     size_t need = sizeof(float2) * (size_t)R * K;
     if (need > (size_t)optin) {
       snprintf(err, SONG2_ERRLEN, "r_size * k_size = %d * %d too large for the k1 integral's shared memory", R, K);
@@ -1117,9 +1147,10 @@ extern "C" int song2_bispectra_run(song2_bispectra *h, const double *transfer2_d
           k2.l = h->d_l;
           k2.k = h->d_k;
           k2.I3 = h->d_I3;
-          k2.C = h->d_C + (size_t)Y * slab;
+          k2.C = h->d_C2 + (size_t)Y * slab;
+          k2.Ce = h->d_Ce + (size_t)Y * R * L;
           k2.I2 = h->d_I2;
-          k2_kernel<<<L * R, BI_THREADS, sizeof(double) * K * K, st>>>(k2);
+          k2_kernel<<<L * R, BI_THREADS, (sizeof(double) + sizeof(float2)) * K * K, st>>>(k2);
           CKB(cudaGetLastError());
           K1Args k1{};
           k1.l_size = L;
