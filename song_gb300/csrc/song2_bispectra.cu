@@ -115,20 +115,20 @@ __device__ double w6j(int a, int b, int c, int d, int e, int f, const double *__
 struct JTab {
   const double *tab, *dd;
   const int *xmin;     // per row: first stored x index
-  const double *xmin_x;  // per row: its x (the lin_space node)
+  const double *xmin_u;  // per row: its x (the lin_space node) over x_step
   int x_size;
   double x_max, x_step, inv_step;
   int cubic;
   int *status;
 };
 
-__device__ __forceinline__ double jl_at(const JTab &t, int row, double x) {
-  const double xm = __ldg(&t.xmin_x[row]);
-  if (x < xm) return 0.0;
-  const int x0 = __ldg(&t.xmin[row]);
+// j_L(k r) with rs = r / x_step: u = (k r - x_min) / x_step as one fma
+__device__ __forceinline__ double jl_at(const JTab &t, int row, double k, double rs) {
   // index and weight of bessel2_convolution, (xm + x_step (ix + 1) - x) / x_step,
-  // written as ix + 1 - u with u = (x - xm) / x_step
-  const double u = (x - xm) * t.inv_step;
+  // written as ix + 1 - u
+  const double u = fma(k, rs, -__ldg(&t.xmin_u[row]));
+  if (u < 0.0) return 0.0;
+  const int x0 = __ldg(&t.xmin[row]);
   int ix = (int)u;
   if (x0 + ix + 1 >= t.x_size) {  // outside the table: record and drop the term
     atomicOr(t.status, 1);
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(128) coef_kernel(CoefArgs a) {
     for (int k = threadIdx.x; k < a.k_size; k += blockDim.x) out[k] = 0.0;
     return;
   }
-  const double r = a.r[ir];
+  const double rs = a.r[ir] * a.jt.inv_step;
   const double *T = a.T1 + (size_t)il * a.q_size;
   for (int i = threadIdx.x; i < a.k_size; i += blockDim.x) {
     double sa = 0, sb = 0, ssa = 0, ssb = 0;
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(128) coef_kernel(CoefArgs a) {
       for (int iq = a.qbeg[i]; iq < a.qbeg[i + 1]; ++iq) {
         double g = T[iq];
         if (g == 0.0) continue;
-        double c = a.qw[iq] * jl_at(a.jt, row, a.q[iq] * r) * g;
+        double c = a.qw[iq] * jl_at(a.jt, row, a.q[iq], rs) * g;
         double wa = a.qa[iq], wb = a.qb[iq];
         sa += c * wa;
         sb += c * wb;
@@ -248,12 +248,12 @@ __global__ void __launch_bounds__(BI_THREADS) k3_kernel(K3Args a) {
   const int n = a.unit_n[p];
   const double *T = a.T2 + (size_t)tt * a.n_units + u0;
   const double *kk = a.unit_k + u0, *wk = a.unit_w + u0;
-  const double r = a.r[ir];
+  const double rs = a.r[ir] * a.jt.inv_step;
   double s = 0.0;
   for (int i = 0; i < n; ++i) {
     double f = __ldg(&T[i]);
     if (f == 0.0) continue;
-    double j = jl_at(a.jt, row, __ldg(&kk[i]) * r);
+    double j = jl_at(a.jt, row, __ldg(&kk[i]), rs);
     s = fma(__ldg(&wk[i]) * f, j, s);
   }
   double v = 0.5 * s;
@@ -924,10 +924,10 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   std::vector<double> ones(R, 0.5);  // the k2 trapezoid's 1/2
   std::vector<double> T1(bs->transfer1, bs->transfer1 + (size_t)h->bf * L * Q);
   const int *d_jxmin;
-  const double *d_jxmin_x;
+  const double *d_jxmin_u;
   std::vector<int> jx(v.jxmin, v.jxmin + v.n_l1);
-  std::vector<double> jxx(v.n_l1);
-  for (int i = 0; i < v.n_l1; ++i) jxx[i] = s2los_x_of(jx[i], v.x_size, v.x_max);
+  std::vector<double> jxu(v.n_l1);
+  for (int i = 0; i < v.n_l1; ++i) jxu[i] = s2los_x_of(jx[i], v.x_size, v.x_max) / v.x_step;
   if (bup(h, lv, &h->d_l, err) || bup(h, row_of, &h->d_row_of_L, err) || bup(h, h->tri_min, &h->d_tri_min, err) ||
       bup(h, h->tri_max, &h->d_tri_max, err) || bup(h, h->tri_off, &h->d_tri_off, err) ||
       bup(h, un, &h->d_unit_n, err) || bup(h, uoff, &h->d_unit_off, err) || bup(h, udk, &h->d_unit_w, err) ||
@@ -936,7 +936,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
       bup(h, lf, &h->d_lf, err) || bup(h, q, &d_q, err) || bup(h, qw, &d_qw, err) || bup(h, qa, &d_qa, err) ||
       bup(h, qb, &d_qb, err) || bup(h, hk, &d_hk, err) || bup(h, S, &d_S, err) || bup(h, window, &d_win, err) ||
       bup(h, rfac, &d_rfac, err) || bup(h, ones, &d_ones, err) || bup(h, T1, &d_T1, err) ||
-      bup(h, qbeg, &d_qbeg, err) || bup(h, jx, &d_jxmin, err) || bup(h, jxx, &d_jxmin_x, err) ||
+      bup(h, qbeg, &d_qbeg, err) || bup(h, jx, &d_jxmin, err) || bup(h, jxu, &d_jxmin_u, err) ||
       bup(h, ta, &h->d_ta, err) || bup(h, tb, &h->d_tb, err) || bup(h, tc, &h->d_tc, err))
     return fail();
   void *tmp;
@@ -946,7 +946,7 @@ extern "C" int song2_bispectra_create(song2_los *los, const song2_bispectra_spec
   h->jt.tab = v.jtab_dev;
   h->jt.dd = v.ddj_dev;
   h->jt.xmin = d_jxmin;
-  h->jt.xmin_x = d_jxmin_x;
+  h->jt.xmin_u = d_jxmin_u;
   h->jt.x_size = v.x_size;
   h->jt.x_max = v.x_max;
   h->jt.x_step = v.x_step;
