@@ -31,7 +31,11 @@ not available).
                and the error on the accuracy sample.
   transfer2    the line-of-sight integral (transfer2) of this run's sources on
                the device: transfer functions/s, the projection-table build, the
-               CPU restatement on the heaviest pairs as baseline and parity check.
+               CPU restatement on the heaviest pairs as baseline and parity check;
+               inside it, bispectra: the intrinsic bispectrum (bispectra2) of
+               those transfers still in HBM (T and E, synthetic first-order
+               transfers), and the CPU restatement against the GPU on the same
+               inputs with the l list cut to --bi-cpu-l multipoles.
   err_vs_fp64_oracle
                per (source type, triplet) max_tau |S - S_ref| / max_tau |S_ref| of
                the GPU sources against the oracle at rtol 1e-8, on triplets spread
