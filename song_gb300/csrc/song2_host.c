@@ -233,42 +233,80 @@ static double dtau_dlna(const bg_params *p, double lna) {
 
 /* Peebles three-level hydrogen recombination (Peebles 1968, with the
    case-B recombination fit of Pequignot et al. 1991 and the fudge factor 1.14
-   of Seager, Sasselov & Scott 1999); helium is taken as neutral and the
-   matter temperature equal to the radiation temperature.  Returns x_e(z) on
-   a table of z. */
+   of Seager, Sasselov & Scott 1999), helium in Saha equilibrium for both of
+   its ionisations (He III -> He II at 54.4 eV, He II -> He I at 24.6 eV, the
+   way RECFAST starts its history), and the matter temperature equal to the
+   radiation temperature.  Returns x_e(z) = n_e / n_H on a table of z. */
 typedef struct { int n; double z0, dz; double *xe; } xe_table;
 
-static double saha_xe(double T, double nH) {
-  /* x^2/(1-x) = (2 pi m_e k T / h^2)^{3/2} e^{-13.6eV/kT} / n_H */
-  double S = pow(2.0 * M_PI * M_ELECTRON * K_B * T / (H_PLANCK * H_PLANCK), 1.5) *
-             exp(-13.605693 * EV / (K_B * T)) / nH;
-  if (S > 1e20) return 1.0;
-  return 0.5 * (-S + sqrt(S * S + 4.0 * S));
+
+/* Saha factors (2 pi m_e k T / h^2)^{3/2} e^{-E/kT} times the ratio of the
+   statistical weights, for hydrogen (1), He II -> He III (1) and He I -> He II (4) */
+typedef struct { double H, He2, He1; } saha_s;
+
+static saha_s saha_factors(double T) {
+  double q = pow(2.0 * M_PI * M_ELECTRON * K_B * T / (H_PLANCK * H_PLANCK), 1.5);
+  saha_s f;
+  f.H = q * exp(-13.605693 * EV / (K_B * T));
+  f.He2 = q * exp(-54.4177650 * EV / (K_B * T));
+  f.He1 = 4.0 * q * exp(-24.5873876 * EV / (K_B * T));
+  return f;
+}
+
+/* electrons per hydrogen nucleus from helium at electron density ne (m^-3) */
+static double helium_electrons(const saha_s *f, double ne, double fHe) {
+  double r1 = f->He1 / ne, r2 = f->He2 / ne; /* n_HeII/n_HeI, n_HeIII/n_HeII */
+  if (!(r1 < 1e300)) return 2.0 * fHe;
+  double den = 1.0 + r1 + r1 * r2;
+  if (!(den < 1e300)) return 2.0 * fHe;
+  return fHe * (r1 + 2.0 * r1 * r2) / den;
+}
+
+/* x_e with hydrogen and helium all in Saha equilibrium: bisection on the
+   increasing x - (x_HII(x) + helium(x)) over [0, 1 + 2 fHe]; also returns x_HII */
+static double saha_all(const saha_s *f, double nH, double fHe, double *xH_out) {
+  double lo = 0.0, hi = 1.0 + 2.0 * fHe;
+  for (int it = 0; it < 200; ++it) {
+    double x = 0.5 * (lo + hi);
+    double ne = x * nH;
+    double xH = 1.0 / (1.0 + ne / f->H);
+    double g = x - (xH + helium_electrons(f, ne, fHe));
+    if (g > 0) hi = x;
+    else lo = x;
+  }
+  double x = 0.5 * (lo + hi);
+  *xH_out = 1.0 / (1.0 + x * nH / f->H);
+  return x;
 }
 
 static int recombination(const song2_cosmo *c, const bg_params *bp, xe_table *tab) {
   double h = c->h;
   double nH0 = (1.0 - c->YHe) * c->omega_b * RHO_CRIT_H2 / M_H; /* m^-3 (omega_b = Omega_b h^2) */
+  /* helium nuclei per hydrogen nucleus, with RECFAST's m_He / m_H */
+  double fHe = c->YHe / (3.9715 * (1.0 - c->YHe));
   tab->n = 40001; tab->z0 = 0.0; tab->dz = 0.25; /* z in [0, 10000] */
   tab->xe = (double *)malloc(sizeof(double) * tab->n);
   if (!tab->xe) return 1;
   (void)h;
   const double lambda_a = 121.5682e-9, Lambda2s = 8.2245809, E2s = 13.605693 * EV / 4.0;
   const double Ealpha = 13.605693 * EV * 0.75;
-  /* march from z = 10000 down; Saha until x drops below 0.985, then Peebles
-     with a backward-Euler step solved by Newton iteration on x */
+  /* march from z = 10000 down; everything in Saha equilibrium until x_HII
+     drops below 0.985, then Peebles for x = x_HII with a backward-Euler step
+     solved by Newton iteration, helium in Saha at the electron density of the
+     step */
   int peebles = 0;
   double x = 1.0;
   for (int i = tab->n - 1; i >= 0; --i) {
     double z = tab->z0 + i * tab->dz;
     double T = c->T_cmb * (1.0 + z);
     double nH = nH0 * pow(1.0 + z, 3);
+    saha_s sf = saha_factors(T);
     if (!peebles) {
-      double xs = saha_xe(T, nH);
-      if (xs > 0.985) { x = xs; tab->xe[i] = x; continue; }
-      peebles = 1;
-      x = xs;
-      tab->xe[i] = x;
+      double xH;
+      double xe = saha_all(&sf, nH, fHe, &xH);
+      x = xH;
+      tab->xe[i] = xe;
+      if (xH <= 0.985) peebles = 1;
       continue;
     }
     /* one backward-Euler step from z+dz to z: x_new = x_old - dz * f(z, x_new) where
@@ -300,7 +338,7 @@ static int recombination(const song2_cosmo *c, const bg_params *bp, xe_table *ta
       if (fabs(step) < 1e-14 * fabs(xn)) break;
     }
     x = xn;
-    tab->xe[i] = x;
+    tab->xe[i] = x + helium_electrons(&sf, x * nH, fHe);
   }
   return 0;
 }
