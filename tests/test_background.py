@@ -30,3 +30,22 @@ def test_start_time_bisection(lib):
     assert lib.song2_start_time(C.byref(p.spec), C.byref(p.tables), 0.1, 200.0, C.byref(ti), err) == 0
     # k/aH = 0.07 at the start for large k: tau_ini ~ 0.7 Mpc in the radiation era
     assert 0.5 < ti.value < 0.8
+
+
+def test_ionisation_history_with_helium(lib):
+    """x_e = n_e / n_H from the tabulated kappa' = a n_e sigma_T (n_H scales as
+    a^-3): the plateaux of fully ionised helium (1 + 2 f_He), singly ionised
+    helium (1 + f_He) and neutral helium with ionised hydrogen (1), f_He =
+    Y_He / (3.9715 (1 - Y_He)) for Y_He = 0.24, then hydrogen recombination."""
+    p = problem()
+    a = np.exp(p.bg[:, capi.BG_LN_A])
+    z = 1 / a - 1
+    xr = np.exp(p.bg[:, capi.BG_LN_KAPPA_DOT]) * a * a   # proportional to x_e
+    f_he = 0.24 / (3.9715 * 0.76)
+
+    def xe_at(zz):
+        return np.interp(zz, z[::-1], xr[::-1])
+    norm = xe_at(9500.0) / (1 + 2 * f_he)                # z = 9500: everything ionised
+    assert abs(xe_at(3500.0) / norm - (1 + f_he)) < 2e-3 * (1 + f_he)
+    assert abs(xe_at(1800.0) / norm - 1.0) < 5e-3
+    assert xe_at(800.0) / norm < 0.01
