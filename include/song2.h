@@ -80,9 +80,13 @@ enum song2_fo_index {
   SONG2_FO_I  /* first multipole block; E, N follow, see song2_fo_size() */
 };
 
-/* Cosmological parameters of the flat LCDM background. */
+/* Cosmological parameters of the flat LCDM background.  z_reio > 0 adds
+   reionisation in the form of CLASS's reio_camb: hydrogen and helium's first
+   ionisation by a tanh in (1+z)^{3/2} of width 0.5 in z centred on z_reio,
+   helium's second by a tanh of width 0.5 at z = 3.5; z_reio = 0: none. */
 typedef struct {
   double h, omega_b, omega_cdm, N_eff, T_cmb, YHe;
+  double z_reio;
 } song2_cosmo;
 
 /* Problem specification: the hot-path subset of SONG's precision2/perturbs2

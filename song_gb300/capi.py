@@ -44,7 +44,7 @@ def fo_size(fo_l_max):
 
 class Cosmo(C.Structure):
     _fields_ = [("h", C.c_double), ("omega_b", C.c_double), ("omega_cdm", C.c_double),
-                ("N_eff", C.c_double), ("T_cmb", C.c_double), ("YHe", C.c_double)]
+                ("N_eff", C.c_double), ("T_cmb", C.c_double), ("YHe", C.c_double), ("z_reio", C.c_double)]
 
 
 class Spec(C.Structure):

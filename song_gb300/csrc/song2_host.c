@@ -343,6 +343,17 @@ static int recombination(const song2_cosmo *c, const bg_params *bp, xe_table *ta
   return 0;
 }
 
+/* reionisation (CLASS's reio_camb with its default widths): x_e rises from its
+   recombination value to 1 + f_He around z_reio along a tanh in (1+z)^{3/2},
+   and by f_He more around z = 3.5 as helium ionises again */
+static double xe_reio(double xe_rec, double z, double z_reio, double fHe) {
+  const double ex = 1.5, width = 0.5, z_he = 3.5, width_he = 0.5;
+  double arg = (pow(1.0 + z_reio, ex) - pow(1.0 + z, ex)) / (ex * pow(1.0 + z_reio, ex - 1.0)) / width;
+  double xe = (1.0 + fHe - xe_rec) * (tanh(arg) + 1.0) / 2.0 + xe_rec;
+  xe += fHe * (tanh((z_he - z) / width_he) + 1.0) / 2.0;
+  return xe;
+}
+
 static double xe_at_z(const xe_table *t, double z) {
   if (z >= t->z0 + (t->n - 1) * t->dz) return t->xe[t->n - 1];
   if (z <= t->z0) return t->xe[0];
@@ -419,6 +430,7 @@ int song2_background_compute(const song2_cosmo *c, int bg_size, double *bg, doub
     double taun = exp(lt);
     double z = 1.0 / a - 1.0;
     double xe = xe_at_z(&xt, z);
+    if (c->z_reio > 0) xe = xe_reio(xe, z, c->z_reio, c->YHe / (3.9715 * (1.0 - c->YHe)));
     double ne = xe * nH0 / (a * a * a);
     kdot[i] = a * ne * SIGMA_T * MPC_M;
     double *row = bg + (size_t)i * SONG2_BG_SIZE;

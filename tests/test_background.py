@@ -49,3 +49,30 @@ def test_ionisation_history_with_helium(lib):
     assert abs(xe_at(3500.0) / norm - (1 + f_he)) < 2e-3 * (1 + f_he)
     assert abs(xe_at(1800.0) / norm - 1.0) < 5e-3
     assert xe_at(800.0) / norm < 0.01
+
+
+def test_reionisation_optical_depth(lib):
+    """z_reio = 7.7 (CLASS's reio_camb): x_e = 1 + 2 f_He today, 1 + f_He at
+    z = 5, the recombination value at z = 30, and an optical depth to z = 30 of
+    about 0.055 (Planck's tau_reio for that redshift); z_reio = 0 leaves the
+    history untouched."""
+    from song_gb300.problem import DEFAULT_COSMO
+    base = problem()
+    cosmo = dict(DEFAULT_COSMO, z_reio=7.7)
+    p = problem(cosmo=cosmo)
+    a = np.exp(p.bg[:, capi.BG_LN_A])
+    z = 1 / a - 1
+    xr = np.exp(p.bg[:, capi.BG_LN_KAPPA_DOT]) * a * a
+    xr0 = np.exp(base.bg[:, capi.BG_LN_KAPPA_DOT]) * a * a
+    f_he = 0.24 / (3.9715 * 0.76)
+    norm = np.interp(9500.0, z[::-1], xr0[::-1]) / (1 + 2 * f_he)
+
+    def at(arr, zz):
+        return np.interp(zz, z[::-1], arr[::-1]) / norm
+    assert abs(at(xr, 0.0) - (1 + 2 * f_he)) < 1e-3
+    assert abs(at(xr, 5.0) - (1 + f_he)) < 5e-3
+    assert abs(at(xr, 30.0) - at(xr0, 30.0)) < 1e-6
+    i30 = np.argmin(np.abs(z - 30.0))
+    tau_reio = p.bg[i30, capi.BG_KAPPA] - base.bg[i30, capi.BG_KAPPA]
+    assert 0.045 < tau_reio < 0.065, tau_reio
+    assert np.array_equal(problem().bg, base.bg)
