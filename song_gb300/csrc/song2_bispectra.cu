@@ -15,16 +15,23 @@
 // k2 step drops from l3 r k1 (q + l2 q) to l3 r k1 l2 k.
 //
 // Kernels:
-//   coef_kernel   C[Y][r][l2][k] and D[Z, M3, offset_L1][r][l1][k], once per
+//   coef_kernel   C[Y][r][l2][k] and D[Z, M3, offset_L1][l1][r][k], once per
 //                 handle (they depend only on the first-order inputs);
+//                 split_rows_kernel scales their rows by powers of two and
+//                 splits them into double-float (hi + lo floats);
 //   k3_kernel     I3[l3][r][pair] = 2 c_M3 * 1/2 sum dk3 k3^2 j_L3(r k3) T2,
-//                 one warp per (l3, pair), lanes over r;
+//                 one thread per (l3, pair, r), FP64;
 //   k2_kernel     I2[l3][l2][r][k1] = sum_k C[r][l2][k] I3sym[l3][r][k1][k],
-//                 one block per (l3, r);
-//   k1r_kernel    sum_r sum_k D[r][l1][k] I2[l3][l2][r][k] for every l1 of the
-//                 (l3, l2) triangle, then the geometrical factors, accumulated
-//                 into the unsymmetrised bispectrum; one block per (l3, l2);
+//                 one block per (l3, r), double-float dot products;
+//   geo_kernel    the geometrical factor of every (l3, l2, l1) triangle and L1
+//                 offset for one (M3, L3 offset);
+//   k1r_kernel    sum_r sum_k D[l1][r][k] I2[l3][l2][r][k] for every l1 of the
+//                 (l3, l2) triangles of two l2, every Z and L1 offset, times
+//                 the geometrical factors, accumulated into the unsymmetrised
+//                 bispectrum; double-float dot products;
 //   sym_kernel    the sum over the position of the second-order field.
+// Double-float keeps about 46 bits: GB300's FP32 pipe has 64 times the rate of
+// its FP64 pipe, and these contractions are the bulk of the work.
 #include <cuda_runtime.h>
 
 #include <algorithm>
