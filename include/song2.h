@@ -601,6 +601,14 @@ int song2_k3_grids_smart(const double *k, int k_size, int k3_size_min, int *k3_s
    Not reentrant. */
 int song2_read_params(const char *ini_path, const char *pre_path, song2_spec *spec, song2_params *grids,
                       song2_los_spec *los, char *err);
+/* The cosmology keys of the same files (CLASS's input names): h or H0, T_cmb,
+   omega_b or Omega_b, omega_cdm or Omega_cdm, N_ur or N_eff, YHe, and
+   reio_parametrization = reio_none or reio_camb with z_reio; absent keys take
+   the benchmark cosmology (h 0.678, omega_b 0.0224, omega_cdm 0.120, N_eff
+   3.046, T_cmb 2.7255, YHe 0.24, no reionisation).  Settings the input
+   provider cannot honour (100*theta_s, massive neutrinos, curvature,
+   YHe = BBN, tau_reio) are errors.  Not reentrant. */
+int song2_read_cosmo(const char *ini_path, const char *pre_path, song2_cosmo *cosmo, char *err);
 
 /* Defaults of the reference (input2.c) for the spec's k range and tables:
    x_max = k_max * 18000 for the lin/log k samplings (input2.c:1986-1989), plus

@@ -223,6 +223,7 @@ SIGNATURES = {
     "song2_sound_horizon": (_D, [C.POINTER(Tables), _D]),
     "song2_tau_grid_class": (_I, [C.POINTER(Tables), _D, _D, _D, _D, _I, _PD, C.c_char_p]),
     "song2_k3_grids_theta12": (_I, [_PD, _I, _I, _PI, _PD, C.c_char_p]),
+    "song2_read_cosmo": (_I, [C.c_char_p, C.c_char_p, C.POINTER(Cosmo), C.c_char_p]),
     "song2_k_grid_smart": (_I, [C.POINTER(Params), _D, _D, _I, _PD, C.c_char_p]),
     "song2_k3_grids_smart": (_I, [_PD, _I, _I, _PI, _PD, C.c_char_p]),
     "song2_read_params": (_I, [C.c_char_p, C.c_char_p, C.POINTER(Spec), C.POINTER(Params), C.POINTER(LosSpec),

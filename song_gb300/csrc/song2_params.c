@@ -799,3 +799,118 @@ int song2_k3_grids_theta12(const double *k, int k_size, int k3_size, int *k3_siz
     }
   return 0;
 }
+
+/* ------------------------------------------------- cosmology keys */
+
+int song2_read_cosmo(const char *ini_path, const char *pre_path, song2_cosmo *c, char *err) {
+  static plist list; /* large; the reader is not reentrant */
+  plist *pl = &list;
+  pl->n = 0;
+  if (read_file(ini_path, "ini", pl, err) || read_file(pre_path, "pre", pl, err)) return 1;
+  /* the benchmark cosmology where a key is absent */
+  c->h = 0.678;
+  c->omega_b = 0.0224;
+  c->omega_cdm = 0.120;
+  c->N_eff = 3.046;
+  c->T_cmb = 2.7255;
+  c->YHe = 0.24;
+  c->z_reio = 0.0;
+  const char *v;
+  const char *h = get(pl, "h"), *H0 = get(pl, "H0");
+  if (h && H0) {
+    snprintf(err, SONG2_ERRLEN, "give one of h and H0");
+    return 1;
+  }
+  if (h && num(h, "h", &c->h, err)) return 1;
+  if (H0) {
+    double d;
+    if (num(H0, "H0", &d, err)) return 1;
+    c->h = d / 100.0;
+  }
+  if (get(pl, "100*theta_s")) {
+    snprintf(err, SONG2_ERRLEN, "100*theta_s is not supported: give h or H0");
+    return 1;
+  }
+  RD_D("T_cmb", c->T_cmb);
+  /* physical or relative densities */
+  {
+    const char *ob = get(pl, "omega_b"), *Ob = get(pl, "Omega_b");
+    const char *oc = get(pl, "omega_cdm"), *Oc = get(pl, "Omega_cdm");
+    if ((ob && Ob) || (oc && Oc)) {
+      snprintf(err, SONG2_ERRLEN, "give one of omega_b and Omega_b (omega_cdm and Omega_cdm)");
+      return 1;
+    }
+    double d;
+    if (ob && num(ob, "omega_b", &c->omega_b, err)) return 1;
+    if (Ob) {
+      if (num(Ob, "Omega_b", &d, err)) return 1;
+      c->omega_b = d * c->h * c->h;
+    }
+    if (oc && num(oc, "omega_cdm", &c->omega_cdm, err)) return 1;
+    if (Oc) {
+      if (num(Oc, "Omega_cdm", &d, err)) return 1;
+      c->omega_cdm = d * c->h * c->h;
+    }
+  }
+  {
+    const char *n1 = get(pl, "N_ur"), *n2 = get(pl, "N_eff");
+    if (n1 && n2) {
+      snprintf(err, SONG2_ERRLEN, "give one of N_ur and N_eff");
+      return 1;
+    }
+    const char *w = n1 ? n1 : n2;
+    if (w && num(w, n1 ? "N_ur" : "N_eff", &c->N_eff, err)) return 1;
+  }
+  if ((v = get(pl, "N_ncdm"))) {
+    double d;
+    if (num(v, "N_ncdm", &d, err)) return 1;
+    if (d != 0) {
+      snprintf(err, SONG2_ERRLEN, "massive neutrinos (N_ncdm = %g) are not supported", d);
+      return 1;
+    }
+  }
+  if ((v = get(pl, "Omega_k"))) {
+    double d;
+    if (num(v, "Omega_k", &d, err)) return 1;
+    if (d != 0) {
+      snprintf(err, SONG2_ERRLEN, "curvature (Omega_k = %g) is not supported: the background is flat", d);
+      return 1;
+    }
+  }
+  if ((v = get(pl, "YHe"))) {
+    if (strstr(v, "BBN") || strstr(v, "bbn")) {
+      snprintf(err, SONG2_ERRLEN, "YHe = BBN needs CLASS's BBN table: give a number");
+      return 1;
+    }
+    if (num(v, "YHe", &c->YHe, err)) return 1;
+  }
+  /* reionisation: none, or the tanh model at a given z_reio */
+  {
+    const char *p = get(pl, "reio_parametrization");
+    int camb = 0;
+    if (p) {
+      if (strstr(p, "reio_none")) camb = 0;
+      else if (strstr(p, "reio_camb")) camb = 1;
+      else {
+        snprintf(err, SONG2_ERRLEN, "reio_parametrization = %.200s (reio_none or reio_camb)", p);
+        return 1;
+      }
+    }
+    if (get(pl, "tau_reio")) {
+      snprintf(err, SONG2_ERRLEN, "tau_reio is not supported: give z_reio");
+      return 1;
+    }
+    const char *zr = get(pl, "z_reio");
+    if (camb && !zr) {
+      snprintf(err, SONG2_ERRLEN, "reio_camb needs z_reio");
+      return 1;
+    }
+    if (camb && num(zr, "z_reio", &c->z_reio, err)) return 1;
+  }
+  if (!(c->h > 0) || !(c->omega_b > 0) || !(c->omega_cdm >= 0) || !(c->T_cmb > 0) || !(c->YHe >= 0 && c->YHe < 1) ||
+      !(c->N_eff >= 0) || !(c->z_reio >= 0)) {
+    snprintf(err, SONG2_ERRLEN, "cosmological parameters out of range");
+    return 1;
+  }
+  return 0;
+}

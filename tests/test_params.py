@@ -375,3 +375,41 @@ def test_theta12_k3_grids_match_oracle(lib):
             th = np.arccos(np.clip(cos_t, -1, 1))
             assert np.allclose(np.diff(th), np.diff(th)[0], rtol=1e-6, atol=1e-12)
     assert lib.song2_k3_grids_theta12(capi.dptr(k), n, 1, capi.iptr(sz), None, err) == 1
+
+
+def read_cosmo(lib, tmp_path, ini, pre=""):
+    pi, pp = tmp_path / "c.ini", tmp_path / "c.pre"
+    pi.write_text(ini)
+    pp.write_text(pre)
+    c = capi.Cosmo()
+    err = capi.errbuf()
+    rc = lib.song2_read_cosmo(str(pi).encode(), str(pp).encode(), C.byref(c), err)
+    return rc, c, err.value.decode()
+
+
+def test_reader_cosmology_keys(lib, tmp_path):
+    rc, c, err = read_cosmo(lib, tmp_path, "output = tBisp\nH0 = 67.0\nOmega_b = 0.05\nomega_cdm = 0.12\n"
+                                          "N_ur = 3.04\nT_cmb = 2.725\nYHe = 0.25\n"
+                                          "reio_parametrization = reio_camb\nz_reio = 8\n")
+    assert rc == 0, err
+    assert (c.h, c.omega_cdm, c.N_eff, c.T_cmb, c.YHe, c.z_reio) == (0.67, 0.12, 3.04, 2.725, 0.25, 8.0)
+    assert abs(c.omega_b - 0.05 * 0.67 ** 2) < 1e-15
+    rc, c, err = read_cosmo(lib, tmp_path, "output = tBisp\n")
+    assert rc == 0, err
+    assert (c.h, c.omega_b, c.omega_cdm, c.N_eff, c.T_cmb, c.YHe, c.z_reio) == (0.678, 0.0224, 0.12, 3.046, 2.7255,
+                                                                               0.24, 0.0)
+
+
+@pytest.mark.parametrize("ini,msg", [
+    ("h = 0.7\nH0 = 70\n", "one of h and H0"),
+    ("100*theta_s = 1.04\n", "theta_s"),
+    ("N_ncdm = 1\n", "massive neutrinos"),
+    ("Omega_k = 0.01\n", "curvature"),
+    ("YHe = BBN\n", "BBN"),
+    ("reio_parametrization = reio_camb\n", "needs z_reio"),
+    ("reio_parametrization = reio_camb\ntau_reio = 0.06\nz_reio = 7\n", "tau_reio"),
+    ("omega_b = 0.022\nOmega_b = 0.05\n", "one of omega_b"),
+])
+def test_reader_cosmology_errors(lib, tmp_path, ini, msg):
+    rc, c, err = read_cosmo(lib, tmp_path, ini)
+    assert rc == 1 and msg in err
