@@ -1,8 +1,9 @@
 """Intrinsic bispectrum of the second-order transfer functions (SONG's
 bispectra2.c): the k3, k2, k1 and r integrals and the geometrical factors.
 
-CPU: the oracle's 6j symbols against sympy; the reference's own check that the
-full geometrical factor of M3 = 0 reduces to 8/pi^3 (bispectra2.c:2826-2840);
+CPU: the oracle's 6j symbols against sympy; the reference's own checks that the
+full geometrical factor of M3 = 0 reduces to 8/pi^3 (bispectra2.c:2826-2840)
+and that odd l1 + l2 + l3 vanish for T and E when M3 > 0 (:660-675);
 the configuration list; linearity of the oracle in the second-order transfers;
 the quadratic correction.  GPU: the product against the oracle on seeded
 synthetic transfers for every option (fields T, E and B, m lists with and
@@ -258,3 +259,51 @@ def test_bispectra_argument_errors(lib):
         assert b"distinct" in err.value
     finally:
         lib.song2_los_destroy(lh)
+
+
+def unsym_checks(lib, ls, b, nbf):
+    """The reference's own checks after its bispectrum loops (bispectra2.c:640-705),
+    on the symmetrised output: for an even-parity bispectrum with M3 > 0 in the m
+    list every configuration with odd l1 + l2 + l3 vanishes; returns the largest
+    such value relative to the largest value."""
+    ls = np.ascontiguousarray(ls, dtype=np.int32)
+    n = lib.song2_bispectra_configs(len(ls), capi.iptr(ls), None, None, None)
+    i1, i2, i3 = (np.zeros(n, dtype=np.int32) for _ in range(3))
+    lib.song2_bispectra_configs(len(ls), capi.iptr(ls), capi.iptr(i1), capi.iptr(i2), capi.iptr(i3))
+    odd = (ls[i1] + ls[i2] + ls[i3]) % 2 == 1
+    bb = b.reshape(nbf ** 3, n)
+    return float(np.max(np.abs(bb[:, odd])) / np.max(np.abs(bb))) if odd.any() else 0.0, odd
+
+
+def test_oracle_parity_check(lib):
+    """bispectra2.c:660-675: with m_max > 0, odd l1 + l2 + l3 give exactly zero
+    for T and E (the (L1 l2 L3; 0 0 0) symbol vanishes for them)."""
+    prob = problem(**BI_PROBLEM, m=(0, 1, 2))
+    los = los_spec(lib, prob, l_max=12, l_logstep=1.5, l_linstep=4)
+    fields = [0, 1]
+    r, q, pk, T1 = first_order_inputs(prob, los, fields, r_size=4, q_size=30)
+    bs = bispectra_spec(fields, r, q, pk, T1)
+    t2, _, _ = synthetic_transfers(lib, prob, los)
+    n = n_configs(lib, los._keep) * 8
+    b = oracle.bispectra(prob, los, bs, t2, n)
+    worst, odd = unsym_checks(lib, los._keep, b, 2)
+    assert odd.any() and worst == 0.0
+
+
+@pytest.mark.gpu
+def test_bispectra_reference_checks_on_gpu(lib):
+    """The same parity check on the GPU output (bispectra2.c:660-675): with
+    M3 > 0 in the m list, odd l1 + l2 + l3 give exactly zero for T and E."""
+    prob = problem(**BI_PROBLEM, m=(0, 1, 2))
+    los = los_spec(lib, prob, l_max=30, l_logstep=1.25, l_linstep=6)
+    fields = [0, 1]
+    r, q, pk, T1 = first_order_inputs(prob, los, fields)
+    bs = bispectra_spec(fields, r, q, pk, T1)
+    t2, n_tt, nu = synthetic_transfers(lib, prob, los)
+    n = n_configs(lib, los._keep) * 8
+    got = np.zeros(n)
+    err = capi.errbuf()
+    assert lib.song2_gpu_bispectra(C.byref(prob.spec), C.byref(los), C.byref(bs), capi.dptr(t2), capi.dptr(got),
+                                   err) == 0, err.value
+    worst, odd = unsym_checks(lib, los._keep, got, 2)
+    assert odd.any() and worst == 0.0
