@@ -549,6 +549,10 @@ typedef struct {
   double tau_stepsize;       /* perturb_sampling_stepsize_song (default 0.4) */
   double tau_late_boost;     /* perturb_sampling_late_time_boost (default 1) */
   double tau_start_c_over_h; /* start_sources_at_tau_c_over_tau_h (CLASS default 0.008) */
+  /* intrinsic bispectrum (song2_bispectra_spec) */
+  int bi_k1_interpolation;   /* transfers_k1_interpolation: SONG2_INTERP_LINEAR (default) / _CUBIC */
+  int bi_k2_interpolation;   /* transfers_k2_interpolation */
+  int bi_r_size;             /* r_size (0: not given) */
 } song2_params;
 void song2_params_defaults(song2_params *grids);
 /* The source time sampling of perturb2_timesampling_for_sources when no custom

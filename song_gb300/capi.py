@@ -138,7 +138,8 @@ class Params(C.Structure):
                 ("k_per_decade_for_pk", C.c_double), ("k_per_decade_for_bao", C.c_double),
                 ("k_bao_center", C.c_double), ("k_bao_width", C.c_double), ("k_max_for_pk", C.c_double),
                 ("h", C.c_double), ("k3_size_min", C.c_int), ("has_cmb", C.c_int), ("has_lss", C.c_int),
-                ("tau_stepsize", C.c_double), ("tau_late_boost", C.c_double), ("tau_start_c_over_h", C.c_double)]
+                ("tau_stepsize", C.c_double), ("tau_late_boost", C.c_double), ("tau_start_c_over_h", C.c_double),
+                ("bi_k1_interpolation", C.c_int), ("bi_k2_interpolation", C.c_int), ("bi_r_size", C.c_int)]
 
 
 SAMPLING_LIN, SAMPLING_LOG, SAMPLING_SMART, SAMPLING_SYM, SAMPLING_THETA12 = 0, 1, 2, 3, 4

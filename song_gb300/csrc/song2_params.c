@@ -368,6 +368,22 @@ int song2_read_params(const char *ini_path, const char *pre_path, song2_spec *s,
       return 1;
     }
   }
+  /* the intrinsic bispectrum's interpolation in k1, k2 and its r sampling size */
+  if ((v = get(pl, "transfers_k1_interpolation")))
+    g->bi_k1_interpolation = strstr(v, "cubic") ? SONG2_INTERP_CUBIC : SONG2_INTERP_LINEAR;
+  if ((v = get(pl, "transfers_k2_interpolation")))
+    g->bi_k2_interpolation = strstr(v, "cubic") ? SONG2_INTERP_CUBIC : SONG2_INTERP_LINEAR;
+  {
+    double d;
+    if ((v = get(pl, "r_size"))) {
+      if (num(v, "r_size", &d, err)) return 1;
+      if (d < 2) {
+        snprintf(err, SONG2_ERRLEN, "r_size = %g must be at least 2", d);
+        return 1;
+      }
+      g->bi_r_size = (int)d;
+    }
+  }
   /* input2.c:362-377 (the first key is the obsolete spelling) */
   RD_D2("perturb_sampling_stepsize_for_2nd_order", "perturb_sampling_stepsize_song", g->tau_stepsize);
   RD_D("perturb_sampling_late_time_boost", g->tau_late_boost);

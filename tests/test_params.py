@@ -413,3 +413,12 @@ def test_reader_cosmology_keys(lib, tmp_path):
 def test_reader_cosmology_errors(lib, tmp_path, ini, msg):
     rc, c, err = read_cosmo(lib, tmp_path, ini)
     assert rc == 1 and msg in err
+
+
+def test_reader_bispectrum_settings(lib, tmp_path):
+    rc, s, g, ls, err = read(lib, tmp_path, "output = tBisp\n",
+                             "transfers_k1_interpolation = linear\ntransfers_k2_interpolation = cubic\nr_size = 75\n")
+    assert rc == 0, err
+    assert (g.bi_k1_interpolation, g.bi_k2_interpolation, g.bi_r_size) == (capi.INTERP_LINEAR, capi.INTERP_CUBIC, 75)
+    rc, *_, err = read(lib, tmp_path, "output = tBisp\n", "r_size = 1\n")
+    assert rc == 1 and "r_size" in err
